@@ -1,0 +1,387 @@
+#!/usr/bin/env python
+"""Benchmark: tree-likelihood lnL + gradient evaluations per second on one GB300.
+
+Workload (default ``gtr_g4_t1000_b8``): GTR+Gamma4 on a 1,000-taxon Yule tree
+with 100,000 simulated DNA sites (compressed to N unique patterns), a batch of
+8 branch-length samples.  One *step* = one batched evaluation: transition
+matrices, post-order pass, pre-order adjoint pass and all reductions, giving
+lnL and the full gradient (branch lengths, eigen system -> exchangeabilities
+and frequencies, category rates/weights) for every sample.  One *evaluation*
+= lnL + gradient for one sample; ``value`` = evaluations / second over all
+ranks.  Inputs stay resident in HBM; the stored partials (tens of GB) exceed
+the 129 MB L2, so no explicit L2 flush is used.
+
+``--impl reference`` times the CPU restatement of the reference path (the
+oracle port: torch CPU FP64 ops and autograd, all host threads) on a bounded
+pattern prefix of the same workload, scaled to the full pattern count.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+METRIC = "lnL+grad evals/s: FP32-rescaled batched vs FP64 drop-in, 1 GB300; p99 latency"
+UNIT = "evals/s"
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("gb300", "reference"), default="gb300")
+    ap.add_argument("--workload", default="gtr_g4_t1000_b8")
+    ap.add_argument("--precision", choices=("f32", "f64"), default="f32")
+    ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the FP64 drop-in comparison (0: skip)")
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--cpu-patterns", type=int, default=3000, help="pattern prefix of the CPU sample")
+    ap.add_argument("--sites", type=int, default=None, help="override the workload's site count")
+    ap.add_argument("--tips", type=int, default=None, help="override the workload's tip count")
+    ap.add_argument("--batch", type=int, default=None, help="override the workload's batch")
+    return ap.parse_args()
+
+
+class ClockSampler:
+    """Samples SM clocks and throttle reasons with nvidia-smi while running."""
+
+    FIELDS = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.FIELDS}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.lines:
+            return None
+        sm, mx, reasons = [], None, set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 8:
+                continue
+            try:
+                sm.append(float(parts[0]))
+                mx = float(parts[1])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[4:8]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def workload(args):
+    from torchtree_gb300 import patterns, synthetic
+
+    over = {}
+    if args.sites:
+        over["site_count"] = args.sites
+    if args.tips:
+        over["tip_count"] = args.tips
+    if args.batch:
+        over["batch"] = args.batch
+    wl = synthetic.named_workload(args.workload, **over)
+    ca = patterns.compress(wl.sequences)
+    return wl, ca
+
+
+def cpu_baseline(wl, ca, n_patterns, repeats=3):
+    from oracle import cpu_baseline as CB
+    from torchtree_gb300 import synthetic
+
+    rates = (synthetic.discrete_gamma_np(float(wl.shape[0, 0]), wl.categories) if wl.site_model == "gamma"
+             else synthetic.discrete_weibull_np(float(wl.shape[0, 0]), wl.categories))
+    d = CB.prepare(wl.topology.postorder, ca.codes, ca.table, ca.weights, wl.branch_lengths[0], wl.exch[0],
+                   wl.pi[0], rates, n_patterns)
+    sec, threads, _ = CB.time_evaluations(d, repeats=repeats, warmup=1)
+    per_eval = sec * ca.pattern_count / d["n"]
+    return {"value": 1.0 / per_eval, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": (f"oracle port (torch CPU FP64 + autograd, rescaled) on the first {d['n']} of "
+                       f"{ca.pattern_count} patterns, 1 sample, median of {repeats}; seconds scaled "
+                       f"by N/{d['n']}"),
+            "seconds_per_sample_eval": per_eval}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    wl, ca = workload(args)
+    from oracle import cpu_baseline as CB
+    from torchtree_gb300 import synthetic
+
+    rates = synthetic.discrete_gamma_np(float(wl.shape[0, 0]), wl.categories)
+    d = CB.prepare(wl.topology.postorder, ca.codes, ca.table, ca.weights, wl.branch_lengths[0], wl.exch[0],
+                   wl.pi[0], rates, args.cpu_patterns)
+    for _ in range(args.warmup):
+        CB.one_evaluation(d)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        CB.one_evaluation(d)
+    dt = (time.perf_counter() - t0) / args.steps
+    per_eval = dt * ca.pattern_count / d["n"]
+    value = 1.0 / per_eval
+    import torch
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": per_eval * 1e3 * wl.branch_lengths.shape[0],
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": "synthetic (seeded Yule tree + simulated alignment)", "impl": "reference",
+        "config": {"workload": args.workload, "tips": wl.topology.tip_count, "patterns": ca.pattern_count,
+                   "batch": int(wl.branch_lengths.shape[0])},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": torch.get_num_threads(), "kind": "port",
+                         "sample": f"first {d['n']} of {ca.pattern_count} patterns per step, 1 sample, "
+                                   f"scaled by N/{d['n']}"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+        return
+    import torch
+    import torch.distributed as dist
+
+    from torchtree_gb300 import site_models, substitution
+    from torchtree_gb300.engine import LikelihoodEngine
+    from torchtree_gb300.likelihood import PhyloLikelihood, batch_inputs
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    if world > 1:
+        dist.init_process_group("nccl", device_id=dev)
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+
+    wl, ca = workload(args)
+    b = int(wl.branch_lengths.shape[0])
+    T, N, K, S = wl.topology.tip_count, ca.pattern_count, wl.categories, 4
+    bl, exch, pi, shape = batch_inputs(wl, dev)
+    rates, probs = site_models.gamma_rates(shape, K)
+    probs = probs.expand(b, K).contiguous()
+    q = substitution.gtr_q(exch, pi)
+    lam, u, w = (t.detach().contiguous() for t in substitution.eigen_system(q, pi))
+    zeros = torch.zeros(b, 1, dtype=torch.float64, device=dev)
+    bls = torch.cat([bl, zeros], -1).contiguous()
+    rates = rates.detach().contiguous()
+
+    def make_engine(precision):
+        return LikelihoodEngine(wl.topology.postorder, T, S, K, ca.codes, ca.table, ca.weights, batch=b,
+                                precision=precision, device=dev)
+
+    eng = make_engine(args.precision)
+    stream = torch.cuda.current_stream()
+
+    def step(e):
+        e.set_eigen(lam, u, w, bls, rates)
+        e.log_likelihood(probs, pi, rescale=True, keep_partials=True)
+        e.gradient(probs, pi)
+        return e.eigen_gradient(lam, u, w, bls, rates)
+
+    for _ in range(max(args.warmup, 3)):
+        step(eng)
+    torch.cuda.synchronize()
+    assert eng.device_status() == 0
+    launches0 = eng.launch_count
+    barrier()
+    torch.cuda.synchronize()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(local) as clocks:
+        ev[0].record(stream)
+        for i in range(args.steps):
+            step(eng)
+            ev[i + 1].record(stream)
+        torch.cuda.synchronize()
+    barrier()
+    launches = eng.launch_count - launches0
+    per_step = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
+    total_ms = ev[0].elapsed_time(ev[-1])
+    t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    total_ms = float(t.item())
+    value = b * args.steps * world / (total_ms / 1e3)
+
+    # per-call timing of the two pruning kernels (each call: one pruning
+    # kernel + its small reduction kernels) for the roofline
+    fw, bw = [], []
+    for _ in range(3):
+        e0, e1, e2, e3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
+        eng.set_eigen(lam, u, w, bls, rates)
+        e0.record(stream)
+        eng.log_likelihood(probs, pi, rescale=True, keep_partials=True)
+        e1.record(stream)
+        eng.gradient(probs, pi)
+        e2.record(stream)
+        torch.cuda.synchronize()
+        fw.append(e0.elapsed_time(e1))
+        bw.append(e1.elapsed_time(e2))
+    fw_ms, bw_ms = statistics.median(fw), statistics.median(bw)
+    elem = 4 if args.precision == "f32" else 8
+    I = T - 1
+    tile = 128 if args.precision == "f32" else 64
+    ntiles = -(-N // tile)
+    part_bytes = b * (I - 1) * K * S * N * elem
+    side = b * (T * N + 8 * N)
+    fw_bytes = part_bytes + side
+    bw_bytes = part_bytes + side + b * (2 * T - 2) * ntiles * K * S * S * elem
+    peak, peak_kind = measured_peaks()
+    kernels = {
+        "post_order": {"ms": fw_ms, "bytes": fw_bytes, "gbs": fw_bytes / fw_ms / 1e6},
+        "pre_order_adjoint": {"ms": bw_ms, "bytes": bw_bytes, "gbs": bw_bytes / bw_ms / 1e6},
+    }
+    dom = max(kernels, key=lambda k: kernels[k]["ms"])
+    achieved = kernels[dom]["gbs"]
+    roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
+                "frac": achieved / peak, "peak_source": peak_kind, "traffic": None,
+                "per_launch_bytes": kernels[dom]["bytes"], "kernels": kernels}
+    traffic_file = ROOT / "profiles" / "traffic.json"
+    if traffic_file.exists():
+        tr = json.loads(traffic_file.read_text()).get(args.workload, {}).get(dom)
+        if tr:
+            roofline["traffic"] = tr
+
+    # FP64 drop-in on the same workload
+    fp64 = None
+    if args.fp64_steps > 0 and args.precision == "f32":
+        del eng
+        torch.cuda.empty_cache()
+        e64 = make_engine("f64")
+        step(e64)
+        torch.cuda.synchronize()
+        a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(args.fp64_steps):
+            step(e64)
+        z.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(z) / args.fp64_steps
+        fp64 = {"value": b / (ms / 1e3), "unit": UNIT, "ms_per_step": ms, "steps": args.fp64_steps}
+        del e64
+        torch.cuda.empty_cache()
+        eng = None
+
+    # end to end through the public API: host inputs -> H2D -> lnL+grad -> D2H
+    e2e = None
+    if not args.no_e2e:
+        lik = PhyloLikelihood(wl.topology, ca, S, K, batch=b, precision=args.precision, device=dev)
+        lik.rescale = True
+        hosts = [x.detach().cpu().pin_memory() for x in (bl, exch, pi, shape)]
+        h2d = sum(x.numel() * x.element_size() for x in hosts)
+
+        def e2e_step():
+            d_bl, d_ex, d_pi, d_sh = (x.to(dev, non_blocking=True) for x in hosts)
+            d_bl.requires_grad_()
+            d_ex.requires_grad_()
+            d_pi.requires_grad_()
+            r, p = site_models.gamma_rates(d_sh, K)
+            lnl = lik(d_bl, substitution.gtr_q(d_ex, d_pi), d_pi, r, p.expand(b, K))
+            grads = torch.autograd.grad(lnl.sum(), [d_bl, d_ex, d_pi])
+            out = [lnl.detach().cpu()] + [g.cpu() for g in grads]
+            return sum(o.numel() * o.element_size() for o in out)
+
+        for _ in range(2):
+            e2e_step()
+        torch.cuda.synchronize()
+        barrier()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            d2h = e2e_step()
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        tt = torch.tensor([dt], dtype=torch.float64, device=dev)
+        if world > 1:
+            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        e2e = {"value": b * args.steps * world / float(tt.item()), "unit": UNIT, "h2d_bytes_per_step": h2d,
+               "d2h_bytes_per_step": d2h}
+        del lik
+
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(wl, ca, args.cpu_patterns)
+
+    if rank == 0:
+        lat = sorted(per_step)
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+            "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
+            "data": "synthetic (seeded Yule tree, simulated GTR+G4 alignment)",
+            "config": {"workload": args.workload, "tips": T, "sites": int(sum(ca.weights)),
+                       "patterns": N, "batch": b, "categories": K, "states": S,
+                       "model": "GTR+Gamma4", "l2": "inputs (stored partials) larger than L2; no flush",
+                       "parallelism": f"replicas x{world}"},
+            "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
+                           "what": "one batched lnL+gradient call (all samples)"},
+            "fp64_dropin": fp64,
+            "speedup_vs_fp64": (value / world / fp64["value"]) if fp64 else None,
+            "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
+            "clocks": clocks.summary(),
+        }
+        print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

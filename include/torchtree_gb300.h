@@ -1,0 +1,174 @@
+/*
+ * torchtree_gb300 — C ABI of the GB300 tree-likelihood engine.
+ *
+ * Felsenstein pruning log-likelihood and its gradient for a batch of
+ * samples that share one tree topology and one compressed alignment.
+ * All entry points take plain pointers and sizes; device pointers are
+ * CUDA global-memory addresses on the current device, `stream` is a
+ * cudaStream_t (NULL = legacy default stream).  Every call returns a
+ * tt_status (0 = success); tt_last_error() gives a message for the calling
+ * thread's most recent failure.
+ *
+ * Index conventions (torchtree/evolution/tree_model.py:37-53):
+ *   tips 0..T-1 in taxa order, internal nodes T..2T-2, root = 2T-2;
+ *   the branch above node i carries index i, so there are B = 2T-2 branches.
+ * Layouts (row-major, batch outermost):
+ *   eigenvalues [b][S], eigenvectors U [b][S][S], inverse W [b][S][S],
+ *   branch_lengths [b][B], category_rates [b][K], category_weights [b][K],
+ *   frequencies [b][S], transition matrices [b][B][K][S][S] (P[i][j] =
+ *   P(j at child | i at parent), the reference's `mats`).
+ */
+#ifndef TORCHTREE_GB300_H
+#define TORCHTREE_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef enum {
+  TT_OK = 0,
+  TT_ERR_INVALID_ARGUMENT = 1,
+  TT_ERR_UNSUPPORTED = 2,
+  TT_ERR_OUT_OF_MEMORY = 3,
+  TT_ERR_CUDA = 4,
+  TT_ERR_DEVICE_TIMEOUT = 5, /* a bounded device-side wait gave up */
+  TT_ERR_NOT_READY = 6       /* a required earlier call was not made */
+} tt_status;
+
+enum { TT_PRECISION_F32 = 0, TT_PRECISION_F64 = 1 };
+
+typedef struct tt_plan tt_plan;
+
+/* Library version string. */
+const char *tt_version(void);
+
+/* Message of the calling thread's last failed call ("" if none). */
+const char *tt_last_error(void);
+
+/*
+ * Create a plan for one topology.  Replaces the per-call set-up that
+ * TreeLikelihoodModel.__init__ / _call do in Python
+ * (torchtree/evolution/tree_likelihood.py:283-311, 313-356).
+ *   postorder: host int32 [T-1][3] of (node, left, right) triples in a
+ *              valid post-order (tree_model.py:187-195); the last triple is
+ *              the root.
+ *   precision: TT_PRECISION_F32 (partials in FP32 with rescaling; log
+ *              scalers and the pattern sum in FP64) or TT_PRECISION_F64.
+ * Allocates all device workspace on the current device.
+ */
+int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
+                   int32_t state_count, int32_t category_count,
+                   int32_t pattern_count, int32_t batch, int32_t precision);
+
+/* Release a plan and its device memory (NULL is accepted). */
+int tt_plan_destroy(tt_plan *plan);
+
+/* Device bytes held by the plan. */
+int tt_plan_workspace_bytes(const tt_plan *plan, size_t *bytes);
+
+/*
+ * Upload the compressed alignment (site_pattern.py:100-151): per tip and
+ * pattern a uint8 code indexing `code_table`, the distinct tip partial
+ * vectors.  A tip-state alignment (compute_tips_states) uses the table
+ * [one-hot rows 0..S-1, all-ones row S]; a partial-vector alignment
+ * (compute_tips_partials) uses its distinct columns.
+ *   codes:      host uint8 [T][N], every value < code_count
+ *   code_table: host double [code_count][S], code_count <= 256
+ *   weights:    host double [N] (the reference's int64 pattern counts)
+ */
+int tt_plan_set_tips(tt_plan *plan, const uint8_t *codes,
+                     const double *code_table, int32_t code_count,
+                     const double *weights);
+
+/*
+ * Transition matrices from an eigen system, all branches x categories x
+ * samples in one launch (substitution_model/abstract.py:57-76):
+ *   P[b][i][k] = U[b] diag(exp(lambda[b] * t[b][i] * r[b][k])) W[b]
+ * computed in FP64 and stored at the plan's precision.
+ */
+int tt_update_transition_matrices(tt_plan *plan, const double *eigenvalues,
+                                  const double *eigenvectors,
+                                  const double *inverse_eigenvectors,
+                                  const double *branch_lengths,
+                                  const double *category_rates, void *stream);
+
+/*
+ * Transition matrices given directly (the reference's `mats` argument,
+ * tree_likelihood.py:40-75): device double [b][B][K][S][S].
+ */
+int tt_set_transition_matrices(tt_plan *plan, const double *matrices,
+                               void *stream);
+
+/*
+ * Log-likelihood per sample (tree_likelihood.py:40-75 without rescaling,
+ * 186-221 with rescaling):
+ *   lnL[b] = sum_n w_n log( sum_k c[b][k] sum_i pi[b][i] L_root[b][k][i][n] )
+ * rescale != 0 rescales every internal partial by a power of two and
+ * accumulates the exponents exactly; rescale == 0 runs unscaled.
+ * keep_partials != 0 stores the internal partials for tt_gradient.
+ *   log_likelihood:      device double [b]
+ *   site_log_likelihood: device double [b][N] or NULL
+ */
+int tt_log_likelihood(tt_plan *plan, const double *category_weights,
+                      const double *frequencies, int32_t rescale,
+                      int32_t keep_partials, double *log_likelihood,
+                      double *site_log_likelihood, void *stream);
+
+/*
+ * Gradient of sum_b lnL[b] after tt_log_likelihood(keep_partials=1),
+ * by a pre-order adjoint pass (replaces autograd through
+ * tree_likelihood.py:186-221):
+ *   grad_matrices:          device double [b][B][K][S][S] or NULL
+ *   grad_frequencies:       device double [b][S] or NULL
+ *   grad_category_weights:  device double [b][K] or NULL
+ * The gradient with respect to P is always kept inside the plan for
+ * tt_transition_matrices_gradient.
+ */
+int tt_gradient(tt_plan *plan, const double *category_weights,
+                const double *frequencies, double *grad_matrices,
+                double *grad_frequencies, double *grad_category_weights,
+                void *stream);
+
+/*
+ * Chain the plan's dlnL/dP (from tt_gradient) through
+ * P = U diag(exp(lambda t r)) W (abstract.py:67-76).  Outputs (device
+ * double, any may be NULL): grad_eigenvalues [b][S], grad_eigenvectors
+ * [b][S][S], grad_inverse_eigenvectors [b][S][S], grad_branch_lengths
+ * [b][B], grad_category_rates [b][K].
+ */
+int tt_transition_matrices_gradient(
+    tt_plan *plan, const double *eigenvalues, const double *eigenvectors,
+    const double *inverse_eigenvectors, const double *branch_lengths,
+    const double *category_rates, double *grad_eigenvalues,
+    double *grad_eigenvectors, double *grad_inverse_eigenvectors,
+    double *grad_branch_lengths, double *grad_category_rates, void *stream);
+
+/*
+ * Device status word: TT_OK, or TT_ERR_DEVICE_TIMEOUT when a kernel's
+ * bounded wait gave up since the last reset.  Synchronises the stream.
+ */
+int tt_plan_device_status(tt_plan *plan, void *stream, int32_t *status,
+                          int32_t reset);
+
+/*
+ * Host-only: the execution schedule a plan would use (no device needed).
+ *   steps: int32 [T-1][12] per step (node, left, right, forward slot of
+ *          left / right / output, adjoint slot of input / left / right, 3
+ *          unused), -1 where a slot does not apply;
+ *   slot_counts: int32 [2] shared-memory slots of the forward and adjoint.
+ * Validates `postorder` exactly as tt_plan_create does.
+ */
+int tt_schedule(int32_t tip_count, const int32_t *postorder, int32_t *steps,
+                int32_t *slot_counts);
+
+/* Number of kernel launches the plan issued since creation. */
+int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TORCHTREE_GB300_H */

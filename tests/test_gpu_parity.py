@@ -1,0 +1,274 @@
+"""GPU parity: the sm_103a engine against the reference's own numbers.
+
+Every case of tests/golden/likelihood.json (produced by the reference
+torchtree's TreeLikelihoodModel + autograd in FP64) is evaluated through the
+package's public path (pattern compression -> C-ABI plan -> kernels ->
+autograd chain):
+
+* FP64 drop-in: lnL within 1e-10 relative, gradients within 1e-10 of the
+  largest component (``rtol=atol/max = 1e-10``);
+* FP32 rescaled: lnL within 1e-6 relative, gradients within 1e-4 of the
+  largest component.
+"""
+import math
+
+import numpy as np
+import pytest
+import torch
+
+from tests.oracle_cases import GRAD_KEYS, as_np, record_inputs
+
+pytestmark = pytest.mark.gpu
+
+F64_RTOL = 1e-10
+F32_LNL_RTOL = 1e-6
+F32_GRAD_TOL = 1e-4
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from torchtree_gb300 import _native
+
+    _native.load()
+
+
+def _keys():
+    import json
+
+    from tests.conftest import GOLDEN
+
+    return sorted(json.loads((GOLDEN / "likelihood.json").read_text()))
+
+
+def engine_eval(rec, precision, rescale=None):
+    """lnL [b] and gradients of sum(lnL) w.r.t. the record's leaves, via the package.
+
+    The 4x4 eigendecompositions run on the CPU (one LAPACK call per matrix),
+    so a batch member's inputs are bit-identical to its single evaluation.
+    """
+    from torchtree_gb300 import patterns, site_models, substitution
+    from torchtree_gb300.datatype import Nucleotide
+    from torchtree_gb300.likelihood import PhyloLikelihood
+    from torchtree_gb300.tree import Topology
+
+    dev = torch.device("cuda")
+    x = {k: v.detach().to(dev).requires_grad_() for k, v in record_inputs(rec, False).items()}
+    batched = x["bl"].dim() == 2
+    b = x["bl"].shape[0] if batched else 1
+    lead = lambda t: t if batched else t.unsqueeze(0)  # noqa: E731
+    topo = Topology(rec["postorder"], rec["names"])
+    ca = patterns.compress(rec["sequences"], Nucleotide(), use_ambiguities=rec.get("use_ambiguities", False),
+                           tip_states=rec.get("tip_states", False))
+    if rec["site_model"] == "weibull":
+        rates, probs = site_models.weibull_rates(lead(x["shape"]), rec["categories"],
+                                                 lead(x["invariant"]) if "invariant" in x else None)
+    elif rec["site_model"] == "constant":
+        rates = torch.ones(b, 1, dtype=torch.float64, device=dev)
+        probs = torch.ones(b, 1, dtype=torch.float64, device=dev)
+    else:
+        rates = torch.tensor(rec["category_rates"], dtype=torch.float64, device=dev).expand(b, -1)
+        probs = torch.full((b, rec["categories"]), 1.0 / rec["categories"], dtype=torch.float64, device=dev)
+    K = rates.shape[-1]
+    probs = probs.expand(b, K)
+    lik = PhyloLikelihood(topo, ca, 4, K, batch=b, precision=precision)
+    if rescale is not None:
+        lik.rescale = rescale
+    bls = lik.node_branch_lengths(lead(x["bl"]))
+    if rec["model"] == "jc69":
+        t = bls.unsqueeze(-1) * rates.unsqueeze(-2)
+        e = torch.exp(-4.0 / 3.0 * t)
+        eye = torch.eye(4, dtype=torch.float64, device=dev)
+        mats = (0.25 - 0.25 * e)[..., None, None] * (1 - eye) + (0.25 + 0.75 * e)[..., None, None] * eye
+        pi = torch.full((b, 4), 0.25, dtype=torch.float64, device=dev)
+        lnl = lik.evaluate_matrices(mats, probs, pi)
+    else:
+        pi = lead(x["pi"])
+        q = substitution.gtr_q(lead(x["exch"]), pi) if rec["model"] == "gtr" else \
+            substitution.hky_q(lead(x["exch"]), pi)
+        lam, u, w = (t.to(dev) for t in substitution.eigen_system(q.cpu(), pi.cpu()))
+        lnl = lik.evaluate_eigen(lam, u, w, bls, rates, probs, pi)
+    leaves = [(k, g) for k, g in GRAD_KEYS if k in x and g in rec]
+    grads = torch.autograd.grad(lnl.sum(), [x[k] for k, _ in leaves])
+    return lnl.detach().cpu().numpy(), {g: gr.cpu().numpy() for (_, g), gr in zip(leaves, grads)}, lik
+
+
+@pytest.mark.parametrize("key", _keys())
+def test_fp64_dropin_matches_reference(golden_likelihood, key):
+    rec = golden_likelihood[key]
+    lnl, grads, _ = engine_eval(rec, "f64")
+    np.testing.assert_allclose(lnl, rec["lnl"], rtol=F64_RTOL)
+    for g, got in grads.items():
+        exp = as_np(rec[g])
+        np.testing.assert_allclose(got, exp, rtol=F64_RTOL, atol=F64_RTOL * np.abs(exp).max(), err_msg=g)
+
+
+@pytest.mark.parametrize("key", _keys())
+def test_fp32_rescaled_matches_reference(golden_likelihood, key):
+    rec = golden_likelihood[key]
+    lnl, grads, _ = engine_eval(rec, "f32")
+    np.testing.assert_allclose(lnl, rec["lnl"], rtol=F32_LNL_RTOL)
+    for g, got in grads.items():
+        exp = as_np(rec[g])
+        np.testing.assert_allclose(got, exp, rtol=F32_GRAD_TOL, atol=F32_GRAD_TOL * np.abs(exp).max(),
+                                   err_msg=g)
+
+
+def test_tiny_known_answer_on_gpu(golden_likelihood):
+    lnl, _, _ = engine_eval(golden_likelihood["tiny_jc69"], "f64")
+    assert abs(lnl[0] - (-83.329016)) < 1e-6  # test_tree_likelihood.py:84
+
+
+def test_underflow_switch_is_sticky(golden_likelihood):
+    rec = golden_likelihood["gtr_w4_t700_underflow"]
+    lnl, _, lik = engine_eval(rec, "f64")
+    assert lik.rescale is True  # tree_likelihood.py:378-388
+    np.testing.assert_allclose(lnl, rec["lnl"], rtol=F64_RTOL)
+
+
+def test_batch_element_equals_single(golden_likelihood):
+    # test_tree_likelihood.py:204-297: a batch member equals its own evaluation exactly
+    rec = golden_likelihood["hky_w4_t12_b3"]
+    lnl_b, _, _ = engine_eval(rec, "f64")
+    single = dict(rec)
+    for k in ("branch_lengths", "exch", "pi", "shape"):
+        single[k] = rec[k][1]
+    lnl_1, _, _ = engine_eval(single, "f64")
+    assert lnl_b[1] == lnl_1[0]
+    lnl_b32, _, _ = engine_eval(rec, "f32")
+    lnl_132, _, _ = engine_eval(single, "f32")
+    assert lnl_b32[1] == lnl_132[0]
+
+
+def test_rescaled_equals_unscaled_fp64(golden_likelihood):
+    rec = golden_likelihood["gtr_w4_t69"]
+    a, _, _ = engine_eval(rec, "f64", rescale=False)
+    b_, _, _ = engine_eval(rec, "f64", rescale=True)
+    np.testing.assert_allclose(a, b_, rtol=1e-13)
+
+
+def test_finite_differences_fp64(golden_likelihood):
+    """Central differences of the engine's own FP64 lnL vs its adjoint gradient."""
+    from torchtree_gb300 import patterns, site_models, substitution
+    from torchtree_gb300.datatype import Nucleotide
+    from torchtree_gb300.likelihood import PhyloLikelihood
+    from torchtree_gb300.tree import Topology
+
+    rec = golden_likelihood["gtr_w4_t9_ambiguities"]
+    dev = torch.device("cuda")
+    topo = Topology(rec["postorder"], rec["names"])
+    ca = patterns.compress(rec["sequences"], Nucleotide(), use_ambiguities=True)
+    lik = PhyloLikelihood(topo, ca, 4, 4, batch=1, precision="f64")
+
+    def f(bl, exch, pi, shape):
+        rates, probs = site_models.weibull_rates(shape, 4)
+        q = substitution.gtr_q(exch, pi)
+        lam, u, w = substitution.eigen_system(q, pi)
+        return lik.evaluate_eigen(lam, u, w, lik.node_branch_lengths(bl), rates, probs.expand(1, 4), pi).sum()
+
+    t = lambda v: torch.tensor([v], dtype=torch.float64, device=dev, requires_grad=True)  # noqa: E731
+    args = [t(rec["branch_lengths"]), t(rec["exch"]), t(rec["pi"]), t(rec["shape"])]
+    grads = torch.autograd.grad(f(*args), args)
+    for a, g in zip(args, grads):
+        flat = a.detach().clone()
+        fd = torch.empty_like(flat)
+        for i in range(flat.numel()):
+            h = 1e-6 * max(1.0, abs(flat.view(-1)[i].item()))
+            up = flat.clone(); up.view(-1)[i] += h
+            dn = flat.clone(); dn.view(-1)[i] -= h
+            with torch.no_grad():
+                vals = []
+                for z in (up, dn):
+                    call = [z if b is a else b.detach() for b in args]
+                    vals.append(f(*call).item())
+            fd.view(-1)[i] = (vals[0] - vals[1]) / (2 * h)
+        np.testing.assert_allclose(g.cpu().numpy(), fd.cpu().numpy(), rtol=1e-5, atol=1e-6)
+
+
+def test_functional_mirrors_match_oracle(golden_likelihood):
+    """torchtree_gb300.functional vs the oracle's restatement of the same functions."""
+    from oracle import likelihood as OL
+    from tests.oracle_cases import model_pieces, tips_from_record
+    from torchtree_gb300 import functional as F
+
+    rec = golden_likelihood["hky_w4_t12_b3"]
+    x = record_inputs(rec, requires_grad=False)
+    tips, w = tips_from_record(rec)
+    q, pi, rates, probs, bls = model_pieces(rec, x)
+    mats = OL.p_t_symmetric(q, pi, bls.unsqueeze(-1) * rates.unsqueeze(-2)).detach()
+    freqs = pi.unsqueeze(-2).detach()
+    props = probs.unsqueeze(-1).unsqueeze(-1).detach()
+    parts = list(tips) + [None] * (len(tips) - 1)
+    post = rec["postorder"]
+    for ref_fn, gpu_fn in ((OL.treelikelihood_discrete, F.calculate_treelikelihood_discrete),
+                           (OL.treelikelihood_discrete_rescaled, F.calculate_treelikelihood_discrete_rescaled)):
+        m1 = mats.clone().requires_grad_()
+        expected = ref_fn(parts, w, post, m1, freqs, props)
+        (g_ref,) = torch.autograd.grad(expected.sum(), [m1])
+        m2 = mats.cuda().requires_grad_()
+        got = gpu_fn(parts, w, post, m2, freqs.cuda(), props.cuda())
+        assert got.shape == expected.shape
+        np.testing.assert_allclose(got.detach().cpu().numpy(), expected.numpy(), rtol=1e-12)
+        (g_gpu,) = torch.autograd.grad(got.sum(), [m2])
+        np.testing.assert_allclose(g_gpu.cpu().numpy(), g_ref.numpy(), rtol=1e-9,
+                                   atol=1e-9 * g_ref.abs().max().item())
+    # tip-state variants
+    srec = dict(rec, tip_states=True)
+    stips, sw = tips_from_record(srec)
+    sparts = list(stips) + [None] * (len(stips) - 1)
+    expected = OL.treelikelihood_tip_states_discrete_rescaled(sparts, sw, post, mats, freqs, props)
+    got = F.calculate_treelikelihood_tip_states_discrete_rescaled(sparts, sw, post, mats.cuda(), freqs.cuda(),
+                                                                  props.cuda())
+    np.testing.assert_allclose(got.cpu().numpy(), expected.numpy(), rtol=1e-12)
+    # single-category function (tree_likelihood.py:14-37)
+    m0 = mats[..., 0, :, :]
+    expected = OL.treelikelihood(parts, w, post, m0, freqs)
+    got = F.calculate_treelikelihood(parts, w, post, m0.cuda(), freqs.cuda())
+    np.testing.assert_allclose(got.cpu().numpy(), expected.numpy(), rtol=1e-12)
+
+
+def test_large_tree_properties():
+    """Size-independent checks at a larger size: FP32 vs FP64, determinism, batch slicing."""
+    from torchtree_gb300 import patterns, site_models, substitution, synthetic
+    from torchtree_gb300.likelihood import PhyloLikelihood, batch_inputs
+
+    wl = synthetic.dna_workload("prop", tip_count=400, site_count=6000, batch=4, seed=21, model="gtr",
+                                site_model="gamma", shape=0.5)
+    ca = patterns.compress(wl.sequences)
+    dev = torch.device("cuda")
+    bl, exch, pi, shape = batch_inputs(wl, dev)
+    rates, probs = site_models.gamma_rates(shape, 4)
+    q = substitution.gtr_q(exch, pi)
+    lam, u, w = substitution.eigen_system(q, pi)
+    out = {}
+    for prec in ("f64", "f32"):
+        lik = PhyloLikelihood(wl.topology, ca, 4, 4, batch=4, precision=prec)
+        lik.rescale = True
+        bls = lik.node_branch_lengths(bl)
+        b = bl.clone().requires_grad_()
+        l1 = lik.evaluate_eigen(lam, u, w, lik.node_branch_lengths(b), rates, probs, pi)
+        (g1,) = torch.autograd.grad(l1.sum(), [b])
+        l2 = lik.evaluate_eigen(lam, u, w, bls, rates, probs, pi)
+        assert torch.equal(l1.detach(), l2.detach())  # deterministic
+        out[prec] = (l1.detach().cpu().numpy(), g1.cpu().numpy())
+    np.testing.assert_allclose(out["f32"][0], out["f64"][0], rtol=F32_LNL_RTOL)
+    g64 = out["f64"][1]
+    np.testing.assert_allclose(out["f32"][1], g64, rtol=F32_GRAD_TOL, atol=F32_GRAD_TOL * np.abs(g64).max())
+    assert math.isfinite(float(out["f64"][0].sum()))
+
+
+def test_forward_without_gradient_matches(golden_likelihood):
+    """keep_partials=0 (forward only, no HBM partials) gives the same lnL."""
+    rec = golden_likelihood["gtr_w4_t69"]
+    lnl, _, lik = engine_eval(rec, "f32")
+    eng = lik.engine
+    # the last forward kept partials; rerun without keeping them on the same matrices
+    with torch.no_grad():
+        p = torch.full((1, 4), 0.25, dtype=torch.float64, device="cuda")
+        f = torch.tensor([rec["pi"]], dtype=torch.float64, device="cuda")
+        a = eng.log_likelihood(p, f, rescale=True, keep_partials=False)
+        b = eng.log_likelihood(p, f, rescale=True, keep_partials=True)
+    assert torch.equal(a, b)
+    np.testing.assert_allclose(a.cpu().numpy(), rec["lnl"], rtol=F32_LNL_RTOL)
+    assert eng.device_status() == 0

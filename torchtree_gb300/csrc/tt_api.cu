@@ -1,0 +1,564 @@
+// C ABI of the engine: plan construction (schedule + shared-memory slot
+// assignment), device workspace and the entry points declared in
+// include/torchtree_gb300.h.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <cstring>
+#include <set>
+#include <string>
+#include <vector>
+
+#include "../../include/torchtree_gb300.h"
+#include "tt_launch.h"
+
+namespace {
+
+thread_local std::string g_last_error;
+
+int fail(int code, const std::string &msg) {
+  g_last_error = msg;
+  return code;
+}
+
+int cuda_fail(cudaError_t e, const char *where) {
+  return fail(e == cudaErrorMemoryAllocation ? TT_ERR_OUT_OF_MEMORY : TT_ERR_CUDA,
+              std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+constexpr unsigned long long kTimeoutNs = 2000000000ull;  // bounded device waits: 2 s
+
+}  // namespace
+
+struct tt_plan {
+  int device = 0;
+  int T = 0, I = 0, B = 0, S = 0, K = 0, N = 0, batch = 0, precision = 0;
+  int C = 0, tile = 0, ntiles = 0, slots_fwd = 0, slots_bwd = 0;
+  size_t elem = 0;  // bytes per partial value
+  bool tips_set = false, pmat_set = false, partials_valid = false, grads_valid = false;
+  long long launches = 0;
+  std::vector<int> steps;       // host copy of the schedule (I x 12)
+  std::vector<int> branch_pos;  // B
+  // device buffers
+  int4 *d_steps = nullptr;
+  int *d_branch_pos = nullptr;
+  uint8_t *d_codes = nullptr;
+  void *d_table = nullptr;
+  double *d_weights = nullptr;
+  void *d_pmat = nullptr;
+  void *d_partials = nullptr;
+  double *d_tile_lnl = nullptr;
+  void *d_gpart = nullptr;
+  void *d_rootpart = nullptr;
+  double *d_G = nullptr;
+  double *d_rootgrad = nullptr;
+  int *d_status = nullptr;
+  size_t bytes = 0;
+};
+
+namespace {
+
+template <typename P>
+int dev_alloc(tt_plan *p, P **ptr, size_t bytes, const char *what) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(ptr), bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail(TT_ERR_OUT_OF_MEMORY,
+                std::string("cudaMalloc of ") + what + " (" + std::to_string(bytes) + " bytes) failed: " +
+                    cudaGetErrorString(e));
+  }
+  p->bytes += bytes;
+  return TT_OK;
+}
+
+void release(tt_plan *p) {
+  void *bufs[] = {p->d_steps, p->d_branch_pos, p->d_codes,    p->d_table,   p->d_weights,
+                  p->d_pmat,  p->d_partials,   p->d_tile_lnl, p->d_gpart,   p->d_rootpart,
+                  p->d_G,     p->d_rootgrad,   p->d_status};
+  for (void *b : bufs)
+    if (b) cudaFree(b);
+}
+
+// Build the execution order and the shared-memory slot plan.
+// Post-order: at every node the child whose subtree needs more stack slots
+// is evaluated first (Sethi-Ullman), so the forward stack depth is at most
+// log2(T)+1.  The adjoint walks the same list backwards.
+int build_schedule(tt_plan *p, const int32_t *post) {
+  const int T = p->T, I = p->I, NN = 2 * T - 1;
+  std::vector<int> left(NN, -1), right(NN, -1), parent(NN, -1);
+  std::vector<char> done(NN, 0);
+  for (int t = 0; t < T; ++t) done[t] = 1;
+  for (int s = 0; s < I; ++s) {
+    const int v = post[3 * s], l = post[3 * s + 1], r = post[3 * s + 2];
+    char buf[160];
+    if (v < T || v >= NN || l < 0 || l >= NN || r < 0 || r >= NN || l == r || l == v || r == v) {
+      snprintf(buf, sizeof buf, "postorder triple %d = (%d, %d, %d) is out of range for %d tips", s, v,
+               l, r, T);
+      return fail(TT_ERR_INVALID_ARGUMENT, buf);
+    }
+    if (done[v]) {
+      snprintf(buf, sizeof buf, "node %d appears twice as a parent", v);
+      return fail(TT_ERR_INVALID_ARGUMENT, buf);
+    }
+    if (!done[l] || !done[r]) {
+      snprintf(buf, sizeof buf, "triple %d uses child before it is computed (not a post-order)", s);
+      return fail(TT_ERR_INVALID_ARGUMENT, buf);
+    }
+    if (parent[l] >= 0 || parent[r] >= 0) {
+      snprintf(buf, sizeof buf, "triple %d reuses a child that already has a parent", s);
+      return fail(TT_ERR_INVALID_ARGUMENT, buf);
+    }
+    left[v] = l;
+    right[v] = r;
+    parent[l] = v;
+    parent[r] = v;
+    done[v] = 1;
+  }
+  const int root = post[3 * (I - 1)];
+  if (root != 2 * T - 2)
+    return fail(TT_ERR_INVALID_ARGUMENT,
+                "the last postorder triple must be the root with index 2T-2 (branch i is the branch "
+                "above node i, so B = 2T-2)");
+  for (int v = 0; v < NN; ++v)
+    if (v != root && parent[v] < 0)
+      return fail(TT_ERR_INVALID_ARGUMENT, "node " + std::to_string(v) + " is not connected to the root");
+
+  // stack need per node and child order
+  std::vector<int> need(NN, 0), first(NN, -1);
+  for (int s = 0; s < I; ++s) {
+    const int v = post[3 * s], l = left[v], r = right[v];
+    const int f = need[l] >= need[r] ? l : r;
+    const int g = f == l ? r : l;
+    first[v] = f;
+    need[v] = std::max({need[f], (f >= T ? 1 : 0) + need[g], 1});
+  }
+  std::vector<int> order;
+  order.reserve(I);
+  {
+    std::vector<std::pair<int, int>> st;  // (node, visited children)
+    st.push_back({root, 0});
+    while (!st.empty()) {
+      auto &top = st.back();
+      const int v = top.first;
+      if (v < T) {
+        st.pop_back();
+        continue;
+      }
+      if (top.second == 0) {
+        top.second = 1;
+        st.push_back({first[v], 0});
+      } else if (top.second == 1) {
+        top.second = 2;
+        st.push_back({first[v] == left[v] ? right[v] : left[v], 0});
+      } else {
+        order.push_back(v);
+        st.pop_back();
+      }
+    }
+  }
+  // forward slots
+  p->steps.assign(size_t(I) * tt::kStepInts, -1);
+  std::vector<int> fslot(NN, -1), bslot(NN, -1);
+  std::set<int> free_slots;
+  int next_slot = 0;
+  auto alloc = [&]() {
+    if (!free_slots.empty()) {
+      int s = *free_slots.begin();
+      free_slots.erase(free_slots.begin());
+      return s;
+    }
+    return next_slot++;
+  };
+  for (int s = 0; s < I; ++s) {
+    const int v = order[s], l = left[v], r = right[v];
+    int *rec = &p->steps[size_t(s) * tt::kStepInts];
+    rec[0] = v;
+    rec[1] = l;
+    rec[2] = r;
+    rec[3] = l >= T ? fslot[l] : -1;
+    rec[4] = r >= T ? fslot[r] : -1;
+    if (rec[3] >= 0) free_slots.insert(rec[3]);
+    if (rec[4] >= 0) free_slots.insert(rec[4]);
+    rec[5] = v == root ? -1 : alloc();
+    fslot[v] = rec[5];
+  }
+  p->slots_fwd = std::max(next_slot, 1);
+  free_slots.clear();
+  next_slot = 0;
+  for (int s = I - 1; s >= 0; --s) {
+    const int v = order[s], l = left[v], r = right[v];
+    int *rec = &p->steps[size_t(s) * tt::kStepInts];
+    rec[6] = v == root ? -1 : bslot[v];
+    if (rec[6] >= 0) free_slots.insert(rec[6]);
+    rec[7] = l >= T ? alloc() : -1;
+    rec[8] = r >= T ? alloc() : -1;
+    bslot[l] = rec[7];
+    bslot[r] = rec[8];
+  }
+  p->slots_bwd = std::max(next_slot, 1);
+  p->branch_pos.assign(p->B, -1);
+  for (int s = 0; s < I; ++s) {
+    const int *rec = &p->steps[size_t(s) * tt::kStepInts];
+    p->branch_pos[rec[1]] = 2 * s;
+    p->branch_pos[rec[2]] = 2 * s + 1;
+  }
+  return TT_OK;
+}
+
+int check_device(const tt_plan *p) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return cuda_fail(e, "cudaGetDevice");
+  if (dev != p->device)
+    return fail(TT_ERR_INVALID_ARGUMENT, "the current CUDA device differs from the plan's device");
+  return TT_OK;
+}
+
+template <typename T>
+tt::PruneArgs<T> make_args(tt_plan *p, const double *props, const double *freqs, int rescale,
+                           bool keep, double *site_lnl) {
+  tt::PruneArgs<T> a;
+  a.steps = p->d_steps;
+  a.n_steps = p->I;
+  a.tip_count = p->T;
+  a.branch_count = p->B;
+  a.N = p->N;
+  a.K = p->K;
+  a.C = p->C;
+  a.rescale = rescale;
+  a.ntiles = p->ntiles;
+  a.codes = p->d_codes;
+  a.table = static_cast<const T *>(p->d_table);
+  a.pmat = static_cast<const T *>(p->d_pmat);
+  a.props = props;
+  a.freqs = freqs;
+  a.weights = p->d_weights;
+  a.partials = keep ? static_cast<T *>(p->d_partials) : nullptr;
+  a.site_lnl = site_lnl;
+  a.tile_lnl = p->d_tile_lnl;
+  a.gpart = static_cast<T *>(p->d_gpart);
+  a.rootpart = static_cast<T *>(p->d_rootpart);
+  a.status = p->d_status;
+  a.timeout_ns = kTimeoutNs;
+  a.slots = 0;
+  return a;
+}
+
+}  // namespace
+
+extern "C" {
+
+const char *tt_version(void) { return "torchtree_gb300 0.1.0 (sm_103a)"; }
+
+const char *tt_last_error(void) { return g_last_error.c_str(); }
+
+int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
+                   int32_t state_count, int32_t category_count, int32_t pattern_count,
+                   int32_t batch, int32_t precision) {
+  if (!plan || !postorder) return fail(TT_ERR_INVALID_ARGUMENT, "plan and postorder must not be NULL");
+  *plan = nullptr;
+  if (tip_count < 2) return fail(TT_ERR_INVALID_ARGUMENT, "a tree needs at least 2 tips");
+  if (state_count != 4)
+    return fail(TT_ERR_UNSUPPORTED, "this build's pruning kernels support 4-state (nucleotide) models");
+  if (category_count < 1 || category_count > 8)
+    return fail(TT_ERR_INVALID_ARGUMENT, "category_count must be in [1, 8]");
+  if (pattern_count < 1) return fail(TT_ERR_INVALID_ARGUMENT, "pattern_count must be >= 1");
+  if (batch < 1 || batch > 65535) return fail(TT_ERR_INVALID_ARGUMENT, "batch must be in [1, 65535]");
+  if (precision != TT_PRECISION_F32 && precision != TT_PRECISION_F64)
+    return fail(TT_ERR_INVALID_ARGUMENT, "precision must be TT_PRECISION_F32 or TT_PRECISION_F64");
+
+  tt_plan *p = new tt_plan();
+  cudaError_t ce = cudaGetDevice(&p->device);
+  if (ce != cudaSuccess) {
+    delete p;
+    return cuda_fail(ce, "cudaGetDevice");
+  }
+  p->T = tip_count;
+  p->I = tip_count - 1;
+  p->B = 2 * tip_count - 2;
+  p->S = state_count;
+  p->K = category_count;
+  p->N = pattern_count;
+  p->batch = batch;
+  p->precision = precision;
+  p->elem = precision == TT_PRECISION_F32 ? 4 : 8;
+  int rc = build_schedule(p, postorder);
+  if (rc != TT_OK) {
+    delete p;
+    return rc;
+  }
+  int smem_max = 0;
+  cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
+  const int *tiles = precision == TT_PRECISION_F32 ? tt::kTilesF32 : tt::kTilesF64;
+  p->tile = 0;
+  for (int i = 0; i < 2 && !p->tile; ++i) {
+    size_t f, b;
+    if (precision == TT_PRECISION_F32) {
+      f = tt::prune_smem_bytes<float>(4, p->K, 256, p->slots_fwd, tiles[i], false);
+      b = tt::prune_smem_bytes<float>(4, p->K, 256, p->slots_bwd, tiles[i], true);
+    } else {
+      f = tt::prune_smem_bytes<double>(4, p->K, 256, p->slots_fwd, tiles[i], false);
+      b = tt::prune_smem_bytes<double>(4, p->K, 256, p->slots_bwd, tiles[i], true);
+    }
+    if (std::max(f, b) <= size_t(smem_max)) p->tile = tiles[i];
+  }
+  if (!p->tile) {
+    delete p;
+    return fail(TT_ERR_UNSUPPORTED, "tree needs " + std::to_string(std::max(p->slots_fwd, p->slots_bwd)) +
+                                        " shared-memory slots, more than one CTA can hold");
+  }
+  p->ntiles = (p->N + p->tile - 1) / p->tile;
+
+  const size_t kss = size_t(p->K) * p->S * p->S;
+  const size_t I1 = size_t(std::max(p->I - 1, 1));
+  rc = TT_OK;
+  if (!rc) rc = dev_alloc(p, &p->d_steps, p->steps.size() * sizeof(int), "schedule");
+  if (!rc) rc = dev_alloc(p, &p->d_branch_pos, size_t(p->B) * sizeof(int), "branch map");
+  if (!rc) rc = dev_alloc(p, &p->d_codes, size_t(p->T) * p->N, "tip codes");
+  if (!rc) rc = dev_alloc(p, &p->d_table, size_t(256) * p->S * p->elem, "code table");
+  if (!rc) rc = dev_alloc(p, &p->d_weights, size_t(p->N) * sizeof(double), "weights");
+  if (!rc) rc = dev_alloc(p, &p->d_pmat, size_t(batch) * p->I * 2 * kss * p->elem, "transition matrices");
+  if (!rc)
+    rc = dev_alloc(p, &p->d_partials, size_t(batch) * I1 * p->K * size_t(p->N) * p->S * p->elem,
+                   "partials");
+  if (!rc) rc = dev_alloc(p, &p->d_tile_lnl, size_t(batch) * p->ntiles * sizeof(double), "tile sums");
+  if (!rc)
+    rc = dev_alloc(p, &p->d_gpart, size_t(batch) * p->B * p->ntiles * kss * p->elem, "gradient tiles");
+  if (!rc)
+    rc = dev_alloc(p, &p->d_rootpart, size_t(batch) * p->ntiles * (p->S + p->K) * p->elem, "root tiles");
+  if (!rc) rc = dev_alloc(p, &p->d_G, size_t(batch) * p->B * kss * sizeof(double), "dlnL/dP");
+  if (!rc) rc = dev_alloc(p, &p->d_rootgrad, size_t(batch) * (p->S + p->K) * sizeof(double), "root grads");
+  if (!rc) rc = dev_alloc(p, &p->d_status, sizeof(int), "status");
+  if (rc) {
+    release(p);
+    delete p;
+    return rc;
+  }
+  ce = cudaMemcpy(p->d_steps, p->steps.data(), p->steps.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess)
+    ce = cudaMemcpy(p->d_branch_pos, p->branch_pos.data(), p->branch_pos.size() * sizeof(int),
+                    cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) ce = cudaMemset(p->d_status, 0, sizeof(int));
+  if (ce != cudaSuccess) {
+    release(p);
+    delete p;
+    return cuda_fail(ce, "plan upload");
+  }
+  *plan = p;
+  return TT_OK;
+}
+
+int tt_plan_destroy(tt_plan *plan) {
+  if (!plan) return TT_OK;
+  release(plan);
+  delete plan;
+  return TT_OK;
+}
+
+int tt_plan_workspace_bytes(const tt_plan *plan, size_t *bytes) {
+  if (!plan || !bytes) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  *bytes = plan->bytes;
+  return TT_OK;
+}
+
+int tt_plan_set_tips(tt_plan *p, const uint8_t *codes, const double *code_table, int32_t code_count,
+                     const double *weights) {
+  if (!p || !codes || !code_table || !weights) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (code_count < 1 || code_count > 256)
+    return fail(TT_ERR_INVALID_ARGUMENT, "code_count must be in [1, 256]");
+  int rc = check_device(p);
+  if (rc) return rc;
+  const size_t tn = size_t(p->T) * p->N;
+  for (size_t i = 0; i < tn; ++i)
+    if (codes[i] >= code_count)
+      return fail(TT_ERR_INVALID_ARGUMENT, "tip code " + std::to_string(codes[i]) + " at position " +
+                                               std::to_string(i) + " is >= code_count");
+  for (int n = 0; n < p->N; ++n)
+    if (!(weights[n] >= 0.0)) return fail(TT_ERR_INVALID_ARGUMENT, "pattern weights must be >= 0");
+  std::vector<unsigned char> table(size_t(code_count) * p->S * p->elem);
+  for (size_t i = 0; i < size_t(code_count) * p->S; ++i) {
+    if (p->precision == TT_PRECISION_F32) {
+      float f = float(code_table[i]);
+      std::memcpy(&table[i * 4], &f, 4);
+    } else {
+      std::memcpy(&table[i * 8], &code_table[i], 8);
+    }
+  }
+  cudaError_t e = cudaMemcpy(p->d_codes, codes, tn, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(p->d_table, table.data(), table.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(p->d_weights, weights, size_t(p->N) * sizeof(double), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_fail(e, "tt_plan_set_tips upload");
+  p->C = code_count;
+  p->tips_set = true;
+  p->partials_valid = false;
+  return TT_OK;
+}
+
+int tt_update_transition_matrices(tt_plan *p, const double *lam, const double *U, const double *W,
+                                  const double *bl, const double *rates, void *stream) {
+  if (!p || !lam || !U || !W || !bl || !rates) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  int rc = check_device(p);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e =
+      p->precision == TT_PRECISION_F32
+          ? tt::launch_pmatrix_f32(lam, U, W, bl, rates, p->d_branch_pos, static_cast<float *>(p->d_pmat),
+                                   p->S, p->B, p->K, p->I, p->batch, s)
+          : tt::launch_pmatrix_f64(lam, U, W, bl, rates, p->d_branch_pos, static_cast<double *>(p->d_pmat),
+                                   p->S, p->B, p->K, p->I, p->batch, s);
+  if (e != cudaSuccess) return cuda_fail(e, "transition-matrix launch");
+  p->launches += 1;
+  p->pmat_set = true;
+  p->partials_valid = false;
+  return TT_OK;
+}
+
+int tt_set_transition_matrices(tt_plan *p, const double *matrices, void *stream) {
+  if (!p || !matrices) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  int rc = check_device(p);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  const int kss = p->K * p->S * p->S;
+  cudaError_t e = p->precision == TT_PRECISION_F32
+                      ? tt::launch_scatter_f32(matrices, p->d_branch_pos, static_cast<float *>(p->d_pmat),
+                                               p->B, kss, p->I, p->batch, s)
+                      : tt::launch_scatter_f64(matrices, p->d_branch_pos, static_cast<double *>(p->d_pmat),
+                                               p->B, kss, p->I, p->batch, s);
+  if (e != cudaSuccess) return cuda_fail(e, "transition-matrix scatter launch");
+  p->launches += 1;
+  p->pmat_set = true;
+  p->partials_valid = false;
+  return TT_OK;
+}
+
+int tt_log_likelihood(tt_plan *p, const double *props, const double *freqs, int32_t rescale,
+                      int32_t keep_partials, double *lnl, double *site_lnl, void *stream) {
+  if (!p || !props || !freqs || !lnl) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!p->tips_set) return fail(TT_ERR_NOT_READY, "tt_plan_set_tips has not been called");
+  if (!p->pmat_set) return fail(TT_ERR_NOT_READY, "transition matrices have not been set");
+  int rc = check_device(p);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (p->precision == TT_PRECISION_F32) {
+    auto a = make_args<float>(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, site_lnl);
+    a.slots = p->slots_fwd;
+    e = tt::launch_prune_f32(a, false, p->tile, p->batch, s);
+  } else {
+    auto a = make_args<double>(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, site_lnl);
+    a.slots = p->slots_fwd;
+    e = tt::launch_prune_f64(a, false, p->tile, p->batch, s);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "post-order launch");
+  e = tt::launch_reduce_lnl(p->d_tile_lnl, lnl, p->batch, p->ntiles, s);
+  if (e != cudaSuccess) return cuda_fail(e, "likelihood reduction launch");
+  p->launches += 2;
+  p->partials_valid = keep_partials != 0;
+  return TT_OK;
+}
+
+int tt_gradient(tt_plan *p, const double *props, const double *freqs, double *grad_matrices,
+                double *grad_frequencies, double *grad_weights, void *stream) {
+  if (!p || !props || !freqs) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!p->partials_valid)
+    return fail(TT_ERR_NOT_READY,
+                "tt_gradient needs a preceding tt_log_likelihood with keep_partials=1 for the same matrices");
+  int rc = check_device(p);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaError_t e;
+  if (p->precision == TT_PRECISION_F32) {
+    auto a = make_args<float>(p, props, freqs, 1, true, nullptr);
+    a.slots = p->slots_bwd;
+    e = tt::launch_prune_f32(a, true, p->tile, p->batch, s);
+    if (e == cudaSuccess)
+      e = tt::launch_reduce_f32(static_cast<const float *>(p->d_gpart),
+                                static_cast<const float *>(p->d_rootpart), p->d_G, p->d_rootgrad,
+                                p->d_rootgrad + size_t(p->batch) * p->S, p->batch, p->B, p->ntiles, p->S,
+                                p->K, s);
+  } else {
+    auto a = make_args<double>(p, props, freqs, 1, true, nullptr);
+    a.slots = p->slots_bwd;
+    e = tt::launch_prune_f64(a, true, p->tile, p->batch, s);
+    if (e == cudaSuccess)
+      e = tt::launch_reduce_f64(static_cast<const double *>(p->d_gpart),
+                                static_cast<const double *>(p->d_rootpart), p->d_G, p->d_rootgrad,
+                                p->d_rootgrad + size_t(p->batch) * p->S, p->batch, p->B, p->ntiles, p->S,
+                                p->K, s);
+  }
+  if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
+  p->launches += 3;
+  const size_t kss = size_t(p->K) * p->S * p->S;
+  if (grad_matrices) {
+    e = cudaMemcpyAsync(grad_matrices, p->d_G, size_t(p->batch) * p->B * kss * sizeof(double),
+                        cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "dlnL/dP copy");
+  }
+  if (grad_frequencies) {
+    e = cudaMemcpyAsync(grad_frequencies, p->d_rootgrad, size_t(p->batch) * p->S * sizeof(double),
+                        cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "dlnL/dpi copy");
+  }
+  if (grad_weights) {
+    e = cudaMemcpyAsync(grad_weights, p->d_rootgrad + size_t(p->batch) * p->S,
+                        size_t(p->batch) * p->K * sizeof(double), cudaMemcpyDeviceToDevice, s);
+    if (e != cudaSuccess) return cuda_fail(e, "dlnL/dc copy");
+  }
+  p->grads_valid = true;
+  return TT_OK;
+}
+
+int tt_transition_matrices_gradient(tt_plan *p, const double *lam, const double *U, const double *W,
+                                    const double *bl, const double *rates, double *dlam, double *dU,
+                                    double *dW, double *dbl, double *drates, void *stream) {
+  if (!p || !lam || !U || !W || !bl || !rates) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!p->grads_valid) return fail(TT_ERR_NOT_READY, "tt_gradient has not been called");
+  int rc = check_device(p);
+  if (rc) return rc;
+  cudaError_t e = tt::launch_pmatrix_backward(p->d_G, lam, U, W, bl, rates, p->S, p->B, p->K, p->batch,
+                                              dlam, dU, dW, dbl, drates, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "transition-matrix gradient launch");
+  p->launches += 1;
+  return TT_OK;
+}
+
+int tt_plan_device_status(tt_plan *p, void *stream, int32_t *status, int32_t reset) {
+  if (!p || !status) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  int v = 0;
+  cudaError_t e = cudaMemcpyAsync(&v, p->d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return cuda_fail(e, "status read");
+  *status = v;
+  if (reset) {
+    e = cudaMemsetAsync(p->d_status, 0, sizeof(int), s);
+    if (e != cudaSuccess) return cuda_fail(e, "status reset");
+  }
+  return TT_OK;
+}
+
+int tt_schedule(int32_t tip_count, const int32_t *postorder, int32_t *steps, int32_t *slot_counts) {
+  if (!postorder || !steps || !slot_counts) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (tip_count < 2) return fail(TT_ERR_INVALID_ARGUMENT, "a tree needs at least 2 tips");
+  tt_plan tmp;
+  tmp.T = tip_count;
+  tmp.I = tip_count - 1;
+  tmp.B = 2 * tip_count - 2;
+  const int rc = build_schedule(&tmp, postorder);
+  if (rc != TT_OK) return rc;
+  std::memcpy(steps, tmp.steps.data(), tmp.steps.size() * sizeof(int));
+  slot_counts[0] = tmp.slots_fwd;
+  slot_counts[1] = tmp.slots_bwd;
+  return TT_OK;
+}
+
+int tt_plan_launch_count(const tt_plan *p, int64_t *count) {
+  if (!p || !count) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  *count = p->launches;
+  return TT_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,159 @@
+"""Python handle on a C-ABI plan (``include/torchtree_gb300.h``).
+
+A ``LikelihoodEngine`` owns one plan: the topology schedule, the resident
+tip codes and pattern weights, and the device workspace for a fixed batch
+size.  Every method launches on torch's current CUDA stream and takes
+contiguous CUDA float64 tensors.
+"""
+from __future__ import annotations
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native
+from ._native import check, ptr
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _dev(t: torch.Tensor, device) -> torch.Tensor:
+    return t.detach().to(device=device, dtype=torch.float64).contiguous()
+
+
+class LikelihoodEngine:
+    """Batched pruning likelihood + gradient for one topology and alignment.
+
+    ``postorder``: ``[T-1, 3]`` (node, left, right) triples, root 2T-2 last.
+    ``codes [T, N]`` uint8 indexing ``table [C, S]``; ``weights [N]``.
+    ``precision``: ``"f32"`` (rescaled FP32 partials) or ``"f64"``.
+    """
+
+    def __init__(self, postorder, tip_count: int, state_count: int, category_count: int,
+                 codes, table, weights, batch: int = 1, precision: str = "f32", device=None):
+        if not torch.cuda.is_available():
+            raise RuntimeError("torchtree_gb300 needs a CUDA device; there is no CPU fallback")
+        self.lib = _native.load()
+        self.device = (torch.device("cuda", torch.cuda.current_device()) if device is None
+                       else torch.device(device))
+        self.tip_count = int(tip_count)
+        self.state_count = int(state_count)
+        self.category_count = int(category_count)
+        codes = np.ascontiguousarray(np.asarray(codes, dtype=np.uint8))
+        self.pattern_count = int(codes.shape[1])
+        self.batch = int(batch)
+        self.precision = precision
+        self.branch_count = 2 * self.tip_count - 2
+        post = np.ascontiguousarray(np.asarray(postorder, dtype=np.int32).reshape(-1, 3))
+        prec = {"f32": _native.TT_PRECISION_F32, "f64": _native.TT_PRECISION_F64}[precision]
+        handle = ctypes.c_void_p()
+        with torch.cuda.device(self.device):
+            check(self.lib.tt_plan_create(ctypes.byref(handle), self.tip_count,
+                                          post.ctypes.data_as(ctypes.POINTER(ctypes.c_int32)),
+                                          self.state_count, self.category_count, self.pattern_count,
+                                          self.batch, prec))
+        self._plan = handle
+        table = np.ascontiguousarray(np.asarray(table, dtype=np.float64))
+        w = np.ascontiguousarray(np.asarray(weights, dtype=np.float64))
+        with torch.cuda.device(self.device):
+            check(self.lib.tt_plan_set_tips(self._plan, ptr(codes), ptr(table), int(table.shape[0]),
+                                            ptr(w)))
+        self.token = 0  # bumped by every forward that keeps partials
+
+    # ---------------------------------------------------------------- lifetime
+    def close(self):
+        if getattr(self, "_plan", None):
+            self.lib.tt_plan_destroy(self._plan)
+            self._plan = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    @property
+    def workspace_bytes(self) -> int:
+        n = ctypes.c_size_t()
+        check(self.lib.tt_plan_workspace_bytes(self._plan, ctypes.byref(n)))
+        return int(n.value)
+
+    @property
+    def launch_count(self) -> int:
+        n = ctypes.c_int64()
+        check(self.lib.tt_plan_launch_count(self._plan, ctypes.byref(n)))
+        return int(n.value)
+
+    def device_status(self, reset: bool = True) -> int:
+        s = ctypes.c_int32()
+        check(self.lib.tt_plan_device_status(self._plan, _stream(), ctypes.byref(s), int(reset)))
+        return int(s.value)
+
+    # ------------------------------------------------------------- operations
+    def set_eigen(self, lam, u, w, branch_lengths, rates):
+        """Transition matrices from ``Q = U diag(lam) W`` (all FP64 device tensors).
+
+        ``lam [b,S]``, ``u``/``w`` ``[b,S,S]``, ``branch_lengths [b,2T-2]``,
+        ``rates [b,K]``.
+        """
+        args = [_dev(x, self.device) for x in (lam, u, w, branch_lengths, rates)]
+        self._check_shapes(*args)
+        check(self.lib.tt_update_transition_matrices(self._plan, *map(ptr, args), _stream()))
+        self._keep = args  # keep alive until the launch has consumed them
+
+    def set_matrices(self, mats):
+        """Transition matrices ``[b, 2T-2, K, S, S]`` given directly."""
+        m = _dev(mats, self.device)
+        exp = (self.batch, self.branch_count, self.category_count, self.state_count, self.state_count)
+        if tuple(m.shape) != exp:
+            raise ValueError(f"matrices must have shape {exp}, got {tuple(m.shape)}")
+        check(self.lib.tt_set_transition_matrices(self._plan, ptr(m), _stream()))
+        self._keep = [m]
+
+    def log_likelihood(self, props, freqs, rescale: bool = True, keep_partials: bool = False,
+                       site: bool = False):
+        """lnL ``[b]`` (and per-pattern site lnL ``[b,N]`` when ``site``)."""
+        p = _dev(props, self.device).expand(self.batch, self.category_count).contiguous()
+        f = _dev(freqs, self.device).expand(self.batch, self.state_count).contiguous()
+        out = torch.empty(self.batch, dtype=torch.float64, device=self.device)
+        site_out = torch.empty(self.batch, self.pattern_count, dtype=torch.float64,
+                               device=self.device) if site else None
+        check(self.lib.tt_log_likelihood(self._plan, ptr(p), ptr(f), int(rescale), int(keep_partials),
+                                         ptr(out), ptr(site_out), _stream()))
+        if keep_partials:
+            self.token += 1
+        self._root_inputs = (p, f)
+        return (out, site_out) if site else out
+
+    def gradient(self, props, freqs, want_matrices: bool = False):
+        """``(dlnL/dP [b,B,K,S,S] or None, dlnL/dpi [b,S], dlnL/dc [b,K])``."""
+        p = _dev(props, self.device).expand(self.batch, self.category_count).contiguous()
+        f = _dev(freqs, self.device).expand(self.batch, self.state_count).contiguous()
+        dP = torch.empty(self.batch, self.branch_count, self.category_count, self.state_count,
+                         self.state_count, dtype=torch.float64, device=self.device) if want_matrices else None
+        dpi = torch.empty(self.batch, self.state_count, dtype=torch.float64, device=self.device)
+        dc = torch.empty(self.batch, self.category_count, dtype=torch.float64, device=self.device)
+        check(self.lib.tt_gradient(self._plan, ptr(p), ptr(f), ptr(dP), ptr(dpi), ptr(dc), _stream()))
+        return dP, dpi, dc
+
+    def eigen_gradient(self, lam, u, w, branch_lengths, rates):
+        """Chain dlnL/dP through the eigen form: ``(dlam, dU, dW, dt, dr)``."""
+        args = [_dev(x, self.device) for x in (lam, u, w, branch_lengths, rates)]
+        b, S, K, B = self.batch, self.state_count, self.category_count, self.branch_count
+        kw = dict(dtype=torch.float64, device=self.device)
+        dlam, du, dw = torch.empty(b, S, **kw), torch.empty(b, S, S, **kw), torch.empty(b, S, S, **kw)
+        dt, dr = torch.empty(b, B, **kw), torch.empty(b, K, **kw)
+        check(self.lib.tt_transition_matrices_gradient(self._plan, *map(ptr, args), ptr(dlam), ptr(du),
+                                                       ptr(dw), ptr(dt), ptr(dr), _stream()))
+        return dlam, du, dw, dt, dr
+
+    def _check_shapes(self, lam, u, w, bl, r):
+        b, S, K, B = self.batch, self.state_count, self.category_count, self.branch_count
+        for name, t, shp in (("eigenvalues", lam, (b, S)), ("eigenvectors", u, (b, S, S)),
+                             ("inverse eigenvectors", w, (b, S, S)), ("branch lengths", bl, (b, B)),
+                             ("category rates", r, (b, K))):
+            if tuple(t.shape) != shp:
+                raise ValueError(f"{name} must have shape {shp}, got {tuple(t.shape)}")

@@ -1,0 +1,123 @@
+"""Site-pattern compression (vectorised; bit-exact with torchtree).
+
+torchtree's ``compress`` (torchtree/evolution/site_pattern.py:69-97) counts
+alignment columns with a ``Counter`` and sorts the distinct columns as
+tuples of characters in taxa order.  Comparing such tuples is comparing the
+columns' bytes lexicographically, which is exactly the order
+``numpy.unique(axis=1)`` produces on a ``[T, L]`` uint8 matrix, with the
+counts as the int64 weights (site_pattern.py:94).
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass
+
+import numpy as np
+
+from .datatype import DataType, Nucleotide
+
+
+@dataclass
+class CompressedAlignment:
+    """Device-ready compressed alignment.
+
+    ``codes``: uint8 ``[T, N]`` indexing ``table`` ``[C, S]`` (float64);
+    ``weights``: int64 ``[N]``; ``columns``: uint8 ``[T, N]`` raw bytes of
+    the distinct columns.
+    """
+
+    codes: np.ndarray
+    table: np.ndarray
+    weights: np.ndarray
+    columns: np.ndarray
+
+    @property
+    def pattern_count(self) -> int:
+        return int(self.weights.shape[0])
+
+    def tip_partials(self) -> np.ndarray:
+        """Partials ``[T, S, N]`` (the reference's per-tip ``[S, N]`` tensors)."""
+        return np.transpose(self.table[self.codes], (0, 2, 1))
+
+
+def as_byte_matrix(sequences) -> np.ndarray:
+    """Stack equal-length sequences (str or bytes) into a uint8 ``[T, L]``."""
+    rows = [np.frombuffer(s.encode("latin-1") if isinstance(s, str) else bytes(s), dtype=np.uint8)
+            for s in sequences]
+    length = {len(r) for r in rows}
+    if len(length) != 1:
+        raise ValueError("sequences must all have the same length")
+    return np.stack(rows)
+
+
+def select_sites(matrix: np.ndarray, indices) -> np.ndarray:
+    """Columns picked by a list of ints / slices, in the given order (site_pattern.py:85-89)."""
+    if indices is None:
+        return matrix
+    picks = []
+    L = matrix.shape[1]
+    for idx in indices:
+        if isinstance(idx, slice):
+            picks.extend(range(L)[idx])
+        else:
+            picks.append(int(idx))
+    return matrix[:, picks]
+
+
+def unique_columns(matrix: np.ndarray):
+    """Distinct columns in lexicographic (taxa-order) byte order and counts."""
+    if matrix.shape[1] == 0:
+        return matrix, np.zeros(0, dtype=np.int64)
+    cols, counts = np.unique(matrix, axis=1, return_counts=True)
+    return cols, counts.astype(np.int64)
+
+
+def compress(sequences, data_type: DataType | None = None, use_ambiguities: bool = False,
+             tip_states: bool = False, indices=None) -> CompressedAlignment:
+    """Compress an alignment given as per-tip sequences in taxa order.
+
+    ``use_ambiguities`` / ``tip_states`` select torchtree's
+    ``compute_tips_partials(use_ambiguities)`` or ``compute_tips_states()``
+    encodings.  Only single-character alphabets are handled here.
+    """
+    data_type = data_type or Nucleotide()
+    if data_type.size != 1:
+        raise ValueError("multi-character data types are compressed by the codon packer")
+    matrix = select_sites(as_byte_matrix(sequences), indices)
+    cols, weights = unique_columns(matrix)
+    table, lut = data_type.byte_luts(use_ambiguities, tip_states)
+    codes = lut[cols]
+    # keep only the table rows in use, preserving order
+    used = np.unique(codes)
+    remap = np.zeros(table.shape[0], dtype=np.uint8)
+    remap[used] = np.arange(used.size, dtype=np.uint8)
+    if not tip_states:
+        table = table[used]
+        codes = remap[codes]
+    return CompressedAlignment(codes=np.ascontiguousarray(codes), table=table, weights=weights,
+                               columns=cols)
+
+
+def from_tip_partials(tips, weights) -> CompressedAlignment:
+    """Codes and table from arbitrary tip partial tensors ``T x [S, N]``.
+
+    The distinct tip columns become the table; at most 256 are allowed.
+    """
+    arr = np.stack([np.asarray(t, dtype=np.float64) for t in tips])  # [T,S,N]
+    T, S, N = arr.shape
+    cols = np.ascontiguousarray(np.transpose(arr, (0, 2, 1)).reshape(T * N, S))
+    table, inverse = np.unique(cols, axis=0, return_inverse=True)
+    if table.shape[0] > 256:
+        raise ValueError(f"{table.shape[0]} distinct tip partial vectors; at most 256 are supported")
+    codes = inverse.reshape(T, N).astype(np.uint8)
+    return CompressedAlignment(codes=codes, table=table, weights=np.asarray(weights),
+                               columns=np.zeros((T, 0), dtype=np.uint8))
+
+
+def from_tip_states(tips, state_count: int, weights) -> CompressedAlignment:
+    """Codes from tip state tensors ``T x [N]`` with values in ``[0, S]``."""
+    codes = np.stack([np.asarray(t, dtype=np.int64) for t in tips])
+    if codes.min() < 0 or codes.max() > state_count:
+        raise ValueError("tip states must lie in [0, state_count]")
+    table = np.vstack([np.eye(state_count), np.ones((1, state_count))])
+    return CompressedAlignment(codes=codes.astype(np.uint8), table=table, weights=np.asarray(weights),
+                               columns=np.zeros((codes.shape[0], 0), dtype=np.uint8))
