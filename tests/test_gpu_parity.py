@@ -167,7 +167,10 @@ def test_finite_differences_fp64(golden_likelihood):
         lam, u, w = substitution.eigen_system(q, pi)
         return lik.evaluate_eigen(lam, u, w, lik.node_branch_lengths(bl), rates, probs.expand(1, 4), pi).sum()
 
-    t = lambda v: torch.tensor([v], dtype=torch.float64, device=dev, requires_grad=True)  # noqa: E731
+    def t(v):
+        x = torch.tensor(v, dtype=torch.float64, device=dev)
+        return (x if x.dim() == 2 else x.unsqueeze(0)).requires_grad_()
+
     args = [t(rec["branch_lengths"]), t(rec["exch"]), t(rec["pi"]), t(rec["shape"])]
     grads = torch.autograd.grad(f(*args), args)
     for a, g in zip(args, grads):
@@ -209,7 +212,7 @@ def test_functional_mirrors_match_oracle(golden_likelihood):
         m2 = mats.cuda().requires_grad_()
         got = gpu_fn(parts, w, post, m2, freqs.cuda(), props.cuda())
         assert got.shape == expected.shape
-        np.testing.assert_allclose(got.detach().cpu().numpy(), expected.numpy(), rtol=1e-12)
+        np.testing.assert_allclose(got.detach().cpu().numpy(), expected.detach().numpy(), rtol=1e-12)
         (g_gpu,) = torch.autograd.grad(got.sum(), [m2])
         np.testing.assert_allclose(g_gpu.cpu().numpy(), g_ref.numpy(), rtol=1e-9,
                                    atol=1e-9 * g_ref.abs().max().item())
@@ -266,7 +269,7 @@ def test_forward_without_gradient_matches(golden_likelihood):
     # the last forward kept partials; rerun without keeping them on the same matrices
     with torch.no_grad():
         p = torch.full((1, 4), 0.25, dtype=torch.float64, device="cuda")
-        f = torch.tensor([rec["pi"]], dtype=torch.float64, device="cuda")
+        f = torch.tensor(rec["pi"], dtype=torch.float64, device="cuda").reshape(1, 4)
         a = eng.log_likelihood(p, f, rescale=True, keep_partials=False)
         b = eng.log_likelihood(p, f, rescale=True, keep_partials=True)
     assert torch.equal(a, b)

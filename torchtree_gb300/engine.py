@@ -116,8 +116,8 @@ class LikelihoodEngine:
     def log_likelihood(self, props, freqs, rescale: bool = True, keep_partials: bool = False,
                        site: bool = False):
         """lnL ``[b]`` (and per-pattern site lnL ``[b,N]`` when ``site``)."""
-        p = _dev(props, self.device).expand(self.batch, self.category_count).contiguous()
-        f = _dev(freqs, self.device).expand(self.batch, self.state_count).contiguous()
+        p = self._per_sample(props, self.category_count)
+        f = self._per_sample(freqs, self.state_count)
         out = torch.empty(self.batch, dtype=torch.float64, device=self.device)
         site_out = torch.empty(self.batch, self.pattern_count, dtype=torch.float64,
                                device=self.device) if site else None
@@ -130,8 +130,8 @@ class LikelihoodEngine:
 
     def gradient(self, props, freqs, want_matrices: bool = False):
         """``(dlnL/dP [b,B,K,S,S] or None, dlnL/dpi [b,S], dlnL/dc [b,K])``."""
-        p = _dev(props, self.device).expand(self.batch, self.category_count).contiguous()
-        f = _dev(freqs, self.device).expand(self.batch, self.state_count).contiguous()
+        p = self._per_sample(props, self.category_count)
+        f = self._per_sample(freqs, self.state_count)
         dP = torch.empty(self.batch, self.branch_count, self.category_count, self.state_count,
                          self.state_count, dtype=torch.float64, device=self.device) if want_matrices else None
         dpi = torch.empty(self.batch, self.state_count, dtype=torch.float64, device=self.device)
@@ -149,6 +149,13 @@ class LikelihoodEngine:
         check(self.lib.tt_transition_matrices_gradient(self._plan, *map(ptr, args), ptr(dlam), ptr(du),
                                                        ptr(dw), ptr(dt), ptr(dr), _stream()))
         return dlam, du, dw, dt, dr
+
+    def _per_sample(self, x, width):
+        """``[..., width]`` (one row or one per sample) -> contiguous ``[batch, width]``."""
+        t = _dev(x, self.device).reshape(-1, width)
+        if t.shape[0] not in (1, self.batch):
+            raise ValueError(f"expected 1 or {self.batch} rows of width {width}, got {tuple(x.shape)}")
+        return t.expand(self.batch, width).contiguous()
 
     def _check_shapes(self, lam, u, w, bl, r):
         b, S, K, B = self.batch, self.state_count, self.category_count, self.branch_count
