@@ -164,6 +164,34 @@ int tt_plan_device_status(tt_plan *plan, void *stream, int32_t *status,
 int tt_schedule(int32_t tip_count, const int32_t *postorder, int32_t *steps,
                 int32_t *slot_counts);
 
+/*
+ * FP64 log-likelihood that allocates no device memory.  No counterpart in
+ * the reference: it exists for callers that cannot call cudaMalloc (an
+ * application whose own memory manager owns every device byte, or a host
+ * that hands a plug-in device buffers but no right to allocate), for whom
+ * tt_plan_create is closed.  Same result as tt_set_transition_matrices +
+ * tt_log_likelihood on a TT_PRECISION_F64 plan.
+ *   postorder: host int32 [T-1][3]; 2 <= T <= 1024; state_count 4;
+ *   codes device uint8 [T][N] (< code_count), code_table device double
+ *   [code_count][4], weights device double [N], matrices device double
+ *   [b][B][K][4][4], category_weights device [b][K], frequencies device
+ *   [b][4], log_likelihood device double [b].
+ * Scratch lives in one 8 MiB static device array held by every GPU that
+ * loads the library; a problem needing more is rejected with
+ * TT_ERR_INVALID_ARGUMENT.  The first call on a device looks the array up
+ * (make it before any stream capture).  Calls share the array: calls that
+ * overlap on the GPU race and must be serialised by the caller.
+ */
+int tt_log_likelihood_static(int32_t tip_count, const int32_t *postorder,
+                             int32_t state_count, int32_t category_count,
+                             int32_t pattern_count, int32_t batch,
+                             const uint8_t *codes, const double *code_table,
+                             int32_t code_count, const double *weights,
+                             const double *matrices,
+                             const double *category_weights,
+                             const double *frequencies, int32_t rescale,
+                             double *log_likelihood, void *stream);
+
 /* Number of kernel launches the plan issued since creation. */
 int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
 

@@ -41,6 +41,8 @@ SIGNATURES = {
     "tt_plan_device_status": (ctypes.c_int, [_P, _P, _PI32, _I32]),
     "tt_plan_launch_count": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
     "tt_schedule": (ctypes.c_int, [_I32, _PI32, _PI32, _PI32]),
+    "tt_log_likelihood_static": (ctypes.c_int, [_I32, _PI32, _I32, _I32, _I32, _I32, _P, _P, _I32, _P, _P, _P,
+                                                _P, _I32, _P, _P]),
 }
 
 _lib = None

@@ -31,6 +31,11 @@ constexpr unsigned long long kTimeoutNs = 2000000000ull;  // bounded device wait
 
 }  // namespace
 
+namespace tt {
+// Error reporting for entry points defined in other translation units.
+int record_error(int code, const char *msg) { return fail(code, msg); }
+}  // namespace tt
+
 struct tt_plan {
   int device = 0;
   int T = 0, I = 0, B = 0, S = 0, K = 0, N = 0, batch = 0, precision = 0;

@@ -8,6 +8,9 @@
 
 namespace tt {
 
+// Set the calling thread's tt_last_error() message; returns `code`.
+int record_error(int code, const char *msg);
+
 // Pattern tile widths compiled per precision (largest first).
 constexpr int kTilesF32[2] = {128, 64};
 constexpr int kTilesF64[2] = {64, 32};

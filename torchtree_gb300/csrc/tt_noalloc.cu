@@ -1,0 +1,268 @@
+// tt_log_likelihood_static: the FP64 log-likelihood without any device
+// allocation.
+//
+// Some callers cannot call cudaMalloc: code that runs inside an
+// application's own memory manager (which owns every device byte and
+// forbids other allocations), and embedding hosts that give a plug-in
+// device pointers but no permission to allocate.  The plan-based entry
+// points allocate their workspace in tt_plan_create, so they are closed
+// to those callers.  This entry point takes every input and output from
+// the caller and keeps its scratch (step table, transition matrices in
+// step order, padded tip-code table, per-tile sums, status word) in one
+// file-scope __device__ array of kScratchBytes, which every GPU that loads
+// the library holds until the process exits.
+//
+// The first call on each device looks up the array's device address with
+// cudaGetSymbolAddress (this can load the module), so make that first call
+// before any stream capture.  All calls share the array and it keeps the
+// last call's contents; calls whose work overlaps on the GPU (two streams,
+// two host threads) race on it and must be serialised by the caller.
+#include <cuda_runtime.h>
+
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/torchtree_gb300.h"
+#include "tt_launch.h"
+
+namespace {
+
+constexpr size_t kScratchBytes = size_t(8) << 20;  // 8 MiB of scratch
+constexpr int kMaxTips = 1024;
+constexpr int kMaxDevices = 64;
+constexpr int kTableRows = 256;  // codes are uint8: pad the table to every value
+
+}  // namespace
+
+static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
+
+namespace {
+
+std::mutex g_scratch_lock;
+unsigned char *g_scratch_addr[kMaxDevices] = {};
+
+int fail(int code, const char *msg) { return tt::record_error(code, msg); }
+
+// Device address of g_scratch on the current device (looked up once per device).
+int scratch_address(unsigned char **out) {
+  int dev = -1;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail(TT_ERR_CUDA, cudaGetErrorString(e));
+  if (dev < 0 || dev >= kMaxDevices) return fail(TT_ERR_UNSUPPORTED, "device index out of range");
+  std::lock_guard<std::mutex> guard(g_scratch_lock);
+  if (!g_scratch_addr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_scratch);
+    if (e != cudaSuccess) {
+      char buf[200];
+      snprintf(buf, sizeof buf, "cudaGetSymbolAddress of the static scratch failed: %s",
+               cudaGetErrorString(e));
+      return fail(TT_ERR_CUDA, buf);
+    }
+    g_scratch_addr[dev] = static_cast<unsigned char *>(p);
+  }
+  *out = g_scratch_addr[dev];
+  return TT_OK;
+}
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Post-order schedule with shared-memory slots (forward only), built in
+// fixed-size host arrays: the child whose subtree needs more slots is
+// evaluated first, so at most log2(T)+1 slots are live.
+int static_schedule(int T, const int32_t *post, int *steps, int *branch_pos, int *slots_out) {
+  const int I = T - 1, NN = 2 * T - 1;
+  int left[2 * kMaxTips], right[2 * kMaxTips], parent[2 * kMaxTips], need[2 * kMaxTips];
+  int first[2 * kMaxTips], slot[2 * kMaxTips], order[kMaxTips];
+  int stk_node[2 * kMaxTips];
+  unsigned char stk_state[2 * kMaxTips], done[2 * kMaxTips];
+  for (int v = 0; v < NN; ++v) {
+    left[v] = right[v] = parent[v] = first[v] = slot[v] = -1;
+    need[v] = 0;
+    done[v] = v < T;
+  }
+  for (int s = 0; s < I; ++s) {
+    const int v = post[3 * s], l = post[3 * s + 1], r = post[3 * s + 2];
+    if (v < T || v >= NN || l < 0 || l >= NN || r < 0 || r >= NN || l == r || l == v || r == v)
+      return fail(TT_ERR_INVALID_ARGUMENT, "postorder triple out of range");
+    if (done[v]) return fail(TT_ERR_INVALID_ARGUMENT, "a node appears twice as a parent");
+    if (!done[l] || !done[r]) return fail(TT_ERR_INVALID_ARGUMENT, "postorder uses a child before it is computed");
+    if (parent[l] >= 0 || parent[r] >= 0) return fail(TT_ERR_INVALID_ARGUMENT, "a child has two parents");
+    left[v] = l;
+    right[v] = r;
+    parent[l] = parent[r] = v;
+    done[v] = 1;
+    const int f = need[l] >= need[r] ? l : r, g = f == l ? r : l;
+    first[v] = f;
+    int n = need[f] > (f >= T) + need[g] ? need[f] : (f >= T) + need[g];
+    need[v] = n > 1 ? n : 1;
+  }
+  const int root = post[3 * (I - 1)];
+  if (root != 2 * T - 2) return fail(TT_ERR_INVALID_ARGUMENT, "the last postorder triple must be the root 2T-2");
+  for (int v = 0; v < NN; ++v)
+    if (v != root && parent[v] < 0) return fail(TT_ERR_INVALID_ARGUMENT, "a node is not connected to the root");
+  int top = 0, count = 0;
+  stk_node[0] = root;
+  stk_state[0] = 0;
+  while (top >= 0) {
+    const int v = stk_node[top];
+    if (v < T) {
+      --top;
+    } else if (stk_state[top] == 0) {
+      stk_state[top] = 1;
+      ++top;
+      stk_node[top] = first[v];
+      stk_state[top] = 0;
+    } else if (stk_state[top] == 1) {
+      stk_state[top] = 2;
+      ++top;
+      stk_node[top] = first[v] == left[v] ? right[v] : left[v];
+      stk_state[top] = 0;
+    } else {
+      order[count++] = v;
+      --top;
+    }
+  }
+  unsigned long long used = 0;
+  int slots = 1;
+  for (int s = 0; s < I; ++s) {
+    const int v = order[s], l = left[v], r = right[v];
+    int *rec = steps + s * tt::kStepInts;
+    for (int k = 0; k < tt::kStepInts; ++k) rec[k] = -1;
+    rec[0] = v;
+    rec[1] = l;
+    rec[2] = r;
+    rec[3] = l >= T ? slot[l] : -1;
+    rec[4] = r >= T ? slot[r] : -1;
+    if (rec[3] >= 0) used &= ~(1ull << rec[3]);
+    if (rec[4] >= 0) used &= ~(1ull << rec[4]);
+    if (v != root) {
+      int f = 0;
+      while (f < 64 && (used >> f) & 1ull) ++f;
+      if (f == 64) return fail(TT_ERR_UNSUPPORTED, "tree needs more than 64 shared-memory slots");
+      used |= 1ull << f;
+      rec[5] = f;
+      slot[v] = f;
+      if (f + 1 > slots) slots = f + 1;
+    }
+    branch_pos[l] = 2 * s;
+    branch_pos[r] = 2 * s + 1;
+  }
+  *slots_out = slots;
+  return TT_OK;
+}
+
+}  // namespace
+
+extern "C" int tt_log_likelihood_static(int32_t tip_count, const int32_t *postorder, int32_t state_count,
+                                        int32_t category_count, int32_t pattern_count, int32_t batch,
+                                        const uint8_t *codes, const double *code_table, int32_t code_count,
+                                        const double *weights, const double *matrices,
+                                        const double *category_weights, const double *frequencies,
+                                        int32_t rescale, double *log_likelihood, void *stream) {
+  if (!postorder || !codes || !code_table || !weights || !matrices || !category_weights || !frequencies ||
+      !log_likelihood)
+    return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (tip_count < 2 || tip_count > kMaxTips)
+    return fail(TT_ERR_INVALID_ARGUMENT, "tt_log_likelihood_static supports 2 to 1024 tips");
+  if (state_count != 4) return fail(TT_ERR_UNSUPPORTED, "tt_log_likelihood_static supports 4 states");
+  if (category_count < 1 || category_count > 8)
+    return fail(TT_ERR_INVALID_ARGUMENT, "category_count must be in [1, 8]");
+  if (pattern_count < 1 || batch < 1 || batch > 65535)
+    return fail(TT_ERR_INVALID_ARGUMENT, "pattern_count and batch must be >= 1 (batch <= 65535)");
+  if (code_count < 1 || code_count > kTableRows)
+    return fail(TT_ERR_INVALID_ARGUMENT, "code_count must be in [1, 256]");
+
+  const int T = tip_count, I = T - 1, B = 2 * T - 2, S = 4, K = category_count, N = pattern_count;
+  const int kss = K * S * S;
+  int smem_max = 0, dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+
+  int steps[(kMaxTips - 1) * tt::kStepInts];
+  int branch_pos[2 * kMaxTips - 2];
+  int slots = 0;
+  int rc = static_schedule(T, postorder, steps, branch_pos, &slots);
+  if (rc != TT_OK) return rc;
+  int tile = 0;
+  for (int t : tt::kTilesF64)
+    if (!tile && tt::prune_smem_bytes<double>(S, K, kTableRows, slots, t, false) <= size_t(smem_max)) tile = t;
+  if (!tile) return fail(TT_ERR_UNSUPPORTED, "tree needs more shared memory than one CTA can hold");
+  const int ntiles = (N + tile - 1) / tile;
+
+  // carve the scratch
+  size_t off = 0;
+  const size_t o_status = off;
+  off = align256(off + sizeof(int));
+  const size_t o_table = off;
+  off = align256(off + size_t(kTableRows) * S * sizeof(double));
+  const size_t o_steps = off;
+  off = align256(off + size_t(I) * tt::kStepInts * sizeof(int));
+  const size_t o_bpos = off;
+  off = align256(off + size_t(B) * sizeof(int));
+  const size_t o_pmat = off;
+  off = align256(off + size_t(batch) * I * 2 * kss * sizeof(double));
+  const size_t o_tiles = off;
+  off = align256(off + size_t(batch) * ntiles * sizeof(double));
+  if (off > kScratchBytes) {
+    char buf[240];
+    snprintf(buf, sizeof buf,
+             "problem needs %zu bytes of scratch, more than the %zu-byte static scratch of "
+             "tt_log_likelihood_static (fewer tips, categories, samples or patterns, or use the plan API)",
+             off, kScratchBytes);
+    return fail(TT_ERR_INVALID_ARGUMENT, buf);
+  }
+  unsigned char *scratch = nullptr;
+  rc = scratch_address(&scratch);
+  if (rc != TT_OK) return rc;
+  int *d_status = reinterpret_cast<int *>(scratch + o_status);
+  double *d_table = reinterpret_cast<double *>(scratch + o_table);
+  int *d_steps = reinterpret_cast<int *>(scratch + o_steps);
+  int *d_bpos = reinterpret_cast<int *>(scratch + o_bpos);
+  double *d_pmat = reinterpret_cast<double *>(scratch + o_pmat);
+  double *d_tiles = reinterpret_cast<double *>(scratch + o_tiles);
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+
+  // Start-of-call state: status cleared; table rows past code_count and the
+  // tile sums set to NaN, so an out-of-range code or a CTA that gave up on a
+  // bounded wait shows up as a NaN log-likelihood instead of stale data.
+  cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(int), s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_table, 0xff, size_t(kTableRows) * S * sizeof(double), s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_table, code_table, size_t(code_count) * S * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_tiles, 0xff, size_t(batch) * ntiles * sizeof(double), s);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(d_steps, steps, size_t(I) * tt::kStepInts * sizeof(int), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(d_bpos, branch_pos, size_t(B) * sizeof(int), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = tt::launch_scatter_f64(matrices, d_bpos, d_pmat, B, kss, I, batch, s);
+  if (e != cudaSuccess) return fail(TT_ERR_CUDA, cudaGetErrorString(e));
+
+  tt::PruneArgs<double> a;
+  std::memset(&a, 0, sizeof a);
+  a.steps = reinterpret_cast<const int4 *>(d_steps);
+  a.n_steps = I;
+  a.tip_count = T;
+  a.branch_count = B;
+  a.N = N;
+  a.K = K;
+  a.C = kTableRows;
+  a.slots = slots;
+  a.rescale = rescale ? 1 : 0;
+  a.ntiles = ntiles;
+  a.codes = codes;
+  a.table = d_table;
+  a.pmat = d_pmat;
+  a.props = category_weights;
+  a.freqs = frequencies;
+  a.weights = weights;
+  a.partials = nullptr;
+  a.site_lnl = nullptr;
+  a.tile_lnl = d_tiles;
+  a.status = d_status;
+  a.timeout_ns = 2000000000ull;
+  e = tt::launch_prune_f64(a, false, tile, batch, s);
+  if (e == cudaSuccess) e = tt::launch_reduce_lnl(d_tiles, log_likelihood, batch, ntiles, s);
+  if (e != cudaSuccess) return fail(TT_ERR_CUDA, cudaGetErrorString(e));
+  return TT_OK;
+}
