@@ -219,8 +219,9 @@ def main():
     bl, exch, pi, shape = batch_inputs(wl, dev)
     rates, probs = site_models.gamma_rates(shape, K)
     probs = probs.expand(b, K).contiguous()
-    q = substitution.gtr_q(exch, pi)
-    lam, u, w = (t.detach().contiguous() for t in substitution.eigen_system(q, pi))
+    # resident inputs of the timed step: the eigen system is set-up work (host LAPACK)
+    q = substitution.gtr_q(exch.cpu(), pi.cpu())
+    lam, u, w = (t.detach().to(dev).contiguous() for t in substitution.eigen_system(q, pi.cpu()))
     zeros = torch.zeros(b, 1, dtype=torch.float64, device=dev)
     bls = torch.cat([bl, zeros], -1).contiguous()
     rates = rates.detach().contiguous()
@@ -264,7 +265,7 @@ def main():
 
     # per-call timing of the two pruning kernels (each call: one pruning
     # kernel + its small reduction kernels) for the roofline
-    fw, bw = [], []
+    fw, bw, fo = [], [], []
     for _ in range(3):
         e0, e1, e2, e3 = (torch.cuda.Event(enable_timing=True) for _ in range(4))
         eng.set_eigen(lam, u, w, bls, rates)
@@ -273,10 +274,13 @@ def main():
         e1.record(stream)
         eng.gradient(probs, pi)
         e2.record(stream)
+        eng.log_likelihood(probs, pi, rescale=True, keep_partials=False)  # lnL only
+        e3.record(stream)
         torch.cuda.synchronize()
         fw.append(e0.elapsed_time(e1))
         bw.append(e1.elapsed_time(e2))
-    fw_ms, bw_ms = statistics.median(fw), statistics.median(bw)
+        fo.append(e2.elapsed_time(e3))
+    fw_ms, bw_ms, fo_ms = statistics.median(fw), statistics.median(bw), statistics.median(fo)
     elem = 4 if args.precision == "f32" else 8
     I = T - 1
     tile = 128 if args.precision == "f32" else 64
@@ -290,6 +294,8 @@ def main():
         "post_order": {"ms": fw_ms, "bytes": fw_bytes, "gbs": fw_bytes / fw_ms / 1e6},
         "pre_order_adjoint": {"ms": bw_ms, "bytes": bw_bytes, "gbs": bw_bytes / bw_ms / 1e6},
     }
+    lnl_only = {"ms": fo_ms, "evals_per_s": b / (fo_ms / 1e3),
+                "what": "post-order pass without storing partials (lnL only, no gradient)"}
     dom = max(kernels, key=lambda k: kernels[k]["ms"])
     achieved = kernels[dom]["gbs"]
     roofline = {"bound": "hbm", "kernel": dom, "achieved": achieved, "peak": peak, "unit": "GB/s",
@@ -375,6 +381,7 @@ def main():
                            "what": "one batched lnL+gradient call (all samples)"},
             "fp64_dropin": fp64,
             "speedup_vs_fp64": (value / world / fp64["value"]) if fp64 else None,
+            "lnl_only": lnl_only,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
             "clocks": clocks.summary(),
         }

@@ -5,6 +5,7 @@
 
 #include <algorithm>
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <set>
 #include <string>
@@ -39,7 +40,9 @@ int record_error(int code, const char *msg) { return fail(code, msg); }
 struct tt_plan {
   int device = 0;
   int T = 0, I = 0, B = 0, S = 0, K = 0, N = 0, batch = 0, precision = 0;
-  int C = 0, tile = 0, ntiles = 0, slots_fwd = 0, slots_bwd = 0;
+  int C = 0, slots_fwd = 0, slots_bwd = 0;
+  int tile_f = 0, tile_b = 0, ntiles_f = 0, ntiles_b = 0, code_stride = 0;
+  int nstage_f = tt::kStages, nstage_b = tt::kStages;
   size_t elem = 0;  // bytes per partial value
   bool tips_set = false, pmat_set = false, partials_valid = false, grads_valid = false;
   long long launches = 0;
@@ -47,6 +50,7 @@ struct tt_plan {
   std::vector<int> branch_pos;  // B
   // device buffers
   int4 *d_steps = nullptr;
+  int4 *d_steps_rev = nullptr;
   int *d_branch_pos = nullptr;
   uint8_t *d_codes = nullptr;
   void *d_table = nullptr;
@@ -79,7 +83,7 @@ int dev_alloc(tt_plan *p, P **ptr, size_t bytes, const char *what) {
 }
 
 void release(tt_plan *p) {
-  void *bufs[] = {p->d_steps, p->d_branch_pos, p->d_codes,    p->d_table,   p->d_weights,
+  void *bufs[] = {p->d_steps, p->d_steps_rev, p->d_branch_pos, p->d_codes,    p->d_table,   p->d_weights,
                   p->d_pmat,  p->d_partials,   p->d_tile_lnl, p->d_gpart,   p->d_rootpart,
                   p->d_G,     p->d_rootgrad,   p->d_status};
   for (void *b : bufs)
@@ -233,7 +237,10 @@ tt::PruneArgs<T> make_args(tt_plan *p, const double *props, const double *freqs,
   a.K = p->K;
   a.C = p->C;
   a.rescale = rescale;
-  a.ntiles = p->ntiles;
+  a.ntiles = p->ntiles_f;
+  a.code_stride = p->code_stride;
+  a.nstage = p->nstage_f;
+  a.steps_rev = p->d_steps_rev;
   a.codes = p->d_codes;
   a.table = static_cast<const T *>(p->d_table);
   a.pmat = static_cast<const T *>(p->d_pmat);
@@ -296,43 +303,69 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
   }
   int smem_max = 0;
   cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
-  const int *tiles = precision == TT_PRECISION_F32 ? tt::kTilesF32 : tt::kTilesF64;
-  p->tile = 0;
-  for (int i = 0; i < 2 && !p->tile; ++i) {
-    size_t f, b;
-    if (precision == TT_PRECISION_F32) {
-      f = tt::prune_smem_bytes<float>(4, p->K, 256, p->slots_fwd, tiles[i], false);
-      b = tt::prune_smem_bytes<float>(4, p->K, 256, p->slots_bwd, tiles[i], true);
-    } else {
-      f = tt::prune_smem_bytes<double>(4, p->K, 256, p->slots_fwd, tiles[i], false);
-      b = tt::prune_smem_bytes<double>(4, p->K, 256, p->slots_bwd, tiles[i], true);
-    }
-    if (std::max(f, b) <= size_t(smem_max)) p->tile = tiles[i];
+  const bool f32 = precision == TT_PRECISION_F32;
+  const int *ftiles = f32 ? tt::kFwdTilesF32 : tt::kFwdTilesF64;
+  const int *btiles = f32 ? tt::kBwdTilesF32 : tt::kBwdTilesF64;
+  if (f32) {  // ring depths of the FP32 kernels; TT_FWD_STAGES / TT_BWD_STAGES override
+    p->nstage_f = getenv("TT_FWD_STAGES") ? std::max(2, atoi(getenv("TT_FWD_STAGES"))) : tt::kTlFwdStages;
+    p->nstage_b = getenv("TT_BWD_STAGES") ? std::max(2, atoi(getenv("TT_BWD_STAGES"))) : tt::kTlBwdStages;
   }
-  if (!p->tile) {
+  auto smem_of = [&](int tile, bool bwd) {
+    const int slots = bwd ? p->slots_bwd : p->slots_fwd;
+    return f32 ? tt::tl_smem_bytes(p->K, 256, slots, bwd, bwd ? p->nstage_b : p->nstage_f)
+               : tt::prune_smem_bytes<double>(4, p->K, 256, slots, tile, bwd);
+  };
+  // optional overrides for tuning sweeps: TT_FWD_TILE / TT_BWD_TILE.  FP32 rings
+  // shrink (down to 3 stages) before a smaller tile is tried.
+  auto fits = [&](int tile, bool bwd) {
+    int &ns = bwd ? p->nstage_b : p->nstage_f;
+    const int want = ns;
+    for (; ns >= (f32 ? 3 : want); --ns)
+      if (smem_of(tile, bwd) <= size_t(smem_max)) return true;
+    ns = want;
+    return false;
+  };
+  auto pick = [&](const int *cand, bool bwd, const char *env) {
+    const char *o = getenv(env);
+    if (o) {
+      const int want = atoi(o);
+      for (int i = 0; i < 2; ++i)
+        if (cand[i] == want && fits(want, bwd)) return want;
+    }
+    for (int i = 0; i < 2; ++i)
+      if (fits(cand[i], bwd)) return cand[i];
+    return 0;
+  };
+  p->tile_f = pick(ftiles, false, "TT_FWD_TILE");
+  p->tile_b = pick(btiles, true, "TT_BWD_TILE");
+  if (!p->tile_f || !p->tile_b) {
     delete p;
     return fail(TT_ERR_UNSUPPORTED, "tree needs " + std::to_string(std::max(p->slots_fwd, p->slots_bwd)) +
                                         " shared-memory slots, more than one CTA can hold");
   }
-  p->ntiles = (p->N + p->tile - 1) / p->tile;
+  p->ntiles_f = (p->N + p->tile_f - 1) / p->tile_f;
+  p->ntiles_b = (p->N + p->tile_b - 1) / p->tile_b;
+  p->code_stride = (p->N + tt::kCodeAlign - 1) / tt::kCodeAlign * tt::kCodeAlign;
 
   const size_t kss = size_t(p->K) * p->S * p->S;
   const size_t I1 = size_t(std::max(p->I - 1, 1));
   rc = TT_OK;
   if (!rc) rc = dev_alloc(p, &p->d_steps, p->steps.size() * sizeof(int), "schedule");
+  if (!rc) rc = dev_alloc(p, &p->d_steps_rev, p->steps.size() * sizeof(int), "reversed schedule");
   if (!rc) rc = dev_alloc(p, &p->d_branch_pos, size_t(p->B) * sizeof(int), "branch map");
-  if (!rc) rc = dev_alloc(p, &p->d_codes, size_t(p->T) * p->N, "tip codes");
+  if (!rc) rc = dev_alloc(p, &p->d_codes, size_t(p->T) * p->code_stride, "tip codes");
   if (!rc) rc = dev_alloc(p, &p->d_table, size_t(256) * p->S * p->elem, "code table");
   if (!rc) rc = dev_alloc(p, &p->d_weights, size_t(p->N) * sizeof(double), "weights");
-  if (!rc) rc = dev_alloc(p, &p->d_pmat, size_t(batch) * p->I * 2 * kss * p->elem, "transition matrices");
+  // FP32 plans: category pairs (K padded to even), partials per tile (N padded to whole tiles)
+  const size_t kpad = f32 ? size_t(2 * tt::kpairs_for(p->K)) : size_t(p->K);
+  const size_t npad = f32 ? size_t(p->ntiles_b) * p->tile_b : size_t(p->N);
+  if (!rc) rc = dev_alloc(p, &p->d_pmat, size_t(batch) * p->I * 2 * kpad * p->S * p->S * p->elem, "transition matrices");
+  if (!rc) rc = dev_alloc(p, &p->d_partials, size_t(batch) * I1 * kpad * npad * p->S * p->elem, "partials");
+  if (!rc) rc = dev_alloc(p, &p->d_tile_lnl, size_t(batch) * p->ntiles_f * sizeof(double), "tile sums");
   if (!rc)
-    rc = dev_alloc(p, &p->d_partials, size_t(batch) * I1 * p->K * size_t(p->N) * p->S * p->elem,
-                   "partials");
-  if (!rc) rc = dev_alloc(p, &p->d_tile_lnl, size_t(batch) * p->ntiles * sizeof(double), "tile sums");
+    rc = dev_alloc(p, &p->d_gpart, size_t(batch) * p->B * p->ntiles_b * kss * p->elem, "gradient tiles");
   if (!rc)
-    rc = dev_alloc(p, &p->d_gpart, size_t(batch) * p->B * p->ntiles * kss * p->elem, "gradient tiles");
-  if (!rc)
-    rc = dev_alloc(p, &p->d_rootpart, size_t(batch) * p->ntiles * (p->S + p->K) * p->elem, "root tiles");
+    rc = dev_alloc(p, &p->d_rootpart, size_t(batch) * p->ntiles_b * (p->S + p->K) * p->elem, "root tiles");
   if (!rc) rc = dev_alloc(p, &p->d_G, size_t(batch) * p->B * kss * sizeof(double), "dlnL/dP");
   if (!rc) rc = dev_alloc(p, &p->d_rootgrad, size_t(batch) * (p->S + p->K) * sizeof(double), "root grads");
   if (!rc) rc = dev_alloc(p, &p->d_status, sizeof(int), "status");
@@ -342,10 +375,19 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
     return rc;
   }
   ce = cudaMemcpy(p->d_steps, p->steps.data(), p->steps.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (ce == cudaSuccess) {
+    std::vector<int> rev(p->steps.size());
+    for (int s2 = 0; s2 < p->I; ++s2)
+      std::memcpy(&rev[size_t(s2) * tt::kStepInts], &p->steps[size_t(p->I - 1 - s2) * tt::kStepInts],
+                  tt::kStepInts * sizeof(int));
+    ce = cudaMemcpy(p->d_steps_rev, rev.data(), rev.size() * sizeof(int), cudaMemcpyHostToDevice);
+  }
   if (ce == cudaSuccess)
     ce = cudaMemcpy(p->d_branch_pos, p->branch_pos.data(), p->branch_pos.size() * sizeof(int),
                     cudaMemcpyHostToDevice);
   if (ce == cudaSuccess) ce = cudaMemset(p->d_status, 0, sizeof(int));
+  if (ce == cudaSuccess)  // padded category pairs must read as zero matrices
+    ce = cudaMemset(p->d_pmat, 0, size_t(batch) * p->I * 2 * kpad * p->S * p->S * p->elem);
   if (ce != cudaSuccess) {
     release(p);
     delete p;
@@ -391,7 +433,9 @@ int tt_plan_set_tips(tt_plan *p, const uint8_t *codes, const double *code_table,
       std::memcpy(&table[i * 8], &code_table[i], 8);
     }
   }
-  cudaError_t e = cudaMemcpy(p->d_codes, codes, tn, cudaMemcpyHostToDevice);
+  cudaError_t e = cudaMemset(p->d_codes, 0, size_t(p->T) * p->code_stride);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2D(p->d_codes, p->code_stride, codes, p->N, p->N, p->T, cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(p->d_table, table.data(), table.size(), cudaMemcpyHostToDevice);
   if (e == cudaSuccess)
     e = cudaMemcpy(p->d_weights, weights, size_t(p->N) * sizeof(double), cudaMemcpyHostToDevice);
@@ -451,14 +495,14 @@ int tt_log_likelihood(tt_plan *p, const double *props, const double *freqs, int3
   if (p->precision == TT_PRECISION_F32) {
     auto a = make_args<float>(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, site_lnl);
     a.slots = p->slots_fwd;
-    e = tt::launch_prune_f32(a, false, p->tile, p->batch, s);
+    e = tt::launch_prune_f32(a, false, p->tile_f, p->batch, s);
   } else {
     auto a = make_args<double>(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, site_lnl);
     a.slots = p->slots_fwd;
-    e = tt::launch_prune_f64(a, false, p->tile, p->batch, s);
+    e = tt::launch_prune_f64(a, false, p->tile_f, p->batch, s);
   }
   if (e != cudaSuccess) return cuda_fail(e, "post-order launch");
-  e = tt::launch_reduce_lnl(p->d_tile_lnl, lnl, p->batch, p->ntiles, s);
+  e = tt::launch_reduce_lnl(p->d_tile_lnl, lnl, p->batch, p->ntiles_f, s);
   if (e != cudaSuccess) return cuda_fail(e, "likelihood reduction launch");
   p->launches += 2;
   p->partials_valid = keep_partials != 0;
@@ -478,20 +522,23 @@ int tt_gradient(tt_plan *p, const double *props, const double *freqs, double *gr
   if (p->precision == TT_PRECISION_F32) {
     auto a = make_args<float>(p, props, freqs, 1, true, nullptr);
     a.slots = p->slots_bwd;
-    e = tt::launch_prune_f32(a, true, p->tile, p->batch, s);
+    a.ntiles = p->ntiles_b;
+    a.nstage = p->nstage_b;
+    e = tt::launch_prune_f32(a, true, p->tile_b, p->batch, s);
     if (e == cudaSuccess)
       e = tt::launch_reduce_f32(static_cast<const float *>(p->d_gpart),
                                 static_cast<const float *>(p->d_rootpart), p->d_G, p->d_rootgrad,
-                                p->d_rootgrad + size_t(p->batch) * p->S, p->batch, p->B, p->ntiles, p->S,
+                                p->d_rootgrad + size_t(p->batch) * p->S, p->batch, p->B, p->ntiles_b, p->S,
                                 p->K, s);
   } else {
     auto a = make_args<double>(p, props, freqs, 1, true, nullptr);
     a.slots = p->slots_bwd;
-    e = tt::launch_prune_f64(a, true, p->tile, p->batch, s);
+    a.ntiles = p->ntiles_b;
+    e = tt::launch_prune_f64(a, true, p->tile_b, p->batch, s);
     if (e == cudaSuccess)
       e = tt::launch_reduce_f64(static_cast<const double *>(p->d_gpart),
                                 static_cast<const double *>(p->d_rootpart), p->d_G, p->d_rootgrad,
-                                p->d_rootgrad + size_t(p->batch) * p->S, p->batch, p->B, p->ntiles, p->S,
+                                p->d_rootgrad + size_t(p->batch) * p->S, p->batch, p->B, p->ntiles_b, p->S,
                                 p->K, s);
   }
   if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");

@@ -5,16 +5,33 @@
 #include <stddef.h>
 
 #include "tt_prune.cuh"
+#include "tt_prune_tl.cuh"
 
 namespace tt {
 
 // Set the calling thread's tt_last_error() message; returns `code`.
 int record_error(int code, const char *msg);
 
-// Pattern tile widths compiled per precision (largest first).
-constexpr int kTilesF32[2] = {128, 64};
-constexpr int kTilesF64[2] = {64, 32};
+// Pattern tile widths compiled per precision and pass (preferred first).
+// FP32 plans: both passes use one tile width (the stored partials are laid
+// out per tile): forward kTlFwdThreads threads x (kTlTile / kTlFwdThreads)
+// patterns each, adjoint one pattern per thread.
+constexpr int kTlTile = 64;
+constexpr int kTlFwdThreads = 32;
+constexpr int kTlBwdThreads = 64;
+constexpr int kFwdTilesF32[2] = {kTlTile, kTlTile};
+constexpr int kBwdTilesF32[2] = {kTlTile, kTlTile};
+constexpr int kFwdTilesF64[2] = {64, 32};
+constexpr int kBwdTilesF64[2] = {64, 32};
 constexpr int kStages = 4;
+// default staging-ring depths of the FP32 kernels (reduced to fit shared memory)
+constexpr int kTlFwdStages = 6;
+constexpr int kTlBwdStages = 3;
+
+// category pairs of the FP32 kernels (K padded to an even count)
+inline int kpairs_for(int K) { return (K + 1) / 2; }
+// Tip-code rows are padded to a multiple of this many patterns.
+constexpr int kCodeAlign = 128;
 
 inline int kmax_for(int K) { return K <= 1 ? 1 : (K <= 4 ? 4 : 8); }
 
@@ -23,7 +40,15 @@ size_t prune_smem_bytes(int S, int K, int C, int slots, int tile, bool backward)
   return stack_layout<T>(S, K, C, slots, tile, kStages, kmax_for(K), backward).total;
 }
 
-// Launch the pruning kernels (S = 4).  Return cudaSuccess or the launch error.
+// FP32 kernels (packed FP32x2, category pairs)
+inline size_t tl_smem_bytes(int K, int C, int slots, bool backward, int nstage) {
+  return size_t(tl_layout(kpairs_for(K), C, slots, kTlTile, backward ? kTlBwdThreads : kTlFwdThreads, nstage,
+                          backward)
+                    .total);
+}
+
+// Launch the pruning kernels (S = 4) with a tile width from the pass's
+// candidate list.  Return cudaSuccess or the launch error.
 cudaError_t launch_prune_f32(const PruneArgs<float> &a, bool backward, int tile, int batch,
                              cudaStream_t stream);
 cudaError_t launch_prune_f64(const PruneArgs<double> &a, bool backward, int tile, int batch,

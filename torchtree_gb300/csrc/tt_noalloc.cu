@@ -186,10 +186,11 @@ extern "C" int tt_log_likelihood_static(int32_t tip_count, const int32_t *postor
   int rc = static_schedule(T, postorder, steps, branch_pos, &slots);
   if (rc != TT_OK) return rc;
   int tile = 0;
-  for (int t : tt::kTilesF64)
+  for (int t : tt::kFwdTilesF64)
     if (!tile && tt::prune_smem_bytes<double>(S, K, kTableRows, slots, t, false) <= size_t(smem_max)) tile = t;
   if (!tile) return fail(TT_ERR_UNSUPPORTED, "tree needs more shared memory than one CTA can hold");
   const int ntiles = (N + tile - 1) / tile;
+  const int code_stride = (N + tt::kCodeAlign - 1) / tt::kCodeAlign * tt::kCodeAlign;
 
   // carve the scratch
   size_t off = 0;
@@ -205,6 +206,8 @@ extern "C" int tt_log_likelihood_static(int32_t tip_count, const int32_t *postor
   off = align256(off + size_t(batch) * I * 2 * kss * sizeof(double));
   const size_t o_tiles = off;
   off = align256(off + size_t(batch) * ntiles * sizeof(double));
+  const size_t o_codes = off;  // tip codes with rows padded for 16-byte-aligned bulk copies
+  off = align256(off + size_t(T) * code_stride);
   if (off > kScratchBytes) {
     char buf[240];
     snprintf(buf, sizeof buf,
@@ -222,6 +225,7 @@ extern "C" int tt_log_likelihood_static(int32_t tip_count, const int32_t *postor
   int *d_bpos = reinterpret_cast<int *>(scratch + o_bpos);
   double *d_pmat = reinterpret_cast<double *>(scratch + o_pmat);
   double *d_tiles = reinterpret_cast<double *>(scratch + o_tiles);
+  uint8_t *d_codes = scratch + o_codes;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
 
   // Start-of-call state: status cleared; table rows past code_count and the
@@ -235,6 +239,9 @@ extern "C" int tt_log_likelihood_static(int32_t tip_count, const int32_t *postor
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(d_steps, steps, size_t(I) * tt::kStepInts * sizeof(int), cudaMemcpyHostToDevice, s);
   if (e == cudaSuccess) e = cudaMemcpyAsync(d_bpos, branch_pos, size_t(B) * sizeof(int), cudaMemcpyHostToDevice, s);
+  if (e == cudaSuccess) e = cudaMemsetAsync(d_codes, 0, size_t(T) * code_stride, s);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2DAsync(d_codes, code_stride, codes, N, N, T, cudaMemcpyDeviceToDevice, s);
   if (e == cudaSuccess) e = tt::launch_scatter_f64(matrices, d_bpos, d_pmat, B, kss, I, batch, s);
   if (e != cudaSuccess) return fail(TT_ERR_CUDA, cudaGetErrorString(e));
 
@@ -250,7 +257,9 @@ extern "C" int tt_log_likelihood_static(int32_t tip_count, const int32_t *postor
   a.slots = slots;
   a.rescale = rescale ? 1 : 0;
   a.ntiles = ntiles;
-  a.codes = codes;
+  a.code_stride = code_stride;
+  a.nstage = tt::kStages;
+  a.codes = d_codes;
   a.table = d_table;
   a.pmat = d_pmat;
   a.props = category_weights;

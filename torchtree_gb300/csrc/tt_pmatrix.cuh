@@ -3,8 +3,9 @@
 // Forward (replaces torchtree/evolution/substitution_model/abstract.py:67-76):
 //   P[b][i][k] = U[b] diag(exp(lambda[b] * t[b][i] * r[b][k])) W[b]
 // for every sample, branch and rate category in one launch, in FP64, stored
-// at the pruning precision in step order [b][step][side][K][S][S] so the
-// pruning kernels stage one contiguous block per step.
+// at the pruning precision in step order [b][step][side][K][mstride] (each
+// S x S matrix padded to mstride elements) so the pruning kernels stage one
+// contiguous block per step.
 //
 // Backward: chains dlnL/dP through the same product to the eigen system,
 // the branch lengths and the category rates (what autograd does through
@@ -22,7 +23,7 @@ __global__ void pmatrix_from_eigen_kernel(const double *__restrict__ lam,
                                           const double *__restrict__ bl,
                                           const double *__restrict__ rates,
                                           const int *__restrict__ branch_pos, T *__restrict__ pmat,
-                                          int B, int K, int n_steps, int batch) {
+                                          int B, int K, int n_steps, int batch, int mstride) {
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long total = (long long)batch * B * K;
   if (idx >= total) return;
@@ -37,7 +38,7 @@ __global__ void pmatrix_from_eigen_kernel(const double *__restrict__ lam,
   double e[S];
 #pragma unroll
   for (int m = 0; m < S; ++m) e[m] = exp(lam[size_t(b) * S + m] * t);
-  T *dst = pmat + ((size_t(b) * n_steps * 2 + pos) * K + k) * S * S;
+  T *dst = pmat + ((size_t(b) * n_steps * 2 + pos) * K + k) * mstride;
 #pragma unroll
   for (int i = 0; i < S; ++i) {
     double ue[S];
@@ -55,11 +56,12 @@ __global__ void pmatrix_from_eigen_kernel(const double *__restrict__ lam,
   }
 }
 
-// Matrices given by the caller ([b][B][K][S][S], FP64) -> step order.
+// Matrices given by the caller ([b][B][K][S][S], FP64) -> step order, each
+// S x S matrix at a stride of `mstride` elements.
 template <typename T>
 __global__ void pmatrix_scatter_kernel(const double *__restrict__ src,
                                        const int *__restrict__ branch_pos, T *__restrict__ pmat,
-                                       int B, int KSS, int n_steps, int batch) {
+                                       int B, int KSS, int n_steps, int batch, int SS, int mstride) {
   const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const long long total = (long long)batch * B * KSS;
   if (idx >= total) return;
@@ -68,7 +70,61 @@ __global__ void pmatrix_scatter_kernel(const double *__restrict__ src,
   const int b = int(idx / ((long long)KSS * B));
   const int pos = branch_pos[br];
   if (pos < 0) return;
-  pmat[(size_t(b) * n_steps * 2 + pos) * KSS + e] = T(src[idx]);
+  pmat[(size_t(b) * n_steps * 2 + pos) * (KSS / SS) * mstride + (e / SS) * mstride + e % SS] = T(src[idx]);
+}
+
+// FP32 plans: the same matrices stored as category pairs,
+// [b][step][side][KQ][4][4] float2 with (category 2q, category 2q+1); slots of
+// padded categories are never written (the buffer is zeroed once).
+static __global__ void pmatrix_pairs_from_eigen_kernel(const double *__restrict__ lam, const double *__restrict__ U,
+                                                const double *__restrict__ W, const double *__restrict__ bl,
+                                                const double *__restrict__ rates,
+                                                const int *__restrict__ branch_pos, float *__restrict__ pmat,
+                                                int B, int K, int KQ, int n_steps, int batch) {
+  constexpr int S = 4;
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long total = (long long)batch * B * K;
+  if (idx >= total) return;
+  const int k = int(idx % K);
+  const int br = int((idx / K) % B);
+  const int b = int(idx / ((long long)K * B));
+  const int pos = branch_pos[br];
+  if (pos < 0) return;
+  const double t = bl[size_t(b) * B + br] * rates[size_t(b) * K + k];
+  const double *Ub = U + size_t(b) * S * S;
+  const double *Wb = W + size_t(b) * S * S;
+  double e[S];
+#pragma unroll
+  for (int m = 0; m < S; ++m) e[m] = exp(lam[size_t(b) * S + m] * t);
+  float *dst = pmat + ((size_t(b) * n_steps * 2 + pos) * KQ + (k >> 1)) * 32 + (k & 1);
+#pragma unroll
+  for (int i = 0; i < S; ++i) {
+    double ue[S];
+#pragma unroll
+    for (int m = 0; m < S; ++m) ue[m] = Ub[i * S + m] * e[m];
+#pragma unroll
+    for (int j = 0; j < S; ++j) {
+      double acc = 0.0;
+#pragma unroll
+      for (int m = 0; m < S; ++m) acc = fma(ue[m], Wb[m * S + j], acc);
+      dst[(i * S + j) * 2] = float(acc);
+    }
+  }
+}
+
+static __global__ void pmatrix_pairs_scatter_kernel(const double *__restrict__ src, const int *__restrict__ branch_pos,
+                                             float *__restrict__ pmat, int B, int K, int KQ, int n_steps,
+                                             int batch) {
+  const long long idx = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long total = (long long)batch * B * K * 16;
+  if (idx >= total) return;
+  const int e = int(idx % 16);
+  const int k = int((idx / 16) % K);
+  const int br = int((idx / (16 * K)) % B);
+  const int b = int(idx / ((long long)16 * K * B));
+  const int pos = branch_pos[br];
+  if (pos < 0) return;
+  pmat[((size_t(b) * n_steps * 2 + pos) * KQ + (k >> 1)) * 32 + e * 2 + (k & 1)] = float(src[idx]);
 }
 
 // Gradient of sum_b lnL[b] through P = U diag(exp(lambda t r)) W.

@@ -3,22 +3,28 @@
 // Patterns are independent up to the final weighted sum
 // (torchtree/evolution/tree_likelihood.py:186-221 rescales per pattern), so
 // one CTA owns a tile of TILE patterns of one batch sample and walks the
-// whole post-order itself.  Each thread owns one pattern and all K rate
+// whole post-order itself; each thread owns one pattern and all K rate
 // categories.  Child partials that are still needed live in a shared-memory
-// stack whose slots the host assigned (Sethi-Ullman order keeps the stack
-// depth <= log2(T)+1); the transition matrices of each step are staged into
-// shared memory by the TMA engine (cp.async.bulk) a few steps ahead.
+// stack whose slots the host assigned (Sethi-Ullman order keeps the depth
+// <= log2(T)+1).
 //
-// Forward  (replaces tree_likelihood.py:40-75 / 186-221): the only HBM
-// traffic is writing each non-root internal partial once (when the gradient
-// needs it) plus tip codes.
-// Backward (replaces autograd through the same lines): walks the schedule in
-// reverse (a pre-order), keeps the pre-order ("outside") partials in the
-// shared-memory stack, reads each stored post-order partial once, and emits
-// per-tile partial sums of dlnL/dP for every branch.
+// Everything a step reads from global memory is staged into a shared-memory
+// ring a few steps ahead by the TMA engine (cp.async.bulk, completion on one
+// mbarrier per stage): the step record, the pair of transition matrices, the
+// tip-code rows of tip children and, in the adjoint, the stored partial
+// tiles of internal children.  The warps then read shared memory only.
 //
-// Global partial layout: [batch][internal node - T][K][N][S], S innermost,
-// so a warp's S-vector loads/stores of one category are fully coalesced.
+// Forward (replaces tree_likelihood.py:40-75 / 186-221): HBM traffic is the
+// write of each non-root internal partial (only when the gradient needs it).
+// Adjoint (replaces autograd through the same lines): walks the schedule in
+// reverse (a pre-order), keeps the outside partials in the shared-memory
+// stack, reads each stored partial once, and reduces dlnL/dP of each branch
+// over the tile through a shared-memory transpose.
+//
+// Global partial layout: [batch][internal node - T][K][N][S], S innermost:
+// one category of one tile is a contiguous TILE*S run (one bulk copy).
+// Tip codes: [T][code_stride] bytes, rows padded so each tile's run of
+// codes is 16-byte aligned.
 #pragma once
 
 #include "tt_common.cuh"
@@ -35,6 +41,7 @@ constexpr int kStepInts = 12;
 template <typename T>
 struct PruneArgs {
   const int4 *steps;
+  const int4 *steps_rev;  // the same records in reverse order (adjoint issue order)
   int n_steps;    // internal nodes (T-1)
   int tip_count;  // T
   int branch_count;
@@ -44,7 +51,9 @@ struct PruneArgs {
   int slots;
   int rescale;
   int ntiles;
-  const uint8_t *codes;   // [T][N]
+  int code_stride;        // bytes per tip row of `codes` (multiple of 16, >= ntiles*TILE)
+  int nstage;             // depth of the staging ring (kernels with a runtime ring depth)
+  const uint8_t *codes;   // [T][code_stride]
   const T *table;         // [C][S]
   const T *pmat;          // [batch][n_steps][2][K][S][S]
   const double *props;    // [batch][K]
@@ -59,32 +68,59 @@ struct PruneArgs {
   unsigned long long timeout_ns;
 };
 
-struct StackLayout {
-  size_t pbuf, bars, table, stack, red, red_root, total;
+__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+
+// Layout of one ring stage: step record | matrix pair | 2 code rows | 2 child tiles
+struct StageLayout {
+  size_t rec, pm, codes, kids, bytes;
 };
 
-__host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
+template <typename T>
+__host__ __device__ inline StageLayout stage_layout(int S, int K, int tile, bool backward) {
+  StageLayout g;
+  size_t off = 0;
+  g.rec = off;
+  off = align16(off + 3 * 16);
+  g.pm = off;
+  off = align16(off + size_t(2) * K * S * S * sizeof(T));
+  g.codes = off;
+  off = align16(off + size_t(2) * tile);
+  g.kids = off;
+  if (backward) off = align16(off + size_t(2) * K * tile * S * sizeof(T));
+  g.bytes = off;
+  return g;
+}
+
+struct StackLayout {
+  size_t stages, bars, table, stack, xbuf, red, red_root, total;
+};
 
 // Shared-memory carve-up shared by the host (launch size) and the kernels.
 template <typename T>
-__host__ __device__ inline StackLayout stack_layout(int S, int K, int C, int slots, int tile,
-                                                    int nstage, int kmax, bool backward) {
+__host__ __device__ inline StackLayout stack_layout(int S, int K, int C, int slots, int tile, int nstage,
+                                                    int kmax, bool backward) {
   StackLayout L;
+  const StageLayout g = stage_layout<T>(S, K, tile, backward);
   size_t off = 0;
-  L.pbuf = off;
-  off = align16(off + size_t(nstage) * 2 * K * S * S * sizeof(T));
+  L.stages = off;
+  off = align16(off + size_t(nstage) * g.bytes);
   L.bars = off;
   off = align16(off + size_t(nstage) * 8);
   L.table = off;
   off = align16(off + size_t(C) * S * sizeof(T));
   L.stack = off;
   off = align16(off + size_t(slots) * K * tile * S * sizeof(T));
+  L.xbuf = off;
+  if (backward) off = align16(off + size_t(2) * tile * (K * S + 16 / sizeof(T)) * sizeof(T));
   L.red = off;
-  const int vp = ((kmax * S * S + 31) / 32) * 32;
-  if (backward) off = align16(off + size_t(2) * (tile / 32) * 2 * vp * sizeof(T));
+  // per-row partial sums of the transpose reduction, double-buffered
+  const int rows = 2 * K * S;
+  const int q = tile >= rows ? tile / rows : 1;
+  if (backward) off = align16(off + size_t(2) * rows * q * S * sizeof(T));
   L.red_root = off;
   if (backward) off = align16(off + size_t(tile / 32) * (S + kmax) * sizeof(T));
   L.total = off;
+  (void)kmax;
   return L;
 }
 
@@ -99,20 +135,6 @@ __device__ __forceinline__ void matvec(T (&out)[S], const T *P, const T (&v)[S])
 #pragma unroll
     for (int j = 0; j < S; ++j) acc = fma(row[j], v[j], acc);
     out[i] = acc;
-  }
-}
-
-// out[j] = sum_i P[i][j] x[i]
-template <typename T, int S>
-__device__ __forceinline__ void matvec_t(T (&out)[S], const T *P, const T (&x)[S]) {
-#pragma unroll
-  for (int j = 0; j < S; ++j) out[j] = T(0);
-#pragma unroll
-  for (int i = 0; i < S; ++i) {
-    T row[S];
-    load_vec<T, S>(row, P + i * S);
-#pragma unroll
-    for (int j = 0; j < S; ++j) out[j] = fma(row[j], x[i], out[j]);
   }
 }
 
@@ -135,23 +157,55 @@ __device__ __forceinline__ void rescale_pow2(T (&v)[KMAX][S], int K, int &E) {
   }
 }
 
-// Issue the bulk copy of step `s`'s matrix pair into stage `st`.
-template <typename T>
-__device__ __forceinline__ void issue_pmat(T *pbuf, uint64_t *bars, const T *pm, int s, int st,
-                                           size_t pstep) {
-  const uint32_t bytes = static_cast<uint32_t>(pstep * sizeof(T));
-  mbar_arrive_expect_tx(&bars[st], bytes);
-  bulk_copy_g2s(pbuf + st * pstep, pm + size_t(s) * pstep, bytes, &bars[st]);
+// Producer side of the ring (one thread): stage everything step `s` needs.
+// `rec` is the step's record (already loaded by the caller).
+template <typename T, int S, bool BACKWARD>
+__device__ __forceinline__ void issue_step(const PruneArgs<T> &a, unsigned char *stage, uint64_t *bar,
+                                           const int4 (&rec)[3], int s, int b, int tile, int TILE,
+                                           const StageLayout &g) {
+  const int K = a.K;
+  const size_t kss = size_t(K) * S * S;
+  int4 *r = reinterpret_cast<int4 *>(stage + g.rec);
+  r[0] = rec[0];
+  r[1] = rec[1];
+  r[2] = rec[2];
+  const int left = rec[0].y, right = rec[0].z;
+  const int rem = min(TILE, a.N - tile * TILE);
+  const uint32_t pbytes = uint32_t(2 * kss * sizeof(T));
+  const uint32_t kid_bytes = uint32_t(rem) * S * sizeof(T);
+  uint32_t total = pbytes;
+  total += (left < a.tip_count ? TILE : 0) + (right < a.tip_count ? TILE : 0);
+  if (BACKWARD) total += (left >= a.tip_count ? K * kid_bytes : 0) + (right >= a.tip_count ? K * kid_bytes : 0);
+  mbar_arrive_expect_tx(bar, total);
+  bulk_copy_g2s(stage + g.pm, a.pmat + (size_t(b) * a.n_steps + s) * 2 * kss, pbytes, bar);
+  const int child[2] = {left, right};
+#pragma unroll
+  for (int c = 0; c < 2; ++c) {
+    if (child[c] < a.tip_count) {
+      bulk_copy_g2s(stage + g.codes + c * TILE, a.codes + size_t(child[c]) * a.code_stride + size_t(tile) * TILE,
+                    uint32_t(TILE), bar);
+    } else if (BACKWARD) {
+      const T *src = a.partials +
+                     ((size_t(b) * (a.n_steps - 1) + (child[c] - a.tip_count)) * K) * size_t(a.N) * S +
+                     size_t(tile) * TILE * S;
+      T *dst = reinterpret_cast<T *>(stage + g.kids) + size_t(c) * K * TILE * S;
+      for (int k = 0; k < K; ++k) bulk_copy_g2s(dst + size_t(k) * TILE * S, src + size_t(k) * a.N * S, kid_bytes, bar);
+    }
+  }
 }
 
 // On a timeout: record it, then give in-flight copies a bounded chance to
 // land before the CTA exits.
 template <int NSTAGE>
-__device__ __forceinline__ void drain_after_timeout(uint64_t *bars, int first, int last,
-                                                    int *status) {
+__device__ __forceinline__ void drain_after_timeout(uint64_t *bars, int first, int last, int *status) {
   atomicExch(status, kDeviceTimeout);
-  for (int j = first; j <= last; ++j)
-    mbar_wait_bounded(&bars[j % NSTAGE], (j / NSTAGE) & 1, 100000000ull);
+  for (int j = first; j <= last; ++j) mbar_wait_bounded(&bars[j % NSTAGE], (j / NSTAGE) & 1, 100000000ull);
+}
+
+__device__ __forceinline__ void load_rec(int4 (&r)[3], const int4 *steps, int s) {
+  r[0] = __ldg(steps + 3 * s);
+  r[1] = __ldg(steps + 3 * s + 1);
+  r[2] = __ldg(steps + 3 * s + 2);
 }
 
 // ------------------------------------------------------------------ forward
@@ -165,16 +219,15 @@ __global__ void __launch_bounds__(TILE) prune_forward_kernel(const PruneArgs<T> 
   const int n = tile * TILE + tid;
   const bool act = n < a.N;
   const int K = a.K;
-  const int KSS = K * S * S;
+  const int nst = a.n_steps;
   const StackLayout L = stack_layout<T>(S, K, a.C, a.slots, TILE, NSTAGE, KMAX, false);
-  T *pbuf = reinterpret_cast<T *>(smem + L.pbuf);
+  const StageLayout G = stage_layout<T>(S, K, TILE, false);
+  unsigned char *stages = smem + L.stages;
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.bars);
   T *tab = reinterpret_cast<T *>(smem + L.table);
   T *stk = reinterpret_cast<T *>(smem + L.stack);
-  const size_t pstep = 2 * size_t(KSS);
-  const T *pm = a.pmat + size_t(b) * a.n_steps * pstep;
-  const int nst = a.n_steps;
 
+  int4 nxt[3];  // producer's prefetched record (thread 0)
   if (tid == 0) {
 #pragma unroll
     for (int st = 0; st < NSTAGE; ++st) mbar_init(&bars[st], 1);
@@ -187,8 +240,14 @@ __global__ void __launch_bounds__(TILE) prune_forward_kernel(const PruneArgs<T> 
 #pragma unroll
   for (int i = 0; i < S; ++i) freqs[i] = a.freqs[b * S + i];
   __syncthreads();
-  if (tid == 0)
-    for (int s = 0; s < NSTAGE - 1 && s < nst; ++s) issue_pmat(pbuf, bars, pm, s, s, pstep);
+  if (tid == 0) {
+    load_rec(nxt, a.steps, 0);
+    for (int s = 0; s < NSTAGE - 1 && s < nst; ++s) {
+      int4 cur[3] = {nxt[0], nxt[1], nxt[2]};
+      if (s + 1 < nst) load_rec(nxt, a.steps, s + 1);
+      issue_step<T, S, false>(a, stages + s * G.bytes, &bars[s], cur, s, b, tile, TILE, G);
+    }
+  }
   bool timed_out = !mbar_wait_bounded(&bars[0], 0, a.timeout_ns);
   if (__syncthreads_or(timed_out)) {
     if (tid == 0) drain_after_timeout<NSTAGE>(bars, 0, min(NSTAGE - 2, nst - 1), a.status);
@@ -200,56 +259,45 @@ __global__ void __launch_bounds__(TILE) prune_forward_kernel(const PruneArgs<T> 
   for (int s = 0; s < nst; ++s) {
     if (tid == 0 && s + NSTAGE - 1 < nst) {
       const int sp = s + NSTAGE - 1;
-      issue_pmat(pbuf, bars, pm, sp, sp % NSTAGE, pstep);
+      int4 cur[3] = {nxt[0], nxt[1], nxt[2]};
+      if (sp + 1 < nst) load_rec(nxt, a.steps, sp + 1);
+      issue_step<T, S, false>(a, stages + (sp % NSTAGE) * G.bytes, &bars[sp % NSTAGE], cur, sp, b, tile, TILE, G);
     }
-    const T *Pl = pbuf + (s % NSTAGE) * pstep;
-    const T *Pr = Pl + KSS;
-    const int4 r0 = __ldg(a.steps + 3 * s);
-    const int4 r1 = __ldg(a.steps + 3 * s + 1);
+    const unsigned char *stg = stages + (s % NSTAGE) * G.bytes;
+    const int4 *rec = reinterpret_cast<const int4 *>(stg + G.rec);
+    const int4 r0 = rec[0], r1 = rec[1];
     const int node = r0.x, left = r0.y, right = r0.z;
+    const bool ltip = left < a.tip_count, rtip = right < a.tip_count;
+    const T *Pl = reinterpret_cast<const T *>(stg + G.pm);
+    const T *Pr = Pl + K * S * S;
+    T tl[S], tr[S];
+    if (ltip) load_vec<T, S>(tl, tab + int(stg[G.codes + tid]) * S);
+    if (rtip) load_vec<T, S>(tr, tab + int(stg[G.codes + TILE + tid]) * S);
     T prod[KMAX][S];
-    // left child term
-    if (left < a.tip_count) {
-      const int code = act ? a.codes[size_t(left) * a.N + n] : 0;
-      T v[S];
-      load_vec<T, S>(v, tab + code * S);
 #pragma unroll
-      for (int k = 0; k < KMAX; ++k)
-        if (k < K) matvec<T, S>(prod[k], Pl + k * S * S, v);
-    } else {
-      const int slot = r0.w;
+    for (int k = 0; k < KMAX; ++k) {
+      if (k < K) {
+        T vl[S], vr[S], al[S], ar[S];
+        if (ltip) {
 #pragma unroll
-      for (int k = 0; k < KMAX; ++k)
-        if (k < K) {
-          T v[S];
-          load_vec<T, S>(v, stk + (size_t(slot * K + k) * TILE + tid) * S);
-          matvec<T, S>(prod[k], Pl + k * S * S, v);
+          for (int i = 0; i < S; ++i) vl[i] = tl[i];
+        } else {
+          load_vec<T, S>(vl, stk + (size_t(r0.w * K + k) * TILE + tid) * S);
         }
-    }
-    // right child term, multiplied in
-    if (right < a.tip_count) {
-      const int code = act ? a.codes[size_t(right) * a.N + n] : 0;
-      T v[S];
-      load_vec<T, S>(v, tab + code * S);
+        if (rtip) {
 #pragma unroll
-      for (int k = 0; k < KMAX; ++k)
-        if (k < K) {
-          T t[S];
-          matvec<T, S>(t, Pr + k * S * S, v);
-#pragma unroll
-          for (int i = 0; i < S; ++i) prod[k][i] *= t[i];
+          for (int i = 0; i < S; ++i) vr[i] = tr[i];
+        } else {
+          load_vec<T, S>(vr, stk + (size_t(r1.x * K + k) * TILE + tid) * S);
         }
-    } else {
-      const int slot = r1.x;
+        matvec<T, S>(al, Pl + k * S * S, vl);
+        matvec<T, S>(ar, Pr + k * S * S, vr);
 #pragma unroll
-      for (int k = 0; k < KMAX; ++k)
-        if (k < K) {
-          T v[S], t[S];
-          load_vec<T, S>(v, stk + (size_t(slot * K + k) * TILE + tid) * S);
-          matvec<T, S>(t, Pr + k * S * S, v);
+        for (int i = 0; i < S; ++i) prod[k][i] = al[i] * ar[i];
+      } else {
 #pragma unroll
-          for (int i = 0; i < S; ++i) prod[k][i] *= t[i];
-        }
+        for (int i = 0; i < S; ++i) prod[k][i] = T(0);
+      }
     }
     if (a.rescale) rescale_pow2<T, S, KMAX>(prod, K, E);
     const int out_slot = r1.y;
@@ -275,8 +323,8 @@ __global__ void __launch_bounds__(TILE) prune_forward_kernel(const PruneArgs<T> 
         }
       ll = log(site) + double(E) * 0.69314718055994530942;
     }
-    if (s + 1 < nst) timed_out = !mbar_wait_bounded(&bars[(s + 1) % NSTAGE], ((s + 1) / NSTAGE) & 1,
-                                                    a.timeout_ns);
+    if (s + 1 < nst)
+      timed_out = !mbar_wait_bounded(&bars[(s + 1) % NSTAGE], ((s + 1) / NSTAGE) & 1, a.timeout_ns);
     if (__syncthreads_or(timed_out)) {
       if (tid == 0) drain_after_timeout<NSTAGE>(bars, s + 1, min(s + NSTAGE - 1, nst - 1), a.status);
       return;
@@ -297,78 +345,38 @@ __global__ void __launch_bounds__(TILE) prune_forward_kernel(const PruneArgs<T> 
 }
 
 // ----------------------------------------------------------------- backward
-// Child values for the adjoint: the tip's table vector (same for every
-// category) or the stored post-order partial of an internal child.
-template <typename T, int S, int KMAX>
-__device__ __forceinline__ void child_values(T (&v)[KMAX][S], int child, const PruneArgs<T> &a,
-                                             const T *tab, int b, int n, bool act) {
-  const int K = a.K;
-  if (child < a.tip_count) {
-    const int code = act ? a.codes[size_t(child) * a.N + n] : 0;
-    T t[S];
-    load_vec<T, S>(t, tab + code * S);
-#pragma unroll
-    for (int k = 0; k < KMAX; ++k)
-#pragma unroll
-      for (int i = 0; i < S; ++i) v[k][i] = t[i];
-  } else {
-    const T *src =
-        a.partials + (size_t(b) * (a.n_steps - 1) + (child - a.tip_count)) * K * size_t(a.N) * S;
-    const int nn = act ? n : 0;
-#pragma unroll
-    for (int k = 0; k < KMAX; ++k)
-      if (k < K) load_vec_stream<T, S>(v[k], src + (size_t(k) * a.N + nn) * S);
-  }
-}
-
-// Reduce the per-pattern outer products coef * x[k][i] * v[k][j] over the
-// warp, chunk by chunk of 32 values; lane l stores element 32c+l of the
-// padded vector.
-template <typename T, int S, int KMAX, int VP>
-__device__ __forceinline__ void reduce_outer(T *dst, const T (&x)[KMAX][S], const T (&v)[KMAX][S],
-                                             T coef, int K, int lane) {
-#pragma unroll
-  for (int c = 0; c < VP / 32; ++c) {
-    T g[32];
-#pragma unroll
-    for (int jj = 0; jj < 32; ++jj) {
-      const int e = c * 32 + jj;
-      const int k = e / (S * S);
-      const int i = (e / S) % S;
-      const int j = e % S;
-      g[jj] = (k < KMAX && k < K) ? coef * x[k < KMAX ? k : 0][i] * v[k < KMAX ? k : 0][j] : T(0);
-    }
-    warp_reduce_halving<32, T>(g, lane);
-    dst[c * 32 + lane] = g[0];
-  }
-}
-
 template <typename T, int S, int KMAX, int TILE, int NSTAGE>
 __global__ void __launch_bounds__(TILE) prune_backward_kernel(const PruneArgs<T> a) {
   extern __shared__ __align__(128) unsigned char smem[];
   constexpr int NW = TILE / 32;
-  constexpr int VP = ((KMAX * S * S + 31) / 32) * 32;
-  constexpr int RV = 2 * VP;
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int b = blockIdx.y;
   const int tile = blockIdx.x;
   const int n = tile * TILE + tid;
   const bool act = n < a.N;
+  const int rem = min(TILE, a.N - tile * TILE);
   const int K = a.K;
+  const int KS = K * S;
   const int KSS = K * S * S;
   const int RK = S + K;
+  const int XS = KS + 16 / int(sizeof(T));  // padded row: conflict-free vector stores
+  const int nst = a.n_steps;
   const StackLayout L = stack_layout<T>(S, K, a.C, a.slots, TILE, NSTAGE, KMAX, true);
-  T *pbuf = reinterpret_cast<T *>(smem + L.pbuf);
+  const StageLayout G = stage_layout<T>(S, K, TILE, true);
+  unsigned char *stages = smem + L.stages;
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.bars);
   T *tab = reinterpret_cast<T *>(smem + L.table);
   T *stk = reinterpret_cast<T *>(smem + L.stack);
-  T *red = reinterpret_cast<T *>(smem + L.red);
+  T *xbuf = reinterpret_cast<T *>(smem + L.xbuf);  // [2][TILE][XS]  coef * outside partial
+  T *red = reinterpret_cast<T *>(smem + L.red);    // [2][rows][Q][S]
   T *redr = reinterpret_cast<T *>(smem + L.red_root);
-  const size_t pstep = 2 * size_t(KSS);
-  const T *pm = a.pmat + size_t(b) * a.n_steps * pstep;
-  const int nst = a.n_steps;
+  // transpose-reduction work split: rows (child, k, i), Q pattern chunks
+  const int rows = 2 * KS;
+  const int Q = TILE >= rows ? TILE / rows : 1;
+  const int chunk = (TILE + Q - 1) / Q;
   const T w = act ? T(a.weights[n]) : T(0);
 
+  int4 nxt[3];
   if (tid == 0) {
 #pragma unroll
     for (int st = 0; st < NSTAGE; ++st) mbar_init(&bars[st], 1);
@@ -382,8 +390,14 @@ __global__ void __launch_bounds__(TILE) prune_backward_kernel(const PruneArgs<T>
   for (int i = 0; i < S; ++i) freqs[i] = a.freqs[b * S + i];
   __syncthreads();
   // iteration j handles step nst-1-j and uses stage j % NSTAGE
-  if (tid == 0)
-    for (int j = 0; j < NSTAGE - 1 && j < nst; ++j) issue_pmat(pbuf, bars, pm, nst - 1 - j, j, pstep);
+  if (tid == 0) {
+    load_rec(nxt, a.steps, nst - 1);
+    for (int j = 0; j < NSTAGE - 1 && j < nst; ++j) {
+      int4 cur[3] = {nxt[0], nxt[1], nxt[2]};
+      if (j + 1 < nst) load_rec(nxt, a.steps, nst - 2 - j);
+      issue_step<T, S, true>(a, stages + j * G.bytes, &bars[j], cur, nst - 1 - j, b, tile, TILE, G);
+    }
+  }
   bool timed_out = !mbar_wait_bounded(&bars[0], 0, a.timeout_ns);
   if (__syncthreads_or(timed_out)) {
     if (tid == 0) drain_after_timeout<NSTAGE>(bars, 0, min(NSTAGE - 2, nst - 1), a.status);
@@ -391,147 +405,215 @@ __global__ void __launch_bounds__(TILE) prune_backward_kernel(const PruneArgs<T>
   }
 
   int prev_left = -1, prev_right = -1;
-  bool prev_root = false;
   for (int j = 0; j <= nst; ++j) {
-    // finish the block reduction of iteration j-1 (its smem writes are
-    // visible after the barrier that closed it)
+    // finish the transpose reduction of iteration j-1 (published by the barrier that closed it)
     if (j > 0) {
-      const T *rb = red + ((j - 1) & 1) * NW * RV;
+      const T *rb = red + size_t((j - 1) & 1) * rows * Q * S;
       for (int e = tid; e < 2 * KSS; e += TILE) {
         const int side = e >= KSS;
-        const int ei = side ? e - KSS : e;
+        const int ei = side ? e - KSS : e;  // (k, i, jj) of this child
+        const int row = side * KS + ei / S;
+        const int jj = ei % S;
         T acc = T(0);
-#pragma unroll
-        for (int ww = 0; ww < NW; ++ww) acc += rb[ww * RV + side * VP + ei];
+        for (int q = 0; q < Q; ++q) acc += rb[(row * Q + q) * S + jj];
         const int branch = side ? prev_right : prev_left;
         a.gpart[((size_t(b) * a.branch_count + branch) * a.ntiles + tile) * KSS + ei] = acc;
       }
-      if (prev_root)
-        for (int e = tid; e < RK; e += TILE) {
-          T acc = T(0);
-#pragma unroll
-          for (int ww = 0; ww < NW; ++ww) acc += redr[ww * (S + KMAX) + e];
-          a.rootpart[(size_t(b) * a.ntiles + tile) * RK + e] = acc;
-        }
     }
     if (j == nst) break;
-    const int s = nst - 1 - j;
     if (tid == 0 && j + NSTAGE - 1 < nst) {
       const int jp = j + NSTAGE - 1;
-      issue_pmat(pbuf, bars, pm, nst - 1 - jp, jp % NSTAGE, pstep);
+      int4 cur[3] = {nxt[0], nxt[1], nxt[2]};
+      if (jp + 1 < nst) load_rec(nxt, a.steps, nst - 2 - jp);
+      issue_step<T, S, true>(a, stages + (jp % NSTAGE) * G.bytes, &bars[jp % NSTAGE], cur, nst - 1 - jp, b,
+                             tile, TILE, G);
     }
-    const T *Pl = pbuf + (j % NSTAGE) * pstep;
-    const T *Pr = Pl + KSS;
-    const int4 r0 = __ldg(a.steps + 3 * s);
-    const int4 r1 = __ldg(a.steps + 3 * s + 1);
-    const int4 r2 = __ldg(a.steps + 3 * s + 2);
+    const unsigned char *stg = stages + (j % NSTAGE) * G.bytes;
+    const int4 *rec = reinterpret_cast<const int4 *>(stg + G.rec);
+    const int4 r0 = rec[0], r1 = rec[1], r2 = rec[2];
     const int left = r0.y, right = r0.z;
     const int slot_in = r1.z, slot_l = r1.w, slot_r = r2.x;
     const bool is_root = slot_in < 0;
+    const bool ltip = left < a.tip_count, rtip = right < a.tip_count;
+    const T *Pl = reinterpret_cast<const T *>(stg + G.pm);
+    const T *Pr = Pl + KSS;
+    const T *kidl = reinterpret_cast<const T *>(stg + G.kids);
+    const T *kidr = kidl + size_t(K) * TILE * S;
+    T tl[S], tr[S];
+    if (ltip) load_vec<T, S>(tl, tab + int(stg[G.codes + tid]) * S);
+    if (rtip) load_vec<T, S>(tr, tab + int(stg[G.codes + TILE + tid]) * S);
 
-    T vl[KMAX][S], vr[KMAX][S];
-    child_values<T, S, KMAX>(vl, left, a, tab, b, n, act);
-    child_values<T, S, KMAX>(vr, right, a, tab, b, n, act);
+    // ---- phase A: per pattern, all categories
     T xl[KMAX][S], xr[KMAX][S];  // outside partials at the tops of the two branches
-    T rg_pi[S], rg_c[KMAX];      // root only: sums for the frequency / weight gradients
+    T ol[KMAX][S], orr[KMAX][S];  // outside partials at the bottoms of the children
+    T rg_pi[S], rg_c[KMAX];
 #pragma unroll
     for (int i = 0; i < S; ++i) rg_pi[i] = T(0);
-#pragma unroll
-    for (int k = 0; k < KMAX; ++k) rg_c[k] = T(0);
     T den = T(0);
 #pragma unroll
     for (int k = 0; k < KMAX; ++k) {
+      rg_c[k] = T(0);
       if (k < K) {
-        T pre[S];
+        T pre[S], vl[S], vr[S], al[S], ar[S];
         if (is_root) {
 #pragma unroll
           for (int i = 0; i < S; ++i) pre[i] = T(props[k] * freqs[i]);
         } else {
           load_vec<T, S>(pre, stk + (size_t(slot_in * K + k) * TILE + tid) * S);
         }
-        T al[S], ar[S];
-        matvec<T, S>(al, Pl + k * S * S, vl[k]);
-        matvec<T, S>(ar, Pr + k * S * S, vr[k]);
+        if (ltip) {
+#pragma unroll
+          for (int i = 0; i < S; ++i) vl[i] = tl[i];
+        } else {
+          load_vec<T, S>(vl, kidl + (size_t(k) * TILE + tid) * S);
+        }
+        if (rtip) {
+#pragma unroll
+          for (int i = 0; i < S; ++i) vr[i] = tr[i];
+        } else {
+          load_vec<T, S>(vr, kidr + (size_t(k) * TILE + tid) * S);
+        }
+        T pl[S][S], pr[S][S];  // this category's two matrices, read once
+#pragma unroll
+        for (int i = 0; i < S; ++i) {
+          load_vec<T, S>(pl[i], Pl + (k * S + i) * S);
+          load_vec<T, S>(pr[i], Pr + (k * S + i) * S);
+        }
+#pragma unroll
+        for (int i = 0; i < S; ++i) {
+          T sa = T(0), sb = T(0);
+#pragma unroll
+          for (int jj = 0; jj < S; ++jj) {
+            sa = fma(pl[i][jj], vl[jj], sa);
+            sb = fma(pr[i][jj], vr[jj], sb);
+          }
+          al[i] = sa;
+          ar[i] = sb;
+        }
 #pragma unroll
         for (int i = 0; i < S; ++i) {
           xl[k][i] = pre[i] * ar[i];
           xr[k][i] = pre[i] * al[i];
           den = fma(xl[k][i], al[i], den);
-        }
-        if (is_root) {
-#pragma unroll
-          for (int i = 0; i < S; ++i) {
+          if (is_root) {
             const T r = al[i] * ar[i];
             rg_pi[i] = fma(T(props[k]), r, rg_pi[i]);
             rg_c[k] = fma(T(freqs[i]), r, rg_c[k]);
           }
         }
+        // outside partials of the children (scale-free: no coefficient)
+#pragma unroll
+        for (int jj = 0; jj < S; ++jj) {
+          T sa = T(0), sb = T(0);
+#pragma unroll
+          for (int i = 0; i < S; ++i) {
+            sa = fma(pl[i][jj], xl[k][i], sa);
+            sb = fma(pr[i][jj], xr[k][i], sb);
+          }
+          ol[k][jj] = sa;
+          orr[k][jj] = sb;
+        }
       } else {
 #pragma unroll
-        for (int i = 0; i < S; ++i) xl[k][i] = xr[k][i] = T(0);
+        for (int i = 0; i < S; ++i) xl[k][i] = xr[k][i] = ol[k][i] = orr[k][i] = T(0);
       }
     }
-    // dlnL_n/dP = w_n * x (outer) v / L_n; the per-pattern scale of every
-    // factor cancels against den, so no scaler bookkeeping is needed.
+    // dlnL_n/dP = w_n * x (outer) v / L_n; every factor's per-pattern scale
+    // cancels against den, so no scaler bookkeeping is needed.
     const T coef = (act && den > T(0)) ? w / den : T(0);
-    T *rw = red + (j & 1) * NW * RV + warp * RV;
-    reduce_outer<T, S, KMAX, VP>(rw, xl, vl, coef, K, lane);
-    reduce_outer<T, S, KMAX, VP>(rw + VP, xr, vr, coef, K, lane);
-    if (is_root) {
-      // dlnL/dpi_i = sum_k c_k R[k][i] / L and dlnL/dc_k = sum_i pi_i R[k][i] / L
-      // with R = al * ar the root partial (the root's outside vector is c_k pi_i)
+    {
+      T *xl_dst = xbuf + size_t(tid) * XS;
+      T *xr_dst = xbuf + size_t(TILE + tid) * XS;
 #pragma unroll
-      for (int i = 0; i < S; ++i) {
-        const T acc = warp_sum(coef * rg_pi[i]);
+      for (int k = 0; k < KMAX; ++k)
+        if (k < K) {
+          T u[S], v[S];
+#pragma unroll
+          for (int i = 0; i < S; ++i) {
+            u[i] = coef * xl[k][i];
+            v[i] = coef * xr[k][i];
+          }
+          store_vec<T, S>(xl_dst + k * S, u);
+          store_vec<T, S>(xr_dst + k * S, v);
+        }
+    }
+    if (is_root) {
+#pragma unroll
+      for (int i = 0; i < S; ++i) {  // lanes past the last pattern hold stale data: mask them
+        const T acc = warp_sum(act ? coef * rg_pi[i] : T(0));
         if (lane == 0) redr[warp * (S + KMAX) + i] = acc;
       }
 #pragma unroll
       for (int k = 0; k < KMAX; ++k)
         if (k < K) {
-          const T acc = warp_sum(coef * rg_c[k]);
+          const T acc = warp_sum(act ? coef * rg_c[k] : T(0));
           if (lane == 0) redr[warp * (S + KMAX) + S + k] = acc;
         }
     }
-    // outside partials at the bottoms of internal children -> stack
-    if (left >= a.tip_count) {
-      T o[KMAX][S];
-#pragma unroll
-      for (int k = 0; k < KMAX; ++k)
-        if (k < K) matvec_t<T, S>(o[k], Pl + k * S * S, xl[k]);
+    if (!ltip) {
       int E = 0;
-      rescale_pow2<T, S, KMAX>(o, K, E);
+      rescale_pow2<T, S, KMAX>(ol, K, E);
 #pragma unroll
       for (int k = 0; k < KMAX; ++k)
-        if (k < K) store_vec<T, S>(stk + (size_t(slot_l * K + k) * TILE + tid) * S, o[k]);
+        if (k < K) store_vec<T, S>(stk + (size_t(slot_l * K + k) * TILE + tid) * S, ol[k]);
     }
-    if (right >= a.tip_count) {
-      T o[KMAX][S];
-#pragma unroll
-      for (int k = 0; k < KMAX; ++k)
-        if (k < K) matvec_t<T, S>(o[k], Pr + k * S * S, xr[k]);
+    if (!rtip) {
       int E = 0;
-      rescale_pow2<T, S, KMAX>(o, K, E);
+      rescale_pow2<T, S, KMAX>(orr, K, E);
 #pragma unroll
       for (int k = 0; k < KMAX; ++k)
-        if (k < K) store_vec<T, S>(stk + (size_t(slot_r * K + k) * TILE + tid) * S, o[k]);
+        if (k < K) store_vec<T, S>(stk + (size_t(slot_r * K + k) * TILE + tid) * S, orr[k]);
+    }
+    __syncthreads();  // xbuf complete
+
+    // ---- phase C: G[c][k][i][:] = sum_n xbuf[c][n][k,i] * v_c[k][n][:]
+    {
+      T *rw = red + size_t(j & 1) * rows * Q * S;
+      for (int item = tid; item < rows * Q; item += TILE) {
+        const int row = item / Q, q = item % Q;
+        const int c = row >= KS;
+        const int ki = c ? row - KS : row;
+        const int k = ki / S;
+        const bool tipc = c ? rtip : ltip;
+        const T *xs = xbuf + size_t(c) * TILE * XS + ki;
+        const T *vs = (c ? kidr : kidl) + size_t(k) * TILE * S;
+        const unsigned char *cs = stg + G.codes + c * TILE;
+        T acc[S];
+#pragma unroll
+        for (int jj = 0; jj < S; ++jj) acc[jj] = T(0);
+        const int n0 = q * chunk, n1 = min(n0 + chunk, rem);
+        for (int m = n0; m < n1; ++m) {
+          const T x = xs[size_t(m) * XS];
+          T v[S];
+          load_vec<T, S>(v, tipc ? tab + int(cs[m]) * S : vs + size_t(m) * S);
+#pragma unroll
+          for (int jj = 0; jj < S; ++jj) acc[jj] = fma(x, v[jj], acc[jj]);
+        }
+        store_vec<T, S>(rw + (size_t(row) * Q + q) * S, acc);
+      }
     }
     prev_left = left;
     prev_right = right;
-    prev_root = is_root;
     if (j + 1 < nst)
       timed_out = !mbar_wait_bounded(&bars[(j + 1) % NSTAGE], ((j + 1) / NSTAGE) & 1, a.timeout_ns);
     if (__syncthreads_or(timed_out)) {
       if (tid == 0) drain_after_timeout<NSTAGE>(bars, j + 1, min(j + NSTAGE - 1, nst - 1), a.status);
       return;
     }
+    if (is_root)
+      for (int e = tid; e < RK; e += TILE) {
+        T acc = T(0);
+#pragma unroll
+        for (int ww = 0; ww < NW; ++ww) acc += redr[ww * (S + KMAX) + e];
+        a.rootpart[(size_t(b) * a.ntiles + tile) * RK + e] = acc;
+      }
   }
 }
 
 // ------------------------------------------------------------- reductions
 // dlnL/dP[b][branch] = sum over pattern tiles (fixed order, FP64).
 template <typename T>
-__global__ void reduce_branch_grads_kernel(const T *gpart, double *G, int branch_count, int ntiles,
-                                           int kss) {
+__global__ void reduce_branch_grads_kernel(const T *gpart, double *G, int branch_count, int ntiles, int kss) {
   const int branch = blockIdx.x, b = blockIdx.y;
   const T *src = gpart + (size_t(b) * branch_count + branch) * ntiles * size_t(kss);
   for (int e = threadIdx.x; e < kss; e += blockDim.x) {
@@ -549,8 +631,8 @@ __global__ void reduce_branch_grads_kernel(const T *gpart, double *G, int branch
 }
 
 template <typename T>
-__global__ void reduce_root_grads_kernel(const T *rootpart, double *dfreq, double *dprop, int ntiles,
-                                         int S, int K) {
+__global__ void reduce_root_grads_kernel(const T *rootpart, double *dfreq, double *dprop, int ntiles, int S,
+                                         int K) {
   const int b = blockIdx.x;
   const int RK = S + K;
   for (int e = threadIdx.x; e < RK; e += blockDim.x) {

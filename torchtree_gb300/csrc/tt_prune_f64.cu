@@ -8,11 +8,11 @@ namespace tt {
 
 namespace {
 
-template <int KMAX, int TILE>
-cudaError_t launch_one(const PruneArgs<double> &a, bool backward, int batch, cudaStream_t stream) {
-  const size_t smem = prune_smem_bytes<double>(4, a.K, a.C, a.slots, TILE, backward);
+template <int KMAX, int TILE, bool BACKWARD>
+cudaError_t launch_one(const PruneArgs<double> &a, int batch, cudaStream_t stream) {
+  const size_t smem = prune_smem_bytes<double>(4, a.K, a.C, a.slots, TILE, BACKWARD);
   const dim3 grid(a.ntiles, batch);
-  if (backward) {
+  if (BACKWARD) {
     auto kern = prune_backward_kernel<double, 4, KMAX, TILE, kStages>;
     cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
     if (e != cudaSuccess) return e;
@@ -26,12 +26,12 @@ cudaError_t launch_one(const PruneArgs<double> &a, bool backward, int batch, cud
   return cudaGetLastError();
 }
 
-template <int TILE>
-cudaError_t by_k(const PruneArgs<double> &a, bool backward, int batch, cudaStream_t stream) {
+template <int TILE, bool BACKWARD>
+cudaError_t by_k(const PruneArgs<double> &a, int batch, cudaStream_t stream) {
   switch (kmax_for(a.K)) {
-    case 1: return launch_one<1, TILE>(a, backward, batch, stream);
-    case 4: return launch_one<4, TILE>(a, backward, batch, stream);
-    default: return launch_one<8, TILE>(a, backward, batch, stream);
+    case 1: return launch_one<1, TILE, BACKWARD>(a, batch, stream);
+    case 4: return launch_one<4, TILE, BACKWARD>(a, batch, stream);
+    default: return launch_one<8, TILE, BACKWARD>(a, batch, stream);
   }
 }
 
@@ -54,8 +54,14 @@ __global__ void reduce_lnl_kernel(const double *tile_lnl, double *lnl, int ntile
 
 cudaError_t launch_prune_f64(const PruneArgs<double> &a, bool backward, int tile, int batch,
                              cudaStream_t stream) {
-  if (tile == kTilesF64[0]) return by_k<kTilesF64[0]>(a, backward, batch, stream);
-  return by_k<kTilesF64[1]>(a, backward, batch, stream);
+  if (backward) {
+    if (tile == kBwdTilesF64[0]) return by_k<kBwdTilesF64[0], true>(a, batch, stream);
+    if (tile == kBwdTilesF64[1]) return by_k<kBwdTilesF64[1], true>(a, batch, stream);
+  } else {
+    if (tile == kFwdTilesF64[0]) return by_k<kFwdTilesF64[0], false>(a, batch, stream);
+    if (tile == kFwdTilesF64[1]) return by_k<kFwdTilesF64[1], false>(a, batch, stream);
+  }
+  return cudaErrorInvalidValue;
 }
 
 cudaError_t launch_reduce_f64(const double *gpart, const double *rootpart, double *G,
@@ -82,7 +88,7 @@ cudaError_t launch_pmatrix_f64(const double *lam, const double *U, const double 
   const int threads = 128;
   const unsigned blocks = unsigned((total + threads - 1) / threads);
   pmatrix_from_eigen_kernel<double, 4><<<blocks, threads, 0, stream>>>(
-      lam, U, W, bl, rates, branch_pos, pmat, B, K, n_steps, batch);
+      lam, U, W, bl, rates, branch_pos, pmat, B, K, n_steps, batch, 16);
   return cudaGetLastError();
 }
 
@@ -91,7 +97,7 @@ cudaError_t launch_scatter_f64(const double *src, const int *branch_pos, double 
   const long long total = (long long)batch * B * KSS;
   const unsigned blocks = unsigned((total + 255) / 256);
   pmatrix_scatter_kernel<double><<<blocks, 256, 0, stream>>>(src, branch_pos, pmat, B, KSS, n_steps,
-                                                             batch);
+                                                             batch, 16, 16);
   return cudaGetLastError();
 }
 
