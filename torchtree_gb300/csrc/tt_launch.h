@@ -17,7 +17,7 @@ int record_error(int code, const char *msg);
 // out per tile): forward kTlFwdThreads threads x (kTlTile / kTlFwdThreads)
 // patterns each, adjoint one pattern per thread.
 constexpr int kTlTile = 64;
-constexpr int kTlFwdThreads = 32;
+constexpr int kTlFwdThreads = 64;
 constexpr int kTlBwdThreads = 64;
 constexpr int kFwdTilesF32[2] = {kTlTile, kTlTile};
 constexpr int kBwdTilesF32[2] = {kTlTile, kTlTile};

@@ -58,11 +58,6 @@ struct TlLayout {
 
 constexpr int kTlRecChunk = 32;
 
-// rows of the adjoint's transpose reduction: (child, i, j); Q pattern subsets
-__host__ __device__ inline int tl_q(int NT, int P) {
-  const int q = NT / 32;
-  return q < 1 ? 1 : (q > P ? P : q);
-}
 
 __host__ __device__ inline TlLayout tl_layout(int KQ, int C, int slots, int P, int NT, int nstage, bool backward) {
   TlLayout L;
@@ -82,7 +77,7 @@ __host__ __device__ inline TlLayout tl_layout(int KQ, int C, int slots, int P, i
   L.xbuf = off;
   if (backward) off = int(align16(off + 2 * P * vbytes));
   L.red = off;
-  if (backward) off = int(align16(off + 2 * 32 * tl_q(NT, P) * 2 * KQ * 4));
+  if (backward) off = int(align16(off + 16 * (NT + 1) * 8));  // 4x4 float2 block per thread, [16][NT+1]
   L.red_root = off;
   if (backward) off = int(align16(off + (NT / 32) * 12 * 4));
   L.total = off;
@@ -443,10 +438,12 @@ __global__ void __launch_bounds__(NT) tl_backward_kernel(const PruneArgs<float> 
   float2 *tab2 = reinterpret_cast<float2 *>(smem + L.table);
   float4 *stk = reinterpret_cast<float4 *>(smem + L.stack);
   float4 *xbuf = reinterpret_cast<float4 *>(smem + L.xbuf);  // [2][NC][P] float4: coef * outside partial
-  float *red = reinterpret_cast<float *>(smem + L.red);      // [2][32 rows][Q][2KQ]
+  float2 *red = reinterpret_cast<float2 *>(smem + L.red);    // [16][NT+1] float2: element ij of each thread's block
   float *redr = reinterpret_cast<float *>(smem + L.red_root);
   const TlRecRing ring{reinterpret_cast<int4 *>(smem + L.recs), bars + NSTAGE, a.steps_rev, nst, a.timeout_ns};
-  const int Q = tl_q(NT, P);
+  // reduction split: unit = (child, category pair), U threads per unit
+  constexpr int UNITS = 2 * KQ;
+  constexpr int U = NT / UNITS;
   const float w = act ? float(a.weights[n]) : 0.0f;
 
   if (tid == 0) {
@@ -482,15 +479,16 @@ __global__ void __launch_bounds__(NT) tl_backward_kernel(const PruneArgs<float> 
   int prev_left = -1, prev_right = -1;
   int cs = 0, cph = 0, is = NSTAGE - 1;
   for (int j = 0; j <= nst; ++j) {
-    if (j > 0) {  // finish iteration j-1's per-branch sums: row (c, i, jj) holds 2KQ categories
-      const float *rb = red + ((j - 1) & 1) * 32 * Q * 2 * KQ;
+    if (j > 0) {  // finish iteration j-1's per-branch sums (fixed order over the U partial blocks)
       for (int e = tid; e < 2 * KSS; e += NT) {
         const int side = e >= KSS;
         const int ei = side ? e - KSS : e;  // (k, i, jj) in the output order
-        const int k = ei >> 4, i = (ei >> 2) & 3, jj = ei & 3;
-        const int row = side * 16 + i * 4 + jj;
+        const int k = ei >> 4, ij = ei & 15;
+        const int unit = side * KQ + (k >> 1);
+        const float2 *rb = red + ij * (NT + 1) + unit * U;
         float acc = 0.0f;
-        for (int q = 0; q < Q; ++q) acc += rb[(row * Q + q) * 2 * KQ + k];
+#pragma unroll 4
+        for (int u = 0; u < U; ++u) acc += (k & 1) ? rb[u].y : rb[u].x;
         const int branch = side ? prev_right : prev_left;
         a.gpart[((size_t(b) * a.branch_count + branch) * a.ntiles + tile) * KSS + ei] = acc;
       }
@@ -631,37 +629,55 @@ __global__ void __launch_bounds__(NT) tl_backward_kernel(const PruneArgs<float> 
     }
     __syncthreads();  // xbuf complete
 
-    // transpose reduction over the tile's patterns:
+    // reduction over the tile's patterns, register-blocked:
     //   G[c][k][i][jj] = sum_p (coef x_c)[p][i][k] * v_c[p][jj][k]
-    // item = (row = c*16 + i*4 + jj, q): all 2KQ categories at once as pairs
+    // a thread owns the 4x4 block of one (child, category pair) over patterns
+    // s, s+U, ...; the U partial blocks are summed by the next finalize.
     {
-      float *rw = red + (j & 1) * 32 * Q * 2 * KQ;
-      for (int item = tid; item < 32 * Q; item += NT) {
-        const int row = item / Q, q = item % Q;
-        const int c = row >> 4, i = (row >> 2) & 3, jj = row & 3;
+      const int unit = tid / U, sidx = tid - unit * U;
+      if (unit < UNITS) {
+        const int c = unit / KQ, t = unit - c * KQ;
         const bool tipc = c ? rtip : ltip;
         const float2 *xs = reinterpret_cast<const float2 *>(xbuf + c * NC * P);
         const float2 *vs = reinterpret_cast<const float2 *>(c ? kidr : kidl);
         const unsigned char *csd = stg + G.codes + c * P;
-        float2 acc[KQ];
+        float2 acc[4][4];
 #pragma unroll
-        for (int t = 0; t < KQ; ++t) acc[t] = make_float2(0.0f, 0.0f);
-        for (int m = q; m < rem; m += Q) {
+        for (int i = 0; i < 4; ++i)
 #pragma unroll
-          for (int t = 0; t < KQ; ++t) {
-            // pair t of state i (x) and state jj (v): float index (i*2KQ + 2t), chunk-split over P
-            const int ex = i * 2 * KQ + 2 * t, ev = jj * 2 * KQ + 2 * t;
-            const float2 x = xs[((ex >> 2) * P + m) * 2 + ((ex >> 1) & 1)];
-            const float2 v = tipc ? tab2[int(csd[m]) * 4 + jj] : vs[((ev >> 2) * P + m) * 2 + ((ev >> 1) & 1)];
-            acc[t] = __ffma2_rn(x, v, acc[t]);
+          for (int jj = 0; jj < 4; ++jj) acc[i][jj] = make_float2(0.0f, 0.0f);
+#pragma unroll 4
+        for (int m = sidx; m < rem; m += U) {
+          float2 x[4], v[4];
+#pragma unroll
+          for (int i = 0; i < 4; ++i) {
+            const int e = i * 2 * KQ + 2 * t;  // pair t of state i: chunk e/4, half (e/2)&1
+            x[i] = xs[((e >> 2) * P + m) * 2 + ((e >> 1) & 1)];
           }
-        }
-        float *dst = rw + (row * Q + q) * 2 * KQ;
+          if (tipc) {
+            const float4 *tr = reinterpret_cast<const float4 *>(tab2 + int(csd[m]) * 4);
+            const float4 t0 = tr[0], t1 = tr[1];
+            v[0] = make_float2(t0.x, t0.y);
+            v[1] = make_float2(t0.z, t0.w);
+            v[2] = make_float2(t1.x, t1.y);
+            v[3] = make_float2(t1.z, t1.w);
+          } else {
 #pragma unroll
-        for (int t = 0; t < KQ; ++t) {
-          dst[2 * t] = acc[t].x;
-          dst[2 * t + 1] = acc[t].y;
+            for (int jj = 0; jj < 4; ++jj) {
+              const int e = jj * 2 * KQ + 2 * t;
+              v[jj] = vs[((e >> 2) * P + m) * 2 + ((e >> 1) & 1)];
+            }
+          }
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) acc[i][jj] = __ffma2_rn(x[i], v[jj], acc[i][jj]);
         }
+        // element-major with a padded row: consecutive threads write consecutive words
+#pragma unroll
+        for (int i = 0; i < 4; ++i)
+#pragma unroll
+          for (int jj = 0; jj < 4; ++jj) red[(i * 4 + jj) * (NT + 1) + tid] = acc[i][jj];
       }
     }
     prev_left = left;
