@@ -320,7 +320,7 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
   auto fits = [&](int tile, bool bwd) {
     int &ns = bwd ? p->nstage_b : p->nstage_f;
     const int want = ns;
-    for (; ns >= (f32 ? 3 : want); --ns)
+    for (; ns >= (f32 ? std::min(3, want) : want); --ns)
       if (smem_of(tile, bwd) <= size_t(smem_max)) return true;
     ns = want;
     return false;
