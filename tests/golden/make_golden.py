@@ -186,9 +186,9 @@ def main(ref_root: str) -> None:
             raise NotImplementedError
 
     def run_model(topo, seqs, bl, subst, site_model, clock=None, amb=False, tip_states=False,
-                  rescale=False, params=()):
+                  rescale=False, params=(), data_type=None):
         names = topo.tip_names
-        aln = alignment_of(list(seqs), names, nuc)
+        aln = alignment_of(list(seqs), names, data_type or nuc)
         sp = SitePattern(None, aln)
         blp = Parameter(None, bl)
         tree = FixedTree(topo.postorder, names, blp)
@@ -293,6 +293,40 @@ def main(ref_root: str) -> None:
     urng = np.random.default_rng(12)
     wlu.sequences = ["".join(urng.choice(list("ACGT"), 40)) for _ in range(700)]
     dna_case("gtr_w4_t700_underflow", wlu)
+    # 20-state amino acids (general symmetric model) and 61-state codons (MG94)
+    def wide_case(key, wl, sample=slice(None), rescale=False, tip_states=False):
+        topo = wl.topology
+        bl = torch.tensor(wl.branch_lengths[sample], requires_grad=True)
+        pi = torch.tensor(wl.pi[sample], requires_grad=True)
+        shape = torch.tensor(wl.shape[sample], requires_grad=True)
+        ex = torch.tensor(wl.exch[sample], requires_grad=True)
+        if wl.model == "general":
+            dtype = aa
+            subst = GeneralSymmetricSubstitutionModel(None, aa, Parameter(None, torch.arange(190)),
+                                                      Parameter(None, ex), Parameter(None, pi))
+        else:  # MG94 with alpha = 1, beta = omega
+            dtype = codon
+            subst = MG94(None, codon, Parameter(None, torch.ones_like(ex[..., :1])), Parameter(None, ex[..., 1:2]),
+                         Parameter(None, ex[..., 0:1]), Parameter(None, pi))
+        site = WeibullSiteModel(None, Parameter(None, shape), wl.categories)
+        lnl, grads, flag = run_model(topo, wl.sequences, bl, subst, site, rescale=rescale, tip_states=tip_states,
+                                     params=[ex, pi, shape], data_type=dtype)
+        lik[key] = {"postorder": topo.postorder.tolist(), "names": topo.tip_names, "sequences": wl.sequences,
+                    "branch_lengths": bl.tolist(), "model": wl.model, "data_type": wl.data_type,
+                    "exch": ex.tolist(), "pi": pi.tolist(), "shape": shape.tolist(), "categories": wl.categories,
+                    "site_model": "weibull", "rescale": rescale, "tip_states": tip_states, "use_ambiguities": False,
+                    "rescaled_after": flag, "lnl": lnl.reshape(-1).tolist(),
+                    "grad_branch_lengths": grads[0].tolist(), "grad_exch": grads[1].tolist(),
+                    "grad_pi": grads[2].tolist(), "grad_shape": grads[3].tolist()}
+
+    wlp = synthetic.protein_workload("prot", tip_count=16, site_count=150, batch=2, seed=21, site_model="weibull",
+                                     shape=0.6, branch_mean=0.1)
+    wide_case("prot_w4_t16_b2", wlp)
+    wide_case("prot_w4_t16_b2_tipstates", wlp, tip_states=True)
+    wlc = synthetic.codon_workload("codon", tip_count=10, site_count=60, batch=2, seed=22, site_model="weibull",
+                                   shape=0.8, branch_mean=0.1)
+    wide_case("codon_w4_t10_b2", wlc)
+    wide_case("codon_w4_t10_b2_rescaled", wlc, rescale=True)
     with io.open(HERE / "likelihood.json", "w") as fh:
         json.dump(lik, fh)
     print("wrote", sorted(p.name for p in HERE.glob("*.json")))

@@ -12,13 +12,29 @@ from oracle import likelihood as OL
 from oracle import patterns as OP
 
 
+def record_encoding(rec):
+    """(code_fn, partial_fn(use_ambiguities), state_count, characters per site) of a record's data type."""
+    kind = rec.get("data_type", "nucleotide")
+    if kind == "amino_acid":
+        return OP.amino_acid_code, OP.amino_acid_partial, 20, 1
+    if kind == "codon":
+        cc = OP.CodonCode(OL.UNIVERSAL_CODE)
+        return cc.code, cc.partial, cc.state_count, 3
+    return OP.nucleotide_code, OP.nucleotide_partial, 4, 1
+
+
+def state_count_of(rec) -> int:
+    return record_encoding(rec)[2]
+
+
 def tips_from_record(rec, dtype=torch.float64):
     seqs = rec["sequences"]
+    code_fn, partial_fn, S, size = record_encoding(rec)
     if rec.get("tip_states"):
-        tips, w = OP.compress_states(seqs, OP.nucleotide_code, 4)
+        tips, w = OP.compress_states(seqs, code_fn, S, size=size)
         return [torch.tensor(t, dtype=torch.long) for t in tips], torch.tensor(w)
     amb = rec.get("use_ambiguities", False)
-    tips, w = OP.compress_partials(seqs, lambda c: OP.nucleotide_partial(c, amb))
+    tips, w = OP.compress_partials(seqs, lambda c: partial_fn(c, amb), size=size)
     return [torch.tensor(t, dtype=dtype) for t in tips], torch.tensor(w)
 
 
@@ -45,6 +61,13 @@ def model_pieces(rec, x):
     elif rec["model"] == "gtr":
         pi = x["pi"]
         q = OL.q_gtr(x["exch"], pi)
+    elif rec["model"] == "general":
+        pi = x["pi"]
+        q = OL.q_general_symmetric(x["exch"], pi, pi.shape[-1])
+    elif rec["model"] == "mg94":  # exch = (kappa, omega), alpha = 1
+        pi = x["pi"]
+        kappa, omega = x["exch"][..., 0:1], x["exch"][..., 1:2]
+        q = OL.q_mg94(torch.ones_like(kappa), omega, kappa, pi)
     else:
         pi = x["pi"]
         q = OL.q_hky(x["exch"], pi)

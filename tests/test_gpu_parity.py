@@ -48,8 +48,7 @@ def engine_eval(rec, precision, rescale=None):
     The 4x4 eigendecompositions run on the CPU (one LAPACK call per matrix),
     so a batch member's inputs are bit-identical to its single evaluation.
     """
-    from torchtree_gb300 import patterns, site_models, substitution
-    from torchtree_gb300.datatype import Nucleotide
+    from torchtree_gb300 import datatype, patterns, site_models, substitution
     from torchtree_gb300.likelihood import PhyloLikelihood
     from torchtree_gb300.tree import Topology
 
@@ -59,7 +58,9 @@ def engine_eval(rec, precision, rescale=None):
     b = x["bl"].shape[0] if batched else 1
     lead = lambda t: t if batched else t.unsqueeze(0)  # noqa: E731
     topo = Topology(rec["postorder"], rec["names"])
-    ca = patterns.compress(rec["sequences"], Nucleotide(), use_ambiguities=rec.get("use_ambiguities", False),
+    dt = datatype.get(rec.get("data_type", "nucleotide"))
+    S = dt.state_count
+    ca = patterns.compress(rec["sequences"], dt, use_ambiguities=rec.get("use_ambiguities", False),
                            tip_states=rec.get("tip_states", False))
     if rec["site_model"] == "weibull":
         rates, probs = site_models.weibull_rates(lead(x["shape"]), rec["categories"],
@@ -72,7 +73,7 @@ def engine_eval(rec, precision, rescale=None):
         probs = torch.full((b, rec["categories"]), 1.0 / rec["categories"], dtype=torch.float64, device=dev)
     K = rates.shape[-1]
     probs = probs.expand(b, K)
-    lik = PhyloLikelihood(topo, ca, 4, K, batch=b, precision=precision)
+    lik = PhyloLikelihood(topo, ca, S, K, batch=b, precision=precision)
     if rescale is not None:
         lik.rescale = rescale
     bls = lik.node_branch_lengths(lead(x["bl"]))
@@ -85,8 +86,15 @@ def engine_eval(rec, precision, rescale=None):
         lnl = lik.evaluate_matrices(mats, probs, pi)
     else:
         pi = lead(x["pi"])
-        q = substitution.gtr_q(lead(x["exch"]), pi) if rec["model"] == "gtr" else \
-            substitution.hky_q(lead(x["exch"]), pi)
+        ex = lead(x["exch"])
+        if rec["model"] == "gtr":
+            q = substitution.gtr_q(ex, pi)
+        elif rec["model"] == "hky":
+            q = substitution.hky_q(ex, pi)
+        elif rec["model"] == "general":
+            q = substitution.general_symmetric_q(ex, pi, S)
+        else:  # mg94: (kappa, omega), alpha = 1
+            q = substitution.mg94_q(torch.ones_like(ex[..., 0:1]), ex[..., 1:2], ex[..., 0:1], pi)
         lam, u, w = (t.to(dev) for t in substitution.eigen_system(q.cpu(), pi.cpu()))
         lnl = lik.evaluate_eigen(lam, u, w, bls, rates, probs, pi)
     leaves = [(k, g) for k, g in GRAD_KEYS if k in x and g in rec]
@@ -150,15 +158,14 @@ def test_rescaled_equals_unscaled_fp64(golden_likelihood):
 
 def test_finite_differences_fp64(golden_likelihood):
     """Central differences of the engine's own FP64 lnL vs its adjoint gradient."""
-    from torchtree_gb300 import patterns, site_models, substitution
-    from torchtree_gb300.datatype import Nucleotide
+    from torchtree_gb300 import datatype, patterns, site_models, substitution
     from torchtree_gb300.likelihood import PhyloLikelihood
     from torchtree_gb300.tree import Topology
 
     rec = golden_likelihood["gtr_w4_t9_ambiguities"]
     dev = torch.device("cuda")
     topo = Topology(rec["postorder"], rec["names"])
-    ca = patterns.compress(rec["sequences"], Nucleotide(), use_ambiguities=True)
+    ca = patterns.compress(rec["sequences"], datatype.Nucleotide(), use_ambiguities=True)
     lik = PhyloLikelihood(topo, ca, 4, 4, batch=1, precision="f64")
 
     def f(bl, exch, pi, shape):

@@ -13,6 +13,7 @@
 
 #include "../../include/torchtree_gb300.h"
 #include "tt_launch.h"
+#include "tt_plan.h"
 
 namespace {
 
@@ -37,34 +38,7 @@ namespace tt {
 int record_error(int code, const char *msg) { return fail(code, msg); }
 }  // namespace tt
 
-struct tt_plan {
-  int device = 0;
-  int T = 0, I = 0, B = 0, S = 0, K = 0, N = 0, batch = 0, precision = 0;
-  int C = 0, slots_fwd = 0, slots_bwd = 0;
-  int tile_f = 0, tile_b = 0, ntiles_f = 0, ntiles_b = 0, code_stride = 0;
-  int nstage_f = tt::kStages, nstage_b = tt::kStages;
-  size_t elem = 0;  // bytes per partial value
-  bool tips_set = false, pmat_set = false, partials_valid = false, grads_valid = false;
-  long long launches = 0;
-  std::vector<int> steps;       // host copy of the schedule (I x 12)
-  std::vector<int> branch_pos;  // B
-  // device buffers
-  int4 *d_steps = nullptr;
-  int4 *d_steps_rev = nullptr;
-  int *d_branch_pos = nullptr;
-  uint8_t *d_codes = nullptr;
-  void *d_table = nullptr;
-  double *d_weights = nullptr;
-  void *d_pmat = nullptr;
-  void *d_partials = nullptr;
-  double *d_tile_lnl = nullptr;
-  void *d_gpart = nullptr;
-  void *d_rootpart = nullptr;
-  double *d_G = nullptr;
-  double *d_rootgrad = nullptr;
-  int *d_status = nullptr;
-  size_t bytes = 0;
-};
+
 
 namespace {
 
@@ -88,6 +62,7 @@ void release(tt_plan *p) {
                   p->d_G,     p->d_rootgrad,   p->d_status};
   for (void *b : bufs)
     if (b) cudaFree(b);
+  tt::wide_destroy(p);
 }
 
 // Build the execution order and the shared-memory slot plan.
@@ -272,8 +247,8 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
   if (!plan || !postorder) return fail(TT_ERR_INVALID_ARGUMENT, "plan and postorder must not be NULL");
   *plan = nullptr;
   if (tip_count < 2) return fail(TT_ERR_INVALID_ARGUMENT, "a tree needs at least 2 tips");
-  if (state_count != 4)
-    return fail(TT_ERR_UNSUPPORTED, "this build's pruning kernels support 4-state (nucleotide) models");
+  if (state_count < 2 || state_count > 64)
+    return fail(TT_ERR_UNSUPPORTED, "state_count must be in [2, 64]");
   if (category_count < 1 || category_count > 8)
     return fail(TT_ERR_INVALID_ARGUMENT, "category_count must be in [1, 8]");
   if (pattern_count < 1) return fail(TT_ERR_INVALID_ARGUMENT, "pattern_count must be >= 1");
@@ -300,6 +275,16 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
   if (rc != TT_OK) {
     delete p;
     return rc;
+  }
+  if (p->S != 4) {  // amino-acid / codon / general models: level-scheduled wide-state kernels
+    rc = tt::wide_create(p);
+    if (rc != TT_OK) {
+      release(p);
+      delete p;
+      return rc;
+    }
+    *plan = p;
+    return TT_OK;
   }
   int smem_max = 0;
   cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
@@ -424,6 +409,14 @@ int tt_plan_set_tips(tt_plan *p, const uint8_t *codes, const double *code_table,
                                                std::to_string(i) + " is >= code_count");
   for (int n = 0; n < p->N; ++n)
     if (!(weights[n] >= 0.0)) return fail(TT_ERR_INVALID_ARGUMENT, "pattern weights must be >= 0");
+  if (p->wide) {
+    rc = tt::wide_set_tips(p, codes, code_table, code_count, weights);
+    if (rc) return rc;
+    p->C = code_count;
+    p->tips_set = true;
+    p->partials_valid = false;
+    return TT_OK;
+  }
   std::vector<unsigned char> table(size_t(code_count) * p->S * p->elem);
   for (size_t i = 0; i < size_t(code_count) * p->S; ++i) {
     if (p->precision == TT_PRECISION_F32) {
@@ -452,6 +445,13 @@ int tt_update_transition_matrices(tt_plan *p, const double *lam, const double *U
   int rc = check_device(p);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->wide) {
+    rc = tt::wide_update_matrices(p, lam, U, W, bl, rates, s);
+    if (rc) return rc;
+    p->pmat_set = true;
+    p->partials_valid = false;
+    return TT_OK;
+  }
   cudaError_t e =
       p->precision == TT_PRECISION_F32
           ? tt::launch_pmatrix_f32(lam, U, W, bl, rates, p->d_branch_pos, static_cast<float *>(p->d_pmat),
@@ -470,6 +470,13 @@ int tt_set_transition_matrices(tt_plan *p, const double *matrices, void *stream)
   int rc = check_device(p);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->wide) {
+    rc = tt::wide_set_matrices(p, matrices, s);
+    if (rc) return rc;
+    p->pmat_set = true;
+    p->partials_valid = false;
+    return TT_OK;
+  }
   const int kss = p->K * p->S * p->S;
   cudaError_t e = p->precision == TT_PRECISION_F32
                       ? tt::launch_scatter_f32(matrices, p->d_branch_pos, static_cast<float *>(p->d_pmat),
@@ -491,6 +498,12 @@ int tt_log_likelihood(tt_plan *p, const double *props, const double *freqs, int3
   int rc = check_device(p);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->wide) {
+    rc = tt::wide_log_likelihood(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, lnl, site_lnl, s);
+    if (rc) return rc;
+    p->partials_valid = keep_partials != 0;
+    return TT_OK;
+  }
   cudaError_t e;
   if (p->precision == TT_PRECISION_F32) {
     auto a = make_args<float>(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, site_lnl);
@@ -518,6 +531,13 @@ int tt_gradient(tt_plan *p, const double *props, const double *freqs, double *gr
   int rc = check_device(p);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
+  if (p->wide) {  // the wide-state adjoint overwrites the stored partials
+    rc = tt::wide_gradient(p, props, freqs, grad_matrices, grad_frequencies, grad_weights, s);
+    if (rc) return rc;
+    p->partials_valid = false;
+    p->grads_valid = true;
+    return TT_OK;
+  }
   cudaError_t e;
   if (p->precision == TT_PRECISION_F32) {
     auto a = make_args<float>(p, props, freqs, 1, true, nullptr);
@@ -570,6 +590,9 @@ int tt_transition_matrices_gradient(tt_plan *p, const double *lam, const double 
   if (!p->grads_valid) return fail(TT_ERR_NOT_READY, "tt_gradient has not been called");
   int rc = check_device(p);
   if (rc) return rc;
+  if (p->wide)
+    return tt::wide_matrices_gradient(p, lam, U, W, bl, rates, dlam, dU, dW, dbl, drates,
+                                      static_cast<cudaStream_t>(stream));
   cudaError_t e = tt::launch_pmatrix_backward(p->d_G, lam, U, W, bl, rates, p->S, p->B, p->K, p->batch,
                                               dlam, dU, dW, dbl, drates, static_cast<cudaStream_t>(stream));
   if (e != cudaSuccess) return cuda_fail(e, "transition-matrix gradient launch");

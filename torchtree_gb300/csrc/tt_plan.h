@@ -1,0 +1,61 @@
+// Internal plan state shared by the C-ABI translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <vector>
+
+#include "tt_launch.h"
+
+namespace tt {
+struct WideState;  // state of the wide-state (S != 4) path, tt_wide.cu
+}
+
+struct tt_plan {
+  int device = 0;
+  int T = 0, I = 0, B = 0, S = 0, K = 0, N = 0, batch = 0, precision = 0;
+  int C = 0, slots_fwd = 0, slots_bwd = 0;
+  int tile_f = 0, tile_b = 0, ntiles_f = 0, ntiles_b = 0, code_stride = 0;
+  int nstage_f = tt::kStages, nstage_b = tt::kStages;
+  size_t elem = 0;  // bytes per partial value
+  bool tips_set = false, pmat_set = false, partials_valid = false, grads_valid = false;
+  long long launches = 0;
+  std::vector<int> steps;       // host copy of the schedule (I x 12)
+  std::vector<int> branch_pos;  // B
+  // device buffers
+  int4 *d_steps = nullptr;
+  int4 *d_steps_rev = nullptr;
+  int *d_branch_pos = nullptr;
+  uint8_t *d_codes = nullptr;
+  void *d_table = nullptr;
+  double *d_weights = nullptr;
+  void *d_pmat = nullptr;
+  void *d_partials = nullptr;
+  double *d_tile_lnl = nullptr;
+  void *d_gpart = nullptr;
+  void *d_rootpart = nullptr;
+  double *d_G = nullptr;
+  double *d_rootgrad = nullptr;
+  int *d_status = nullptr;
+  size_t bytes = 0;
+  tt::WideState *wide = nullptr;  // non-NULL for S != 4 plans
+};
+
+namespace tt {
+// Wide-state path (tt_wide.cu): same contracts as the C entry points.
+int wide_create(tt_plan *p);
+void wide_destroy(tt_plan *p);
+int wide_set_tips(tt_plan *p, const uint8_t *codes, const double *code_table, int code_count,
+                  const double *weights);
+int wide_update_matrices(tt_plan *p, const double *lam, const double *U, const double *W, const double *bl,
+                         const double *rates, cudaStream_t s);
+int wide_set_matrices(tt_plan *p, const double *matrices, cudaStream_t s);
+int wide_log_likelihood(tt_plan *p, const double *props, const double *freqs, int rescale, bool keep,
+                        double *lnl, double *site_lnl, cudaStream_t s);
+int wide_gradient(tt_plan *p, const double *props, const double *freqs, double *grad_matrices,
+                  double *grad_frequencies, double *grad_weights, cudaStream_t s);
+int wide_matrices_gradient(tt_plan *p, const double *lam, const double *U, const double *W, const double *bl,
+                           const double *rates, double *dlam, double *dU, double *dW, double *dbl,
+                           double *drates, cudaStream_t s);
+}  // namespace tt

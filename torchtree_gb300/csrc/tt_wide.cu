@@ -1,0 +1,417 @@
+// Host side of the wide-state path (S != 4: amino acids, codons): level
+// schedule, workspace and launch sequences behind the C entry points.
+#include <algorithm>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/torchtree_gb300.h"
+#include "tt_plan.h"
+#include "tt_wide.cuh"
+
+namespace tt {
+
+__global__ void wide_root_kernel(const double *root_site, const int *root_expo, const double *props,
+                                 const double *weights, double *site_lnl, double *log2L, double *block_lnl,
+                                 int K, int N, int Npad) {
+  __shared__ double part[8];
+  const int b = blockIdx.y, n = blockIdx.x * 256 + threadIdx.x;
+  double contrib = 0.0;
+  if (n < N) {
+    int emax = INT_MIN;
+    for (int k = 0; k < K; ++k) emax = max(emax, root_expo[(size_t(b) * K + k) * Npad + n]);
+    double s = 0.0;
+    for (int k = 0; k < K; ++k) {
+      const size_t o = (size_t(b) * K + k) * Npad + n;
+      s += props[size_t(b) * K + k] * ldexp(root_site[o], root_expo[o] - emax);
+    }
+    const double l2 = log2(s) + double(emax);
+    const double ll = l2 * 0.69314718055994530942;
+    if (site_lnl) site_lnl[size_t(b) * N + n] = ll;
+    log2L[size_t(b) * Npad + n] = l2;
+    contrib = weights[n] * ll;
+  }
+  contrib = warp_sum(contrib);
+  if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = contrib;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t = 0.0;
+    for (int w = 0; w < 8; ++w) t += part[w];
+    block_lnl[size_t(b) * gridDim.x + blockIdx.x] = t;
+  }
+}
+
+__global__ void wide_pmatrix_grad_reduce_kernel(const double *part, int nchunks, int S, int K, double *dlam,
+                                                double *dU, double *dW, double *drates) {
+  const int b = blockIdx.x;
+  const int width = 2 * S * S + S + K;
+  for (int e = threadIdx.x; e < width; e += blockDim.x) {
+    double s = 0.0;
+    for (int c = 0; c < nchunks; ++c) s += part[(size_t(b) * nchunks + c) * width + e];
+    if (e < S * S) {
+      if (dU) dU[size_t(b) * S * S + e] = s;
+    } else if (e < 2 * S * S) {
+      if (dW) dW[size_t(b) * S * S + e - S * S] = s;
+    } else if (e < 2 * S * S + S) {
+      if (dlam) dlam[size_t(b) * S + e - 2 * S * S] = s;
+    } else if (drates) {
+      drates[size_t(b) * K + e - 2 * S * S - S] = s;
+    }
+  }
+}
+
+struct WideState {
+  int SP = 0, PTf = 0, PTb = 0, Npad = 0, ntiles_f = 0, ntiles_b = 0, nchunks = 1, tpc = 1, nblk = 0;
+  int bchunk = 8, nbchunks = 1;
+  std::vector<int> fwd_off, bwd_off;  // level boundaries in d_fwd / d_bwd
+  int *d_left = nullptr, *d_right = nullptr, *d_fwd = nullptr, *d_bwd = nullptr;
+  void *d_part = nullptr;
+  int *d_expo = nullptr;
+  double *d_root_site = nullptr;
+  int *d_root_expo = nullptr;
+  double *d_log2L = nullptr;
+  double *d_block_lnl = nullptr;
+  void *d_gpart = nullptr;
+  void *d_rootpart = nullptr;
+  double *d_pgpart = nullptr;
+};
+
+namespace {
+
+int wfail(int code, const std::string &m) { return record_error(code, m.c_str()); }
+
+int wcuda(cudaError_t e, const char *where) {
+  return wfail(e == cudaErrorMemoryAllocation ? TT_ERR_OUT_OF_MEMORY : TT_ERR_CUDA,
+               std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+template <typename P>
+int walloc(tt_plan *p, P **ptr, size_t bytes, const char *what) {
+  if (bytes == 0) bytes = 16;
+  cudaError_t e = cudaMalloc(reinterpret_cast<void **>(ptr), bytes);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return wfail(TT_ERR_OUT_OF_MEMORY, std::string("cudaMalloc of ") + what + " (" + std::to_string(bytes) +
+                                           " bytes) failed: " + cudaGetErrorString(e));
+  }
+  p->bytes += bytes;
+  return TT_OK;
+}
+
+// compiled (precision, padded states) -> pattern tiles of the two passes
+void tiles_for(bool f32, int SP, int &ptf, int &ptb) {
+  if (SP == 20) {
+    ptf = ptb = 128;
+  } else {
+    ptf = ptb = f32 ? 64 : 32;
+  }
+}
+
+template <typename T, int SP, int PTF, int PTB>
+struct Wide {
+  static cudaError_t prepare() {
+    cudaError_t e = cudaFuncSetAttribute(wide_forward_kernel<T, SP, PTF>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                         int(wide_fwd_smem<T, SP, PTF>()));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(wide_backward_kernel<T, SP, PTB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               int(wide_bwd_smem<T, SP, PTB>()));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(wide_pmatrix_kernel<T, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               int(2 * SP * SP * sizeof(T) + SP * sizeof(double)));
+    if (e == cudaSuccess)
+      e = cudaFuncSetAttribute(wide_pmatrix_backward_kernel<double, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               int(Wide<double, SP, PTF, PTB>::pback_smem()));
+    return e;
+  }
+  static size_t pback_smem() { return 4 * SP * SP * sizeof(T) + (SP / 4 * SP + 3 * SP + 8) * sizeof(double); }
+
+  static WideArgs<T> args(tt_plan *p, const double *props, const double *freqs, int rescale) {
+    WideState &w = *p->wide;
+    WideArgs<T> a;
+    a.tips = p->T;
+    a.N = p->N;
+    a.Npad = w.Npad;
+    a.K = p->K;
+    a.B = p->B;
+    a.I = p->I;
+    a.S = p->S;
+    a.code_stride = p->code_stride;
+    a.rescale = rescale;
+    a.nchunks = w.nchunks;
+    a.tiles_per_chunk = w.tpc;
+    a.ntiles = w.ntiles_b;
+    a.nodes = nullptr;
+    a.left = w.d_left;
+    a.right = w.d_right;
+    a.codes = p->d_codes;
+    a.table = static_cast<const T *>(p->d_table);
+    a.pmat = static_cast<const T *>(p->d_pmat);
+    a.part = static_cast<T *>(w.d_part);
+    a.expo = w.d_expo;
+    a.props = props;
+    a.freqs = freqs;
+    a.weights = p->d_weights;
+    a.root_site = w.d_root_site;
+    a.root_expo = w.d_root_expo;
+    a.log2L = w.d_log2L;
+    a.gpart = static_cast<T *>(w.d_gpart);
+    a.rootpart = static_cast<T *>(w.d_rootpart);
+    return a;
+  }
+
+  static cudaError_t forward(tt_plan *p, const double *props, const double *freqs, int rescale, double *lnl,
+                             double *site_lnl, cudaStream_t s) {
+    WideState &w = *p->wide;
+    WideArgs<T> a = args(p, props, freqs, rescale);
+    constexpr int NT = WideCfg<T, SP, PTF>::NT;
+    const size_t smem = wide_fwd_smem<T, SP, PTF>();
+    for (size_t lv = 0; lv + 1 < w.fwd_off.size(); ++lv) {
+      a.nodes = w.d_fwd + w.fwd_off[lv];
+      const dim3 grid(w.ntiles_f, w.fwd_off[lv + 1] - w.fwd_off[lv], p->batch * p->K);
+      wide_forward_kernel<T, SP, PTF><<<grid, NT, smem, s>>>(a);
+      p->launches += 1;
+    }
+    wide_root_kernel<<<dim3(w.nblk, p->batch), 256, 0, s>>>(w.d_root_site, w.d_root_expo, props, p->d_weights,
+                                                           site_lnl, w.d_log2L, w.d_block_lnl, p->K, p->N, w.Npad);
+    cudaError_t e = launch_reduce_lnl(w.d_block_lnl, lnl, p->batch, w.nblk, s);
+    p->launches += 2;
+    return e == cudaSuccess ? cudaGetLastError() : e;
+  }
+
+  static cudaError_t backward(tt_plan *p, const double *props, const double *freqs, cudaStream_t s) {
+    WideState &w = *p->wide;
+    WideArgs<T> a = args(p, props, freqs, 1);
+    constexpr int NT = WideCfg<T, SP, PTB>::NT;
+    const size_t smem = wide_bwd_smem<T, SP, PTB>();
+    for (size_t lv = 0; lv + 1 < w.bwd_off.size(); ++lv) {
+      a.nodes = w.d_bwd + w.bwd_off[lv];
+      const dim3 grid(w.nchunks, w.bwd_off[lv + 1] - w.bwd_off[lv], p->batch * p->K);
+      wide_backward_kernel<T, SP, PTB><<<grid, NT, smem, s>>>(a);
+      p->launches += 1;
+    }
+    wide_grad_reduce_kernel<T><<<dim3(p->B, p->batch), 256, 0, s>>>(static_cast<const T *>(w.d_gpart), p->d_G,
+                                                                     p->B, w.nchunks, p->K, p->S, SP);
+    wide_root_reduce_kernel<T><<<p->batch, 64, 0, s>>>(static_cast<const T *>(w.d_rootpart), p->d_rootgrad,
+                                                       p->d_rootgrad + size_t(p->batch) * p->S, w.nchunks, p->K,
+                                                       p->S, SP);
+    p->launches += 2;
+    return cudaGetLastError();
+  }
+
+  static cudaError_t pmatrix(tt_plan *p, const double *lam, const double *U, const double *W, const double *bl,
+                             const double *rates, cudaStream_t s) {
+    wide_pmatrix_kernel<T, SP><<<dim3(p->B, p->batch), 256, 2 * SP * SP * sizeof(T) + SP * sizeof(double), s>>>(
+        lam, U, W, bl, rates, static_cast<T *>(p->d_pmat), p->S, p->B, p->K);
+    p->launches += 1;
+    return cudaGetLastError();
+  }
+
+  static cudaError_t pmatrix_backward(tt_plan *p, const double *lam, const double *U, const double *W,
+                                      const double *bl, const double *rates, double *dlam, double *dU, double *dW,
+                                      double *dbl, double *drates, cudaStream_t s) {
+    WideState &w = *p->wide;
+    wide_pmatrix_backward_kernel<double, SP><<<dim3(w.nbchunks, p->batch), 256, Wide<double, SP, PTF, PTB>::pback_smem(), s>>>(
+        p->d_G, lam, U, W, bl, rates, p->S, p->B, p->K, w.bchunk, dbl, w.d_pgpart);
+    wide_pmatrix_grad_reduce_kernel<<<p->batch, 256, 0, s>>>(w.d_pgpart, w.nbchunks, p->S, p->K, dlam, dU, dW,
+                                                             drates);
+    p->launches += 2;
+    return cudaGetLastError();
+  }
+};
+
+// dispatch on (precision, SP)
+template <typename F>
+cudaError_t dispatch(tt_plan *p, F &&f) {
+  const bool f32 = p->precision == TT_PRECISION_F32;
+  if (p->wide->SP == 20) {
+    if (f32) return f(Wide<float, 20, 128, 128>());
+    return f(Wide<double, 20, 128, 128>());
+  }
+  if (f32) return f(Wide<float, 64, 64, 64>());
+  return f(Wide<double, 64, 32, 32>());
+}
+
+}  // namespace
+
+int wide_create(tt_plan *p) {
+  if (p->S < 2 || p->S > 64) return wfail(TT_ERR_UNSUPPORTED, "state_count must be in [2, 64]");
+  WideState *w = new WideState();
+  p->wide = w;
+  const bool f32 = p->precision == TT_PRECISION_F32;
+  w->SP = p->S <= 20 ? 20 : 64;
+  tiles_for(f32, w->SP, w->PTf, w->PTb);
+  w->Npad = (p->N + 127) / 128 * 128;
+  w->ntiles_f = w->Npad / w->PTf;
+  w->ntiles_b = w->Npad / w->PTb;
+  w->nblk = (p->N + 255) / 256;
+  if (size_t(p->batch) * p->K > 65535) return wfail(TT_ERR_INVALID_ARGUMENT, "batch * category_count must be <= 65535");
+  {
+    const int want = (2 * 152 + p->batch * p->K - 1) / (p->batch * p->K);
+    w->nchunks = std::max(1, std::min({want, w->ntiles_b, 64}));
+    w->tpc = (w->ntiles_b + w->nchunks - 1) / w->nchunks;
+    w->nchunks = (w->ntiles_b + w->tpc - 1) / w->tpc;
+  }
+  w->nbchunks = (p->B + w->bchunk - 1) / w->bchunk;
+  p->code_stride = w->Npad;
+
+  // children, levels by height (forward) and by depth (adjoint); the postorder
+  // was validated by build_schedule
+  const int T = p->T, I = p->I, NN = 2 * T - 1;
+  std::vector<int> left(I), right(I), height(NN, 0), depth(NN, 0);
+  // the schedule holds (node, left, right) in an evaluation order that is a post-order
+  for (int s = 0; s < I; ++s) {
+    const int *rec = &p->steps[size_t(s) * kStepInts];
+    const int v = rec[0], l = rec[1], r = rec[2];
+    left[v - T] = l;
+    right[v - T] = r;
+    height[v] = 1 + std::max(height[l], height[r]);
+  }
+  for (int s = I - 1; s >= 0; --s) {
+    const int *rec = &p->steps[size_t(s) * kStepInts];
+    depth[rec[1]] = depth[rec[0]] + 1;
+    depth[rec[2]] = depth[rec[0]] + 1;
+  }
+  int H = 0, D = 0;
+  for (int v = T; v < NN; ++v) {
+    H = std::max(H, height[v]);
+    D = std::max(D, depth[v]);
+  }
+  std::vector<int> fwd, bwd;
+  w->fwd_off.push_back(0);
+  for (int h = 1; h <= H; ++h) {
+    for (int v = T; v < NN; ++v)
+      if (height[v] == h) fwd.push_back(v);
+    w->fwd_off.push_back(int(fwd.size()));
+  }
+  w->bwd_off.push_back(0);
+  for (int d = 0; d <= D; ++d) {
+    for (int v = T; v < NN; ++v)
+      if (depth[v] == d) bwd.push_back(v);
+    w->bwd_off.push_back(int(bwd.size()));
+  }
+  const size_t es = p->elem, SP = size_t(w->SP), b = size_t(p->batch), K = size_t(p->K);
+  int rc = TT_OK;
+  if (!rc) rc = walloc(p, &w->d_left, I * sizeof(int), "children");
+  if (!rc) rc = walloc(p, &w->d_right, I * sizeof(int), "children");
+  if (!rc) rc = walloc(p, &w->d_fwd, I * sizeof(int), "levels");
+  if (!rc) rc = walloc(p, &w->d_bwd, I * sizeof(int), "levels");
+  if (!rc) rc = walloc(p, &p->d_codes, size_t(T) * p->code_stride, "tip codes");
+  if (!rc) rc = walloc(p, &p->d_table, 256 * SP * es, "code table");
+  if (!rc) rc = walloc(p, &p->d_weights, size_t(p->N) * sizeof(double), "weights");
+  if (!rc) rc = walloc(p, &p->d_pmat, b * p->B * K * SP * SP * es, "transition matrices");
+  if (!rc) rc = walloc(p, &w->d_part, b * I * K * SP * w->Npad * es, "partials");
+  if (!rc) rc = walloc(p, &w->d_expo, b * I * K * w->Npad * sizeof(int), "scale exponents");
+  if (!rc) rc = walloc(p, &w->d_root_site, b * K * w->Npad * sizeof(double), "root sums");
+  if (!rc) rc = walloc(p, &w->d_root_expo, b * K * w->Npad * sizeof(int), "root exponents");
+  if (!rc) rc = walloc(p, &w->d_log2L, b * w->Npad * sizeof(double), "site log-likelihoods");
+  if (!rc) rc = walloc(p, &w->d_block_lnl, b * w->nblk * sizeof(double), "block sums");
+  if (!rc) rc = walloc(p, &w->d_gpart, b * p->B * w->nchunks * K * SP * SP * es, "gradient chunks");
+  if (!rc) rc = walloc(p, &w->d_rootpart, b * w->nchunks * K * (SP + 1) * es, "root gradient chunks");
+  if (!rc)
+    rc = walloc(p, &w->d_pgpart, b * w->nbchunks * (2 * p->S * p->S + p->S + K) * sizeof(double),
+                "matrix gradient chunks");
+  if (!rc) rc = walloc(p, &p->d_G, b * p->B * K * p->S * p->S * sizeof(double), "dlnL/dP");
+  if (!rc) rc = walloc(p, &p->d_rootgrad, b * (p->S + K) * sizeof(double), "root grads");
+  if (!rc) rc = walloc(p, &p->d_status, sizeof(int), "status");
+  if (rc) return rc;
+  cudaError_t e = cudaMemcpy(w->d_left, left.data(), I * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(w->d_right, right.data(), I * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(w->d_fwd, fwd.data(), I * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(w->d_bwd, bwd.data(), I * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, sizeof(int));
+  if (e == cudaSuccess)
+    e = dispatch(p, [](auto W) { return decltype(W)::prepare(); });
+  if (e != cudaSuccess) return wcuda(e, "wide-state plan set-up");
+  return TT_OK;
+}
+
+void wide_destroy(tt_plan *p) {
+  WideState *w = p->wide;
+  if (!w) return;
+  void *bufs[] = {w->d_left, w->d_right, w->d_fwd, w->d_bwd, w->d_part, w->d_expo, w->d_root_site, w->d_root_expo,
+                  w->d_log2L, w->d_block_lnl, w->d_gpart, w->d_rootpart, w->d_pgpart};
+  for (void *x : bufs)
+    if (x) cudaFree(x);
+  delete w;
+  p->wide = nullptr;
+}
+
+int wide_set_tips(tt_plan *p, const uint8_t *codes, const double *code_table, int code_count,
+                  const double *weights) {
+  const int SP = p->wide->SP;
+  std::vector<unsigned char> table(size_t(code_count) * SP * p->elem, 0);
+  for (int c = 0; c < code_count; ++c)
+    for (int j = 0; j < p->S; ++j) {
+      const double v = code_table[size_t(c) * p->S + j];
+      if (p->precision == TT_PRECISION_F32) {
+        const float f = float(v);
+        std::memcpy(&table[(size_t(c) * SP + j) * 4], &f, 4);
+      } else {
+        std::memcpy(&table[(size_t(c) * SP + j) * 8], &v, 8);
+      }
+    }
+  cudaError_t e = cudaMemset(p->d_codes, 0, size_t(p->T) * p->code_stride);
+  if (e == cudaSuccess)
+    e = cudaMemcpy2D(p->d_codes, p->code_stride, codes, p->N, p->N, p->T, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(p->d_table, table.data(), table.size(), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(p->d_weights, weights, size_t(p->N) * sizeof(double), cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return wcuda(e, "tt_plan_set_tips upload");
+  return TT_OK;
+}
+
+int wide_update_matrices(tt_plan *p, const double *lam, const double *U, const double *W, const double *bl,
+                         const double *rates, cudaStream_t s) {
+  cudaError_t e = dispatch(p, [&](auto X) { return decltype(X)::pmatrix(p, lam, U, W, bl, rates, s); });
+  return e == cudaSuccess ? TT_OK : wcuda(e, "transition-matrix launch");
+}
+
+int wide_set_matrices(tt_plan *p, const double *matrices, cudaStream_t s) {
+  const int SP = p->wide->SP;
+  const long long count = (long long)p->batch * p->B * p->K * SP * SP;
+  const unsigned blocks = unsigned((count + 255) / 256);
+  if (p->precision == TT_PRECISION_F32)
+    wide_pmatrix_copy_kernel<float><<<blocks, 256, 0, s>>>(matrices, static_cast<float *>(p->d_pmat), p->S, SP, count);
+  else
+    wide_pmatrix_copy_kernel<double><<<blocks, 256, 0, s>>>(matrices, static_cast<double *>(p->d_pmat), p->S, SP,
+                                                            count);
+  p->launches += 1;
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? TT_OK : wcuda(e, "transition-matrix copy launch");
+}
+
+int wide_log_likelihood(tt_plan *p, const double *props, const double *freqs, int rescale, bool keep, double *lnl,
+                        double *site_lnl, cudaStream_t s) {
+  (void)keep;
+  cudaError_t e =
+      dispatch(p, [&](auto X) { return decltype(X)::forward(p, props, freqs, rescale, lnl, site_lnl, s); });
+  return e == cudaSuccess ? TT_OK : wcuda(e, "wide-state post-order launch");
+}
+
+int wide_gradient(tt_plan *p, const double *props, const double *freqs, double *grad_matrices,
+                  double *grad_frequencies, double *grad_weights, cudaStream_t s) {
+  cudaError_t e = dispatch(p, [&](auto X) { return decltype(X)::backward(p, props, freqs, s); });
+  if (e != cudaSuccess) return wcuda(e, "wide-state adjoint launch");
+  const size_t kss = size_t(p->K) * p->S * p->S;
+  if (grad_matrices)
+    e = cudaMemcpyAsync(grad_matrices, p->d_G, size_t(p->batch) * p->B * kss * sizeof(double),
+                        cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess && grad_frequencies)
+    e = cudaMemcpyAsync(grad_frequencies, p->d_rootgrad, size_t(p->batch) * p->S * sizeof(double),
+                        cudaMemcpyDeviceToDevice, s);
+  if (e == cudaSuccess && grad_weights)
+    e = cudaMemcpyAsync(grad_weights, p->d_rootgrad + size_t(p->batch) * p->S,
+                        size_t(p->batch) * p->K * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  return e == cudaSuccess ? TT_OK : wcuda(e, "gradient copy");
+}
+
+int wide_matrices_gradient(tt_plan *p, const double *lam, const double *U, const double *W, const double *bl,
+                           const double *rates, double *dlam, double *dU, double *dW, double *dbl, double *drates,
+                           cudaStream_t s) {
+  cudaError_t e = dispatch(p, [&](auto X) {
+    return decltype(X)::pmatrix_backward(p, lam, U, W, bl, rates, dlam, dU, dW, dbl, drates, s);
+  });
+  return e == cudaSuccess ? TT_OK : wcuda(e, "transition-matrix gradient launch");
+}
+
+}  // namespace tt

@@ -127,9 +127,46 @@ class General(DataType):
         return self.alias.get(chr(byte), self.state_count)
 
 
+class Codon(DataType):
+    """Codons of one genetic code (datatype.py:180-297): a site is three
+    bytes; the state is 16*n1 + 4*n2 + n3 over A,C,G,T(U) minus the stop
+    codons before it; any other byte in the triplet makes the codon unknown
+    (all states, tip-state code ``state_count``).  Ambiguity flags are ignored,
+    as in the reference, and a stop codon takes the code of the sense codon
+    before it (the reference subtracts the stop count including itself)."""
+
+    name = "codon"
+    size = 3
+    UNIVERSAL = "KNKNTTTTRSRSIIMIQHQHPPPPRRRRLLLLEDEDAAAAGGGGVVVV*Y*YSSSS*CWCLFLF"
+
+    def __init__(self, table: str = UNIVERSAL):
+        self.table = table
+        stops = np.array([c == "*" for c in table[:64]], dtype=np.int64)
+        self.state_count = int(64 - stops.sum())
+        self._shift = np.cumsum(stops)
+        nuc = np.full(256, 4, dtype=np.int64)
+        for ch, v in (("A", 0), ("C", 1), ("G", 2), ("T", 3), ("U", 3)):
+            nuc[ord(ch)] = nuc[ord(ch.lower())] = v
+        self._nuc = nuc
+
+    def triplet_codes(self, b1: np.ndarray, b2: np.ndarray, b3: np.ndarray) -> np.ndarray:
+        """Codes (0..S-1, or S for unknown/stop) of byte triplets."""
+        n1, n2, n3 = self._nuc[b1], self._nuc[b2], self._nuc[b3]
+        ok = (n1 < 4) & (n2 < 4) & (n3 < 4)
+        idx = np.where(ok, n1 * 16 + n2 * 4 + n3, 0)
+        code = idx - self._shift[idx]  # a stop codon lands on the sense codon before it, as in the reference
+        return np.where(ok, code, self.state_count)
+
+    def table_rows(self) -> np.ndarray:
+        S = self.state_count
+        return np.vstack([np.eye(S), np.ones((1, S))])
+
+
 def get(name: str) -> DataType:
     if name in ("nucleotide", "dna"):
         return Nucleotide()
     if name in ("amino_acid", "protein", "aa"):
         return AminoAcid()
+    if name in ("codon", "codon_universal"):
+        return Codon()
     raise ValueError(f"unknown data type {name!r}")

@@ -137,6 +137,8 @@ class LikelihoodEngine:
         dpi = torch.empty(self.batch, self.state_count, dtype=torch.float64, device=self.device)
         dc = torch.empty(self.batch, self.category_count, dtype=torch.float64, device=self.device)
         check(self.lib.tt_gradient(self._plan, ptr(p), ptr(f), ptr(dP), ptr(dpi), ptr(dc), _stream()))
+        if self.state_count != 4:  # the wide-state adjoint consumes the stored partials
+            self.token += 1
         return dP, dpi, dc
 
     def eigen_gradient(self, lam, u, w, branch_lengths, rates):

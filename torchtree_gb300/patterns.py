@@ -80,8 +80,10 @@ def compress(sequences, data_type: DataType | None = None, use_ambiguities: bool
     encodings.  Only single-character alphabets are handled here.
     """
     data_type = data_type or Nucleotide()
+    if data_type.size == 3:
+        return _compress_codons(sequences, data_type, indices)
     if data_type.size != 1:
-        raise ValueError("multi-character data types are compressed by the codon packer")
+        raise ValueError("only single-character and codon data types are supported")
     matrix = select_sites(as_byte_matrix(sequences), indices)
     cols, weights = unique_columns(matrix)
     table, lut = data_type.byte_luts(use_ambiguities, tip_states)
@@ -94,6 +96,23 @@ def compress(sequences, data_type: DataType | None = None, use_ambiguities: bool
         table = table[used]
         codes = remap[codes]
     return CompressedAlignment(codes=np.ascontiguousarray(codes), table=table, weights=weights,
+                               columns=cols)
+
+
+def _compress_codons(sequences, data_type, indices=None) -> CompressedAlignment:
+    """Codon sites (site_pattern.py:77-82): a column is the per-taxon tuple of
+    triplets, ordered lexicographically like the reference's sorted tuples,
+    i.e. by the interleaved bytes (taxon 0 positions 1-3, taxon 1, ...)."""
+    raw = as_byte_matrix(sequences)
+    T, L = raw.shape
+    if L % 3:
+        raise ValueError("codon sequences must have a multiple of 3 characters")
+    trip = raw.reshape(T, L // 3, 3)
+    trip = select_sites(np.ascontiguousarray(np.transpose(trip, (0, 2, 1)).reshape(T * 3, L // 3)), indices)
+    cols, weights = unique_columns(trip)
+    c3 = cols.reshape(T, 3, -1)
+    codes = data_type.triplet_codes(c3[:, 0], c3[:, 1], c3[:, 2]).astype(np.uint8)
+    return CompressedAlignment(codes=np.ascontiguousarray(codes), table=data_type.table_rows(), weights=weights,
                                columns=cols)
 
 

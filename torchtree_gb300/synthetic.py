@@ -134,11 +134,14 @@ def discrete_weibull_np(shape: float, k: int) -> np.ndarray:
 
 @dataclass
 class DnaWorkload:
-    """A simulated DNA data set plus per-sample likelihood inputs.
+    """A simulated data set plus per-sample likelihood inputs.
 
     ``branch_lengths [b, 2T-3]`` are the unrooted tree's free lengths
-    (the engine appends the zero branch of node 2T-3); ``exch [b,6]``,
-    ``pi [b,4]``, ``shape [b,1]``.
+    (the engine appends the zero branch of node 2T-3); ``pi [b,S]``,
+    ``shape [b,1]``; ``exch`` holds the model's rate parameters: GTR
+    ``[b,6]`` exchangeabilities, HKY ``[b,6]`` with kappa at the transitions,
+    general ``[b,S(S-1)/2]`` upper-triangle exchangeabilities, MG94 ``[b,2]``
+    = (kappa, omega) with alpha = 1.
     """
 
     name: str
@@ -151,7 +154,12 @@ class DnaWorkload:
     shape: np.ndarray
     categories: int
     site_model: str  # "weibull" | "gamma"
-    model: str       # "gtr" | "hky"
+    model: str       # "gtr" | "hky" | "general" | "mg94"
+    data_type: str = "nucleotide"  # "nucleotide" | "amino_acid" | "codon"
+
+    @property
+    def state_count(self) -> int:
+        return self.pi.shape[-1]
 
 
 def dna_workload(name: str, tip_count: int, site_count: int, batch: int, seed: int,
@@ -195,6 +203,87 @@ def dna_workload(name: str, tip_count: int, site_count: int, batch: int, seed: i
                        site_model=site_model, model=model)
 
 
+AMINO_ACIDS = "ACDEFGHIKLMNPQRSTVWY"
+
+
+def protein_workload(name: str, tip_count: int, site_count: int, batch: int, seed: int,
+                     site_model: str = "gamma", shape: float = 0.5, categories: int = 4,
+                     branch_mean: float = 0.05, branch_jitter: float = 0.1) -> DnaWorkload:
+    """20-state amino-acid workload: exchangeabilities ~ Gamma(shape 1, scale 1)
+    (190, upper triangle row-major), frequencies ~ Dirichlet(1^20), Yule tree,
+    Exponential(mean ``branch_mean``) branches."""
+    rng = np.random.default_rng(seed)
+    topo = yule_topology(tip_count, rng)
+    B = 2 * tip_count - 2
+    bl0 = exp_branch_lengths(B - 1, branch_mean, rng)
+    exch = rng.gamma(1.0, 1.0, 190)
+    pi = rng.dirichlet(np.ones(20))
+    rates = discrete_weibull_np(shape, categories) if site_model == "weibull" else \
+        discrete_gamma_np(shape, categories)
+    q = normalised_q_np(general_q_np(exch, pi), pi)
+    seqs = simulate_alignment(topo, np.concatenate([bl0, [0.0]]), q, pi, rates, np.full(categories, 1.0 / categories),
+                              site_count, rng, alphabet=AMINO_ACIDS)
+    jitter = np.ones((batch, B - 1))
+    if batch > 1:
+        jitter[1:] = rng.lognormal(0.0, branch_jitter, size=(batch - 1, B - 1))
+    return DnaWorkload(name=name, seed=seed, topology=topo, sequences=seqs, branch_lengths=bl0[None, :] * jitter,
+                       exch=np.repeat(exch[None, :], batch, 0), pi=np.repeat(pi[None, :], batch, 0),
+                       shape=np.full((batch, 1), shape), categories=categories, site_model=site_model,
+                       model="general", data_type="amino_acid")
+
+
+def sense_codons(table: str = "KNKNTTTTRSRSIIMIQHQHPPPPRRRRLLLLEDEDAAAAGGGGVVVV*Y*YSSSS*CWCLFLF"):
+    trip = ["".join(t) for t in __import__("itertools").product("ACGT", repeat=3)]
+    return [t for t, a in zip(trip, table) if a != "*"]
+
+
+def f3x4_np(pos_freqs: np.ndarray) -> np.ndarray:
+    """Codon frequencies from per-position nucleotide frequencies [3,4] (sense codons, normalised)."""
+    idx = {"A": 0, "C": 1, "G": 2, "T": 3}
+    f = np.array([np.prod([pos_freqs[p, idx[c[p]]] for p in range(3)]) for c in sense_codons()])
+    return f / f.sum()
+
+
+def mg94_q_np(kappa: float, omega: float, pi: np.ndarray) -> np.ndarray:
+    import torch
+
+    from .substitution import mg94_q
+
+    q = mg94_q(torch.tensor(1.0, dtype=torch.float64), torch.tensor(omega, dtype=torch.float64),
+               torch.tensor(kappa, dtype=torch.float64), torch.tensor(pi, dtype=torch.float64))
+    return q.numpy()
+
+
+def codon_workload(name: str, tip_count: int, site_count: int, batch: int, seed: int,
+                   site_model: str = "gamma", shape: float = 0.5, categories: int = 4,
+                   branch_mean: float = 0.05, branch_jitter: float = 0.1) -> DnaWorkload:
+    """61-state codon workload (MG94 with alpha = 1, beta = omega): omega ~
+    Gamma(shape 2, scale 0.25), kappa ~ LogNormal(1, 0.5) (log scale), F3x4
+    frequencies from per-position Dirichlet(1^4); ``site_count`` codons."""
+    rng = np.random.default_rng(seed)
+    topo = yule_topology(tip_count, rng)
+    B = 2 * tip_count - 2
+    bl0 = exp_branch_lengths(B - 1, branch_mean, rng)
+    omega = rng.gamma(2.0, 0.25)
+    kappa = rng.lognormal(1.0, 0.5)
+    pi = f3x4_np(rng.dirichlet(np.ones(4), size=3))
+    rates = discrete_weibull_np(shape, categories) if site_model == "weibull" else \
+        discrete_gamma_np(shape, categories)
+    q = normalised_q_np(mg94_q_np(kappa, omega, pi), pi)
+    letters = "".join(chr(48 + i) for i in range(61))
+    states = simulate_alignment(topo, np.concatenate([bl0, [0.0]]), q, pi, rates,
+                                np.full(categories, 1.0 / categories), site_count, rng, alphabet=letters)
+    codons = sense_codons()
+    seqs = ["".join(codons[ord(ch) - 48] for ch in s) for s in states]
+    jitter = np.ones((batch, B - 1))
+    if batch > 1:
+        jitter[1:] = rng.lognormal(0.0, branch_jitter, size=(batch - 1, B - 1))
+    return DnaWorkload(name=name, seed=seed, topology=topo, sequences=seqs, branch_lengths=bl0[None, :] * jitter,
+                       exch=np.repeat(np.array([[kappa, omega]]), batch, 0), pi=np.repeat(pi[None, :], batch, 0),
+                       shape=np.full((batch, 1), shape), categories=categories, site_model=site_model,
+                       model="mg94", data_type="codon")
+
+
 # The workloads of the benchmark configurations (sizes and distributions
 # as stated there).
 CONFIGS = {
@@ -207,7 +296,20 @@ CONFIGS = {
 }
 
 
+WIDE_CONFIGS = {
+    "codon_g4_t200_b16": (codon_workload, dict(tip_count=200, site_count=3000, batch=16, seed=4,
+                                               site_model="gamma", shape=0.5)),
+    "protein_g4_t200_b4": (protein_workload, dict(tip_count=200, site_count=5000, batch=4, seed=5,
+                                                  site_model="gamma", shape=0.5)),
+}
+
+
 def named_workload(name: str, **overrides) -> DnaWorkload:
+    if name in WIDE_CONFIGS:
+        fn, kw = WIDE_CONFIGS[name]
+        kw = dict(kw)
+        kw.update(overrides)
+        return fn(name, **kw)
     kw = dict(CONFIGS[name])
     kw.update(overrides)
     return dna_workload(name, **kw)
