@@ -1,0 +1,104 @@
+"""GPU checks of the amino-acid / codon (wide-state) path beyond the golden cases.
+
+* the tensor-core codon post-order (split-TF32 tcgen05) equals the CUDA-core
+  kernel within FP32 rounding;
+* a batch member equals its own evaluation, rescaled equals unscaled (FP64);
+* FP32 against FP64 on a larger codon problem (lnL within 1e-6 relative).
+"""
+import os
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module", autouse=True)
+def _need_gpu():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from torchtree_gb300 import _native
+
+    _native.load()
+
+
+def _setup(wl):
+    from torchtree_gb300 import datatype, patterns, site_models, substitution
+
+    dt = datatype.get(wl.data_type)
+    ca = patterns.compress(wl.sequences, dt)
+    b, K, S = wl.branch_lengths.shape[0], wl.categories, dt.state_count
+    pi = torch.tensor(wl.pi, dtype=torch.float64)
+    ex = torch.tensor(wl.exch, dtype=torch.float64)
+    if wl.model == "mg94":
+        q = substitution.mg94_q(torch.ones_like(ex[:, :1]), ex[:, 1:2], ex[:, :1], pi)
+    else:
+        q = substitution.general_symmetric_q(ex, pi, S)
+    dev = torch.device("cuda")
+    lam, u, w = (t.to(dev).contiguous() for t in substitution.eigen_system(q, pi))
+    rates, probs = site_models.gamma_rates(torch.tensor(wl.shape, dtype=torch.float64), K)
+    bls = torch.cat([torch.tensor(wl.branch_lengths), torch.zeros(b, 1, dtype=torch.float64)], -1)
+    return ca, S, K, b, [lam, u, w, bls.to(dev).contiguous(), rates.to(dev).contiguous()], \
+        probs.expand(b, K).to(dev).contiguous(), pi.to(dev)
+
+
+def _run(wl, precision, tc=True, rescale=True, grads=True):
+    from torchtree_gb300.engine import LikelihoodEngine
+
+    ca, S, K, b, eig, probs, pi = _setup(wl)
+    old = os.environ.get("TT_WIDE_TC")
+    os.environ["TT_WIDE_TC"] = "1" if tc else "0"
+    try:
+        eng = LikelihoodEngine(wl.topology.postorder, wl.topology.tip_count, S, K, ca.codes, ca.table, ca.weights,
+                               batch=b, precision=precision)
+    finally:
+        if old is None:
+            del os.environ["TT_WIDE_TC"]
+        else:
+            os.environ["TT_WIDE_TC"] = old
+    eng.set_eigen(*eig)
+    lnl = eng.log_likelihood(probs, pi, rescale=rescale, keep_partials=grads)
+    out = {"lnl": lnl.cpu().numpy()}
+    if grads:
+        _, dpi, dc = eng.gradient(probs, pi)
+        dlam, du, dw, dt, dr = eng.eigen_gradient(*eig)
+        out.update(dpi=dpi.cpu().numpy(), dt=dt.cpu().numpy())
+    assert eng.device_status() == 0
+    return out
+
+
+def test_codon_tensor_core_matches_cuda_core():
+    from torchtree_gb300 import synthetic
+
+    wl = synthetic.codon_workload("c", tip_count=40, site_count=400, batch=2, seed=31, shape=0.5)
+    a = _run(wl, "f32", tc=True)
+    c = _run(wl, "f32", tc=False)
+    np.testing.assert_allclose(a["lnl"], c["lnl"], rtol=1e-6)  # split-TF32 products, FP32 tensor accumulation
+    np.testing.assert_allclose(a["dt"], c["dt"], rtol=1e-4, atol=1e-4 * np.abs(c["dt"]).max())
+
+
+def test_codon_fp32_against_fp64():
+    from torchtree_gb300 import synthetic
+
+    wl = synthetic.codon_workload("c", tip_count=60, site_count=600, batch=2, seed=32, shape=0.5)
+    a = _run(wl, "f32")
+    d = _run(wl, "f64")
+    np.testing.assert_allclose(a["lnl"], d["lnl"], rtol=1e-6)
+    np.testing.assert_allclose(a["dt"], d["dt"], rtol=1e-3, atol=1e-3 * np.abs(d["dt"]).max())
+
+
+def test_protein_batch_member_and_rescaling():
+    from torchtree_gb300 import synthetic
+
+    wl = synthetic.protein_workload("p", tip_count=50, site_count=800, batch=3, seed=33, shape=0.5)
+    full = _run(wl, "f64")
+    single = synthetic.protein_workload("p", tip_count=50, site_count=800, batch=3, seed=33, shape=0.5)
+    single.branch_lengths = single.branch_lengths[1:2]
+    single.exch, single.pi, single.shape = single.exch[1:2], single.pi[1:2], single.shape[1:2]
+    one = _run(single, "f64")
+    assert one["lnl"][0] == full["lnl"][1]
+    unscaled = _run(wl, "f64", rescale=False, grads=False)
+    np.testing.assert_allclose(unscaled["lnl"], full["lnl"], rtol=1e-13)
+    f32 = _run(wl, "f32")
+    np.testing.assert_allclose(f32["lnl"], full["lnl"], rtol=1e-6)

@@ -1,13 +1,16 @@
 // Host side of the wide-state path (S != 4: amino acids, codons): level
 // schedule, workspace and launch sequences behind the C entry points.
 #include <algorithm>
+#include <cstdlib>
 #include <cstring>
+#include <type_traits>
 #include <string>
 #include <vector>
 
 #include "../../include/torchtree_gb300.h"
 #include "tt_plan.h"
 #include "tt_wide.cuh"
+#include "tt_wide_tc.cuh"
 
 namespace tt {
 
@@ -63,6 +66,7 @@ __global__ void wide_pmatrix_grad_reduce_kernel(const double *part, int nchunks,
 struct WideState {
   int SP = 0, PTf = 0, PTb = 0, Npad = 0, ntiles_f = 0, ntiles_b = 0, nchunks = 1, tpc = 1, nblk = 0;
   int bchunk = 8, nbchunks = 1;
+  bool tc = false;  // FP32 codon post-order on the tensor cores
   std::vector<int> fwd_off, bwd_off;  // level boundaries in d_fwd / d_bwd
   int *d_left = nullptr, *d_right = nullptr, *d_fwd = nullptr, *d_bwd = nullptr;
   void *d_part = nullptr;
@@ -115,6 +119,8 @@ struct Wide {
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(wide_backward_kernel<T, SP, PTB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                int(wide_bwd_smem<T, SP, PTB>()));
+    if (std::is_same<T, float>::value && SP == 64 && e == cudaSuccess)
+      e = cudaFuncSetAttribute(wide_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::kSmem);
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(wide_pmatrix_kernel<T, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                int(2 * SP * SP * sizeof(T) + SP * sizeof(double)));
@@ -167,6 +173,14 @@ struct Wide {
     const size_t smem = wide_fwd_smem<T, SP, PTF>();
     for (size_t lv = 0; lv + 1 < w.fwd_off.size(); ++lv) {
       a.nodes = w.d_fwd + w.fwd_off[lv];
+      if constexpr (std::is_same<T, float>::value && SP == 64) {
+        if (w.tc) {
+          const dim3 grid(w.Npad / tc::kPT, w.fwd_off[lv + 1] - w.fwd_off[lv], p->batch * p->K);
+          wide_forward_tc_kernel<<<grid, tc::kThreads, tc::kSmem, s>>>(a, p->d_status, 2000000000ull);
+          p->launches += 1;
+          continue;
+        }
+      }
       const dim3 grid(w.ntiles_f, w.fwd_off[lv + 1] - w.fwd_off[lv], p->batch * p->K);
       wide_forward_kernel<T, SP, PTF><<<grid, NT, smem, s>>>(a);
       p->launches += 1;
@@ -252,6 +266,10 @@ int wide_create(tt_plan *p) {
     w->nchunks = (w->ntiles_b + w->tpc - 1) / w->tpc;
   }
   w->nbchunks = (p->B + w->bchunk - 1) / w->bchunk;
+  {  // tensor-core post-order for FP32 codon plans (TT_WIDE_TC=0 selects the CUDA-core kernel)
+    const char *env = getenv("TT_WIDE_TC");
+    w->tc = f32 && w->SP == 64 && !(env && atoi(env) == 0);
+  }
   p->code_stride = w->Npad;
 
   // children, levels by height (forward) and by depth (adjoint); the postorder
