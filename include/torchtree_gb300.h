@@ -195,6 +195,20 @@ int tt_log_likelihood_static(int32_t tip_count, const int32_t *postorder,
 /* Number of kernel launches the plan issued since creation. */
 int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
 
+/*
+ * Kernel-shape options of a plan, for autotuning (no reference counterpart:
+ * the reference has no kernels to shape).  Results do not depend on them.
+ *   TT_OPT_FWD_STAGES / TT_OPT_BWD_STAGES: staging-ring depth of the FP32
+ *     4-state post-order / adjoint kernels (2..8; rejected when the ring
+ *     does not fit in shared memory);
+ *   TT_OPT_TENSOR_CORES: 1 = FP32 codon post-order on the tensor cores,
+ *     0 = CUDA-core kernel.
+ * tt_plan_get_option reads the value in use.
+ */
+enum { TT_OPT_FWD_STAGES = 1, TT_OPT_BWD_STAGES = 2, TT_OPT_TENSOR_CORES = 3 };
+int tt_plan_set_option(tt_plan *plan, int32_t option, int32_t value);
+int tt_plan_get_option(const tt_plan *plan, int32_t option, int32_t *value);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,171 @@
+"""Serving loop: continuous batching, admission by HBM footprint, and results
+that are the same alone and in a mix.
+
+The scheduler tests run on the CPU with stand-in executors; the end-to-end
+test (``gpu``) serves three resident data sets (two DNA, one amino-acid)
+through captured CUDA graphs.
+"""
+import threading
+import time
+
+import numpy as np
+import pytest
+
+from torchtree_gb300 import serving
+
+
+class FakeExecutor:
+    """Stands in for a GraphExecutor: a batch completes when the test says so."""
+
+    def __init__(self, ds, footprint, log):
+        self.ds, self.footprint, self.log = ds, footprint, log
+        self.busy, self.batch, self.release = False, None, False
+        self.last_used = time.perf_counter()
+        self.closed = False
+
+    def launch(self, reqs):
+        self.busy, self.batch, self.release = True, reqs, False
+        self.log.append((self.ds.name, [r.params["i"] for r in reqs]))
+
+    def poll(self):
+        if not self.busy or not self.release:
+            return None
+        done = [(r, {"lnl": -float(r.params["i"])}, None) for r in self.batch]
+        self.batch, self.busy = None, False
+        self.last_used = time.perf_counter()
+        return done
+
+    def close(self):
+        self.closed = True
+
+
+def _server(budget, slots, sizes):
+    log, made = [], {}
+
+    def factory(ds):
+        ex = FakeExecutor(ds, sizes[ds.name], log)
+        made[ds.name] = ex
+        return ex
+
+    srv = serving.LikelihoodServer(slots=slots, hbm_budget=budget, executor_factory=factory, device="cpu")
+    srv.estimate = lambda ds: sizes[ds.name]
+    for name in sizes:
+        srv.add_dataset(name, None, None, 4, serving.ModelSpec("gtr"))
+    return srv, log, made
+
+
+def test_continuous_batching_admits_arrivals_after_the_batch_in_flight():
+    srv, log, made = _server(budget=100, slots=4, sizes={"a": 10})
+    futs = [srv.submit("a", {"i": i}) for i in range(3)]
+    srv.step()
+    assert log == [("a", [0, 1, 2])]
+    futs += [srv.submit("a", {"i": i}) for i in range(3, 9)]  # arrive while the batch is on the GPU
+    srv.step()
+    assert len(log) == 1  # one batch per data set in flight
+    made["a"].release = True
+    srv.step()  # completes the first batch and launches the next four waiting requests
+    assert log[1] == ("a", [3, 4, 5, 6])
+    made["a"].release = True
+    srv.step()
+    assert log[2] == ("a", [7, 8])
+    made["a"].release = True
+    srv.step()
+    assert [f.result(timeout=1)["lnl"] for f in futs] == [-float(i) for i in range(9)]
+    assert srv.latency_stats()["count"] == 9
+
+
+def test_admission_by_footprint_waits_and_evicts_idle_plans():
+    srv, log, made = _server(budget=100, slots=2, sizes={"a": 60, "b": 60, "c": 30})
+    fa = srv.submit("a", {"i": 0})
+    fb = srv.submit("b", {"i": 1})
+    fc = srv.submit("c", {"i": 2})
+    srv.step()
+    # a (60) and c (30) fit together; b (60) must wait for memory
+    assert [name for name, _ in log] == ["a", "c"]
+    assert "b" not in made and srv.used == 90
+    made["a"].release = True
+    made["c"].release = True
+    srv.step()  # a and c complete; both idle -> the least recently used is evicted for b
+    assert "b" in made and made["a"].closed and srv.evictions == 1
+    made["b"].release = True
+    srv.step()
+    assert fa.result(timeout=1)["lnl"] == 0.0 and fb.result(timeout=1)["lnl"] == -1.0
+    assert fc.result(timeout=1)["lnl"] == -2.0
+    assert srv.used <= srv.budget
+
+
+def test_request_for_unknown_dataset_is_rejected():
+    srv, _, _ = _server(budget=100, slots=2, sizes={"a": 10})
+    with pytest.raises(KeyError):
+        srv.submit("zzz", {"i": 0})
+
+
+# ------------------------------------------------------------------ GPU
+def _datasets():
+    from torchtree_gb300 import datatype, patterns, synthetic
+
+    out = {}
+    w1 = synthetic.dna_workload("d1", tip_count=20, site_count=300, batch=6, seed=41, model="gtr",
+                                site_model="gamma", shape=0.5, branch_mean=0.05)
+    w2 = synthetic.dna_workload("d2", tip_count=33, site_count=200, batch=6, seed=42, model="hky",
+                                site_model="weibull", shape=0.8, branch_mean=0.05)
+    w3 = synthetic.protein_workload("p1", tip_count=15, site_count=120, batch=6, seed=43, site_model="gamma",
+                                    shape=0.5)
+    for name, w, spec, dt in (("d1", w1, serving.ModelSpec("gtr"), datatype.Nucleotide()),
+                              ("d2", w2, serving.ModelSpec("gtr", site_model="weibull"), datatype.Nucleotide()),
+                              ("p1", w3, serving.ModelSpec("general"), datatype.AminoAcid())):
+        ca = patterns.compress(w.sequences, dt)
+        reqs = [{"branch_lengths": w.branch_lengths[i], "exch": w.exch[i], "pi": w.pi[i], "shape": w.shape[i]}
+                for i in range(w.branch_lengths.shape[0])]
+        out[name] = (w.topology, ca, dt.state_count, spec, reqs)
+    return out
+
+
+@pytest.mark.gpu
+def test_results_same_alone_and_in_the_mix():
+    import torch
+
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    data = _datasets()
+
+    def make():
+        srv = serving.LikelihoodServer(slots=4, precision="f32")
+        for name, (topo, ca, S, spec, _) in data.items():
+            srv.add_dataset(name, topo, ca, S, spec)
+        return srv.start()
+
+    alone = {}
+    srv = make()
+    for name, (_, _, _, _, reqs) in data.items():
+        for i, p in enumerate(reqs):
+            alone[(name, i)] = srv.submit(name, p).result(timeout=300)
+    srv.stop()
+
+    srv = make()
+    futs = {}
+    rng = np.random.default_rng(0)
+    keys = [(name, i) for name, d in data.items() for i in range(len(d[4]))]
+    order = rng.permutation(len(keys))
+
+    def chain(idx):
+        for j in idx:
+            name, i = keys[j]
+            time.sleep(float(rng.uniform(0, 0.002)))
+            futs[(name, i)] = srv.submit(name, data[name][4][i])
+
+    threads = [threading.Thread(target=chain, args=(order[t::4],)) for t in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    mixed = {k: f.result(timeout=300) for k, f in futs.items()}
+    stats = srv.latency_stats()
+    srv.stop()
+    assert stats["count"] == len(keys) and stats["p99_ms"] >= stats["p50_ms"] > 0
+    for k in keys:
+        a, b = alone[k], mixed[k]
+        assert np.isfinite(a["lnl"])
+        np.testing.assert_allclose(b["lnl"], a["lnl"], rtol=1e-12, err_msg=str(k))
+        for g in ("grad_branch_lengths", "grad_exch", "grad_pi", "grad_shape"):
+            np.testing.assert_allclose(b[g], a[g], rtol=1e-12, atol=1e-12 * np.abs(a[g]).max(), err_msg=f"{k} {g}")

@@ -26,6 +26,8 @@ _I32 = ctypes.c_int32
 _PI32 = ctypes.POINTER(ctypes.c_int32)
 
 # name -> (restype, argtypes); every symbol the header declares
+TT_OPT_FWD_STAGES, TT_OPT_BWD_STAGES, TT_OPT_TENSOR_CORES = 1, 2, 3
+
 SIGNATURES = {
     "tt_version": (ctypes.c_char_p, []),
     "tt_last_error": (ctypes.c_char_p, []),
@@ -41,6 +43,8 @@ SIGNATURES = {
     "tt_plan_device_status": (ctypes.c_int, [_P, _P, _PI32, _I32]),
     "tt_plan_launch_count": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
     "tt_schedule": (ctypes.c_int, [_I32, _PI32, _PI32, _PI32]),
+    "tt_plan_set_option": (ctypes.c_int, [_P, _I32, _I32]),
+    "tt_plan_get_option": (ctypes.c_int, [_P, _I32, _PI32]),
     "tt_log_likelihood_static": (ctypes.c_int, [_I32, _PI32, _I32, _I32, _I32, _I32, _P, _P, _I32, _P, _P, _P,
                                                 _P, _I32, _P, _P]),
 }

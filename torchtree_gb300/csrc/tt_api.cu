@@ -630,6 +630,39 @@ int tt_schedule(int32_t tip_count, const int32_t *postorder, int32_t *steps, int
   return TT_OK;
 }
 
+int tt_plan_set_option(tt_plan *p, int32_t option, int32_t value) {
+  if (!p) return fail(TT_ERR_INVALID_ARGUMENT, "NULL plan");
+  switch (option) {
+    case TT_OPT_FWD_STAGES:
+    case TT_OPT_BWD_STAGES: {
+      if (p->wide || p->precision != TT_PRECISION_F32)
+        return fail(TT_ERR_UNSUPPORTED, "ring depths apply to FP32 4-state plans");
+      if (value < 2 || value > 8) return fail(TT_ERR_INVALID_ARGUMENT, "ring depth must be in [2, 8]");
+      const bool bwd = option == TT_OPT_BWD_STAGES;
+      int smem_max = 0;
+      cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
+      if (tt::tl_smem_bytes(p->K, 256, bwd ? p->slots_bwd : p->slots_fwd, bwd, value) > size_t(smem_max))
+        return fail(TT_ERR_UNSUPPORTED, "ring does not fit in shared memory");
+      (bwd ? p->nstage_b : p->nstage_f) = value;
+      return TT_OK;
+    }
+    case TT_OPT_TENSOR_CORES:
+      return tt::wide_set_tensor_cores(p, value != 0);
+    default:
+      return fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
+  }
+}
+
+int tt_plan_get_option(const tt_plan *p, int32_t option, int32_t *value) {
+  if (!p || !value) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  switch (option) {
+    case TT_OPT_FWD_STAGES: *value = p->nstage_f; return TT_OK;
+    case TT_OPT_BWD_STAGES: *value = p->nstage_b; return TT_OK;
+    case TT_OPT_TENSOR_CORES: *value = tt::wide_tensor_cores(p) ? 1 : 0; return TT_OK;
+    default: return fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
+  }
+}
+
 int tt_plan_launch_count(const tt_plan *p, int64_t *count) {
   if (!p || !count) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
   *count = p->launches;

@@ -58,4 +58,6 @@ int wide_gradient(tt_plan *p, const double *props, const double *freqs, double *
 int wide_matrices_gradient(tt_plan *p, const double *lam, const double *U, const double *W, const double *bl,
                            const double *rates, double *dlam, double *dU, double *dW, double *dbl,
                            double *drates, cudaStream_t s);
+int wide_set_tensor_cores(tt_plan *p, bool on);
+bool wide_tensor_cores(const tt_plan *p);
 }  // namespace tt

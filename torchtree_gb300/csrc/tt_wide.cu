@@ -343,6 +343,15 @@ int wide_create(tt_plan *p) {
   return TT_OK;
 }
 
+int wide_set_tensor_cores(tt_plan *p, bool on) {
+  if (!p->wide || p->precision != TT_PRECISION_F32 || p->wide->SP != 64)
+    return on ? wfail(TT_ERR_UNSUPPORTED, "the tensor-core post-order serves FP32 codon (> 20-state) plans") : TT_OK;
+  p->wide->tc = on;
+  return TT_OK;
+}
+
+bool wide_tensor_cores(const tt_plan *p) { return p->wide && p->wide->tc; }
+
 void wide_destroy(tt_plan *p) {
   WideState *w = p->wide;
   if (!w) return;

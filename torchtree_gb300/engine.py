@@ -87,6 +87,15 @@ class LikelihoodEngine:
         check(self.lib.tt_plan_launch_count(self._plan, ctypes.byref(n)))
         return int(n.value)
 
+    def set_option(self, option: int, value: int) -> None:
+        """Kernel-shape option (``_native.TT_OPT_*``); results do not depend on it."""
+        check(self.lib.tt_plan_set_option(self._plan, int(option), int(value)))
+
+    def get_option(self, option: int) -> int:
+        v = ctypes.c_int32()
+        check(self.lib.tt_plan_get_option(self._plan, int(option), ctypes.byref(v)))
+        return int(v.value)
+
     def device_status(self, reset: bool = True) -> int:
         s = ctypes.c_int32()
         check(self.lib.tt_plan_device_status(self._plan, _stream(), ctypes.byref(s), int(reset)))

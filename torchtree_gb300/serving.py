@@ -1,0 +1,370 @@
+"""Continuous-batching likelihood server.
+
+Many concurrent samplers (HMC / ADVI chains) send lnL + gradient requests for
+a set of resident data sets (tree topology + compressed alignment + model
+family).  The server keeps each admitted data set's tip codes, pattern
+weights and workspace resident in one plan with ``slots`` batch slots, and
+runs its step -- transition matrices, post-order, adjoint, matrix-gradient
+chain -- as one captured CUDA graph on the data set's own stream:
+
+* continuous batching: a scheduler thread launches a data set's waiting
+  requests (up to ``slots``) as soon as its previous batch has left the GPU;
+  requests that arrive while a batch is in flight wait only for that batch,
+  and batches of different data sets run concurrently on their streams;
+* admission by HBM footprint: a data set's plan is created only when its
+  workspace fits the budget, evicting idle plans (least recently used)
+  otherwise; requests of a data set that does not fit wait;
+* kernel shapes of each plan come from ``autotune.tune`` before capture;
+* every request's result (lnL and the gradient with respect to its branch
+  lengths, rate-matrix parameters, frequencies and site-model shape) is the
+  same whether it runs alone or in a mix: slots are independent and the
+  kernels are deterministic.
+
+The rate-matrix construction, its eigen system and the site model stay in
+torch on the host (FP64, autograd), as in ``PhyloLikelihood``; the graph
+receives ``(lambda, U, W)``, branch lengths, category rates and weights
+through pinned host buffers and returns the engine's gradients, which the
+host chains back to the request's parameters.
+"""
+from __future__ import annotations
+
+import queue
+import threading
+import time
+from concurrent.futures import Future
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import autotune, site_models, substitution
+from .engine import LikelihoodEngine
+from .patterns import CompressedAlignment
+from .tree import Topology
+
+
+@dataclass
+class ModelSpec:
+    """Substitution model family and site model of a data set.
+
+    ``substitution``: "gtr" (6 exchangeabilities), "hky" (kappa), "general"
+    (S(S-1)/2 exchangeabilities) or "mg94" ((kappa, omega), alpha = 1);
+    ``site_model``: "gamma" or "weibull" with ``categories`` rates.
+    """
+
+    substitution: str
+    categories: int = 4
+    site_model: str = "gamma"
+
+
+@dataclass
+class Dataset:
+    name: str
+    topology: Topology
+    alignment: CompressedAlignment
+    state_count: int
+    spec: ModelSpec
+
+
+@dataclass
+class Request:
+    dataset: str
+    params: dict
+    future: Future = field(default_factory=Future)
+    t_submit: float = 0.0
+    t_launch: float = 0.0
+    t_done: float = 0.0
+
+
+def rate_matrix(spec: ModelSpec, exch: torch.Tensor, pi: torch.Tensor, state_count: int) -> torch.Tensor:
+    if spec.substitution == "gtr":
+        return substitution.gtr_q(exch, pi)
+    if spec.substitution == "hky":
+        return substitution.hky_q(exch, pi)
+    if spec.substitution == "general":
+        return substitution.general_symmetric_q(exch, pi, state_count)
+    if spec.substitution == "mg94":
+        return substitution.mg94_q(torch.ones_like(exch[..., :1]), exch[..., 1:2], exch[..., :1], pi)
+    raise ValueError(f"unknown substitution model {spec.substitution!r}")
+
+
+def host_prepare(ds: Dataset, params: dict) -> dict:
+    """Leaf tensors and engine inputs of one request (host, FP64, autograd on)."""
+    f64 = torch.float64
+    exch = torch.tensor(np.asarray(params["exch"], dtype=np.float64), dtype=f64, requires_grad=True)
+    pi = torch.tensor(np.asarray(params["pi"], dtype=np.float64), dtype=f64, requires_grad=True)
+    shape = torch.tensor(np.asarray(params["shape"], dtype=np.float64).reshape(1), dtype=f64, requires_grad=True)
+    q = rate_matrix(ds.spec, exch, pi, ds.state_count)
+    lam, u, w = substitution.eigen_system(q, pi)
+    K = ds.spec.categories
+    if ds.spec.site_model == "gamma":
+        rates, probs = site_models.gamma_rates(shape, K)
+    else:
+        rates, probs = site_models.weibull_rates(shape, K)
+    probs = probs.expand(K)
+    bl = np.asarray(params["branch_lengths"], dtype=np.float64)
+    bls = np.concatenate([bl, [0.0]]) if bl.shape[-1] == 2 * ds.topology.tip_count - 3 else bl
+    return {"leaves": (exch, pi, shape), "lam": lam, "u": u, "w": w, "rates": rates, "probs": probs, "pi": pi,
+            "bls": torch.tensor(bls, dtype=f64), "free": bl.shape[-1]}
+
+
+def host_finish(p: dict, out: dict) -> dict:
+    """Chain the engine's gradients to the request's parameters."""
+    exch, pi, shape = p["leaves"]
+    pairs = [(p[k], out[g]) for k, g in (("lam", "dlam"), ("u", "du"), ("w", "dw"), ("rates", "dr"),
+                                          ("probs", "dc"), ("pi", "dpi")) if p[k].requires_grad]
+    torch.autograd.backward([t for t, _ in pairs], [g.to(t.dtype).reshape(t.shape) for t, g in pairs])
+    return {"lnl": float(out["lnl"]), "grad_branch_lengths": out["dt"][: p["free"]].numpy().copy(),
+            "grad_exch": exch.grad.numpy().copy(), "grad_pi": pi.grad.numpy().copy(),
+            "grad_shape": shape.grad.numpy().copy()}
+
+
+def estimate_bytes(ds: Dataset, slots: int, precision: str) -> int:
+    """Device bytes a plan for ``ds`` with ``slots`` samples will hold (upper estimate)."""
+    T, N, S, K = ds.topology.tip_count, ds.alignment.pattern_count, ds.state_count, ds.spec.categories
+    elem = 4 if precision == "f32" else 8
+    B = 2 * T - 2
+    if S == 4:
+        npad = -(-N // 64) * 64
+        kp = K + (K & 1)
+        part = slots * T * kp * npad * S * elem
+        grad = slots * B * (npad // 32) * K * S * S * elem
+        return int(1.1 * (part + grad + slots * B * kp * S * S * elem + T * npad)) + (64 << 20)
+    sp = 20 if S <= 20 else 64
+    npad = -(-N // 128) * 128
+    part = slots * T * K * npad * (sp * elem + 4)
+    chunks = min(64, max(1, -(-304 // (slots * K))))
+    grad = slots * B * K * sp * sp * (chunks * elem + elem + 8)
+    return int(1.1 * (part + grad + T * npad)) + (64 << 20)
+
+
+class GraphExecutor:
+    """One admitted data set: plan, stream, static buffers, captured step."""
+
+    def __init__(self, ds: Dataset, slots: int, precision: str, device, use_graph: bool = True,
+                 tune: bool = True):
+        self.ds = ds
+        self.slots = slots
+        self.device = device
+        T, S, K = ds.topology.tip_count, ds.state_count, ds.spec.categories
+        B = 2 * T - 2
+        self.engine = LikelihoodEngine(ds.topology.postorder, T, S, K, ds.alignment.codes, ds.alignment.table,
+                                       ds.alignment.weights, batch=slots, precision=precision, device=device)
+        kw = dict(dtype=torch.float64, device=device)
+        eye = torch.eye(S, **kw).expand(slots, S, S).contiguous()
+        self.inputs = {"lam": torch.zeros(slots, S, **kw), "u": eye.clone(), "w": eye.clone(),
+                       "bls": torch.full((slots, B), 0.1, **kw), "rates": torch.ones(slots, K, **kw),
+                       "props": torch.full((slots, K), 1.0 / K, **kw), "pi": torch.full((slots, S), 1.0 / S, **kw)}
+        self.host_in = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in self.inputs.items()}
+        self.stream = torch.cuda.Stream(device)
+        self.graph = None
+        with torch.cuda.device(device), torch.cuda.stream(self.stream):
+            if tune:
+                autotune.tune(self.engine, self._step)
+            outs = self._step()  # eager warm-up (also sets the plan's state for capture)
+            self.stream.synchronize()
+            if use_graph:
+                self.graph = torch.cuda.CUDAGraph()
+                with torch.cuda.graph(self.graph, stream=self.stream):
+                    outs = self._step()
+        self.outputs = outs
+        self.host_out = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in outs.items()}
+        self.event = torch.cuda.Event()
+        self.footprint = self.engine.workspace_bytes + sum(v.numel() * 8 for v in self.inputs.values()) * 2
+        self.busy = False
+        self.batch = None
+        self.last_used = time.perf_counter()
+
+    def _step(self) -> dict:
+        e, x = self.engine, self.inputs
+        e.set_eigen(x["lam"], x["u"], x["w"], x["bls"], x["rates"])
+        lnl = e.log_likelihood(x["props"], x["pi"], rescale=True, keep_partials=True)
+        _, dpi, dc = e.gradient(x["props"], x["pi"])
+        dlam, du, dw, dt, dr = e.eigen_gradient(x["lam"], x["u"], x["w"], x["bls"], x["rates"])
+        return {"lnl": lnl, "dpi": dpi, "dc": dc, "dlam": dlam, "du": du, "dw": dw, "dt": dt, "dr": dr}
+
+    def launch(self, reqs: list) -> None:
+        preps = [host_prepare(self.ds, r.params) for r in reqs]
+        for name, key in (("lam", "lam"), ("u", "u"), ("w", "w"), ("bls", "bls"), ("rates", "rates"),
+                          ("props", "probs"), ("pi", "pi")):
+            buf = self.host_in[name]
+            for s in range(self.slots):
+                buf[s].copy_(preps[min(s, len(preps) - 1)][key].detach())
+        now = time.perf_counter()
+        for r in reqs:
+            r.t_launch = now
+        with torch.cuda.device(self.device), torch.cuda.stream(self.stream):
+            for k, v in self.inputs.items():
+                v.copy_(self.host_in[k], non_blocking=True)
+            if self.graph is not None:
+                self.graph.replay()
+            else:
+                self.outputs = self._step()
+            for k, v in self.outputs.items():
+                self.host_out[k].copy_(v, non_blocking=True)
+            self.event.record(self.stream)
+        self.busy = True
+        self.batch = (reqs, preps)
+
+    def poll(self):
+        """``[(request, result, exception)]`` of the batch in flight once it
+        has left the GPU, else None.  The caller resolves the futures."""
+        if not self.busy or not self.event.query():
+            return None
+        reqs, preps = self.batch
+        done = []
+        for s, (r, p) in enumerate(zip(reqs, preps)):
+            out = {k: v[s] for k, v in self.host_out.items()}
+            try:
+                done.append((r, host_finish(p, out), None))
+            except Exception as exc:  # report, keep serving
+                done.append((r, None, exc))
+        self.busy = False
+        self.batch = None
+        self.last_used = time.perf_counter()
+        return done
+
+    def close(self) -> None:
+        self.graph = None
+        self.engine.close()
+
+
+class LikelihoodServer:
+    """Persistent request loop over resident data sets (see the module docstring)."""
+
+    def __init__(self, slots: int = 8, precision: str = "f32", device=None, hbm_budget: int | None = None,
+                 use_graphs: bool = True, tune: bool = True, executor_factory=None):
+        self.slots = slots
+        self.precision = precision
+        self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
+        if hbm_budget is None and executor_factory is None:
+            free, _ = torch.cuda.mem_get_info(self.device)
+            hbm_budget = int(0.85 * free)
+        self.budget = hbm_budget
+        self.factory = executor_factory or (lambda ds: GraphExecutor(ds, slots, precision, self.device,
+                                                                     use_graph=use_graphs, tune=tune))
+        self.estimate = (lambda ds: estimate_bytes(ds, slots, precision))
+        self.datasets: dict = {}
+        self.executors: dict = {}
+        self.pending: dict = {}
+        self.used = 0
+        self.completed: list = []
+        self.admissions = 0
+        self.evictions = 0
+        self.batches = 0
+        self._queue: queue.Queue = queue.Queue()
+        self._stop = threading.Event()
+        self._thread = None
+        self._error = None
+
+    # -------------------------------------------------------------- client API
+    def add_dataset(self, name: str, topology: Topology, alignment: CompressedAlignment, state_count: int,
+                    spec: ModelSpec) -> None:
+        self.datasets[name] = Dataset(name, topology, alignment, state_count, spec)
+
+    def submit(self, dataset: str, params: dict) -> Future:
+        if dataset not in self.datasets:
+            raise KeyError(f"unknown data set {dataset!r}")
+        r = Request(dataset, params, t_submit=time.perf_counter())
+        self._queue.put(r)
+        return r.future
+
+    def start(self) -> "LikelihoodServer":
+        self._stop.clear()
+        self._thread = threading.Thread(target=self._loop, name="likelihood-server", daemon=True)
+        self._thread.start()
+        return self
+
+    def stop(self) -> None:
+        self._stop.set()
+        if self._thread is not None:
+            self._thread.join()
+            self._thread = None
+        for ex in self.executors.values():
+            ex.close()
+        self.executors.clear()
+        self.used = 0
+        if self._error is not None:
+            raise self._error
+
+    def latency_stats(self) -> dict:
+        lat = np.array([r.t_done - r.t_submit for r in self.completed]) * 1e3
+        if lat.size == 0:
+            return {"count": 0}
+        return {"count": int(lat.size), "p50_ms": float(np.percentile(lat, 50)),
+                "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+                "batches": self.batches, "admissions": self.admissions, "evictions": self.evictions}
+
+    # -------------------------------------------------------------- scheduler
+    def _admit(self, name: str):
+        ds = self.datasets[name]
+        need = self.estimate(ds)
+        while self.used + need > self.budget:
+            idle = [(ex.last_used, n) for n, ex in self.executors.items() if not ex.busy and not self.pending.get(n)]
+            if not idle:
+                return None
+            _, victim = min(idle)
+            ex = self.executors.pop(victim)
+            self.used -= ex.footprint
+            ex.close()
+            self.evictions += 1
+        ex = self.factory(ds)
+        self.executors[name] = ex
+        self.used += max(ex.footprint, need)
+        self.admissions += 1
+        return ex
+
+    def step(self) -> bool:
+        """One scheduler iteration; True if anything progressed."""
+        progressed = False
+        for ex in list(self.executors.values()):
+            done = ex.poll()
+            if done is None:
+                continue
+            progressed = True
+            now = time.perf_counter()
+            for r, res, exc in done:
+                r.t_done = now
+                if exc is None:
+                    self.completed.append(r)
+                    r.future.set_result(res)
+                else:
+                    r.future.set_exception(exc)
+        while True:
+            try:
+                r = self._queue.get_nowait()
+            except queue.Empty:
+                break
+            self.pending.setdefault(r.dataset, []).append(r)
+        order = sorted((reqs[0].t_submit, n) for n, reqs in self.pending.items() if reqs)
+        for _, name in order:
+            ex = self.executors.get(name)
+            if ex is None:
+                ex = self._admit(name)
+                if ex is None:
+                    continue
+            if not ex.busy:
+                reqs = self.pending[name][: self.slots]
+                del self.pending[name][: len(reqs)]
+                ex.launch(reqs)
+                self.batches += 1
+                progressed = True
+        return progressed
+
+    def _busy(self) -> bool:
+        return any(ex.busy for ex in self.executors.values()) or any(self.pending.values()) or \
+            not self._queue.empty()
+
+    def _loop(self) -> None:
+        try:
+            if self.device.type == "cuda":
+                torch.cuda.set_device(self.device)
+            while not self._stop.is_set() or self._busy():
+                if not self.step():
+                    time.sleep(50e-6)
+        except Exception as exc:  # surface on stop(); fail the waiting requests
+            self._error = exc
+            for reqs in self.pending.values():
+                for r in reqs:
+                    if not r.future.done():
+                        r.future.set_exception(exc)
