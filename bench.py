@@ -51,6 +51,15 @@ def parse():
     ap.add_argument("--sites", type=int, default=None, help="override the workload's site count")
     ap.add_argument("--tips", type=int, default=None, help="override the workload's tip count")
     ap.add_argument("--batch", type=int, default=None, help="override the workload's batch")
+    ap.add_argument("--serving", action="store_true",
+                    help="serving mix instead of the batched step: Poisson arrivals from many chains over "
+                         "resident data sets, continuous batching through captured CUDA graphs")
+    ap.add_argument("--serving-datasets", type=int, default=32)
+    ap.add_argument("--serving-chains", type=int, default=256)
+    ap.add_argument("--serving-requests", type=int, default=1024)
+    ap.add_argument("--serving-slots", type=int, default=4)
+    ap.add_argument("--serving-max-tips", type=int, default=2000)
+    ap.add_argument("--serving-max-sites", type=int, default=50000)
     return ap.parse_args()
 
 
@@ -189,10 +198,139 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def serving_mix(args, rng):
+    """Resident data sets of the serving mix: taxa log-uniform in [20, max tips], sites
+    log-uniform in [500, max sites], 70 % DNA GTR+G4 / 30 % amino-acid general
+    symmetric + G4 (exchangeabilities ~ Gamma(1,1), frequencies ~ Dirichlet(1^20)).
+    Tip states are i.i.d. uniform (only the shapes matter for the timing), one
+    pattern per site."""
+    from torchtree_gb300 import synthetic
+    from torchtree_gb300.patterns import CompressedAlignment
+    from torchtree_gb300.serving import ModelSpec
+
+    out = []
+    for d in range(args.serving_datasets):
+        T = int(round(np.exp(rng.uniform(np.log(20), np.log(args.serving_max_tips)))))
+        N = int(round(np.exp(rng.uniform(np.log(500), np.log(args.serving_max_sites)))))
+        protein = rng.random() < 0.3
+        S = 20 if protein else 4
+        topo = synthetic.yule_topology(T, rng)
+        codes = rng.integers(0, S, size=(T, N), dtype=np.uint8)
+        ca = CompressedAlignment(codes=codes, table=np.vstack([np.eye(S), np.ones((1, S))]),
+                                 weights=np.ones(N), columns=np.zeros((T, 0), dtype=np.uint8))
+        spec = ModelSpec("general" if protein else "gtr")
+        out.append((f"ds{d}", topo, ca, S, spec))
+    return out
+
+
+def chain_params(rng, topo, S):
+    B = 2 * topo.tip_count - 3
+    exch = rng.gamma(1.0, 1.0, S * (S - 1) // 2) if S == 20 else rng.dirichlet(np.ones(6))
+    return {"branch_lengths": rng.exponential(0.05, B), "exch": exch, "pi": rng.dirichlet(np.ones(S)),
+            "shape": np.array([0.5])}
+
+
+def run_serving(args):
+    import torch
+
+    from torchtree_gb300 import serving
+    from torchtree_gb300.likelihood import PhyloLikelihood
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    rng = np.random.default_rng(7)
+    mix = serving_mix(args, rng)
+    chains = [(c % len(mix), chain_params(rng, mix[c % len(mix)][1], mix[c % len(mix)][3]))
+              for c in range(args.serving_chains)]
+    srv = serving.LikelihoodServer(slots=args.serving_slots, precision="f32")
+    for name, topo, ca, S, spec in mix:
+        srv.add_dataset(name, topo, ca, S, spec)
+    srv.start()
+
+    def request(c):
+        d, p = chains[c]
+        q = dict(p)
+        q["branch_lengths"] = p["branch_lengths"] * np.exp(rng.normal(0.0, 0.01, p["branch_lengths"].shape))
+        return mix[d][0], q
+
+    # warm-up: every data set once (plan creation, autotuning, graph capture), then a
+    # closed-loop burst to estimate capacity
+    t0 = time.perf_counter()
+    for c in range(len(mix)):
+        srv.submit(*request(c)).result()
+    setup_s = time.perf_counter() - t0
+    burst = [srv.submit(*request(c)) for c in range(min(len(chains), 4 * len(mix)))]
+    t1 = time.perf_counter()
+    for f in burst:
+        f.result()
+    capacity = len(burst) / (time.perf_counter() - t1)
+    rate = 0.7 * capacity
+    srv.completed.clear()
+    # open-loop Poisson arrivals at 70 % of the measured capacity
+    gaps = rng.exponential(1.0 / rate, args.serving_requests)
+    picks = rng.integers(0, len(chains), args.serving_requests)
+    futs = []
+    start = time.perf_counter()
+    due = start
+    for g, c in zip(gaps, picks):
+        due += g
+        wait = due - time.perf_counter()
+        if wait > 0:
+            time.sleep(wait)
+        futs.append(srv.submit(*request(int(c))))
+    for f in futs:
+        f.result()
+    wall = time.perf_counter() - start
+    stats = srv.latency_stats()
+    srv.stop()
+    # one-at-a-time FP64 drop-in calls (batch 1, eager) on a sample of the same requests
+    sample = [request(int(c)) for c in picks[: min(32, len(picks))]]
+    lik_cache = {}
+    t2 = time.perf_counter()
+    for name, p in sample:
+        d = next(i for i, m in enumerate(mix) if m[0] == name)
+        _, topo, ca, S, spec = mix[d]
+        if name not in lik_cache:
+            lik_cache.clear()
+            torch.cuda.empty_cache()
+            lik_cache[name] = PhyloLikelihood(topo, ca, S, 4, batch=1, precision="f64")
+        lik = lik_cache[name]
+        prep = serving.host_prepare(serving.Dataset(name, topo, ca, S, spec), p)
+        dev = lik.device
+        x = [prep[k].to(dev).unsqueeze(0) for k in ("lam", "u", "w", "bls", "rates", "probs", "pi")]
+        lik.rescale = True
+        lnl = lik.evaluate_eigen(*x)
+        lnl.sum().backward()
+        torch.cuda.synchronize()
+    fp64_rate = len(sample) / (time.perf_counter() - t2)
+    lik_cache.clear()
+    sizes = [(m[1].tip_count, m[2].pattern_count, m[3]) for m in mix]
+    line = {
+        "metric": "serving lnL+grad requests/s, Poisson mix over resident data sets, 1 GB300; p50/p99 latency",
+        "value": len(futs) / wall, "unit": "requests/s", "higher_is_better": True, "n_gpus": 1,
+        "latency_ms": {"p50": stats.get("p50_ms"), "p99": stats.get("p99_ms"), "mean": stats.get("mean_ms")},
+        "offered_rate": rate, "capacity_closed_loop": capacity, "requests": len(futs),
+        "batches": stats.get("batches"), "admissions": stats.get("admissions"), "evictions": stats.get("evictions"),
+        "setup_s": setup_s, "dtype": "f32",
+        "fp64_one_at_a_time": {"value": fp64_rate, "unit": "requests/s", "sample": len(sample),
+                               "what": "PhyloLikelihood FP64, batch 1, eager, sequential"},
+        "speedup_vs_fp64_one_at_a_time": (len(futs) / wall) / fp64_rate,
+        "data": "synthetic: Yule trees, i.i.d. uniform tip states, GTR+G4 / general 20-state+G4",
+        "config": {"workload": "serving_mix", "datasets": len(mix), "chains": len(chains),
+                   "slots": args.serving_slots, "dna": sum(1 for s in sizes if s[2] == 4),
+                   "protein": sum(1 for s in sizes if s[2] == 20), "tips_range": [min(s[0] for s in sizes),
+                                                                                    max(s[0] for s in sizes)],
+                   "patterns_range": [min(s[1] for s in sizes), max(s[1] for s in sizes)]},
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
         run_reference(args)
+        return
+    if args.serving:
+        run_serving(args)
         return
     import torch
     import torch.distributed as dist
