@@ -202,10 +202,12 @@ int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
  *     4-state post-order / adjoint kernels (2..8; rejected when the ring
  *     does not fit in shared memory);
  *   TT_OPT_TENSOR_CORES: 1 = FP32 codon post-order on the tensor cores,
- *     0 = CUDA-core kernel.
+ *     0 = CUDA-core kernel;
+ *   TT_OPT_PAIR_THREADS: FP32 4-state kernels with one thread per (pattern,
+ *     category pair) (1) or per pattern (0, the default).
  * tt_plan_get_option reads the value in use.
  */
-enum { TT_OPT_FWD_STAGES = 1, TT_OPT_BWD_STAGES = 2, TT_OPT_TENSOR_CORES = 3 };
+enum { TT_OPT_FWD_STAGES = 1, TT_OPT_BWD_STAGES = 2, TT_OPT_TENSOR_CORES = 3, TT_OPT_PAIR_THREADS = 4 };
 int tt_plan_set_option(tt_plan *plan, int32_t option, int32_t value);
 int tt_plan_get_option(const tt_plan *plan, int32_t option, int32_t *value);
 

@@ -282,3 +282,37 @@ def test_forward_without_gradient_matches(golden_likelihood):
     assert torch.equal(a, b)
     np.testing.assert_allclose(a.cpu().numpy(), rec["lnl"], rtol=F32_LNL_RTOL)
     assert eng.device_status() == 0
+
+
+def test_pair_thread_kernels_match_one_thread_kernels():
+    """FP32 4-state kernels: one thread per (pattern, category pair) vs one per pattern."""
+    from torchtree_gb300 import _native, patterns, site_models, substitution, synthetic
+    from torchtree_gb300.engine import LikelihoodEngine
+
+    for K, shape in ((4, 0.5), (1, 1.0), (8, 0.7)):
+        wl = synthetic.dna_workload("pt", tip_count=70, site_count=500, batch=2, seed=51 + K, shape=shape,
+                                    categories=K, site_model="gamma")
+        ca = patterns.compress(wl.sequences)
+        dev = torch.device("cuda")
+        pi = torch.tensor(wl.pi, dtype=torch.float64)
+        q = substitution.gtr_q(torch.tensor(wl.exch, dtype=torch.float64), pi)
+        lam, u, w = (t.to(dev).contiguous() for t in substitution.eigen_system(q, pi))
+        rates, probs = site_models.gamma_rates(torch.tensor(wl.shape, dtype=torch.float64), K)
+        b = wl.branch_lengths.shape[0]
+        bls = torch.cat([torch.tensor(wl.branch_lengths), torch.zeros(b, 1, dtype=torch.float64)], -1).to(dev)
+        eig = [lam, u, w, bls.contiguous(), rates.to(dev).contiguous()]
+        props, pid = probs.expand(b, K).to(dev).contiguous(), pi.to(dev)
+        eng = LikelihoodEngine(wl.topology.postorder, wl.topology.tip_count, 4, K, ca.codes, ca.table, ca.weights,
+                               batch=b, precision="f32")
+        out = {}
+        for mode in (0, 1):
+            eng.set_option(_native.TT_OPT_PAIR_THREADS, mode)
+            eng.set_eigen(*eig)
+            lnl = eng.log_likelihood(props, pid, rescale=True, keep_partials=True)
+            _, dpi, dc = eng.gradient(props, pid, want_matrices=False)
+            dP, _, _ = eng.gradient(props, pid, want_matrices=True)
+            out[mode] = (lnl.cpu().numpy(), dP.cpu().numpy(), dpi.cpu().numpy(), dc.cpu().numpy())
+        # identical FP32 partials; the FP64 root sums run in a different order
+        np.testing.assert_allclose(out[1][0], out[0][0], rtol=1e-13)
+        for a_, b_ in zip(out[0][1:], out[1][1:]):
+            np.testing.assert_allclose(b_, a_, rtol=1e-5, atol=1e-5 * np.abs(a_).max())

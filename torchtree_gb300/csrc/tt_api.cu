@@ -297,7 +297,8 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
   }
   auto smem_of = [&](int tile, bool bwd) {
     const int slots = bwd ? p->slots_bwd : p->slots_fwd;
-    return f32 ? tt::tl_smem_bytes(p->K, 256, slots, bwd, bwd ? p->nstage_b : p->nstage_f)
+    const int ns = bwd ? p->nstage_b : p->nstage_f;
+    return f32 ? std::max(tt::tl_smem_bytes(p->K, 256, slots, bwd, ns), tt::tq_smem_bytes(p->K, 256, slots, bwd, ns))
                : tt::prune_smem_bytes<double>(4, p->K, 256, slots, tile, bwd);
   };
   // optional overrides for tuning sweeps: TT_FWD_TILE / TT_BWD_TILE.  FP32 rings
@@ -327,6 +328,10 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
     delete p;
     return fail(TT_ERR_UNSUPPORTED, "tree needs " + std::to_string(std::max(p->slots_fwd, p->slots_bwd)) +
                                         " shared-memory slots, more than one CTA can hold");
+  }
+  if (f32 && tt::pair_threads_supported(p->K)) {  // measured slower on GB300: off unless TT_PAIR_THREADS=1
+    const char *env = getenv("TT_PAIR_THREADS");
+    p->pair_threads = env && atoi(env) == 1;
   }
   p->ntiles_f = (p->N + p->tile_f - 1) / p->tile_f;
   p->ntiles_b = (p->N + p->tile_b - 1) / p->tile_b;
@@ -508,7 +513,7 @@ int tt_log_likelihood(tt_plan *p, const double *props, const double *freqs, int3
   if (p->precision == TT_PRECISION_F32) {
     auto a = make_args<float>(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, site_lnl);
     a.slots = p->slots_fwd;
-    e = tt::launch_prune_f32(a, false, p->tile_f, p->batch, s);
+    e = tt::launch_prune_f32(a, false, p->tile_f, p->batch, p->pair_threads, s);
   } else {
     auto a = make_args<double>(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, site_lnl);
     a.slots = p->slots_fwd;
@@ -544,7 +549,7 @@ int tt_gradient(tt_plan *p, const double *props, const double *freqs, double *gr
     a.slots = p->slots_bwd;
     a.ntiles = p->ntiles_b;
     a.nstage = p->nstage_b;
-    e = tt::launch_prune_f32(a, true, p->tile_b, p->batch, s);
+    e = tt::launch_prune_f32(a, true, p->tile_b, p->batch, p->pair_threads, s);
     if (e == cudaSuccess)
       e = tt::launch_reduce_f32(static_cast<const float *>(p->d_gpart),
                                 static_cast<const float *>(p->d_rootpart), p->d_G, p->d_rootgrad,
@@ -641,13 +646,20 @@ int tt_plan_set_option(tt_plan *p, int32_t option, int32_t value) {
       const bool bwd = option == TT_OPT_BWD_STAGES;
       int smem_max = 0;
       cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
-      if (tt::tl_smem_bytes(p->K, 256, bwd ? p->slots_bwd : p->slots_fwd, bwd, value) > size_t(smem_max))
+      const int sl = bwd ? p->slots_bwd : p->slots_fwd;
+      if (std::max(tt::tl_smem_bytes(p->K, 256, sl, bwd, value), tt::tq_smem_bytes(p->K, 256, sl, bwd, value)) >
+          size_t(smem_max))
         return fail(TT_ERR_UNSUPPORTED, "ring does not fit in shared memory");
       (bwd ? p->nstage_b : p->nstage_f) = value;
       return TT_OK;
     }
     case TT_OPT_TENSOR_CORES:
       return tt::wide_set_tensor_cores(p, value != 0);
+    case TT_OPT_PAIR_THREADS:
+      if (value && (p->wide || p->precision != TT_PRECISION_F32 || !tt::pair_threads_supported(p->K)))
+        return fail(TT_ERR_UNSUPPORTED, "pair-thread kernels serve FP32 4-state plans with 1-4 or 7-8 categories");
+      p->pair_threads = value != 0;
+      return TT_OK;
     default:
       return fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
   }
@@ -659,6 +671,7 @@ int tt_plan_get_option(const tt_plan *p, int32_t option, int32_t *value) {
     case TT_OPT_FWD_STAGES: *value = p->nstage_f; return TT_OK;
     case TT_OPT_BWD_STAGES: *value = p->nstage_b; return TT_OK;
     case TT_OPT_TENSOR_CORES: *value = tt::wide_tensor_cores(p) ? 1 : 0; return TT_OK;
+    case TT_OPT_PAIR_THREADS: *value = p->pair_threads ? 1 : 0; return TT_OK;
     default: return fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
   }
 }

@@ -2,6 +2,7 @@
 #include "tt_launch.h"
 #include "tt_pmatrix.cuh"
 #include "tt_prune_tl.cuh"
+#include "tt_prune_tq.cuh"
 
 namespace tt {
 
@@ -25,11 +26,47 @@ cudaError_t launch_tl(const PruneArgs<float> &a, bool backward, int batch, cudaS
   return cudaGetLastError();
 }
 
+template <int KQ>
+cudaError_t launch_tq(const PruneArgs<float> &a, bool backward, int batch, cudaStream_t stream) {
+  const size_t smem = tq_smem_bytes(a.K, a.C, a.slots, backward, a.nstage);
+  const dim3 grid(a.ntiles, batch);
+  if (backward) {
+    auto kern = tq_backward_kernel<KQ>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    kern<<<grid, kTqTile * KQ, smem, stream>>>(a);
+  } else {
+    auto kern = tq_forward_kernel<KQ>;
+    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    if (e != cudaSuccess) return e;
+    kern<<<grid, kTqTile * KQ, smem, stream>>>(a);
+  }
+  return cudaGetLastError();
+}
+
 }  // namespace
 
-cudaError_t launch_prune_f32(const PruneArgs<float> &a, bool backward, int tile, int batch,
+size_t tq_smem_bytes(int K, int C, int slots, bool backward, int nstage) {
+  const int KQ = kpairs_for(K);
+  return size_t(tl_layout(KQ, C, slots, kTqTile, kTqTile * KQ, nstage, backward, kTqRed2).total);
+}
+
+bool pair_threads_supported(int K) {
+  const int KQ = kpairs_for(K);
+  return KQ == 1 || KQ == 2 || KQ == 4;
+}
+
+cudaError_t launch_prune_f32(const PruneArgs<float> &a, bool backward, int tile, int batch, bool pair_threads,
                              cudaStream_t stream) {
   if (tile != kTlTile) return cudaErrorInvalidValue;
+  if (pair_threads) {
+    switch (kpairs_for(a.K)) {
+      case 1: return launch_tq<1>(a, backward, batch, stream);
+      case 2: return launch_tq<2>(a, backward, batch, stream);
+      case 4: return launch_tq<4>(a, backward, batch, stream);
+      default: return cudaErrorInvalidValue;
+    }
+  }
   switch (kpairs_for(a.K)) {
     case 1: return launch_tl<1>(a, backward, batch, stream);
     case 2: return launch_tl<2>(a, backward, batch, stream);

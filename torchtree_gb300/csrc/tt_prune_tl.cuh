@@ -59,7 +59,9 @@ struct TlLayout {
 constexpr int kTlRecChunk = 32;
 
 
-__host__ __device__ inline TlLayout tl_layout(int KQ, int C, int slots, int P, int NT, int nstage, bool backward) {
+// red2: float2 partial-block elements per thread of the adjoint's pattern reduction
+__host__ __device__ inline TlLayout tl_layout(int KQ, int C, int slots, int P, int NT, int nstage, bool backward,
+                                              int red2 = 16) {
   TlLayout L;
   const TlStage g = tl_stage(KQ, P, backward);
   const int vbytes = 2 * KQ * 4 * 4;  // bytes of one pattern vector (4 states x 2KQ categories)
@@ -77,7 +79,7 @@ __host__ __device__ inline TlLayout tl_layout(int KQ, int C, int slots, int P, i
   L.xbuf = off;
   if (backward) off = int(align16(off + 2 * P * vbytes));
   L.red = off;
-  if (backward) off = int(align16(off + 16 * (NT + 1) * 8));  // 4x4 float2 block per thread, [16][NT+1]
+  if (backward) off = int(align16(off + red2 * (NT + 1) * 8));  // red2 float2 per thread, [red2][NT+1]
   L.red_root = off;
   if (backward) off = int(align16(off + (NT / 32) * 12 * 4));
   L.total = off;
