@@ -130,8 +130,15 @@ def measured_peaks():
     return 6800.0, "fallback"
 
 
+def measured_tensor_peak():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return float(json.loads(p.read_text())["bf16_tflops"])
+    return 1900.0
+
+
 def workload(args):
-    from torchtree_gb300 import patterns, synthetic
+    from torchtree_gb300 import datatype, patterns, synthetic
 
     over = {}
     if args.sites:
@@ -141,8 +148,21 @@ def workload(args):
     if args.batch:
         over["batch"] = args.batch
     wl = synthetic.named_workload(args.workload, **over)
-    ca = patterns.compress(wl.sequences)
+    ca = patterns.compress(wl.sequences, datatype.get(wl.data_type))
     return wl, ca
+
+
+def rate_matrix(model, exch, pi):
+    """Unnormalised Q of a workload's model (torch, differentiable)."""
+    import torch
+
+    from torchtree_gb300 import substitution
+
+    if model in ("gtr", "hky"):
+        return substitution.gtr_q(exch, pi)
+    if model == "general":
+        return substitution.general_symmetric_q(exch, pi, pi.shape[-1])
+    return substitution.mg94_q(torch.ones_like(exch[..., :1]), exch[..., 1:2], exch[..., :1], pi)
 
 
 def cpu_baseline(wl, ca, n_patterns, repeats=3):
@@ -152,7 +172,7 @@ def cpu_baseline(wl, ca, n_patterns, repeats=3):
     rates = (synthetic.discrete_gamma_np(float(wl.shape[0, 0]), wl.categories) if wl.site_model == "gamma"
              else synthetic.discrete_weibull_np(float(wl.shape[0, 0]), wl.categories))
     d = CB.prepare(wl.topology.postorder, ca.codes, ca.table, ca.weights, wl.branch_lengths[0], wl.exch[0],
-                   wl.pi[0], rates, n_patterns)
+                   wl.pi[0], rates, n_patterns, model=wl.model)
     sec, threads, _ = CB.time_evaluations(d, repeats=repeats, warmup=1)
     per_eval = sec * ca.pattern_count / d["n"]
     return {"value": 1.0 / per_eval, "unit": UNIT, "cores": threads, "kind": "port",
@@ -172,7 +192,7 @@ def run_reference(args):
 
     rates = synthetic.discrete_gamma_np(float(wl.shape[0, 0]), wl.categories)
     d = CB.prepare(wl.topology.postorder, ca.codes, ca.table, ca.weights, wl.branch_lengths[0], wl.exch[0],
-                   wl.pi[0], rates, args.cpu_patterns)
+                   wl.pi[0], rates, args.cpu_patterns, model=wl.model)
     for _ in range(args.warmup):
         CB.one_evaluation(d)
     t0 = time.perf_counter()
@@ -353,12 +373,12 @@ def main():
 
     wl, ca = workload(args)
     b = int(wl.branch_lengths.shape[0])
-    T, N, K, S = wl.topology.tip_count, ca.pattern_count, wl.categories, 4
+    T, N, K, S = wl.topology.tip_count, ca.pattern_count, wl.categories, ca.table.shape[1]
     bl, exch, pi, shape = batch_inputs(wl, dev)
     rates, probs = site_models.gamma_rates(shape, K)
     probs = probs.expand(b, K).contiguous()
     # resident inputs of the timed step: the eigen system is set-up work (host LAPACK)
-    q = substitution.gtr_q(exch.cpu(), pi.cpu())
+    q = rate_matrix(wl.model, exch.cpu(), pi.cpu())
     lam, u, w = (t.detach().to(dev).contiguous() for t in substitution.eigen_system(q, pi.cpu()))
     zeros = torch.zeros(b, 1, dtype=torch.float64, device=dev)
     bls = torch.cat([bl, zeros], -1).contiguous()
@@ -450,6 +470,19 @@ def main():
                 "bytes_model": "level-by-level pruning traffic (5 partial passes per evaluation)",
                 "dram_achieved": kernels[dom]["dram_gbs"], "dram_frac": kernels[dom]["dram_gbs"] / peak,
                 "kernels": kernels}
+    if S != 4:  # amino-acid / codon: level-scheduled kernels; flops per SURVEY-style model
+        s_flop = 2 * S * S * K * N * b  # one S x S matrix applied to one category's patterns
+        fw_flops = I * 2 * s_flop
+        bw_flops = 2 * fw_flops + (2 * T - 2) * s_flop
+        for name, fl in (("post_order", fw_flops), ("pre_order_adjoint", bw_flops)):
+            kernels[name]["flops"] = fl
+            kernels[name]["tflops"] = fl / kernels[name]["ms"] / 1e9
+        tflops_peak = measured_tensor_peak()
+        roofline["tensor_post_order"] = {
+            "bound": "tensor", "achieved": kernels["post_order"]["tflops"], "peak": tflops_peak,
+            "unit": "TFLOP/s", "frac": kernels["post_order"]["tflops"] / tflops_peak,
+            "what": "codon post-order as split-TF32 tcgen05 MMAs (3 MMAs per product, counted once); "
+                    "peak = measured dense BF16 (TF32 runs at half that rate)"} if S > 20 else None
     traffic_file = ROOT / "profiles" / "traffic.json"
     if traffic_file.exists():
         tr = json.loads(traffic_file.read_text()).get(args.workload, {}).get(dom)
@@ -490,7 +523,7 @@ def main():
             d_ex.requires_grad_()
             d_pi.requires_grad_()
             r, p = site_models.gamma_rates(d_sh, K)
-            lnl = lik(d_bl, substitution.gtr_q(d_ex, d_pi), d_pi, r, p.expand(b, K))
+            lnl = lik(d_bl, rate_matrix(wl.model, d_ex, d_pi), d_pi, r, p.expand(b, K))
             grads = torch.autograd.grad(lnl.sum(), [d_bl, d_ex, d_pi])
             out = [lnl.detach().cpu()] + [g.cpu() for g in grads]
             return sum(o.numel() * o.element_size() for o in out)
@@ -521,10 +554,12 @@ def main():
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
             "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
-            "data": "synthetic (seeded Yule tree, simulated GTR+G4 alignment)",
+            "data": f"synthetic (seeded Yule tree, alignment simulated under the model: {wl.data_type})",
             "config": {"workload": args.workload, "tips": T, "sites": int(sum(ca.weights)),
                        "patterns": N, "batch": b, "categories": K, "states": S,
-                       "model": "GTR+Gamma4", "l2": "inputs (stored partials) larger than L2; no flush",
+                       "model": {"gtr": "GTR", "hky": "HKY", "general": "general symmetric 20-state",
+                                 "mg94": "MG94 codon (GY94-style)"}[wl.model] + f"+Gamma{K}",
+                       "l2": "inputs (stored partials) larger than L2; no flush",
                        "parallelism": f"replicas x{world}"},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "what": "one batched lnL+gradient call (all samples)"},

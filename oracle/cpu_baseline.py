@@ -20,13 +20,24 @@ from . import likelihood as OL
 
 
 def prepare(topology_postorder, codes, table, weights, branch_lengths, exch, pi, category_rates,
-            n_patterns: int):
+            n_patterns: int, model: str = "gtr"):
     n = min(n_patterns, codes.shape[1])
     tips = [torch.tensor(np.ascontiguousarray(table[codes[t, :n]].T)) for t in range(codes.shape[0])]
     return dict(post=[list(map(int, x)) for x in topology_postorder], tips=tips,
                 weights=torch.tensor(np.asarray(weights[:n], dtype=np.float64)),
                 bl=torch.tensor(branch_lengths), exch=torch.tensor(exch), pi=torch.tensor(pi),
-                rates=torch.tensor(category_rates), n=n)
+                rates=torch.tensor(category_rates), n=n, model=model)
+
+
+def _rate_matrix(model, exch, pi):
+    """GTR / HKY (6 exchangeabilities), general symmetric, MG94 ((kappa, omega), alpha = 1)."""
+    if model in ("gtr", "hky"):
+        return OL.q_gtr(exch, pi)
+    if model == "general":
+        return OL.q_general_symmetric(exch, pi, pi.shape[-1])
+    if model == "mg94":
+        return OL.q_mg94(torch.ones_like(exch[..., :1]), exch[..., 1:2], exch[..., :1], pi)
+    raise ValueError(model)
 
 
 def one_evaluation(d) -> float:
@@ -35,7 +46,7 @@ def one_evaluation(d) -> float:
     pi = d["pi"].clone().requires_grad_()
     k = d["rates"].shape[-1]
     props = torch.full((k, 1, 1), 1.0 / k, dtype=torch.float64)
-    mats = OL.p_t_symmetric(OL.q_gtr(exch, pi), pi,
+    mats = OL.p_t_symmetric(_rate_matrix(d.get("model", "gtr"), exch, pi), pi,
                             OL.model_branch_lengths(bl).unsqueeze(-1) * d["rates"].unsqueeze(-2))
     parts = list(d["tips"]) + [None] * (len(d["tips"]) - 1)
     lnl = OL.treelikelihood_discrete_rescaled(parts, d["weights"], d["post"], mats, pi.unsqueeze(-2), props)

@@ -617,16 +617,18 @@ __global__ void reduce_branch_grads_kernel(const T *gpart, double *G, int branch
   const int branch = blockIdx.x, b = blockIdx.y;
   const T *src = gpart + (size_t(b) * branch_count + branch) * ntiles * size_t(kss);
   for (int e = threadIdx.x; e < kss; e += blockDim.x) {
-    double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+    // blocks of 8 tiles are summed at T precision (4 independent chains), the
+    // block sums in FP64: few FP64 operations, fixed order
+    double acc = 0.0;
     int t = 0;
-    for (; t + 4 <= ntiles; t += 4) {
-      a0 += double(src[size_t(t) * kss + e]);
-      a1 += double(src[size_t(t + 1) * kss + e]);
-      a2 += double(src[size_t(t + 2) * kss + e]);
-      a3 += double(src[size_t(t + 3) * kss + e]);
+    for (; t + 8 <= ntiles; t += 8) {
+      const T *q = src + size_t(t) * kss + e;
+      const T s0 = q[0] + q[size_t(4) * kss], s1 = q[size_t(kss)] + q[size_t(5) * kss];
+      const T s2 = q[size_t(2) * kss] + q[size_t(6) * kss], s3 = q[size_t(3) * kss] + q[size_t(7) * kss];
+      acc += double((s0 + s1) + (s2 + s3));
     }
-    for (; t < ntiles; ++t) a0 += double(src[size_t(t) * kss + e]);
-    G[(size_t(b) * branch_count + branch) * kss + e] = (a0 + a1) + (a2 + a3);
+    for (; t < ntiles; ++t) acc += double(src[size_t(t) * kss + e]);
+    G[(size_t(b) * branch_count + branch) * kss + e] = acc;
   }
 }
 
