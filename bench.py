@@ -122,6 +122,19 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def replica_throughput(seconds: float, units_per_rank: int, world: int, device=None) -> tuple:
+    """Whole-job throughput of ``world`` independent replicas: the slowest
+    rank's time (max over ranks) and units/s over all ranks."""
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([float(seconds)], dtype=torch.float64, device=device)
+    if world > 1:
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    slowest = float(t.item())
+    return slowest, units_per_rank * world / slowest
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -414,12 +427,8 @@ def main():
     barrier()
     launches = eng.launch_count - launches0
     per_step = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
-    total_ms = ev[0].elapsed_time(ev[-1])
-    t = torch.tensor([total_ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-    total_ms = float(t.item())
-    value = b * args.steps * world / (total_ms / 1e3)
+    slowest_s, value = replica_throughput(ev[0].elapsed_time(ev[-1]) / 1e3, b * args.steps, world, dev)
+    total_ms = slowest_s * 1e3
 
     # per-call timing of the two pruning kernels (each call: one pruning
     # kernel + its small reduction kernels) for the roofline
@@ -536,12 +545,8 @@ def main():
         for _ in range(args.steps):
             d2h = e2e_step()
         torch.cuda.synchronize()
-        dt = time.perf_counter() - t0
-        tt = torch.tensor([dt], dtype=torch.float64, device=dev)
-        if world > 1:
-            dist.all_reduce(tt, op=dist.ReduceOp.MAX)
-        e2e = {"value": b * args.steps * world / float(tt.item()), "unit": UNIT, "h2d_bytes_per_step": h2d,
-               "d2h_bytes_per_step": d2h}
+        _, e2e_value = replica_throughput(time.perf_counter() - t0, b * args.steps, world, dev)
+        e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
         del lik
 
     cpu = None

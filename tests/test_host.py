@@ -1,0 +1,204 @@
+"""Host-side checks that need no GPU: the C-ABI library and its exports, the
+schedule, the package's tip encodings / pattern compression / tree glue
+against the reference's golden vectors, the eigen form, the site-model
+gradient, and the replica timing over two gloo ranks."""
+import ctypes
+import json
+import os
+import re
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+# ------------------------------------------------------------------ C ABI
+def _header_functions():
+    text = "\n".join(p.read_text() for p in sorted((ROOT / "include").glob("*.h")))
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"\b(tt_[a-z0-9_]+)\s*\(", text)))
+
+
+def test_library_loads_and_exports_every_header_symbol():
+    from torchtree_gb300 import _build, _native
+
+    _build.build()
+    lib = ctypes.CDLL(str(_native.LIB_PATH))
+    names = _header_functions()
+    assert len(names) >= 15
+    missing = [n for n in names if not hasattr(lib, n)]
+    assert not missing, missing
+    assert set(_native.SIGNATURES) == set(names)  # every export is declared to ctypes
+    lib.tt_version.restype = ctypes.c_char_p
+    assert lib.tt_version().startswith(b"torchtree_gb300")
+
+
+def test_invalid_postorder_is_rejected_by_the_schedule():
+    from torchtree_gb300 import _native
+
+    with pytest.raises(ValueError):
+        _native.schedule(3, [[3, 0, 1], [3, 2, 3]])  # node 3 parents itself
+    with pytest.raises(ValueError):
+        _native.schedule(3, [[4, 0, 1], [3, 4, 2]])  # child used before it is computed
+
+
+@pytest.mark.parametrize("T,seed", [(2, 0), (9, 1), (200, 2), (1000, 3)])
+def test_schedule_is_a_valid_walk_with_logarithmic_stack(T, seed):
+    from torchtree_gb300 import _native, synthetic
+
+    topo = synthetic.yule_topology(T, np.random.default_rng(seed))
+    steps, (fs, bs) = _native.schedule(T, topo.postorder)
+    assert steps.shape == (T - 1, 12)
+    assert fs <= int(np.ceil(np.log2(T))) + 1 and bs <= int(np.ceil(np.log2(T))) + 2
+    done = set(range(T))
+    live = {}  # forward slot -> node
+    for s in range(T - 1):
+        v, l, r, sl, sr, so = steps[s, :6]
+        assert l in done and r in done and v not in done
+        for c, slot in ((l, sl), (r, sr)):
+            if c >= T:
+                assert live.pop(slot) == c
+            else:
+                assert slot == -1
+        if s < T - 2:
+            assert so >= 0 and so not in live
+            live[so] = v
+        else:
+            assert v == 2 * T - 2 and so == -1
+        done.add(v)
+    assert not live
+    # the reversed walk: a node's outside slot is assigned by its parent before use
+    have = {2 * T - 2: -1}
+    for s in range(T - 2, -1, -1):
+        v, l, r = steps[s, :3]
+        assert steps[s, 6] == have.pop(v)
+        for c, slot in ((l, steps[s, 7]), (r, steps[s, 8])):
+            if c >= T:
+                assert slot >= 0 and slot not in have.values()
+                have[c] = slot
+            else:
+                assert slot == -1
+    assert not have
+
+
+# --------------------------------------------------- encodings and patterns
+def test_package_encodings_match_the_reference(golden_encodings):
+    from torchtree_gb300 import datatype
+
+    for name, dt in (("nucleotide", datatype.Nucleotide()), ("amino_acid", datatype.AminoAcid())):
+        S = dt.state_count
+        for o, (enc, amb, plain) in enumerate(golden_encodings[name]):
+            assert dt.partial_vector(o, True) == tuple(amb), (name, chr(o))
+            assert dt.partial_vector(o, False) == tuple(plain), (name, chr(o))
+            assert dt.state_code(o) == min(enc, S), (name, chr(o))
+    codon = datatype.Codon()
+    g = golden_encodings["codon_universal"]
+    assert codon.state_count == g["state_count"]
+    for t, enc in g["codes"].items():
+        b = np.frombuffer(t.encode(), dtype=np.uint8)
+        assert int(codon.triplet_codes(b[0:1], b[1:2], b[2:3])[0]) == min(enc, codon.state_count), t
+
+
+def test_package_compression_matches_the_reference(golden_patterns):
+    from torchtree_gb300 import datatype, patterns
+
+    for case in golden_patterns:
+        if case.get("codon"):
+            ca = patterns.compress(case["sequences"], datatype.Codon())
+            assert ca.weights.tolist() == case["weights"]
+            assert ca.codes.tolist() == case["states"]
+            continue
+        for amb in (0, 1):
+            ca = patterns.compress(case["sequences"], datatype.Nucleotide(), use_ambiguities=bool(amb))
+            assert ca.weights.tolist() == case["weights"]
+            np.testing.assert_array_equal(ca.tip_partials(), np.asarray(case[f"partials_amb{amb}"]))
+        st = patterns.compress(case["sequences"], datatype.Nucleotide(), tip_states=True)
+        assert st.codes.tolist() == case["states"]
+        idx = [slice(*i) if isinstance(i, list) else i for i in case["indices"]]
+        ca = patterns.compress(case["sequences"], datatype.Nucleotide(), indices=idx)
+        assert ca.weights.tolist() == case["indexed_weights"]
+        np.testing.assert_array_equal(ca.tip_partials(), np.asarray(case["indexed_partials"]))
+
+
+def test_newick_topology_and_unrooted_lengths_match_the_reference(golden_likelihood):
+    from torchtree_gb300.tree import Topology
+
+    rec = golden_likelihood["tiny_jc69"]
+    topo = Topology.from_newick(rec["newick"], rec["names"])
+    assert topo.postorder.tolist() == rec["postorder"]
+    np.testing.assert_allclose(topo.unrooted_branch_lengths(), rec["branch_lengths"], rtol=0, atol=0)
+
+
+# --------------------------------------------------------- models
+def test_eigen_form_reproduces_reference_transition_matrices(golden_transition):
+    from torchtree_gb300 import substitution
+
+    g = golden_transition["gtr"]
+    pi = torch.tensor(g["pi"], dtype=torch.float64)
+    lam, u, w = substitution.eigen_system(substitution.gtr_q(torch.tensor(g["rates"], dtype=torch.float64), pi), pi)
+    for t, P in zip(g["t"], g["P"]):
+        mine = u @ torch.diag(torch.exp(lam * t)) @ w
+        np.testing.assert_allclose(mine.numpy(), np.asarray(P), rtol=1e-10, atol=1e-13)
+    g = golden_transition["general20"]
+    pi = torch.tensor(g["pi"], dtype=torch.float64)
+    q = substitution.general_symmetric_q(torch.tensor(g["rates"], dtype=torch.float64), pi, 20)
+    lam, u, w = substitution.eigen_system(q, pi)
+    np.testing.assert_allclose((u @ torch.diag(lam) @ w).numpy(), substitution.normalise(q, pi).numpy(),
+                               atol=1e-12)
+    for t, P in zip(g["t"], g["P"]):
+        mine = u @ torch.diag(torch.exp(lam * t)) @ w
+        np.testing.assert_allclose(mine.numpy(), np.asarray(P), rtol=1e-9, atol=1e-12)
+    g = golden_transition["mg94"]
+    pi = torch.tensor(g["pi"], dtype=torch.float64)
+    q = substitution.mg94_q(torch.tensor(g["alpha"], dtype=torch.float64), torch.tensor(g["beta"], dtype=torch.float64),
+                            torch.tensor(g["kappa"], dtype=torch.float64), pi)
+    np.testing.assert_allclose(torch.diagonal(q).numpy(), np.asarray(g["Q_diag"]), rtol=1e-12)
+    for i, row in g["Q_rows"].items():
+        np.testing.assert_allclose(q[int(i)].numpy(), np.asarray(row), rtol=1e-12, atol=1e-15)
+
+
+def test_gamma_rates_shape_derivative_matches_finite_differences():
+    from torchtree_gb300 import site_models
+
+    shape = torch.tensor([0.37], dtype=torch.float64, requires_grad=True)
+    rates, _ = site_models.gamma_rates(shape, 4)
+    wts = torch.tensor([0.3, -1.2, 0.7, 2.0], dtype=torch.float64)
+    (g,) = torch.autograd.grad((rates * wts).sum(), shape)
+    h = 1e-6
+    f = lambda a: float((site_models.gamma_rates(torch.tensor([a], dtype=torch.float64), 4)[0] * wts).sum())  # noqa
+    fd = (f(0.37 + h) - f(0.37 - h)) / (2 * h)
+    assert abs(g.item() - fd) < 1e-6 * max(1.0, abs(fd))
+
+
+# ------------------------------------------------------ replicas (gloo)
+def _replica_rank(rank, world, port, out):
+    import torch.distributed as dist
+
+    sys.path.insert(0, str(ROOT))
+    os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port))
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    import bench
+
+    seconds = 1.0 + rank  # rank 1 is the slow one
+    slowest, value = bench.replica_throughput(seconds, units_per_rank=8 * 10, world=world)
+    out[rank] = (slowest, value)
+    dist.destroy_process_group()
+
+
+def test_replica_throughput_uses_the_slowest_of_two_gloo_ranks():
+    import socket
+
+    import torch.multiprocessing as mp
+
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    out = mp.Manager().dict()
+    mp.spawn(_replica_rank, args=(2, port, out), nprocs=2, join=True)
+    for r in range(2):
+        slowest, value = out[r]
+        assert slowest == 2.0 and value == pytest.approx(2 * 80 / 2.0)
