@@ -18,11 +18,12 @@
 // Layouts (FP32 plans):
 //   matrices  [batch][step][side][KQ][4][4] float2 pairs (categories 2q, 2q+1;
 //             padded categories are zero)
-//   partials  [batch][internal node - T][tile][chunk][P][4]: a pattern's
-//             4*KE floats are NC = KE float4 chunks, each chunk stored
-//             structure-of-arrays over the tile, so one tile of one node is a
-//             contiguous run (one bulk copy) and every warp access to the
-//             shared-memory stack or a staged tile is conflict-free.
+//   partials  [batch][internal node - T][tile][pair q][state j][P] float2:
+//             one tile of one node is a contiguous run (one bulk copy), and
+//             a (pair, state) row over the tile's patterns is contiguous, so
+//             every warp access to a staged tile is conflict-free.  The
+//             shared-memory stack keeps [chunk][P] float4 (each thread only
+//             touches its own patterns there).
 //   table     [code][4] float2: each tip value duplicated for a category pair
 #pragma once
 
@@ -207,6 +208,34 @@ __device__ __forceinline__ void vec_store_stream(float4 *base, int stride, const
   }
 }
 
+// Tiles in HBM, the adjoint's staged child tiles and its x buffer use the
+// pair-major layout [pair q][state j][pattern p] float2 (a pattern's vector
+// is 4 KQ float2 strided by P), so the pattern reduction's reads of one
+// (pair, state) row over consecutive patterns are contiguous.
+template <int KQ>
+__device__ __forceinline__ void vec_load_pm(Vec<KQ> &x, const float2 *base, int p, int P) {
+#pragma unroll
+  for (int q = 0; q < KQ; ++q)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) x.v[j][q] = base[(q * 4 + j) * P + p];
+}
+
+template <int KQ>
+__device__ __forceinline__ void vec_store_pm(float2 *base, int p, int P, const Vec<KQ> &x) {
+#pragma unroll
+  for (int q = 0; q < KQ; ++q)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) base[(q * 4 + j) * P + p] = x.v[j][q];
+}
+
+template <int KQ>
+__device__ __forceinline__ void vec_store_pm_stream(float2 *base, int p, int P, const Vec<KQ> &x) {
+#pragma unroll
+  for (int q = 0; q < KQ; ++q)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) __stcs(base + (q * 4 + j) * P + p, x.v[j][q]);
+}
+
 // tip vector: the table row duplicated over every category pair
 template <int KQ>
 __device__ __forceinline__ void vec_tip(Vec<KQ> &x, const float2 *tab2, int code) {
@@ -371,7 +400,9 @@ __global__ void __launch_bounds__(NT) tl_forward_kernel(const PruneArgs<float> a
       if (a.rescale) vec_rescale<KQ>(al, E[r]);
       if (out_slot >= 0) {
         vec_store<KQ>(stk + out_slot * NC * P + p, P, al);
-        if (gtile) vec_store_stream<KQ>(gtile + size_t(node - a.tip_count) * node_stride + p, P, al);
+        if (gtile)
+          vec_store_pm_stream<KQ>(reinterpret_cast<float2 *>(gtile + size_t(node - a.tip_count) * node_stride), p, P,
+                                  al);
       } else {
         double site = 0.0;
 #pragma unroll
@@ -439,7 +470,7 @@ __global__ void __launch_bounds__(NT) tl_backward_kernel(const PruneArgs<float> 
   uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.bars);
   float2 *tab2 = reinterpret_cast<float2 *>(smem + L.table);
   float4 *stk = reinterpret_cast<float4 *>(smem + L.stack);
-  float4 *xbuf = reinterpret_cast<float4 *>(smem + L.xbuf);  // [2][NC][P] float4: coef * outside partial
+  float4 *xbuf = reinterpret_cast<float4 *>(smem + L.xbuf);  // [2] pair-major tiles: coef * outside partial
   float2 *red = reinterpret_cast<float2 *>(smem + L.red);    // [16][NT+1] float2: element ij of each thread's block
   float *redr = reinterpret_cast<float *>(smem + L.red_root);
   const TlRecRing ring{reinterpret_cast<int4 *>(smem + L.recs), bars + NSTAGE, a.steps_rev, nst, a.timeout_ns};
@@ -513,8 +544,8 @@ __global__ void __launch_bounds__(NT) tl_backward_kernel(const PruneArgs<float> 
     const bool ltip = left < a.tip_count, rtip = right < a.tip_count;
     const float2 *pml = reinterpret_cast<const float2 *>(stg + G.pm);
     const float2 *pmr = pml + KQ * 16;
-    const float4 *kidl = reinterpret_cast<const float4 *>(stg + G.kids);
-    const float4 *kidr = kidl + NC * P;
+    const float2 *kidl = reinterpret_cast<const float2 *>(stg + G.kids);  // pair-major tiles
+    const float2 *kidr = kidl + NC * P * 2;
 
     Vec<KQ> pre, vl, vr, al, ar;
     if (is_root) {
@@ -527,11 +558,32 @@ __global__ void __launch_bounds__(NT) tl_backward_kernel(const PruneArgs<float> 
       vec_load<KQ>(pre, stk + slot_in * NC * P + tid, P);
     }
     if (ltip) vec_tip<KQ>(vl, tab2, stg[G.codes + tid]);
-    else vec_load<KQ>(vl, kidl + tid, P);
+    else vec_load_pm<KQ>(vl, kidl, tid, P);
     if (rtip) vec_tip<KQ>(vr, tab2, stg[G.codes + P + tid]);
-    else vec_load<KQ>(vr, kidr + tid, P);
-    mat_vec<KQ>(al, pml, vl);
+    else vec_load_pm<KQ>(vr, kidr, tid, P);
     mat_vec<KQ>(ar, pmr, vr);
+    // the left matrices stay in registers for the outside product below
+    float2 ml[KQ][4][4];
+#pragma unroll
+    for (int q = 0; q < KQ; ++q)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const float4 r0v = reinterpret_cast<const float4 *>(pml + (q * 4 + i) * 4)[0];
+        const float4 r1v = reinterpret_cast<const float4 *>(pml + (q * 4 + i) * 4)[1];
+        ml[q][i][0] = make_float2(r0v.x, r0v.y);
+        ml[q][i][1] = make_float2(r0v.z, r0v.w);
+        ml[q][i][2] = make_float2(r1v.x, r1v.y);
+        ml[q][i][3] = make_float2(r1v.z, r1v.w);
+      }
+#pragma unroll
+    for (int q = 0; q < KQ; ++q)
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        float2 acc = __fmul2_rn(ml[q][i][0], vl.v[0][q]);
+        acc = __ffma2_rn(ml[q][i][1], vl.v[1][q], acc);
+        acc = __ffma2_rn(ml[q][i][2], vl.v[2][q], acc);
+        al.v[i][q] = __ffma2_rn(ml[q][i][3], vl.v[3][q], acc);
+      }
     // outside partials at the tops of the two branches: xl = pre*ar, xr = pre*al
     Vec<KQ> xl, xr;
     float2 d2 = make_float2(0.0f, 0.0f);
@@ -581,12 +633,12 @@ __global__ void __launch_bounds__(NT) tl_backward_kernel(const PruneArgs<float> 
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int q = 0; q < KQ; ++q) u.v[i][q] = __fmul2_rn(xl.v[i][q], c2);
-      vec_store<KQ>(xbuf + tid, P, u);
+      vec_store_pm<KQ>(reinterpret_cast<float2 *>(xbuf), tid, P, u);
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int q = 0; q < KQ; ++q) u.v[i][q] = __fmul2_rn(xr.v[i][q], c2);
-      vec_store<KQ>(xbuf + NC * P + tid, P, u);
+      vec_store_pm<KQ>(reinterpret_cast<float2 *>(xbuf + NC * P), tid, P, u);
     }
     // o[jj][q] = sum_i P_q[i][jj] * x[i][q] (scale-free: no coefficient)
     if (!ltip) {
@@ -597,12 +649,10 @@ __global__ void __launch_bounds__(NT) tl_backward_kernel(const PruneArgs<float> 
         for (int jj = 0; jj < 4; ++jj) o.v[jj][q] = make_float2(0.0f, 0.0f);
 #pragma unroll
         for (int i = 0; i < 4; ++i) {
-          const float4 r0v = reinterpret_cast<const float4 *>(pml + (q * 4 + i) * 4)[0];
-          const float4 r1v = reinterpret_cast<const float4 *>(pml + (q * 4 + i) * 4)[1];
-          o.v[0][q] = __ffma2_rn(make_float2(r0v.x, r0v.y), xl.v[i][q], o.v[0][q]);
-          o.v[1][q] = __ffma2_rn(make_float2(r0v.z, r0v.w), xl.v[i][q], o.v[1][q]);
-          o.v[2][q] = __ffma2_rn(make_float2(r1v.x, r1v.y), xl.v[i][q], o.v[2][q]);
-          o.v[3][q] = __ffma2_rn(make_float2(r1v.z, r1v.w), xl.v[i][q], o.v[3][q]);
+          o.v[0][q] = __ffma2_rn(ml[q][i][0], xl.v[i][q], o.v[0][q]);
+          o.v[1][q] = __ffma2_rn(ml[q][i][1], xl.v[i][q], o.v[1][q]);
+          o.v[2][q] = __ffma2_rn(ml[q][i][2], xl.v[i][q], o.v[2][q]);
+          o.v[3][q] = __ffma2_rn(ml[q][i][3], xl.v[i][q], o.v[3][q]);
         }
       }
       int E = 0;
@@ -640,8 +690,8 @@ __global__ void __launch_bounds__(NT) tl_backward_kernel(const PruneArgs<float> 
       if (unit < UNITS) {
         const int c = unit / KQ, t = unit - c * KQ;
         const bool tipc = c ? rtip : ltip;
-        const float2 *xs = reinterpret_cast<const float2 *>(xbuf + c * NC * P);
-        const float2 *vs = reinterpret_cast<const float2 *>(c ? kidr : kidl);
+        const float2 *xs = reinterpret_cast<const float2 *>(xbuf + c * NC * P) + t * 4 * P;  // pair t rows
+        const float2 *vs = (c ? kidr : kidl) + t * 4 * P;
         const unsigned char *csd = stg + G.codes + c * P;
         float2 acc[4][4];
 #pragma unroll
@@ -652,10 +702,7 @@ __global__ void __launch_bounds__(NT) tl_backward_kernel(const PruneArgs<float> 
         for (int m = sidx; m < rem; m += U) {
           float2 x[4], v[4];
 #pragma unroll
-          for (int i = 0; i < 4; ++i) {
-            const int e = i * 2 * KQ + 2 * t;  // pair t of state i: chunk e/4, half (e/2)&1
-            x[i] = xs[((e >> 2) * P + m) * 2 + ((e >> 1) & 1)];
-          }
+          for (int i = 0; i < 4; ++i) x[i] = xs[i * P + m];
           if (tipc) {
             const float4 *tr = reinterpret_cast<const float4 *>(tab2 + int(csd[m]) * 4);
             const float4 t0 = tr[0], t1 = tr[1];
@@ -665,10 +712,7 @@ __global__ void __launch_bounds__(NT) tl_backward_kernel(const PruneArgs<float> 
             v[3] = make_float2(t1.z, t1.w);
           } else {
 #pragma unroll
-            for (int jj = 0; jj < 4; ++jj) {
-              const int e = jj * 2 * KQ + 2 * t;
-              v[jj] = vs[((e >> 2) * P + m) * 2 + ((e >> 1) & 1)];
-            }
+            for (int jj = 0; jj < 4; ++jj) v[jj] = vs[jj * P + m];
           }
 #pragma unroll
           for (int i = 0; i < 4; ++i)

@@ -21,11 +21,12 @@ namespace tt {
 constexpr int kTqTile = 64;    // patterns per CTA
 constexpr int kTqRed2 = 8;     // float2 partial-block elements per adjoint thread
 
-// float2 index of (state j, pair q) of pattern p in a [NC][P] float4 tile
+// float2 index of (state j, pair q) of pattern p in a pair-major tile
+// [pair][state][P] float2 (the layout of stored partials, staged child tiles,
+// the x buffer and, in these kernels, the stack)
 template <int KQ>
 __device__ __forceinline__ int tq_index(int j, int q, int p) {
-  const int f = j * 2 * KQ + 2 * q;
-  return ((f >> 2) * kTqTile + p) * 2 + ((f >> 1) & 1);
+  return (q * 4 + j) * kTqTile + p;
 }
 
 struct PairVec {
