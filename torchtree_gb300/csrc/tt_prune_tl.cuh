@@ -278,12 +278,15 @@ __device__ __forceinline__ void mat_vec(Vec<KQ> &out, const float2 *pm, const Ve
 
 template <int KQ>
 __device__ __forceinline__ float vec_max(const Vec<KQ> &x) {
-  float m = 0.0f;
+  // pairwise tree (the maximum is exact in any order): short dependency chains
+  float m[4];
 #pragma unroll
-  for (int j = 0; j < 4; ++j)
+  for (int j = 0; j < 4; ++j) {
+    m[j] = fmaxf(x.v[j][0].x, x.v[j][0].y);
 #pragma unroll
-    for (int q = 0; q < KQ; ++q) m = fmaxf(m, fmaxf(x.v[j][q].x, x.v[j][q].y));
-  return m;
+    for (int q = 1; q < KQ; ++q) m[j] = fmaxf(m[j], fmaxf(x.v[j][q].x, x.v[j][q].y));
+  }
+  return fmaxf(fmaxf(fmaxf(m[0], m[1]), fmaxf(m[2], m[3])), 0.0f);
 }
 
 // exact power-of-two rescale: multiply by 2^-e with e = floor(log2(max)) for a
@@ -519,11 +522,12 @@ __global__ void __launch_bounds__(NT) tl_backward_kernel(const PruneArgs<float> 
         const int k = ei >> 4, ij = ei & 15;
         const int unit = side * KQ + (k >> 1);
         const float2 *rb = red + ij * (NT + 1) + unit * U;
-        float acc = 0.0f;
-#pragma unroll 4
-        for (int u = 0; u < U; ++u) acc += (k & 1) ? rb[u].y : rb[u].x;
+        float acc[4] = {0.0f, 0.0f, 0.0f, 0.0f};  // four chains, fixed order
+#pragma unroll
+        for (int u = 0; u < U; ++u) acc[u & 3] += (k & 1) ? rb[u].y : rb[u].x;
         const int branch = side ? prev_right : prev_left;
-        a.gpart[((size_t(b) * a.branch_count + branch) * a.ntiles + tile) * KSS + ei] = acc;
+        a.gpart[((size_t(b) * a.branch_count + branch) * a.ntiles + tile) * KSS + ei] =
+            (acc[0] + acc[1]) + (acc[2] + acc[3]);
       }
     }
     if (j == nst) break;
@@ -586,16 +590,16 @@ __global__ void __launch_bounds__(NT) tl_backward_kernel(const PruneArgs<float> 
       }
     // outside partials at the tops of the two branches: xl = pre*ar, xr = pre*al
     Vec<KQ> xl, xr;
-    float2 d2 = make_float2(0.0f, 0.0f);
+    float2 d2[2] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};  // two chains
 #pragma unroll
     for (int i = 0; i < 4; ++i)
 #pragma unroll
       for (int q = 0; q < KQ; ++q) {
         xl.v[i][q] = __fmul2_rn(pre.v[i][q], ar.v[i][q]);
         xr.v[i][q] = __fmul2_rn(pre.v[i][q], al.v[i][q]);
-        d2 = __ffma2_rn(xl.v[i][q], al.v[i][q], d2);
+        d2[i & 1] = __ffma2_rn(xl.v[i][q], al.v[i][q], d2[i & 1]);
       }
-    const float den = d2.x + d2.y;
+    const float den = (d2[0].x + d2[1].x) + (d2[0].y + d2[1].y);
     // dlnL_n/dP = w_n * x (outer) v / L_n; per-pattern scales cancel against den
     const float coef = (act && den > 0.0f) ? w / den : 0.0f;
     if (is_root) {

@@ -114,10 +114,9 @@ __device__ __forceinline__ float pair_max(float x) {
 // exact power-of-two rescale by the pattern maximum over all pairs (as vec_rescale)
 template <int KQ>
 __device__ __forceinline__ void pv_rescale(PairVec &x, int &E) {
-  float m = 0.0f;
-#pragma unroll
-  for (int j = 0; j < 4; ++j) m = fmaxf(m, fmaxf(x.v[j].x, x.v[j].y));
-  m = pair_max<KQ>(m);
+  float m = fmaxf(fmaxf(fmaxf(x.v[0].x, x.v[0].y), fmaxf(x.v[1].x, x.v[1].y)),
+                  fmaxf(fmaxf(x.v[2].x, x.v[2].y), fmaxf(x.v[3].x, x.v[3].y)));
+  m = pair_max<KQ>(fmaxf(m, 0.0f));
   const int be = (__float_as_int(m) >> 23) & 0xff;
   const int e = (be == 0 || be == 0xff) ? 0 : min(be - 127, 126);
   const float f = __int_as_float((127 - e) << 23);
