@@ -204,10 +204,19 @@ int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
  *   TT_OPT_TENSOR_CORES: 1 = FP32 codon post-order on the tensor cores,
  *     0 = CUDA-core kernel;
  *   TT_OPT_PAIR_THREADS: FP32 4-state kernels with one thread per (pattern,
- *     category pair) (1) or per pattern (0, the default).
+ *     category pair) (1) or per pattern (0, the default);
+ *   TT_OPT_PRODUCER_WARP: FP32 4-state post-order with a warp that only
+ *     issues the staging copies (1, the default) or with the copies issued
+ *     by the first compute thread and a block barrier per step (0).
  * tt_plan_get_option reads the value in use.
  */
-enum { TT_OPT_FWD_STAGES = 1, TT_OPT_BWD_STAGES = 2, TT_OPT_TENSOR_CORES = 3, TT_OPT_PAIR_THREADS = 4 };
+enum {
+  TT_OPT_FWD_STAGES = 1,
+  TT_OPT_BWD_STAGES = 2,
+  TT_OPT_TENSOR_CORES = 3,
+  TT_OPT_PAIR_THREADS = 4,
+  TT_OPT_PRODUCER_WARP = 5
+};
 int tt_plan_set_option(tt_plan *plan, int32_t option, int32_t value);
 int tt_plan_get_option(const tt_plan *plan, int32_t option, int32_t *value);
 

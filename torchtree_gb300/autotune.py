@@ -23,7 +23,8 @@ def candidates(engine) -> list:
     """Option sets worth timing for this plan."""
     if engine.precision == "f32" and engine.state_count == 4:
         F, B, Q = _native.TT_OPT_FWD_STAGES, _native.TT_OPT_BWD_STAGES, _native.TT_OPT_PAIR_THREADS
-        return [{Q: 0, F: 6, B: 3}, {Q: 0, F: 3, B: 2}, {Q: 1, F: 6, B: 3}]
+        W = _native.TT_OPT_PRODUCER_WARP
+        return [{Q: 0, W: 1, F: 6, B: 3}, {Q: 0, W: 1, F: 4, B: 2}, {Q: 0, W: 0, F: 6, B: 3}, {Q: 1, W: 0, F: 6, B: 3}]
     if engine.precision == "f32" and engine.state_count > 20:
         return [{_native.TT_OPT_TENSOR_CORES: 1}, {_native.TT_OPT_TENSOR_CORES: 0}]
     return [{}]

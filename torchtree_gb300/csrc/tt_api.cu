@@ -329,6 +329,10 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
     return fail(TT_ERR_UNSUPPORTED, "tree needs " + std::to_string(std::max(p->slots_fwd, p->slots_bwd)) +
                                         " shared-memory slots, more than one CTA can hold");
   }
+  {
+    const char *env = getenv("TT_PRODUCER_WARP");
+    p->producer_warp = f32 && !(env && atoi(env) == 0);
+  }
   if (f32 && tt::pair_threads_supported(p->K)) {  // measured slower on GB300: off unless TT_PAIR_THREADS=1
     const char *env = getenv("TT_PAIR_THREADS");
     p->pair_threads = env && atoi(env) == 1;
@@ -513,7 +517,7 @@ int tt_log_likelihood(tt_plan *p, const double *props, const double *freqs, int3
   if (p->precision == TT_PRECISION_F32) {
     auto a = make_args<float>(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, site_lnl);
     a.slots = p->slots_fwd;
-    e = tt::launch_prune_f32(a, false, p->tile_f, p->batch, p->pair_threads, s);
+    e = tt::launch_prune_f32(a, false, p->tile_f, p->batch, (p->pair_threads ? tt::kF32PairThreads : 0) | (p->producer_warp ? tt::kF32ProducerWarp : 0), s);
   } else {
     auto a = make_args<double>(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, site_lnl);
     a.slots = p->slots_fwd;
@@ -549,7 +553,7 @@ int tt_gradient(tt_plan *p, const double *props, const double *freqs, double *gr
     a.slots = p->slots_bwd;
     a.ntiles = p->ntiles_b;
     a.nstage = p->nstage_b;
-    e = tt::launch_prune_f32(a, true, p->tile_b, p->batch, p->pair_threads, s);
+    e = tt::launch_prune_f32(a, true, p->tile_b, p->batch, p->pair_threads ? tt::kF32PairThreads : 0, s);
     if (e == cudaSuccess)
       e = tt::launch_reduce_f32(static_cast<const float *>(p->d_gpart),
                                 static_cast<const float *>(p->d_rootpart), p->d_G, p->d_rootgrad,
@@ -655,6 +659,12 @@ int tt_plan_set_option(tt_plan *p, int32_t option, int32_t value) {
     }
     case TT_OPT_TENSOR_CORES:
       return tt::wide_set_tensor_cores(p, value != 0);
+    case TT_OPT_PRODUCER_WARP:
+      if (value && (p->wide || p->precision != TT_PRECISION_F32))
+        return fail(TT_ERR_UNSUPPORTED, "the producer-warp post-order serves FP32 4-state plans");
+      if (value && p->nstage_f > 8) return fail(TT_ERR_UNSUPPORTED, "the producer-warp post-order takes <= 8 stages");
+      p->producer_warp = value != 0;
+      return TT_OK;
     case TT_OPT_PAIR_THREADS:
       if (value && (p->wide || p->precision != TT_PRECISION_F32 || !tt::pair_threads_supported(p->K)))
         return fail(TT_ERR_UNSUPPORTED, "pair-thread kernels serve FP32 4-state plans with 1-4 or 7-8 categories");
@@ -672,6 +682,7 @@ int tt_plan_get_option(const tt_plan *p, int32_t option, int32_t *value) {
     case TT_OPT_BWD_STAGES: *value = p->nstage_b; return TT_OK;
     case TT_OPT_TENSOR_CORES: *value = tt::wide_tensor_cores(p) ? 1 : 0; return TT_OK;
     case TT_OPT_PAIR_THREADS: *value = p->pair_threads ? 1 : 0; return TT_OK;
+    case TT_OPT_PRODUCER_WARP: *value = p->producer_warp ? 1 : 0; return TT_OK;
     default: return fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
   }
 }

@@ -49,8 +49,10 @@ inline size_t tl_smem_bytes(int K, int C, int slots, bool backward, int nstage) 
 
 // Launch the pruning kernels (S = 4) with a tile width from the pass's
 // candidate list.  Return cudaSuccess or the launch error.
-// pair_threads: one thread per (pattern, category pair) kernels (K in 1-4 or 7-8)
-cudaError_t launch_prune_f32(const PruneArgs<float> &a, bool backward, int tile, int batch, bool pair_threads,
+// flags: kF32PairThreads = one thread per (pattern, category pair) kernels
+// (K in 1-4 or 7-8); kF32ProducerWarp = post-order with a producer warp
+constexpr int kF32PairThreads = 1, kF32ProducerWarp = 2;
+cudaError_t launch_prune_f32(const PruneArgs<float> &a, bool backward, int tile, int batch, int flags,
                              cudaStream_t stream);
 size_t tq_smem_bytes(int K, int C, int slots, bool backward, int nstage);
 bool pair_threads_supported(int K);

@@ -20,6 +20,7 @@ struct tt_plan {
   int nstage_f = tt::kStages, nstage_b = tt::kStages;
   size_t elem = 0;  // bytes per partial value
   bool pair_threads = false;  // FP32 4-state: one thread per (pattern, category pair)
+  bool producer_warp = true;  // FP32 4-state post-order with a producer warp
   bool tips_set = false, pmat_set = false, partials_valid = false, grads_valid = false;
   long long launches = 0;
   std::vector<int> steps;       // host copy of the schedule (I x 12)

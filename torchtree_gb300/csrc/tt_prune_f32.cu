@@ -56,9 +56,29 @@ bool pair_threads_supported(int K) {
   return KQ == 1 || KQ == 2 || KQ == 4;
 }
 
-cudaError_t launch_prune_f32(const PruneArgs<float> &a, bool backward, int tile, int batch, bool pair_threads,
+template <int KQ>
+cudaError_t launch_tl_ws(const PruneArgs<float> &a, int batch, cudaStream_t stream) {
+  const size_t smem = tl_smem_bytes(a.K, a.C, a.slots, false, a.nstage);
+  const dim3 grid(a.ntiles, batch);
+  auto kern = tl_forward_ws_kernel<KQ, kTlTile>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e != cudaSuccess) return e;
+  kern<<<grid, kTlTile + 32, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
+cudaError_t launch_prune_f32(const PruneArgs<float> &a, bool backward, int tile, int batch, int flags,
                              cudaStream_t stream) {
   if (tile != kTlTile) return cudaErrorInvalidValue;
+  const bool pair_threads = flags & kF32PairThreads;
+  if (!backward && !pair_threads && (flags & kF32ProducerWarp) && a.nstage <= 8) {
+    switch (kpairs_for(a.K)) {
+      case 1: return launch_tl_ws<1>(a, batch, stream);
+      case 2: return launch_tl_ws<2>(a, batch, stream);
+      case 3: return launch_tl_ws<3>(a, batch, stream);
+      default: return launch_tl_ws<4>(a, batch, stream);
+    }
+  }
   if (pair_threads) {
     switch (kpairs_for(a.K)) {
       case 1: return launch_tq<1>(a, backward, batch, stream);

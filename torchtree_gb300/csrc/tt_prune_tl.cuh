@@ -449,6 +449,142 @@ __global__ void __launch_bounds__(NT) tl_forward_kernel(const PruneArgs<float> a
   }
 }
 
+// Post-order with a producer warp: warp NT/32 issues the staging copies
+// (waiting for each stage's "empty" barrier), the NT compute threads wait only
+// on the stage's "full" barrier and never on each other -- a thread touches
+// only its own pattern's stack entries, so the compute warps need no block
+// barrier per step and drift up to NSTAGE - 1 steps apart.
+template <int KQ, int NT>
+__global__ void __launch_bounds__(NT + 32) tl_forward_ws_kernel(const PruneArgs<float> a) {
+  constexpr int P = NT;
+  constexpr int NC = 2 * KQ;
+  constexpr int NW = NT / 32;
+  extern __shared__ __align__(128) unsigned char smem[];
+  __shared__ double warp_tot[NW];
+  __shared__ uint64_t empty[8];
+  __shared__ int abort_flag;
+  const int NSTAGE = a.nstage;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const int K = a.K;
+  const int b = blockIdx.y;
+  const int tile = blockIdx.x;
+  const int nst = a.n_steps;
+  const TlLayout L = tl_layout(KQ, a.C, a.slots, P, NT, NSTAGE, false);
+  const TlStage G = tl_stage(KQ, P, false);
+  unsigned char *stages = smem + L.stages;
+  uint64_t *bars = reinterpret_cast<uint64_t *>(smem + L.bars);
+  float2 *tab2 = reinterpret_cast<float2 *>(smem + L.table);
+  float4 *stk = reinterpret_cast<float4 *>(smem + L.stack);
+
+  if (tid == 0) {
+    for (int st = 0; st < NSTAGE + 2; ++st) mbar_init(&bars[st], 1);
+    for (int st = 0; st < NSTAGE; ++st) mbar_init(&empty[st], NW);
+    abort_flag = 0;
+    fence_barrier_init();
+  }
+  for (int i = tid; i < a.C * 4; i += NT + 32) tab2[i] = make_float2(a.table[i], a.table[i]);
+  __syncthreads();
+
+  if (tid >= NT) {  // producer warp
+    if (lane == 0) {
+      const TlRecRing ring{reinterpret_cast<int4 *>(smem + L.recs), bars + NSTAGE, a.steps, nst, a.timeout_ns};
+      ring.load_chunk(0);
+      ring.load_chunk(1);
+      int issued = 0;
+      bool ok = true;
+      for (int s = 0; s < nst && ok; ++s) {
+        const int st = s % NSTAGE, round = s / NSTAGE;
+        if (round > 0) ok = mbar_wait_bounded(&empty[st], (round - 1) & 1, a.timeout_ns);
+        if (ok && atomicAdd(&abort_flag, 0) != 0) ok = false;
+        int4 cur[3];
+        if (ok) ok = ring.get(s, cur);
+        if (ok) {
+          tl_issue<false>(a, KQ, stages + st * G.bytes, &bars[st], cur, s, b, tile, P, G);
+          issued = s + 1;
+        }
+      }
+      if (!ok) {
+        atomicExch(&abort_flag, 1);
+        // wait (bounded) for the copies already issued before leaving
+        tl_drain(NSTAGE, bars, max(0, issued - NSTAGE), issued - 1, a.status);
+        ring.drain(issued);
+      }
+    }
+  } else {  // compute threads: one pattern each
+    double props[2 * KQ], freqs[4];
+#pragma unroll
+    for (int k = 0; k < 2 * KQ; ++k) props[k] = k < K ? a.props[b * K + k] : 0.0;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) freqs[i] = a.freqs[b * 4 + i];
+    float4 *gtile = a.partials
+                        ? reinterpret_cast<float4 *>(a.partials) + (size_t(b) * (nst - 1) * a.ntiles + tile) * NC * P
+                        : nullptr;
+    const size_t node_stride = size_t(a.ntiles) * NC * P;  // float4 per node
+    const int p = tid;
+    int E = 0;
+    double ll = 0.0;
+    for (int s = 0; s < nst; ++s) {
+      const int st = s % NSTAGE;
+      if (!mbar_wait_bounded(&bars[st], (s / NSTAGE) & 1, a.timeout_ns)) {
+        atomicExch(&abort_flag, 1);
+        atomicExch(a.status, kDeviceTimeout);
+        break;
+      }
+      const unsigned char *stg = stages + st * G.bytes;
+      const int4 r0 = reinterpret_cast<const int4 *>(stg + G.rec)[0];
+      const int4 r1 = reinterpret_cast<const int4 *>(stg + G.rec)[1];
+      const int node = r0.x;
+      const bool ltip = r0.y < a.tip_count, rtip = r0.z < a.tip_count;
+      const float2 *pml = reinterpret_cast<const float2 *>(stg + G.pm);
+      const float2 *pmr = pml + KQ * 16;
+      const int out_slot = r1.y;
+      Vec<KQ> v, al, ar;
+      if (ltip) vec_tip<KQ>(v, tab2, stg[G.codes + p]);
+      else vec_load<KQ>(v, stk + r0.w * NC * P + p, P);
+      mat_vec<KQ>(al, pml, v);
+      if (rtip) vec_tip<KQ>(v, tab2, stg[G.codes + P + p]);
+      else vec_load<KQ>(v, stk + r1.x * NC * P + p, P);
+      mat_vec<KQ>(ar, pmr, v);
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&empty[st]);  // stage consumed by this warp
+#pragma unroll
+      for (int j = 0; j < 4; ++j)
+#pragma unroll
+        for (int q = 0; q < KQ; ++q) al.v[j][q] = __fmul2_rn(al.v[j][q], ar.v[j][q]);
+      if (a.rescale) vec_rescale<KQ>(al, E);
+      if (out_slot >= 0) {
+        vec_store<KQ>(stk + out_slot * NC * P + p, P, al);
+        if (gtile)
+          vec_store_pm_stream<KQ>(reinterpret_cast<float2 *>(gtile + size_t(node - a.tip_count) * node_stride), p,
+                                  P, al);
+      } else {
+        double site = 0.0;
+#pragma unroll
+        for (int j = 0; j < 4; ++j)
+#pragma unroll
+          for (int q = 0; q < KQ; ++q)
+            site = fma(freqs[j], fma(props[2 * q], double(al.v[j][q].x), props[2 * q + 1] * double(al.v[j][q].y)),
+                       site);
+        ll = log(site) + double(E) * 0.69314718055994530942;
+      }
+    }
+    double contrib = 0.0;
+    const int n = tile * P + p;
+    if (n < a.N) {
+      if (a.site_lnl) a.site_lnl[size_t(b) * a.N + n] = ll;
+      contrib = a.weights[n] * ll;
+    }
+    contrib = warp_sum(contrib);
+    if (lane == 0) warp_tot[tid >> 5] = contrib;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double tot = 0.0;
+    for (int w = 0; w < NW; ++w) tot += warp_tot[w];
+    a.tile_lnl[size_t(b) * a.ntiles + tile] = tot;
+  }
+}
+
 // ----------------------------------------------------------------- backward
 // One pattern per thread (R = 1): the adjoint keeps too many vectors live.
 template <int KQ, int NT>
