@@ -96,6 +96,69 @@ struct V4<double> {
   }
 };
 
+// acc[i][j] += a[i] b[j] over a 4 x 4 register tile; FP32 runs as packed
+// FP32x2 FMAs (pairs along j), FP64 as scalar FMAs
+__device__ __forceinline__ void outer4(double (&acc)[4][4], const double (&a)[4], const double (&b)[4]) {
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+}
+
+__device__ __forceinline__ void outer4(float (&acc)[4][4], const float (&a)[4], const float (&b)[4]) {
+  const float2 b01 = make_float2(b[0], b[1]), b23 = make_float2(b[2], b[3]);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const float2 ai = make_float2(a[i], a[i]);
+    const float2 lo = __ffma2_rn(ai, b01, make_float2(acc[i][0], acc[i][1]));
+    const float2 hi = __ffma2_rn(ai, b23, make_float2(acc[i][2], acc[i][3]));
+    acc[i][0] = lo.x, acc[i][1] = lo.y, acc[i][2] = hi.x, acc[i][3] = hi.y;
+  }
+}
+
+// Gradient tile: acc[i][s] += sum_q u[i][q] x[s][q]; FP32 keeps the even and
+// odd q in the two halves of a float2 accumulator (packed FMAs along q)
+template <typename T>
+struct GradTile {
+  T v[4][4];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int s = 0; s < 4; ++s) v[i][s] = T(0);
+  }
+  __device__ __forceinline__ void add(const T (&u)[4][4], const T (&x)[4][4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int s = 0; s < 4; ++s)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) v[i][s] = fma(u[i][q], x[s][q], v[i][s]);
+  }
+  __device__ __forceinline__ T get(int i, int s) const { return v[i][s]; }
+};
+
+template <>
+struct GradTile<float> {
+  float2 v[4][4];
+  __device__ __forceinline__ void zero() {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int s = 0; s < 4; ++s) v[i][s] = make_float2(0.0f, 0.0f);
+  }
+  __device__ __forceinline__ void add(const float (&u)[4][4], const float (&x)[4][4]) {
+#pragma unroll
+    for (int i = 0; i < 4; ++i)
+#pragma unroll
+      for (int s = 0; s < 4; ++s) {
+        v[i][s] = __ffma2_rn(make_float2(u[i][0], u[i][1]), make_float2(x[s][0], x[s][1]), v[i][s]);
+        v[i][s] = __ffma2_rn(make_float2(u[i][2], u[i][3]), make_float2(x[s][2], x[s][3]), v[i][s]);
+      }
+  }
+  __device__ __forceinline__ float get(int i, int s) const { return v[i][s].x + v[i][s].y; }
+};
+
 template <typename T>
 struct WideArgs {
   int tips, N, Npad, K, B, I, S, code_stride, rescale, nchunks, tiles_per_chunk, ntiles;
@@ -181,13 +244,8 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT) wide_forward_kernel(co
     V4<T>::ld(plt + SP * SP + j * SP + ib * 4, pc);
     V4<T>::ld(xs + j * XS + pb * 4, xa);
     V4<T>::ld(xs + SP * XS + j * XS + pb * 4, xc);
-#pragma unroll
-    for (int i = 0; i < 4; ++i)
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        al[i][q] = fma(pa[i], xa[q], al[i][q]);
-        ar[i][q] = fma(pc[i], xc[q], ar[i][q]);
-      }
+    outer4(al, pa, xa);
+    outer4(ar, pc, xc);
   }
 #pragma unroll
   for (int i = 0; i < 4; ++i)
@@ -288,15 +346,11 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT) wide_backward_kernel(c
   // GEMM3 ownership: block (gi, gj) of the SP x SP gradient, pattern quads grp, grp + NG, ...
   const int grp = NT >= IB * IB ? tid / (IB * IB) : 0;
   const bool g3 = grp < NG;
-  T gacc[2][GB][4][4];
+  GradTile<T> gacc[2][GB];
 #pragma unroll
   for (int c = 0; c < 2; ++c)
 #pragma unroll
-    for (int m = 0; m < GB; ++m)
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int s = 0; s < 4; ++s) gacc[c][m][i][s] = T(0);
+    for (int m = 0; m < GB; ++m) gacc[c][m].zero();
   T rp[4] = {T(0), T(0), T(0), T(0)}, rw = T(0);  // root: dlnL/dpi rows, dlnL/dw_k
   double fr[4];
 #pragma unroll
@@ -348,13 +402,8 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT) wide_backward_kernel(c
       V4<T>::ld(plt + SP * SP + j * SP + ib * 4, pc);
       V4<T>::ld(xs + j * XS + pb * 4, xa);
       V4<T>::ld(xs + SP * XS + j * XS + pb * 4, xc);
-#pragma unroll
-      for (int i = 0; i < 4; ++i)
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          al[i][q] = fma(pa[i], xa[q], al[i][q]);
-          ar[i][q] = fma(pc[i], xc[q], ar[i][q]);
-        }
+      outer4(al, pa, xa);
+      outer4(ar, pc, xc);
     }
     if (is_root) {
 #pragma unroll
@@ -393,10 +442,7 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT) wide_backward_kernel(c
           T pa[4], ua[4];
           V4<T>::ld(pm + i * SP + ib * 4, pa);
           V4<T>::ld(us + i * XS + pb * 4, ua);
-#pragma unroll
-          for (int s = 0; s < 4; ++s)
-#pragma unroll
-            for (int q = 0; q < 4; ++q) o[s][q] = fma(pa[s], ua[q], o[s][q]);
+          outer4(o, pa, ua);
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
@@ -443,12 +489,7 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT) wide_backward_kernel(c
             }
 #pragma unroll
             for (int s = 0; s < 4; ++s) V4<T>::ld(xc + (gj + IB * s) * XS + qd * 4, xx[s]);
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-              for (int s = 0; s < 4; ++s)
-#pragma unroll
-                for (int q = 0; q < 4; ++q) gacc[side][m][i][s] = fma(uu[i][q], xx[s][q], gacc[side][m][i][s]);
+            gacc[side][m].add(uu, xx);
           }
         }
       }
@@ -471,7 +512,7 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT) wide_backward_kernel(c
 #pragma unroll
           for (int i = 0; i < 4; ++i)
 #pragma unroll
-            for (int s = 0; s < 4; ++s) dst[(gi + IB * i) * SP + gj + IB * s] = gacc[side][m][i][s];
+            for (int s = 0; s < 4; ++s) dst[(gi + IB * i) * SP + gj + IB * s] = gacc[side][m].get(i, s);
         }
       }
     } else {
@@ -482,7 +523,7 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT) wide_backward_kernel(c
 #pragma unroll
         for (int i = 0; i < 4; ++i)
 #pragma unroll
-          for (int s = 0; s < 4; ++s) gsum[grp * SP * SP + (gi + IB * i) * SP + gj + IB * s] = gacc[side][0][i][s];
+          for (int s = 0; s < 4; ++s) gsum[grp * SP * SP + (gi + IB * i) * SP + gj + IB * s] = gacc[side][0].get(i, s);
       }
       __syncthreads();
       for (int e = tid; e < SP * SP; e += NT) {
@@ -587,10 +628,7 @@ __global__ void __launch_bounds__(256) wide_pmatrix_kernel(const double *lam, co
         T ua[4], wa[4];
         V4<T>::ld(ut + m * SP + bi * 4, ua);
         V4<T>::ld(wm + m * SP + bj * 4, wa);
-#pragma unroll
-        for (int i = 0; i < 4; ++i)
-#pragma unroll
-          for (int j = 0; j < 4; ++j) acc[i][j] = fma(ua[i], wa[j], acc[i][j]);
+        outer4(acc, ua, wa);
       }
 #pragma unroll
       for (int i = 0; i < 4; ++i)
@@ -683,20 +721,14 @@ __global__ void __launch_bounds__(256) wide_pmatrix_backward_kernel(const double
             T ga[4], wa[4];
             V4<T>::ld(gt + j * SP + bi * 4, ga);
             V4<T>::ld(wt + j * SP + bm * 4, wa);
-#pragma unroll
-            for (int x = 0; x < 4; ++x)
-#pragma unroll
-              for (int y = 0; y < 4; ++y) h[x][y] = fma(ga[x], wa[y], h[x][y]);
+            outer4(h, ga, wa);
           }
           // Y block: rows m = bi + IB*x, cols j = bm + IB*y  (Y = U^T G)
           for (int i = 0; i < SP; ++i) {
             T ua[4], ga[4];
             V4<T>::ld(ug + i * SP + bi * 4, ua);
             V4<T>::ld(gg + i * SP + bm * 4, ga);
-#pragma unroll
-            for (int x = 0; x < 4; ++x)
-#pragma unroll
-              for (int y = 0; y < 4; ++y) y4[x][y] = fma(ua[x], ga[y], y4[x][y]);
+            outer4(y4, ua, ga);
           }
           // dU[i][m] += H[i][m] d_m ; dW[m][j] += d_m Y[m][j] ; diagonal partials sum_i U[i][m] H[i][m]
           double dd[4], dr4[4];
