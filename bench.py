@@ -408,7 +408,7 @@ def main():
         e.set_eigen(lam, u, w, bls, rates)
         e.log_likelihood(probs, pi, rescale=True, keep_partials=True)
         e.gradient(probs, pi)
-        return e.eigen_gradient(lam, u, w, bls, rates)
+        return e.rate_matrix_gradient(lam, u, w, bls, rates)
 
     for _ in range(max(args.warmup, 3)):
         step(eng)

@@ -147,6 +147,28 @@ int tt_transition_matrices_gradient(
     double *grad_branch_lengths, double *grad_category_rates, void *stream);
 
 /*
+ * Chain the plan's dlnL/dP (from tt_gradient) to the rate matrix itself:
+ * with Q = U diag(lambda) W and P = exp(Q t r), dlnL/dQ = W^T X U^T where
+ * X = sum over branches and categories of F(t r) .* (U^T G W^T) and
+ * F_mn = (e^(lambda_m t r) - e^(lambda_n t r)) / (lambda_m - lambda_n)
+ * (t r e^(lambda_m t r) when equal) -- the derivative of the matrix
+ * exponential in its eigenbasis.  This replaces autograd through
+ * abstract.py:57-79 including the eigendecomposition, so callers chain
+ * dlnL/dQ straight into the rate-matrix parameters (no eigenvector
+ * derivatives).  Outputs (device double, any may be NULL):
+ * grad_rate_matrix [b][S][S], grad_branch_lengths [b][B],
+ * grad_category_rates [b][K].
+ */
+int tt_rate_matrix_gradient(tt_plan *plan, const double *eigenvalues,
+                            const double *eigenvectors,
+                            const double *inverse_eigenvectors,
+                            const double *branch_lengths,
+                            const double *category_rates,
+                            double *grad_rate_matrix,
+                            double *grad_branch_lengths,
+                            double *grad_category_rates, void *stream);
+
+/*
  * Device status word: TT_OK, or TT_ERR_DEVICE_TIMEOUT when a kernel's
  * bounded wait gave up since the last reset.  Synchronises the stream.
  */

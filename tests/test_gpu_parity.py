@@ -42,7 +42,7 @@ def _keys():
     return sorted(json.loads((GOLDEN / "likelihood.json").read_text()))
 
 
-def engine_eval(rec, precision, rescale=None):
+def engine_eval(rec, precision, rescale=None, route="eigen"):
     """lnL [b] and gradients of sum(lnL) w.r.t. the record's leaves, via the package.
 
     The 4x4 eigendecompositions run on the CPU (one LAPACK call per matrix),
@@ -95,8 +95,11 @@ def engine_eval(rec, precision, rescale=None):
             q = substitution.general_symmetric_q(ex, pi, S)
         else:  # mg94: (kappa, omega), alpha = 1
             q = substitution.mg94_q(torch.ones_like(ex[..., 0:1]), ex[..., 1:2], ex[..., 0:1], pi)
-        lam, u, w = (t.to(dev) for t in substitution.eigen_system(q.cpu(), pi.cpu()))
-        lnl = lik.evaluate_eigen(lam, u, w, bls, rates, probs, pi)
+        if route == "q":  # dlnL/dQ through the matrix-exponential derivative
+            lnl = lik.evaluate_rate_matrix(substitution.normalise(q, pi), pi, bls, rates, probs, pi)
+        else:
+            lam, u, w = (t.to(dev) for t in substitution.eigen_system(q.cpu(), pi.cpu()))
+            lnl = lik.evaluate_eigen(lam, u, w, bls, rates, probs, pi)
     leaves = [(k, g) for k, g in GRAD_KEYS if k in x and g in rec]
     grads = torch.autograd.grad(lnl.sum(), [x[k] for k, _ in leaves])
     return lnl.detach().cpu().numpy(), {g: gr.cpu().numpy() for (_, g), gr in zip(leaves, grads)}, lik
@@ -121,6 +124,18 @@ def test_fp32_rescaled_matches_reference(golden_likelihood, key):
         exp = as_np(rec[g])
         np.testing.assert_allclose(got, exp, rtol=F32_GRAD_TOL, atol=F32_GRAD_TOL * np.abs(exp).max(),
                                    err_msg=g)
+
+
+@pytest.mark.parametrize("precision", ["f64", "f32"])
+@pytest.mark.parametrize("key", [k for k in _keys() if k != "tiny_jc69"])
+def test_rate_matrix_gradient_route_matches_reference(golden_likelihood, key, precision):
+    rec = golden_likelihood[key]
+    lnl, grads, _ = engine_eval(rec, precision, route="q")
+    tol = F64_RTOL if precision == "f64" else F32_GRAD_TOL
+    np.testing.assert_allclose(lnl, rec["lnl"], rtol=F64_RTOL if precision == "f64" else F32_LNL_RTOL)
+    for g, got in grads.items():
+        exp = as_np(rec[g])
+        np.testing.assert_allclose(got, exp, rtol=tol, atol=tol * np.abs(exp).max(), err_msg=g)
 
 
 def test_tiny_known_answer_on_gpu(golden_likelihood):

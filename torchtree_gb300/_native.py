@@ -40,6 +40,7 @@ SIGNATURES = {
     "tt_log_likelihood": (ctypes.c_int, [_P, _P, _P, _I32, _I32, _P, _P, _P]),
     "tt_gradient": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "tt_transition_matrices_gradient": (ctypes.c_int, [_P] + [_P] * 10 + [_P]),
+    "tt_rate_matrix_gradient": (ctypes.c_int, [_P] + [_P] * 8 + [_P]),
     "tt_plan_device_status": (ctypes.c_int, [_P, _P, _PI32, _I32]),
     "tt_plan_launch_count": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
     "tt_schedule": (ctypes.c_int, [_I32, _PI32, _PI32, _PI32]),

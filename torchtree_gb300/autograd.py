@@ -12,6 +12,8 @@ from __future__ import annotations
 
 import torch
 
+from .substitution import eigen_of_normalised
+
 
 def _scale(g: torch.Tensor, x: torch.Tensor, like: torch.Tensor) -> torch.Tensor:
     shape = g.shape + (1,) * (x.dim() - 1)
@@ -44,6 +46,42 @@ class EigenLikelihood(torch.autograd.Function):
         g = g.to(torch.float64)
         return (_scale(g, dlam, lam), _scale(g, du, u), _scale(g, dw, w), _scale(g, dt, bls),
                 _scale(g, dr, rates), _scale(g, dc, props), _scale(g, dpi, freqs), None, None)
+
+
+class RateMatrixLikelihood(torch.autograd.Function):
+    """lnL ``[b]`` from the normalised rate matrix ``q [b,S,S]`` (stationary
+    distribution ``pi_q``), node branch lengths, category rates/weights and
+    root frequencies.  The eigen system is formed here without autograd; the
+    backward returns dlnL/dQ from the derivative of the matrix exponential in
+    the eigenbasis (``tt_rate_matrix_gradient``), so no eigenvector
+    derivative enters the chain to the rate-matrix parameters."""
+
+    @staticmethod
+    def forward(ctx, q, pi_q, bls, rates, props, freqs, engine, rescale):
+        lam, u, w = eigen_of_normalised(q.detach().cpu(), pi_q.detach().cpu())
+        lam, u, w = (t.to(q.device).contiguous() for t in (lam, u, w))
+        engine.set_eigen(lam, u, w, bls, rates)
+        keep = any(ctx.needs_input_grad[:6])
+        lnl = engine.log_likelihood(props, freqs, rescale=rescale, keep_partials=keep)
+        ctx.engine = engine
+        ctx.token = engine.token
+        ctx.rescale = rescale
+        ctx.q_like = q.new_empty(0)
+        ctx.save_for_backward(lam, u, w, bls, rates, props, freqs)
+        return lnl.to(q.dtype)
+
+    @staticmethod
+    def backward(ctx, g):
+        lam, u, w, bls, rates, props, freqs = ctx.saved_tensors
+        eng = ctx.engine
+        if eng.token != ctx.token:
+            eng.set_eigen(lam, u, w, bls, rates)
+            eng.log_likelihood(props, freqs, rescale=ctx.rescale, keep_partials=True)
+        _, dpi, dc = eng.gradient(props, freqs)
+        dq, dt, dr = eng.rate_matrix_gradient(lam, u, w, bls, rates)
+        g = g.to(torch.float64)
+        return (_scale(g, dq, ctx.q_like), None, _scale(g, dt, bls), _scale(g, dr, rates),
+                _scale(g, dc, props), _scale(g, dpi, freqs), None, None)
 
 
 class MatrixLikelihood(torch.autograd.Function):

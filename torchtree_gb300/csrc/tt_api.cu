@@ -59,7 +59,7 @@ int dev_alloc(tt_plan *p, P **ptr, size_t bytes, const char *what) {
 void release(tt_plan *p) {
   void *bufs[] = {p->d_steps, p->d_steps_rev, p->d_branch_pos, p->d_codes,    p->d_table,   p->d_weights,
                   p->d_pmat,  p->d_partials,   p->d_tile_lnl, p->d_gpart,   p->d_rootpart,
-                  p->d_G,     p->d_rootgrad,   p->d_status};
+                  p->d_G,     p->d_rootgrad,   p->d_status, p->d_qpart};
   for (void *b : bufs)
     if (b) cudaFree(b);
   tt::wide_destroy(p);
@@ -607,6 +607,15 @@ int tt_transition_matrices_gradient(tt_plan *p, const double *lam, const double 
   if (e != cudaSuccess) return cuda_fail(e, "transition-matrix gradient launch");
   p->launches += 1;
   return TT_OK;
+}
+
+int tt_rate_matrix_gradient(tt_plan *p, const double *lam, const double *U, const double *W, const double *bl,
+                            const double *rates, double *dQ, double *dbl, double *drates, void *stream) {
+  if (!p || !lam || !U || !W || !bl || !rates) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  if (!p->grads_valid) return fail(TT_ERR_NOT_READY, "tt_gradient has not been called");
+  int rc = check_device(p);
+  if (rc) return rc;
+  return tt::rate_matrix_gradient(p, lam, U, W, bl, rates, dQ, dbl, drates, static_cast<cudaStream_t>(stream));
 }
 
 int tt_plan_device_status(tt_plan *p, void *stream, int32_t *status, int32_t reset) {

@@ -40,6 +40,7 @@ struct tt_plan {
   double *d_G = nullptr;
   double *d_rootgrad = nullptr;
   int *d_status = nullptr;
+  double *d_qpart = nullptr;  // rate-matrix gradient partials (first use)
   size_t bytes = 0;
   tt::WideState *wide = nullptr;  // non-NULL for S != 4 plans
 };
@@ -61,5 +62,8 @@ int wide_matrices_gradient(tt_plan *p, const double *lam, const double *U, const
                            const double *rates, double *dlam, double *dU, double *dW, double *dbl,
                            double *drates, cudaStream_t s);
 int wide_set_tensor_cores(tt_plan *p, bool on);
+// dlnL/dQ, branch lengths and category rates from the plan's dlnL/dP (tt_qgrad.cu)
+int rate_matrix_gradient(tt_plan *p, const double *lam, const double *U, const double *W, const double *bl,
+                         const double *rates, double *dQ, double *dbl, double *drates, cudaStream_t s);
 bool wide_tensor_cores(const tt_plan *p);
 }  // namespace tt

@@ -161,6 +161,15 @@ class LikelihoodEngine:
                                                        ptr(dw), ptr(dt), ptr(dr), _stream()))
         return dlam, du, dw, dt, dr
 
+    def rate_matrix_gradient(self, lam, u, w, branch_lengths, rates):
+        """Chain dlnL/dP to the rate matrix: ``(dQ [b,S,S], dt [b,B], dr [b,K])``."""
+        args = [_dev(x, self.device) for x in (lam, u, w, branch_lengths, rates)]
+        b, S, K, B = self.batch, self.state_count, self.category_count, self.branch_count
+        kw = dict(dtype=torch.float64, device=self.device)
+        dq, dt, dr = torch.empty(b, S, S, **kw), torch.empty(b, B, **kw), torch.empty(b, K, **kw)
+        check(self.lib.tt_rate_matrix_gradient(self._plan, *map(ptr, args), ptr(dq), ptr(dt), ptr(dr), _stream()))
+        return dq, dt, dr
+
     def _per_sample(self, x, width):
         """``[..., width]`` (one row or one per sample) -> contiguous ``[batch, width]``."""
         t = _dev(x, self.device).reshape(-1, width)

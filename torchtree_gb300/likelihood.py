@@ -17,10 +17,10 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from .autograd import EigenLikelihood, MatrixLikelihood
+from .autograd import EigenLikelihood, MatrixLikelihood, RateMatrixLikelihood
 from .engine import LikelihoodEngine
 from .patterns import CompressedAlignment
-from .substitution import eigen_system
+from .substitution import normalise
 from .tree import Topology
 
 
@@ -56,8 +56,18 @@ class PhyloLikelihood:
         ``frequencies [b,S]``; ``rates``/``props`` ``[b,K]``.
         """
         bls = self.node_branch_lengths(branch_lengths, clock_rates)
-        lam, u, w = eigen_system(q_unnorm, frequencies)
-        return self.evaluate_eigen(lam, u, w, bls, rates, props, frequencies)
+        return self.evaluate_rate_matrix(normalise(q_unnorm, frequencies), frequencies, bls, rates, props,
+                                         frequencies)
+
+    def evaluate_rate_matrix(self, q, pi_q, bls, rates, props, frequencies):
+        """lnL from the normalised rate matrix; gradients reach ``q`` as dlnL/dQ."""
+        if self.rescale:
+            return RateMatrixLikelihood.apply(q, pi_q, bls, rates, props, frequencies, self.engine, True)
+        lnl = RateMatrixLikelihood.apply(q, pi_q, bls, rates, props, frequencies, self.engine, False)
+        if torch.isinf(lnl).any():
+            self.rescale = True
+            lnl = RateMatrixLikelihood.apply(q, pi_q, bls, rates, props, frequencies, self.engine, True)
+        return lnl
 
     def evaluate_eigen(self, lam, u, w, bls, rates, props, frequencies):
         if self.rescale:

@@ -20,10 +20,11 @@ chain -- as one captured CUDA graph on the data set's own stream:
   same whether it runs alone or in a mix: slots are independent and the
   kernels are deterministic.
 
-The rate-matrix construction, its eigen system and the site model stay in
-torch on the host (FP64, autograd), as in ``PhyloLikelihood``; the graph
-receives ``(lambda, U, W)``, branch lengths, category rates and weights
-through pinned host buffers and returns the engine's gradients, which the
+The rate-matrix construction and the site model stay in torch on the host
+(FP64, autograd), as in ``PhyloLikelihood``; the graph receives the eigen
+system of the normalised Q, branch lengths, category rates and weights
+through pinned host buffers and returns dlnL/dQ (matrix-exponential
+derivative), branch-length, rate, weight and frequency gradients, which the
 host chains back to the request's parameters.
 """
 from __future__ import annotations
@@ -94,8 +95,8 @@ def host_prepare(ds: Dataset, params: dict) -> dict:
     exch = torch.tensor(np.asarray(params["exch"], dtype=np.float64), dtype=f64, requires_grad=True)
     pi = torch.tensor(np.asarray(params["pi"], dtype=np.float64), dtype=f64, requires_grad=True)
     shape = torch.tensor(np.asarray(params["shape"], dtype=np.float64).reshape(1), dtype=f64, requires_grad=True)
-    q = rate_matrix(ds.spec, exch, pi, ds.state_count)
-    lam, u, w = substitution.eigen_system(q, pi)
+    q = substitution.normalise(rate_matrix(ds.spec, exch, pi, ds.state_count), pi)
+    lam, u, w = substitution.eigen_of_normalised(q.detach(), pi.detach())
     K = ds.spec.categories
     if ds.spec.site_model == "gamma":
         rates, probs = site_models.gamma_rates(shape, K)
@@ -104,15 +105,15 @@ def host_prepare(ds: Dataset, params: dict) -> dict:
     probs = probs.expand(K)
     bl = np.asarray(params["branch_lengths"], dtype=np.float64)
     bls = np.concatenate([bl, [0.0]]) if bl.shape[-1] == 2 * ds.topology.tip_count - 3 else bl
-    return {"leaves": (exch, pi, shape), "lam": lam, "u": u, "w": w, "rates": rates, "probs": probs, "pi": pi,
+    return {"leaves": (exch, pi, shape), "q": q, "lam": lam, "u": u, "w": w, "rates": rates, "probs": probs, "pi": pi,
             "bls": torch.tensor(bls, dtype=f64), "free": bl.shape[-1]}
 
 
 def host_finish(p: dict, out: dict) -> dict:
     """Chain the engine's gradients to the request's parameters."""
     exch, pi, shape = p["leaves"]
-    pairs = [(p[k], out[g]) for k, g in (("lam", "dlam"), ("u", "du"), ("w", "dw"), ("rates", "dr"),
-                                          ("probs", "dc"), ("pi", "dpi")) if p[k].requires_grad]
+    pairs = [(p[k], out[g]) for k, g in (("q", "dq"), ("rates", "dr"), ("probs", "dc"), ("pi", "dpi"))
+             if p[k].requires_grad]
     torch.autograd.backward([t for t, _ in pairs], [g.to(t.dtype).reshape(t.shape) for t, g in pairs])
     return {"lnl": float(out["lnl"]), "grad_branch_lengths": out["dt"][: p["free"]].numpy().copy(),
             "grad_exch": exch.grad.numpy().copy(), "grad_pi": pi.grad.numpy().copy(),
@@ -180,8 +181,8 @@ class GraphExecutor:
         e.set_eigen(x["lam"], x["u"], x["w"], x["bls"], x["rates"])
         lnl = e.log_likelihood(x["props"], x["pi"], rescale=True, keep_partials=True)
         _, dpi, dc = e.gradient(x["props"], x["pi"])
-        dlam, du, dw, dt, dr = e.eigen_gradient(x["lam"], x["u"], x["w"], x["bls"], x["rates"])
-        return {"lnl": lnl, "dpi": dpi, "dc": dc, "dlam": dlam, "du": du, "dw": dw, "dt": dt, "dr": dr}
+        dq, dt, dr = e.rate_matrix_gradient(x["lam"], x["u"], x["w"], x["bls"], x["rates"])
+        return {"lnl": lnl, "dpi": dpi, "dc": dc, "dq": dq, "dt": dt, "dr": dr}
 
     def launch(self, reqs: list) -> None:
         preps = [host_prepare(self.ds, r.params) for r in reqs]

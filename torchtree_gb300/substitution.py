@@ -24,7 +24,11 @@ def normalise(q: torch.Tensor, pi: torch.Tensor) -> torch.Tensor:
 
 def eigen_system(q_unnorm: torch.Tensor, pi: torch.Tensor):
     """``(lambda [...,S], U [...,S,S], W [...,S,S])`` of the normalised Q."""
-    q = normalise(q_unnorm, pi)
+    return eigen_of_normalised(normalise(q_unnorm, pi), pi)
+
+
+def eigen_of_normalised(q: torch.Tensor, pi: torch.Tensor):
+    """Eigen system of an already normalised reversible Q with stationary ``pi``."""
     sp = pi.sqrt()
     a = sp.unsqueeze(-1) * q / sp.unsqueeze(-2)
     lam, v = torch.linalg.eigh(a)
