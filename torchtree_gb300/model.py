@@ -31,9 +31,9 @@ from torchtree.evolution.tree_likelihood import TreeLikelihoodModel as _Referenc
 from torchtree.evolution.tree_model import TreeModel
 
 from . import patterns
-from .autograd import EigenLikelihood, MatrixLikelihood
+from .autograd import MatrixLikelihood, RateMatrixLikelihood
 from .engine import LikelihoodEngine
-from .substitution import eigen_system
+from .substitution import normalise
 
 
 def _uses_eigen_form(subst_model) -> bool:
@@ -105,11 +105,11 @@ class TreeLikelihoodModel(_ReferenceModel):
         if _uses_eigen_form(self.subst_model):
             q = self.subst_model.q()
             q = q.expand(sample_shape + (S, S)) if q.dim() == 2 else q.reshape(sample_shape + (S, S))
-            lam, u, w = eigen_system(flat(q, S, S), flat(freqs, S))
+            qn = normalise(flat(q, S, S), flat(freqs, S))  # abstract.py:49-50
 
-            def run(rescale):
-                return EigenLikelihood.apply(lam, u, w, flat(bls, bls.shape[-1]), flat(rates, K),
-                                             flat(probs, K), flat(freqs, S), eng, rescale)
+            def run(rescale):  # gradients reach Q through dlnL/dQ (no eigenvector derivatives)
+                return RateMatrixLikelihood.apply(qn, flat(freqs, S), flat(bls, bls.shape[-1]), flat(rates, K),
+                                                  flat(probs, K), flat(freqs, S), eng, rescale)
         else:
             mats = self.subst_model.p_t(bls.reshape(sample_shape + (-1, 1)) * rates.unsqueeze(-2))
 
