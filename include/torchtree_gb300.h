@@ -214,6 +214,19 @@ int tt_log_likelihood_static(int32_t tip_count, const int32_t *postorder,
                              const double *frequencies, int32_t rescale,
                              double *log_likelihood, void *stream);
 
+/*
+ * Site-pattern compression on the host (site_pattern.py:69-97): the distinct
+ * columns of `matrix` (uint8 [rows][sites], row-major; one row per taxon, or
+ * per taxon and codon position) in lexicographic order of the column read
+ * from row 0 down -- the reference's sorted(Counter(zip(*sequences))) -- and
+ * their counts.  Outputs: *n_patterns; first_site [sites] (a site holding
+ * pattern p, its first occurrence); counts [sites]; site_pattern [sites] or
+ * NULL (the pattern of every site).  No device memory is touched.
+ */
+int tt_compress_columns(const uint8_t *matrix, int64_t rows, int64_t sites,
+                        int64_t *n_patterns, int64_t *first_site,
+                        int64_t *counts, int64_t *site_pattern);
+
 /* Number of kernel launches the plan issued since creation. */
 int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
 

@@ -202,3 +202,26 @@ def test_replica_throughput_uses_the_slowest_of_two_gloo_ranks():
     for r in range(2):
         slowest, value = out[r]
         assert slowest == 2.0 and value == pytest.approx(2 * 80 / 2.0)
+
+
+def test_native_column_compression_matches_numpy_and_reference_order(golden_patterns):
+    from torchtree_gb300 import _build, datatype, patterns
+
+    _build.build()
+    rng = np.random.default_rng(5)
+    for T, L in ((1, 1), (3, 10), (9, 700), (40, 5000)):
+        m = rng.choice(np.frombuffer(b"ACGT-N?R", dtype=np.uint8), size=(T, L))
+        if L > 10:
+            m[:, L // 2:] = m[:, : L - L // 2]  # many repeated columns
+        a = patterns.unique_columns(m, native=True)
+        b = patterns.unique_columns(m, native=False)
+        np.testing.assert_array_equal(a[0], b[0])
+        np.testing.assert_array_equal(a[1], b[1])
+    for case in golden_patterns:  # the reference's own order and counts
+        if case.get("codon"):
+            continue
+        m = patterns.as_byte_matrix(case["sequences"])
+        cols, w = patterns.unique_columns(m, native=True)
+        assert w.tolist() == case["weights"]
+        st = datatype.Nucleotide().byte_luts(False, tip_states=True)[1][cols]
+        assert st.tolist() == case["states"]

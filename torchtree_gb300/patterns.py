@@ -11,6 +11,8 @@ from __future__ import annotations
 
 from dataclasses import dataclass
 
+import ctypes
+
 import numpy as np
 
 from .datatype import DataType, Nucleotide
@@ -63,10 +65,29 @@ def select_sites(matrix: np.ndarray, indices) -> np.ndarray:
     return matrix[:, picks]
 
 
-def unique_columns(matrix: np.ndarray):
-    """Distinct columns in lexicographic (taxa-order) byte order and counts."""
+def unique_columns(matrix: np.ndarray, native: bool | None = None):
+    """Distinct columns in lexicographic (taxa-order) byte order and counts.
+
+    ``native`` (default: when the engine library is built) runs the C++
+    hash-and-sort compressor (``tt_compress_columns``); otherwise numpy's
+    ``unique(axis=1)``.  Both give the reference's order exactly."""
     if matrix.shape[1] == 0:
         return matrix, np.zeros(0, dtype=np.int64)
+    from . import _native
+
+    if native is None:
+        native = _native.LIB_PATH.exists()
+    if native:
+        m = np.ascontiguousarray(matrix, dtype=np.uint8)
+        T, L = m.shape
+        n = ctypes.c_int64()
+        first = np.empty(L, dtype=np.int64)
+        counts = np.empty(L, dtype=np.int64)
+        lib = _native.load()
+        _native.check(lib.tt_compress_columns(_native.ptr(m), T, L, ctypes.byref(n), _native.ptr(first),
+                                              _native.ptr(counts), None))
+        k = int(n.value)
+        return np.ascontiguousarray(m[:, first[:k]]), counts[:k].copy()
     cols, counts = np.unique(matrix, axis=1, return_counts=True)
     return cols, counts.astype(np.int64)
 
