@@ -139,48 +139,61 @@ __global__ void __launch_bounds__(tc::kThreads, 1) wide_forward_tc_kernel(const 
     fence_barrier_init();
   }
   // B operands: P_c[i][j], N = i, K = j
-  for (int e = tid; e < 2 * SP * SP; e += tc::kThreads) {
-    const int c = e / (SP * SP), ij = e - c * SP * SP, i = ij / SP, j = ij - i * SP;
-    const float val = a.pmat[((size_t(b) * a.B + (c ? r : l)) * a.K + k) * SP * SP + ij];
-    float big, small;
-    tc::split_tf32(val, big, small);
-    const uint32_t off = tc::kmajor_off(i, j, 1024);
-    *reinterpret_cast<float *>(sB + (2 * c) * tc::kBbytes + off) = big;
-    *reinterpret_cast<float *>(sB + (2 * c + 1) * tc::kBbytes + off) = small;
+  // B operands: P_c[i][j], N = i, K = j.  Sixteen 16-byte loads per thread are
+  // issued before any is used (latency), then split and stored as float4.
+  {
+    float4 pv[16];
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int e4 = tid + m * tc::kThreads;  // float4 index over both sides: 2 * 64 * 16
+      const int c = e4 >> 10, f = (e4 & 1023) * 4, i = f / SP;
+      pv[m] = __ldg(reinterpret_cast<const float4 *>(
+          a.pmat + ((size_t(b) * a.B + (c ? r : l)) * a.K + k) * SP * SP + (f - i * SP) + i * SP));
+    }
+#pragma unroll
+    for (int m = 0; m < 16; ++m) {
+      const int e4 = tid + m * tc::kThreads;
+      const int c = e4 >> 10, f = (e4 & 1023) * 4, i = f / SP, j = f - i * SP;
+      float4 hb, hs;
+      tc::split_tf32(pv[m].x, hb.x, hs.x);
+      tc::split_tf32(pv[m].y, hb.y, hs.y);
+      tc::split_tf32(pv[m].z, hb.z, hs.z);
+      tc::split_tf32(pv[m].w, hb.w, hs.w);
+      const uint32_t off = tc::kmajor_off(i, j, 1024);
+      *reinterpret_cast<float4 *>(sB + (2 * c) * tc::kBbytes + off) = hb;
+      *reinterpret_cast<float4 *>(sB + (2 * c + 1) * tc::kBbytes + off) = hs;
+    }
   }
-  // A operands: x_c^T, M = pattern (this thread's), K = j; four j per 16-byte store
+  // A operands: x_c^T, M = pattern (this thread's), K = j; all 64 loads of a
+  // side in flight before the split, four j per 16-byte store
 #pragma unroll
   for (int c = 0; c < 2; ++c) {
     const int child = c ? r : l;
     unsigned char *abig = sA + (2 * c) * tc::kAbytes, *asmall = sA + (2 * c + 1) * tc::kAbytes;
+    float xv[SP];
     if (child < a.tips) {
       const int code = a.codes[size_t(child) * a.code_stride + n0 + tid];
-      const float *row = a.table + size_t(code) * SP;
+      const float4 *row = reinterpret_cast<const float4 *>(a.table + size_t(code) * SP);
+#pragma unroll
       for (int j = 0; j < SP; j += 4) {
-        const float4 t4 = __ldg(reinterpret_cast<const float4 *>(row + j));
-        float4 hb, hs;
-        tc::split_tf32(t4.x, hb.x, hs.x);
-        tc::split_tf32(t4.y, hb.y, hs.y);
-        tc::split_tf32(t4.z, hb.z, hs.z);
-        tc::split_tf32(t4.w, hb.w, hs.w);
-        const uint32_t off = tc::kmajor_off(tid, j, 2048);
-        *reinterpret_cast<float4 *>(abig + off) = hb;
-        *reinterpret_cast<float4 *>(asmall + off) = hs;
+        const float4 t4 = __ldg(row + j / 4);
+        xv[j] = t4.x, xv[j + 1] = t4.y, xv[j + 2] = t4.z, xv[j + 3] = t4.w;
       }
     } else {
       const float *src = a.part + ((size_t(b) * a.I + (child - a.tips)) * a.K + k) * SP * size_t(a.Npad) + n0 + tid;
-      for (int j = 0; j < SP; j += 4) {
-        float4 x4 = make_float4(__ldg(src + size_t(j) * a.Npad), __ldg(src + size_t(j + 1) * a.Npad),
-                                __ldg(src + size_t(j + 2) * a.Npad), __ldg(src + size_t(j + 3) * a.Npad));
-        float4 hb, hs;
-        tc::split_tf32(x4.x, hb.x, hs.x);
-        tc::split_tf32(x4.y, hb.y, hs.y);
-        tc::split_tf32(x4.z, hb.z, hs.z);
-        tc::split_tf32(x4.w, hb.w, hs.w);
-        const uint32_t off = tc::kmajor_off(tid, j, 2048);
-        *reinterpret_cast<float4 *>(abig + off) = hb;
-        *reinterpret_cast<float4 *>(asmall + off) = hs;
-      }
+#pragma unroll
+      for (int j = 0; j < SP; ++j) xv[j] = __ldg(src + size_t(j) * a.Npad);
+    }
+#pragma unroll
+    for (int j = 0; j < SP; j += 4) {
+      float4 hb, hs;
+      tc::split_tf32(xv[j], hb.x, hs.x);
+      tc::split_tf32(xv[j + 1], hb.y, hs.y);
+      tc::split_tf32(xv[j + 2], hb.z, hs.z);
+      tc::split_tf32(xv[j + 3], hb.w, hs.w);
+      const uint32_t off = tc::kmajor_off(tid, j, 2048);
+      *reinterpret_cast<float4 *>(abig + off) = hb;
+      *reinterpret_cast<float4 *>(asmall + off) = hs;
     }
   }
   // generic-proxy writes -> visible to the tensor cores (async proxy)
