@@ -227,6 +227,41 @@ int tt_compress_columns(const uint8_t *matrix, int64_t rows, int64_t sites,
                         int64_t *n_patterns, int64_t *first_site,
                         int64_t *counts, int64_t *site_pattern);
 
+/*
+ * Time-tree operations (no reference kernels; the reference evaluates them
+ * with torch ops and autograd):
+ *   tt_time_tree_create: topology (postorder as for tt_plan_create) and the
+ *     tips' sampling times (host double [T]); lower bounds of internal nodes
+ *     are the largest sampling time below them (tree_height_transform.py:38-60).
+ *   tt_ratio_transform: GeneralNodeHeightTransform._call and
+ *     log_abs_det_jacobian (tree_height_transform.py:62-99): ratios [b][T-1]
+ *     (internal nodes T..2T-3 by index - T, root height last) -> internal
+ *     heights [b][T-1], branch lengths [b][2T-2] (h[parent] - h[child],
+ *     tree_model.py:23-40; may be NULL), log|J| [b].  Device pointers.
+ *   tt_ratio_transform_backward: dlnL/dratios [b][T-1] from dlnL/dheights,
+ *     dlnL/dbranch_lengths, dlnL/dlog|J| (any of the three may be NULL).
+ *   tt_constant_coalescent: ConstantCoalescent.log_prob
+ *     (coalescent.py:112-134) for internal heights [b][T-1] and theta [b]:
+ *     log_prob [b], gradients [b][T-1] and [b] (may be NULL); T <= 4,096.
+ */
+typedef struct tt_time_tree tt_time_tree;
+int tt_time_tree_create(tt_time_tree **tree, int32_t tip_count,
+                        const int32_t *postorder, const double *sampling_times);
+int tt_time_tree_destroy(tt_time_tree *tree);
+int tt_ratio_transform(tt_time_tree *tree, int32_t batch, const double *ratios,
+                       double *heights, double *branch_lengths,
+                       double *log_det_jacobian, void *stream);
+int tt_ratio_transform_backward(tt_time_tree *tree, int32_t batch,
+                                const double *ratios, const double *heights,
+                                const double *grad_heights,
+                                const double *grad_branch_lengths,
+                                const double *grad_log_det, double *grad_ratios,
+                                void *stream);
+int tt_constant_coalescent(tt_time_tree *tree, int32_t batch,
+                           const double *heights, const double *theta,
+                           double *log_prob, double *grad_heights,
+                           double *grad_theta, void *stream);
+
 /* Number of kernel launches the plan issued since creation. */
 int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
 

@@ -327,6 +327,56 @@ def main(ref_root: str) -> None:
                                    shape=0.8, branch_mean=0.1)
     wide_case("codon_w4_t10_b2", wlc)
     wide_case("codon_w4_t10_b2_rescaled", wlc, rescale=True)
+    # ------------------------------------------------------ time-tree operations
+    from types import SimpleNamespace
+
+    from torchtree.evolution.coalescent import ConstantCoalescent
+    from torchtree.evolution.tree_height_transform import GeneralNodeHeightTransform
+    from torchtree.evolution.tree_model import heights_to_branch_lengths
+
+    tt_cases = {}
+    for key, T, seed, hetero in (("isochronous_t12", 12, 31, False), ("heterochronous_t40", 40, 32, True)):
+        trng = np.random.default_rng(seed)
+        topo = synthetic.yule_topology(T, trng)
+        times = trng.uniform(0.0, 2.0, T) if hetero else np.zeros(T)
+        times[0] = 0.0
+        heights = np.zeros(2 * T - 1)
+        heights[:T] = times
+        for v, l, r in topo.postorder:
+            heights[v] = max(heights[l], heights[r]) + trng.exponential(0.5)
+        kids = {int(v): (int(l), int(r)) for v, l, r in topo.postorder}
+        pre = []
+        stack = [2 * T - 2]
+        while stack:  # parent before child (dendropy preorder_node_iter)
+            v = stack.pop()
+            if v >= T:
+                for c in kids[v]:
+                    pre.append((v, c))
+                    stack.append(c)
+        fake = SimpleNamespace(taxa_count=T, postorder=[list(map(int, t)) for t in topo.postorder],
+                               preorder=torch.tensor(pre), sampling_times=torch.tensor(times))
+        tr = GeneralNodeHeightTransform(fake)
+        internal = torch.tensor(heights[T:])
+        ratios = tr.inv(internal).detach().clone().requires_grad_()
+        h = tr(ratios)
+        ld = tr.log_abs_det_jacobian(ratios, h)
+        bl = heights_to_branch_lengths(h, tr._bounds, fake.preorder)
+        w1 = torch.tensor(trng.normal(size=T - 1))
+        w3 = torch.tensor(trng.normal(size=2 * T - 2))
+        obj = (h * w1).sum() + 0.7 * ld + (bl * w3).sum()
+        (gx,) = torch.autograd.grad(obj, ratios)
+        theta = torch.tensor([1.3], requires_grad=True)
+        hh = internal.clone().requires_grad_()
+        lp = ConstantCoalescent(theta).log_prob(torch.cat((torch.tensor(times), hh)))
+        gh, gth = torch.autograd.grad(lp.sum(), [hh, theta])
+        tt_cases[key] = {"postorder": topo.postorder.tolist(), "sampling_times": times.tolist(),
+                         "internal_heights": internal.tolist(), "ratios": ratios.detach().tolist(),
+                         "heights": h.detach().tolist(), "log_det": float(ld), "branch_lengths": bl.detach().tolist(),
+                         "w_heights": w1.tolist(), "w_log_det": 0.7, "w_branch_lengths": w3.tolist(),
+                         "grad_ratios": gx.tolist(), "theta": 1.3, "coalescent_log_prob": float(lp.reshape(-1)[0]),
+                         "coalescent_grad_heights": gh.tolist(), "coalescent_grad_theta": float(gth.reshape(-1)[0])}
+    (HERE / "timetree.json").write_text(json.dumps(tt_cases))
+
     with io.open(HERE / "likelihood.json", "w") as fh:
         json.dump(lik, fh)
     print("wrote", sorted(p.name for p in HERE.glob("*.json")))

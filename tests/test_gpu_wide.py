@@ -102,3 +102,50 @@ def test_protein_batch_member_and_rescaling():
     np.testing.assert_allclose(unscaled["lnl"], full["lnl"], rtol=1e-13)
     f32 = _run(wl, "f32")
     np.testing.assert_allclose(f32["lnl"], full["lnl"], rtol=1e-6)
+
+
+def test_nonreversible_model_through_given_matrices():
+    """Non-reversible Q (no eigen form): P = matrix_exp(Q t) in torch, handed to
+    the engine (tt_set_transition_matrices); lnL and dlnL/dQ-rates vs the oracle."""
+    from oracle import likelihood as OL
+    from torchtree_gb300 import patterns, synthetic
+    from torchtree_gb300.likelihood import PhyloLikelihood
+
+    wl = synthetic.dna_workload("nr", tip_count=25, site_count=300, batch=1, seed=61, shape=0.5,
+                                site_model="weibull")
+    ca = patterns.compress(wl.sequences)
+    rng = np.random.default_rng(2)
+    off = torch.tensor(rng.gamma(1.0, 1.0, 12), dtype=torch.float64)  # 12 free off-diagonal rates
+    rates, probs = OL.weibull_rates(torch.tensor(wl.shape[0], dtype=torch.float64), 4)
+
+    def q_of(r):
+        q = torch.zeros(4, 4, dtype=torch.float64, device=r.device)
+        mask = ~torch.eye(4, dtype=torch.bool, device=r.device)
+        q = q.masked_scatter(mask, r)
+        q = q - torch.diag(q.sum(-1))
+        return q
+
+    def mats_of(r, bl):
+        times = OL.model_branch_lengths(bl).unsqueeze(-1) * rates.to(bl.device).unsqueeze(-2)  # [B,K]
+        return torch.linalg.matrix_exp(q_of(r) * times[..., None, None])  # [B,K,4,4]
+
+    # stationary distribution of the non-reversible Q as root frequencies
+    qn = q_of(off).numpy()
+    w, v = np.linalg.eig(qn.T)
+    pi = np.real(v[:, np.argmin(np.abs(w))])
+    pi = torch.tensor(pi / pi.sum())
+    bl = torch.tensor(wl.branch_lengths[0])
+    r_cpu = off.clone().requires_grad_()
+    tips = [torch.tensor(t) for t in ca.tip_partials()]
+    ref = OL.treelikelihood_discrete_rescaled(tips + [None] * (len(tips) - 1), torch.tensor(ca.weights),
+                                              wl.topology.postorder_list(), mats_of(r_cpu, bl), pi.unsqueeze(-2),
+                                              probs[:, None, None])
+    (gref,) = torch.autograd.grad(ref.sum(), r_cpu)
+    for precision, ltol, gtol in (("f64", 1e-10, 1e-9), ("f32", 1e-6, 1e-4)):
+        lik = PhyloLikelihood(wl.topology, ca, 4, 4, batch=1, precision=precision)
+        r = off.cuda().requires_grad_()
+        lnl = lik.evaluate_matrices(mats_of(r, bl.cuda()).unsqueeze(0), probs.cuda().unsqueeze(0),
+                                    pi.cuda().unsqueeze(0))
+        (g,) = torch.autograd.grad(lnl.sum(), r)
+        np.testing.assert_allclose(lnl.detach().cpu().numpy(), ref.detach().numpy().reshape(-1), rtol=ltol)
+        np.testing.assert_allclose(g.cpu().numpy(), gref.numpy(), rtol=gtol, atol=gtol * np.abs(gref.numpy()).max())

@@ -213,3 +213,36 @@ def test_gamma_rates_by_scipy():
     np.testing.assert_allclose(rates.numpy(), raw / raw.mean(), rtol=1e-14)
     np.testing.assert_allclose(gammainc(shape, raw * shape), q, rtol=1e-10)
     assert abs(float((rates * probs).sum()) - 1.0) < 1e-14
+
+
+# ------------------------------------------------------- time-tree operations
+def _timetree_cases():
+    import json
+
+    from tests.conftest import GOLDEN
+
+    return json.loads((GOLDEN / "timetree.json").read_text())
+
+
+@pytest.mark.parametrize("key", sorted(_timetree_cases()))
+def test_oracle_time_tree_operations_match_reference(key):
+    from oracle import timetree as OT
+
+    c = _timetree_cases()[key]
+    x = torch.tensor(c["ratios"], dtype=torch.float64, requires_grad=True)
+    h, bl, ld = OT.ratio_transform(c["postorder"], c["sampling_times"], x)
+    np.testing.assert_allclose(h.detach().numpy(), c["heights"], rtol=1e-12)
+    np.testing.assert_allclose(bl.detach().numpy(), c["branch_lengths"], rtol=1e-12, atol=1e-13)
+    assert abs(ld.item() - c["log_det"]) < 1e-12 * max(1.0, abs(c["log_det"]))
+    w1 = torch.tensor(c["w_heights"], dtype=torch.float64)
+    w3 = torch.tensor(c["w_branch_lengths"], dtype=torch.float64)
+    obj = (h * w1).sum() + c["w_log_det"] * ld + (bl * w3).sum()
+    (gx,) = torch.autograd.grad(obj, x)
+    np.testing.assert_allclose(gx.numpy(), c["grad_ratios"], rtol=1e-10, atol=1e-12)
+    hh = torch.tensor(c["internal_heights"], dtype=torch.float64, requires_grad=True)
+    th = torch.tensor([c["theta"]], dtype=torch.float64, requires_grad=True)
+    lp = OT.constant_coalescent(c["sampling_times"], hh, th)
+    assert abs(lp.item() - c["coalescent_log_prob"]) < 1e-12 * abs(c["coalescent_log_prob"])
+    gh, gth = torch.autograd.grad(lp.sum(), [hh, th])
+    np.testing.assert_allclose(gh.numpy(), c["coalescent_grad_heights"], rtol=1e-12, atol=1e-12)
+    assert abs(gth.item() - c["coalescent_grad_theta"]) < 1e-12 * max(1.0, abs(c["coalescent_grad_theta"]))

@@ -45,6 +45,11 @@ SIGNATURES = {
     "tt_plan_launch_count": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_int64)]),
     "tt_schedule": (ctypes.c_int, [_I32, _PI32, _PI32, _PI32]),
     "tt_plan_set_option": (ctypes.c_int, [_P, _I32, _I32]),
+    "tt_time_tree_create": (ctypes.c_int, [ctypes.POINTER(_P), _I32, _PI32, _P]),
+    "tt_time_tree_destroy": (ctypes.c_int, [_P]),
+    "tt_ratio_transform": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P, _P]),
+    "tt_ratio_transform_backward": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P, _P, _P, _P]),
+    "tt_constant_coalescent": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P, _P, _P]),
     "tt_compress_columns": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P, _P]),
     "tt_plan_get_option": (ctypes.c_int, [_P, _I32, _PI32]),
     "tt_log_likelihood_static": (ctypes.c_int, [_I32, _PI32, _I32, _I32, _I32, _I32, _P, _P, _I32, _P, _P, _P,
