@@ -125,7 +125,10 @@ int tt_log_likelihood(tt_plan *plan, const double *category_weights,
  *   grad_frequencies:       device double [b][S] or NULL
  *   grad_category_weights:  device double [b][K] or NULL
  * The gradient with respect to P is always kept inside the plan for
- * tt_transition_matrices_gradient.
+ * tt_transition_matrices_gradient.  FP32 plans (unless
+ * TT_OPT_INPLACE_ADJOINT is 0) and plans with S != 4 consume the stored
+ * partials: a second tt_gradient needs a new tt_log_likelihood with
+ * keep_partials=1 (TT_ERR_NOT_READY otherwise).
  */
 int tt_gradient(tt_plan *plan, const double *category_weights,
                 const double *frequencies, double *grad_matrices,
@@ -277,7 +280,11 @@ int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
  *     category pair) (1) or per pattern (0, the default);
  *   TT_OPT_PRODUCER_WARP: FP32 4-state post-order with a warp that only
  *     issues the staging copies (1, the default) or with the copies issued
- *     by the first compute thread and a block barrier per step (0).
+ *     by the first compute thread and a block barrier per step (0);
+ *   TT_OPT_INPLACE_ADJOINT: FP32 4-state adjoint that writes the outside
+ *     partials over the stored post-order tiles (1, the default: a second
+ *     tt_gradient then needs a new tt_log_likelihood with keep_partials=1)
+ *     or keeps them in a shared-memory stack (0).
  * tt_plan_get_option reads the value in use.
  */
 enum {
@@ -285,7 +292,8 @@ enum {
   TT_OPT_BWD_STAGES = 2,
   TT_OPT_TENSOR_CORES = 3,
   TT_OPT_PAIR_THREADS = 4,
-  TT_OPT_PRODUCER_WARP = 5
+  TT_OPT_PRODUCER_WARP = 5,
+  TT_OPT_INPLACE_ADJOINT = 6
 };
 int tt_plan_set_option(tt_plan *plan, int32_t option, int32_t value);
 int tt_plan_get_option(const tt_plan *plan, int32_t option, int32_t *value);

@@ -300,7 +300,9 @@ def test_forward_without_gradient_matches(golden_likelihood):
 
 
 def test_pair_thread_kernels_match_one_thread_kernels():
-    """FP32 4-state kernels: one thread per (pattern, category pair) vs one per pattern."""
+    """FP32 4-state kernels: one thread per (pattern, category pair) vs one per
+    pattern, and the adjoint with a shared-memory stack vs the one that stores
+    outside partials over the post-order tiles (which consumes them)."""
     from torchtree_gb300 import _native, patterns, site_models, substitution, synthetic
     from torchtree_gb300.engine import LikelihoodEngine
 
@@ -320,14 +322,18 @@ def test_pair_thread_kernels_match_one_thread_kernels():
         eng = LikelihoodEngine(wl.topology.postorder, wl.topology.tip_count, 4, K, ca.codes, ca.table, ca.weights,
                                batch=b, precision="f32")
         out = {}
-        for mode in (0, 1):
-            eng.set_option(_native.TT_OPT_PAIR_THREADS, mode)
+        for mode, (pair, inplace) in {"stack": (0, 0), "inplace": (0, 1), "pair": (1, 0)}.items():
+            eng.set_option(_native.TT_OPT_PAIR_THREADS, pair)
+            eng.set_option(_native.TT_OPT_INPLACE_ADJOINT, inplace)
             eng.set_eigen(*eig)
             lnl = eng.log_likelihood(props, pid, rescale=True, keep_partials=True)
-            _, dpi, dc = eng.gradient(props, pid, want_matrices=False)
-            dP, _, _ = eng.gradient(props, pid, want_matrices=True)
+            dP, dpi, dc = eng.gradient(props, pid, want_matrices=True)
             out[mode] = (lnl.cpu().numpy(), dP.cpu().numpy(), dpi.cpu().numpy(), dc.cpu().numpy())
-        # identical FP32 partials; the FP64 root sums run in a different order
-        np.testing.assert_allclose(out[1][0], out[0][0], rtol=1e-13)
-        for a_, b_ in zip(out[0][1:], out[1][1:]):
-            np.testing.assert_allclose(b_, a_, rtol=1e-5, atol=1e-5 * np.abs(a_).max())
+            if inplace:  # the post-order tiles are gone: a second adjoint is refused
+                with pytest.raises(_native.EngineError):
+                    eng.gradient(props, pid)
+        for mode in ("inplace", "pair"):
+            # identical FP32 partials; the FP64 root sums run in a different order
+            np.testing.assert_allclose(out[mode][0], out["stack"][0], rtol=1e-13)
+            for a_, b_ in zip(out["stack"][1:], out[mode][1:]):
+                np.testing.assert_allclose(b_, a_, rtol=1e-5, atol=1e-5 * np.abs(a_).max())

@@ -126,7 +126,8 @@ def test_nonreversible_model_through_given_matrices():
         return q
 
     def mats_of(r, bl):
-        times = OL.model_branch_lengths(bl).unsqueeze(-1) * rates.to(bl.device).unsqueeze(-2)  # [B,K]
+        node_bl = torch.cat((bl, bl.new_zeros(1)))  # node 2T-3 hangs from the root by a zero-length branch
+        times = node_bl.unsqueeze(-1) * rates.to(bl.device).unsqueeze(-2)  # [B,K]
         return torch.linalg.matrix_exp(q_of(r) * times[..., None, None])  # [B,K,4,4]
 
     # stationary distribution of the non-reversible Q as root frequencies

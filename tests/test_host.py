@@ -83,6 +83,33 @@ def test_schedule_is_a_valid_walk_with_logarithmic_stack(T, seed):
             else:
                 assert slot == -1
     assert not have
+    # in-place adjoint: an internal child is either carried to the next
+    # reversed step (which is that child) or stored, and then staged back at
+    # a step at least two after its parent's, whose reversed index it holds
+    rev = steps[::-1]
+    at = {int(rev[j, 0]): j for j in range(T - 1)}
+    pre_from = {}
+    for j in range(T - 1):
+        l, r, fl = int(rev[j, 1]), int(rev[j, 2]), int(rev[j, 9])
+        for c, carry, store in ((l, 2, 8), (r, 4, 16)):
+            if c < T:
+                assert not fl & (carry | store)
+                continue
+            assert bool(fl & carry) != bool(fl & store)
+            if fl & carry:
+                assert at[c] == j + 1
+                pre_from[c] = "carry"
+            else:
+                assert at[c] >= j + 2 and rev[at[c], 10] == j
+                pre_from[c] = "stored"
+    for j in range(T - 1):
+        v = int(rev[j, 0])
+        if j == 0:
+            assert v == 2 * T - 2 and rev[j, 9] & 1 == 0
+        else:
+            assert bool(rev[j, 9] & 1) == (pre_from[v] == "stored")
+            if pre_from[v] == "carry":
+                assert rev[j, 10] == -1
 
 
 # --------------------------------------------------- encodings and patterns

@@ -182,6 +182,34 @@ int build_schedule(tt_plan *p, const int32_t *post) {
     bslot[r] = rec[8];
   }
   p->slots_bwd = std::max(next_slot, 1);
+  // In-place FP32 adjoint.  The reversed walk visits, right after a node with
+  // an internal child, one of its children (the one that precedes it in the
+  // post-order): that child's outside partial stays in registers.  The other
+  // internal child's outside partial overwrites the child's own post-order
+  // tile, read for the last time at this step, and is staged back at the
+  // child's step, which must not be staged before this step has written it.
+  std::vector<int> pos(NN, -1);
+  for (int s = 0; s < I; ++s) pos[order[s]] = s;
+  for (int s = 0; s < I; ++s) {
+    const int v = order[s], l = left[v], r = right[v];
+    int *rec = &p->steps[size_t(s) * tt::kStepInts];
+    const int nxt = s > 0 ? order[s - 1] : -1;
+    int flags = 0;
+    if (l >= T) flags |= nxt == l ? tt::kTaCarryLeft : tt::kTaStoreLeft;
+    if (r >= T) flags |= nxt == r ? tt::kTaCarryRight : tt::kTaStoreRight;
+    rec[9] = flags;
+    rec[10] = -1;
+  }
+  for (int s = 0; s < I; ++s) {
+    const int v = order[s];
+    if (v == root) continue;
+    const int ps = pos[parent[v]];
+    const int pf = p->steps[size_t(ps) * tt::kStepInts + 9];
+    if (pf & (v == left[parent[v]] ? tt::kTaStoreLeft : tt::kTaStoreRight)) {
+      p->steps[size_t(s) * tt::kStepInts + 9] |= tt::kTaPreStored;
+      p->steps[size_t(s) * tt::kStepInts + 10] = I - 1 - ps;
+    }
+  }
   p->branch_pos.assign(p->B, -1);
   for (int s = 0; s < I; ++s) {
     const int *rec = &p->steps[size_t(s) * tt::kStepInts];
@@ -298,7 +326,8 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
   auto smem_of = [&](int tile, bool bwd) {
     const int slots = bwd ? p->slots_bwd : p->slots_fwd;
     const int ns = bwd ? p->nstage_b : p->nstage_f;
-    return f32 ? std::max(tt::tl_smem_bytes(p->K, 256, slots, bwd, ns), tt::tq_smem_bytes(p->K, 256, slots, bwd, ns))
+    return f32 ? std::max({tt::tl_smem_bytes(p->K, 256, slots, bwd, ns), tt::tq_smem_bytes(p->K, 256, slots, bwd, ns),
+                           bwd ? tt::ta_smem_bytes(p->K, 256, ns) : size_t(0)})
                : tt::prune_smem_bytes<double>(4, p->K, 256, slots, tile, bwd);
   };
   // optional overrides for tuning sweeps: TT_FWD_TILE / TT_BWD_TILE.  FP32 rings
@@ -332,6 +361,10 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
   {
     const char *env = getenv("TT_PRODUCER_WARP");
     p->producer_warp = f32 && !(env && atoi(env) == 0);
+  }
+  {
+    const char *env = getenv("TT_INPLACE_ADJOINT");
+    p->inplace_adjoint = f32 && !(env && atoi(env) == 0);
   }
   if (f32 && tt::pair_threads_supported(p->K)) {  // measured slower on GB300: off unless TT_PAIR_THREADS=1
     const char *env = getenv("TT_PAIR_THREADS");
@@ -553,7 +586,8 @@ int tt_gradient(tt_plan *p, const double *props, const double *freqs, double *gr
     a.slots = p->slots_bwd;
     a.ntiles = p->ntiles_b;
     a.nstage = p->nstage_b;
-    e = tt::launch_prune_f32(a, true, p->tile_b, p->batch, p->pair_threads ? tt::kF32PairThreads : 0, s);
+    e = tt::launch_prune_f32(a, true, p->tile_b, p->batch,
+                             p->pair_threads ? tt::kF32PairThreads : (p->inplace_adjoint ? tt::kF32InPlaceAdjoint : 0), s);
     if (e == cudaSuccess)
       e = tt::launch_reduce_f32(static_cast<const float *>(p->d_gpart),
                                 static_cast<const float *>(p->d_rootpart), p->d_G, p->d_rootgrad,
@@ -572,6 +606,8 @@ int tt_gradient(tt_plan *p, const double *props, const double *freqs, double *gr
   }
   if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
   p->launches += 3;
+  if (p->precision == TT_PRECISION_F32 && !p->pair_threads && p->inplace_adjoint)
+    p->partials_valid = false;  // the outside partials overwrote the post-order tiles
   const size_t kss = size_t(p->K) * p->S * p->S;
   if (grad_matrices) {
     e = cudaMemcpyAsync(grad_matrices, p->d_G, size_t(p->batch) * p->B * kss * sizeof(double),
@@ -660,8 +696,8 @@ int tt_plan_set_option(tt_plan *p, int32_t option, int32_t value) {
       int smem_max = 0;
       cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
       const int sl = bwd ? p->slots_bwd : p->slots_fwd;
-      if (std::max(tt::tl_smem_bytes(p->K, 256, sl, bwd, value), tt::tq_smem_bytes(p->K, 256, sl, bwd, value)) >
-          size_t(smem_max))
+      if (std::max({tt::tl_smem_bytes(p->K, 256, sl, bwd, value), tt::tq_smem_bytes(p->K, 256, sl, bwd, value),
+                    bwd ? tt::ta_smem_bytes(p->K, 256, value) : size_t(0)}) > size_t(smem_max))
         return fail(TT_ERR_UNSUPPORTED, "ring does not fit in shared memory");
       (bwd ? p->nstage_b : p->nstage_f) = value;
       return TT_OK;
@@ -679,6 +715,11 @@ int tt_plan_set_option(tt_plan *p, int32_t option, int32_t value) {
         return fail(TT_ERR_UNSUPPORTED, "pair-thread kernels serve FP32 4-state plans with 1-4 or 7-8 categories");
       p->pair_threads = value != 0;
       return TT_OK;
+    case TT_OPT_INPLACE_ADJOINT:
+      if (value && (p->wide || p->precision != TT_PRECISION_F32))
+        return fail(TT_ERR_UNSUPPORTED, "the in-place adjoint serves FP32 4-state plans");
+      p->inplace_adjoint = value != 0;
+      return TT_OK;
     default:
       return fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
   }
@@ -692,6 +733,7 @@ int tt_plan_get_option(const tt_plan *p, int32_t option, int32_t *value) {
     case TT_OPT_TENSOR_CORES: *value = tt::wide_tensor_cores(p) ? 1 : 0; return TT_OK;
     case TT_OPT_PAIR_THREADS: *value = p->pair_threads ? 1 : 0; return TT_OK;
     case TT_OPT_PRODUCER_WARP: *value = p->producer_warp ? 1 : 0; return TT_OK;
+    case TT_OPT_INPLACE_ADJOINT: *value = p->inplace_adjoint ? 1 : 0; return TT_OK;
     default: return fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
   }
 }

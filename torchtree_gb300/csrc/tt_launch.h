@@ -26,7 +26,7 @@ constexpr int kBwdTilesF64[2] = {64, 32};
 constexpr int kStages = 4;
 // default staging-ring depths of the FP32 kernels (reduced to fit shared memory)
 constexpr int kTlFwdStages = 6;
-constexpr int kTlBwdStages = 3;
+constexpr int kTlBwdStages = 2;
 
 // category pairs of the FP32 kernels (K padded to an even count)
 inline int kpairs_for(int K) { return (K + 1) / 2; }
@@ -50,11 +50,14 @@ inline size_t tl_smem_bytes(int K, int C, int slots, bool backward, int nstage) 
 // Launch the pruning kernels (S = 4) with a tile width from the pass's
 // candidate list.  Return cudaSuccess or the launch error.
 // flags: kF32PairThreads = one thread per (pattern, category pair) kernels
-// (K in 1-4 or 7-8); kF32ProducerWarp = post-order with a producer warp
-constexpr int kF32PairThreads = 1, kF32ProducerWarp = 2;
+// (K in 1-4 or 7-8); kF32ProducerWarp = post-order with a producer warp;
+// kF32InPlaceAdjoint = adjoint that stores outside partials over the
+// post-order tiles (consumes them) instead of a shared-memory stack
+constexpr int kF32PairThreads = 1, kF32ProducerWarp = 2, kF32InPlaceAdjoint = 4;
 cudaError_t launch_prune_f32(const PruneArgs<float> &a, bool backward, int tile, int batch, int flags,
                              cudaStream_t stream);
 size_t tq_smem_bytes(int K, int C, int slots, bool backward, int nstage);
+size_t ta_smem_bytes(int K, int C, int nstage);
 bool pair_threads_supported(int K);
 cudaError_t launch_prune_f64(const PruneArgs<double> &a, bool backward, int tile, int batch,
                              cudaStream_t stream);

@@ -21,6 +21,7 @@ struct tt_plan {
   size_t elem = 0;  // bytes per partial value
   bool pair_threads = false;  // FP32 4-state: one thread per (pattern, category pair)
   bool producer_warp = true;  // FP32 4-state post-order with a producer warp
+  bool inplace_adjoint = true;  // FP32 4-state adjoint storing outside partials over the post-order tiles
   bool tips_set = false, pmat_set = false, partials_valid = false, grads_valid = false;
   long long launches = 0;
   std::vector<int> steps;       // host copy of the schedule (I x 12)

@@ -35,8 +35,15 @@ namespace tt {
 //  [0] node [1] left [2] right [3] fwd slot of left (-1: tip)
 //  [4] fwd slot of right [5] fwd output slot (-1: root) [6] bwd input slot
 //  (-1: root) [7] bwd output slot of left (-1: tip) [8] bwd output slot of
-//  right [9..11] unused
+//  right [9] flags of the in-place FP32 adjoint (kTa*) [10] for a node
+//  whose outside partial is stored in place: the reversed-walk index of its
+//  parent's step (-1 otherwise) [11] unused
 constexpr int kStepInts = 12;
+// [9]: this node's outside partial was stored in place over its post-order
+// tile (else it arrives in registers from the previous step, or is the root);
+// the left / right child's outside partial stays in registers for the next
+// step (carry) or is stored in place.
+constexpr int kTaPreStored = 1, kTaCarryLeft = 2, kTaCarryRight = 4, kTaStoreLeft = 8, kTaStoreRight = 16;
 
 template <typename T>
 struct PruneArgs {

@@ -1,6 +1,7 @@
 // FP32 (rescaled) pruning kernels on packed FP32x2 arithmetic, S = 4.
 #include "tt_launch.h"
 #include "tt_pmatrix.cuh"
+#include "tt_prune_ta.cuh"
 #include "tt_prune_tl.cuh"
 #include "tt_prune_tq.cuh"
 
@@ -67,10 +68,35 @@ cudaError_t launch_tl_ws(const PruneArgs<float> &a, int batch, cudaStream_t stre
   return cudaGetLastError();
 }
 
+size_t ta_smem_bytes(int K, int C, int nstage) {
+  return size_t(ta_layout(kpairs_for(K), C, kTlTile, kTlBwdThreads, nstage).total);
+}
+
+template <int KQ>
+cudaError_t launch_ta(const PruneArgs<float> &a, int batch, cudaStream_t stream) {
+  const size_t smem = ta_smem_bytes(a.K, a.C, a.nstage);
+  const dim3 grid(a.ntiles, batch);
+  auto kern = ta_backward_kernel<KQ, kTlBwdThreads>;
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, int(cudaSharedmemCarveoutMaxShared));
+  if (e != cudaSuccess) return e;
+  kern<<<grid, kTlBwdThreads, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_prune_f32(const PruneArgs<float> &a, bool backward, int tile, int batch, int flags,
                              cudaStream_t stream) {
   if (tile != kTlTile) return cudaErrorInvalidValue;
   const bool pair_threads = flags & kF32PairThreads;
+  if (backward && !pair_threads && (flags & kF32InPlaceAdjoint)) {
+    switch (kpairs_for(a.K)) {
+      case 1: return launch_ta<1>(a, batch, stream);
+      case 2: return launch_ta<2>(a, batch, stream);
+      case 3: return launch_ta<3>(a, batch, stream);
+      default: return launch_ta<4>(a, batch, stream);
+    }
+  }
   if (!backward && !pair_threads && (flags & kF32ProducerWarp) && a.nstage <= 8) {
     switch (kpairs_for(a.K)) {
       case 1: return launch_tl_ws<1>(a, batch, stream);

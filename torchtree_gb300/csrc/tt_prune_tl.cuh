@@ -89,40 +89,42 @@ __host__ __device__ inline TlLayout tl_layout(int KQ, int C, int slots, int P, i
 
 // ------------------------------------------------------------ record ring
 // Producer-side ring of step records (one thread): records are bulk-copied in
-// chunks into two shared-memory slots one chunk ahead; `steps` is in issue
-// order.
-struct TlRecRing {
+// chunks of CH into two shared-memory slots one chunk ahead; `steps` is in
+// issue order.
+template <int CH>
+struct TlRecRingT {
   int4 *recs;
   uint64_t *bars;
   const int4 *steps;
   int count;
   unsigned long long timeout;
   __device__ __forceinline__ void load_chunk(int c) const {
-    if (c * kTlRecChunk >= count) return;
-    const int n = min(kTlRecChunk, count - c * kTlRecChunk);
+    if (c * CH >= count) return;
+    const int n = min(CH, count - c * CH);
     const uint32_t bytes = uint32_t(n) * 48;
     mbar_arrive_expect_tx(&bars[c & 1], bytes);
-    bulk_copy_g2s(recs + (c & 1) * kTlRecChunk * 3, steps + size_t(c) * kTlRecChunk * 3, bytes, &bars[c & 1]);
+    bulk_copy_g2s(recs + (c & 1) * CH * 3, steps + size_t(c) * CH * 3, bytes, &bars[c & 1]);
   }
   __device__ __forceinline__ bool get(int i, int4 (&r)[3]) const {
-    const int c = i / kTlRecChunk, o = i - c * kTlRecChunk;
+    const int c = i / CH, o = i - c * CH;
     if (o == 0 && !mbar_wait_bounded(&bars[c & 1], (c >> 1) & 1, timeout)) return false;
-    const int4 *src = recs + ((c & 1) * kTlRecChunk + o) * 3;
+    const int4 *src = recs + ((c & 1) * CH + o) * 3;
     r[0] = src[0];
     r[1] = src[1];
     r[2] = src[2];
-    if (o == kTlRecChunk - 1) {  // slot free again: order the reads before the refill
+    if (o == CH - 1) {  // slot free again: order the reads before the refill
       asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       load_chunk(c + 2);
     }
     return true;
   }
   __device__ __forceinline__ void drain(int next_issue) const {
-    const int c = next_issue / kTlRecChunk;
+    const int c = next_issue / CH;
     for (int d = 0; d < 2; ++d)
-      if ((c + d) * kTlRecChunk < count) mbar_wait_bounded(&bars[(c + d) & 1], ((c + d) >> 1) & 1, 100000000ull);
+      if ((c + d) * CH < count) mbar_wait_bounded(&bars[(c + d) & 1], ((c + d) >> 1) & 1, 100000000ull);
   }
 };
+using TlRecRing = TlRecRingT<kTlRecChunk>;
 
 // Stage step s of tile `tile`: record, matrix pairs, code rows of tip
 // children and (adjoint) the stored tiles of internal children.

@@ -146,7 +146,7 @@ class LikelihoodEngine:
         dpi = torch.empty(self.batch, self.state_count, dtype=torch.float64, device=self.device)
         dc = torch.empty(self.batch, self.category_count, dtype=torch.float64, device=self.device)
         check(self.lib.tt_gradient(self._plan, ptr(p), ptr(f), ptr(dP), ptr(dpi), ptr(dc), _stream()))
-        if self.state_count != 4:  # the wide-state adjoint consumes the stored partials
+        if self.state_count != 4 or self.precision == "f32":  # these adjoints consume the stored partials
             self.token += 1
         return dP, dpi, dc
 
