@@ -368,7 +368,7 @@ def main():
     import torch
     import torch.distributed as dist
 
-    from torchtree_gb300 import site_models, substitution
+    from torchtree_gb300 import _native, site_models, substitution
     from torchtree_gb300.engine import LikelihoodEngine
     from torchtree_gb300.likelihood import PhyloLikelihood, batch_inputs
 
@@ -461,6 +461,10 @@ def main():
     ntiles = -(-N // tile)
     design_fw = b * ((I - 1) * p_n + T * N + 8 * N)
     design_bw = b * ((I - 1) * p_n + T * N + 8 * N + (2 * T - 2) * ntiles * K * S * S * elem)
+    if S == 4 and args.precision == "f32" and eng.get_option(_native.TT_OPT_INPLACE_ADJOINT):
+        # outside partials stored over the post-order tiles: written once, read once
+        sched, _ = _native.schedule(T, wl.topology.postorder)
+        design_bw += b * 2 * int((sched[:, 9] & 1).sum()) * p_n
     peak, peak_kind = measured_peaks()
 
     def entry(ms, model, design):

@@ -9,18 +9,28 @@ namespace tt {
 
 namespace {
 
+// dynamic shared memory of a kernel, with the largest carveout so that the
+// CTAs the shared memory allows per SM are all resident
+template <typename F>
+cudaError_t set_smem(F kern, size_t smem) {
+  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, int(cudaSharedmemCarveoutMaxShared));
+  return e;
+}
+
 template <int KQ>
 cudaError_t launch_tl(const PruneArgs<float> &a, bool backward, int batch, cudaStream_t stream) {
   const size_t smem = tl_smem_bytes(a.K, a.C, a.slots, backward, a.nstage);
   const dim3 grid(a.ntiles, batch);
   if (backward) {
     auto kern = tl_backward_kernel<KQ, kTlBwdThreads>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaError_t e = set_smem(kern, smem);
     if (e != cudaSuccess) return e;
     kern<<<grid, kTlBwdThreads, smem, stream>>>(a);
   } else {
     auto kern = tl_forward_kernel<KQ, kTlFwdThreads, kTlTile / kTlFwdThreads>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaError_t e = set_smem(kern, smem);
     if (e != cudaSuccess) return e;
     kern<<<grid, kTlFwdThreads, smem, stream>>>(a);
   }
@@ -33,12 +43,12 @@ cudaError_t launch_tq(const PruneArgs<float> &a, bool backward, int batch, cudaS
   const dim3 grid(a.ntiles, batch);
   if (backward) {
     auto kern = tq_backward_kernel<KQ>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaError_t e = set_smem(kern, smem);
     if (e != cudaSuccess) return e;
     kern<<<grid, kTqTile * KQ, smem, stream>>>(a);
   } else {
     auto kern = tq_forward_kernel<KQ>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaError_t e = set_smem(kern, smem);
     if (e != cudaSuccess) return e;
     kern<<<grid, kTqTile * KQ, smem, stream>>>(a);
   }
@@ -62,7 +72,7 @@ cudaError_t launch_tl_ws(const PruneArgs<float> &a, int batch, cudaStream_t stre
   const size_t smem = tl_smem_bytes(a.K, a.C, a.slots, false, a.nstage);
   const dim3 grid(a.ntiles, batch);
   auto kern = tl_forward_ws_kernel<KQ, kTlTile>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaError_t e = set_smem(kern, smem);
   if (e != cudaSuccess) return e;
   kern<<<grid, kTlTile + 32, smem, stream>>>(a);
   return cudaGetLastError();
@@ -77,9 +87,7 @@ cudaError_t launch_ta(const PruneArgs<float> &a, int batch, cudaStream_t stream)
   const size_t smem = ta_smem_bytes(a.K, a.C, a.nstage);
   const dim3 grid(a.ntiles, batch);
   auto kern = ta_backward_kernel<KQ, kTlBwdThreads>;
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, int(cudaSharedmemCarveoutMaxShared));
+  cudaError_t e = set_smem(kern, smem);
   if (e != cudaSuccess) return e;
   kern<<<grid, kTlBwdThreads, smem, stream>>>(a);
   return cudaGetLastError();

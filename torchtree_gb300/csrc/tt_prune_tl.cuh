@@ -58,6 +58,9 @@ struct TlLayout {
 };
 
 constexpr int kTlRecChunk = 32;
+// CTAs per SM the producer-warp post-order's register budget is sized for:
+// six fit the shared memory of up to two category pairs
+__host__ __device__ constexpr int tl_ws_min_blocks(int KQ) { return KQ <= 2 ? 6 : 1; }
 
 
 // red2: float2 partial-block elements per thread of the adjoint's pattern reduction
@@ -457,7 +460,7 @@ __global__ void __launch_bounds__(NT) tl_forward_kernel(const PruneArgs<float> a
 // only its own pattern's stack entries, so the compute warps need no block
 // barrier per step and drift up to NSTAGE - 1 steps apart.
 template <int KQ, int NT>
-__global__ void __launch_bounds__(NT + 32) tl_forward_ws_kernel(const PruneArgs<float> a) {
+__global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ)) tl_forward_ws_kernel(const PruneArgs<float> a) {
   constexpr int P = NT;
   constexpr int NC = 2 * KQ;
   constexpr int NW = NT / 32;
