@@ -337,3 +337,67 @@ def test_pair_thread_kernels_match_one_thread_kernels():
             np.testing.assert_allclose(out[mode][0], out["stack"][0], rtol=1e-13)
             for a_, b_ in zip(out["stack"][1:], out[mode][1:]):
                 np.testing.assert_allclose(b_, a_, rtol=1e-5, atol=1e-5 * np.abs(a_).max())
+
+
+def _newick_shape(shape: str, T: int) -> str:
+    names = [f"t{i}" for i in range(T)]
+    if shape == "caterpillar":
+        s = names[0]
+        for n in names[1:]:
+            s = f"({s},{n})"
+        return s + ";"
+
+    def bal(xs):
+        if len(xs) == 1:
+            return xs[0]
+        h = len(xs) // 2
+        return f"({bal(xs[:h])},{bal(xs[h:])})"
+
+    return bal(names) + ";"
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("K", [1, 3, 5])
+@pytest.mark.parametrize("shape,T", [("balanced", 2), ("caterpillar", 3), ("balanced", 4), ("caterpillar", 50),
+                                     ("balanced", 64)])
+def test_fp32_adjoints_on_edge_trees(shape, T, K):
+    """FP32 adjoints against the FP64 engine on trees that drive the in-place
+    adjoint's paths: a root with tips only, carried children only (caterpillar),
+    a root with two cherries (one child stored in place), and a balanced tree
+    (half of all internal children stored); odd category counts pad a pair."""
+    from torchtree_gb300 import _native, patterns, site_models, substitution, synthetic
+    from torchtree_gb300.engine import LikelihoodEngine
+    from torchtree_gb300.tree import Topology
+
+    rng = np.random.default_rng(7 * T + K)
+    topo = Topology.from_newick(_newick_shape(shape, T))
+    pi = rng.dirichlet(np.ones(4))
+    exch = rng.dirichlet(np.ones(6))
+    q = synthetic.normalised_q_np(synthetic.gtr_q_np(exch, pi), pi)
+    rates_np = synthetic.discrete_gamma_np(0.6, K)
+    node_bl = np.concatenate([rng.exponential(0.2, 2 * T - 3), [0.0]])
+    seqs = synthetic.simulate_alignment(topo, node_bl, q, pi, rates_np, np.full(K, 1.0 / K), 700, rng)
+    ca = patterns.compress(seqs)
+    dev = torch.device("cuda")
+    b = 2
+    pit = torch.tensor(pi, dtype=torch.float64)
+    qt = substitution.gtr_q(torch.tensor(exch, dtype=torch.float64), pit)
+    lam, u, w = (t.expand(b, *t.shape).to(dev).contiguous() for t in substitution.eigen_system(qt, pit))
+    rates, probs = site_models.gamma_rates(torch.tensor([[0.6]] * b, dtype=torch.float64), K)
+    bls = torch.tensor(np.stack([node_bl, node_bl * 1.3]), dtype=torch.float64, device=dev)
+    eig = [lam, u, w, bls, rates.to(dev).contiguous()]
+    props, pid = probs.expand(b, K).to(dev).contiguous(), pit.to(dev)
+    out = {}
+    for name, precision, inplace in (("f64", "f64", None), ("f32", "f32", 1), ("f32_stack", "f32", 0)):
+        eng = LikelihoodEngine(topo.postorder, T, 4, K, ca.codes, ca.table, ca.weights, batch=b, precision=precision)
+        if inplace is not None:
+            eng.set_option(_native.TT_OPT_INPLACE_ADJOINT, inplace)
+        eng.set_eigen(*eig)
+        lnl = eng.log_likelihood(props, pid, rescale=precision == "f32", keep_partials=True)
+        dP, dpi, dc = eng.gradient(props, pid, want_matrices=True)
+        out[name] = [x.cpu().numpy() for x in (lnl, dP, dpi, dc)]
+    ref = out["f64"]
+    for name in ("f32", "f32_stack"):
+        np.testing.assert_allclose(out[name][0], ref[0], rtol=1e-6)
+        for got, want in zip(out[name][1:], ref[1:]):
+            np.testing.assert_allclose(got, want, rtol=1e-4, atol=1e-4 * np.abs(want).max())
