@@ -177,6 +177,10 @@ struct WideArgs {
   const double *log2L;      // [b][Npad] site log2-likelihoods (adjoint)
   T *gpart;                 // [b][B][nchunks][K][SP][SP]
   T *rootpart;              // [b][nchunks][K][SP + 1]
+  // the children's products P_l x_l, P_r x_r of every internal node as the
+  // post-order formed them, [b][I][K][2][SP][Npad], or nullptr: the adjoint
+  // reads them instead of recomputing them
+  T *prod;
 };
 
 // Stage a child's tile [SP][PT] (row stride XS): stored partial rows, or the
@@ -246,6 +250,14 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT) wide_forward_kernel(co
     V4<T>::ld(xs + SP * XS + j * XS + pb * 4, xc);
     outer4(al, pa, xa);
     outer4(ar, pc, xc);
+  }
+  if (a.prod) {
+    T *pd = a.prod + ((size_t(b) * a.I + (v - a.tips)) * a.K + k) * 2 * SP * size_t(a.Npad) + n0 + pb * 4;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) {
+      V4<T>::st(pd + size_t(ib + IB * i) * a.Npad, al[i]);
+      V4<T>::st(pd + size_t(SP + ib + IB * i) * a.Npad, ar[i]);
+    }
   }
 #pragma unroll
   for (int i = 0; i < 4; ++i)
@@ -340,7 +352,7 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT) wide_backward_kernel(c
   for (int e = tid; e < 2 * SP * SP; e += NT) {
     const int c = e / (SP * SP), ij = e - c * SP * SP, i = ij / SP, j = ij - i * SP;
     const T val = a.pmat[((size_t(b) * a.B + (c ? r : l)) * a.K + k) * SP * SP + ij];
-    plt[c * SP * SP + j * SP + wperm<IB>(i)] = val;
+    if (!a.prod) plt[c * SP * SP + j * SP + wperm<IB>(i)] = val;
     pl[c * SP * SP + i * SP + wperm<IB>(j)] = val;
   }
   // GEMM3 ownership: block (gi, gj) of the SP x SP gradient, pattern quads grp, grp + NG, ...
@@ -391,19 +403,29 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT) wide_backward_kernel(c
     __syncthreads();
 
     T al[4][4], ar[4][4];
+    if (a.prod) {  // the post-order's products
+      const T *pd =
+          a.prod + ((size_t(b) * a.I + (v - a.tips)) * a.K + k) * 2 * SP * size_t(a.Npad) + n0 + pb * 4;
 #pragma unroll
-    for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < 4; ++i) {
+        V4<T>::ldg(pd + size_t(ib + IB * i) * a.Npad, al[i]);
+        V4<T>::ldg(pd + size_t(SP + ib + IB * i) * a.Npad, ar[i]);
+      }
+    } else {
 #pragma unroll
-      for (int q = 0; q < 4; ++q) al[i][q] = ar[i][q] = T(0);
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int q = 0; q < 4; ++q) al[i][q] = ar[i][q] = T(0);
 #pragma unroll 4
-    for (int j = 0; j < SP; ++j) {
-      T pa[4], pc[4], xa[4], xc[4];
-      V4<T>::ld(plt + j * SP + ib * 4, pa);
-      V4<T>::ld(plt + SP * SP + j * SP + ib * 4, pc);
-      V4<T>::ld(xs + j * XS + pb * 4, xa);
-      V4<T>::ld(xs + SP * XS + j * XS + pb * 4, xc);
-      outer4(al, pa, xa);
-      outer4(ar, pc, xc);
+      for (int j = 0; j < SP; ++j) {
+        T pa[4], pc[4], xa[4], xc[4];
+        V4<T>::ld(plt + j * SP + ib * 4, pa);
+        V4<T>::ld(plt + SP * SP + j * SP + ib * 4, pc);
+        V4<T>::ld(xs + j * XS + pb * 4, xa);
+        V4<T>::ld(xs + SP * XS + j * XS + pb * 4, xc);
+        outer4(al, pa, xa);
+        outer4(ar, pc, xc);
+      }
     }
     if (is_root) {
 #pragma unroll

@@ -230,16 +230,25 @@ __global__ void __launch_bounds__(tc::kThreads, 1) wide_forward_tc_kernel(const 
   } else {
     // this thread's pattern = TMEM lane 32 * warp + lane
     const uint32_t lane_addr = tmem + (uint32_t(32 * warp) << 16);
+    const int n = n0 + tid;
+    float *pd = a.prod ? a.prod + ((size_t(b) * a.I + (v - a.tips)) * a.K + k) * 2 * SP * size_t(a.Npad) + n
+                       : nullptr;
     float L[64];
 #pragma unroll
     for (int h = 0; h < 2; ++h) {
       float dl[32], dr[32];
       tc::tmem_ld32(lane_addr + uint32_t(32 * h), dl);
       tc::tmem_ld32(lane_addr + uint32_t(64 + 32 * h), dr);
+      if (pd) {  // the children's products for the adjoint
+#pragma unroll
+        for (int i = 0; i < 32; ++i) {
+          pd[size_t(32 * h + i) * a.Npad] = dl[i];
+          pd[size_t(SP + 32 * h + i) * a.Npad] = dr[i];
+        }
+      }
 #pragma unroll
       for (int i = 0; i < 32; ++i) L[32 * h + i] = dl[i] * dr[i];
     }
-    const int n = n0 + tid;
     const int El = wide_child_expo(a, l, b, k, n), Er = wide_child_expo(a, r, b, k, n);
     if (is_root) {
       double s = 0.0;

@@ -133,7 +133,8 @@ def estimate_bytes(ds: Dataset, slots: int, precision: str) -> int:
         return int(1.1 * (part + grad + slots * B * kp * S * S * elem + T * npad)) + (64 << 20)
     sp = 20 if S <= 20 else 64
     npad = -(-N // 128) * 128
-    part = slots * T * K * npad * (sp * elem + 4)
+    # partials and exponents; FP32 codon plans also keep the children's products (2 rows per state)
+    part = slots * T * K * npad * (sp * elem * (3 if precision == "f32" and sp == 64 else 1) + 4)
     chunks = min(64, max(1, -(-304 // (slots * K))))
     grad = slots * B * K * sp * sp * (chunks * elem + elem + 8)
     return int(1.1 * (part + grad + T * npad)) + (64 << 20)
