@@ -120,6 +120,9 @@ struct Wide {
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(wide_backward_kernel<T, SP, PTB>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                int(wide_bwd_smem<T, SP, PTB>()));
+    if (e == cudaSuccess)  // the CTAs the shared memory allows per SM all resident
+      e = cudaFuncSetAttribute(wide_backward_kernel<T, SP, PTB>, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               int(cudaSharedmemCarveoutMaxShared));
     if (std::is_same<T, float>::value && SP == 64 && e == cudaSuccess)
       e = cudaFuncSetAttribute(wide_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::kSmem);
     if (e == cudaSuccess)
@@ -200,7 +203,7 @@ struct Wide {
     WideArgs<T> a = args(p, props, freqs, 1);
     a.prod = static_cast<T *>(w.d_prod);
     constexpr int NT = WideCfg<T, SP, PTB>::NT;
-    const size_t smem = wide_bwd_smem<T, SP, PTB>();
+    const size_t smem = wide_bwd_smem<T, SP, PTB>(a.prod != nullptr);
     for (size_t lv = 0; lv + 1 < w.bwd_off.size(); ++lv) {
       a.nodes = w.d_bwd + w.bwd_off[lv];
       const dim3 grid(w.nchunks, w.bwd_off[lv + 1] - w.bwd_off[lv], p->batch * p->K);

@@ -53,10 +53,12 @@ constexpr size_t wide_fwd_smem() {
   using C = WideCfg<T, SP, PT>;
   return sizeof(T) * (2 * SP * SP + 2 * SP * C::XS) + sizeof(double) * C::IB * PT + sizeof(int) * PT;
 }
+// (stored_products: the adjoint reads the post-order's products and keeps no P^T)
 template <typename T, int SP, int PT>
-constexpr size_t wide_bwd_smem() {
+constexpr size_t wide_bwd_smem(bool stored_products = false) {
   using C = WideCfg<T, SP, PT>;
-  return sizeof(T) * (4 * SP * SP + 3 * SP * C::XS + PT) + sizeof(double) * C::IB * PT + sizeof(int) * 4 * PT;
+  return sizeof(T) * ((stored_products ? 2 : 4) * SP * SP + 3 * SP * C::XS + PT) + sizeof(double) * C::IB * PT +
+         sizeof(int) * 4 * PT;
 }
 
 template <int IB>
@@ -328,13 +330,21 @@ __global__ void wide_root_kernel(const double *root_site, const int *root_expo, 
                                  int K, int N, int Npad);
 
 // --------------------------------------------------------------- adjoint
+// CTAs per SM the adjoint's registers are sized for: FP32 codon plans read
+// the stored products and need no transposed matrices, so two CTAs fit
+template <typename T, int SP>
+__host__ __device__ constexpr int wide_bwd_min_blocks() {
+  return sizeof(T) == 4 && SP == 64 ? 2 : 1;
+}
+
 template <typename T, int SP, int PT>
-__global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT) wide_backward_kernel(const WideArgs<T> a) {
+__global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT, wide_bwd_min_blocks<T, SP>())
+    wide_backward_kernel(const WideArgs<T> a) {
   using C = WideCfg<T, SP, PT>;
   constexpr int IB = C::IB, NT = C::NT, XS = C::XS, NG = C::NG, GB = C::GB;
   extern __shared__ __align__(128) unsigned char smem[];
-  T *plt = reinterpret_cast<T *>(smem);  // [2][SP j][SP perm i]   P^T (GEMM1)
-  T *pl = plt + 2 * SP * SP;             // [2][SP i][SP perm j]   P   (GEMM2)
+  T *plt = reinterpret_cast<T *>(smem);               // [2][SP j][SP perm i]   P^T (GEMM1, absent with a.prod)
+  T *pl = a.prod ? plt : plt + 2 * SP * SP;           // [2][SP i][SP perm j]   P   (GEMM2)
   T *xs = pl + 2 * SP * SP;              // [2][SP][XS] child tiles
   T *us = xs + 2 * SP * XS;              // [SP][XS]    u of the current side
   T *cf = us + SP * XS;                  // [PT]        coefficients
