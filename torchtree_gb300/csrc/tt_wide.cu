@@ -125,6 +125,9 @@ struct Wide {
                                int(cudaSharedmemCarveoutMaxShared));
     if (std::is_same<T, float>::value && SP == 64 && e == cudaSuccess)
       e = cudaFuncSetAttribute(wide_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::kSmem);
+    if (std::is_same<T, float>::value && SP == 64 && e == cudaSuccess)  // two CTAs per SM
+      e = cudaFuncSetAttribute(wide_forward_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               int(cudaSharedmemCarveoutMaxShared));
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(wide_pmatrix_kernel<T, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                int(2 * SP * SP * sizeof(T) + SP * sizeof(double)));

@@ -13,6 +13,9 @@
 // 8 rows SBO = 128 B further, the next 4 K-elements LBO further.
 //   A (x^T, 128 x 64): LBO = 2048 B,  one MMA K-step (8 elements) = 4096 B
 //   B (P,    64 x 64): LBO = 1024 B,  one MMA K-step               = 2048 B
+// The two sides are staged one after the other in the same 96 KB (the
+// second once the first side's MMAs have completed), so that two CTAs fit
+// per SM and one CTA's staging overlaps the other's MMAs and epilogue.
 // After the MMAs complete (tcgen05.commit -> mbarrier, bounded wait) each
 // thread loads its pattern's 64 + 64 accumulators with tcgen05.ld, forms
 // the product, rescales by the power of two of its maximum and stores the
@@ -29,14 +32,11 @@ constexpr int kPT = 128;                 // patterns per CTA (MMA M)
 constexpr int kThreads = 128;
 constexpr int kAbytes = 128 * 64 * 4;    // one A operand (big or small)
 constexpr int kBbytes = 64 * 64 * 4;     // one B operand
-// shared memory: [B: Pl big, Pl small, Pr big, Pr small][A: xl big, xl small, xr big, xr small][barrier, tmem slot]
+// shared memory (one side at a time): [B: P big, P small][A: x big, x small][barrier, tmem slot]
 constexpr int kOffB = 0;
-constexpr int kOffA = 4 * kBbytes;
-constexpr int kOffBar = kOffA + 4 * kAbytes;
-// the allocation is padded so that every descriptor's reach stays inside it
-// for either reading of the leading / stride offsets
-constexpr int kSmem = 224 * 1024;
-static_assert(kOffBar + 64 <= kSmem, "shared-memory layout");
+constexpr int kOffA = 2 * kBbytes;
+constexpr int kOffBar = kOffA + 2 * kAbytes;
+constexpr int kSmem = kOffBar + 64;
 constexpr uint32_t kTmemCols = 128;
 
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
@@ -118,7 +118,7 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 }  // namespace tc
 
 // Post-order level kernel for FP32 codon plans on the tensor cores.
-__global__ void __launch_bounds__(tc::kThreads, 1) wide_forward_tc_kernel(const WideArgs<float> a, int *status,
+__global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const WideArgs<float> a, int *status,
                                                                          unsigned long long timeout_ns) {
   constexpr int SP = 64;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -138,79 +138,77 @@ __global__ void __launch_bounds__(tc::kThreads, 1) wide_forward_tc_kernel(const 
     mbar_init(bar, 1);
     fence_barrier_init();
   }
-  // B operands: P_c[i][j], N = i, K = j
-  // B operands: P_c[i][j], N = i, K = j.  Sixteen 16-byte loads per thread are
-  // issued before any is used (latency), then split and stored as float4.
-  {
-    float4 pv[16];
-#pragma unroll
-    for (int m = 0; m < 16; ++m) {
-      const int e4 = tid + m * tc::kThreads;  // float4 index over both sides: 2 * 64 * 16
-      const int c = e4 >> 10, f = (e4 & 1023) * 4, i = f / SP;
-      pv[m] = __ldg(reinterpret_cast<const float4 *>(
-          a.pmat + ((size_t(b) * a.B + (c ? r : l)) * a.K + k) * SP * SP + (f - i * SP) + i * SP));
-    }
-#pragma unroll
-    for (int m = 0; m < 16; ++m) {
-      const int e4 = tid + m * tc::kThreads;
-      const int c = e4 >> 10, f = (e4 & 1023) * 4, i = f / SP, j = f - i * SP;
-      float4 hb, hs;
-      tc::split_tf32(pv[m].x, hb.x, hs.x);
-      tc::split_tf32(pv[m].y, hb.y, hs.y);
-      tc::split_tf32(pv[m].z, hb.z, hs.z);
-      tc::split_tf32(pv[m].w, hb.w, hs.w);
-      const uint32_t off = tc::kmajor_off(i, j, 1024);
-      *reinterpret_cast<float4 *>(sB + (2 * c) * tc::kBbytes + off) = hb;
-      *reinterpret_cast<float4 *>(sB + (2 * c + 1) * tc::kBbytes + off) = hs;
-    }
-  }
-  // A operands: x_c^T, M = pattern (this thread's), K = j; all 64 loads of a
-  // side in flight before the split, four j per 16-byte store
-#pragma unroll
-  for (int c = 0; c < 2; ++c) {
+  // per side c: stage, then one thread issues the side's MMAs into TMEM
+  // columns [64c, 64c + 64); the next side's staging waits for their completion
+  bool ok = true;
+  int phase = 0;
+  uint32_t tmem = 0;  // read from the slot after the first barrier
+  for (int c = 0; c < 2 && ok; ++c) {
     const int child = c ? r : l;
-    unsigned char *abig = sA + (2 * c) * tc::kAbytes, *asmall = sA + (2 * c + 1) * tc::kAbytes;
-    float xv[SP];
-    if (child < a.tips) {
-      const int code = a.codes[size_t(child) * a.code_stride + n0 + tid];
-      const float4 *row = reinterpret_cast<const float4 *>(a.table + size_t(code) * SP);
+    // B operand: P_c[i][j], N = i, K = j; eight 16-byte loads per thread in
+    // flight before the split
+    {
+      float4 pv[8];
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const int f = (tid + m * tc::kThreads) * 4, i = f / SP;
+        pv[m] = __ldg(reinterpret_cast<const float4 *>(
+            a.pmat + ((size_t(b) * a.B + child) * a.K + k) * SP * SP + (f - i * SP) + i * SP));
+      }
+#pragma unroll
+      for (int m = 0; m < 8; ++m) {
+        const int f = (tid + m * tc::kThreads) * 4, i = f / SP, j = f - i * SP;
+        float4 hb, hs;
+        tc::split_tf32(pv[m].x, hb.x, hs.x);
+        tc::split_tf32(pv[m].y, hb.y, hs.y);
+        tc::split_tf32(pv[m].z, hb.z, hs.z);
+        tc::split_tf32(pv[m].w, hb.w, hs.w);
+        const uint32_t off = tc::kmajor_off(i, j, 1024);
+        *reinterpret_cast<float4 *>(sB + off) = hb;
+        *reinterpret_cast<float4 *>(sB + tc::kBbytes + off) = hs;
+      }
+    }
+    // A operand: x_c^T, M = pattern (this thread's), K = j; all 64 loads in
+    // flight before the split, four j per 16-byte store
+    {
+      float xv[SP];
+      if (child < a.tips) {
+        const int code = a.codes[size_t(child) * a.code_stride + n0 + tid];
+        const float4 *row = reinterpret_cast<const float4 *>(a.table + size_t(code) * SP);
+#pragma unroll
+        for (int j = 0; j < SP; j += 4) {
+          const float4 t4 = __ldg(row + j / 4);
+          xv[j] = t4.x, xv[j + 1] = t4.y, xv[j + 2] = t4.z, xv[j + 3] = t4.w;
+        }
+      } else {
+        const float *src =
+            a.part + ((size_t(b) * a.I + (child - a.tips)) * a.K + k) * SP * size_t(a.Npad) + n0 + tid;
+#pragma unroll
+        for (int j = 0; j < SP; ++j) xv[j] = __ldg(src + size_t(j) * a.Npad);
+      }
 #pragma unroll
       for (int j = 0; j < SP; j += 4) {
-        const float4 t4 = __ldg(row + j / 4);
-        xv[j] = t4.x, xv[j + 1] = t4.y, xv[j + 2] = t4.z, xv[j + 3] = t4.w;
+        float4 hb, hs;
+        tc::split_tf32(xv[j], hb.x, hs.x);
+        tc::split_tf32(xv[j + 1], hb.y, hs.y);
+        tc::split_tf32(xv[j + 2], hb.z, hs.z);
+        tc::split_tf32(xv[j + 3], hb.w, hs.w);
+        const uint32_t off = tc::kmajor_off(tid, j, 2048);
+        *reinterpret_cast<float4 *>(sA + off) = hb;
+        *reinterpret_cast<float4 *>(sA + tc::kAbytes + off) = hs;
       }
-    } else {
-      const float *src = a.part + ((size_t(b) * a.I + (child - a.tips)) * a.K + k) * SP * size_t(a.Npad) + n0 + tid;
-#pragma unroll
-      for (int j = 0; j < SP; ++j) xv[j] = __ldg(src + size_t(j) * a.Npad);
     }
-#pragma unroll
-    for (int j = 0; j < SP; j += 4) {
-      float4 hb, hs;
-      tc::split_tf32(xv[j], hb.x, hs.x);
-      tc::split_tf32(xv[j + 1], hb.y, hs.y);
-      tc::split_tf32(xv[j + 2], hb.z, hs.z);
-      tc::split_tf32(xv[j + 3], hb.w, hs.w);
-      const uint32_t off = tc::kmajor_off(tid, j, 2048);
-      *reinterpret_cast<float4 *>(abig + off) = hb;
-      *reinterpret_cast<float4 *>(asmall + off) = hs;
-    }
-  }
-  // generic-proxy writes -> visible to the tensor cores (async proxy)
-  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-  tc::fence_before_sync();
-  __syncthreads();
-  tc::fence_after_sync();
-  const uint32_t tmem = *tslot;
-
-  if (tid == 0) {
-    constexpr uint32_t idesc = tc::idesc_tf32(128, 64);
-    const uint32_t a0 = smem_u32(sA), b0 = smem_u32(sB);
-#pragma unroll
-    for (int c = 0; c < 2; ++c) {
+    // generic-proxy writes -> visible to the tensor cores (async proxy)
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+    tc::fence_before_sync();
+    __syncthreads();
+    tc::fence_after_sync();
+    tmem = *tslot;
+    if (tid == 0) {
+      constexpr uint32_t idesc = tc::idesc_tf32(128, 64);
       const uint32_t d = tmem + uint32_t(64 * c);
-      const uint32_t ab = a0 + (2 * c) * tc::kAbytes, as = ab + tc::kAbytes;
-      const uint32_t bb = b0 + (2 * c) * tc::kBbytes, bs = bb + tc::kBbytes;
+      const uint32_t ab = smem_u32(sA), as = ab + tc::kAbytes;
+      const uint32_t bb = smem_u32(sB), bs = bb + tc::kBbytes;
 #pragma unroll
       for (int kk = 0; kk < SP / 8; ++kk) {
         const uint64_t dab = tc::smem_desc(ab + kk * 4096, 2048, 128), das = tc::smem_desc(as + kk * 4096, 2048, 128);
@@ -219,14 +217,17 @@ __global__ void __launch_bounds__(tc::kThreads, 1) wide_forward_tc_kernel(const 
         tc::mma_tf32(d, dab, dbs, idesc, 1u);
         tc::mma_tf32(d, das, dbb, idesc, 1u);
       }
+      tc::mma_commit(bar);
     }
-    tc::mma_commit(bar);
+    // every thread sees the side's MMAs complete before the shared memory is restaged or TMEM read
+    ok = mbar_wait_bounded(bar, phase, timeout_ns);
+    tc::fence_after_sync();
+    ok = !__syncthreads_or(!ok);
+    if (ok) phase ^= 1;
   }
-  const bool ok = mbar_wait_bounded(bar, 0, timeout_ns);
-  tc::fence_after_sync();
   if (!ok) {
     if (tid == 0) atomicExch(status, kDeviceTimeout);
-    mbar_wait_bounded(bar, 0, 100000000ull);  // give the tensor cores a last chance before freeing TMEM
+    mbar_wait_bounded(bar, phase, 100000000ull);  // give the tensor cores a last chance before freeing TMEM
   } else {
     // this thread's pattern = TMEM lane 32 * warp + lane
     const uint32_t lane_addr = tmem + (uint32_t(32 * warp) << 16);
