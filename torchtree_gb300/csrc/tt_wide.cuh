@@ -253,7 +253,7 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT) wide_forward_kernel(co
     outer4(al, pa, xa);
     outer4(ar, pc, xc);
   }
-  if (a.prod) {
+  if (sizeof(T) == 4 && SP == 64 && a.prod) {
     T *pd = a.prod + ((size_t(b) * a.I + (v - a.tips)) * a.K + k) * 2 * SP * size_t(a.Npad) + n0 + pb * 4;
 #pragma unroll
     for (int i = 0; i < 4; ++i) {
@@ -330,11 +330,12 @@ __global__ void wide_root_kernel(const double *root_site, const int *root_expo, 
                                  int K, int N, int Npad);
 
 // --------------------------------------------------------------- adjoint
-// CTAs per SM the adjoint's registers are sized for: FP32 codon plans read
-// the stored products and need no transposed matrices, so two CTAs fit
+// CTAs per SM the adjoint's registers are sized for: two for FP32 plans
+// (codon plans read the stored products and keep no transposed matrices, so
+// two fit the shared memory too)
 template <typename T, int SP>
 __host__ __device__ constexpr int wide_bwd_min_blocks() {
-  return sizeof(T) == 4 && SP == 64 ? 2 : 1;
+  return sizeof(T) == 4 ? 2 : 1;
 }
 
 template <typename T, int SP, int PT>
@@ -343,8 +344,11 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT, wide_bwd_min_blocks<T,
   using C = WideCfg<T, SP, PT>;
   constexpr int IB = C::IB, NT = C::NT, XS = C::XS, NG = C::NG, GB = C::GB;
   extern __shared__ __align__(128) unsigned char smem[];
-  T *plt = reinterpret_cast<T *>(smem);               // [2][SP j][SP perm i]   P^T (GEMM1, absent with a.prod)
-  T *pl = a.prod ? plt : plt + 2 * SP * SP;           // [2][SP i][SP perm j]   P   (GEMM2)
+  // stored products: FP32 codon plans only (the other instantiations keep GEMM1)
+  constexpr bool kProd = sizeof(T) == 4 && SP == 64;
+  const bool prod = kProd && a.prod != nullptr;
+  T *plt = reinterpret_cast<T *>(smem);       // [2][SP j][SP perm i]   P^T (GEMM1, absent with stored products)
+  T *pl = prod ? plt : plt + 2 * SP * SP;     // [2][SP i][SP perm j]   P   (GEMM2)
   T *xs = pl + 2 * SP * SP;              // [2][SP][XS] child tiles
   T *us = xs + 2 * SP * XS;              // [SP][XS]    u of the current side
   T *cf = us + SP * XS;                  // [PT]        coefficients
@@ -362,7 +366,7 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT, wide_bwd_min_blocks<T,
   for (int e = tid; e < 2 * SP * SP; e += NT) {
     const int c = e / (SP * SP), ij = e - c * SP * SP, i = ij / SP, j = ij - i * SP;
     const T val = a.pmat[((size_t(b) * a.B + (c ? r : l)) * a.K + k) * SP * SP + ij];
-    if (!a.prod) plt[c * SP * SP + j * SP + wperm<IB>(i)] = val;
+    if (!prod) plt[c * SP * SP + j * SP + wperm<IB>(i)] = val;
     pl[c * SP * SP + i * SP + wperm<IB>(j)] = val;
   }
   // GEMM3 ownership: block (gi, gj) of the SP x SP gradient, pattern quads grp, grp + NG, ...
@@ -413,7 +417,7 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT, wide_bwd_min_blocks<T,
     __syncthreads();
 
     T al[4][4], ar[4][4];
-    if (a.prod) {  // the post-order's products
+    if (prod) {  // the post-order's products
       const T *pd =
           a.prod + ((size_t(b) * a.I + (v - a.tips)) * a.K + k) * 2 * SP * size_t(a.Npad) + n0 + pb * 4;
 #pragma unroll
