@@ -60,6 +60,10 @@ def parse():
     ap.add_argument("--serving-slots", type=int, default=4)
     ap.add_argument("--serving-max-tips", type=int, default=2000)
     ap.add_argument("--serving-max-sites", type=int, default=50000)
+    ap.add_argument("--timetree", action="store_true",
+                    help="time-tree prior step instead: node-height ratio transform with log|det J| and the "
+                         "constant-size coalescent, values and gradients, for a batch of samples")
+    ap.add_argument("--timetree-cpu-batch", type=int, default=32, help="samples in the CPU oracle's sample")
     return ap.parse_args()
 
 
@@ -357,6 +361,127 @@ def run_serving(args):
     print(json.dumps(line), flush=True)
 
 
+def run_timetree(args):
+    """Time-tree prior step for a batch of samples: ratios -> internal heights,
+    branch lengths and log|det J| (tree_height_transform.py:7-99), the
+    constant-size coalescent log-density of the heights (coalescent.py:86-134),
+    and the gradient of log p + log|det J| with respect to the ratios and the
+    population size.  The reference times the same operations one sample at a
+    time (benchmarks/benchmark.py:441-789)."""
+    import torch
+
+    from torchtree_gb300 import synthetic
+    from torchtree_gb300.timetree import TimeTree
+
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dev = torch.device("cuda", local)
+    rng = np.random.default_rng(11)
+    T = args.tips or 1000
+    b = args.batch or 16384
+    topo = synthetic.yule_topology(T, rng)
+    times = rng.uniform(0.0, 5.0, T)  # heterochronous tips (sampling times before the present)
+    lb = np.zeros(T - 1)
+    for v, l, r in topo.postorder:
+        lb[v - T] = max(times[l] if l < T else lb[l - T], times[r] if r < T else lb[r - T])
+    x_host = rng.uniform(0.05, 0.95, (b, T - 1))
+    x_host[:, T - 2] = lb[T - 2] + rng.exponential(5.0, b)  # root height above its lower bound
+    th_host = rng.lognormal(1.0, 0.3, b)
+    tree = TimeTree(topo.postorder, times)
+    x = torch.tensor(x_host, device=dev)
+    th = torch.tensor(th_host, device=dev)
+
+    def step(xx, tt):
+        xx = xx.detach().requires_grad_()
+        tt = tt.detach().requires_grad_()
+        h, bl, ld = tree.ratio_transform(xx)
+        lp = tree.constant_coalescent(h, tt)
+        total = lp + ld
+        gx, gth = torch.autograd.grad(total.sum(), (xx, tt))
+        return total, gx, gth
+
+    for _ in range(max(args.warmup, 3)):
+        step(x, th)
+    torch.cuda.synchronize()
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps + 1)]
+    with ClockSampler(local) as clocks:
+        ev[0].record(stream)
+        for i in range(args.steps):
+            step(x, th)
+            ev[i + 1].record(stream)
+        torch.cuda.synchronize()
+    total_ms = ev[0].elapsed_time(ev[-1])
+    per = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
+    value = b * args.steps / (total_ms / 1e3)
+    # per-kernel times (the C-ABI calls on the stream)
+    e = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    xx = x.detach().requires_grad_()
+    e[0].record(stream)
+    h, bl, ld = tree.ratio_transform(xx)
+    e[1].record(stream)
+    lp = tree.constant_coalescent(h, th)
+    e[2].record(stream)
+    torch.autograd.grad((lp + ld).sum(), xx)
+    e[3].record(stream)
+    torch.cuda.synchronize()
+    k_ms = {"ratio_transform": e[0].elapsed_time(e[1]), "constant_coalescent": e[1].elapsed_time(e[2]),
+            "backward": e[2].elapsed_time(e[3])}
+    # end to end: host ratios and population sizes in (pinned), values and gradients out
+    xp, tp = torch.tensor(x_host).pin_memory(), torch.tensor(th_host).pin_memory()
+    outs = [torch.empty(b, dtype=torch.float64).pin_memory(), torch.empty(b, T - 1, dtype=torch.float64).pin_memory(),
+            torch.empty(b, dtype=torch.float64).pin_memory()]
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        res = step(xp.to(dev, non_blocking=True), tp.to(dev, non_blocking=True))
+        for o, r in zip(outs, res):
+            o.copy_(r, non_blocking=True)
+        torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    # CPU oracle (torch FP64 + autograd, all host threads) on a sample of the batch
+    from oracle import timetree as OT
+
+    nb = min(args.timetree_cpu_batch, b)
+    xc = torch.tensor(x_host[:nb]).requires_grad_()
+    tc_ = torch.tensor(th_host[:nb]).requires_grad_()
+    t1 = time.perf_counter()
+    hc, _, ldc = OT.ratio_transform(topo.postorder_list(), list(times), xc)
+    lpc = OT.constant_coalescent(list(times), hc, tc_)
+    gxc, _ = torch.autograd.grad((lpc + ldc).sum(), (xc, tc_))
+    cpu_s = time.perf_counter() - t1
+    res = step(x[:nb], th[:nb])
+    check = float(torch.max(torch.abs(res[0].cpu() - (lpc + ldc).detach())))
+    I = T - 1
+    # bytes a launch sequence must move per sample: ratios in, heights / branch
+    # lengths out (ratio transform); heights in, height gradients out
+    # (coalescent); ratios, heights and the three incoming gradients in, ratio
+    # gradients out (backward)
+    per_sample = 8 * (I + I + (2 * T - 2) + 1) + 8 * (I + I + 2) + 8 * (I + I + I + (2 * T - 2) + 1 + I)
+    peak, peak_kind = measured_peaks()
+    achieved = per_sample * b / (sum(k_ms.values()) / 1e3) / 1e9
+    line = {
+        "metric": "time-tree prior evals/s: ratio transform + log|det J| + constant coalescent, values and gradients",
+        "value": value, "unit": "samples/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": total_ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f64", "data": "synthetic (seeded Yule tree, uniform tip dates, uniform ratios)",
+        "config": {"workload": f"timetree_t{T}_b{b}", "tips": T, "batch": b,
+                   "l2": f"inputs {b * I * 8 / 1e6:.0f} MB per tensor; no flush"},
+        "latency_ms": {"p50": float(np.percentile(per, 50)), "p99": float(np.percentile(per, 99))},
+        "kernels_ms": k_ms,
+        "roofline": {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                     "peak_source": peak_kind, "traffic": None, "per_launch_bytes": per_sample * b},
+        "cpu_baseline": {"value": nb / cpu_s, "unit": "samples/s", "cores": torch.get_num_threads(), "kind": "port",
+                         "sample": f"{nb} samples of the same tree and inputs (oracle: torch FP64 + autograd)",
+                         "max_abs_diff": check},
+        "e2e": {"value": b * args.steps / e2e_s, "unit": "samples/s",
+                "h2d_bytes_per_step": int(xp.numel() * 8 + tp.numel() * 8),
+                "d2h_bytes_per_step": int(sum(o.numel() for o in outs) * 8)},
+        "gpu_launches": 3, "clocks": clocks.summary(),
+    }
+    print(json.dumps(line), flush=True)
+
+
 def main():
     args = parse()
     if args.impl == "reference":
@@ -364,6 +489,9 @@ def main():
         return
     if args.serving:
         run_serving(args)
+        return
+    if args.timetree:
+        run_timetree(args)
         return
     import torch
     import torch.distributed as dist

@@ -124,26 +124,51 @@ __global__ void coalescent_kernel(const double *times, const double *hint, const
       }
       __syncthreads();
     }
-  // lineages after position i: (#tips at or before i) - (#internal at or before i); a
-  // sequential scan by one thread keeps the summation order fixed
-  const double th = theta[b];
+  // Lineages through sorted position p: L_p = (#tips at or before p) - (#internal
+  // nodes at or before p), a block-wide prefix sum over contiguous chunks of
+  // positions.  With c_p = L_p (L_p - 1) / 2 for p < n - 1 (0 at the last):
+  //   log p = -sum_p c_p (t_{p+1} - t_p) / theta - (T - 1) log theta,
+  //   d/dt_p = (c_p - c_{p-1}) / theta  (each internal node written once),
+  //   d/dtheta = sum_p c_p (t_{p+1} - t_p) / theta^2 - (T - 1) / theta.
+  // The sum runs in a fixed order (per-thread chunks, then warps, then warp totals).
+  const double th = theta[b], inv_th = 1.0 / th;
+  const int E = (n + NT - 1) / NT;
+  const int p0 = min(n, tid * E), p1 = min(n, p0 + E);
+  int dsum = 0;
+  for (int p = p0; p < p1; ++p) dsum += idx[p] < T ? 1 : -1;
+  const int lane = tid & 31, warp = tid >> 5, NW = (NT + 31) >> 5;
+  int incl = dsum;  // inclusive warp scan
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int y = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += y;
+  }
+  __shared__ int wsum[32];
+  __shared__ double wacc[32];
+  if (lane == 31) wsum[warp] = incl;
+  __syncthreads();
+  int off = incl - dsum;
+  for (int w = 0; w < warp; ++w) off += wsum[w];
+  int L = off;
+  double c_prev = 0.5 * double(off) * double(off - 1);  // c_{p0 - 1} (0 before the first position)
+  if (p0 == 0) c_prev = 0.0;
+  double acc = 0.0;
+  for (int p = p0; p < p1; ++p) {
+    L += idx[p] < T ? 1 : -1;
+    const double c = p < n - 1 ? 0.5 * double(L) * double(L - 1) : 0.0;
+    if (p < n - 1) acc = fma(c, key[p + 1] - key[p], acc);
+    if (gh && idx[p] >= T) gh[size_t(b) * I + idx[p] - T] = (c - c_prev) * inv_th;
+    c_prev = c;
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, o);
+  if (lane == 0) wacc[warp] = acc;
+  __syncthreads();
   if (tid == 0) {
-    int lineages = 0;
-    double s = 0.0, dth = 0.0;
-    for (int i = 0; i + 1 < n; ++i) {
-      lineages += idx[i] < T ? 1 : -1;
-      const double c = 0.5 * double(lineages) * double(lineages - 1);
-      const double dur = key[i + 1] - key[i];
-      s -= c * dur / th;
-      dth += c * dur / (th * th);
-      // d/dt_(i+1) = -c/theta, d/dt_i = +c/theta, scattered to the internal nodes
-      if (gh) {
-        if (idx[i + 1] >= T) gh[size_t(b) * I + idx[i + 1] - T] -= c / th;
-        if (idx[i] >= T) gh[size_t(b) * I + idx[i] - T] += c / th;
-      }
-    }
-    logp[b] = s - double(T - 1) * log(th);
-    if (gtheta) gtheta[b] = dth - double(T - 1) / th;
+    double total = 0.0;
+    for (int w = 0; w < NW; ++w) total += wacc[w];
+    logp[b] = -total * inv_th - double(T - 1) * log(th);
+    if (gtheta) gtheta[b] = total * inv_th * inv_th - double(T - 1) * inv_th;
   }
 }
 
@@ -249,9 +274,7 @@ int tt_constant_coalescent(tt_time_tree *t, int32_t batch, const double *heights
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t smem = size_t(n2) * (sizeof(double) + sizeof(int));
   cudaError_t e = cudaFuncSetAttribute(coalescent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (e == cudaSuccess && grad_heights)
-    e = cudaMemsetAsync(grad_heights, 0, size_t(batch) * (t->T - 1) * sizeof(double), s);
-  if (e == cudaSuccess) {
+  if (e == cudaSuccess) {  // every internal node's gradient is written once: no clearing needed
     coalescent_kernel<<<batch, 256, smem, s>>>(t->d_times, heights, theta, t->T, n2, log_prob, grad_heights,
                                                grad_theta);
     e = cudaGetLastError();
