@@ -243,6 +243,7 @@ int tt_compress_columns(const uint8_t *matrix, int64_t rows, int64_t sites,
  *     tree_model.py:23-40; may be NULL), log|J| [b].  Device pointers.
  *   tt_ratio_transform_backward: dlnL/dratios [b][T-1] from dlnL/dheights,
  *     dlnL/dbranch_lengths, dlnL/dlog|J| (any of the three may be NULL).
+ *     Both transform calls take T <= 9,600 (a sample's rows in shared memory).
  *   tt_constant_coalescent: ConstantCoalescent.log_prob
  *     (coalescent.py:112-134) for internal heights [b][T-1] and theta [b]:
  *     log_prob [b], gradients [b][T-1] and [b] (may be NULL); T <= 4,096.

@@ -68,3 +68,40 @@ def test_batched_time_tree_kernels_match_the_oracle():
     (g,) = torch.autograd.grad(lp.sum() + ld.sum() + bl.sum(), xd)
     (gc,) = torch.autograd.grad(lpc.sum() + ldc.sum() + blc.sum(), xc)
     np.testing.assert_allclose(g.cpu().numpy(), gc.numpy(), rtol=1e-9, atol=1e-9 * np.abs(gc.numpy()).max())
+
+
+@pytest.mark.parametrize("T", [2, 3, 17])
+def test_small_trees_and_tied_heights(T):
+    """Tiny trees against the oracle (values and gradients), and internal nodes
+    placed exactly at a tip's sampling time (ratio 0): the log-density is the
+    same in any order of tied heights (their interval is empty)."""
+    from oracle import timetree as OT
+    from torchtree_gb300 import synthetic
+    from torchtree_gb300.timetree import TimeTree
+
+    rng = np.random.default_rng(T)
+    topo = synthetic.yule_topology(T, rng)
+    times = np.round(rng.uniform(0.0, 1.0, T), 1)  # repeated sampling times
+    b = 8
+    x = np.column_stack([rng.uniform(0.05, 0.95, (b, T - 2)), rng.uniform(2.0, 3.0, (b, 1))])
+    tree = TimeTree(topo.postorder, times)
+    theta = torch.linspace(0.5, 2.0, b, dtype=torch.float64)
+    xd = torch.tensor(x, device="cuda", requires_grad=True)
+    xc = torch.tensor(x, requires_grad=True)
+    h, bl, ld = tree.ratio_transform(xd)
+    hc, blc, ldc = OT.ratio_transform(topo.postorder.tolist(), times.tolist(), xc)
+    lp = tree.constant_coalescent(h, theta.cuda())
+    lpc = OT.constant_coalescent(times.tolist(), hc, theta)
+    np.testing.assert_allclose(h.detach().cpu().numpy(), hc.detach().numpy(), rtol=1e-12)
+    np.testing.assert_allclose(lp.detach().cpu().numpy(), lpc.detach().numpy(), rtol=1e-11)
+    (g,) = torch.autograd.grad(lp.sum() + ld.sum() + bl.sum(), xd)
+    (gc,) = torch.autograd.grad(lpc.sum() + ldc.sum() + blc.sum(), xc)
+    np.testing.assert_allclose(g.cpu().numpy(), gc.numpy(), rtol=1e-9, atol=1e-9 * np.abs(gc.numpy()).max())
+    if T > 2:  # ratio 0: a node at its lower bound, the sampling time of a tip below it
+        x0 = x.copy()
+        x0[:, : T - 2 : 2] = 0.0
+        h0, _, _ = tree.ratio_transform(torch.tensor(x0, device="cuda"))
+        hc0, _, _ = OT.ratio_transform(topo.postorder.tolist(), times.tolist(), torch.tensor(x0))
+        lp0 = tree.constant_coalescent(h0, theta.cuda())
+        lpc0 = OT.constant_coalescent(times.tolist(), hc0, theta)
+        np.testing.assert_allclose(lp0.cpu().numpy(), lpc0.numpy(), rtol=1e-11)

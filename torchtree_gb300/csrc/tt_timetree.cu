@@ -11,10 +11,14 @@
 //     log p = -sum_i C(l_i, 2) (t_(i+1) - t_i) / theta - (T - 1) log theta
 //   over the sorted node heights t with l_i lineages between t_i and t_(i+1).
 //
-// One thread per sample walks the pre-order (the transform is a chain along
-// each root-to-tip path); one CTA per sample sorts the node heights for the
-// coalescent (bitonic sort in shared memory, then one ordered scan for the
-// lineage counts and sums).
+// One CTA per sample. The transform walks the tree level by level (all nodes
+// of one depth in parallel, a barrier between depths) on the sample's row in
+// shared memory, loaded and stored coalesced; its adjoint walks the levels
+// back, each parent gathering its internal children's terms (fixed order, no
+// atomics). The coalescent sorts the sample's internal heights (bitonic sort
+// in shared memory), merges them by rank with the tip times sorted once at
+// set-up, and sums over the merged order with a block prefix sum of the
+// lineage counts.
 #include <algorithm>
 #include <cmath>
 #include <string>
@@ -27,103 +31,170 @@
 struct tt_time_tree {
   int device = 0;
   int T = 0;
-  int *d_pre_child = nullptr;   // [T-2] internal non-root nodes (index - T) in pre-order
-  int *d_pre_parent = nullptr;  // [T-2] their parents (index - T)
+  int levels = 0;               // depths of internal nodes (root: depth 0)
+  int *d_lvl_nodes = nullptr;   // [T-1] internal nodes (index - T) by depth, root first
+  int *d_lvl_off = nullptr;     // [levels + 1] offsets into d_lvl_nodes
+  int2 *d_kids = nullptr;       // [T-1] children (node indices) of internal node index - T
   int *d_parent = nullptr;      // [2T-2] parent node index of every non-root node
   double *d_lb = nullptr;       // [T-1] lower bounds of internal nodes
   double *d_times = nullptr;    // [T] sampling times
+  double *d_tip_t = nullptr;    // [T] sampling times in ascending (time, tip) order
+  int *d_tip_i = nullptr;       // [T] the tips in that order
 };
 
 namespace {
 
+constexpr int kTimeTreeThreads = 128;  // threads of the per-sample transform CTAs
+
 int tfail(int code, const std::string &m) { return tt::record_error(code, m.c_str()); }
 
-__global__ void ratio_forward_kernel(const int *pre_child, const int *pre_parent, const int *parent,
+// sum of v over the CTA in a fixed order (warps, then warp totals); valid in thread 0
+__device__ __forceinline__ double cta_sum(double v, double *wred) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5, nw = (blockDim.x + 31) >> 5;
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(0xffffffffu, v, o);
+  if (lane == 0) wred[warp] = v;
+  __syncthreads();
+  double t = 0.0;
+  if (threadIdx.x == 0)
+    for (int w = 0; w < nw; ++w) t += wred[w];
+  return t;
+}
+
+__global__ void ratio_forward_kernel(const int *lvl_nodes, const int *lvl_off, int levels, const int *parent,
                                      const double *lb, const double *times, const double *x, double *h,
-                                     double *bl, double *logdet, int T, int batch) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= batch) return;
-  const int I = T - 1;
-  const double *xb = x + size_t(b) * I;
-  double *hb = h + size_t(b) * I;
-  hb[I - 1] = xb[I - 1];  // root height
+                                     double *bl, double *logdet, int T) {
+  extern __shared__ __align__(16) double rs[];
+  __shared__ double wred[32];
+  const int b = blockIdx.x, tid = threadIdx.x, NT = blockDim.x, I = T - 1;
+  double *xs = rs, *hs = rs + I;  // this sample's ratios and heights
+  for (int v = tid; v < I; v += NT) xs[v] = x[size_t(b) * I + v];
+  __syncthreads();
+  if (tid == 0) hs[I - 1] = xs[I - 1];  // root height
+  __syncthreads();
   double ld = 0.0;
-  for (int s = 0; s < I - 1; ++s) {
-    const int v = pre_child[s], pv = pre_parent[s];
-    const double span = hb[pv] - lb[v];
-    hb[v] = lb[v] + xb[v] * span;
-    ld += log(span);
+  for (int d = 1; d < levels; ++d) {  // one depth at a time, parents before children
+    for (int e = lvl_off[d] + tid; e < lvl_off[d + 1]; e += NT) {
+      const int v = lvl_nodes[e], pv = parent[v + T] - T;
+      const double span = hs[pv] - lb[v];
+      hs[v] = lb[v] + xs[v] * span;
+      ld += log(span);
+    }
+    __syncthreads();
   }
-  logdet[b] = ld;
+  const double tot = cta_sum(ld, wred);
+  if (tid == 0) logdet[b] = tot;
+  for (int v = tid; v < I; v += NT) h[size_t(b) * I + v] = hs[v];
   if (bl)
-    for (int n = 0; n < 2 * T - 2; ++n) {
-      const double hn = n < T ? times[n] : hb[n - T];
-      bl[size_t(b) * (2 * T - 2) + n] = hb[parent[n] - T] - hn;
+    for (int n = tid; n < 2 * T - 2; n += NT) {
+      const double hn = n < T ? times[n] : hs[n - T];
+      bl[size_t(b) * (2 * T - 2) + n] = hs[parent[n] - T] - hn;
     }
 }
 
-// gx holds g_h on entry (filled here), dlnL/dx on exit
-__global__ void ratio_backward_kernel(const int *pre_child, const int *pre_parent, const int *parent,
+// dlnL/dx from dlnL/dh, dlnL/dbranch lengths and dlnL/dlog|J|
+__global__ void ratio_backward_kernel(const int *lvl_nodes, const int *lvl_off, int levels, const int2 *kids,
                                       const double *lb, const double *x, const double *h, const double *gh_in,
-                                      const double *gbl, const double *gld, double *gx, int T, int batch) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b >= batch) return;
-  const int I = T - 1;
-  const double *xb = x + size_t(b) * I, *hb = h + size_t(b) * I;
-  double *g = gx + size_t(b) * I;
-  for (int v = 0; v < I; ++v) g[v] = gh_in ? gh_in[size_t(b) * I + v] : 0.0;
-  if (gbl)
-    for (int n = 0; n < 2 * T - 2; ++n) {
-      const double gn = gbl[size_t(b) * (2 * T - 2) + n];
-      g[parent[n] - T] += gn;
-      if (n >= T) g[n - T] -= gn;
+                                      const double *gbl, const double *gld, double *gx, int T) {
+  extern __shared__ __align__(16) double rs[];
+  const int b = blockIdx.x, tid = threadIdx.x, NT = blockDim.x, I = T - 1, B = 2 * T - 2;
+  double *xs = rs, *hs = rs + I, *g = rs + 2 * I;
+  for (int v = tid; v < I; v += NT) {
+    xs[v] = x[size_t(b) * I + v];
+    hs[v] = h[size_t(b) * I + v];
+    double gv = gh_in ? gh_in[size_t(b) * I + v] : 0.0;
+    if (gbl) {  // branch c above node c has length h[parent c] - h[c]
+      const int2 k = kids[v];
+      gv += gbl[size_t(b) * B + k.x] + gbl[size_t(b) * B + k.y];
+      if (v < I - 1) gv -= gbl[size_t(b) * B + v + T];
     }
-  const double gl = gld ? gld[b] : 0.0;
-  for (int s = I - 2; s >= 0; --s) {
-    const int v = pre_child[s], pv = pre_parent[s];
-    const double span = hb[pv] - lb[v];
-    const double gv = g[v];
-    g[v] = gv * span;                          // dh_v/dx_v = span
-    g[pv] += gv * xb[v] + gl / span;           // dh_v/dh_p = x_v; d log(span)/dh_p
-  }
-  // the root entry keeps g_h[root] (h_root = x_root)
-}
-
-// one CTA per sample: heights of all 2T-1 nodes, bitonic sort in shared memory
-__global__ void coalescent_kernel(const double *times, const double *hint, const double *theta, int T, int n2,
-                                  double *logp, double *gh, double *gtheta) {
-  extern __shared__ __align__(16) unsigned char sm[];
-  double *key = reinterpret_cast<double *>(sm);  // [n2]
-  int *idx = reinterpret_cast<int *>(key + n2);  // [n2]
-  const int b = blockIdx.x, tid = threadIdx.x, NT = blockDim.x;
-  const int n = 2 * T - 1, I = T - 1;
-  for (int e = tid; e < n2; e += NT) {
-    if (e < n) {
-      key[e] = e < T ? times[e] : hint[size_t(b) * I + e - T];
-      idx[e] = e;
-    } else {
-      key[e] = INFINITY;
-      idx[e] = e;
-    }
+    g[v] = gv;
   }
   __syncthreads();
-  for (int k = 2; k <= n2; k <<= 1)
+  const double gl = gld ? gld[b] : 0.0;
+  // deepest parents first: a parent gathers d/dh of its internal children,
+  // which are final, then turns them into d/dx
+  for (int d = levels - 2; d >= 0; --d) {
+    for (int e = lvl_off[d] + tid; e < lvl_off[d + 1]; e += NT) {
+      const int p = lvl_nodes[e];
+      const int2 k = kids[p];
+      double gp = g[p];
+      const int c2[2] = {k.x, k.y};
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        if (c2[c] < T) continue;
+        const int cv = c2[c] - T;
+        const double span = hs[p] - lb[cv], gc = g[cv];
+        g[cv] = gc * span;                   // dh_c/dx_c = span
+        gp += gc * xs[cv] + gl / span;       // dh_c/dh_p = x_c; d log(span)/dh_p
+      }
+      g[p] = gp;
+    }
+    __syncthreads();
+  }
+  // the root entry keeps d/dh[root] (h_root = x_root)
+  for (int v = tid; v < I; v += NT) gx[size_t(b) * I + v] = g[v];
+}
+
+// one CTA per sample: the internal heights sorted in shared memory (bitonic,
+// ties by node index), merged by rank with the tips (sorted at set-up; a tip
+// precedes an internal node of equal height, as its index is smaller)
+__global__ void coalescent_kernel(const double *tip_t, const int *tip_i, const double *hint, const double *theta,
+                                  int T, int m2, double *logp, double *gh, double *gtheta) {
+  extern __shared__ __align__(16) unsigned char sm[];
+  const int b = blockIdx.x, tid = threadIdx.x, NT = blockDim.x;
+  const int n = 2 * T - 1, I = T - 1;
+  double *ik = reinterpret_cast<double *>(sm);  // [m2] internal heights
+  double *key = ik + m2;                        // [n] merged heights
+  double *tk = key + n;                         // [T] tip times, sorted
+  int *ii = reinterpret_cast<int *>(tk + T);    // [m2] internal node indices
+  int *idx = ii + m2;                           // [n] merged node indices
+  for (int e = tid; e < m2; e += NT) {
+    ik[e] = e < I ? hint[size_t(b) * I + e] : INFINITY;
+    ii[e] = T + e;
+  }
+  for (int e = tid; e < T; e += NT) tk[e] = tip_t[e];
+  __syncthreads();
+  for (int k = 2; k <= m2; k <<= 1)
     for (int j = k >> 1; j > 0; j >>= 1) {
-      for (int e = tid; e < n2; e += NT) {
+      for (int e = tid; e < m2; e += NT) {
         const int o = e ^ j;
         if (o > e) {
           const bool up = (e & k) == 0;
-          const double ke = key[e], ko = key[o];
-          const int ie = idx[e], io = idx[o];
+          const double ke = ik[e], ko = ik[o];
+          const int ie = ii[e], io = ii[o];
           const bool gt = ke > ko || (ke == ko && ie > io);
           if (gt == up) {
-            key[e] = ko, key[o] = ke;
-            idx[e] = io, idx[o] = ie;
+            ik[e] = ko, ik[o] = ke;
+            ii[e] = io, ii[o] = ie;
           }
         }
       }
       __syncthreads();
     }
+  for (int a = tid; a < I; a += NT) {  // tips at or below this height come first
+    const double v = ik[a];
+    int lo = 0, hi = T;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (tk[mid] <= v) lo = mid + 1;
+      else hi = mid;
+    }
+    key[a + lo] = v;
+    idx[a + lo] = ii[a];
+  }
+  for (int t = tid; t < T; t += NT) {  // internal nodes strictly below this time come first
+    const double v = tk[t];
+    int lo = 0, hi = I;
+    while (lo < hi) {
+      const int mid = (lo + hi) >> 1;
+      if (ik[mid] < v) lo = mid + 1;
+      else hi = mid;
+    }
+    key[t + lo] = v;
+    idx[t + lo] = tip_i[t];
+  }
+  __syncthreads();
   // Lineages through sorted position p: L_p = (#tips at or before p) - (#internal
   // nodes at or before p), a block-wide prefix sum over contiguous chunks of
   // positions.  With c_p = L_p (L_p - 1) / 2 for p < n - 1 (0 at the last):
@@ -199,27 +270,50 @@ int tt_time_tree_create(tt_time_tree **tree, int32_t tip_count, const int32_t *p
     auto h = [&](int c) { return c < T ? sampling_times[c] : lb[c - T]; };
     lb[v - T] = std::max(h(left[v]), h(right[v]));
   }
-  // pre-order of the non-root internal nodes: reversed post-order
-  std::vector<int> pc, pp;
-  for (int s = I - 2; s >= 0; --s) {
+  // internal nodes by depth (root at depth 0; a parent precedes its children)
+  std::vector<int> depth(NN, 0);
+  int levels = 1;
+  for (int s = I - 1; s >= 0; --s) {  // reversed post-order: parents first
     const int v = postorder[3 * s];
-    pc.push_back(v - T);
-    pp.push_back(parent[v] - T);
+    if (v != NN - 1) depth[v] = depth[parent[v]] + 1;
+    levels = std::max(levels, depth[v] + 1);
   }
+  std::vector<int> lvl_off(levels + 1, 0), lvl_nodes;
+  lvl_nodes.reserve(I);
+  for (int d = 0; d < levels; ++d) {
+    lvl_off[d] = int(lvl_nodes.size());
+    for (int v = T; v < NN; ++v)
+      if (depth[v] == d) lvl_nodes.push_back(v - T);
+  }
+  lvl_off[levels] = int(lvl_nodes.size());
+  std::vector<int2> kids(I);
+  for (int v = T; v < NN; ++v) kids[v - T] = make_int2(left[v], right[v]);
+  // tips in ascending (sampling time, index) order
+  std::vector<int> tip_i(T);
+  for (int i = 0; i < T; ++i) tip_i[i] = i;
+  std::sort(tip_i.begin(), tip_i.end(), [&](int a, int b) {
+    return sampling_times[a] != sampling_times[b] ? sampling_times[a] < sampling_times[b] : a < b;
+  });
+  std::vector<double> tip_t(T);
+  for (int i = 0; i < T; ++i) tip_t[i] = sampling_times[tip_i[i]];
   tt_time_tree *t = new tt_time_tree();
   cudaGetDevice(&t->device);
   t->T = T;
+  t->levels = levels;
   cudaError_t e = cudaSuccess;
   auto up = [&](auto **dst, const auto *src, size_t n) {
     if (e != cudaSuccess) return;
     e = cudaMalloc(reinterpret_cast<void **>(dst), std::max<size_t>(n, 1) * sizeof(**dst));
     if (e == cudaSuccess && n) e = cudaMemcpy(*dst, src, n * sizeof(**dst), cudaMemcpyHostToDevice);
   };
-  up(&t->d_pre_child, pc.data(), pc.size());
-  up(&t->d_pre_parent, pp.data(), pp.size());
+  up(&t->d_lvl_nodes, lvl_nodes.data(), lvl_nodes.size());
+  up(&t->d_lvl_off, lvl_off.data(), lvl_off.size());
+  up(&t->d_kids, kids.data(), kids.size());
   up(&t->d_parent, parent.data(), size_t(2 * T - 2));
   up(&t->d_lb, lb.data(), lb.size());
   up(&t->d_times, sampling_times, size_t(T));
+  up(&t->d_tip_t, tip_t.data(), tip_t.size());
+  up(&t->d_tip_i, tip_i.data(), tip_i.size());
   if (e != cudaSuccess) {
     tt_time_tree_destroy(t);
     return tfail(TT_ERR_OUT_OF_MEMORY, std::string("time-tree upload: ") + cudaGetErrorString(e));
@@ -230,7 +324,7 @@ int tt_time_tree_create(tt_time_tree **tree, int32_t tip_count, const int32_t *p
 
 int tt_time_tree_destroy(tt_time_tree *t) {
   if (!t) return TT_OK;
-  void *bufs[] = {t->d_pre_child, t->d_pre_parent, t->d_parent, t->d_lb, t->d_times};
+  void *bufs[] = {t->d_lvl_nodes, t->d_lvl_off, t->d_kids, t->d_parent, t->d_lb, t->d_times, t->d_tip_t, t->d_tip_i};
   for (void *p : bufs)
     if (p) cudaFree(p);
   delete t;
@@ -242,10 +336,16 @@ int tt_ratio_transform(tt_time_tree *t, int32_t batch, const double *ratios, dou
   if (!t || !ratios || !heights || !log_det_jacobian || batch < 1)
     return tfail(TT_ERR_INVALID_ARGUMENT, "NULL argument or empty batch");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  ratio_forward_kernel<<<(batch + 127) / 128, 128, 0, s>>>(t->d_pre_child, t->d_pre_parent, t->d_parent, t->d_lb,
-                                                          t->d_times, ratios, heights, branch_lengths,
-                                                          log_det_jacobian, t->T, batch);
-  const cudaError_t e = cudaGetLastError();
+  const size_t smem = 2 * size_t(t->T - 1) * sizeof(double);
+  if (3 * size_t(t->T - 1) * sizeof(double) > 227 * 1024)
+    return tfail(TT_ERR_UNSUPPORTED, "the ratio transform holds a sample's rows in shared memory: at most 9,600 tips");
+  cudaError_t e = cudaFuncSetAttribute(ratio_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e == cudaSuccess) {
+    ratio_forward_kernel<<<batch, kTimeTreeThreads, smem, s>>>(t->d_lvl_nodes, t->d_lvl_off, t->levels, t->d_parent,
+                                                               t->d_lb, t->d_times, ratios, heights, branch_lengths,
+                                                               log_det_jacobian, t->T);
+    e = cudaGetLastError();
+  }
   return e == cudaSuccess ? TT_OK : tfail(TT_ERR_CUDA, std::string("ratio transform launch: ") + cudaGetErrorString(e));
 }
 
@@ -255,10 +355,16 @@ int tt_ratio_transform_backward(tt_time_tree *t, int32_t batch, const double *ra
   if (!t || !ratios || !heights || !grad_ratios || batch < 1)
     return tfail(TT_ERR_INVALID_ARGUMENT, "NULL argument or empty batch");
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  ratio_backward_kernel<<<(batch + 127) / 128, 128, 0, s>>>(t->d_pre_child, t->d_pre_parent, t->d_parent, t->d_lb,
-                                                           ratios, heights, grad_heights, grad_branch_lengths,
-                                                           grad_log_det, grad_ratios, t->T, batch);
-  const cudaError_t e = cudaGetLastError();
+  const size_t smem = 3 * size_t(t->T - 1) * sizeof(double);
+  if (smem > 227 * 1024)
+    return tfail(TT_ERR_UNSUPPORTED, "the ratio transform holds a sample's rows in shared memory: at most 9,600 tips");
+  cudaError_t e = cudaFuncSetAttribute(ratio_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  if (e == cudaSuccess) {
+    ratio_backward_kernel<<<batch, kTimeTreeThreads, smem, s>>>(t->d_lvl_nodes, t->d_lvl_off, t->levels, t->d_kids,
+                                                                t->d_lb, ratios, heights, grad_heights,
+                                                                grad_branch_lengths, grad_log_det, grad_ratios, t->T);
+    e = cudaGetLastError();
+  }
   return e == cudaSuccess ? TT_OK
                           : tfail(TT_ERR_CUDA, std::string("ratio transform backward launch: ") + cudaGetErrorString(e));
 }
@@ -267,16 +373,16 @@ int tt_constant_coalescent(tt_time_tree *t, int32_t batch, const double *heights
                            double *log_prob, double *grad_heights, double *grad_theta, void *stream) {
   if (!t || !heights || !theta || !log_prob || batch < 1)
     return tfail(TT_ERR_INVALID_ARGUMENT, "NULL argument or empty batch");
-  const int n = 2 * t->T - 1;
-  if (n > 8191) return tfail(TT_ERR_UNSUPPORTED, "the coalescent kernel sorts at most 4,096 tips");
-  int n2 = 1;
-  while (n2 < n) n2 <<= 1;
+  const int T = t->T, I = T - 1, n = 2 * T - 1;
+  if (T > 4096) return tfail(TT_ERR_UNSUPPORTED, "the coalescent kernel sorts at most 4,096 tips");
+  int m2 = 1;
+  while (m2 < I) m2 <<= 1;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  const size_t smem = size_t(n2) * (sizeof(double) + sizeof(int));
+  const size_t smem = size_t(m2 + n + T) * sizeof(double) + size_t(m2 + n) * sizeof(int);
   cudaError_t e = cudaFuncSetAttribute(coalescent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
   if (e == cudaSuccess) {  // every internal node's gradient is written once: no clearing needed
-    coalescent_kernel<<<batch, 256, smem, s>>>(t->d_times, heights, theta, t->T, n2, log_prob, grad_heights,
-                                               grad_theta);
+    coalescent_kernel<<<batch, 256, smem, s>>>(t->d_tip_t, t->d_tip_i, heights, theta, T, m2, log_prob,
+                                               grad_heights, grad_theta);
     e = cudaGetLastError();
   }
   return e == cudaSuccess ? TT_OK : tfail(TT_ERR_CUDA, std::string("coalescent launch: ") + cudaGetErrorString(e));
