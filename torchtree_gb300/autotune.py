@@ -1,8 +1,8 @@
 """Kernel-shape autotuner.
 
 A plan's kernel shapes (staging-ring depths of the FP32 4-state kernels,
-tensor-core or CUDA-core codon post-order) do not change results, only
-speed.  ``tune`` times one full step under each candidate option set with
+the in-place or shared-memory-stack adjoint, pair-thread kernels, tensor-core
+or CUDA-core codon post-order) do not change results, only speed.  ``tune`` times one full step under each candidate option set with
 CUDA events and leaves the fastest set on the plan.  Choices are cached per
 problem shape (tips, patterns, states, categories, batch, precision), so a
 serving process tunes each shape once.
@@ -23,8 +23,9 @@ def candidates(engine) -> list:
     """Option sets worth timing for this plan."""
     if engine.precision == "f32" and engine.state_count == 4:
         F, B, Q = _native.TT_OPT_FWD_STAGES, _native.TT_OPT_BWD_STAGES, _native.TT_OPT_PAIR_THREADS
-        W = _native.TT_OPT_PRODUCER_WARP
-        return [{Q: 0, W: 1, F: 6, B: 3}, {Q: 0, W: 1, F: 4, B: 2}, {Q: 0, W: 0, F: 6, B: 3}, {Q: 1, W: 0, F: 6, B: 3}]
+        W, P = _native.TT_OPT_PRODUCER_WARP, _native.TT_OPT_INPLACE_ADJOINT
+        return [{Q: 0, W: 1, P: 1, F: 6, B: 2}, {Q: 0, W: 1, P: 1, F: 4, B: 3}, {Q: 0, W: 1, P: 0, F: 6, B: 2},
+                {Q: 1, W: 0, P: 0, F: 6, B: 3}]
     if engine.precision == "f32" and engine.state_count > 20:
         return [{_native.TT_OPT_TENSOR_CORES: 1}, {_native.TT_OPT_TENSOR_CORES: 0}]
     return [{}]
