@@ -219,6 +219,12 @@ __global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const 
       }
       tc::mma_commit(bar);
     }
+    if (c == 0 && r >= a.tips) {  // while the MMAs run: the other child's rows into L2 (lane j: rows j, j + 32)
+      const float *nxt = a.part + ((size_t(b) * a.I + (r - a.tips)) * a.K + k) * SP * size_t(a.Npad) + n0 + 32 * warp;
+      const int lane = tid & 31;
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(nxt + size_t(lane) * a.Npad));
+      asm volatile("prefetch.global.L2 [%0];" ::"l"(nxt + size_t(lane + 32) * a.Npad));
+    }
     // every thread sees the side's MMAs complete before the shared memory is restaged or TMEM read
     ok = mbar_wait_bounded(bar, phase, timeout_ns);
     tc::fence_after_sync();
