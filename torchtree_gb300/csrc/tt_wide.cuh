@@ -389,6 +389,28 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT, wide_bwd_min_blocks<T,
   for (int tile = t0; tile < t1; ++tile) {
     const int n0 = tile * PT;
     __syncthreads();  // previous tile's readers are done
+    if (tile + 1 < t1) {  // the next tile's rows into L2 while this one computes
+      constexpr int LPR = PT * int(sizeof(T)) / 128;  // 128-byte lines per tile row
+      const int rows_l = l >= a.tips ? SP : 0, rows_r = r >= a.tips ? SP : 0, rows_p = is_root ? 0 : SP;
+      const int rows_q = (kProd && a.prod) ? 2 * SP : 0;
+      const int nrows = rows_l + rows_r + rows_p + rows_q;
+      for (int e = tid; e < nrows * LPR; e += NT) {
+        int row = e / LPR;
+        const int seg = e - row * LPR;
+        const T *base;
+        if (row < rows_l) {
+          base = a.part + ((size_t(b) * a.I + (l - a.tips)) * a.K + k) * SP * size_t(a.Npad);
+        } else if ((row -= rows_l) < rows_r) {
+          base = a.part + ((size_t(b) * a.I + (r - a.tips)) * a.K + k) * SP * size_t(a.Npad);
+        } else if ((row -= rows_r) < rows_p) {
+          base = a.part + ((size_t(b) * a.I + (v - a.tips)) * a.K + k) * SP * size_t(a.Npad);
+        } else {
+          row -= rows_p;
+          base = a.prod + ((size_t(b) * a.I + (v - a.tips)) * a.K + k) * 2 * SP * size_t(a.Npad);
+        }
+        asm volatile("prefetch.global.L2 [%0];" ::"l"(base + size_t(row) * a.Npad + n0 + PT + seg * (128 / int(sizeof(T)))));
+      }
+    }
     wide_stage_child<T, SP, PT>(a, l, b, k, n0, xs);
     wide_stage_child<T, SP, PT>(a, r, b, k, n0, xs + SP * XS);
     if (tid < PT) {
