@@ -327,6 +327,7 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
     const int slots = bwd ? p->slots_bwd : p->slots_fwd;
     const int ns = bwd ? p->nstage_b : p->nstage_f;
     return f32 ? std::max({tt::tl_smem_bytes(p->K, 256, slots, bwd, ns), tt::tq_smem_bytes(p->K, 256, slots, bwd, ns),
+                           bwd ? size_t(0) : tt::tl_ws_smem_bytes(p->K, 256, slots, ns),
                            bwd ? tt::ta_smem_bytes(p->K, 256, ns) : size_t(0)})
                : tt::prune_smem_bytes<double>(4, p->K, 256, slots, tile, bwd);
   };
@@ -697,6 +698,7 @@ int tt_plan_set_option(tt_plan *p, int32_t option, int32_t value) {
       cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
       const int sl = bwd ? p->slots_bwd : p->slots_fwd;
       if (std::max({tt::tl_smem_bytes(p->K, 256, sl, bwd, value), tt::tq_smem_bytes(p->K, 256, sl, bwd, value),
+                    bwd ? size_t(0) : tt::tl_ws_smem_bytes(p->K, 256, sl, value),
                     bwd ? tt::ta_smem_bytes(p->K, 256, value) : size_t(0)}) > size_t(smem_max))
         return fail(TT_ERR_UNSUPPORTED, "ring does not fit in shared memory");
       (bwd ? p->nstage_b : p->nstage_f) = value;

@@ -25,7 +25,7 @@ constexpr int kFwdTilesF64[2] = {64, 32};
 constexpr int kBwdTilesF64[2] = {64, 32};
 constexpr int kStages = 4;
 // default staging-ring depths of the FP32 kernels (reduced to fit shared memory)
-constexpr int kTlFwdStages = 6;
+constexpr int kTlFwdStages = 3;
 constexpr int kTlBwdStages = 2;
 
 // category pairs of the FP32 kernels (K padded to an even count)
@@ -40,7 +40,14 @@ size_t prune_smem_bytes(int S, int K, int C, int slots, int tile, bool backward)
   return stack_layout<T>(S, K, C, slots, tile, kStages, kmax_for(K), backward).total;
 }
 
+// patterns per CTA of the producer-warp post-order (kTlPartTile-wide stored tiles)
+constexpr int kTlWsPatterns = 128;
+static_assert(kTlTile == kTlPartTile, "stored tile width");
+
 // FP32 kernels (packed FP32x2, category pairs)
+inline size_t tl_ws_smem_bytes(int K, int C, int slots, int nstage) {
+  return size_t(tl_layout(kpairs_for(K), C, slots, kTlWsPatterns, kTlWsPatterns, nstage, false).total);
+}
 inline size_t tl_smem_bytes(int K, int C, int slots, bool backward, int nstage) {
   return size_t(tl_layout(kpairs_for(K), C, slots, kTlTile, backward ? kTlBwdThreads : kTlFwdThreads, nstage,
                           backward)

@@ -69,12 +69,13 @@ bool pair_threads_supported(int K) {
 
 template <int KQ>
 cudaError_t launch_tl_ws(const PruneArgs<float> &a, int batch, cudaStream_t stream) {
-  const size_t smem = tl_smem_bytes(a.K, a.C, a.slots, false, a.nstage);
-  const dim3 grid(a.ntiles, batch);
-  auto kern = tl_forward_ws_kernel<KQ, kTlTile>;
+  const size_t smem = tl_ws_smem_bytes(a.K, a.C, a.slots, a.nstage);
+  constexpr int TPC = kTlWsPatterns / kTlTile;
+  const dim3 grid((a.ntiles + TPC - 1) / TPC, batch);
+  auto kern = tl_forward_ws_kernel<KQ, kTlWsPatterns>;
   cudaError_t e = set_smem(kern, smem);
   if (e != cudaSuccess) return e;
-  kern<<<grid, kTlTile + 32, smem, stream>>>(a);
+  kern<<<grid, kTlWsPatterns + 32, smem, stream>>>(a);
   return cudaGetLastError();
 }
 

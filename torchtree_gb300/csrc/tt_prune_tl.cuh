@@ -60,7 +60,10 @@ struct TlLayout {
 constexpr int kTlRecChunk = 32;
 // CTAs per SM the producer-warp post-order's register budget is sized for:
 // six fit the shared memory of up to two category pairs
-__host__ __device__ constexpr int tl_ws_min_blocks(int KQ) { return KQ <= 2 ? 6 : 1; }
+__host__ __device__ constexpr int tl_ws_min_blocks(int KQ, int NT) { return KQ <= 2 ? (NT <= 64 ? 6 : 4) : 1; }
+// width of a stored post-order tile (patterns); the producer-warp post-order
+// may walk several tiles of one sample in one CTA
+constexpr int kTlPartTile = 64;
 
 
 // red2: float2 partial-block elements per thread of the adjoint's pattern reduction
@@ -460,8 +463,10 @@ __global__ void __launch_bounds__(NT) tl_forward_kernel(const PruneArgs<float> a
 // only its own pattern's stack entries, so the compute warps need no block
 // barrier per step and drift up to NSTAGE - 1 steps apart.
 template <int KQ, int NT>
-__global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ)) tl_forward_ws_kernel(const PruneArgs<float> a) {
-  constexpr int P = NT;
+__global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ, NT)) tl_forward_ws_kernel(const PruneArgs<float> a) {
+  constexpr int P = NT;  // patterns of this CTA: NT / kTlPartTile stored tiles of one sample
+  constexpr int TPC = NT / kTlPartTile;
+  static_assert(NT % kTlPartTile == 0, "whole stored tiles per CTA");
   constexpr int NC = 2 * KQ;
   constexpr int NW = NT / 32;
   extern __shared__ __align__(128) unsigned char smem[];
@@ -521,11 +526,13 @@ __global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ)) tl_forward_ws_k
     for (int k = 0; k < 2 * KQ; ++k) props[k] = k < K ? a.props[b * K + k] : 0.0;
 #pragma unroll
     for (int i = 0; i < 4; ++i) freqs[i] = a.freqs[b * 4 + i];
-    float4 *gtile = a.partials
-                        ? reinterpret_cast<float4 *>(a.partials) + (size_t(b) * (nst - 1) * a.ntiles + tile) * NC * P
-                        : nullptr;
-    const size_t node_stride = size_t(a.ntiles) * NC * P;  // float4 per node
     const int p = tid;
+    const int my_tile = tile * TPC + p / kTlPartTile, pl = p % kTlPartTile;  // stored tile, column in it
+    float4 *gtile = a.partials && my_tile < a.ntiles
+                        ? reinterpret_cast<float4 *>(a.partials) +
+                              (size_t(b) * (nst - 1) * a.ntiles + my_tile) * NC * kTlPartTile
+                        : nullptr;
+    const size_t node_stride = size_t(a.ntiles) * NC * kTlPartTile;  // float4 per node
     int E = 0;
     double ll = 0.0;
     for (int s = 0; s < nst; ++s) {
@@ -560,8 +567,8 @@ __global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ)) tl_forward_ws_k
       if (out_slot >= 0) {
         vec_store<KQ>(stk + out_slot * NC * P + p, P, al);
         if (gtile)
-          vec_store_pm_stream<KQ>(reinterpret_cast<float2 *>(gtile + size_t(node - a.tip_count) * node_stride), p,
-                                  P, al);
+          vec_store_pm_stream<KQ>(reinterpret_cast<float2 *>(gtile + size_t(node - a.tip_count) * node_stride), pl,
+                                  kTlPartTile, al);
       } else {
         double site = 0.0;
 #pragma unroll
@@ -583,10 +590,11 @@ __global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ)) tl_forward_ws_k
     if (lane == 0) warp_tot[tid >> 5] = contrib;
   }
   __syncthreads();
-  if (tid == 0) {
+  if (tid < TPC) {  // one sum per stored tile, its warps in order
+    constexpr int WPT = kTlPartTile / 32;
     double tot = 0.0;
-    for (int w = 0; w < NW; ++w) tot += warp_tot[w];
-    a.tile_lnl[size_t(b) * a.ntiles + tile] = tot;
+    for (int w = 0; w < WPT; ++w) tot += warp_tot[tid * WPT + w];
+    if (tile * TPC + tid < a.ntiles) a.tile_lnl[size_t(b) * a.ntiles + tile * TPC + tid] = tot;
   }
 }
 
