@@ -57,7 +57,7 @@ int dev_alloc(tt_plan *p, P **ptr, size_t bytes, const char *what) {
 }
 
 void release(tt_plan *p) {
-  void *bufs[] = {p->d_steps, p->d_steps_rev, p->d_branch_pos, p->d_codes,    p->d_table,   p->d_weights,
+  void *bufs[] = {p->d_steps, p->d_steps_rev, p->d_steps_ws, p->d_branch_pos, p->d_codes,    p->d_table,   p->d_weights,
                   p->d_pmat,  p->d_partials,   p->d_tile_lnl, p->d_gpart,   p->d_rootpart,
                   p->d_G,     p->d_rootgrad,   p->d_status, p->d_qpart};
   for (void *b : bufs)
@@ -210,6 +210,33 @@ int build_schedule(tt_plan *p, const int32_t *post) {
       p->steps[size_t(s) * tt::kStepInts + 10] = I - 1 - ps;
     }
   }
+  // producer-warp post-order: a node whose next step is its parent hands its
+  // partial over in registers and takes no stack slot
+  p->steps_ws.assign(size_t(I) * tt::kStepInts, -1);
+  {
+    std::vector<int> wslot(NN, -1);
+    free_slots.clear();
+    next_slot = 0;
+    for (int s = 0; s < I; ++s) {
+      const int v = order[s], l = left[v], r = right[v];
+      int *rec = &p->steps_ws[size_t(s) * tt::kStepInts];
+      rec[0] = v;
+      rec[1] = l;
+      rec[2] = r;
+      const int kid[2] = {l, r};
+      for (int c = 0; c < 2; ++c) {
+        const int k = kid[c];
+        if (k < T) continue;
+        const bool carried = s > 0 && order[s - 1] == k;
+        rec[3 + c] = carried ? tt::kWsCarry : wslot[k];
+        if (!carried) free_slots.insert(wslot[k]);
+      }
+      const bool carry_out = s + 1 < I && parent[v] == order[s + 1];
+      rec[5] = v == root ? -1 : (carry_out ? tt::kWsCarry : alloc());
+      wslot[v] = rec[5];
+    }
+    p->slots_ws = std::max(next_slot, 1);
+  }
   p->branch_pos.assign(p->B, -1);
   for (int s = 0; s < I; ++s) {
     const int *rec = &p->steps[size_t(s) * tt::kStepInts];
@@ -244,6 +271,7 @@ tt::PruneArgs<T> make_args(tt_plan *p, const double *props, const double *freqs,
   a.code_stride = p->code_stride;
   a.nstage = p->nstage_f;
   a.steps_rev = p->d_steps_rev;
+  a.steps_ws = p->d_steps_ws;
   a.codes = p->d_codes;
   a.table = static_cast<const T *>(p->d_table);
   a.pmat = static_cast<const T *>(p->d_pmat);
@@ -327,7 +355,7 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
     const int slots = bwd ? p->slots_bwd : p->slots_fwd;
     const int ns = bwd ? p->nstage_b : p->nstage_f;
     return f32 ? std::max({tt::tl_smem_bytes(p->K, 256, slots, bwd, ns), tt::tq_smem_bytes(p->K, 256, slots, bwd, ns),
-                           bwd ? size_t(0) : tt::tl_ws_smem_bytes(p->K, 256, slots, ns),
+                           bwd ? size_t(0) : tt::tl_ws_smem_bytes(p->K, 256, p->slots_ws, ns),
                            bwd ? tt::ta_smem_bytes(p->K, 256, ns) : size_t(0)})
                : tt::prune_smem_bytes<double>(4, p->K, 256, slots, tile, bwd);
   };
@@ -380,6 +408,7 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
   rc = TT_OK;
   if (!rc) rc = dev_alloc(p, &p->d_steps, p->steps.size() * sizeof(int), "schedule");
   if (!rc) rc = dev_alloc(p, &p->d_steps_rev, p->steps.size() * sizeof(int), "reversed schedule");
+  if (!rc) rc = dev_alloc(p, &p->d_steps_ws, p->steps_ws.size() * sizeof(int), "post-order schedule");
   if (!rc) rc = dev_alloc(p, &p->d_branch_pos, size_t(p->B) * sizeof(int), "branch map");
   if (!rc) rc = dev_alloc(p, &p->d_codes, size_t(p->T) * p->code_stride, "tip codes");
   if (!rc) rc = dev_alloc(p, &p->d_table, size_t(256) * p->S * p->elem, "code table");
@@ -410,6 +439,8 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
                   tt::kStepInts * sizeof(int));
     ce = cudaMemcpy(p->d_steps_rev, rev.data(), rev.size() * sizeof(int), cudaMemcpyHostToDevice);
   }
+  if (ce == cudaSuccess)
+    ce = cudaMemcpy(p->d_steps_ws, p->steps_ws.data(), p->steps_ws.size() * sizeof(int), cudaMemcpyHostToDevice);
   if (ce == cudaSuccess)
     ce = cudaMemcpy(p->d_branch_pos, p->branch_pos.data(), p->branch_pos.size() * sizeof(int),
                     cudaMemcpyHostToDevice);
@@ -550,7 +581,7 @@ int tt_log_likelihood(tt_plan *p, const double *props, const double *freqs, int3
   cudaError_t e;
   if (p->precision == TT_PRECISION_F32) {
     auto a = make_args<float>(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, site_lnl);
-    a.slots = p->slots_fwd;
+    a.slots = p->producer_warp && !p->pair_threads ? p->slots_ws : p->slots_fwd;
     e = tt::launch_prune_f32(a, false, p->tile_f, p->batch, (p->pair_threads ? tt::kF32PairThreads : 0) | (p->producer_warp ? tt::kF32ProducerWarp : 0), s);
   } else {
     auto a = make_args<double>(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, site_lnl);
@@ -698,7 +729,7 @@ int tt_plan_set_option(tt_plan *p, int32_t option, int32_t value) {
       cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, p->device);
       const int sl = bwd ? p->slots_bwd : p->slots_fwd;
       if (std::max({tt::tl_smem_bytes(p->K, 256, sl, bwd, value), tt::tq_smem_bytes(p->K, 256, sl, bwd, value),
-                    bwd ? size_t(0) : tt::tl_ws_smem_bytes(p->K, 256, sl, value),
+                    bwd ? size_t(0) : tt::tl_ws_smem_bytes(p->K, 256, p->slots_ws, value),
                     bwd ? tt::ta_smem_bytes(p->K, 256, value) : size_t(0)}) > size_t(smem_max))
         return fail(TT_ERR_UNSUPPORTED, "ring does not fit in shared memory");
       (bwd ? p->nstage_b : p->nstage_f) = value;

@@ -16,6 +16,7 @@ struct tt_plan {
   int device = 0;
   int T = 0, I = 0, B = 0, S = 0, K = 0, N = 0, batch = 0, precision = 0;
   int C = 0, slots_fwd = 0, slots_bwd = 0;
+  int slots_ws = 0;  // stack slots of the producer-warp post-order (register carry to the parent)
   int tile_f = 0, tile_b = 0, ntiles_f = 0, ntiles_b = 0, code_stride = 0;
   int nstage_f = tt::kStages, nstage_b = tt::kStages;
   size_t elem = 0;  // bytes per partial value
@@ -25,10 +26,12 @@ struct tt_plan {
   bool tips_set = false, pmat_set = false, partials_valid = false, grads_valid = false;
   long long launches = 0;
   std::vector<int> steps;       // host copy of the schedule (I x 12)
+  std::vector<int> steps_ws;    // records of the producer-warp post-order (I x 12)
   std::vector<int> branch_pos;  // B
   // device buffers
   int4 *d_steps = nullptr;
   int4 *d_steps_rev = nullptr;
+  int4 *d_steps_ws = nullptr;
   int *d_branch_pos = nullptr;
   uint8_t *d_codes = nullptr;
   void *d_table = nullptr;

@@ -43,6 +43,11 @@ constexpr int kStepInts = 12;
 // tile (else it arrives in registers from the previous step, or is the root);
 // the left / right child's outside partial stays in registers for the next
 // step (carry) or is stored in place.
+// Records of the producer-warp post-order (tt_plan::d_steps_ws): [0] node
+// [1] left [2] right [3] [4] stack slot of the left / right child (-1: tip,
+// kWsCarry: the child was the previous step and its partial is in registers)
+// [5] output slot (-1: root, kWsCarry: the next step is the parent)
+constexpr int kWsCarry = -2;
 constexpr int kTaPreStored = 1, kTaCarryLeft = 2, kTaCarryRight = 4, kTaStoreLeft = 8, kTaStoreRight = 16;
 
 template <typename T>
@@ -73,6 +78,8 @@ struct PruneArgs {
   T *rootpart;            // [batch][ntiles][S+K]
   int *status;
   unsigned long long timeout_ns;
+  // records of the producer-warp post-order (kWs* slots), or nullptr
+  const int4 *steps_ws = nullptr;
 };
 
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }

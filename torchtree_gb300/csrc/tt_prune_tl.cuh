@@ -497,7 +497,7 @@ __global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ, NT)) tl_forward_
 
   if (tid >= NT) {  // producer warp
     if (lane == 0) {
-      const TlRecRing ring{reinterpret_cast<int4 *>(smem + L.recs), bars + NSTAGE, a.steps, nst, a.timeout_ns};
+      const TlRecRing ring{reinterpret_cast<int4 *>(smem + L.recs), bars + NSTAGE, a.steps_ws, nst, a.timeout_ns};
       ring.load_chunk(0);
       ring.load_chunk(1);
       int issued = 0;
@@ -521,13 +521,13 @@ __global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ, NT)) tl_forward_
       }
     }
   } else {  // compute threads: one pattern each
-    double props[2 * KQ], freqs[4];
-#pragma unroll
-    for (int k = 0; k < 2 * KQ; ++k) props[k] = k < K ? a.props[b * K + k] : 0.0;
-#pragma unroll
-    for (int i = 0; i < 4; ++i) freqs[i] = a.freqs[b * 4 + i];
     const int p = tid;
     const int my_tile = tile * TPC + p / kTlPartTile, pl = p % kTlPartTile;  // stored tile, column in it
+    Vec<KQ> carry;  // partial of the previous step's node when this step is its parent
+#pragma unroll
+    for (int j = 0; j < 4; ++j)
+#pragma unroll
+      for (int q = 0; q < KQ; ++q) carry.v[j][q] = make_float2(0.0f, 0.0f);
     float4 *gtile = a.partials && my_tile < a.ntiles
                         ? reinterpret_cast<float4 *>(a.partials) +
                               (size_t(b) * (nst - 1) * a.ntiles + my_tile) * NC * kTlPartTile
@@ -552,9 +552,11 @@ __global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ, NT)) tl_forward_
       const int out_slot = r1.y;
       Vec<KQ> v, al, ar;
       if (ltip) vec_tip<KQ>(v, tab2, stg[G.codes + p]);
+      else if (r0.w == kWsCarry) v = carry;
       else vec_load<KQ>(v, stk + r0.w * NC * P + p, P);
       mat_vec<KQ>(al, pml, v);
       if (rtip) vec_tip<KQ>(v, tab2, stg[G.codes + P + p]);
+      else if (r1.x == kWsCarry) v = carry;
       else vec_load<KQ>(v, stk + r1.x * NC * P + p, P);
       mat_vec<KQ>(ar, pmr, v);
       __syncwarp();
@@ -564,19 +566,23 @@ __global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ, NT)) tl_forward_
 #pragma unroll
         for (int q = 0; q < KQ; ++q) al.v[j][q] = __fmul2_rn(al.v[j][q], ar.v[j][q]);
       if (a.rescale) vec_rescale<KQ>(al, E);
-      if (out_slot >= 0) {
-        vec_store<KQ>(stk + out_slot * NC * P + p, P, al);
+      if (out_slot != -1) {  // not the root: to the stack or, for the next step, to registers
+        if (out_slot == kWsCarry) carry = al;
+        else vec_store<KQ>(stk + out_slot * NC * P + p, P, al);
         if (gtile)
           vec_store_pm_stream<KQ>(reinterpret_cast<float2 *>(gtile + size_t(node - a.tip_count) * node_stride), pl,
                                   kTlPartTile, al);
       } else {
-        double site = 0.0;
+        double site = 0.0;  // category weights and root frequencies are read here only
 #pragma unroll
-        for (int j = 0; j < 4; ++j)
+        for (int j = 0; j < 4; ++j) {
+          const double fj = a.freqs[b * 4 + j];
 #pragma unroll
-          for (int q = 0; q < KQ; ++q)
-            site = fma(freqs[j], fma(props[2 * q], double(al.v[j][q].x), props[2 * q + 1] * double(al.v[j][q].y)),
-                       site);
+          for (int q = 0; q < KQ; ++q) {
+            const double p0 = a.props[b * K + 2 * q], p1 = 2 * q + 1 < K ? a.props[b * K + 2 * q + 1] : 0.0;
+            site = fma(fj, fma(p0, double(al.v[j][q].x), p1 * double(al.v[j][q].y)), site);
+          }
+        }
         ll = log(site) + double(E) * 0.69314718055994530942;
       }
     }
