@@ -10,9 +10,10 @@
 //  * the other internal child's outside partial overwrites the child's own
 //    post-order tile in HBM, which this step has just read for the last time
 //    (a node's post-order tile is read only by its parent's step), and is
-//    staged back with the child tiles at the child's step; that step is
-//    staged only after the writing step has passed its closing barrier,
-//    with a generic-to-async proxy fence in between;
+//    staged back into a single shared buffer for the child's step, once the
+//    step before it has read its own outside vector from that buffer (after
+//    that step's first barrier; the writing step, with a generic-to-async
+//    proxy fence, is at least one step earlier still);
 //  * the branch-gradient blocks of the pattern reduction are summed across
 //    lanes by warp shuffles and written at once.
 // The freed shared memory buys CTAs per SM: the walk is latency-bound.
@@ -25,9 +26,9 @@ namespace tt {
 
 constexpr int kTaRecChunk = 16;
 
-// step record | matrix pairs | 2 code rows | 2 child tiles | this node's outside tile
+// step record | matrix pairs | 2 code rows | 2 child tiles
 struct TaStage {
-  int rec, pm, codes, kids, pre, bytes;
+  int rec, pm, codes, kids, bytes;
 };
 
 __host__ __device__ inline TaStage ta_stage(int KQ, int P) {
@@ -42,14 +43,12 @@ __host__ __device__ inline TaStage ta_stage(int KQ, int P) {
   off = int(align16(off + 2 * P));
   g.kids = off;
   off = int(align16(off + 2 * tile_bytes));
-  g.pre = off;
-  off = int(align16(off + tile_bytes));
   g.bytes = off;
   return g;
 }
 
 struct TaLayout {
-  int stages, bars, recs, table, xbuf, red_root, total;
+  int stages, bars, recs, table, xbuf, pre, red_root, total;
 };
 
 __host__ __device__ inline TaLayout ta_layout(int KQ, int C, int P, int NT, int nstage) {
@@ -67,6 +66,8 @@ __host__ __device__ inline TaLayout ta_layout(int KQ, int C, int P, int NT, int 
   off = int(align16(off + C * 32));
   L.xbuf = off;
   off = int(align16(off + 2 * P * vbytes));
+  L.pre = off;  // the next step's stored outside tile (one buffer)
+  off = int(align16(off + P * vbytes));
   L.red_root = off;
   off = int(align16(off + (NT / 32) * 12 * 4));
   L.total = off;
@@ -79,9 +80,9 @@ __host__ __device__ constexpr int ta_red_lanes(int n) {
   return n >= 32 ? 32 : n >= 16 ? 16 : n >= 8 ? 8 : n >= 4 ? 4 : n >= 2 ? 2 : 1;
 }
 
-// CTAs per SM the register budget is sized for: six 64-thread CTAs fit the
+// CTAs per SM the register budget is sized for: seven 64-thread CTAs fit the
 // shared memory of up to two category pairs
-__host__ __device__ constexpr int ta_min_blocks(int KQ) { return KQ <= 2 ? 6 : 1; }
+__host__ __device__ constexpr int ta_min_blocks(int KQ) { return KQ <= 2 ? 7 : 1; }
 
 // the post-order tile of internal node `node` (pair-major, P patterns)
 __device__ __forceinline__ float *ta_tile(const PruneArgs<float> &a, int KQ, int b, int node, int tile, int P) {
@@ -89,8 +90,9 @@ __device__ __forceinline__ float *ta_tile(const PruneArgs<float> &a, int KQ, int
 }
 
 // Stage reversed step s (forward index fs): record, matrix pairs, code rows
-// of tip children, tiles of internal children, and the node's outside tile
-// when it was stored in place.
+// of tip children and tiles of internal children.  The barrier also expects
+// the node's outside tile when it was stored in place; ta_issue_pre copies it
+// later, into the single outside-tile buffer.
 __device__ __forceinline__ void ta_issue(const PruneArgs<float> &a, int KQ, unsigned char *stage, uint64_t *bar,
                                          const int4 (&rec)[3], int fs, int b, int tile, int P, const TaStage &g) {
   int4 *r = reinterpret_cast<int4 *>(stage + g.rec);
@@ -115,7 +117,16 @@ __device__ __forceinline__ void ta_issue(const PruneArgs<float> &a, int KQ, unsi
     else
       bulk_copy_g2s(stage + g.kids + c * int(tile_bytes), ta_tile(a, KQ, b, child[c], tile, P), tile_bytes, bar);
   }
-  if (flags & kTaPreStored) bulk_copy_g2s(stage + g.pre, ta_tile(a, KQ, b, node, tile, P), tile_bytes, bar);
+  (void)node;
+}
+
+// the stored outside tile of the step staged at `stage` (if any) into `dst`
+__device__ __forceinline__ void ta_issue_pre(const PruneArgs<float> &a, int KQ, const unsigned char *stage,
+                                             uint64_t *bar, unsigned char *dst, int b, int tile, int P,
+                                             const TaStage &g) {
+  const int4 r0 = reinterpret_cast<const int4 *>(stage + g.rec)[0];
+  const int4 r2 = reinterpret_cast<const int4 *>(stage + g.rec)[2];
+  if (r2.y & kTaPreStored) bulk_copy_g2s(dst, ta_tile(a, KQ, b, r0.x, tile, P), uint32_t(P) * KQ * 32, bar);
 }
 
 // o[jj][q] = sum_i P_q[i][jj] x[i][q] with the pair matrices of one side in
@@ -181,9 +192,8 @@ __global__ void __launch_bounds__(NT, ta_min_blocks(KQ)) ta_backward_kernel(cons
   bool has_pend = false;
   int4 pend[3];
   bool timed_out = false;
-  // stage steps up to `limit` whose stored outside tile was written by a
-  // step <= `written`
-  auto issue = [&](int limit, int written) {
+  // stage steps up to `limit`
+  auto issue = [&](int limit) {
     while (next_issue < nst && next_issue <= limit) {
       if (!has_pend) {
         if (!ring.get(next_issue, pend)) {
@@ -192,7 +202,6 @@ __global__ void __launch_bounds__(NT, ta_min_blocks(KQ)) ta_backward_kernel(cons
         }
         has_pend = true;
       }
-      if ((pend[2].y & kTaPreStored) && pend[2].z > written) return;
       const int st = next_issue % NSTAGE;
       ta_issue(a, KQ, stages + st * G.bytes, &bars[st], pend, nst - 1 - next_issue, b, tile, P, G);
       has_pend = false;
@@ -208,7 +217,7 @@ __global__ void __launch_bounds__(NT, ta_min_blocks(KQ)) ta_backward_kernel(cons
   if (tid == 0) {
     ring.load_chunk(0);
     ring.load_chunk(1);
-    issue(NSTAGE - 2, -1);
+    issue(NSTAGE - 2);
   }
   timed_out = timed_out || !mbar_wait_bounded(&bars[0], 0, a.timeout_ns);
   if (__syncthreads_or(timed_out)) {
@@ -222,7 +231,7 @@ __global__ void __launch_bounds__(NT, ta_min_blocks(KQ)) ta_backward_kernel(cons
 #pragma unroll
     for (int q = 0; q < KQ; ++q) carry.v[jj][q] = make_float2(0.0f, 0.0f);
   for (int j = 0; j < nst; ++j) {
-    if (tid == 0) issue(j + NSTAGE - 1, j - 1);
+    if (tid == 0) issue(j + NSTAGE - 1);
     const unsigned char *stg = stages + (j % NSTAGE) * G.bytes;
     const int4 r0 = reinterpret_cast<const int4 *>(stg + G.rec)[0];
     const int4 r2 = reinterpret_cast<const int4 *>(stg + G.rec)[2];
@@ -249,7 +258,7 @@ __global__ void __launch_bounds__(NT, ta_min_blocks(KQ)) ta_backward_kernel(cons
           pre.v[jj][q] = make_float2(float(a.props[b * K + 2 * q] * a.freqs[b * 4 + jj]),
                                      2 * q + 1 < K ? float(a.props[b * K + 2 * q + 1] * a.freqs[b * 4 + jj]) : 0.0f);
     } else if (flags & kTaPreStored) {
-      vec_load_pm<KQ>(pre, reinterpret_cast<const float2 *>(stg + G.pre), tid, P);
+      vec_load_pm<KQ>(pre, reinterpret_cast<const float2 *>(smem + L.pre), tid, P);
     } else {
       pre = carry;
     }
@@ -335,7 +344,10 @@ __global__ void __launch_bounds__(NT, ta_min_blocks(KQ)) ta_backward_kernel(cons
     }
     // the stored tile is read back by the TMA engine (async proxy) at a later step
     if (flags & (kTaStoreLeft | kTaStoreRight)) asm volatile("fence.proxy.async.global;" ::: "memory");
-    __syncthreads();  // xbuf complete
+    __syncthreads();  // xbuf complete; every thread has read this step's outside vector
+    if (tid == 0 && j + 1 < next_issue)  // the next step (staged) has its stored outside tile copied into the freed buffer
+      ta_issue_pre(a, KQ, stages + ((j + 1) % NSTAGE) * G.bytes, &bars[(j + 1) % NSTAGE], smem + L.pre, b, tile, P,
+                   G);
 
     // reduction over the tile's patterns, register-blocked:
     //   G[c][k][i][jj] = sum_p (coef x_c)[p][i][k] * v_c[p][jj][k]
