@@ -9,11 +9,9 @@
 //    that child's outside partial stays in registers (the carry);
 //  * the other internal child's outside partial overwrites the child's own
 //    post-order tile in HBM, which this step has just read for the last time
-//    (a node's post-order tile is read only by its parent's step), and is
-//    staged back into a single shared buffer for the child's step, once the
-//    step before it has read its own outside vector from that buffer (after
-//    that step's first barrier; the writing step, with a generic-to-async
-//    proxy fence, is at least one step earlier still);
+//    (a node's post-order tile is read only by its parent's step); at the
+//    child's step each thread loads its own column back (it wrote that
+//    column itself, so program order is all the ordering needed);
 //  * the branch-gradient blocks of the pattern reduction are summed across
 //    lanes by warp shuffles and written at once.
 // The freed shared memory buys CTAs per SM: the walk is latency-bound.
@@ -48,7 +46,7 @@ __host__ __device__ inline TaStage ta_stage(int KQ, int P) {
 }
 
 struct TaLayout {
-  int stages, bars, recs, table, xbuf, pre, red_root, total;
+  int stages, bars, recs, table, xbuf, red_root, total;
 };
 
 __host__ __device__ inline TaLayout ta_layout(int KQ, int C, int P, int NT, int nstage) {
@@ -66,8 +64,6 @@ __host__ __device__ inline TaLayout ta_layout(int KQ, int C, int P, int NT, int 
   off = int(align16(off + C * 32));
   L.xbuf = off;
   off = int(align16(off + 2 * P * vbytes));
-  L.pre = off;  // the next step's stored outside tile (one buffer)
-  off = int(align16(off + P * vbytes));
   L.red_root = off;
   off = int(align16(off + (NT / 32) * 12 * 4));
   L.total = off;
@@ -80,9 +76,9 @@ __host__ __device__ constexpr int ta_red_lanes(int n) {
   return n >= 32 ? 32 : n >= 16 ? 16 : n >= 8 ? 8 : n >= 4 ? 4 : n >= 2 ? 2 : 1;
 }
 
-// CTAs per SM the register budget is sized for: seven 64-thread CTAs fit the
+// CTAs per SM the register budget is sized for: eight 64-thread CTAs fit the
 // shared memory of up to two category pairs
-__host__ __device__ constexpr int ta_min_blocks(int KQ) { return KQ <= 2 ? 7 : 1; }
+__host__ __device__ constexpr int ta_min_blocks(int KQ) { return KQ <= 2 ? 8 : 1; }
 
 // the post-order tile of internal node `node` (pair-major, P patterns)
 __device__ __forceinline__ float *ta_tile(const PruneArgs<float> &a, int KQ, int b, int node, int tile, int P) {
@@ -90,9 +86,7 @@ __device__ __forceinline__ float *ta_tile(const PruneArgs<float> &a, int KQ, int
 }
 
 // Stage reversed step s (forward index fs): record, matrix pairs, code rows
-// of tip children and tiles of internal children.  The barrier also expects
-// the node's outside tile when it was stored in place; ta_issue_pre copies it
-// later, into the single outside-tile buffer.
+// of tip children and tiles of internal children.
 __device__ __forceinline__ void ta_issue(const PruneArgs<float> &a, int KQ, unsigned char *stage, uint64_t *bar,
                                          const int4 (&rec)[3], int fs, int b, int tile, int P, const TaStage &g) {
   int4 *r = reinterpret_cast<int4 *>(stage + g.rec);
@@ -105,7 +99,6 @@ __device__ __forceinline__ void ta_issue(const PruneArgs<float> &a, int KQ, unsi
   uint32_t total = pbytes;
   total += left < a.tip_count ? uint32_t(P) : tile_bytes;
   total += right < a.tip_count ? uint32_t(P) : tile_bytes;
-  if (flags & kTaPreStored) total += tile_bytes;
   mbar_arrive_expect_tx(bar, total);
   bulk_copy_g2s(stage + g.pm, a.pmat + (size_t(b) * a.n_steps + fs) * 2 * KQ * 32, pbytes, bar);
   const int child[2] = {left, right};
@@ -118,15 +111,7 @@ __device__ __forceinline__ void ta_issue(const PruneArgs<float> &a, int KQ, unsi
       bulk_copy_g2s(stage + g.kids + c * int(tile_bytes), ta_tile(a, KQ, b, child[c], tile, P), tile_bytes, bar);
   }
   (void)node;
-}
-
-// the stored outside tile of the step staged at `stage` (if any) into `dst`
-__device__ __forceinline__ void ta_issue_pre(const PruneArgs<float> &a, int KQ, const unsigned char *stage,
-                                             uint64_t *bar, unsigned char *dst, int b, int tile, int P,
-                                             const TaStage &g) {
-  const int4 r0 = reinterpret_cast<const int4 *>(stage + g.rec)[0];
-  const int4 r2 = reinterpret_cast<const int4 *>(stage + g.rec)[2];
-  if (r2.y & kTaPreStored) bulk_copy_g2s(dst, ta_tile(a, KQ, b, r0.x, tile, P), uint32_t(P) * KQ * 32, bar);
+  (void)flags;
 }
 
 // o[jj][q] = sum_i P_q[i][jj] x[i][q] with the pair matrices of one side in
@@ -257,8 +242,8 @@ __global__ void __launch_bounds__(NT, ta_min_blocks(KQ)) ta_backward_kernel(cons
         for (int q = 0; q < KQ; ++q)
           pre.v[jj][q] = make_float2(float(a.props[b * K + 2 * q] * a.freqs[b * 4 + jj]),
                                      2 * q + 1 < K ? float(a.props[b * K + 2 * q + 1] * a.freqs[b * 4 + jj]) : 0.0f);
-    } else if (flags & kTaPreStored) {
-      vec_load_pm<KQ>(pre, reinterpret_cast<const float2 *>(smem + L.pre), tid, P);
+    } else if (flags & kTaPreStored) {  // this thread's column, stored by this thread at the parent's step
+      vec_load_pm<KQ>(pre, reinterpret_cast<const float2 *>(ta_tile(a, KQ, b, r0.x, tile, P)), tid, P);
     } else {
       pre = carry;
     }
@@ -342,12 +327,7 @@ __global__ void __launch_bounds__(NT, ta_min_blocks(KQ)) ta_backward_kernel(cons
       if (flags & kTaCarryRight) carry = o;
       else vec_store_pm<KQ>(reinterpret_cast<float2 *>(ta_tile(a, KQ, b, right, tile, P)), tid, P, o);
     }
-    // the stored tile is read back by the TMA engine (async proxy) at a later step
-    if (flags & (kTaStoreLeft | kTaStoreRight)) asm volatile("fence.proxy.async.global;" ::: "memory");
-    __syncthreads();  // xbuf complete; every thread has read this step's outside vector
-    if (tid == 0 && j + 1 < next_issue)  // the next step (staged) has its stored outside tile copied into the freed buffer
-      ta_issue_pre(a, KQ, stages + ((j + 1) % NSTAGE) * G.bytes, &bars[(j + 1) % NSTAGE], smem + L.pre, b, tile, P,
-                   G);
+    __syncthreads();  // xbuf complete
 
     // reduction over the tile's patterns, register-blocked:
     //   G[c][k][i][jj] = sum_p (coef x_c)[p][i][k] * v_c[p][jj][k]
