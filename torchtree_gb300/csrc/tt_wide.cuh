@@ -335,7 +335,7 @@ __global__ void wide_root_kernel(const double *root_site, const int *root_expo, 
 // two fit the shared memory too)
 template <typename T, int SP>
 __host__ __device__ constexpr int wide_bwd_min_blocks() {
-  return sizeof(T) == 4 ? 2 : 1;
+  return sizeof(T) == 4 ? (SP == 64 ? 2 : 3) : 1;
 }
 
 template <typename T, int SP, int PT>
