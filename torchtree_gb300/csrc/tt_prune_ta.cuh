@@ -93,7 +93,7 @@ __device__ __forceinline__ void ta_issue(const PruneArgs<float> &a, int KQ, unsi
   r[0] = rec[0];
   r[1] = rec[1];
   r[2] = rec[2];
-  const int node = rec[0].x, left = rec[0].y, right = rec[0].z, flags = rec[2].y;
+  const int left = rec[0].y, right = rec[0].z;
   const uint32_t pbytes = uint32_t(2 * KQ * 16 * 8);
   const uint32_t tile_bytes = uint32_t(P) * KQ * 32;
   uint32_t total = pbytes;
@@ -110,8 +110,6 @@ __device__ __forceinline__ void ta_issue(const PruneArgs<float> &a, int KQ, unsi
     else
       bulk_copy_g2s(stage + g.kids + c * int(tile_bytes), ta_tile(a, KQ, b, child[c], tile, P), tile_bytes, bar);
   }
-  (void)node;
-  (void)flags;
 }
 
 // o[jj][q] = sum_i P_q[i][jj] x[i][q] with the pair matrices of one side in
@@ -171,32 +169,25 @@ __global__ void __launch_bounds__(NT, ta_min_blocks(KQ)) ta_backward_kernel(cons
   for (int i = tid; i < a.C * 4; i += NT) tab2[i] = make_float2(a.table[i], a.table[i]);
   __syncthreads();
 
-  // producer state (thread 0): the next reversed step to stage, and its record
-  // once read from the ring when its outside tile is not written yet
+  // producer state (thread 0): the next reversed step to stage
   int next_issue = 0;
-  bool has_pend = false;
-  int4 pend[3];
   bool timed_out = false;
-  // stage steps up to `limit`
-  auto issue = [&](int limit) {
+  auto issue = [&](int limit) {  // stage steps up to `limit`
     while (next_issue < nst && next_issue <= limit) {
-      if (!has_pend) {
-        if (!ring.get(next_issue, pend)) {
-          timed_out = true;
-          return;
-        }
-        has_pend = true;
+      int4 rec[3];
+      if (!ring.get(next_issue, rec)) {
+        timed_out = true;
+        return;
       }
       const int st = next_issue % NSTAGE;
-      ta_issue(a, KQ, stages + st * G.bytes, &bars[st], pend, nst - 1 - next_issue, b, tile, P, G);
-      has_pend = false;
+      ta_issue(a, KQ, stages + st * G.bytes, &bars[st], rec, nst - 1 - next_issue, b, tile, P, G);
       ++next_issue;
     }
   };
   auto give_up = [&](int consumed) {  // wait (bounded) for the copies in flight, then leave
     if (tid == 0) {
       tl_drain(NSTAGE, bars, consumed, next_issue - 1, a.status);
-      ring.drain(next_issue + (has_pend ? 1 : 0));
+      ring.drain(next_issue);
     }
   };
   if (tid == 0) {
