@@ -611,7 +611,7 @@ def main():
                 "bytes_model": "level-by-level pruning traffic (5 partial passes per evaluation)",
                 "dram_achieved": kernels[dom]["dram_gbs"], "dram_frac": kernels[dom]["dram_gbs"] / peak,
                 "kernels": kernels}
-    if S != 4:  # amino-acid / codon: level-scheduled kernels; flops per SURVEY-style model
+    if S != 4:  # amino-acid / codon: level-scheduled kernels; algorithmic flops of the products
         s_flop = 2 * S * S * K * N * b  # one S x S matrix applied to one category's patterns
         fw_flops = I * 2 * s_flop
         bw_flops = 2 * fw_flops + (2 * T - 2) * s_flop
