@@ -169,3 +169,23 @@ def test_results_same_alone_and_in_the_mix():
         np.testing.assert_allclose(b["lnl"], a["lnl"], rtol=1e-12, err_msg=str(k))
         for g in ("grad_branch_lengths", "grad_exch", "grad_pi", "grad_shape"):
             np.testing.assert_allclose(b[g], a[g], rtol=1e-12, atol=1e-12 * np.abs(a[g]).max(), err_msg=f"{k} {g}")
+
+
+def test_autotune_candidates_cover_the_kernel_shape_options():
+    """Host logic only: the option sets the tuner times for each kind of plan."""
+    from types import SimpleNamespace
+
+    from torchtree_gb300 import _native, autotune
+
+    dna = autotune.candidates(SimpleNamespace(precision="f32", state_count=4))
+    assert len(dna) >= 3
+    for opts in dna:
+        assert 2 <= opts[_native.TT_OPT_FWD_STAGES] <= 8 and 2 <= opts[_native.TT_OPT_BWD_STAGES] <= 8
+    # the default shape (in-place adjoint, producer warp, one thread per pattern) comes first
+    first = dna[0]
+    assert first[_native.TT_OPT_INPLACE_ADJOINT] == 1 and first[_native.TT_OPT_PRODUCER_WARP] == 1
+    assert first[_native.TT_OPT_PAIR_THREADS] == 0
+    assert {o[_native.TT_OPT_INPLACE_ADJOINT] for o in dna} == {0, 1}
+    codon = autotune.candidates(SimpleNamespace(precision="f32", state_count=61))
+    assert {o[_native.TT_OPT_TENSOR_CORES] for o in codon} == {0, 1}
+    assert autotune.candidates(SimpleNamespace(precision="f64", state_count=4)) == [{}]
