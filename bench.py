@@ -51,6 +51,9 @@ def parse():
     ap.add_argument("--sites", type=int, default=None, help="override the workload's site count")
     ap.add_argument("--tips", type=int, default=None, help="override the workload's tip count")
     ap.add_argument("--batch", type=int, default=None, help="override the workload's batch")
+    ap.add_argument("--slab-patterns", type=int, default=None,
+                    help="4-state plans: hold this many patterns' partials at once (the gradient recomputes "
+                         "the post-order slab by slab)")
     ap.add_argument("--serving", action="store_true",
                     help="serving mix instead of the batched step: Poisson arrivals from many chains over "
                          "resident data sets, continuous batching through captured CUDA graphs")
@@ -530,6 +533,9 @@ def main():
                                 precision=precision, device=dev)
 
     eng = make_engine(args.precision)
+    if args.slab_patterns is not None:
+        eng.set_option(_native.TT_OPT_SLAB_PATTERNS, args.slab_patterns)
+    slab = eng.get_option(_native.TT_OPT_SLAB_PATTERNS) if S == 4 else 0
     stream = torch.cuda.current_stream()
 
     def step(e):
@@ -697,7 +703,10 @@ def main():
                        "model": {"gtr": "GTR", "hky": "HKY", "general": "general symmetric 20-state",
                                  "mg94": "MG94 codon (GY94-style)"}[wl.model] + f"+Gamma{K}",
                        "l2": "inputs (stored partials) larger than L2; no flush",
-                       "parallelism": f"replicas x{world}"},
+                       "parallelism": f"replicas x{world}",
+                       **({"slab_patterns": slab,
+                           "slabs": "partials held one pattern slab at a time; the pre_order_adjoint time "
+                                    "includes the post-order recompute"} if slab else {})},
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "what": "one batched lnL+gradient call (all samples)"},
             "fp64_dropin": fp64,

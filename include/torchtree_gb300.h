@@ -285,7 +285,18 @@ int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
  *   TT_OPT_INPLACE_ADJOINT: FP32 4-state adjoint that writes the outside
  *     partials over the stored post-order tiles (1, the default: a second
  *     tt_gradient then needs a new tt_log_likelihood with keep_partials=1)
- *     or keeps them in a shared-memory stack (0).
+ *     or keeps them in a shared-memory stack (0);
+ *   TT_OPT_SLAB_PATTERNS: 4-state plans: how many patterns' post-order
+ *     partials are held at once (rounded up to a multiple of 512; 0 = all,
+ *     the default when they fit).  With a slab size set, tt_log_likelihood
+ *     stores nothing and tt_gradient recomputes the post-order one slab at a
+ *     time before each slab's adjoint (one extra post-order pass; a second
+ *     tt_gradient for the same matrices needs no new tt_log_likelihood).
+ *     tt_plan_create picks a slab size itself when the whole alignment's
+ *     partials and per-tile gradient blocks would take more than 7/8 of the
+ *     free device memory.  Setting it reallocates those buffers and drops
+ *     any kept partials.  Results equal the unslabbed ones up to the order
+ *     of the FP64 sums over slabs.
  * tt_plan_get_option reads the value in use.
  */
 enum {
@@ -294,7 +305,8 @@ enum {
   TT_OPT_TENSOR_CORES = 3,
   TT_OPT_PAIR_THREADS = 4,
   TT_OPT_PRODUCER_WARP = 5,
-  TT_OPT_INPLACE_ADJOINT = 6
+  TT_OPT_INPLACE_ADJOINT = 6,
+  TT_OPT_SLAB_PATTERNS = 7
 };
 int tt_plan_set_option(tt_plan *plan, int32_t option, int32_t value);
 int tt_plan_get_option(const tt_plan *plan, int32_t option, int32_t *value);

@@ -4,6 +4,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <cstdint>
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
@@ -289,6 +290,101 @@ tt::PruneArgs<T> make_args(tt_plan *p, const double *props, const double *freqs,
   return a;
 }
 
+// ------------------------------------------------------------ pattern slabs
+// Patterns are independent, so the post-order and adjoint of one slab of
+// patterns equal the corresponding tiles of a whole-alignment pass.  A slab
+// starts at a multiple of kSlabAlign patterns: a whole number of 64- and
+// 32-pattern tiles, of the tile-sum blocks of 8 tiles, and of 128-byte code
+// runs (so every code copy stays inside the padded tip row).
+constexpr int kSlabAlign = 512;
+
+int slab_round(long long patterns, int N) {
+  if (patterns <= 0) return 0;
+  const long long r = (patterns + kSlabAlign - 1) / kSlabAlign * kSlabAlign;
+  return r >= N ? 0 : int(r);
+}
+
+// Bytes of the gradient buffers (stored partials, per-tile gradient blocks,
+// per-tile root blocks) for `npat` patterns, with dev_alloc's 16-byte floor.
+struct GradBytes {
+  size_t partials, gpart, rootpart;
+  size_t total() const { return std::max(partials, size_t(16)) + std::max(gpart, size_t(16)) + std::max(rootpart, size_t(16)); }
+};
+
+GradBytes grad_bytes(const tt_plan *p, int npat) {
+  const bool f32 = p->precision == TT_PRECISION_F32;
+  const size_t kss = size_t(p->K) * p->S * p->S;
+  const size_t I1 = size_t(std::max(p->I - 1, 1));
+  // FP32 plans: category pairs (K padded to even), partials per tile (N padded to whole tiles)
+  const size_t kpad = f32 ? size_t(2 * tt::kpairs_for(p->K)) : size_t(p->K);
+  const size_t ntb = (size_t(npat) + p->tile_b - 1) / p->tile_b;
+  const size_t npad = f32 ? ntb * p->tile_b : size_t(npat);
+  GradBytes g;
+  g.partials = size_t(p->batch) * I1 * kpad * npad * p->S * p->elem;
+  g.gpart = size_t(p->batch) * p->B * ntb * kss * p->elem;
+  g.rootpart = size_t(p->batch) * ntb * (p->S + p->K) * p->elem;
+  return g;
+}
+
+void free_grad_buffers(tt_plan *p) {
+  for (void **b : {&p->d_partials, &p->d_gpart, &p->d_rootpart})
+    if (*b) {
+      cudaFree(*b);
+      *b = nullptr;
+    }
+  p->bytes -= std::min(p->bytes, p->grad_bytes);
+  p->grad_bytes = 0;
+}
+
+// (Re)allocate the gradient buffers for slabs of `slab` patterns (0 = all).
+// On failure the plan keeps no gradient buffers: tt_log_likelihood without
+// keep_partials still works, and a smaller slab may be set.
+int alloc_grad_buffers(tt_plan *p, int slab) {
+  free_grad_buffers(p);
+  p->partials_valid = false;
+  p->grads_valid = false;
+  const GradBytes g = grad_bytes(p, slab ? slab : p->N);
+  const size_t before = p->bytes;
+  int rc = dev_alloc(p, &p->d_partials, g.partials, "partials");
+  if (!rc) rc = dev_alloc(p, &p->d_gpart, g.gpart, "gradient tiles");
+  if (!rc) rc = dev_alloc(p, &p->d_rootpart, g.rootpart, "root tiles");
+  p->grad_bytes = p->bytes - before;
+  if (rc) {
+    const std::string msg = g_last_error;
+    free_grad_buffers(p);
+    return fail(rc, msg + " (a smaller TT_OPT_SLAB_PATTERNS holds fewer patterns' partials at once)");
+  }
+  p->slab = slab;
+  return TT_OK;
+}
+
+// Restrict pruning arguments to patterns [p0, p0 + n) with `tile`-pattern tiles.
+template <typename T>
+void slab_args(tt::PruneArgs<T> &a, int p0, int n, int tile) {
+  a.codes += p0;
+  a.weights += p0;
+  a.N = n;
+  a.ntiles = (n + tile - 1) / tile;
+  a.site_lnl = nullptr;
+}
+
+// Post-order pass over patterns [p0, p0 + n) in the plan's kernel shape;
+// store = keep the partials of that range (for the adjoint).
+template <typename T>
+cudaError_t post_order(tt_plan *p, const double *props, const double *freqs, int rescale, bool store,
+                       double *site_lnl, int p0, int n, cudaStream_t s) {
+  auto a = make_args<T>(p, props, freqs, rescale, store, site_lnl);
+  if (p0 != 0 || n != p->N) slab_args(a, p0, n, p->tile_f);
+  if constexpr (sizeof(T) == 4) {
+    a.slots = p->producer_warp && !p->pair_threads ? p->slots_ws : p->slots_fwd;
+    return tt::launch_prune_f32(a, false, p->tile_f, p->batch,
+                                (p->pair_threads ? tt::kF32PairThreads : 0) | (p->producer_warp ? tt::kF32ProducerWarp : 0), s);
+  } else {
+    a.slots = p->slots_fwd;
+    return tt::launch_prune_f64(a, false, p->tile_f, p->batch, s);
+  }
+}
+
 }  // namespace
 
 extern "C" {
@@ -404,7 +500,6 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
   p->code_stride = (p->N + tt::kCodeAlign - 1) / tt::kCodeAlign * tt::kCodeAlign;
 
   const size_t kss = size_t(p->K) * p->S * p->S;
-  const size_t I1 = size_t(std::max(p->I - 1, 1));
   rc = TT_OK;
   if (!rc) rc = dev_alloc(p, &p->d_steps, p->steps.size() * sizeof(int), "schedule");
   if (!rc) rc = dev_alloc(p, &p->d_steps_rev, p->steps.size() * sizeof(int), "reversed schedule");
@@ -413,19 +508,38 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
   if (!rc) rc = dev_alloc(p, &p->d_codes, size_t(p->T) * p->code_stride, "tip codes");
   if (!rc) rc = dev_alloc(p, &p->d_table, size_t(256) * p->S * p->elem, "code table");
   if (!rc) rc = dev_alloc(p, &p->d_weights, size_t(p->N) * sizeof(double), "weights");
-  // FP32 plans: category pairs (K padded to even), partials per tile (N padded to whole tiles)
+  // FP32 plans: category pairs (K padded to even)
   const size_t kpad = f32 ? size_t(2 * tt::kpairs_for(p->K)) : size_t(p->K);
-  const size_t npad = f32 ? size_t(p->ntiles_b) * p->tile_b : size_t(p->N);
   if (!rc) rc = dev_alloc(p, &p->d_pmat, size_t(batch) * p->I * 2 * kpad * p->S * p->S * p->elem, "transition matrices");
-  if (!rc) rc = dev_alloc(p, &p->d_partials, size_t(batch) * I1 * kpad * npad * p->S * p->elem, "partials");
   if (!rc) rc = dev_alloc(p, &p->d_tile_lnl, size_t(batch) * p->ntiles_f * sizeof(double), "tile sums");
-  if (!rc)
-    rc = dev_alloc(p, &p->d_gpart, size_t(batch) * p->B * p->ntiles_b * kss * p->elem, "gradient tiles");
-  if (!rc)
-    rc = dev_alloc(p, &p->d_rootpart, size_t(batch) * p->ntiles_b * (p->S + p->K) * p->elem, "root tiles");
   if (!rc) rc = dev_alloc(p, &p->d_G, size_t(batch) * p->B * kss * sizeof(double), "dlnL/dP");
   if (!rc) rc = dev_alloc(p, &p->d_rootgrad, size_t(batch) * (p->S + p->K) * sizeof(double), "root grads");
   if (!rc) rc = dev_alloc(p, &p->d_status, sizeof(int), "status");
+  if (!rc) {
+    // Stored partials for the whole alignment when they fit in 7/8 of the
+    // free device memory (or TT_GRADIENT_BUDGET_BYTES), else pattern slabs
+    // sized to it: the gradient then recomputes the post-order slab by slab.
+    // TT_SLAB_PATTERNS sets the slab explicitly.
+    int slab = 0;
+    if (const char *env = getenv("TT_SLAB_PATTERNS")) {
+      slab = slab_round(atoll(env), p->N);
+    } else {
+      size_t free_b = 0, total_b = 0;
+      size_t budget = SIZE_MAX;  // no slabs when the free memory cannot be read
+      if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+        budget = free_b - free_b / 8;
+      else
+        cudaGetLastError();
+      if (const char *env2 = getenv("TT_GRADIENT_BUDGET_BYTES")) budget = std::min(budget, size_t(atoll(env2)));
+      const size_t full = grad_bytes(p, p->N).total();
+      if (full > budget) {
+        const double per_pattern = double(full) / p->N;
+        slab = std::max(kSlabAlign, int(double(budget) / per_pattern) / kSlabAlign * kSlabAlign);
+        slab = slab_round(slab, p->N);
+      }
+    }
+    rc = alloc_grad_buffers(p, slab);
+  }
   if (rc) {
     release(p);
     delete p;
@@ -578,20 +692,17 @@ int tt_log_likelihood(tt_plan *p, const double *props, const double *freqs, int3
     p->partials_valid = keep_partials != 0;
     return TT_OK;
   }
-  cudaError_t e;
-  if (p->precision == TT_PRECISION_F32) {
-    auto a = make_args<float>(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, site_lnl);
-    a.slots = p->producer_warp && !p->pair_threads ? p->slots_ws : p->slots_fwd;
-    e = tt::launch_prune_f32(a, false, p->tile_f, p->batch, (p->pair_threads ? tt::kF32PairThreads : 0) | (p->producer_warp ? tt::kF32ProducerWarp : 0), s);
-  } else {
-    auto a = make_args<double>(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, site_lnl);
-    a.slots = p->slots_fwd;
-    e = tt::launch_prune_f64(a, false, p->tile_f, p->batch, s);
-  }
+  if (keep_partials && !p->d_partials)
+    return fail(TT_ERR_OUT_OF_MEMORY, "the plan holds no gradient buffers: set TT_OPT_SLAB_PATTERNS to a size that fits");
+  // in slab mode the partials are recomputed by tt_gradient, slab by slab
+  const bool store = keep_partials != 0 && !p->slab;
+  cudaError_t e = p->precision == TT_PRECISION_F32 ? post_order<float>(p, props, freqs, rescale ? 1 : 0, store, site_lnl, 0, p->N, s)
+                                                   : post_order<double>(p, props, freqs, rescale ? 1 : 0, store, site_lnl, 0, p->N, s);
   if (e != cudaSuccess) return cuda_fail(e, "post-order launch");
   e = tt::launch_reduce_lnl(p->d_tile_lnl, lnl, p->batch, p->ntiles_f, s);
   if (e != cudaSuccess) return cuda_fail(e, "likelihood reduction launch");
   p->launches += 2;
+  p->last_rescale = rescale ? 1 : 0;
   p->partials_valid = keep_partials != 0;
   return TT_OK;
 }
@@ -612,33 +723,48 @@ int tt_gradient(tt_plan *p, const double *props, const double *freqs, double *gr
     p->grads_valid = true;
     return TT_OK;
   }
-  cudaError_t e;
-  if (p->precision == TT_PRECISION_F32) {
-    auto a = make_args<float>(p, props, freqs, 1, true, nullptr);
-    a.slots = p->slots_bwd;
-    a.ntiles = p->ntiles_b;
-    a.nstage = p->nstage_b;
-    e = tt::launch_prune_f32(a, true, p->tile_b, p->batch,
-                             p->pair_threads ? tt::kF32PairThreads : (p->inplace_adjoint ? tt::kF32InPlaceAdjoint : 0), s);
-    if (e == cudaSuccess)
-      e = tt::launch_reduce_f32(static_cast<const float *>(p->d_gpart),
-                                static_cast<const float *>(p->d_rootpart), p->d_G, p->d_rootgrad,
-                                p->d_rootgrad + size_t(p->batch) * p->S, p->batch, p->B, p->ntiles_b, p->S,
-                                p->K, s);
-  } else {
-    auto a = make_args<double>(p, props, freqs, 1, true, nullptr);
-    a.slots = p->slots_bwd;
-    a.ntiles = p->ntiles_b;
-    e = tt::launch_prune_f64(a, true, p->tile_b, p->batch, s);
-    if (e == cudaSuccess)
-      e = tt::launch_reduce_f64(static_cast<const double *>(p->d_gpart),
-                                static_cast<const double *>(p->d_rootpart), p->d_G, p->d_rootgrad,
-                                p->d_rootgrad + size_t(p->batch) * p->S, p->batch, p->B, p->ntiles_b, p->S,
-                                p->K, s);
+  if (!p->d_partials || !p->d_gpart || !p->d_rootpart)
+    return fail(TT_ERR_OUT_OF_MEMORY, "the plan holds no gradient buffers: set TT_OPT_SLAB_PATTERNS to a size that fits");
+  // one pass over all patterns, or per slab: post-order (storing) + adjoint +
+  // tile sums added to the previous slabs'
+  const int span = p->slab ? p->slab : p->N;
+  cudaError_t e = cudaSuccess;
+  for (int p0 = 0; p0 < p->N && e == cudaSuccess; p0 += span) {
+    const int n = std::min(span, p->N - p0);
+    if (p->slab) {
+      e = p->precision == TT_PRECISION_F32 ? post_order<float>(p, props, freqs, p->last_rescale, true, nullptr, p0, n, s)
+                                           : post_order<double>(p, props, freqs, p->last_rescale, true, nullptr, p0, n, s);
+      p->launches += 1;
+      if (e != cudaSuccess) break;
+    }
+    const int ntiles = (n + p->tile_b - 1) / p->tile_b;
+    if (p->precision == TT_PRECISION_F32) {
+      auto a = make_args<float>(p, props, freqs, 1, true, nullptr);
+      a.slots = p->slots_bwd;
+      a.nstage = p->nstage_b;
+      slab_args(a, p0, n, p->tile_b);
+      e = tt::launch_prune_f32(a, true, p->tile_b, p->batch,
+                               p->pair_threads ? tt::kF32PairThreads : (p->inplace_adjoint ? tt::kF32InPlaceAdjoint : 0), s);
+      if (e == cudaSuccess)
+        e = tt::launch_reduce_f32(static_cast<const float *>(p->d_gpart),
+                                  static_cast<const float *>(p->d_rootpart), p->d_G, p->d_rootgrad,
+                                  p->d_rootgrad + size_t(p->batch) * p->S, p->batch, p->B, ntiles, p->S,
+                                  p->K, p0 > 0, s);
+    } else {
+      auto a = make_args<double>(p, props, freqs, 1, true, nullptr);
+      a.slots = p->slots_bwd;
+      slab_args(a, p0, n, p->tile_b);
+      e = tt::launch_prune_f64(a, true, p->tile_b, p->batch, s);
+      if (e == cudaSuccess)
+        e = tt::launch_reduce_f64(static_cast<const double *>(p->d_gpart),
+                                  static_cast<const double *>(p->d_rootpart), p->d_G, p->d_rootgrad,
+                                  p->d_rootgrad + size_t(p->batch) * p->S, p->batch, p->B, ntiles, p->S,
+                                  p->K, p0 > 0, s);
+    }
+    p->launches += 3;
   }
   if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
-  p->launches += 3;
-  if (p->precision == TT_PRECISION_F32 && !p->pair_threads && p->inplace_adjoint)
+  if (p->precision == TT_PRECISION_F32 && !p->pair_threads && p->inplace_adjoint && !p->slab)
     p->partials_valid = false;  // the outside partials overwrote the post-order tiles
   const size_t kss = size_t(p->K) * p->S * p->S;
   if (grad_matrices) {
@@ -741,18 +867,35 @@ int tt_plan_set_option(tt_plan *p, int32_t option, int32_t value) {
       if (value && (p->wide || p->precision != TT_PRECISION_F32))
         return fail(TT_ERR_UNSUPPORTED, "the producer-warp post-order serves FP32 4-state plans");
       if (value && p->nstage_f > 8) return fail(TT_ERR_UNSUPPORTED, "the producer-warp post-order takes <= 8 stages");
+      if (p->producer_warp != (value != 0)) p->partials_valid = false;
       p->producer_warp = value != 0;
       return TT_OK;
     case TT_OPT_PAIR_THREADS:
       if (value && (p->wide || p->precision != TT_PRECISION_F32 || !tt::pair_threads_supported(p->K)))
         return fail(TT_ERR_UNSUPPORTED, "pair-thread kernels serve FP32 4-state plans with 1-4 or 7-8 categories");
+      if (p->pair_threads != (value != 0)) p->partials_valid = false;  // another partial layout
       p->pair_threads = value != 0;
       return TT_OK;
     case TT_OPT_INPLACE_ADJOINT:
       if (value && (p->wide || p->precision != TT_PRECISION_F32))
         return fail(TT_ERR_UNSUPPORTED, "the in-place adjoint serves FP32 4-state plans");
+      if (p->inplace_adjoint != (value != 0)) p->partials_valid = false;
       p->inplace_adjoint = value != 0;
       return TT_OK;
+    case TT_OPT_SLAB_PATTERNS: {
+      if (p->wide) return fail(TT_ERR_UNSUPPORTED, "pattern slabs serve 4-state plans");
+      if (value < 0) return fail(TT_ERR_INVALID_ARGUMENT, "the slab size must be >= 0 (0 = all patterns)");
+      const int slab = slab_round(value, p->N);
+      if (slab == p->slab && p->d_partials) return TT_OK;
+      const int old = p->slab;
+      const int rc = alloc_grad_buffers(p, slab);
+      if (rc) {
+        const std::string msg = g_last_error;
+        alloc_grad_buffers(p, old);  // keep the previous buffers when they can be had again
+        return fail(rc, msg);
+      }
+      return TT_OK;
+    }
     default:
       return fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
   }
@@ -767,6 +910,7 @@ int tt_plan_get_option(const tt_plan *p, int32_t option, int32_t *value) {
     case TT_OPT_PAIR_THREADS: *value = p->pair_threads ? 1 : 0; return TT_OK;
     case TT_OPT_PRODUCER_WARP: *value = p->producer_warp ? 1 : 0; return TT_OK;
     case TT_OPT_INPLACE_ADJOINT: *value = p->inplace_adjoint ? 1 : 0; return TT_OK;
+    case TT_OPT_SLAB_PATTERNS: *value = p->slab; return TT_OK;
     default: return fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
   }
 }

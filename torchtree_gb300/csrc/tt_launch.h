@@ -69,12 +69,14 @@ bool pair_threads_supported(int K);
 cudaError_t launch_prune_f64(const PruneArgs<double> &a, bool backward, int tile, int batch,
                              cudaStream_t stream);
 
+// Sum the per-tile gradient blocks into G / dfreq / dprop; accumulate = 1
+// adds to what is there (pattern slabs after the first).
 cudaError_t launch_reduce_f32(const float *gpart, const float *rootpart, double *G, double *dfreq,
-                              double *dprop, int batch, int B, int ntiles, int S, int K,
+                              double *dprop, int batch, int B, int ntiles, int S, int K, int accumulate,
                               cudaStream_t stream);
 cudaError_t launch_reduce_f64(const double *gpart, const double *rootpart, double *G,
                               double *dfreq, double *dprop, int batch, int B, int ntiles, int S,
-                              int K, cudaStream_t stream);
+                              int K, int accumulate, cudaStream_t stream);
 cudaError_t launch_reduce_lnl(const double *tile_lnl, double *lnl, int batch, int ntiles,
                               cudaStream_t stream);
 

@@ -24,6 +24,11 @@ struct tt_plan {
   bool producer_warp = true;  // FP32 4-state post-order with a producer warp
   bool inplace_adjoint = true;  // FP32 4-state adjoint storing outside partials over the post-order tiles
   bool tips_set = false, pmat_set = false, partials_valid = false, grads_valid = false;
+  // 4-state plans: patterns whose post-order partials are held at once (0 =
+  // all).  When nonzero, tt_gradient recomputes the post-order one pattern
+  // slab at a time into buffers of that size.
+  int slab = 0;
+  int last_rescale = 1;  // rescale flag of the last post-order (repeated by the slab recompute)
   long long launches = 0;
   std::vector<int> steps;       // host copy of the schedule (I x 12)
   std::vector<int> steps_ws;    // records of the producer-warp post-order (I x 12)
@@ -46,6 +51,7 @@ struct tt_plan {
   int *d_status = nullptr;
   double *d_qpart = nullptr;  // rate-matrix gradient partials (first use)
   size_t bytes = 0;
+  size_t grad_bytes = 0;  // of `bytes`: the stored partials and per-tile gradient blocks
   tt::WideState *wide = nullptr;  // non-NULL for S != 4 plans
 };
 

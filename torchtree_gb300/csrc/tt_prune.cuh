@@ -627,7 +627,8 @@ __global__ void __launch_bounds__(TILE) prune_backward_kernel(const PruneArgs<T>
 // ------------------------------------------------------------- reductions
 // dlnL/dP[b][branch] = sum over pattern tiles (fixed order, FP64).
 template <typename T>
-__global__ void reduce_branch_grads_kernel(const T *gpart, double *G, int branch_count, int ntiles, int kss) {
+__global__ void reduce_branch_grads_kernel(const T *gpart, double *G, int branch_count, int ntiles, int kss,
+                                           int accumulate) {
   const int branch = blockIdx.x, b = blockIdx.y;
   const T *src = gpart + (size_t(b) * branch_count + branch) * ntiles * size_t(kss);
   for (int e = threadIdx.x; e < kss; e += blockDim.x) {
@@ -642,22 +643,24 @@ __global__ void reduce_branch_grads_kernel(const T *gpart, double *G, int branch
       acc += double((s0 + s1) + (s2 + s3));
     }
     for (; t < ntiles; ++t) acc += double(src[size_t(t) * kss + e]);
-    G[(size_t(b) * branch_count + branch) * kss + e] = acc;
+    double *g = G + (size_t(b) * branch_count + branch) * kss + e;
+    *g = accumulate ? *g + acc : acc;
   }
 }
 
 template <typename T>
 __global__ void reduce_root_grads_kernel(const T *rootpart, double *dfreq, double *dprop, int ntiles, int S,
-                                         int K) {
+                                         int K, int accumulate) {
   const int b = blockIdx.x;
   const int RK = S + K;
   for (int e = threadIdx.x; e < RK; e += blockDim.x) {
     double acc = 0.0;
     for (int t = 0; t < ntiles; ++t) acc += double(rootpart[(size_t(b) * ntiles + t) * RK + e]);
     if (e < S) {
-      if (dfreq) dfreq[b * S + e] = acc;
+      if (dfreq) dfreq[b * S + e] = accumulate ? dfreq[b * S + e] + acc : acc;
     } else if (dprop) {
-      dprop[b * K + (e - S)] = acc;
+      double *d = dprop + b * K + (e - S);
+      *d = accumulate ? *d + acc : acc;
     }
   }
 }

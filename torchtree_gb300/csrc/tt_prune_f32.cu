@@ -131,12 +131,12 @@ cudaError_t launch_prune_f32(const PruneArgs<float> &a, bool backward, int tile,
 }
 
 cudaError_t launch_reduce_f32(const float *gpart, const float *rootpart, double *G, double *dfreq,
-                              double *dprop, int batch, int B, int ntiles, int S, int K,
+                              double *dprop, int batch, int B, int ntiles, int S, int K, int accumulate,
                               cudaStream_t stream) {
   const int kss = K * S * S;
   reduce_branch_grads_kernel<float><<<dim3(B, batch), kss <= 64 ? 64 : 128, 0, stream>>>(
-      gpart, G, B, ntiles, kss);
-  reduce_root_grads_kernel<float><<<batch, 32, 0, stream>>>(rootpart, dfreq, dprop, ntiles, S, K);
+      gpart, G, B, ntiles, kss, accumulate);
+  reduce_root_grads_kernel<float><<<batch, 32, 0, stream>>>(rootpart, dfreq, dprop, ntiles, S, K, accumulate);
   return cudaGetLastError();
 }
 

@@ -66,11 +66,11 @@ cudaError_t launch_prune_f64(const PruneArgs<double> &a, bool backward, int tile
 
 cudaError_t launch_reduce_f64(const double *gpart, const double *rootpart, double *G,
                               double *dfreq, double *dprop, int batch, int B, int ntiles, int S,
-                              int K, cudaStream_t stream) {
+                              int K, int accumulate, cudaStream_t stream) {
   const int kss = K * S * S;
   reduce_branch_grads_kernel<double><<<dim3(B, batch), kss <= 64 ? 64 : 128, 0, stream>>>(
-      gpart, G, B, ntiles, kss);
-  reduce_root_grads_kernel<double><<<batch, 32, 0, stream>>>(rootpart, dfreq, dprop, ntiles, S, K);
+      gpart, G, B, ntiles, kss, accumulate);
+  reduce_root_grads_kernel<double><<<batch, 32, 0, stream>>>(rootpart, dfreq, dprop, ntiles, S, K, accumulate);
   return cudaGetLastError();
 }
 
