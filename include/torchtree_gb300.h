@@ -128,7 +128,9 @@ int tt_log_likelihood(tt_plan *plan, const double *category_weights,
  * tt_transition_matrices_gradient.  FP32 plans (unless
  * TT_OPT_INPLACE_ADJOINT is 0) and plans with S != 4 consume the stored
  * partials: a second tt_gradient needs a new tt_log_likelihood with
- * keep_partials=1 (TT_ERR_NOT_READY otherwise).
+ * keep_partials=1 (TT_ERR_NOT_READY otherwise).  4-state plans with pattern
+ * slabs (TT_OPT_SLAB_PATTERNS) recompute the post-order here, one slab at a
+ * time, and need no new tt_log_likelihood.
  */
 int tt_gradient(tt_plan *plan, const double *category_weights,
                 const double *frequencies, double *grad_matrices,
