@@ -202,6 +202,19 @@ def cpu_baseline(wl, ca, n_patterns, repeats=3):
             "seconds_per_sample_eval": per_eval}
 
 
+def fp32_error(got, want):
+    """FP32 results against the FP64 drop-in on the same inputs (the drop-in
+    equals the FP64 oracle to 1e-10 in the parity tests): lnL relative error
+    per sample, and each gradient's largest error relative to its largest
+    entry (dlnL/dQ, dlnL/dt, dlnL/dr)."""
+    lnl, want_lnl = got[0], want[0]
+    out = {"vs": "FP64 drop-in on the same inputs",
+           "lnl_max_rel_err": float(((lnl - want_lnl).abs() / want_lnl.abs()).max())}
+    for name, g, w in zip(("dq", "dbranch", "drate"), got[1:], want[1:]):
+        out[f"{name}_max_err_rel_to_max"] = float((g - w).abs().max() / w.abs().max().clamp_min(1e-300))
+    return out
+
+
 def run_reference(args):
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
@@ -540,9 +553,9 @@ def main():
 
     def step(e):
         e.set_eigen(lam, u, w, bls, rates)
-        e.log_likelihood(probs, pi, rescale=True, keep_partials=True)
+        lnl = e.log_likelihood(probs, pi, rescale=True, keep_partials=True)
         e.gradient(probs, pi)
-        return e.rate_matrix_gradient(lam, u, w, bls, rates)
+        return (lnl,) + e.rate_matrix_gradient(lam, u, w, bls, rates)
 
     for _ in range(max(args.warmup, 3)):
         step(eng)
@@ -636,14 +649,16 @@ def main():
         if tr:
             roofline["traffic"] = tr
 
-    # FP64 drop-in on the same workload
-    fp64 = None
+    # FP64 drop-in on the same workload; its results measure the FP32 error
+    fp64, accuracy = None, None
     if args.fp64_steps > 0 and args.precision == "f32":
+        got = [x.cpu() for x in step(eng)]
         del eng
         torch.cuda.empty_cache()
         e64 = make_engine("f64")
-        step(e64)
+        want = [x.cpu() for x in step(e64)]
         torch.cuda.synchronize()
+        accuracy = fp32_error(got, want)
         a, z = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
         for _ in range(args.fp64_steps):
@@ -710,6 +725,7 @@ def main():
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "what": "one batched lnL+gradient call (all samples)"},
             "fp64_dropin": fp64,
+            "accuracy": accuracy,
             "speedup_vs_fp64": (value / world / fp64["value"]) if fp64 else None,
             "lnl_only": lnl_only,
             "roofline": roofline, "cpu_baseline": cpu, "e2e": e2e, "gpu_launches": launches,
