@@ -1,0 +1,85 @@
+"""torchtree's own known answer on its bundled influenza A data, where the
+reference source tree is present (it is not copied into this repository).
+
+test/test_tree_likelihood.py:268-342 builds a time tree from fluA.tree with
+tip dates parsed from the taxon names and internal heights from the Newick
+branch lengths (keep_branch_lengths: the ratios are the inverse
+GeneralNodeHeightTransform of those heights), a strict clock of 0.001, JC69
+and a 4-category Weibull site model of shape 0.1, and asserts
+lnL = -4618.2062529058 with and without rescaling.  Here the same chain runs
+through this package's Newick parser, tip-date heights and pattern
+compression and the oracle's ratio transform and pruning, which pins the
+oracle's time-tree, clock and Weibull chain to the reference's own number.
+The source location is TORCHTREE_REFERENCE, else the default below; the test
+is skipped where the data are absent.
+"""
+import os
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+KAT = -4618.2062529058
+DATA = Path(os.environ.get("TORCHTREE_REFERENCE", "/root/reference")) / "data"
+
+pytestmark = pytest.mark.skipif(not (DATA / "fluA.fa").exists(), reason="reference data not present")
+
+
+def _fasta(path):
+    names, seqs = [], []
+    for line in path.read_text().splitlines():
+        line = line.strip()
+        if line.startswith(">"):
+            names.append(line[1:].strip())
+            seqs.append([])
+        elif line:
+            seqs[-1].append(line)
+    return names, ["".join(s) for s in seqs]
+
+
+def _sampling_times(names):
+    """Leaf heights from the dates that end the taxon names (tree_model.py:363-378)."""
+    dates = np.array([float(n.split("_")[-1]) for n in names])
+    return dates if dates.min() == 0.0 else dates.max() - dates
+
+
+def test_flu_a_time_tree_weibull_strict_clock_known_answer():
+    from oracle import likelihood as OL
+    from oracle import timetree as OT
+    from torchtree_gb300 import patterns
+    from torchtree_gb300.tree import Topology, node_heights_from_lengths
+
+    names, seqs = _fasta(DATA / "fluA.fa")
+    topo = Topology.from_newick((DATA / "fluA.tree").read_text().strip(), names)
+    T = topo.tip_count
+    assert T == 69
+    times = _sampling_times(names)
+    # keep_branch_lengths: the ratios given in the test are replaced by the
+    # inverse transform of the heights that the Newick lengths imply
+    # (tree_model.py:700-705, 110-122); the forward transform returns them
+    heights = node_heights_from_lengths(topo, times, min_length=1e-6)
+    lb = OT.lower_bounds(topo.postorder_list(), times.tolist())
+    ratios = torch.zeros(T - 1, dtype=torch.float64)
+    ratios[T - 2] = heights[2 * T - 2]
+    for v in range(T, 2 * T - 2):
+        up = heights[topo.parent[v]]
+        ratios[v - T] = (heights[v] - lb[v - T]) / (up - lb[v - T])
+    internal, time_lengths, _ = OT.ratio_transform(topo.postorder_list(), times.tolist(), ratios)
+    np.testing.assert_allclose(internal.numpy(), heights[T:], rtol=1e-12)
+    bls = OL.model_branch_lengths(time_lengths, torch.tensor(0.001, dtype=torch.float64))
+    ca = patterns.compress(seqs)
+    tips = [torch.tensor(t) for t in ca.tip_partials()]
+    weights = torch.tensor(ca.weights, dtype=torch.float64)
+    rates, props = OL.weibull_rates(torch.tensor([0.1], dtype=torch.float64), 4)
+    mats = OL.p_t_jc69(bls.unsqueeze(-1) * rates)  # [B, K, 4, 4]
+    freqs = torch.full((1, 4), 0.25, dtype=torch.float64)
+    p = props.reshape(4, 1, 1)
+    parts = tips + [None] * (T - 1)
+    post = topo.postorder_list()
+    plain = OL.treelikelihood_discrete(parts, weights, post, mats, freqs, p)
+    scaled = OL.treelikelihood_discrete_rescaled(parts, weights, post, mats, freqs, p)
+    # the reference asserts torch.allclose (rtol 1e-5); the value it prints has
+    # 10 decimals, and the oracle lands 4e-11 from it
+    assert abs(float(plain) - KAT) < 1e-9
+    assert abs(float(scaled) - KAT) < 1e-9

@@ -199,12 +199,15 @@ class Topology:
         return rec(self.root) + ";"
 
 
-def node_heights_from_lengths(topo: Topology, tip_heights=None) -> np.ndarray:
-    """Heights of all nodes when tips sit at ``tip_heights`` (default 0)."""
+def node_heights_from_lengths(topo: Topology, tip_heights=None, min_length: float = 0.0) -> np.ndarray:
+    """Heights of all nodes when tips sit at ``tip_heights`` (default 0): a
+    parent sits at the highest child plus its branch, each branch counted as
+    at least ``min_length`` (torchtree's heights_from_branch_lengths,
+    tree_model.py:110-122, uses 1e-6)."""
     T = topo.tip_count
     h = np.zeros(2 * T - 1)
     if tip_heights is not None:
         h[:T] = tip_heights
     for v, l, r in topo.postorder:
-        h[v] = max(h[l] + topo.edge_lengths[l], h[r] + topo.edge_lengths[r])
+        h[v] = max(h[l] + max(min_length, topo.edge_lengths[l]), h[r] + max(min_length, topo.edge_lengths[r]))
     return h
