@@ -48,7 +48,7 @@ def test_flu_a_time_tree_weibull_strict_clock_known_answer():
     from oracle import likelihood as OL
     from oracle import timetree as OT
     from torchtree_gb300 import patterns
-    from torchtree_gb300.tree import Topology, node_heights_from_lengths
+    from torchtree_gb300.tree import Topology
 
     names, seqs = _fasta(DATA / "fluA.fa")
     topo = Topology.from_newick((DATA / "fluA.tree").read_text().strip(), names)
@@ -58,15 +58,9 @@ def test_flu_a_time_tree_weibull_strict_clock_known_answer():
     # keep_branch_lengths: the ratios given in the test are replaced by the
     # inverse transform of the heights that the Newick lengths imply
     # (tree_model.py:700-705, 110-122); the forward transform returns them
-    heights = node_heights_from_lengths(topo, times, min_length=1e-6)
-    lb = OT.lower_bounds(topo.postorder_list(), times.tolist())
-    ratios = torch.zeros(T - 1, dtype=torch.float64)
-    ratios[T - 2] = heights[2 * T - 2]
-    for v in range(T, 2 * T - 2):
-        up = heights[topo.parent[v]]
-        ratios[v - T] = (heights[v] - lb[v - T]) / (up - lb[v - T])
+    ratios, heights = _ratios_from_newick(topo, times)
     internal, time_lengths, _ = OT.ratio_transform(topo.postorder_list(), times.tolist(), ratios)
-    np.testing.assert_allclose(internal.numpy(), heights[T:], rtol=1e-12)
+    np.testing.assert_allclose(internal.numpy(), heights, rtol=1e-12)
     bls = OL.model_branch_lengths(time_lengths, torch.tensor(0.001, dtype=torch.float64))
     ca = patterns.compress(seqs)
     tips = [torch.tensor(t) for t in ca.tip_partials()]
@@ -83,3 +77,49 @@ def test_flu_a_time_tree_weibull_strict_clock_known_answer():
     # 10 decimals, and the oracle lands 4e-11 from it
     assert abs(float(plain) - KAT) < 1e-9
     assert abs(float(scaled) - KAT) < 1e-9
+
+
+def _ratios_from_newick(topo, times):
+    """Ratios whose transform gives the Newick heights (tree_model.py:700-705)."""
+    from oracle import timetree as OT
+    from torchtree_gb300.tree import node_heights_from_lengths
+
+    T = topo.tip_count
+    heights = node_heights_from_lengths(topo, times, min_length=1e-6)
+    lb = OT.lower_bounds(topo.postorder_list(), times.tolist())
+    ratios = torch.zeros(T - 1, dtype=torch.float64)
+    ratios[T - 2] = heights[2 * T - 2]
+    for v in range(T, 2 * T - 2):
+        ratios[v - T] = (heights[v] - lb[v - T]) / (heights[topo.parent[v]] - lb[v - T])
+    return ratios, heights[T:]
+
+
+@pytest.mark.gpu
+def test_flu_a_known_answer_through_the_gpu_path():
+    """The same known answer through the product path on the GPU: the ratio
+    transform kernel gives the time lengths, the pruning kernels the lnL.
+    FP64 unscaled and rescaled within 1e-12 relative; FP32 within 1e-6."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from torchtree_gb300 import patterns, site_models, substitution
+    from torchtree_gb300.likelihood import PhyloLikelihood
+    from torchtree_gb300.timetree import TimeTree
+    from torchtree_gb300.tree import Topology
+
+    names, seqs = _fasta(DATA / "fluA.fa")
+    topo = Topology.from_newick((DATA / "fluA.tree").read_text().strip(), names)
+    times = _sampling_times(names)
+    ratios, heights = _ratios_from_newick(topo, times)
+    dev = torch.device("cuda")
+    h, time_lengths, _ = TimeTree(topo.postorder, times).ratio_transform(ratios[None].to(dev))
+    np.testing.assert_allclose(h[0].cpu().numpy(), heights, rtol=1e-12)
+    ca = patterns.compress(seqs)
+    pi = torch.full((1, 4), 0.25, dtype=torch.float64, device=dev)
+    q = substitution.gtr_q(torch.ones(1, 6, dtype=torch.float64, device=dev), pi)  # JC69
+    rates, props = site_models.weibull_rates(torch.tensor([[0.1]], dtype=torch.float64, device=dev), 4)
+    clock = torch.tensor([[0.001]], dtype=torch.float64, device=dev)
+    for precision, rescale, tol in (("f64", False, 1e-12), ("f64", True, 1e-12), ("f32", True, 1e-6)):
+        lik = PhyloLikelihood(topo, ca, 4, 4, batch=1, precision=precision)
+        lik.rescale = rescale
+        lnl = float(lik(time_lengths, q, pi, rates, props.expand(1, 4), clock_rates=clock)[0])
+        assert abs(lnl - KAT) < tol * abs(KAT), (precision, rescale, lnl)
