@@ -105,3 +105,17 @@ def test_small_trees_and_tied_heights(T):
         lp0 = tree.constant_coalescent(h0, theta.cuda())
         lpc0 = OT.constant_coalescent(times.tolist(), hc0, theta)
         np.testing.assert_allclose(lp0.cpu().numpy(), lpc0.numpy(), rtol=1e-11)
+
+
+def test_constant_coalescent_known_answers():
+    """torchtree's own numbers (test_coalescent.py:46-67) through the kernels:
+    ((A,B),C),D sampled at 0, ratios (2/6, 6/12, 12) under theta 3 and the
+    doubled batch member (4/6, 1, 24) under theta 6."""
+    from torchtree_gb300.timetree import TimeTree
+
+    tree = TimeTree([[4, 0, 1], [5, 4, 2], [6, 5, 3]], np.zeros(4))
+    ratios = torch.tensor([[2.0 / 6.0, 6.0 / 12.0, 12.0], [4.0 / 6.0, 1.0, 24.0]], dtype=torch.float64, device="cuda")
+    h, _, _ = tree.ratio_transform(ratios)
+    np.testing.assert_allclose(h.cpu().numpy(), [[2.0, 6.0, 12.0], [16.0, 24.0, 24.0]], rtol=1e-15)
+    lp = tree.constant_coalescent(h, torch.tensor([3.0, 6.0], dtype=torch.float64, device="cuda"))
+    np.testing.assert_allclose(lp.cpu().numpy(), [-13.295836866, -25.375278407684164], rtol=1e-9)

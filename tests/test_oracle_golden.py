@@ -246,3 +246,23 @@ def test_oracle_time_tree_operations_match_reference(key):
     gh, gth = torch.autograd.grad(lp.sum(), [hh, th])
     np.testing.assert_allclose(gh.numpy(), c["coalescent_grad_heights"], rtol=1e-12, atol=1e-12)
     assert abs(gth.item() - c["coalescent_grad_theta"]) < 1e-12 * max(1.0, abs(c["coalescent_grad_theta"]))
+
+
+# torchtree's constant-coalescent known answers (test_coalescent.py:46-67):
+# tips A-D sampled at 0, ((A,B),C),D with ratios 2/6, 6/12 and root height 12
+# (heights 2, 6, 12) under theta 3, and the batch member with every value
+# doubled (heights 16, 24, 24) under theta 6.
+COALESCENT_KAT = ((2.0, 6.0, 12.0, 3.0, -13.295836866), (16.0, 24.0, 24.0, 6.0, -25.375278407684164))
+
+
+def test_constant_coalescent_known_answers():
+    from oracle import timetree as OT
+
+    for h0, h1, h2, theta, want in COALESCENT_KAT:
+        lp = OT.constant_coalescent([0.0] * 4, torch.tensor([[h0, h1, h2]], dtype=torch.float64),
+                                    torch.tensor([theta], dtype=torch.float64))
+        assert abs(float(lp[0]) - want) < 1e-8 * abs(want)
+    # the same heights from the ratio transform of ((A,B),C),D
+    post = [[4, 0, 1], [5, 4, 2], [6, 5, 3]]
+    h, _, _ = OT.ratio_transform(post, [0.0] * 4, torch.tensor([2.0 / 6.0, 6.0 / 12.0, 12.0], dtype=torch.float64))
+    np.testing.assert_allclose(h.numpy(), [2.0, 6.0, 12.0], rtol=1e-15)
