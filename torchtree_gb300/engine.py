@@ -88,7 +88,9 @@ class LikelihoodEngine:
         return int(n.value)
 
     def set_option(self, option: int, value: int) -> None:
-        """Kernel-shape option (``_native.TT_OPT_*``); results do not depend on it."""
+        """Plan option (``_native.TT_OPT_*``): kernel shapes, which leave results
+        unchanged, or ``TT_OPT_SLAB_PATTERNS``, which changes only the grouping
+        of the gradient's FP64 sums over pattern slabs."""
         check(self.lib.tt_plan_set_option(self._plan, int(option), int(value)))
 
     def get_option(self, option: int) -> int:
