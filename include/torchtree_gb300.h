@@ -272,8 +272,10 @@ int tt_constant_coalescent(tt_time_tree *tree, int32_t batch,
 int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
 
 /*
- * Kernel-shape options of a plan, for autotuning (no reference counterpart:
- * the reference has no kernels to shape).  Results do not depend on them.
+ * Options of a plan (no reference counterpart: the reference has no kernels
+ * to shape and keeps autograd's whole graph).  Kernel shapes, for
+ * autotuning, leave results unchanged; the pattern-slab size changes only
+ * the grouping of FP64 sums.
  *   TT_OPT_FWD_STAGES / TT_OPT_BWD_STAGES: staging-ring depth of the FP32
  *     4-state post-order / adjoint kernels (2..8; rejected when the ring
  *     does not fit in shared memory);
