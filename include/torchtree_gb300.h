@@ -128,9 +128,9 @@ int tt_log_likelihood(tt_plan *plan, const double *category_weights,
  * tt_transition_matrices_gradient.  FP32 plans (unless
  * TT_OPT_INPLACE_ADJOINT is 0) and plans with S != 4 consume the stored
  * partials: a second tt_gradient needs a new tt_log_likelihood with
- * keep_partials=1 (TT_ERR_NOT_READY otherwise).  4-state plans with pattern
- * slabs (TT_OPT_SLAB_PATTERNS) recompute the post-order here, one slab at a
- * time, and need no new tt_log_likelihood.
+ * keep_partials=1 (TT_ERR_NOT_READY otherwise).  Plans with pattern slabs
+ * (TT_OPT_SLAB_PATTERNS) recompute the post-order here, one slab at a time,
+ * and need no new tt_log_likelihood.
  */
 int tt_gradient(tt_plan *plan, const double *category_weights,
                 const double *frequencies, double *grad_matrices,
@@ -290,12 +290,14 @@ int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
  *     partials over the stored post-order tiles (1, the default: a second
  *     tt_gradient then needs a new tt_log_likelihood with keep_partials=1)
  *     or keeps them in a shared-memory stack (0);
- *   TT_OPT_SLAB_PATTERNS: 4-state plans: how many patterns' post-order
- *     partials are held at once (rounded up to a multiple of 512; 0 = all,
- *     the default when they fit).  With a slab size set, tt_log_likelihood
- *     stores nothing and tt_gradient recomputes the post-order one slab at a
- *     time before each slab's adjoint (one extra post-order pass; a second
- *     tt_gradient for the same matrices needs no new tt_log_likelihood).
+ *   TT_OPT_SLAB_PATTERNS: how many patterns' post-order partials are held
+ *     at once (rounded up to a multiple of 512; 0 = all, the default when
+ *     they fit).  With a slab size set, tt_gradient recomputes the post-order
+ *     one slab at a time before each slab's adjoint, and a second
+ *     tt_gradient for the same matrices needs no new tt_log_likelihood.
+ *     4-state plans: tt_log_likelihood stores nothing (one extra post-order
+ *     pass per gradient).  20/61-state plans: tt_log_likelihood also runs
+ *     slab by slab and leaves the last slab's partials for the gradient.
  *     tt_plan_create picks a slab size itself when the whole alignment's
  *     partials and per-tile gradient blocks would take more than 7/8 of the
  *     free device memory.  Setting it reallocates those buffers and drops

@@ -114,3 +114,79 @@ def test_plan_picks_slabs_when_the_gradient_buffers_exceed_the_budget():
     assert slab > 0 and slab % 512 == 0
     assert eng.workspace_bytes < whole.workspace_bytes
     _close(_evaluate(eng, eig, props, pi, True), want)
+
+
+def _wide_problem(kind, precision):
+    from torchtree_gb300 import datatype, patterns, site_models, substitution, synthetic
+
+    if kind == "protein":
+        wl = synthetic.protein_workload("p", tip_count=30, site_count=3000, batch=2, seed=81, shape=0.5)
+    else:
+        wl = synthetic.codon_workload("c", tip_count=20, site_count=3000, batch=2, seed=82, shape=0.5)
+    dt = datatype.get(wl.data_type)
+    ca = patterns.compress(wl.sequences, dt)
+    b, K, S = wl.branch_lengths.shape[0], wl.categories, dt.state_count
+    pi = torch.tensor(wl.pi, dtype=torch.float64)
+    ex = torch.tensor(wl.exch, dtype=torch.float64)
+    if wl.model == "mg94":
+        q = substitution.mg94_q(torch.ones_like(ex[:, :1]), ex[:, 1:2], ex[:, :1], pi)
+    else:
+        q = substitution.general_symmetric_q(ex, pi, S)
+    dev = torch.device("cuda")
+    lam, u, w = (t.to(dev).contiguous() for t in substitution.eigen_system(q, pi))
+    rates, probs = site_models.gamma_rates(torch.tensor(wl.shape, dtype=torch.float64), K)
+    bls = torch.cat([torch.tensor(wl.branch_lengths), torch.zeros(b, 1, dtype=torch.float64)], -1)
+    eig = [lam, u, w, bls.to(dev).contiguous(), rates.to(dev).contiguous()]
+    return wl.topology, ca, S, K, b, eig, probs.expand(b, K).to(dev).contiguous(), pi.to(dev)
+
+
+@pytest.mark.parametrize("kind,precision,tc", [
+    ("protein", "f64", None), ("protein", "f32", None),
+    ("codon", "f64", None), ("codon", "f32", 1), ("codon", "f32", 0),
+])
+def test_wide_slabs_equal_the_whole_alignment(kind, precision, tc):
+    """20- and 61-state plans run both passes slab by slab.  Per-pattern
+    results (site lnL) are bit-identical; lnL differs by the grouping of its
+    FP64 sum; gradients by the grouping of the chunk sums (FP64 plans 1e-12,
+    FP32 plans 1e-5 of the largest entry).  The first gradient after
+    tt_log_likelihood reuses the last slab's post-order, the second
+    recomputes it: both are bit-identical."""
+    from torchtree_gb300 import _native
+    from torchtree_gb300.engine import LikelihoodEngine
+
+    topo, ca, S, K, b, eig, props, pi = _wide_problem(kind, precision)
+    N = ca.weights.shape[0]
+    assert N > 1100
+    eng = LikelihoodEngine(topo.postorder, topo.tip_count, S, K, ca.codes, ca.table, ca.weights, batch=b,
+                           precision=precision)
+    if tc is not None:
+        eng.set_option(_native.TT_OPT_TENSOR_CORES, tc)
+
+    def run(second=False):
+        eng.set_eigen(*eig)
+        lnl, site = eng.log_likelihood(props, pi, rescale=True, keep_partials=True, site=True)
+        out = [x.cpu().numpy() for x in (lnl, site, *eng.gradient(props, pi, want_matrices=True))]
+        if second:
+            again = [x.cpu().numpy() for x in eng.gradient(props, pi, want_matrices=True)]
+            for a, g in zip(again, out[2:]):
+                np.testing.assert_array_equal(a, g)
+        assert eng.device_status() == 0
+        return out
+
+    whole = run()
+    whole_bytes = eng.workspace_bytes
+    gtol = 1e-12 if precision == "f64" else 1e-5
+    for slab in (512, 1024):
+        eng.set_option(_native.TT_OPT_SLAB_PATTERNS, slab)
+        assert eng.get_option(_native.TT_OPT_SLAB_PATTERNS) == slab
+        assert eng.workspace_bytes < whole_bytes
+        got = run(second=True)
+        np.testing.assert_allclose(got[0], whole[0], rtol=1e-13)
+        np.testing.assert_array_equal(got[1], whole[1])
+        for g, w in zip(got[2:], whole[2:]):
+            np.testing.assert_allclose(g, w, rtol=gtol, atol=gtol * np.abs(w).max())
+    eng.set_option(_native.TT_OPT_SLAB_PATTERNS, 0)
+    assert eng.workspace_bytes == whole_bytes
+    again = run()
+    for a, w in zip(again, whole):
+        np.testing.assert_array_equal(a, w)

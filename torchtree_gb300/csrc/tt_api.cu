@@ -358,6 +358,25 @@ int alloc_grad_buffers(tt_plan *p, int slab) {
   return TT_OK;
 }
 
+// Slab size of a new plan whose pattern-sized buffers take `full` bytes for
+// the whole alignment: none when they fit in 7/8 of the free device memory
+// (or TT_GRADIENT_BUDGET_BYTES), else slabs sized to that budget.
+// TT_SLAB_PATTERNS sets the slab explicitly.
+int choose_slab(const tt_plan *p, size_t full) {
+  if (const char *env = getenv("TT_SLAB_PATTERNS")) return slab_round(atoll(env), p->N);
+  size_t free_b = 0, total_b = 0;
+  size_t budget = SIZE_MAX;  // no slabs when the free memory cannot be read
+  if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
+    budget = free_b - free_b / 8;
+  else
+    cudaGetLastError();
+  if (const char *env = getenv("TT_GRADIENT_BUDGET_BYTES")) budget = std::min(budget, size_t(atoll(env)));
+  if (full <= budget) return 0;
+  const double per_pattern = double(full) / p->N;
+  const long long fit = (long long)(double(budget) / per_pattern) / kSlabAlign * kSlabAlign;
+  return slab_round(std::max<long long>(kSlabAlign, fit), p->N);
+}
+
 // Restrict pruning arguments to patterns [p0, p0 + n) with `tile`-pattern tiles.
 template <typename T>
 void slab_args(tt::PruneArgs<T> &a, int p0, int n, int tile) {
@@ -430,6 +449,7 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
   }
   if (p->S != 4) {  // amino-acid / codon / general models: level-scheduled wide-state kernels
     rc = tt::wide_create(p);
+    if (rc == TT_OK) rc = tt::wide_alloc_slab(p, choose_slab(p, tt::wide_pattern_bytes(p, p->N)));
     if (rc != TT_OK) {
       release(p);
       delete p;
@@ -516,29 +536,7 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
   if (!rc) rc = dev_alloc(p, &p->d_rootgrad, size_t(batch) * (p->S + p->K) * sizeof(double), "root grads");
   if (!rc) rc = dev_alloc(p, &p->d_status, sizeof(int), "status");
   if (!rc) {
-    // Stored partials for the whole alignment when they fit in 7/8 of the
-    // free device memory (or TT_GRADIENT_BUDGET_BYTES), else pattern slabs
-    // sized to it: the gradient then recomputes the post-order slab by slab.
-    // TT_SLAB_PATTERNS sets the slab explicitly.
-    int slab = 0;
-    if (const char *env = getenv("TT_SLAB_PATTERNS")) {
-      slab = slab_round(atoll(env), p->N);
-    } else {
-      size_t free_b = 0, total_b = 0;
-      size_t budget = SIZE_MAX;  // no slabs when the free memory cannot be read
-      if (cudaMemGetInfo(&free_b, &total_b) == cudaSuccess)
-        budget = free_b - free_b / 8;
-      else
-        cudaGetLastError();
-      if (const char *env2 = getenv("TT_GRADIENT_BUDGET_BYTES")) budget = std::min(budget, size_t(atoll(env2)));
-      const size_t full = grad_bytes(p, p->N).total();
-      if (full > budget) {
-        const double per_pattern = double(full) / p->N;
-        slab = std::max(kSlabAlign, int(double(budget) / per_pattern) / kSlabAlign * kSlabAlign);
-        slab = slab_round(slab, p->N);
-      }
-    }
-    rc = alloc_grad_buffers(p, slab);
+    rc = alloc_grad_buffers(p, choose_slab(p, grad_bytes(p, p->N).total()));
   }
   if (rc) {
     release(p);
@@ -687,8 +685,11 @@ int tt_log_likelihood(tt_plan *p, const double *props, const double *freqs, int3
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   if (p->wide) {
+    if (!tt::wide_has_buffers(p))
+      return fail(TT_ERR_OUT_OF_MEMORY, "the plan holds no partial buffers: set TT_OPT_SLAB_PATTERNS to a size that fits");
     rc = tt::wide_log_likelihood(p, props, freqs, rescale ? 1 : 0, keep_partials != 0, lnl, site_lnl, s);
     if (rc) return rc;
+    p->last_rescale = rescale ? 1 : 0;
     p->partials_valid = keep_partials != 0;
     return TT_OK;
   }
@@ -699,7 +700,7 @@ int tt_log_likelihood(tt_plan *p, const double *props, const double *freqs, int3
   cudaError_t e = p->precision == TT_PRECISION_F32 ? post_order<float>(p, props, freqs, rescale ? 1 : 0, store, site_lnl, 0, p->N, s)
                                                    : post_order<double>(p, props, freqs, rescale ? 1 : 0, store, site_lnl, 0, p->N, s);
   if (e != cudaSuccess) return cuda_fail(e, "post-order launch");
-  e = tt::launch_reduce_lnl(p->d_tile_lnl, lnl, p->batch, p->ntiles_f, s);
+  e = tt::launch_reduce_lnl(p->d_tile_lnl, lnl, p->batch, p->ntiles_f, 0, s);
   if (e != cudaSuccess) return cuda_fail(e, "likelihood reduction launch");
   p->launches += 2;
   p->last_rescale = rescale ? 1 : 0;
@@ -716,10 +717,12 @@ int tt_gradient(tt_plan *p, const double *props, const double *freqs, double *gr
   int rc = check_device(p);
   if (rc) return rc;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  if (p->wide) {  // the wide-state adjoint overwrites the stored partials
+  if (p->wide) {  // the wide-state adjoint overwrites the stored partials (slab mode recomputes them)
+    if (!tt::wide_has_buffers(p))
+      return fail(TT_ERR_OUT_OF_MEMORY, "the plan holds no partial buffers: set TT_OPT_SLAB_PATTERNS to a size that fits");
     rc = tt::wide_gradient(p, props, freqs, grad_matrices, grad_frequencies, grad_weights, s);
     if (rc) return rc;
-    p->partials_valid = false;
+    p->partials_valid = p->slab != 0;
     p->grads_valid = true;
     return TT_OK;
   }
@@ -883,15 +886,15 @@ int tt_plan_set_option(tt_plan *p, int32_t option, int32_t value) {
       p->inplace_adjoint = value != 0;
       return TT_OK;
     case TT_OPT_SLAB_PATTERNS: {
-      if (p->wide) return fail(TT_ERR_UNSUPPORTED, "pattern slabs serve 4-state plans");
       if (value < 0) return fail(TT_ERR_INVALID_ARGUMENT, "the slab size must be >= 0 (0 = all patterns)");
       const int slab = slab_round(value, p->N);
-      if (slab == p->slab && p->d_partials) return TT_OK;
+      auto alloc = [p](int n) { return p->wide ? tt::wide_alloc_slab(p, n) : alloc_grad_buffers(p, n); };
+      if (slab == p->slab && (p->wide ? tt::wide_has_buffers(p) : p->d_partials != nullptr)) return TT_OK;
       const int old = p->slab;
-      const int rc = alloc_grad_buffers(p, slab);
+      const int rc = alloc(slab);
       if (rc) {
         const std::string msg = g_last_error;
-        alloc_grad_buffers(p, old);  // keep the previous buffers when they can be had again
+        alloc(old);  // keep the previous buffers when they can be had again
         return fail(rc, msg);
       }
       return TT_OK;

@@ -271,7 +271,7 @@ extern "C" int tt_log_likelihood_static(int32_t tip_count, const int32_t *postor
   a.status = d_status;
   a.timeout_ns = 2000000000ull;
   e = tt::launch_prune_f64(a, false, tile, batch, s);
-  if (e == cudaSuccess) e = tt::launch_reduce_lnl(d_tiles, log_likelihood, batch, ntiles, s);
+  if (e == cudaSuccess) e = tt::launch_reduce_lnl(d_tiles, log_likelihood, batch, ntiles, 0, s);
   if (e != cudaSuccess) return fail(TT_ERR_CUDA, cudaGetErrorString(e));
   return TT_OK;
 }

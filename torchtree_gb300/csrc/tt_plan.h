@@ -24,9 +24,10 @@ struct tt_plan {
   bool producer_warp = true;  // FP32 4-state post-order with a producer warp
   bool inplace_adjoint = true;  // FP32 4-state adjoint storing outside partials over the post-order tiles
   bool tips_set = false, pmat_set = false, partials_valid = false, grads_valid = false;
-  // 4-state plans: patterns whose post-order partials are held at once (0 =
-  // all).  When nonzero, tt_gradient recomputes the post-order one pattern
-  // slab at a time into buffers of that size.
+  // patterns whose post-order partials are held at once (0 = all).  When
+  // nonzero, tt_gradient recomputes the post-order one pattern slab at a
+  // time into buffers of that size (wide plans also run tt_log_likelihood
+  // slab by slab).
   int slab = 0;
   int last_rescale = 1;  // rescale flag of the last post-order (repeated by the slab recompute)
   long long launches = 0;
@@ -57,7 +58,12 @@ struct tt_plan {
 
 namespace tt {
 // Wide-state path (tt_wide.cu): same contracts as the C entry points.
-int wide_create(tt_plan *p);
+int wide_create(tt_plan *p);  // everything but the pattern-sized buffers
+// bytes of the pattern-sized buffers for passes over n patterns
+size_t wide_pattern_bytes(const tt_plan *p, int n);
+// (re)allocate the pattern-sized buffers for slabs of `slab` patterns (0 = all)
+int wide_alloc_slab(tt_plan *p, int slab);
+bool wide_has_buffers(const tt_plan *p);
 void wide_destroy(tt_plan *p);
 int wide_set_tips(tt_plan *p, const uint8_t *codes, const double *code_table, int code_count,
                   const double *weights);

@@ -666,6 +666,6 @@ __global__ void reduce_root_grads_kernel(const T *rootpart, double *dfreq, doubl
 }
 
 // lnL[b] = sum over tiles (fixed-order tree reduction).
-__global__ void reduce_lnl_kernel(const double *tile_lnl, double *lnl, int ntiles);
+__global__ void reduce_lnl_kernel(const double *tile_lnl, double *lnl, int ntiles, int accumulate);
 
 }  // namespace tt

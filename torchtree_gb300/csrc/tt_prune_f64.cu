@@ -37,7 +37,7 @@ cudaError_t by_k(const PruneArgs<double> &a, int batch, cudaStream_t stream) {
 
 }  // namespace
 
-__global__ void reduce_lnl_kernel(const double *tile_lnl, double *lnl, int ntiles) {
+__global__ void reduce_lnl_kernel(const double *tile_lnl, double *lnl, int ntiles, int accumulate) {
   __shared__ double part[8];
   const int b = blockIdx.x;
   double acc = 0.0;
@@ -48,7 +48,7 @@ __global__ void reduce_lnl_kernel(const double *tile_lnl, double *lnl, int ntile
   if (threadIdx.x == 0) {
     double s = 0.0;
     for (int w = 0; w < int(blockDim.x >> 5); ++w) s += part[w];
-    lnl[b] = s;
+    lnl[b] = accumulate ? lnl[b] + s : s;
   }
 }
 
@@ -74,9 +74,9 @@ cudaError_t launch_reduce_f64(const double *gpart, const double *rootpart, doubl
   return cudaGetLastError();
 }
 
-cudaError_t launch_reduce_lnl(const double *tile_lnl, double *lnl, int batch, int ntiles,
+cudaError_t launch_reduce_lnl(const double *tile_lnl, double *lnl, int batch, int ntiles, int accumulate,
                               cudaStream_t stream) {
-  reduce_lnl_kernel<<<batch, 256, 0, stream>>>(tile_lnl, lnl, ntiles);
+  reduce_lnl_kernel<<<batch, 256, 0, stream>>>(tile_lnl, lnl, ntiles, accumulate);
   return cudaGetLastError();
 }
 

@@ -64,9 +64,17 @@ __global__ void wide_pmatrix_grad_reduce_kernel(const double *part, int nchunks,
 }
 
 struct WideState {
-  int SP = 0, PTf = 0, PTb = 0, Npad = 0, ntiles_f = 0, ntiles_b = 0, nchunks = 1, tpc = 1, nblk = 0;
+  int SP = 0, PTf = 0, PTb = 0;
+  int Npad = 0;  // whole alignment padded to 128 patterns: the tip-code row stride
   int bchunk = 8, nbchunks = 1;
   bool tc = false;  // FP32 codon post-order on the tensor cores
+  bool store_products = false;  // FP32 codon: the adjoint reads the post-order's children's products
+  // pattern slabs (p->slab != 0): the pattern-sized buffers below hold one
+  // slab; tail_valid = they still hold the last slab's post-order (from a
+  // tt_log_likelihood with keep_partials), which the gradient then reuses
+  bool tail_valid = false;
+  size_t slab_bytes = 0;     // of p->bytes: the pattern-sized buffers
+  double *d_site = nullptr;  // slab mode: one slab's site log-likelihoods [b][slab]
   std::vector<int> fwd_off, bwd_off;  // level boundaries in d_fwd / d_bwd
   int *d_left = nullptr, *d_right = nullptr, *d_fwd = nullptr, *d_bwd = nullptr;
   void *d_part = nullptr;
@@ -84,6 +92,28 @@ struct WideState {
 namespace {
 
 int wfail(int code, const std::string &m) { return record_error(code, m.c_str()); }
+
+// Launch geometry of a pass over `n` patterns (the whole alignment or one
+// slab): padded width, tiles of the two passes, root blocks, and the
+// adjoint's chunks of tiles (about two CTAs per SM over batch x categories;
+// cmax bounds the chunk count of any pass over at most n patterns).
+struct WideGeo {
+  int Npad, ntiles_f, ntiles_b, nblk, nchunks, tpc, cmax;
+};
+
+WideGeo wide_geo(const tt_plan *p, int n) {
+  const WideState &w = *p->wide;
+  WideGeo g;
+  g.Npad = (n + 127) / 128 * 128;
+  g.ntiles_f = g.Npad / w.PTf;
+  g.ntiles_b = g.Npad / w.PTb;
+  g.nblk = (n + 255) / 256;
+  const int want = (2 * 152 + p->batch * p->K - 1) / (p->batch * p->K);
+  g.cmax = std::max(1, std::min({want, g.ntiles_b, 64}));
+  g.tpc = (g.ntiles_b + g.cmax - 1) / g.cmax;
+  g.nchunks = (g.ntiles_b + g.tpc - 1) / g.tpc;
+  return g;
+}
 
 int wcuda(cudaError_t e, const char *where) {
   return wfail(e == cudaErrorMemoryAllocation ? TT_ERR_OUT_OF_MEMORY : TT_ERR_CUDA,
@@ -138,32 +168,36 @@ struct Wide {
   }
   static size_t pback_smem() { return 4 * SP * SP * sizeof(T) + (SP / 4 * SP + 3 * SP + 8) * sizeof(double); }
 
-  static WideArgs<T> args(tt_plan *p, const double *props, const double *freqs, int rescale) {
+  // arguments of a pass over patterns [p0, p0 + n) with geometry g: tip
+  // codes and weights from the slab's first pattern, every pattern-sized
+  // buffer with the slab's own width
+  static WideArgs<T> args(tt_plan *p, const double *props, const double *freqs, int rescale, const WideGeo &g,
+                          int p0, int n) {
     WideState &w = *p->wide;
     WideArgs<T> a;
     a.tips = p->T;
-    a.N = p->N;
-    a.Npad = w.Npad;
+    a.N = n;
+    a.Npad = g.Npad;
     a.K = p->K;
     a.B = p->B;
     a.I = p->I;
     a.S = p->S;
     a.code_stride = p->code_stride;
     a.rescale = rescale;
-    a.nchunks = w.nchunks;
-    a.tiles_per_chunk = w.tpc;
-    a.ntiles = w.ntiles_b;
+    a.nchunks = g.nchunks;
+    a.tiles_per_chunk = g.tpc;
+    a.ntiles = g.ntiles_b;
     a.nodes = nullptr;
     a.left = w.d_left;
     a.right = w.d_right;
-    a.codes = p->d_codes;
+    a.codes = p->d_codes + p0;
     a.table = static_cast<const T *>(p->d_table);
     a.pmat = static_cast<const T *>(p->d_pmat);
     a.part = static_cast<T *>(w.d_part);
     a.expo = w.d_expo;
     a.props = props;
     a.freqs = freqs;
-    a.weights = p->d_weights;
+    a.weights = p->d_weights + p0;
     a.root_site = w.d_root_site;
     a.root_expo = w.d_root_expo;
     a.log2L = w.d_log2L;
@@ -173,10 +207,13 @@ struct Wide {
     return a;
   }
 
+  // post-order over patterns [p0, p0 + n), root sums, and lnL (added to
+  // lnl when accumulate; no lnL when lnl is NULL).  site_lnl [b][n].
   static cudaError_t forward(tt_plan *p, const double *props, const double *freqs, int rescale, bool keep,
-                             double *lnl, double *site_lnl, cudaStream_t s) {
+                             double *lnl, double *site_lnl, int p0, int n, int accumulate, cudaStream_t s) {
     WideState &w = *p->wide;
-    WideArgs<T> a = args(p, props, freqs, rescale);
+    const WideGeo g = wide_geo(p, n);
+    WideArgs<T> a = args(p, props, freqs, rescale, g, p0, n);
     if (keep) a.prod = static_cast<T *>(w.d_prod);
     constexpr int NT = WideCfg<T, SP, PTF>::NT;
     const size_t smem = wide_fwd_smem<T, SP, PTF>();
@@ -184,40 +221,48 @@ struct Wide {
       a.nodes = w.d_fwd + w.fwd_off[lv];
       if constexpr (std::is_same<T, float>::value && SP == 64) {
         if (w.tc) {
-          const dim3 grid(w.Npad / tc::kPT, w.fwd_off[lv + 1] - w.fwd_off[lv], p->batch * p->K);
+          const dim3 grid(g.Npad / tc::kPT, w.fwd_off[lv + 1] - w.fwd_off[lv], p->batch * p->K);
           wide_forward_tc_kernel<<<grid, tc::kThreads, tc::kSmem, s>>>(a, p->d_status, 2000000000ull);
           p->launches += 1;
           continue;
         }
       }
-      const dim3 grid(w.ntiles_f, w.fwd_off[lv + 1] - w.fwd_off[lv], p->batch * p->K);
+      const dim3 grid(g.ntiles_f, w.fwd_off[lv + 1] - w.fwd_off[lv], p->batch * p->K);
       wide_forward_kernel<T, SP, PTF><<<grid, NT, smem, s>>>(a);
       p->launches += 1;
     }
-    wide_root_kernel<<<dim3(w.nblk, p->batch), 256, 0, s>>>(w.d_root_site, w.d_root_expo, props, p->d_weights,
-                                                           site_lnl, w.d_log2L, w.d_block_lnl, p->K, p->N, w.Npad);
-    cudaError_t e = launch_reduce_lnl(w.d_block_lnl, lnl, p->batch, w.nblk, s);
-    p->launches += 2;
+    wide_root_kernel<<<dim3(g.nblk, p->batch), 256, 0, s>>>(w.d_root_site, w.d_root_expo, props, a.weights,
+                                                           site_lnl, w.d_log2L, w.d_block_lnl, p->K, n, g.Npad);
+    p->launches += 1;
+    cudaError_t e = cudaSuccess;
+    if (lnl) {
+      e = launch_reduce_lnl(w.d_block_lnl, lnl, p->batch, g.nblk, accumulate, s);
+      p->launches += 1;
+    }
     return e == cudaSuccess ? cudaGetLastError() : e;
   }
 
-  static cudaError_t backward(tt_plan *p, const double *props, const double *freqs, cudaStream_t s) {
+  // adjoint over patterns [p0, p0 + n) after that range's post-order; the
+  // chunk sums are added to the previous slabs' when accumulate
+  static cudaError_t backward(tt_plan *p, const double *props, const double *freqs, int p0, int n, int accumulate,
+                              cudaStream_t s) {
     WideState &w = *p->wide;
-    WideArgs<T> a = args(p, props, freqs, 1);
+    const WideGeo g = wide_geo(p, n);
+    WideArgs<T> a = args(p, props, freqs, 1, g, p0, n);
     a.prod = static_cast<T *>(w.d_prod);
     constexpr int NT = WideCfg<T, SP, PTB>::NT;
     const size_t smem = wide_bwd_smem<T, SP, PTB>(a.prod != nullptr);
     for (size_t lv = 0; lv + 1 < w.bwd_off.size(); ++lv) {
       a.nodes = w.d_bwd + w.bwd_off[lv];
-      const dim3 grid(w.nchunks, w.bwd_off[lv + 1] - w.bwd_off[lv], p->batch * p->K);
+      const dim3 grid(g.nchunks, w.bwd_off[lv + 1] - w.bwd_off[lv], p->batch * p->K);
       wide_backward_kernel<T, SP, PTB><<<grid, NT, smem, s>>>(a);
       p->launches += 1;
     }
     wide_grad_reduce_kernel<T><<<dim3(p->B, p->batch), 256, 0, s>>>(static_cast<const T *>(w.d_gpart), p->d_G,
-                                                                     p->B, w.nchunks, p->K, p->S, SP);
+                                                                     p->B, g.nchunks, p->K, p->S, SP, accumulate);
     wide_root_reduce_kernel<T><<<p->batch, 64, 0, s>>>(static_cast<const T *>(w.d_rootpart), p->d_rootgrad,
-                                                       p->d_rootgrad + size_t(p->batch) * p->S, w.nchunks, p->K,
-                                                       p->S, SP);
+                                                       p->d_rootgrad + size_t(p->batch) * p->S, g.nchunks, p->K,
+                                                       p->S, SP, accumulate);
     p->launches += 2;
     return cudaGetLastError();
   }
@@ -265,16 +310,7 @@ int wide_create(tt_plan *p) {
   w->SP = p->S <= 20 ? 20 : 64;
   tiles_for(f32, w->SP, w->PTf, w->PTb);
   w->Npad = (p->N + 127) / 128 * 128;
-  w->ntiles_f = w->Npad / w->PTf;
-  w->ntiles_b = w->Npad / w->PTb;
-  w->nblk = (p->N + 255) / 256;
   if (size_t(p->batch) * p->K > 65535) return wfail(TT_ERR_INVALID_ARGUMENT, "batch * category_count must be <= 65535");
-  {
-    const int want = (2 * 152 + p->batch * p->K - 1) / (p->batch * p->K);
-    w->nchunks = std::max(1, std::min({want, w->ntiles_b, 64}));
-    w->tpc = (w->ntiles_b + w->nchunks - 1) / w->nchunks;
-    w->nchunks = (w->ntiles_b + w->tpc - 1) / w->tpc;
-  }
   w->nbchunks = (p->B + w->bchunk - 1) / w->bchunk;
   {  // tensor-core post-order for FP32 codon plans (TT_WIDE_TC=0 selects the CUDA-core kernel)
     const char *env = getenv("TT_WIDE_TC");
@@ -327,21 +363,14 @@ int wide_create(tt_plan *p) {
   if (!rc) rc = walloc(p, &p->d_table, 256 * SP * es, "code table");
   if (!rc) rc = walloc(p, &p->d_weights, size_t(p->N) * sizeof(double), "weights");
   if (!rc) rc = walloc(p, &p->d_pmat, b * p->B * K * SP * SP * es, "transition matrices");
-  if (!rc) rc = walloc(p, &w->d_part, b * I * K * SP * w->Npad * es, "partials");
-  if (!rc) rc = walloc(p, &w->d_expo, b * I * K * w->Npad * sizeof(int), "scale exponents");
   {  // FP32 codon plans keep the children's products for the adjoint (TT_WIDE_STORE_PRODUCTS=0
      // recomputes them): 84.1 -> 80.2 ms per call at 200 tips x 2,608 codon patterns x 16; with 20
      // states the extra stores cost more than the products they save
     const char *env = getenv("TT_WIDE_STORE_PRODUCTS");
-    if (!rc && f32 && SP == 64 && !(env && atoi(env) == 0))
-      rc = walloc(p, &w->d_prod, b * I * K * 2 * SP * w->Npad * es, "children's products");
+    w->store_products = f32 && SP == 64 && !(env && atoi(env) == 0);
   }
-  if (!rc) rc = walloc(p, &w->d_root_site, b * K * w->Npad * sizeof(double), "root sums");
-  if (!rc) rc = walloc(p, &w->d_root_expo, b * K * w->Npad * sizeof(int), "root exponents");
-  if (!rc) rc = walloc(p, &w->d_log2L, b * w->Npad * sizeof(double), "site log-likelihoods");
-  if (!rc) rc = walloc(p, &w->d_block_lnl, b * w->nblk * sizeof(double), "block sums");
-  if (!rc) rc = walloc(p, &w->d_gpart, b * p->B * w->nchunks * K * SP * SP * es, "gradient chunks");
-  if (!rc) rc = walloc(p, &w->d_rootpart, b * w->nchunks * K * (SP + 1) * es, "root gradient chunks");
+  // the pattern-sized buffers (partials, exponents, products, root and
+  // gradient chunks) come from wide_alloc_slab once the slab size is chosen
   if (!rc)
     rc = walloc(p, &w->d_pgpart, b * w->nbchunks * (2 * p->S * p->S + p->S + K) * sizeof(double),
                 "matrix gradient chunks");
@@ -360,6 +389,86 @@ int wide_create(tt_plan *p) {
   return TT_OK;
 }
 
+namespace {
+
+struct SlabBuffers {
+  size_t part, expo, prod, root_site, root_expo, log2L, block, gpart, rootpart, site;
+  size_t total() const {
+    size_t t = 0;
+    for (size_t x : {part, expo, prod, root_site, root_expo, log2L, block, gpart, rootpart, site})
+      t += x ? std::max(x, size_t(16)) : 0;
+    return t;
+  }
+};
+
+// Pattern-sized buffers for passes over at most n patterns (slab = n when
+// the plan works in slabs, 0 for the whole alignment).
+SlabBuffers slab_buffers(const tt_plan *p, int n, bool slab) {
+  const WideState &w = *p->wide;
+  const WideGeo g = wide_geo(p, n);
+  const size_t es = p->elem, SP = size_t(w.SP), b = size_t(p->batch), K = size_t(p->K), I = size_t(p->I);
+  SlabBuffers x;
+  x.part = b * I * K * SP * g.Npad * es;
+  x.expo = b * I * K * g.Npad * sizeof(int);
+  x.prod = w.store_products ? b * I * K * 2 * SP * g.Npad * es : 0;
+  x.root_site = b * K * g.Npad * sizeof(double);
+  x.root_expo = b * K * g.Npad * sizeof(int);
+  x.log2L = b * g.Npad * sizeof(double);
+  x.block = b * g.nblk * sizeof(double);
+  x.gpart = b * p->B * g.cmax * K * SP * SP * es;
+  x.rootpart = b * g.cmax * K * (SP + 1) * es;
+  x.site = slab ? b * size_t(n) * sizeof(double) : 0;
+  return x;
+}
+
+void free_slab_buffers(tt_plan *p) {
+  WideState &w = *p->wide;
+  for (void **x : {reinterpret_cast<void **>(&w.d_part), reinterpret_cast<void **>(&w.d_expo),
+                   reinterpret_cast<void **>(&w.d_prod), reinterpret_cast<void **>(&w.d_root_site),
+                   reinterpret_cast<void **>(&w.d_root_expo), reinterpret_cast<void **>(&w.d_log2L),
+                   reinterpret_cast<void **>(&w.d_block_lnl), reinterpret_cast<void **>(&w.d_gpart),
+                   reinterpret_cast<void **>(&w.d_rootpart), reinterpret_cast<void **>(&w.d_site)})
+    if (*x) {
+      cudaFree(*x);
+      *x = nullptr;
+    }
+  p->bytes -= std::min(p->bytes, w.slab_bytes);
+  w.slab_bytes = 0;
+}
+
+}  // namespace
+
+size_t wide_pattern_bytes(const tt_plan *p, int n) { return slab_buffers(p, n, false).total(); }
+
+int wide_alloc_slab(tt_plan *p, int slab) {
+  WideState &w = *p->wide;
+  free_slab_buffers(p);
+  p->partials_valid = false;
+  p->grads_valid = false;
+  w.tail_valid = false;
+  const SlabBuffers x = slab_buffers(p, slab ? slab : p->N, slab != 0);
+  const size_t before = p->bytes;
+  int rc = walloc(p, &w.d_part, x.part, "partials");
+  if (!rc) rc = walloc(p, &w.d_expo, x.expo, "scale exponents");
+  if (!rc && x.prod) rc = walloc(p, &w.d_prod, x.prod, "children's products");
+  if (!rc) rc = walloc(p, &w.d_root_site, x.root_site, "root sums");
+  if (!rc) rc = walloc(p, &w.d_root_expo, x.root_expo, "root exponents");
+  if (!rc) rc = walloc(p, &w.d_log2L, x.log2L, "site log-likelihoods");
+  if (!rc) rc = walloc(p, &w.d_block_lnl, x.block, "block sums");
+  if (!rc) rc = walloc(p, &w.d_gpart, x.gpart, "gradient chunks");
+  if (!rc) rc = walloc(p, &w.d_rootpart, x.rootpart, "root gradient chunks");
+  if (!rc && x.site) rc = walloc(p, &w.d_site, x.site, "slab site log-likelihoods");
+  w.slab_bytes = p->bytes - before;
+  if (rc) {
+    free_slab_buffers(p);
+    return rc;
+  }
+  p->slab = slab;
+  return TT_OK;
+}
+
+bool wide_has_buffers(const tt_plan *p) { return p->wide && p->wide->d_part; }
+
 int wide_set_tensor_cores(tt_plan *p, bool on) {
   if (!p->wide || p->precision != TT_PRECISION_F32 || p->wide->SP != 64)
     return on ? wfail(TT_ERR_UNSUPPORTED, "the tensor-core post-order serves FP32 codon (> 20-state) plans") : TT_OK;
@@ -373,7 +482,7 @@ void wide_destroy(tt_plan *p) {
   WideState *w = p->wide;
   if (!w) return;
   void *bufs[] = {w->d_left, w->d_right, w->d_fwd, w->d_bwd, w->d_part, w->d_expo, w->d_root_site, w->d_root_expo,
-                  w->d_log2L, w->d_block_lnl, w->d_gpart, w->d_rootpart, w->d_pgpart, w->d_prod};
+                  w->d_log2L, w->d_block_lnl, w->d_gpart, w->d_rootpart, w->d_pgpart, w->d_prod, w->d_site};
   for (void *x : bufs)
     if (x) cudaFree(x);
   delete w;
@@ -426,14 +535,53 @@ int wide_set_matrices(tt_plan *p, const double *matrices, cudaStream_t s) {
 
 int wide_log_likelihood(tt_plan *p, const double *props, const double *freqs, int rescale, bool keep, double *lnl,
                         double *site_lnl, cudaStream_t s) {
-  cudaError_t e =
-      dispatch(p, [&](auto X) { return decltype(X)::forward(p, props, freqs, rescale, keep, lnl, site_lnl, s); });
-  return e == cudaSuccess ? TT_OK : wcuda(e, "wide-state post-order launch");
+  WideState &w = *p->wide;
+  if (!p->slab) {
+    cudaError_t e = dispatch(
+        p, [&](auto X) { return decltype(X)::forward(p, props, freqs, rescale, keep, lnl, site_lnl, 0, p->N, 0, s); });
+    return e == cudaSuccess ? TT_OK : wcuda(e, "wide-state post-order launch");
+  }
+  // slab by slab, lnL summed over slabs; the last slab's post-order stays in
+  // the buffers for the gradient
+  cudaError_t e = cudaSuccess;
+  for (int p0 = 0; p0 < p->N && e == cudaSuccess; p0 += p->slab) {
+    const int n = std::min(p->slab, p->N - p0);
+    const bool last = p0 + n == p->N;
+    e = dispatch(p, [&](auto X) {
+      return decltype(X)::forward(p, props, freqs, rescale, keep && last, lnl, site_lnl ? w.d_site : nullptr, p0, n,
+                                  p0 > 0, s);
+    });
+    if (e == cudaSuccess && site_lnl)  // [b][n] rows into columns p0.. of [b][N]
+      e = cudaMemcpy2DAsync(site_lnl + p0, size_t(p->N) * sizeof(double), w.d_site, size_t(n) * sizeof(double),
+                            size_t(n) * sizeof(double), p->batch, cudaMemcpyDeviceToDevice, s);
+  }
+  if (e != cudaSuccess) return wcuda(e, "wide-state post-order launch");
+  w.tail_valid = keep;
+  return TT_OK;
 }
 
 int wide_gradient(tt_plan *p, const double *props, const double *freqs, double *grad_matrices,
                   double *grad_frequencies, double *grad_weights, cudaStream_t s) {
-  cudaError_t e = dispatch(p, [&](auto X) { return decltype(X)::backward(p, props, freqs, s); });
+  WideState &w = *p->wide;
+  cudaError_t e = cudaSuccess;
+  if (!p->slab) {
+    e = dispatch(p, [&](auto X) { return decltype(X)::backward(p, props, freqs, 0, p->N, 0, s); });
+  } else {
+    // slabs from the last: its post-order is still in the buffers after a
+    // tt_log_likelihood with keep_partials; every other slab's is recomputed
+    const int nslab = (p->N + p->slab - 1) / p->slab;
+    for (int j = nslab - 1; j >= 0 && e == cudaSuccess; --j) {
+      const int p0 = j * p->slab, n = std::min(p->slab, p->N - p0);
+      if (!(j == nslab - 1 && w.tail_valid)) {
+        e = dispatch(p, [&](auto X) {
+          return decltype(X)::forward(p, props, freqs, p->last_rescale, true, nullptr, nullptr, p0, n, 0, s);
+        });
+        if (e != cudaSuccess) break;
+      }
+      e = dispatch(p, [&](auto X) { return decltype(X)::backward(p, props, freqs, p0, n, j != nslab - 1, s); });
+    }
+    w.tail_valid = false;  // the adjoint wrote over the partials
+  }
   if (e != cudaSuccess) return wcuda(e, "wide-state adjoint launch");
   const size_t kss = size_t(p->K) * p->S * p->S;
   if (grad_matrices)

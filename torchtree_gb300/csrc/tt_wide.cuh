@@ -613,9 +613,11 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT, wide_bwd_min_blocks<T,
 }
 
 // Fixed-order sums over chunks: G[b][branch][k][S][S] (FP64, unpadded) and
-// the root gradients dfreq[b][S], dprop[b][K].
+// the root gradients dfreq[b][S], dprop[b][K]; accumulate = 1 adds to what
+// is there (pattern slabs after the first).
 template <typename T>
-__global__ void wide_grad_reduce_kernel(const T *gpart, double *G, int B, int nchunks, int K, int S, int SP) {
+__global__ void wide_grad_reduce_kernel(const T *gpart, double *G, int B, int nchunks, int K, int S, int SP,
+                                        int accumulate) {
   const int br = blockIdx.x, b = blockIdx.y;
   const int kss = K * S * S;
   for (int e = threadIdx.x; e < kss; e += blockDim.x) {
@@ -623,24 +625,27 @@ __global__ void wide_grad_reduce_kernel(const T *gpart, double *G, int B, int nc
     double s = 0.0;
     for (int c = 0; c < nchunks; ++c)
       s += double(gpart[(((size_t(b) * B + br) * nchunks + c) * K + k) * SP * SP + i * SP + j]);
-    G[(size_t(b) * B + br) * kss + e] = s;
+    double *g = G + (size_t(b) * B + br) * kss + e;
+    *g = accumulate ? *g + s : s;
   }
 }
 
 template <typename T>
 __global__ void wide_root_reduce_kernel(const T *rootpart, double *dfreq, double *dprop, int nchunks, int K, int S,
-                                        int SP) {
+                                        int SP, int accumulate) {
   const int b = blockIdx.x;
   for (int e = threadIdx.x; e < S + K; e += blockDim.x) {
     double s = 0.0;
     if (e < S) {
       for (int c = 0; c < nchunks; ++c)
         for (int k = 0; k < K; ++k) s += double(rootpart[((size_t(b) * nchunks + c) * K + k) * (SP + 1) + e]);
-      dfreq[size_t(b) * S + e] = s;
+      double *d = dfreq + size_t(b) * S + e;
+      *d = accumulate ? *d + s : s;
     } else {
       const int k = e - S;
       for (int c = 0; c < nchunks; ++c) s += double(rootpart[((size_t(b) * nchunks + c) * K + k) * (SP + 1) + SP]);
-      dprop[size_t(b) * K + k] = s;
+      double *d = dprop + size_t(b) * K + k;
+      *d = accumulate ? *d + s : s;
     }
   }
 }
