@@ -548,7 +548,7 @@ def main():
     eng = make_engine(args.precision)
     if args.slab_patterns is not None:
         eng.set_option(_native.TT_OPT_SLAB_PATTERNS, args.slab_patterns)
-    slab = eng.get_option(_native.TT_OPT_SLAB_PATTERNS) if S == 4 else 0
+    slab = eng.get_option(_native.TT_OPT_SLAB_PATTERNS)
     stream = torch.cuda.current_stream()
 
     def step(e):
