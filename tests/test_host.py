@@ -252,3 +252,25 @@ def test_native_column_compression_matches_numpy_and_reference_order(golden_patt
         assert w.tolist() == case["weights"]
         st = datatype.Nucleotide().byte_luts(False, tip_states=True)[1][cols]
         assert st.tolist() == case["states"]
+
+
+def test_site_models_match_the_reference_known_answers():
+    """test_site_model.py: Weibull rates for shapes 1.0 and 0.1 (51-56,
+    108-127), the mu scaling (130-138), and the proportion-invariant model's
+    probabilities, unit mean rate and mu scaling (80-105)."""
+    from torchtree_gb300 import site_models
+
+    f64 = lambda *v: torch.tensor(v, dtype=torch.float64)  # noqa: E731
+    rates, probs = site_models.weibull_rates(f64(1.0), 4)
+    np.testing.assert_allclose(rates.numpy(), [0.1457844, 0.5131316, 1.0708310, 2.2702530], rtol=1e-6)
+    np.testing.assert_allclose(probs.numpy(), [0.25] * 4)
+    rates, _ = site_models.weibull_rates(f64(0.1), 4)
+    np.testing.assert_allclose(rates.numpy(), [4.766392e-12, 1.391131e-06, 2.179165e-03, 3.997819], rtol=1e-6)
+    rates, _ = site_models.weibull_rates(f64(1.0), 4, mu=f64(2.0))
+    np.testing.assert_allclose(rates.numpy(), np.array([0.1457844, 0.5131316, 1.0708310, 2.2702530]) * 2, rtol=1e-6)
+    rates, probs = site_models.invariant_rates(f64(0.2))
+    assert probs.tolist() == [0.2, 0.8] and float((rates * probs).sum()) == 1.0
+    rates, _ = site_models.invariant_rates(f64(0.2), mu=f64(2.0))
+    assert float(rates[1]) == 2 / 0.8
+    rates, probs = site_models.invariant_rates(torch.tensor([[0.2], [0.3]], dtype=torch.float64))
+    assert torch.all((rates * probs).sum(-1) == 1.0)

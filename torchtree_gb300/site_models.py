@@ -69,6 +69,15 @@ def gamma_rates(shape: torch.Tensor, categories: int, invariant=None, mu=None):
     return _finish(rates, categories, invariant, mu)
 
 
+def invariant_rates(invariant: torch.Tensor, mu=None):
+    """Proportion-invariant model without rate heterogeneity, torchtree's
+    InvariantSiteModel (site_model.py:77-110): probabilities ``[p, 1-p]``,
+    rates ``[0, 1/(1-p)]`` (mean rate 1), times ``mu`` when given;
+    ``invariant [...,1]``."""
+    ones = torch.ones(invariant.shape[:-1] + (1,), dtype=invariant.dtype, device=invariant.device)
+    return _finish(ones, 1, invariant, mu)
+
+
 def constant_rates(dtype=torch.float64, device=None):
     one = torch.ones(1, dtype=dtype, device=device)
     return one, one.clone()
