@@ -123,3 +123,12 @@ def test_flu_a_known_answer_through_the_gpu_path():
         lik.rescale = rescale
         lnl = float(lik(time_lengths, q, pi, rates, props.expand(1, 4), clock_rates=clock)[0])
         assert abs(lnl - KAT) < tol * abs(KAT), (precision, rescale, lnl)
+    # batched x 3 (test_tree_likelihood.py:334-342): every member equals the single evaluation
+    for rescale in (False, True):
+        lik = PhyloLikelihood(topo, ca, 4, 4, batch=3, precision="f64")
+        lik.rescale = rescale
+        x3 = lambda t: t.expand(3, *t.shape[1:]).contiguous()  # noqa: E731
+        lnl3 = lik(x3(time_lengths), x3(q), x3(pi), x3(rates), props.expand(3, 4).contiguous(),
+                   clock_rates=x3(clock)).cpu().numpy()
+        assert np.all(np.abs(lnl3 - KAT) < 1e-12 * abs(KAT)), (rescale, lnl3)
+        assert lnl3[0] == lnl3[1] == lnl3[2]
