@@ -1,0 +1,210 @@
+"""The plug-in layer above the engine: the CLI hooks that retarget a
+generated configuration, and ``model.TreeLikelihoodModel``'s gathering of
+engine inputs checked against torchtree's own ``TreeLikelihoodModel``.
+
+The model tests import torchtree from its source tree (TORCHTREE_REFERENCE,
+else the default below) with the three-class dendropy stub of
+``tests/golden/_stub``; they are skipped where the source is absent.  They run
+on the CPU: the inputs that ``_call`` would hand to the engine are gathered
+on the CPU and evaluated by the oracle, and the result must equal the
+reference model's own lnL (1e-12 relative).  Without CUDA, ``_call`` itself
+must raise (no CPU fallback).
+"""
+import argparse
+import os
+import sys
+from pathlib import Path
+
+import numpy as np
+import pytest
+import torch
+
+ROOT = Path(__file__).resolve().parents[1]
+REF = Path(os.environ.get("TORCHTREE_REFERENCE", "/root/reference"))
+
+
+def test_cli_hook_retargets_every_likelihood():
+    from torchtree_gb300.cli.evolution import process_tree_likelihood
+
+    data = {"type": "JointDistributionModel", "distributions": [
+        {"id": "like", "type": "TreeLikelihoodModel"},
+        {"type": "JointDistributionModel", "distributions": [{"id": "like2", "type": "TreeLikelihoodModel"}]},
+    ]}
+    process_tree_likelihood(argparse.Namespace(gb300_precision="f32"), data)
+    inner = [data["distributions"][0], data["distributions"][1]["distributions"][0]]
+    for d in inner:
+        assert d["type"] == "torchtree_gb300.TreeLikelihoodModel" and d["precision"] == "f32"
+    single = {"id": "like", "type": "TreeLikelihoodModel"}
+    process_tree_likelihood(argparse.Namespace(), single)
+    assert single["precision"] == "f64"
+
+
+@pytest.fixture(scope="module")
+def torchtree_ref():
+    if not (REF / "torchtree").is_dir():
+        pytest.skip("torchtree source not present")
+    for path in (str(ROOT / "tests" / "golden" / "_stub"), str(REF)):
+        if path not in sys.path:
+            sys.path.insert(0, path)
+    torch.set_default_dtype(torch.float64)
+    import torchtree  # noqa: F401
+
+    yield
+    torch.set_default_dtype(torch.float32)
+
+
+def test_plugin_flag_adds_arguments_and_retargets(torchtree_ref):
+    from torchtree_gb300.plugin import GB300
+
+    parser = argparse.ArgumentParser()
+    sub = parser.add_subparsers()
+    sub.add_parser("advi")
+    sub.add_parser("map")
+    plugin = GB300()
+    plugin.load_arguments(sub)
+    arg = parser.parse_args(["advi", "--gb300", "--gb300-precision", "f32"])
+    data = {"id": "like", "type": "TreeLikelihoodModel"}
+    plugin.process_tree_likelihood(arg, data)
+    assert data["type"] == "torchtree_gb300.TreeLikelihoodModel" and data["precision"] == "f32"
+    data = {"id": "like", "type": "TreeLikelihoodModel"}
+    plugin.process_tree_likelihood(parser.parse_args(["map"]), data)
+    assert data["type"] == "TreeLikelihoodModel"
+
+
+def _fixed_tree_class():
+    from torchtree.evolution.tree_model import TreeModel
+
+    class FixedTree(TreeModel):
+        """Minimal TreeModel: fixed post-order, branch lengths from a Parameter."""
+
+        def __init__(self, post, names, bl):
+            super().__init__(None)
+            self._post = [list(map(int, t)) for t in post]
+            self._names = list(names)
+            self._bl = bl
+            self.taxa_count = len(names)
+
+        def branch_lengths(self):
+            return self._bl.tensor
+
+        @property
+        def postorder(self):
+            return self._post
+
+        @property
+        def taxa(self):
+            return self._names
+
+        def write_newick(self, stream, **kwargs):
+            stream.write("();")
+
+        def _sample_shape(self):
+            return self._bl.tensor.shape[:-1]
+
+        def handle_model_changed(self, model, obj, index):
+            pass
+
+        def handle_parameter_changed(self, variable, index, event):
+            self.fire_model_changed()
+
+        @classmethod
+        def from_json(cls, data, dic):
+            raise NotImplementedError
+
+    return FixedTree
+
+
+def _oracle_lnl(route, tensors, topo, alignment, rescale):
+    """lnL from the gathered engine inputs, by the oracle on the CPU."""
+    from oracle import likelihood as OL
+
+    if route == "rate_matrix":
+        qn, _, bls, rates, probs, freqs = tensors
+        times = bls.unsqueeze(-1) * rates.unsqueeze(-2)  # [b, B, K]
+        mats = torch.linalg.matrix_exp(qn[:, None, None] * times[..., None, None])
+    else:
+        mats, probs, freqs = tensors
+    tips = [torch.tensor(alignment.table[c].T) for c in alignment.codes]  # [S, N] per tip
+    parts = tips + [None] * (len(tips) - 1)
+    fn = OL.treelikelihood_discrete_rescaled if rescale else OL.treelikelihood_discrete
+    return fn(parts, torch.tensor(alignment.weights, dtype=torch.float64), topo.postorder_list(), mats,
+              freqs.unsqueeze(-2), probs[..., None, None]).reshape(-1)
+
+
+def _models(case, wl, b):
+    """Reference-side objects of one case: (tree, site pattern, subst, site, clock, tip_states)."""
+    from torchtree import Parameter
+    from torchtree.evolution.alignment import Alignment, Sequence
+    from torchtree.evolution.branch_model import StrictClockModel
+    from torchtree.evolution.datatype import NucleotideDataType
+    from torchtree.evolution.site_model import ConstantSiteModel, WeibullSiteModel
+    from torchtree.evolution.site_pattern import SitePattern
+    from torchtree.evolution.substitution_model import GTR, HKY, JC69
+    from torchtree.evolution.taxa import Taxa, Taxon
+
+    names = wl.topology.tip_names
+    taxa = Taxa(None, [Taxon(n, {}) for n in names])
+    aln = Alignment(None, [Sequence(n, s) for n, s in zip(names, wl.sequences)], taxa, NucleotideDataType(None))
+    sp = SitePattern(None, aln)
+    T = wl.topology.tip_count
+    bl = torch.tensor(wl.branch_lengths[:b])
+    clock = None
+    if case == "hky_weibull_clock":  # rooted time lengths (2T-2) times a strict clock
+        bl = torch.cat((bl, torch.full((b, 1), 0.02)), -1) * 10.0
+        tree = _fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
+        clock = StrictClockModel(None, Parameter(None, torch.full((b, 1), 0.1)), tree)
+    else:
+        tree = _fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
+    pi = Parameter(None, torch.tensor(wl.pi[:b]))
+    if case.startswith("gtr"):
+        subst = GTR(None, Parameter(None, torch.tensor(wl.exch[:b])), pi)
+    elif case.startswith("hky"):
+        subst = HKY(None, Parameter(None, torch.tensor(wl.exch[:b, 1:2])), pi)
+    else:
+        subst = JC69(None)
+    if "weibull" in case:
+        site = WeibullSiteModel(None, Parameter(None, torch.tensor(wl.shape[:b])), 4)
+    else:
+        site = ConstantSiteModel(None)
+    assert T == len(names)
+    return tree, sp, subst, site, clock, case.endswith("tipstates")
+
+
+@pytest.mark.parametrize("case,b", [("gtr_weibull", 1), ("gtr_weibull", 2), ("jc69_constant", 1),
+                                    ("hky_weibull_clock", 2), ("gtr_weibull_tipstates", 2)])
+def test_model_gathers_the_reference_inputs(torchtree_ref, case, b):
+    """The plug-in's engine inputs, evaluated by the oracle, give the
+    reference model's own lnL (unscaled and rescaled); the route follows the
+    substitution model (eigen-form p_t: rate matrix; JC69's closed form:
+    matrices)."""
+    from torchtree.evolution.tree_likelihood import TreeLikelihoodModel as Reference
+
+    from torchtree_gb300 import synthetic
+    from torchtree_gb300.model import TreeLikelihoodModel
+
+    wl = synthetic.dna_workload("plugin", tip_count=12, site_count=300, batch=2, seed=91, shape=0.5,
+                                site_model="weibull")
+    for rescale in (False, True):
+        tree, sp, subst, site, clock, tip_states = _models(case, wl, b)
+        ref = Reference(None, sp, tree, subst, site, clock, False, tip_states)
+        ref.rescale = rescale
+        want = ref().detach().reshape(-1)
+        ours = TreeLikelihoodModel(None, sp, tree, subst, site, clock, False, tip_states, precision="f64")
+        route, tensors, sample_shape, (nb, S, K) = ours.engine_inputs(torch.device("cpu"))
+        assert route == ("matrices" if case.startswith("jc69") else "rate_matrix")
+        assert (nb, S) == (b, 4) and tuple(sample_shape) == tuple(ref.sample_shape)
+        got = _oracle_lnl(route, [t.detach() for t in tensors], wl.topology, ours._alignment, rescale)
+        np.testing.assert_allclose(got.numpy(), want.numpy(), rtol=1e-12)
+
+
+def test_model_call_fails_loudly_without_cuda(torchtree_ref):
+    if torch.cuda.is_available():
+        pytest.skip("a CUDA device is present")
+    from torchtree_gb300 import synthetic
+    from torchtree_gb300.model import TreeLikelihoodModel
+
+    wl = synthetic.dna_workload("plugin", tip_count=6, site_count=50, batch=1, seed=92)
+    tree, sp, subst, site, clock, tip_states = _models("gtr_weibull", wl, 1)
+    ours = TreeLikelihoodModel(None, sp, tree, subst, site, clock, False, tip_states)
+    with pytest.raises((RuntimeError, AssertionError)):
+        ours()

@@ -73,8 +73,21 @@ class TreeLikelihoodModel(_ReferenceModel):
             self._engines[key] = eng
         return eng
 
-    def _call(self, *args, **kwargs) -> torch.Tensor:
-        dev = torch.device("cuda", torch.cuda.current_device())
+    def engine_inputs(self, device):
+        """The engine's inputs for the current parameters, on ``device``, as
+        ``(route, tensors, sample_shape, (b, S, K))``, mirroring the inputs
+        that ``_call`` gathers (tree_likelihood.py:313-349):
+
+        * route ``"rate_matrix"`` (reversible models with the eigen-form
+          ``p_t``): ``(Q normalised, frequencies, node lengths, rates,
+          probabilities, frequencies)``;
+        * route ``"matrices"`` (any other ``p_t``): ``(P [b, 2T-2, K, S, S],
+          probabilities, frequencies)``.
+
+        Node lengths are the unrooted lengths with the zero branch appended,
+        or clock rates times time lengths; every tensor is flattened to
+        ``b = prod(sample_shape)`` samples.
+        """
         sample_shape = self.sample_shape
         b = math.prod(sample_shape)
         branch_lengths = self.tree_model.branch_lengths()
@@ -97,25 +110,29 @@ class TreeLikelihoodModel(_ReferenceModel):
         freqs = self.subst_model.frequencies
         S = freqs.shape[-1]
         freqs = freqs.expand(sample_shape + (S,))
-        eng = self._engine(b, S, K)
 
         def flat(x, *tail):
-            return x.to(dev).reshape((b,) + tail)
+            return x.to(device).reshape((b,) + tail)
 
         if _uses_eigen_form(self.subst_model):
             q = self.subst_model.q()
             q = q.expand(sample_shape + (S, S)) if q.dim() == 2 else q.reshape(sample_shape + (S, S))
             qn = normalise(flat(q, S, S), flat(freqs, S))  # abstract.py:49-50
+            tensors = (qn, flat(freqs, S), flat(bls, bls.shape[-1]), flat(rates, K), flat(probs, K), flat(freqs, S))
+            return "rate_matrix", tensors, sample_shape, (b, S, K)
+        mats = self.subst_model.p_t(bls.reshape(sample_shape + (-1, 1)) * rates.unsqueeze(-2))
+        tensors = (flat(mats, mats.shape[-4], K, S, S), flat(probs, K), flat(freqs, S))
+        return "matrices", tensors, sample_shape, (b, S, K)
 
-            def run(rescale):  # gradients reach Q through dlnL/dQ (no eigenvector derivatives)
-                return RateMatrixLikelihood.apply(qn, flat(freqs, S), flat(bls, bls.shape[-1]), flat(rates, K),
-                                                  flat(probs, K), flat(freqs, S), eng, rescale)
-        else:
-            mats = self.subst_model.p_t(bls.reshape(sample_shape + (-1, 1)) * rates.unsqueeze(-2))
+    def _call(self, *args, **kwargs) -> torch.Tensor:
+        dev = torch.device("cuda", torch.cuda.current_device())  # raises without CUDA: no CPU fallback
+        route, tensors, sample_shape, (b, S, K) = self.engine_inputs(dev)
+        eng = self._engine(b, S, K)
+        # rate-matrix route: gradients reach Q through dlnL/dQ (no eigenvector derivatives)
+        fn = RateMatrixLikelihood if route == "rate_matrix" else MatrixLikelihood
 
-            def run(rescale):
-                return MatrixLikelihood.apply(flat(mats, mats.shape[-4], K, S, S), flat(probs, K),
-                                              flat(freqs, S), eng, rescale)
+        def run(rescale):
+            return fn.apply(*tensors, eng, rescale)
 
         if self.rescale:
             lnl = run(True)
@@ -124,7 +141,8 @@ class TreeLikelihoodModel(_ReferenceModel):
             if torch.isinf(lnl).any():  # sticky switch (tree_likelihood.py:378-388)
                 self.rescale = True
                 lnl = run(True)
-        return lnl.to(branch_lengths.device).reshape(sample_shape + (1,))
+        device = self.tree_model.branch_lengths().device
+        return lnl.to(device).reshape(sample_shape + (1,))
 
     @classmethod
     def from_json(cls, data, dic):
