@@ -147,35 +147,48 @@ def _models(case, wl, b):
     aln = Alignment(None, [Sequence(n, s) for n, s in zip(names, wl.sequences)], taxa, NucleotideDataType(None))
     sp = SitePattern(None, aln)
     T = wl.topology.tip_count
+    leaf = lambda a: torch.tensor(np.asarray(a), dtype=torch.float64, requires_grad=True)  # noqa: E731
     bl = torch.tensor(wl.branch_lengths[:b])
     clock = None
     if case == "hky_weibull_clock":  # rooted time lengths (2T-2) times a strict clock
-        bl = torch.cat((bl, torch.full((b, 1), 0.02)), -1) * 10.0
+        bl = leaf(torch.cat((bl, torch.full((b, 1), 0.02)), -1).numpy() * 10.0)
+        rate = leaf(np.full((b, 1), 0.1))
         tree = _fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
-        clock = StrictClockModel(None, Parameter(None, torch.full((b, 1), 0.1)), tree)
+        clock = StrictClockModel(None, Parameter(None, rate), tree)
+        leaves = [bl, rate]
     else:
+        bl = leaf(bl.numpy())
         tree = _fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
-    pi = Parameter(None, torch.tensor(wl.pi[:b]))
+        leaves = [bl]
+    pi_t = leaf(wl.pi[:b])
+    pi = Parameter(None, pi_t)
     if case.startswith("gtr"):
-        subst = GTR(None, Parameter(None, torch.tensor(wl.exch[:b])), pi)
+        ex = leaf(wl.exch[:b])
+        subst = GTR(None, Parameter(None, ex), pi)
+        leaves += [ex, pi_t]
     elif case.startswith("hky"):
-        subst = HKY(None, Parameter(None, torch.tensor(wl.exch[:b, 1:2])), pi)
+        kappa = leaf(wl.exch[:b, 1:2])
+        subst = HKY(None, Parameter(None, kappa), pi)
+        leaves += [kappa, pi_t]
     else:
         subst = JC69(None)
     if "weibull" in case:
-        site = WeibullSiteModel(None, Parameter(None, torch.tensor(wl.shape[:b])), 4)
+        shape = leaf(wl.shape[:b])
+        site = WeibullSiteModel(None, Parameter(None, shape), 4)
+        leaves.append(shape)
     else:
         site = ConstantSiteModel(None)
     assert T == len(names)
-    return tree, sp, subst, site, clock, case.endswith("tipstates")
+    return tree, sp, subst, site, clock, case.endswith("tipstates"), leaves
 
 
 @pytest.mark.parametrize("case,b", [("gtr_weibull", 1), ("gtr_weibull", 2), ("jc69_constant", 1),
                                     ("hky_weibull_clock", 2), ("gtr_weibull_tipstates", 2)])
 def test_model_gathers_the_reference_inputs(torchtree_ref, case, b):
     """The plug-in's engine inputs, evaluated by the oracle, give the
-    reference model's own lnL (unscaled and rescaled); the route follows the
-    substitution model (eigen-form p_t: rate matrix; JC69's closed form:
+    reference model's own lnL (unscaled and rescaled) and, through autograd,
+    its gradients with respect to every parameter (1e-9); the route follows
+    the substitution model (eigen-form p_t: rate matrix; JC69's closed form:
     matrices)."""
     from torchtree.evolution.tree_likelihood import TreeLikelihoodModel as Reference
 
@@ -185,16 +198,20 @@ def test_model_gathers_the_reference_inputs(torchtree_ref, case, b):
     wl = synthetic.dna_workload("plugin", tip_count=12, site_count=300, batch=2, seed=91, shape=0.5,
                                 site_model="weibull")
     for rescale in (False, True):
-        tree, sp, subst, site, clock, tip_states = _models(case, wl, b)
+        tree, sp, subst, site, clock, tip_states, leaves = _models(case, wl, b)
         ref = Reference(None, sp, tree, subst, site, clock, False, tip_states)
         ref.rescale = rescale
-        want = ref().detach().reshape(-1)
+        want = ref().reshape(-1)
+        gwant = torch.autograd.grad(want.sum(), leaves)
+        tree, sp, subst, site, clock, tip_states, leaves = _models(case, wl, b)
         ours = TreeLikelihoodModel(None, sp, tree, subst, site, clock, False, tip_states, precision="f64")
         route, tensors, sample_shape, (nb, S, K) = ours.engine_inputs(torch.device("cpu"))
         assert route == ("matrices" if case.startswith("jc69") else "rate_matrix")
         assert (nb, S) == (b, 4) and tuple(sample_shape) == tuple(ref.sample_shape)
-        got = _oracle_lnl(route, [t.detach() for t in tensors], wl.topology, ours._alignment, rescale)
-        np.testing.assert_allclose(got.numpy(), want.numpy(), rtol=1e-12)
+        got = _oracle_lnl(route, tensors, wl.topology, ours._alignment, rescale)
+        np.testing.assert_allclose(got.detach().numpy(), want.detach().numpy(), rtol=1e-12)
+        for g, w in zip(torch.autograd.grad(got.sum(), leaves), gwant):
+            np.testing.assert_allclose(g.numpy(), w.numpy(), rtol=1e-9, atol=1e-9 * float(w.abs().max()))
 
 
 def test_model_call_fails_loudly_without_cuda(torchtree_ref):
@@ -204,7 +221,7 @@ def test_model_call_fails_loudly_without_cuda(torchtree_ref):
     from torchtree_gb300.model import TreeLikelihoodModel
 
     wl = synthetic.dna_workload("plugin", tip_count=6, site_count=50, batch=1, seed=92)
-    tree, sp, subst, site, clock, tip_states = _models("gtr_weibull", wl, 1)
+    tree, sp, subst, site, clock, tip_states, _ = _models("gtr_weibull", wl, 1)
     ours = TreeLikelihoodModel(None, sp, tree, subst, site, clock, False, tip_states)
     with pytest.raises((RuntimeError, AssertionError)):
         ours()
