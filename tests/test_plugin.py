@@ -225,3 +225,23 @@ def test_model_call_fails_loudly_without_cuda(torchtree_ref):
     ours = TreeLikelihoodModel(None, sp, tree, subst, site, clock, False, tip_states)
     with pytest.raises((RuntimeError, AssertionError)):
         ours()
+
+
+def test_json_route_selects_the_plugin_class(torchtree_ref):
+    """A configuration names the class by its dotted path (core/utils.py:116-125)
+    and may add "precision"; the other keys are the reference's."""
+    from torchtree.core.utils import get_class, process_object
+
+    from torchtree_gb300 import synthetic
+    from torchtree_gb300.model import TreeLikelihoodModel
+
+    assert get_class("torchtree_gb300.TreeLikelihoodModel") is TreeLikelihoodModel
+    wl = synthetic.dna_workload("plugin", tip_count=8, site_count=100, batch=1, seed=93, site_model="weibull")
+    tree, sp, subst, site, clock, _, _ = _models("hky_weibull_clock", wl, 1)
+    dic = {"tree": tree, "sp": sp, "subst": subst, "site": site, "clock": clock}
+    like = process_object({"id": "like", "type": "torchtree_gb300.TreeLikelihoodModel", "tree_model": "tree",
+                           "site_model": "site", "substitution_model": "subst", "site_pattern": "sp",
+                           "branch_model": "clock", "precision": "f32"}, dic)
+    assert isinstance(like, TreeLikelihoodModel) and like.precision == "f32" and like.rescale
+    assert like.clock_model is clock and dic["like"] is like
+    assert like._alignment.codes.shape == (8, like.weights.shape[0])
