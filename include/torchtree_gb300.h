@@ -183,8 +183,11 @@ int tt_plan_device_status(tt_plan *plan, void *stream, int32_t *status,
 /*
  * Host-only: the execution schedule a plan would use (no device needed).
  *   steps: int32 [T-1][12] per step (node, left, right, forward slot of
- *          left / right / output, adjoint slot of input / left / right, 3
- *          unused), -1 where a slot does not apply;
+ *          left / right / output, adjoint slot of input / left / right,
+ *          the in-place adjoint's flags: carry or store each internal child
+ *          and whether this node's outside partial was stored, the reversed
+ *          index of the step that stored it, 1 unused), -1 where a slot does
+ *          not apply;
  *   slot_counts: int32 [2] shared-memory slots of the forward and adjoint.
  * Validates `postorder` exactly as tt_plan_create does.
  */
@@ -267,6 +270,15 @@ int tt_constant_coalescent(tt_time_tree *tree, int32_t batch,
                            const double *heights, const double *theta,
                            double *log_prob, double *grad_heights,
                            double *grad_theta, void *stream);
+
+/*
+ * Self-test of the device-side failure path (no reference counterpart): one
+ * kernel waits, with the bounded wait every staged kernel uses, on a barrier
+ * that nothing completes, gives up after limit_ns (1 .. 1e10) and records
+ * TT_ERR_DEVICE_TIMEOUT in the plan's status word, which
+ * tt_plan_device_status then reports.  The context and the plan stay usable.
+ */
+int tt_plan_selftest_timeout(tt_plan *plan, uint64_t limit_ns, void *stream);
 
 /* Number of kernel launches the plan issued since creation. */
 int tt_plan_launch_count(const tt_plan *plan, int64_t *count);

@@ -401,3 +401,27 @@ def test_fp32_adjoints_on_edge_trees(shape, T, K):
         np.testing.assert_allclose(out[name][0], ref[0], rtol=1e-6)
         for got, want in zip(out[name][1:], ref[1:]):
             np.testing.assert_allclose(got, want, rtol=1e-4, atol=1e-4 * np.abs(want).max())
+
+
+def test_bounded_wait_times_out_and_the_plan_stays_usable():
+    """The failure path without a fault: a kernel waits, with the bounded wait
+    of every staged kernel, on a barrier that nothing completes; after 1 ms it
+    gives up and the plan's status word says so (read once, then reset).  The
+    context and the plan stay usable: the next evaluation is unchanged."""
+    from torchtree_gb300 import _native, patterns, site_models, substitution, synthetic
+    from torchtree_gb300.likelihood import PhyloLikelihood, batch_inputs
+
+    wl = synthetic.dna_workload("wait", tip_count=20, site_count=500, batch=2, seed=5, shape=0.5)
+    lik = PhyloLikelihood(wl.topology, patterns.compress(wl.sequences), 4, 4, batch=2, precision="f32")
+    bl, ex, pi, sh = batch_inputs(wl, torch.device("cuda"))
+
+    def lnl():
+        r, p = site_models.gamma_rates(sh, 4)
+        return lik(bl, substitution.gtr_q(ex, pi), pi, r, p.expand(2, 4)).detach().cpu()
+
+    before = lnl()
+    assert lik.engine.device_status() == 0
+    lik.engine.selftest_timeout(1_000_000)
+    assert lik.engine.device_status() == _native.TT_ERR_DEVICE_TIMEOUT
+    assert lik.engine.device_status() == 0
+    assert torch.equal(lnl(), before)

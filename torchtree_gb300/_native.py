@@ -36,6 +36,7 @@ SIGNATURES = {
     "tt_plan_create": (ctypes.c_int, [ctypes.POINTER(_P), _I32, _PI32, _I32, _I32, _I32, _I32, _I32]),
     "tt_plan_destroy": (ctypes.c_int, [_P]),
     "tt_plan_workspace_bytes": (ctypes.c_int, [_P, ctypes.POINTER(ctypes.c_size_t)]),
+    "tt_plan_selftest_timeout": (ctypes.c_int, [_P, ctypes.c_uint64, _P]),
     "tt_plan_set_tips": (ctypes.c_int, [_P, _P, _P, _I32, _P]),
     "tt_update_transition_matrices": (ctypes.c_int, [_P, _P, _P, _P, _P, _P, _P]),
     "tt_set_transition_matrices": (ctypes.c_int, [_P, _P, _P]),

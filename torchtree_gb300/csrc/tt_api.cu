@@ -918,6 +918,17 @@ int tt_plan_get_option(const tt_plan *p, int32_t option, int32_t *value) {
   }
 }
 
+int tt_plan_selftest_timeout(tt_plan *p, uint64_t limit_ns, void *stream) {
+  if (!p) return fail(TT_ERR_INVALID_ARGUMENT, "NULL plan");
+  if (limit_ns < 1 || limit_ns > 10000000000ull) return fail(TT_ERR_INVALID_ARGUMENT, "limit_ns must be in [1, 1e10]");
+  int rc = check_device(p);
+  if (rc) return rc;
+  cudaError_t e = tt::launch_wait_selftest(p->d_status, limit_ns, static_cast<cudaStream_t>(stream));
+  if (e != cudaSuccess) return cuda_fail(e, "self-test launch");
+  p->launches += 1;
+  return TT_OK;
+}
+
 int tt_plan_launch_count(const tt_plan *p, int64_t *count) {
   if (!p || !count) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
   *count = p->launches;

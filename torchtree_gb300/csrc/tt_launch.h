@@ -77,6 +77,8 @@ cudaError_t launch_reduce_f32(const float *gpart, const float *rootpart, double 
 cudaError_t launch_reduce_f64(const double *gpart, const double *rootpart, double *G,
                               double *dfreq, double *dprop, int batch, int B, int ntiles, int S,
                               int K, int accumulate, cudaStream_t stream);
+// one bounded wait that nothing completes (limit_ns), reported in *status
+cudaError_t launch_wait_selftest(int *status, unsigned long long limit_ns, cudaStream_t stream);
 // lnL[b] = sum over tiles (fixed order); accumulate = 1 adds to lnl[b]
 cudaError_t launch_reduce_lnl(const double *tile_lnl, double *lnl, int batch, int ntiles, int accumulate,
                               cudaStream_t stream);

@@ -74,6 +74,23 @@ cudaError_t launch_reduce_f64(const double *gpart, const double *rootpart, doubl
   return cudaGetLastError();
 }
 
+// Self-test of the failure path of every staged kernel: one thread waits on
+// an mbarrier that nothing arrives at, with the same bounded wait, gives up
+// after limit_ns and records the timeout in the status word.
+__global__ void wait_selftest_kernel(int *status, unsigned long long limit_ns) {
+  __shared__ __align__(8) uint64_t bar;
+  if (threadIdx.x == 0) {
+    mbar_init(&bar, 1);
+    fence_barrier_init();
+    if (!mbar_wait_bounded(&bar, 0, limit_ns)) atomicExch(status, kDeviceTimeout);
+  }
+}
+
+cudaError_t launch_wait_selftest(int *status, unsigned long long limit_ns, cudaStream_t stream) {
+  wait_selftest_kernel<<<1, 32, 0, stream>>>(status, limit_ns);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_reduce_lnl(const double *tile_lnl, double *lnl, int batch, int ntiles, int accumulate,
                               cudaStream_t stream) {
   reduce_lnl_kernel<<<batch, 256, 0, stream>>>(tile_lnl, lnl, ntiles, accumulate);

@@ -98,6 +98,11 @@ class LikelihoodEngine:
         check(self.lib.tt_plan_get_option(self._plan, int(option), ctypes.byref(v)))
         return int(v.value)
 
+    def selftest_timeout(self, limit_ns: int = 1_000_000) -> None:
+        """Launch one bounded wait that nothing completes (failure-path self-test);
+        ``device_status()`` then reports ``TT_ERR_DEVICE_TIMEOUT``."""
+        check(self.lib.tt_plan_selftest_timeout(self._plan, int(limit_ns), _stream()))
+
     def device_status(self, reset: bool = True) -> int:
         s = ctypes.c_int32()
         check(self.lib.tt_plan_device_status(self._plan, _stream(), ctypes.byref(s), int(reset)))
