@@ -189,3 +189,42 @@ def test_autotune_candidates_cover_the_kernel_shape_options():
     codon = autotune.candidates(SimpleNamespace(precision="f32", state_count=61))
     assert {o[_native.TT_OPT_TENSOR_CORES] for o in codon} == {0, 1}
     assert autotune.candidates(SimpleNamespace(precision="f64", state_count=4)) == [{}]
+
+
+def test_a_data_set_larger_than_the_budget_is_served_in_pattern_slabs():
+    """Host logic of the slab fallback: the whole-alignment estimate exceeds the
+    budget, so the plan is made with the largest slab whose estimate fits;
+    a data set that does not fit even in the smallest slab fails at once."""
+    from types import SimpleNamespace
+
+    ds_big = SimpleNamespace(name="big", topology=SimpleNamespace(tip_count=1000),
+                             alignment=SimpleNamespace(pattern_count=81808), state_count=4,
+                             spec=SimpleNamespace(categories=4))
+    whole = serving.estimate_bytes(ds_big, 8, "f32")
+    slab, need = serving.slab_fit(ds_big, 8, "f32", whole // 3)
+    assert slab % serving.SLAB_ALIGN == 0 and 0 < slab < 81808 and need <= whole // 3
+    assert serving.estimate_bytes(ds_big, 8, "f32", slab + serving.SLAB_ALIGN) > whole // 3
+    assert serving.slab_fit(ds_big, 8, "f32", 1 << 20) == (0, None)
+
+    log, made = [], {}
+
+    def factory(ds, slab=0):
+        ex = FakeExecutor(ds, 40 if slab else 300, log)
+        ex.slab = slab
+        made[ds.name] = ex
+        return ex
+
+    srv = serving.LikelihoodServer(slots=2, hbm_budget=100, executor_factory=factory, device="cpu")
+    srv.estimate = lambda ds: {"big": 300, "huge": 10 ** 9}[ds.name]
+    srv.slab_fit = lambda ds, room: (1024, 40) if ds.name == "big" else (0, None)
+    srv.add_dataset("big", None, None, 4, serving.ModelSpec("gtr"))
+    srv.add_dataset("huge", None, None, 4, serving.ModelSpec("gtr"))
+    fb = srv.submit("big", {"i": 3})
+    fh = srv.submit("huge", {"i": 4})
+    srv.step()
+    assert made["big"].slab == 1024 and srv.used == 40 and "huge" not in made
+    with pytest.raises(MemoryError):
+        fh.result(timeout=1)
+    made["big"].release = True
+    srv.step()
+    assert fb.result(timeout=1)["lnl"] == -3.0

@@ -13,7 +13,10 @@ chain -- as one captured CUDA graph on the data set's own stream:
   and batches of different data sets run concurrently on their streams;
 * admission by HBM footprint: a data set's plan is created only when its
   workspace fits the budget, evicting idle plans (least recently used)
-  otherwise; requests of a data set that does not fit wait;
+  otherwise; requests of a data set that does not fit wait.  A data set
+  larger than the whole budget gets a plan whose partials are held in
+  pattern slabs (TT_OPT_SLAB_PATTERNS) sized to the budget; one too large
+  even for the smallest slab fails its requests with MemoryError;
 * kernel shapes of each plan come from ``autotune.tune`` before capture;
 * every request's result (lnL and the gradient with respect to its branch
   lengths, rate-matrix parameters, frequencies and site-model shape) is the
@@ -38,7 +41,7 @@ from dataclasses import dataclass, field
 import numpy as np
 import torch
 
-from . import autotune, site_models, substitution
+from . import _native, autotune, site_models, substitution
 from .engine import LikelihoodEngine
 from .patterns import CompressedAlignment
 from .tree import Topology
@@ -120,31 +123,47 @@ def host_finish(p: dict, out: dict) -> dict:
             "grad_shape": shape.grad.numpy().copy()}
 
 
-def estimate_bytes(ds: Dataset, slots: int, precision: str) -> int:
-    """Device bytes a plan for ``ds`` with ``slots`` samples will hold (upper estimate)."""
+SLAB_ALIGN = 512  # pattern-slab sizes are multiples of this (TT_OPT_SLAB_PATTERNS)
+
+
+def estimate_bytes(ds: Dataset, slots: int, precision: str, slab: int = 0) -> int:
+    """Device bytes a plan for ``ds`` with ``slots`` samples will hold (upper
+    estimate); with ``slab`` > 0 its partials cover that many patterns at once."""
     T, N, S, K = ds.topology.tip_count, ds.alignment.pattern_count, ds.state_count, ds.spec.categories
+    n = min(slab, N) if slab else N
     elem = 4 if precision == "f32" else 8
     B = 2 * T - 2
     if S == 4:
-        npad = -(-N // 64) * 64
+        npad = -(-n // 64) * 64
         kp = K + (K & 1)
         part = slots * T * kp * npad * S * elem
         grad = slots * B * (npad // 32) * K * S * S * elem
-        return int(1.1 * (part + grad + slots * B * kp * S * S * elem + T * npad)) + (64 << 20)
+        return int(1.1 * (part + grad + slots * B * kp * S * S * elem + T * -(-N // 64) * 64)) + (64 << 20)
     sp = 20 if S <= 20 else 64
-    npad = -(-N // 128) * 128
+    npad = -(-n // 128) * 128
     # partials and exponents; FP32 codon plans also keep the children's products (2 rows per state)
     part = slots * T * K * npad * (sp * elem * (3 if precision == "f32" and sp == 64 else 1) + 4)
     chunks = min(64, max(1, -(-304 // (slots * K))))
     grad = slots * B * K * sp * sp * (chunks * elem + elem + 8)
-    return int(1.1 * (part + grad + T * npad)) + (64 << 20)
+    return int(1.1 * (part + grad + T * -(-N // 128) * 128)) + (64 << 20)
+
+
+def slab_fit(ds: Dataset, slots: int, precision: str, room: int):
+    """``(slab, bytes)``: the largest pattern slab whose plan fits in ``room``
+    bytes, or ``(0, None)`` when even the smallest slab does not."""
+    N = ds.alignment.pattern_count
+    for k in range(max(1, -(-N // SLAB_ALIGN) - 1), 0, -1):
+        need = estimate_bytes(ds, slots, precision, k * SLAB_ALIGN)
+        if need <= room:
+            return k * SLAB_ALIGN, need
+    return 0, None
 
 
 class GraphExecutor:
     """One admitted data set: plan, stream, static buffers, captured step."""
 
     def __init__(self, ds: Dataset, slots: int, precision: str, device, use_graph: bool = True,
-                 tune: bool = True):
+                 tune: bool = True, slab: int = 0):
         self.ds = ds
         self.slots = slots
         self.device = device
@@ -152,6 +171,8 @@ class GraphExecutor:
         B = 2 * T - 2
         self.engine = LikelihoodEngine(ds.topology.postorder, T, S, K, ds.alignment.codes, ds.alignment.table,
                                        ds.alignment.weights, batch=slots, precision=precision, device=device)
+        if slab:  # partials held one pattern slab at a time (before tuning and capture)
+            self.engine.set_option(_native.TT_OPT_SLAB_PATTERNS, slab)
         kw = dict(dtype=torch.float64, device=device)
         eye = torch.eye(S, **kw).expand(slots, S, S).contiguous()
         self.inputs = {"lam": torch.zeros(slots, S, **kw), "u": eye.clone(), "w": eye.clone(),
@@ -243,9 +264,11 @@ class LikelihoodServer:
             free, _ = torch.cuda.mem_get_info(self.device)
             hbm_budget = int(0.85 * free)
         self.budget = hbm_budget
-        self.factory = executor_factory or (lambda ds: GraphExecutor(ds, slots, precision, self.device,
-                                                                     use_graph=use_graphs, tune=tune))
+        self.factory = executor_factory or (lambda ds, slab=0: GraphExecutor(ds, slots, precision, self.device,
+                                                                             use_graph=use_graphs, tune=tune,
+                                                                             slab=slab))
         self.estimate = (lambda ds: estimate_bytes(ds, slots, precision))
+        self.slab_fit = (lambda ds, room: slab_fit(ds, slots, precision, room))
         self.datasets: dict = {}
         self.executors: dict = {}
         self.pending: dict = {}
@@ -301,6 +324,14 @@ class LikelihoodServer:
     def _admit(self, name: str):
         ds = self.datasets[name]
         need = self.estimate(ds)
+        slab = 0
+        if need > self.budget:  # never fits whole: hold its partials in pattern slabs
+            slab, need = self.slab_fit(ds, self.budget)
+            if not slab:
+                exc = MemoryError(f"data set {name!r} does not fit the HBM budget even in pattern slabs")
+                for r in self.pending.pop(name, []):
+                    r.future.set_exception(exc)
+                return None
         while self.used + need > self.budget:
             idle = [(ex.last_used, n) for n, ex in self.executors.items() if not ex.busy and not self.pending.get(n)]
             if not idle:
@@ -310,7 +341,7 @@ class LikelihoodServer:
             self.used -= ex.footprint
             ex.close()
             self.evictions += 1
-        ex = self.factory(ds)
+        ex = self.factory(ds, slab) if slab else self.factory(ds)
         self.executors[name] = ex
         self.used += max(ex.footprint, need)
         self.admissions += 1
