@@ -715,8 +715,8 @@ def main():
             "data": f"synthetic (seeded Yule tree, alignment simulated under the model: {wl.data_type})",
             "config": {"workload": args.workload, "tips": T, "sites": int(sum(ca.weights)),
                        "patterns": N, "batch": b, "categories": K, "states": S,
-                       "model": {"gtr": "GTR", "hky": "HKY", "general": "general symmetric 20-state",
-                                 "mg94": "MG94 codon (GY94-style)"}[wl.model] + f"+Gamma{K}",
+                       "substitution_model": {"gtr": "GTR", "hky": "HKY", "general": "general symmetric 20-state",
+                                              "mg94": "MG94 codon (GY94-style)"}[wl.model] + f"+Gamma{K}",
                        "l2": "inputs (stored partials) larger than L2; no flush",
                        "parallelism": f"replicas x{world}",
                        **({"slab_patterns": slab,
