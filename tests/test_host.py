@@ -274,3 +274,26 @@ def test_site_models_match_the_reference_known_answers():
     assert float(rates[1]) == 2 / 0.8
     rates, probs = site_models.invariant_rates(torch.tensor([[0.2], [0.3]], dtype=torch.float64))
     assert torch.all((rates * probs).sum(-1) == 1.0)
+
+
+def test_tip_partials_to_codes_fast_path_and_fallbacks(monkeypatch):
+    """Plug-in and functional tips arrive as partial tensors: the codes and table
+    decode back to them exactly, by fingerprints or, after a fingerprint shared
+    by different columns, by the exact lexicographic path."""
+    from torchtree_gb300 import patterns
+
+    rng = np.random.default_rng(12)
+    table = np.vstack([np.eye(4), np.ones((1, 4)), [[1, 0, 1, 0]], [[0, 1, 0, 1]], [[-0.0, 0, 0, 1]]])
+    tips = [table[c].T.copy() for c in rng.integers(0, len(table), size=(9, 700))]
+    w = np.arange(700.0)
+    fast = patterns.from_tip_partials(tips, w)
+    assert fast.table.shape[0] <= len(table) + 1 and fast.codes.dtype == np.uint8
+    np.testing.assert_array_equal(fast.table[fast.codes].transpose(0, 2, 1), np.stack(tips))
+    np.testing.assert_array_equal(fast.weights, w)
+    monkeypatch.setattr(patterns, "_fingerprints", lambda rows: np.zeros(rows.shape[0], dtype=np.uint64))
+    exact = patterns.from_tip_partials(tips, w)  # every column collides: exact path
+    np.testing.assert_array_equal(exact.table[exact.codes].transpose(0, 2, 1), np.stack(tips))
+    monkeypatch.undo()
+    many = [rng.random((4, 300)) for _ in range(2)]  # 600 distinct columns
+    with pytest.raises(ValueError):
+        patterns.from_tip_partials(many, np.ones(300))

@@ -137,12 +137,23 @@ def _compress_codons(sequences, data_type, indices=None) -> CompressedAlignment:
                                columns=cols)
 
 
-def from_tip_partials(tips, weights) -> CompressedAlignment:
-    """Codes and table from arbitrary tip partial tensors ``T x [S, N]``.
+_FP_MULT = np.array([0x9E3779B97F4A7C15, 0xC2B2AE3D27D4EB4F, 0x165667B19E3779F9, 0xD6E8FEB86659FD93],
+                    dtype=np.uint64)
 
-    The distinct tip columns become the table; at most 256 are allowed.
-    """
-    arr = np.stack([np.asarray(t, dtype=np.float64) for t in tips])  # [T,S,N]
+
+def _fingerprints(rows: np.ndarray) -> np.ndarray:
+    """64-bit fingerprint of each row's bytes (``rows [n, S]`` float64)."""
+    words = np.ascontiguousarray(rows).view(np.uint64)
+    h = np.full(rows.shape[0], 0x84222325CBF29CE4, dtype=np.uint64)
+    for j in range(words.shape[1]):
+        w = words[:, j]
+        h = (h ^ (w ^ (w >> np.uint64(31)))) * _FP_MULT[j % 4]
+        h ^= h >> np.uint64(29)
+    return h
+
+
+def _from_tip_partials_exact(arrs, weights) -> CompressedAlignment:
+    arr = np.stack(arrs)  # [T,S,N]
     T, S, N = arr.shape
     cols = np.ascontiguousarray(np.transpose(arr, (0, 2, 1)).reshape(T * N, S))
     table, inverse = np.unique(cols, axis=0, return_inverse=True)
@@ -150,6 +161,45 @@ def from_tip_partials(tips, weights) -> CompressedAlignment:
         raise ValueError(f"{table.shape[0]} distinct tip partial vectors; at most 256 are supported")
     codes = inverse.reshape(T, N).astype(np.uint8)
     return CompressedAlignment(codes=codes, table=table, weights=np.asarray(weights),
+                               columns=np.zeros((T, 0), dtype=np.uint8))
+
+
+def from_tip_partials(tips, weights) -> CompressedAlignment:
+    """Codes and table from arbitrary tip partial tensors ``T x [S, N]``.
+
+    The distinct tip columns become the table (at most 256), in order of
+    first appearance.  Tips are taken one at a time: each column gets a
+    64-bit fingerprint of its bytes, a table row per new fingerprint, and the
+    decoded tip is compared with the original exactly; a fingerprint shared
+    by two different columns (or a NaN) falls back to one lexicographic
+    ``np.unique`` over all columns.
+    """
+    arrs = [np.asarray(t, dtype=np.float64) for t in tips]
+    T = len(arrs)
+    S, N = arrs[0].shape
+    codes = np.empty((T, N), dtype=np.uint8)
+    index: dict = {}  # fingerprint -> code
+    rows_of: list = []  # code -> table row
+    for t, a in enumerate(arrs):
+        if a.shape != (S, N):
+            raise ValueError("every tip partial must have shape [S, N]")
+        rows = np.ascontiguousarray(a.T)  # [N, S]
+        uniq, first, inverse = np.unique(_fingerprints(rows), return_index=True, return_inverse=True)
+        local = np.empty(uniq.size, dtype=np.int64)
+        for i, (key, f) in enumerate(zip(uniq.tolist(), first.tolist())):
+            c = index.get(key)
+            if c is None:  # distinct fingerprints are distinct columns
+                c = len(rows_of)
+                if c >= 256:
+                    raise ValueError("more than 256 distinct tip partial vectors; at most 256 are supported")
+                index[key] = c
+                rows_of.append(rows[f].copy())
+            local[i] = c
+        code = local[inverse.reshape(-1)]
+        if not np.array_equal(np.stack(rows_of)[code], rows):
+            return _from_tip_partials_exact(arrs, weights)
+        codes[t] = code
+    return CompressedAlignment(codes=codes, table=np.stack(rows_of), weights=np.asarray(weights),
                                columns=np.zeros((T, 0), dtype=np.uint8))
 
 
