@@ -132,3 +132,70 @@ def test_flu_a_known_answer_through_the_gpu_path():
                    clock_rates=x3(clock)).cpu().numpy()
         assert np.all(np.abs(lnl3 - KAT) < 1e-12 * abs(KAT)), (rescale, lnl3)
         assert lnl3[0] == lnl3[1] == lnl3[2]
+
+
+def test_flu_a_gradients_of_the_oracle_chain_match_torchtree():
+    """On the same influenza A data, torchtree's own TreeLikelihoodModel
+    (strict clock, JC69, Weibull) and the oracle's pruning agree on lnL and on
+    the autograd gradients with respect to the time lengths, the clock rate
+    and the Weibull shape (1e-9)."""
+    import sys
+
+    root = Path(__file__).resolve().parents[1]
+    for path in (str(root / "tests" / "golden" / "_stub"), str(DATA.parent)):
+        if path not in sys.path:
+            sys.path.insert(0, path)
+    pytest.importorskip("torchtree")
+    from test_plugin import _fixed_tree_class
+    from torchtree import Parameter
+    from torchtree.evolution.alignment import Alignment, Sequence
+    from torchtree.evolution.branch_model import StrictClockModel
+    from torchtree.evolution.datatype import NucleotideDataType
+    from torchtree.evolution.site_model import WeibullSiteModel
+    from torchtree.evolution.site_pattern import SitePattern
+    from torchtree.evolution.substitution_model import JC69
+    from torchtree.evolution.taxa import Taxa, Taxon
+    from torchtree.evolution.tree_likelihood import TreeLikelihoodModel
+
+    from oracle import likelihood as OL
+    from oracle import timetree as OT
+    from torchtree_gb300 import patterns
+    from torchtree_gb300.tree import Topology
+
+    names, seqs = _fasta(DATA / "fluA.fa")
+    topo = Topology.from_newick((DATA / "fluA.tree").read_text().strip(), names)
+    times = _sampling_times(names)
+    ratios, _ = _ratios_from_newick(topo, times)
+    _, lengths, _ = OT.ratio_transform(topo.postorder_list(), times.tolist(), ratios)
+
+    def leaves():
+        return (lengths.detach().clone().requires_grad_(), torch.tensor([0.001], dtype=torch.float64,
+                requires_grad=True), torch.tensor([0.1], dtype=torch.float64, requires_grad=True))
+
+    t_ref, c_ref, s_ref = leaves()
+    dtype = torch.get_default_dtype()
+    torch.set_default_dtype(torch.float64)  # the reference builds its tip partials in the default dtype
+    try:
+        taxa = Taxa(None, [Taxon(n, {}) for n in names])
+        aln = Alignment(None, [Sequence(n, s) for n, s in zip(names, seqs)], taxa, NucleotideDataType(None))
+        tree = _fixed_tree_class()(topo.postorder, names, Parameter(None, t_ref))
+        like = TreeLikelihoodModel(None, SitePattern(None, aln), tree, JC69(None),
+                                   WeibullSiteModel(None, Parameter(None, s_ref), 4),
+                                   StrictClockModel(None, Parameter(None, c_ref), tree))
+        want = like().reshape(-1)
+    finally:
+        torch.set_default_dtype(dtype)
+    assert abs(float(want.detach()[0]) - KAT) < 1e-9 * abs(KAT)
+    g_want = torch.autograd.grad(want.sum(), [t_ref, c_ref, s_ref])
+
+    t, c, s = leaves()
+    ca = patterns.compress(seqs)
+    tips = [torch.tensor(x) for x in ca.tip_partials()]
+    rates, props = OL.weibull_rates(s, 4)
+    mats = OL.p_t_jc69(OL.model_branch_lengths(t, c).unsqueeze(-1) * rates)
+    got = OL.treelikelihood_discrete(tips + [None] * (len(tips) - 1), torch.tensor(ca.weights, dtype=torch.float64),
+                                     topo.postorder_list(), mats, torch.full((1, 4), 0.25, dtype=torch.float64),
+                                     props.reshape(4, 1, 1)).reshape(-1)
+    np.testing.assert_allclose(got.detach().numpy(), want.detach().numpy(), rtol=1e-12)
+    for g, w in zip(torch.autograd.grad(got.sum(), [t, c, s]), g_want):
+        np.testing.assert_allclose(g.numpy(), w.numpy(), rtol=1e-9, atol=1e-9 * float(w.abs().max()))
