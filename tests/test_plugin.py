@@ -245,3 +245,68 @@ def test_json_route_selects_the_plugin_class(torchtree_ref):
     assert isinstance(like, TreeLikelihoodModel) and like.precision == "f32" and like.rescale
     assert like.clock_model is clock and dic["like"] is like
     assert like._alignment.codes.shape == (8, like.weights.shape[0])
+
+
+@pytest.mark.parametrize("seed", range(12))
+def test_compression_matches_torchtree_on_random_alignments(torchtree_ref, seed):
+    """Randomized parity of the compression path (C++ column sort behind
+    ``patterns.compress``) against torchtree's own ``compress_alignment`` /
+    ``compress_alignment_states``: same pattern order and weights, and tip
+    partials / states bit-exact, with IUPAC ambiguity codes, gaps, unknowns and
+    lower case, in unsorted taxon order, with and without ambiguities.  Amino
+    acids and codons (gaps, stop codons) too."""
+    from torchtree.evolution.alignment import Alignment, Sequence
+    from torchtree.evolution.datatype import AminoAcidDataType, NucleotideDataType
+    from torchtree.evolution.site_pattern import compress_alignment, compress_alignment_states
+    from torchtree.evolution.taxa import Taxa, Taxon
+
+    from torchtree_gb300 import datatype, patterns
+
+    rng = np.random.default_rng(100 + seed)
+    T, L = int(rng.integers(2, 12)), int(rng.integers(1, 400))
+    if seed % 4 == 3:
+        _codon_case(rng, T, L)
+        return
+    amino = seed % 4 == 2
+    alphabet = list("ACDEFGHIKLMNPQRSTVWYXBZ-?acd") if amino else list("ACGTACGTACGTRYKMSWBDHVN-?acgtu")
+    repeats = rng.integers(1, 4)  # repeated columns make weights > 1
+    base = rng.choice(alphabet, size=(T, max(1, L // repeats)))
+    cols = np.tile(base, (1, repeats))[:, rng.permutation(base.shape[1] * repeats)]
+    seqs = ["".join(r) for r in cols]
+    names = [f"t{i}" for i in rng.permutation(T)]
+    dt_ref = AminoAcidDataType(None) if amino else NucleotideDataType(None)
+    dt = datatype.AminoAcid() if amino else datatype.Nucleotide()
+    aln = Alignment(None, [Sequence(n, s) for n, s in zip(names, seqs)], Taxa(None, [Taxon(n, {}) for n in names]),
+                    dt_ref)
+    for amb in (False, True):
+        parts, w = compress_alignment(aln, None, amb)
+        ca = patterns.compress(seqs, dt, use_ambiguities=amb)
+        assert ca.weights.tolist() == w.tolist()
+        np.testing.assert_array_equal(ca.tip_partials(), np.stack([p.numpy() for p in parts]))
+    states, w = compress_alignment_states(aln)
+    st = patterns.compress(seqs, dt, tip_states=True)
+    assert st.weights.tolist() == w.tolist()
+    assert st.codes.tolist() == [s.tolist() for s in states]
+
+
+def _codon_case(rng, T, L):
+    from torchtree.evolution.alignment import Alignment, Sequence
+    from torchtree.evolution.datatype import CodonDataType
+    from torchtree.evolution.site_pattern import compress_alignment, compress_alignment_states
+    from torchtree.evolution.taxa import Taxa, Taxon
+
+    from torchtree_gb300 import datatype, patterns
+
+    sense = [a + b + c for a in "ACGT" for b in "ACGT" for c in "ACGT"]
+    pool = sense + ["---", "TAA", "TGA", "TAG"]  # gaps and stop codons
+    n = max(1, L // 3)
+    seqs = ["".join(rng.choice(pool, size=n)) for _ in range(T)]
+    names = [f"c{i}" for i in rng.permutation(T)]
+    aln = Alignment(None, [Sequence(m, s) for m, s in zip(names, seqs)], Taxa(None, [Taxon(m, {}) for m in names]),
+                    CodonDataType(None, "Universal"))
+    parts, w = compress_alignment(aln, None, False)
+    ca = patterns.compress(seqs, datatype.Codon())
+    assert ca.weights.tolist() == w.tolist()
+    np.testing.assert_array_equal(ca.tip_partials(), np.stack([p.numpy() for p in parts]))
+    states, w = compress_alignment_states(aln)
+    assert ca.codes.tolist() == [s.tolist() for s in states]
