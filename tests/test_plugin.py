@@ -310,3 +310,84 @@ def _codon_case(rng, T, L):
     np.testing.assert_array_equal(ca.tip_partials(), np.stack([p.numpy() for p in parts]))
     states, w = compress_alignment_states(aln)
     assert ca.codes.tolist() == [s.tolist() for s in states]
+
+
+@pytest.mark.parametrize("seed", range(10))
+def test_model_inputs_on_random_problems(torchtree_ref, seed):
+    """Randomized form of the input-gathering check: tree size, model (GTR, HKY,
+    JC69), site model (Weibull, Weibull + invariant, constant), clock or not,
+    tip states or partials, rescaling and batch drawn at random; the oracle's
+    lnL and gradients from the plug-in's inputs equal torchtree's own."""
+    from torchtree import Parameter
+    from torchtree.evolution.alignment import Alignment, Sequence
+    from torchtree.evolution.branch_model import StrictClockModel
+    from torchtree.evolution.datatype import NucleotideDataType
+    from torchtree.evolution.site_model import ConstantSiteModel, WeibullSiteModel
+    from torchtree.evolution.site_pattern import SitePattern
+    from torchtree.evolution.substitution_model import GTR, HKY, JC69
+    from torchtree.evolution.taxa import Taxa, Taxon
+    from torchtree.evolution.tree_likelihood import TreeLikelihoodModel as Reference
+
+    from torchtree_gb300 import synthetic
+    from torchtree_gb300.model import TreeLikelihoodModel
+
+    rng = np.random.default_rng(500 + seed)
+    T, b = int(rng.integers(3, 25)), int(rng.integers(1, 3))
+    subst_kind = ["gtr", "hky", "jc69"][seed % 3]
+    site_kind = ["weibull", "weibull_inv", "constant"][(seed // 3) % 3]
+    clock_on, tip_states, rescale = bool(rng.integers(2)), bool(rng.integers(2)), bool(rng.integers(2))
+    wl = synthetic.dna_workload("r", tip_count=T, site_count=int(rng.integers(20, 300)), batch=b,
+                                seed=600 + seed, shape=float(rng.uniform(0.2, 2.0)), site_model="weibull")
+    names = wl.topology.tip_names
+    B = 2 * T - 2
+
+    def build():
+        leaf = lambda a: torch.tensor(np.asarray(a, dtype=np.float64), requires_grad=True)  # noqa: E731
+        leaves = []
+        taxa = Taxa(None, [Taxon(n, {}) for n in names])
+        aln = Alignment(None, [Sequence(n, s) for n, s in zip(names, wl.sequences)], taxa,
+                        NucleotideDataType(None))
+        if clock_on:
+            bl = leaf(np.random.default_rng(seed).uniform(0.5, 5.0, (b, B)))
+            tree = _fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
+            rate = leaf(np.full((b, 1), 0.02))
+            clock = StrictClockModel(None, Parameter(None, rate), tree)
+            leaves += [bl, rate]
+        else:
+            bl = leaf(wl.branch_lengths)
+            tree = _fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
+            clock = None
+            leaves.append(bl)
+        if subst_kind == "jc69":
+            subst = JC69(None)
+        else:
+            pi = leaf(wl.pi)
+            if subst_kind == "gtr":
+                ex = leaf(wl.exch)
+                subst = GTR(None, Parameter(None, ex), Parameter(None, pi))
+            else:
+                ex = leaf(wl.exch[:, 1:2])
+                subst = HKY(None, Parameter(None, ex), Parameter(None, pi))
+            leaves += [ex, pi]
+        if site_kind == "constant":
+            site = ConstantSiteModel(None)
+        else:
+            shape = leaf(wl.shape)
+            inv = leaf(np.full((b, 1), 0.15)) if site_kind == "weibull_inv" else None
+            site = WeibullSiteModel(None, Parameter(None, shape), 4,
+                                    invariant=Parameter(None, inv) if inv is not None else None)
+            leaves += [shape] + ([inv] if inv is not None else [])
+        return tree, SitePattern(None, aln), subst, site, clock, leaves
+
+    tree, sp, subst, site, clock, leaves = build()
+    ref = Reference(None, sp, tree, subst, site, clock, False, tip_states)
+    ref.rescale = rescale
+    want = ref().reshape(-1)
+    gwant = torch.autograd.grad(want.sum(), leaves)
+    tree, sp, subst, site, clock, leaves = build()
+    ours = TreeLikelihoodModel(None, sp, tree, subst, site, clock, False, tip_states)
+    route, tensors, _, _ = ours.engine_inputs(torch.device("cpu"))
+    got = _oracle_lnl(route, tensors, wl.topology, ours._alignment, rescale)
+    np.testing.assert_allclose(got.detach().numpy(), want.detach().numpy(), rtol=1e-12)
+    for g, w in zip(torch.autograd.grad(got.sum(), leaves), gwant):
+        np.testing.assert_allclose(g.numpy(), w.numpy(), rtol=1e-9, atol=1e-9 * float(w.abs().max()))
