@@ -2,25 +2,21 @@
 generated configuration, and ``model.TreeLikelihoodModel``'s gathering of
 engine inputs checked against torchtree's own ``TreeLikelihoodModel``.
 
-The model tests import torchtree from its source tree (TORCHTREE_REFERENCE,
-else the default below) with the three-class dendropy stub of
-``tests/golden/_stub``; they are skipped where the source is absent.  They run
+The model tests import torchtree from its source tree
+(``tests/reference_models.py``); they are skipped where it is absent.  They run
 on the CPU: the inputs that ``_call`` would hand to the engine are gathered
 on the CPU and evaluated by the oracle, and the result must equal the
 reference model's own lnL (1e-12 relative).  Without CUDA, ``_call`` itself
 must raise (no CPU fallback).
 """
 import argparse
-import os
-import sys
-from pathlib import Path
 
 import numpy as np
 import pytest
 import torch
 
-ROOT = Path(__file__).resolve().parents[1]
-REF = Path(os.environ.get("TORCHTREE_REFERENCE", "/root/reference"))
+from tests.reference_models import fixed_tree_class, import_torchtree
+
 
 
 def test_cli_hook_retargets_every_likelihood():
@@ -41,14 +37,9 @@ def test_cli_hook_retargets_every_likelihood():
 
 @pytest.fixture(scope="module")
 def torchtree_ref():
-    if not (REF / "torchtree").is_dir():
+    if not import_torchtree():
         pytest.skip("torchtree source not present")
-    for path in (str(ROOT / "tests" / "golden" / "_stub"), str(REF)):
-        if path not in sys.path:
-            sys.path.insert(0, path)
     torch.set_default_dtype(torch.float64)
-    import torchtree  # noqa: F401
-
     yield
     torch.set_default_dtype(torch.float32)
 
@@ -69,49 +60,6 @@ def test_plugin_flag_adds_arguments_and_retargets(torchtree_ref):
     data = {"id": "like", "type": "TreeLikelihoodModel"}
     plugin.process_tree_likelihood(parser.parse_args(["map"]), data)
     assert data["type"] == "TreeLikelihoodModel"
-
-
-def _fixed_tree_class():
-    from torchtree.evolution.tree_model import TreeModel
-
-    class FixedTree(TreeModel):
-        """Minimal TreeModel: fixed post-order, branch lengths from a Parameter."""
-
-        def __init__(self, post, names, bl):
-            super().__init__(None)
-            self._post = [list(map(int, t)) for t in post]
-            self._names = list(names)
-            self._bl = bl
-            self.taxa_count = len(names)
-
-        def branch_lengths(self):
-            return self._bl.tensor
-
-        @property
-        def postorder(self):
-            return self._post
-
-        @property
-        def taxa(self):
-            return self._names
-
-        def write_newick(self, stream, **kwargs):
-            stream.write("();")
-
-        def _sample_shape(self):
-            return self._bl.tensor.shape[:-1]
-
-        def handle_model_changed(self, model, obj, index):
-            pass
-
-        def handle_parameter_changed(self, variable, index, event):
-            self.fire_model_changed()
-
-        @classmethod
-        def from_json(cls, data, dic):
-            raise NotImplementedError
-
-    return FixedTree
 
 
 def _oracle_lnl(route, tensors, topo, alignment, rescale):
@@ -153,12 +101,12 @@ def _models(case, wl, b):
     if case == "hky_weibull_clock":  # rooted time lengths (2T-2) times a strict clock
         bl = leaf(torch.cat((bl, torch.full((b, 1), 0.02)), -1).numpy() * 10.0)
         rate = leaf(np.full((b, 1), 0.1))
-        tree = _fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
+        tree = fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
         clock = StrictClockModel(None, Parameter(None, rate), tree)
         leaves = [bl, rate]
     else:
         bl = leaf(bl.numpy())
-        tree = _fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
+        tree = fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
         leaves = [bl]
     pi_t = leaf(wl.pi[:b])
     pi = Parameter(None, pi_t)
@@ -349,13 +297,13 @@ def test_model_inputs_on_random_problems(torchtree_ref, seed):
                         NucleotideDataType(None))
         if clock_on:
             bl = leaf(np.random.default_rng(seed).uniform(0.5, 5.0, (b, B)))
-            tree = _fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
+            tree = fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
             rate = leaf(np.full((b, 1), 0.02))
             clock = StrictClockModel(None, Parameter(None, rate), tree)
             leaves += [bl, rate]
         else:
             bl = leaf(wl.branch_lengths)
-            tree = _fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
+            tree = fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
             clock = None
             leaves.append(bl)
         if subst_kind == "jc69":

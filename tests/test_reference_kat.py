@@ -10,18 +10,16 @@ lnL = -4618.2062529058 with and without rescaling.  Here the same chain runs
 through this package's Newick parser, tip-date heights and pattern
 compression and the oracle's ratio transform and pruning, which pins the
 oracle's time-tree, clock and Weibull chain to the reference's own number.
-The source location is TORCHTREE_REFERENCE, else the default below; the test
-is skipped where the data are absent.
+The source location comes from ``tests/reference_models.py``; the tests are
+skipped where the data are absent.
 """
-import os
-from pathlib import Path
-
 import numpy as np
 import pytest
 import torch
 
+from tests.reference_models import DATA, fixed_tree_class, import_torchtree
+
 KAT = -4618.2062529058
-DATA = Path(os.environ.get("TORCHTREE_REFERENCE", "/root/reference")) / "data"
 
 pytestmark = pytest.mark.skipif(not (DATA / "fluA.fa").exists(), reason="reference data not present")
 
@@ -139,14 +137,8 @@ def test_flu_a_gradients_of_the_oracle_chain_match_torchtree():
     (strict clock, JC69, Weibull) and the oracle's pruning agree on lnL and on
     the autograd gradients with respect to the time lengths, the clock rate
     and the Weibull shape (1e-9)."""
-    import sys
-
-    root = Path(__file__).resolve().parents[1]
-    for path in (str(root / "tests" / "golden" / "_stub"), str(DATA.parent)):
-        if path not in sys.path:
-            sys.path.insert(0, path)
-    pytest.importorskip("torchtree")
-    from test_plugin import _fixed_tree_class
+    if not import_torchtree():
+        pytest.skip("torchtree source not present")
     from torchtree import Parameter
     from torchtree.evolution.alignment import Alignment, Sequence
     from torchtree.evolution.branch_model import StrictClockModel
@@ -178,7 +170,7 @@ def test_flu_a_gradients_of_the_oracle_chain_match_torchtree():
     try:
         taxa = Taxa(None, [Taxon(n, {}) for n in names])
         aln = Alignment(None, [Sequence(n, s) for n, s in zip(names, seqs)], taxa, NucleotideDataType(None))
-        tree = _fixed_tree_class()(topo.postorder, names, Parameter(None, t_ref))
+        tree = fixed_tree_class()(topo.postorder, names, Parameter(None, t_ref))
         like = TreeLikelihoodModel(None, SitePattern(None, aln), tree, JC69(None),
                                    WeibullSiteModel(None, Parameter(None, s_ref), 4),
                                    StrictClockModel(None, Parameter(None, c_ref), tree))
