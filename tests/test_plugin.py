@@ -339,3 +339,59 @@ def test_model_inputs_on_random_problems(torchtree_ref, seed):
     np.testing.assert_allclose(got.detach().numpy(), want.detach().numpy(), rtol=1e-12)
     for g, w in zip(torch.autograd.grad(got.sum(), leaves), gwant):
         np.testing.assert_allclose(g.numpy(), w.numpy(), rtol=1e-9, atol=1e-9 * float(w.abs().max()))
+
+
+@pytest.mark.parametrize("kind,seed", [("protein", 0), ("codon", 1), ("protein", 2), ("codon", 3)])
+def test_model_inputs_for_amino_acids_and_codons(torchtree_ref, kind, seed):
+    """The plug-in on 20- and 61-state models (GeneralSymmetricSubstitutionModel
+    with 190 free rates, MG94 with alpha = 1), against torchtree's own lnL and
+    gradients (1e-10 / 1e-8: 61 x 61 matrix exponentials)."""
+    from torchtree import Parameter
+    from torchtree.evolution.alignment import Alignment, Sequence
+    from torchtree.evolution.datatype import AminoAcidDataType, CodonDataType
+    from torchtree.evolution.site_model import WeibullSiteModel
+    from torchtree.evolution.site_pattern import SitePattern
+    from torchtree.evolution.substitution_model import MG94
+    from torchtree.evolution.substitution_model.general import GeneralSymmetricSubstitutionModel
+    from torchtree.evolution.taxa import Taxa, Taxon
+    from torchtree.evolution.tree_likelihood import TreeLikelihoodModel as Reference
+
+    from torchtree_gb300 import synthetic
+    from torchtree_gb300.model import TreeLikelihoodModel
+
+    if kind == "protein":
+        wl = synthetic.protein_workload("p", tip_count=9, site_count=80, batch=1, seed=700 + seed, shape=0.7,
+                                        site_model="weibull", branch_mean=0.1)
+    else:
+        wl = synthetic.codon_workload("c", tip_count=6, site_count=40, batch=1, seed=700 + seed, shape=0.7,
+                                      site_model="weibull", branch_mean=0.1)
+    names = wl.topology.tip_names
+
+    def build():
+        leaf = lambda a: torch.tensor(np.asarray(a, dtype=np.float64), requires_grad=True)  # noqa: E731
+        bl, pi, shape, ex = leaf(wl.branch_lengths), leaf(wl.pi), leaf(wl.shape), leaf(wl.exch)
+        if kind == "protein":
+            dtype = AminoAcidDataType(None)
+            subst = GeneralSymmetricSubstitutionModel(None, dtype, Parameter(None, torch.arange(190)),
+                                                      Parameter(None, ex), Parameter(None, pi))
+        else:
+            dtype = CodonDataType(None, "Universal")
+            subst = MG94(None, dtype, Parameter(None, torch.ones_like(ex[..., :1])), Parameter(None, ex[..., 1:2]),
+                         Parameter(None, ex[..., 0:1]), Parameter(None, pi))
+        taxa = Taxa(None, [Taxon(n, {}) for n in names])
+        aln = Alignment(None, [Sequence(n, s) for n, s in zip(names, wl.sequences)], taxa, dtype)
+        tree = fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
+        site = WeibullSiteModel(None, Parameter(None, shape), 4)
+        return tree, SitePattern(None, aln), subst, site, [bl, ex, pi, shape]
+
+    tree, sp, subst, site, leaves = build()
+    want = Reference(None, sp, tree, subst, site)().reshape(-1)
+    gwant = torch.autograd.grad(want.sum(), leaves)
+    tree, sp, subst, site, leaves = build()
+    ours = TreeLikelihoodModel(None, sp, tree, subst, site)
+    route, tensors, _, (_, S, _) = ours.engine_inputs(torch.device("cpu"))
+    assert route == "rate_matrix" and S == (20 if kind == "protein" else 61)
+    got = _oracle_lnl(route, tensors, wl.topology, ours._alignment, False)
+    np.testing.assert_allclose(got.detach().numpy(), want.detach().numpy(), rtol=1e-10)
+    for g, w in zip(torch.autograd.grad(got.sum(), leaves), gwant):
+        np.testing.assert_allclose(g.numpy(), w.numpy(), rtol=1e-8, atol=1e-8 * float(w.abs().max()))
