@@ -395,3 +395,67 @@ def test_model_inputs_for_amino_acids_and_codons(torchtree_ref, kind, seed):
     np.testing.assert_allclose(got.detach().numpy(), want.detach().numpy(), rtol=1e-10)
     for g, w in zip(torch.autograd.grad(got.sum(), leaves), gwant):
         np.testing.assert_allclose(g.numpy(), w.numpy(), rtol=1e-8, atol=1e-8 * float(w.abs().max()))
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_time_tree_oracle_matches_torchtree_on_random_trees(torchtree_ref, seed):
+    """The oracle behind the time-tree kernels against torchtree's own
+    GeneralNodeHeightTransform (heights, branch lengths, log|J|) and
+    ConstantCoalescent, values and autograd gradients, on random trees with
+    isochronous, heterochronous and tied sampling times."""
+    from types import SimpleNamespace
+
+    from torchtree.evolution.coalescent import ConstantCoalescent
+    from torchtree.evolution.tree_height_transform import GeneralNodeHeightTransform
+    from torchtree.evolution.tree_model import heights_to_branch_lengths
+
+    from oracle import timetree as OT
+    from torchtree_gb300 import synthetic
+
+    rng = np.random.default_rng(800 + seed)
+    T = int(rng.integers(2, 60))
+    topo = synthetic.yule_topology(T, rng)
+    kind = seed % 3
+    times = np.zeros(T) if kind == 0 else (rng.uniform(0, 2, T) if kind == 1 else np.round(rng.uniform(0, 1, T), 1))
+    times[int(rng.integers(T))] = 0.0
+    kids = {int(v): (int(l), int(r)) for v, l, r in topo.postorder}
+    pre, stack = [], [2 * T - 2]
+    while stack:  # parent before child
+        v = stack.pop()
+        if v >= T:
+            for c in kids[v]:
+                pre.append((v, c))
+                stack.append(c)
+    fake = SimpleNamespace(taxa_count=T, postorder=[list(map(int, t)) for t in topo.postorder],
+                           preorder=torch.tensor(pre), sampling_times=torch.tensor(times))
+    tr = GeneralNodeHeightTransform(fake)
+    x = np.concatenate([rng.uniform(0.05, 0.95, T - 2), [float(times.max()) + rng.uniform(0.5, 3.0)]])
+    w_h, w_b = rng.normal(size=T - 1), rng.normal(size=2 * T - 2)
+    theta_v = float(rng.uniform(0.3, 3.0))
+
+    def objective(heights, bl, logdet):
+        return (heights * torch.tensor(w_h)).sum() + 0.7 * logdet.sum() + (bl * torch.tensor(w_b)).sum()
+
+    xr = torch.tensor(x, requires_grad=True)
+    hr = tr(xr)
+    ldr = tr.log_abs_det_jacobian(xr, hr)
+    blr = heights_to_branch_lengths(hr, tr._bounds, fake.preorder)
+    (gr,) = torch.autograd.grad(objective(hr, blr, ldr), xr)
+    xo = torch.tensor(x, requires_grad=True)
+    ho, blo, ldo = OT.ratio_transform(topo.postorder.tolist(), times.tolist(), xo)
+    (go,) = torch.autograd.grad(objective(ho, blo, ldo), xo)
+    np.testing.assert_allclose(ho.detach().numpy(), hr.detach().numpy(), rtol=1e-13)
+    np.testing.assert_allclose(blo.detach().numpy(), blr.detach().numpy(), rtol=1e-12, atol=1e-13)
+    np.testing.assert_allclose(float(ldo.detach()), float(ldr.detach()), rtol=1e-12, atol=1e-12)
+    np.testing.assert_allclose(go.numpy(), gr.numpy(), rtol=1e-10, atol=1e-10 * float(gr.abs().max()))
+
+    h_int = hr.detach().clone()
+    hh_r, th_r = h_int.clone().requires_grad_(), torch.tensor([theta_v], requires_grad=True)
+    lp_r = ConstantCoalescent(th_r).log_prob(torch.cat((torch.tensor(times), hh_r)))
+    g_r = torch.autograd.grad(lp_r.sum(), [hh_r, th_r])
+    hh_o, th_o = h_int.clone().requires_grad_(), torch.tensor([theta_v], requires_grad=True)
+    lp_o = OT.constant_coalescent(times.tolist(), hh_o, th_o)
+    g_o = torch.autograd.grad(lp_o.sum(), [hh_o, th_o])
+    np.testing.assert_allclose(float(lp_o.detach().reshape(-1)[0]), float(lp_r.detach().reshape(-1)[0]), rtol=1e-12)
+    for a, b in zip(g_o, g_r):
+        np.testing.assert_allclose(a.numpy(), b.numpy(), rtol=1e-10, atol=1e-10 * float(b.abs().max()))
