@@ -459,3 +459,56 @@ def test_time_tree_oracle_matches_torchtree_on_random_trees(torchtree_ref, seed)
     np.testing.assert_allclose(float(lp_o.detach().reshape(-1)[0]), float(lp_r.detach().reshape(-1)[0]), rtol=1e-12)
     for a, b in zip(g_o, g_r):
         np.testing.assert_allclose(a.numpy(), b.numpy(), rtol=1e-10, atol=1e-10 * float(b.abs().max()))
+
+
+@pytest.mark.parametrize("seed", range(8))
+def test_oracle_pruning_functions_match_torchtree(torchtree_ref, seed):
+    """Each oracle pruning function against the reference function it restates
+    (tree_likelihood.py:14-278), on random trees, partials, matrices and
+    batches: the unscaled, rescaled and tip-state variants, and the selective
+    rescaling after an underflow."""
+    from torchtree.evolution import tree_likelihood as TL
+
+    from oracle import likelihood as OL
+    from torchtree_gb300 import synthetic
+
+    rng = np.random.default_rng(900 + seed)
+    T, S, K, N = int(rng.integers(2, 30)), [4, 20][seed % 2], int(rng.integers(1, 5)), int(rng.integers(1, 60))
+    bshape = [(), (2,), (3,)][seed % 3]
+    post = synthetic.yule_topology(T, rng).postorder.tolist()
+    B = 2 * T - 2
+    q = rng.random(bshape + (B, K, S, S))
+    mats = torch.tensor(q / q.sum(-1, keepdims=True))
+    f = rng.random(bshape + (1, S))
+    freqs = torch.tensor(f / f.sum(-1, keepdims=True))
+    p = rng.random(bshape + (K, 1, 1))
+    props = torch.tensor(p / p.sum(-3, keepdims=True))
+    weights = torch.tensor(rng.integers(1, 5, N), dtype=torch.float64)
+    tips = [torch.tensor(rng.random((S, N))) for _ in range(T)]
+    states = [torch.tensor(rng.integers(0, S + 1, N)) for _ in range(T)]
+    blank = [None] * (T - 1)
+
+    def close(a, b):
+        np.testing.assert_allclose(a.numpy(), b.numpy(), rtol=1e-12)
+
+    close(OL.treelikelihood_discrete(tips + blank, weights, post, mats, freqs, props),
+          TL.calculate_treelikelihood_discrete(tips + blank, weights, post, mats, freqs, props))
+    close(OL.treelikelihood_discrete_rescaled(tips + blank, weights, post, mats, freqs, props),
+          TL.calculate_treelikelihood_discrete_rescaled(tips + blank, weights, post, mats, freqs, props))
+    close(OL.treelikelihood_tip_states_discrete(states + blank, weights, post, mats, freqs, props),
+          TL.calculate_treelikelihood_tip_states_discrete(states + blank, weights, post, mats, freqs, props))
+    close(OL.treelikelihood_tip_states_discrete_rescaled(states + blank, weights, post, mats, freqs, props),
+          TL.calculate_treelikelihood_tip_states_discrete_rescaled(states + blank, weights, post, mats, freqs,
+                                                                   props))
+    one = mats[..., 0, :, :]  # single category
+    close(OL.treelikelihood(tips + blank, weights, post, one, freqs),
+          TL.calculate_treelikelihood(tips + blank, weights, post, one, freqs))
+    # selective rescaling on the partials an unscaled pass left behind (tiny values underflow)
+    small = [t * 1e-30 for t in tips]
+    failed = small + list(blank)
+    TL.calculate_treelikelihood_discrete(failed, weights, post, mats, freqs, props)  # fills the internals
+    close(OL.treelikelihood_discrete_safe(list(failed), weights, post, mats, freqs, props, 1e-20),
+          TL.calculate_treelikelihood_discrete_safe(list(failed), weights, post, mats, freqs, props, 1e-20))
+    lnl, flag = OL.unscaled_then_safe(small + list(blank), weights, post, mats, freqs, props, 1e-20)
+    close(lnl, TL.calculate_treelikelihood_discrete_safe(list(failed), weights, post, mats, freqs, props, 1e-20)
+          if flag else TL.calculate_treelikelihood_discrete(small + list(blank), weights, post, mats, freqs, props))
