@@ -512,3 +512,52 @@ def test_oracle_pruning_functions_match_torchtree(torchtree_ref, seed):
     lnl, flag = OL.unscaled_then_safe(small + list(blank), weights, post, mats, freqs, props, 1e-20)
     close(lnl, TL.calculate_treelikelihood_discrete_safe(list(failed), weights, post, mats, freqs, props, 1e-20)
           if flag else TL.calculate_treelikelihood_discrete(small + list(blank), weights, post, mats, freqs, props))
+
+
+@pytest.mark.parametrize("seed", range(6))
+def test_rate_matrices_and_eigen_form_match_torchtree(torchtree_ref, seed):
+    """The package's host-side Q builders (GTR, HKY, general symmetric 20-state,
+    MG94) and its eigen form P = U diag(exp(lambda t)) W against the reference
+    models' q() and p_t() on random parameters (batched)."""
+    from torchtree import Parameter
+    from torchtree.evolution.datatype import AminoAcidDataType, CodonDataType
+    from torchtree.evolution.substitution_model import GTR, HKY, MG94
+    from torchtree.evolution.substitution_model.general import GeneralSymmetricSubstitutionModel
+
+    from torchtree_gb300 import substitution
+
+    rng = np.random.default_rng(1000 + seed)
+    b = int(rng.integers(1, 4))
+    kind = ["gtr", "hky", "general", "mg94"][seed % 4]
+    t = torch.tensor(rng.uniform(0.001, 2.0, (b, 5)))
+    if kind in ("gtr", "hky"):
+        S = 4
+    elif kind == "general":
+        S = 20
+    else:
+        S = 61
+    pi = torch.tensor(rng.dirichlet(np.ones(S), size=b))
+    if kind == "gtr":
+        ex = torch.tensor(rng.gamma(1.0, 1.0, (b, 6)))
+        ref, ours = GTR(None, Parameter(None, ex), Parameter(None, pi)), substitution.gtr_q(ex, pi)
+    elif kind == "hky":
+        kappa = torch.tensor(rng.lognormal(1.0, 0.5, (b, 1)))
+        ref, ours = HKY(None, Parameter(None, kappa), Parameter(None, pi)), substitution.hky_q(kappa, pi)
+    elif kind == "general":
+        ex = torch.tensor(rng.gamma(1.0, 1.0, (b, 190)))
+        ref = GeneralSymmetricSubstitutionModel(None, AminoAcidDataType(None), Parameter(None, torch.arange(190)),
+                                                Parameter(None, ex), Parameter(None, pi))
+        ours = substitution.general_symmetric_q(ex, pi, 20)
+    else:
+        omega = torch.tensor(rng.gamma(2.0, 0.25, (b, 1)))
+        kappa = torch.tensor(rng.lognormal(1.0, 0.5, (b, 1)))
+        ref = MG94(None, CodonDataType(None, "Universal"), Parameter(None, torch.ones_like(omega)),
+                   Parameter(None, omega), Parameter(None, kappa), Parameter(None, pi))
+        ours = substitution.mg94_q(torch.ones_like(omega), omega, kappa, pi)
+    q_ref = ref.q()
+    q_ref = q_ref / ref.norm(q_ref)[..., None, None]
+    np.testing.assert_allclose(substitution.normalise(ours, pi).numpy(), q_ref.expand(b, S, S).numpy(),
+                               rtol=1e-12, atol=1e-14)
+    lam, u, w = substitution.eigen_system(ours, pi)
+    mine = u[:, None] @ torch.diag_embed(torch.exp(lam[:, None] * t[..., None])) @ w[:, None]
+    np.testing.assert_allclose(mine.numpy(), ref.p_t(t).expand(b, 5, S, S).numpy(), rtol=1e-9, atol=1e-12)
