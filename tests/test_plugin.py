@@ -561,3 +561,40 @@ def test_rate_matrices_and_eigen_form_match_torchtree(torchtree_ref, seed):
     lam, u, w = substitution.eigen_system(ours, pi)
     mine = u[:, None] @ torch.diag_embed(torch.exp(lam[:, None] * t[..., None])) @ w[:, None]
     np.testing.assert_allclose(mine.numpy(), ref.p_t(t).expand(b, 5, S, S).numpy(), rtol=1e-9, atol=1e-12)
+
+
+@pytest.mark.parametrize("seed", range(4))
+def test_site_models_match_torchtree(torchtree_ref, seed):
+    """The package's Weibull rates (with invariant sites and mu) and the
+    proportion-invariant model against torchtree's own site models on random
+    batched parameters, values and shape gradients."""
+    from torchtree import Parameter
+    from torchtree.evolution.site_model import InvariantSiteModel, WeibullSiteModel
+
+    from torchtree_gb300 import site_models
+
+    rng = np.random.default_rng(1100 + seed)
+    b, K = int(rng.integers(1, 4)), int(rng.integers(1, 9))
+    shape_v = rng.uniform(0.05, 5.0, (b, 1))
+    inv_v = rng.uniform(0.0, 0.6, (b, 1)) if seed % 2 else None
+    mu_v = rng.uniform(0.5, 2.0, (b, 1)) if seed >= 2 else None
+    leaf = lambda a: torch.tensor(a, requires_grad=True)  # noqa: E731
+    s_ref = leaf(shape_v)
+    ref = WeibullSiteModel(None, Parameter(None, s_ref), K,
+                           invariant=Parameter(None, torch.tensor(inv_v)) if inv_v is not None else None,
+                           mu=Parameter(None, torch.tensor(mu_v)) if mu_v is not None else None)
+    s_ours = leaf(shape_v)
+    rates, probs = site_models.weibull_rates(s_ours, K, invariant=torch.tensor(inv_v) if inv_v is not None else None,
+                                             mu=torch.tensor(mu_v) if mu_v is not None else None)
+    np.testing.assert_allclose(rates.detach().numpy(), ref.rates().detach().numpy(), rtol=1e-13, atol=1e-300)
+    np.testing.assert_allclose(probs.numpy(), ref.probabilities().expand(probs.shape).numpy(), rtol=1e-14)
+    wts = torch.tensor(rng.normal(size=rates.shape))
+    (g_ref,) = torch.autograd.grad((ref.rates() * wts).sum(), s_ref)
+    (g_ours,) = torch.autograd.grad((rates * wts).sum(), s_ours)
+    np.testing.assert_allclose(g_ours.numpy(), g_ref.numpy(), rtol=1e-11, atol=1e-300)
+    p = torch.tensor(rng.uniform(0.0, 0.9, (b, 1)))
+    inv_ref = InvariantSiteModel(None, Parameter(None, p), Parameter(None, torch.tensor(mu_v)) if mu_v is not None
+                                 else None)
+    r2, p2 = site_models.invariant_rates(p, mu=torch.tensor(mu_v) if mu_v is not None else None)
+    np.testing.assert_allclose(r2.numpy(), inv_ref.rates().numpy(), rtol=1e-14)
+    np.testing.assert_allclose(p2.numpy(), inv_ref.probabilities().numpy(), rtol=1e-14)
