@@ -3,7 +3,6 @@ schedule, the package's tip encodings / pattern compression / tree glue
 against the reference's golden vectors, the eigen form, the site-model
 gradient, and the replica timing over two gloo ranks."""
 import ctypes
-import json
 import os
 import re
 import sys
