@@ -63,10 +63,13 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
                    int32_t state_count, int32_t category_count,
                    int32_t pattern_count, int32_t batch, int32_t precision);
 
-/* Release a plan and its device memory (NULL is accepted). */
+/* Release a plan and its device memory (NULL is accepted).  The reference
+ * frees its tensors with the TreeLikelihoodModel object: no explicit
+ * counterpart. */
 int tt_plan_destroy(tt_plan *plan);
 
-/* Device bytes held by the plan. */
+/* Device bytes held by the plan (no reference counterpart; admission by
+ * memory footprint uses it). */
 int tt_plan_workspace_bytes(const tt_plan *plan, size_t *bytes);
 
 /*
@@ -175,13 +178,17 @@ int tt_rate_matrix_gradient(tt_plan *plan, const double *eigenvalues,
 
 /*
  * Device status word: TT_OK, or TT_ERR_DEVICE_TIMEOUT when a kernel's
- * bounded wait gave up since the last reset.  Synchronises the stream.
+ * bounded wait gave up since the last reset.  Synchronises the stream.  No
+ * reference counterpart: the reference has no device waits and reports
+ * numeric trouble in-band (a -inf lnL, tree_likelihood.py:378-388).
  */
 int tt_plan_device_status(tt_plan *plan, void *stream, int32_t *status,
                           int32_t reset);
 
 /*
- * Host-only: the execution schedule a plan would use (no device needed).
+ * Host-only: the execution schedule a plan would use (no device needed):
+ * the post-order of update_traversals (tree_model.py:187-195) as the
+ * kernels' step records.
  *   steps: int32 [T-1][12] per step (node, left, right, forward slot of
  *          left / right / output, adjoint slot of input / left / right,
  *          the in-place adjoint's flags: carry or store each internal child
@@ -280,7 +287,8 @@ int tt_constant_coalescent(tt_time_tree *tree, int32_t batch,
  */
 int tt_plan_selftest_timeout(tt_plan *plan, uint64_t limit_ns, void *stream);
 
-/* Number of kernel launches the plan issued since creation. */
+/* Number of kernel launches the plan issued since creation (no reference
+ * counterpart). */
 int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
 
 /*
