@@ -296,3 +296,21 @@ def test_tip_partials_to_codes_fast_path_and_fallbacks(monkeypatch):
     many = [rng.random((4, 300)) for _ in range(2)]  # 600 distinct columns
     with pytest.raises(ValueError):
         patterns.from_tip_partials(many, np.ones(300))
+
+
+def test_every_header_entry_point_cites_what_it_replaces():
+    """Each function the C ABI declares sits under a comment that names the
+    reference code it replaces (file.py:line) or says that it has no
+    counterpart there; declarations grouped under one comment share it."""
+    text = "\n".join(p.read_text() for p in sorted((ROOT / "include").glob("*.h")))
+    last, prev_end, missing = "", 0, []
+    for m in re.finditer(r"\b(?:int|const char \*|void)\s+(tt_[a-z0-9_]+)\s*\(", text):
+        comments = re.findall(r"/\*(.*?)\*/", text[prev_end:m.start()], re.S)
+        if comments:
+            last = comments[-1]
+        prev_end = m.end()
+        if m.group(1) in ("tt_version", "tt_last_error"):
+            continue
+        if not (re.search(r"\.py:\d", last) or "counterpart" in last.lower()):
+            missing.append(m.group(1))
+    assert not missing, missing
