@@ -1,4 +1,10 @@
-"""FP64 CPU restatement of torchtree's likelihood path (oracle; tests only).
+"""FP64 CPU restatement of torchtree's likelihood path.
+
+TEST INFRASTRUCTURE ONLY: the checker of the GPU kernels in ``tests/`` and
+``__graft_entry__.smoke()``, and the timed CPU baseline of ``bench.py``;
+never imported by the package.  Pinned against the reference's golden
+vectors (``tests/golden/``) and, where its source is present, against the
+reference's own functions on random problems.
 
 Every function states the reference code it restates (paths inside the
 torchtree 1.0.2 project).  Tensors are torch CPU tensors; gradients come from

@@ -1,4 +1,8 @@
-"""Restatement of torchtree's data types and site-pattern compression (oracle; tests only).
+"""Restatement of torchtree's data types and site-pattern compression.
+
+TEST INFRASTRUCTURE ONLY (the checker of the package's compression; never
+imported by the package), pinned by the golden fixtures generated from the
+reference.
 
 Pure Python, written for small alignments.  Follows
 evolution/datatype.py:57-335 (state codes and tip partial vectors) and
