@@ -11,9 +11,14 @@ and frequencies, category rates/weights) for every sample.  One *evaluation*
 ranks.  Inputs stay resident in HBM; the stored partials (tens of GB) exceed
 the 129 MB L2, so no explicit L2 flush is used.
 
-``--impl reference`` times the CPU restatement of the reference path (the
-oracle port: torch CPU FP64 ops and autograd, all host threads) on a bounded
-pattern prefix of the same workload, scaled to the full pattern count.
+``--impl reference`` times the reference path on the host cores (all
+threads): torchtree's own ``p_t`` + ``calculate_treelikelihood_discrete_rescaled``
++ ``backward`` in FP64 (the copy installed in ``baseline/_ref``; the oracle
+port where torchtree cannot be imported).  A step is one sample's lnL and
+gradient over one pattern chunk; consecutive steps walk the chunks of the
+whole alignment in order, so every step is measured work of the same
+workload and nothing is extrapolated.  That arm loads nothing from this
+package's native library (the alignment is compressed with numpy).
 """
 from __future__ import annotations
 
@@ -47,7 +52,9 @@ def parse():
     ap.add_argument("--fp64-steps", type=int, default=2, help="steps of the FP64 drop-in comparison (0: skip)")
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--cpu-patterns", type=int, default=3000, help="pattern prefix of the CPU sample")
+    ap.add_argument("--ref-chunk-patterns", type=int, default=10240,
+                    help="patterns per chunk of the reference path on the CPU (one chunk per reference step; "
+                         "the CPU-baseline leg evaluates every chunk of sample 0)")
     ap.add_argument("--sites", type=int, default=None, help="override the workload's site count")
     ap.add_argument("--tips", type=int, default=None, help="override the workload's tip count")
     ap.add_argument("--batch", type=int, default=None, help="override the workload's batch")
@@ -160,14 +167,7 @@ def measured_tensor_peak():
 def workload(args):
     from torchtree_gb300 import datatype, patterns, synthetic
 
-    over = {}
-    if args.sites:
-        over["site_count"] = args.sites
-    if args.tips:
-        over["tip_count"] = args.tips
-    if args.batch:
-        over["batch"] = args.batch
-    wl = synthetic.named_workload(args.workload, **over)
+    wl = synthetic.named_workload(args.workload, **workload_overrides(args))
     ca = patterns.compress(wl.sequences, datatype.get(wl.data_type))
     return wl, ca
 
@@ -185,21 +185,19 @@ def rate_matrix(model, exch, pi):
     return substitution.mg94_q(torch.ones_like(exch[..., :1]), exch[..., 1:2], exch[..., :1], pi)
 
 
-def cpu_baseline(wl, ca, n_patterns, repeats=3):
-    from oracle import cpu_baseline as CB
-    from torchtree_gb300 import synthetic
+def cpu_baseline(wl, chunk_patterns):
+    """The reference path on the host cores: one whole evaluation (all
+    patterns, pattern chunk by pattern chunk) of sample 0, timed."""
+    from oracle import reference_arm as RA
 
-    rates = (synthetic.discrete_gamma_np(float(wl.shape[0, 0]), wl.categories) if wl.site_model == "gamma"
-             else synthetic.discrete_weibull_np(float(wl.shape[0, 0]), wl.categories))
-    d = CB.prepare(wl.topology.postorder, ca.codes, ca.table, ca.weights, wl.branch_lengths[0], wl.exch[0],
-                   wl.pi[0], rates, n_patterns, model=wl.model)
-    sec, threads, _ = CB.time_evaluations(d, repeats=repeats, warmup=1)
-    per_eval = sec * ca.pattern_count / d["n"]
-    return {"value": 1.0 / per_eval, "unit": UNIT, "cores": threads, "kind": "port",
-            "sample": (f"oracle port (torch CPU FP64 + autograd, rescaled) on the first {d['n']} of "
-                       f"{ca.pattern_count} patterns, 1 sample, median of {repeats}; seconds scaled "
-                       f"by N/{d['n']}"),
-            "seconds_per_sample_eval": per_eval}
+    ref = RA.ReferencePath(wl, chunk_patterns)
+    t0 = time.perf_counter()
+    lnl, grads = ref.evaluate(0)
+    sec = time.perf_counter() - t0
+    return {"value": 1.0 / sec, "unit": UNIT, "cores": ref.threads, "kind": ref.kind,
+            "sample": (f"{ref.describe()}; one whole evaluation (lnL + gradient) of sample 0 over all "
+                       f"{ref.N} patterns in {len(ref.chunks)} chunks, timed once"),
+            "seconds_per_eval": sec}, (lnl, grads, ref)
 
 
 def fp32_error(got, want):
@@ -215,38 +213,88 @@ def fp32_error(got, want):
     return out
 
 
+def workload_overrides(args):
+    over = {}
+    if args.sites:
+        over["site_count"] = args.sites
+    if args.tips:
+        over["tip_count"] = args.tips
+    if args.batch:
+        over["batch"] = args.batch
+    return over
+
+
+def bench_config(args, wl, n_patterns, sites, slab=None):
+    """The ``config`` object of both arms' lines (identical for the same workload)."""
+    S = wl.state_count
+    cfg = {"workload": args.workload, "tips": wl.topology.tip_count, "sites": int(sites),
+           "patterns": int(n_patterns), "batch": int(wl.branch_lengths.shape[0]), "categories": wl.categories,
+           "states": S,
+           "substitution_model": {"gtr": "GTR", "hky": "HKY", "general": "general symmetric 20-state",
+                                  "mg94": "MG94 codon (GY94-style)"}[wl.model] + f"+Gamma{wl.categories}",
+           "l2": "inputs (stored partials) larger than L2; no flush",
+           "parallelism": f"replicas x{args.gpus}"}
+    if slab:
+        cfg["slab_patterns"] = slab
+        cfg["slabs"] = ("partials held one pattern slab at a time; the pre_order_adjoint time includes the "
+                        "post-order recompute")
+    return cfg
+
+
+def reference_error(res, ref_lnl, ref_grads, n_free):
+    """A GPU result's sample 0 against the reference path's: lnL relative
+    error, and the branch-length and category-rate gradients' largest error
+    relative to their largest entry."""
+    lnl, _, dbl, dr = (x.double() for x in res)
+    g_bl, g_r = ref_grads[0], ref_grads[3]
+    return {"lnl_rel_err": float(abs(float(lnl[0]) - ref_lnl) / abs(ref_lnl)),
+            "dbranch_err_rel_to_max": float((dbl[0, :n_free] - g_bl).abs().max() / g_bl.abs().max()),
+            "drate_err_rel_to_max": float((dr[0] - g_r).abs().max() / g_r.abs().max())}
+
+
 def run_reference(args):
+    """The reference path on the host cores, timed step by step (rank 0 only)."""
     rank = int(os.environ.get("RANK", "0"))
     if rank != 0:
         return
-    wl, ca = workload(args)
-    from oracle import cpu_baseline as CB
+    from oracle import reference_arm as RA
     from torchtree_gb300 import synthetic
 
-    rates = synthetic.discrete_gamma_np(float(wl.shape[0, 0]), wl.categories)
-    d = CB.prepare(wl.topology.postorder, ca.codes, ca.table, ca.weights, wl.branch_lengths[0], wl.exch[0],
-                   wl.pi[0], rates, args.cpu_patterns, model=wl.model)
-    for _ in range(args.warmup):
-        CB.one_evaluation(d)
-    t0 = time.perf_counter()
-    for _ in range(args.steps):
-        CB.one_evaluation(d)
-    dt = (time.perf_counter() - t0) / args.steps
-    per_eval = dt * ca.pattern_count / d["n"]
-    value = 1.0 / per_eval
-    import torch
+    wl = synthetic.named_workload(args.workload, **workload_overrides(args))
+    ref = RA.ReferencePath(wl, args.ref_chunk_patterns)
+    b, nch = int(wl.branch_lengths.shape[0]), len(ref.chunks)
+    sizes = [hi - lo for lo, hi in ref.chunks]
 
+    def step(i):
+        c = i % nch
+        ref.evaluate_chunk((i // nch) % b, c)
+        return sizes[c]
+
+    for i in range(args.warmup):
+        step(i)
+    per, done = [], 0
+    t0 = time.perf_counter()
+    for i in range(args.steps):
+        t1 = time.perf_counter()
+        done += step(args.warmup + i)
+        per.append(time.perf_counter() - t1)
+    wall = time.perf_counter() - t0
+    value = done / ref.N / wall  # whole evaluations (lnL + gradient of one sample) per second
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
-        "warmup": args.warmup, "ms_per_step": per_eval * 1e3 * wl.branch_lengths.shape[0],
-        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
-        "data": "synthetic (seeded Yule tree + simulated alignment)", "impl": "reference",
-        "config": {"workload": args.workload, "tips": wl.topology.tip_count, "patterns": ca.pattern_count,
-                   "batch": int(wl.branch_lengths.shape[0])},
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": torch.get_num_threads(), "kind": "port",
-                         "sample": f"first {d['n']} of {ca.pattern_count} patterns per step, 1 sample, "
-                                   f"scaled by N/{d['n']}"},
+        "warmup": args.warmup, "ms_per_step": wall / args.steps * 1e3, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+        "data": f"synthetic (seeded Yule tree, alignment simulated under the model: {wl.data_type})",
+        "impl": "reference",
+        "config": bench_config(args, wl, ref.N, ref.sites),
+        "latency_ms": {"p50": float(np.percentile(per, 50)) * 1e3, "p99": float(np.percentile(per, 99)) * 1e3,
+                       "what": "one step: one sample's lnL + gradient over one pattern chunk"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": ref.threads, "kind": ref.kind,
+                         "sample": (f"{ref.describe()}; step = one sample over one chunk of <= "
+                                    f"{args.ref_chunk_patterns} of the {ref.N} patterns ({nch} chunks), "
+                                    f"steps walk the chunks in order ({done} pattern evaluations timed)")},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "setup_s": {"compress": ref.compress_s},
     }
     print(json.dumps(line), flush=True)
 
@@ -650,7 +698,7 @@ def main():
             roofline["traffic"] = tr
 
     # FP64 drop-in on the same workload; its results measure the FP32 error
-    fp64, accuracy = None, None
+    fp64, accuracy, got, want = None, None, None, None
     if args.fp64_steps > 0 and args.precision == "f32":
         got = [x.cpu() for x in step(eng)]
         del eng
@@ -704,7 +752,12 @@ def main():
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(wl, ca, args.cpu_patterns)
+        cpu, (ref_lnl, ref_grads, _) = cpu_baseline(wl, args.ref_chunk_patterns)
+        # the same evaluation through the GPU paths: sample 0 of the FP64 drop-in and of the timed precision
+        cpu["check"] = {"vs": "the reference path's sample 0 (whole alignment, FP64, CPU)"}
+        for name, res in (("fp64_dropin", want), (args.precision, got)):
+            if res is not None:
+                cpu["check"][name] = reference_error(res, ref_lnl, ref_grads, 2 * T - 3)
 
     if rank == 0:
         lat = sorted(per_step)
@@ -713,15 +766,7 @@ def main():
             "warmup": max(args.warmup, 3), "ms_per_step": total_ms / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": args.precision,
             "data": f"synthetic (seeded Yule tree, alignment simulated under the model: {wl.data_type})",
-            "config": {"workload": args.workload, "tips": T, "sites": int(sum(ca.weights)),
-                       "patterns": N, "batch": b, "categories": K, "states": S,
-                       "substitution_model": {"gtr": "GTR", "hky": "HKY", "general": "general symmetric 20-state",
-                                              "mg94": "MG94 codon (GY94-style)"}[wl.model] + f"+Gamma{K}",
-                       "l2": "inputs (stored partials) larger than L2; no flush",
-                       "parallelism": f"replicas x{world}",
-                       **({"slab_patterns": slab,
-                           "slabs": "partials held one pattern slab at a time; the pre_order_adjoint time "
-                                    "includes the post-order recompute"} if slab else {})},
+            "config": bench_config(args, wl, N, int(sum(ca.weights)), slab),
             "latency_ms": {"p50": float(np.percentile(lat, 50)), "p99": float(np.percentile(lat, 99)),
                            "what": "one batched lnL+gradient call (all samples)"},
             "fp64_dropin": fp64,

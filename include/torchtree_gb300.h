@@ -215,9 +215,14 @@ int tt_schedule(int32_t tip_count, const int32_t *postorder, int32_t *steps,
  *   [b][4], log_likelihood device double [b].
  * Scratch lives in one 8 MiB static device array held by every GPU that
  * loads the library; a problem needing more is rejected with
- * TT_ERR_INVALID_ARGUMENT.  The first call on a device looks the array up
- * (make it before any stream capture).  Calls share the array: calls that
- * overlap on the GPU race and must be serialised by the caller.
+ * TT_ERR_INVALID_ARGUMENT.  Every call looks the array's address up in the
+ * current context (the first call on a device loads the module).  A stream
+ * that is being captured is refused (TT_ERR_UNSUPPORTED): the schedule is
+ * copied from pageable host memory.  The call synchronises `stream` before
+ * it returns and reads the kernel's status word back; a bounded wait that
+ * gave up returns TT_ERR_DEVICE_TIMEOUT.  A tip code >= code_count gives a
+ * NaN log-likelihood for the samples it touches.  Calls share the array:
+ * calls that overlap on the GPU race and must be serialised by the caller.
  */
 int tt_log_likelihood_static(int32_t tip_count, const int32_t *postorder,
                              int32_t state_count, int32_t category_count,

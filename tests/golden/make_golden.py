@@ -5,7 +5,7 @@ is available):
 
     python tests/golden/make_golden.py /path/to/torchtree-source
 
-The reference imports dendropy at module load; ``_stub/dendropy.py`` stands
+The reference imports dendropy at module load; ``oracle/_stub/dendropy.py`` stands
 in for it (trees are never parsed through dendropy here: post-order triples
 come from this package's Newick parser or Yule generator and are handed to
 a minimal ``TreeModel``).  Every value written below is computed by the
@@ -28,7 +28,7 @@ REPO = HERE.parent.parent
 
 
 def _setup(ref_root: str):
-    sys.path.insert(0, str(HERE / "_stub"))
+    sys.path.insert(0, str(REPO / "oracle" / "_stub"))
     sys.path.insert(0, ref_root)
     sys.path.insert(0, str(REPO))
 

@@ -1,34 +1,27 @@
-"""Helpers for the tests that import torchtree from its source tree.
+"""Helpers for the tests that run torchtree itself.
 
-The source location is TORCHTREE_REFERENCE, else the default below; tests
-that need it are skipped where it is absent.  torchtree imports dendropy at
-module load; ``tests/golden/_stub/dendropy.py`` stands in for it (trees are
-never parsed through dendropy: post-order triples come from this package's
-Newick parser and are handed to ``fixed_tree_class()``).
+torchtree comes from ``TORCHTREE_REFERENCE`` (a source tree) or, failing
+that, from the unmodified copy installed in ``baseline/_ref``
+(``oracle/reference.py`` does the search; the installed copy has no
+``data/``).  Tests that need it are skipped where neither is present.
+torchtree imports dendropy at module load; ``oracle/_stub/dendropy.py``
+stands in for it (trees are never parsed through dendropy: post-order
+triples come from this package's Newick parser and are handed to
+``fixed_tree_class()``).
 """
 from __future__ import annotations
 
-import os
-import sys
 from pathlib import Path
 
+from oracle import reference as _reference
+
 ROOT = Path(__file__).resolve().parents[1]
-REFERENCE = Path(os.environ.get("TORCHTREE_REFERENCE", "/root/reference"))
-DATA = REFERENCE / "data"
+DATA = _reference.data_dir() or ROOT / "tests" / "_no_reference_data"
 
 
 def import_torchtree() -> bool:
-    """Put torchtree's source and the dendropy stub on the path; True when it imports."""
-    if not (REFERENCE / "torchtree").is_dir():
-        return False
-    for path in (str(ROOT / "tests" / "golden" / "_stub"), str(REFERENCE)):
-        if path not in sys.path:
-            sys.path.insert(0, path)
-    try:
-        import torchtree  # noqa: F401
-    except ImportError:
-        return False
-    return True
+    """Put torchtree and the dendropy stub on the path; True when it imports."""
+    return _reference.import_torchtree() is not None
 
 
 def fixed_tree_class():

@@ -12,11 +12,18 @@
 // file-scope __device__ array of kScratchBytes, which every GPU that loads
 // the library holds until the process exits.
 //
-// The first call on each device looks up the array's device address with
-// cudaGetSymbolAddress (this can load the module), so make that first call
-// before any stream capture.  All calls share the array and it keeps the
-// last call's contents; calls whose work overlaps on the GPU (two streams,
-// two host threads) race on it and must be serialised by the caller.
+// Every call looks up the array's device address on the current device with
+// cudaGetSymbolAddress (the first call on a device loads the module), so a
+// context that was torn down and rebuilt gets the array's new address.  The
+// host-side schedule is built in static host arrays, not on the caller's
+// stack, under one lock that serialises the host side of every call.  The
+// call refuses a stream that is being captured (its host-to-device copies
+// come from pageable memory), and it synchronises the stream before it
+// returns so that the kernel's status word is read back: a bounded wait that
+// gave up is returned as TT_ERR_DEVICE_TIMEOUT.  All calls share the array
+// and it keeps the last call's contents; calls whose work overlaps on the
+// GPU (two streams, two processes' worth of host threads bypassing the lock)
+// race on it and must be serialised by the caller.
 #include <cuda_runtime.h>
 
 #include <cstdio>
@@ -30,7 +37,6 @@ namespace {
 
 constexpr size_t kScratchBytes = size_t(8) << 20;  // 8 MiB of scratch
 constexpr int kMaxTips = 1024;
-constexpr int kMaxDevices = 64;
 constexpr int kTableRows = 256;  // codes are uint8: pad the table to every value
 
 }  // namespace
@@ -39,44 +45,52 @@ static __device__ __align__(256) unsigned char g_scratch[kScratchBytes];
 
 namespace {
 
+// Serialises the host side of every call: the static host arrays below and
+// the order of the copies into the shared device array.
 std::mutex g_scratch_lock;
-unsigned char *g_scratch_addr[kMaxDevices] = {};
 
 int fail(int code, const char *msg) { return tt::record_error(code, msg); }
 
-// Device address of g_scratch on the current device (looked up once per device).
+int fail_cuda(const char *what, cudaError_t e) {
+  char buf[240];
+  snprintf(buf, sizeof buf, "%s: %s", what, cudaGetErrorString(e));
+  return fail(TT_ERR_CUDA, buf);
+}
+
+// Device address of g_scratch in the current device's context, looked up on
+// every call (cheap once the module is loaded) so that it is never stale.
 int scratch_address(unsigned char **out) {
-  int dev = -1;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess) return fail(TT_ERR_CUDA, cudaGetErrorString(e));
-  if (dev < 0 || dev >= kMaxDevices) return fail(TT_ERR_UNSUPPORTED, "device index out of range");
-  std::lock_guard<std::mutex> guard(g_scratch_lock);
-  if (!g_scratch_addr[dev]) {
-    void *p = nullptr;
-    e = cudaGetSymbolAddress(&p, g_scratch);
-    if (e != cudaSuccess) {
-      char buf[200];
-      snprintf(buf, sizeof buf, "cudaGetSymbolAddress of the static scratch failed: %s",
-               cudaGetErrorString(e));
-      return fail(TT_ERR_CUDA, buf);
-    }
-    g_scratch_addr[dev] = static_cast<unsigned char *>(p);
-  }
-  *out = g_scratch_addr[dev];
+  void *p = nullptr;
+  const cudaError_t e = cudaGetSymbolAddress(&p, g_scratch);
+  if (e != cudaSuccess) return fail_cuda("cudaGetSymbolAddress of the static scratch failed", e);
+  *out = static_cast<unsigned char *>(p);
   return TT_OK;
 }
 
-size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
-
-// Post-order schedule with shared-memory slots (forward only), built in
-// fixed-size host arrays: the child whose subtree needs more slots is
-// evaluated first, so at most log2(T)+1 slots are live.
-int static_schedule(int T, const int32_t *post, int *steps, int *branch_pos, int *slots_out) {
-  const int I = T - 1, NN = 2 * T - 1;
+// Host working arrays of one call (about 120 KB), kept off the caller's stack:
+// plug-in hosts may run this on worker threads with small stacks.  Guarded by
+// g_scratch_lock.
+struct HostTables {
   int left[2 * kMaxTips], right[2 * kMaxTips], parent[2 * kMaxTips], need[2 * kMaxTips];
   int first[2 * kMaxTips], slot[2 * kMaxTips], order[kMaxTips];
   int stk_node[2 * kMaxTips];
   unsigned char stk_state[2 * kMaxTips], done[2 * kMaxTips];
+  int steps[(kMaxTips - 1) * tt::kStepInts];
+  int branch_pos[2 * kMaxTips - 2];
+};
+HostTables g_host;
+
+size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Post-order schedule with shared-memory slots (forward only), built in
+// the static host arrays: the child whose subtree needs more slots is
+// evaluated first, so at most log2(T)+1 slots are live.
+int static_schedule(int T, const int32_t *post, HostTables &h, int *slots_out) {
+  const int I = T - 1, NN = 2 * T - 1;
+  int *left = h.left, *right = h.right, *parent = h.parent, *need = h.need;
+  int *first = h.first, *slot = h.slot, *order = h.order, *stk_node = h.stk_node;
+  unsigned char *stk_state = h.stk_state, *done = h.done;
+  int *steps = h.steps, *branch_pos = h.branch_pos;
   for (int v = 0; v < NN; ++v) {
     left[v] = right[v] = parent[v] = first[v] = slot[v] = -1;
     need[v] = 0;
@@ -176,14 +190,24 @@ extern "C" int tt_log_likelihood_static(int32_t tip_count, const int32_t *postor
 
   const int T = tip_count, I = T - 1, B = 2 * T - 2, S = 4, K = category_count, N = pattern_count;
   const int kss = K * S * S;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  cudaStreamCaptureStatus capture = cudaStreamCaptureStatusNone;
+  cudaError_t e = cudaStreamIsCapturing(s, &capture);
+  if (e != cudaSuccess) return fail_cuda("cudaStreamIsCapturing failed", e);
+  if (capture != cudaStreamCaptureStatusNone)
+    return fail(TT_ERR_UNSUPPORTED,
+                "tt_log_likelihood_static must not be called on a capturing stream (its schedule is copied "
+                "from pageable host memory and its status is read back synchronously)");
   int smem_max = 0, dev = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return fail_cuda("cudaGetDevice failed", e);
+  e = cudaDeviceGetAttribute(&smem_max, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  if (e != cudaSuccess) return fail_cuda("cudaDeviceGetAttribute failed", e);
 
-  int steps[(kMaxTips - 1) * tt::kStepInts];
-  int branch_pos[2 * kMaxTips - 2];
+  std::lock_guard<std::mutex> guard(g_scratch_lock);
+  const int *steps = g_host.steps, *branch_pos = g_host.branch_pos;
   int slots = 0;
-  int rc = static_schedule(T, postorder, steps, branch_pos, &slots);
+  int rc = static_schedule(T, postorder, g_host, &slots);
   if (rc != TT_OK) return rc;
   int tile = 0;
   for (int t : tt::kFwdTilesF64)
@@ -226,12 +250,11 @@ extern "C" int tt_log_likelihood_static(int32_t tip_count, const int32_t *postor
   double *d_pmat = reinterpret_cast<double *>(scratch + o_pmat);
   double *d_tiles = reinterpret_cast<double *>(scratch + o_tiles);
   uint8_t *d_codes = scratch + o_codes;
-  cudaStream_t s = static_cast<cudaStream_t>(stream);
 
   // Start-of-call state: status cleared; table rows past code_count and the
   // tile sums set to NaN, so an out-of-range code or a CTA that gave up on a
   // bounded wait shows up as a NaN log-likelihood instead of stale data.
-  cudaError_t e = cudaMemsetAsync(d_status, 0, sizeof(int), s);
+  e = cudaMemsetAsync(d_status, 0, sizeof(int), s);
   if (e == cudaSuccess) e = cudaMemsetAsync(d_table, 0xff, size_t(kTableRows) * S * sizeof(double), s);
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(d_table, code_table, size_t(code_count) * S * sizeof(double), cudaMemcpyDeviceToDevice, s);
@@ -273,5 +296,14 @@ extern "C" int tt_log_likelihood_static(int32_t tip_count, const int32_t *postor
   e = tt::launch_prune_f64(a, false, tile, batch, s);
   if (e == cudaSuccess) e = tt::launch_reduce_lnl(d_tiles, log_likelihood, batch, ntiles, 0, s);
   if (e != cudaSuccess) return fail(TT_ERR_CUDA, cudaGetErrorString(e));
+  // read the status word back (this synchronises the stream)
+  int status = 0;
+  e = cudaMemcpyAsync(&status, d_status, sizeof(int), cudaMemcpyDeviceToHost, s);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return fail_cuda("reading the status word back failed", e);
+  if (status != TT_OK)
+    return fail(status == TT_ERR_DEVICE_TIMEOUT ? TT_ERR_DEVICE_TIMEOUT : TT_ERR_CUDA,
+                "tt_log_likelihood_static: a bounded wait in the kernel gave up (status word set); the "
+                "log-likelihoods are not valid");
   return TT_OK;
 }

@@ -17,7 +17,8 @@ reference.  ``*_rescaled`` and ``*_safe`` rescale every node by a power of
 two; the reference's ``_safe`` rescales only nodes below ``threshold`` after
 an underflow, and both give the same lnL up to rounding.  ``precision``
 selects FP64 (default, the drop-in) or rescaled FP32 partials.  The tip
-data stay resident on the device between calls with the same tensors.
+data stay resident on the device between calls with the same, unmodified
+tensors (an in-place change to a tip or weight tensor makes a new engine).
 """
 from __future__ import annotations
 
@@ -30,14 +31,32 @@ from . import patterns
 from .autograd import MatrixLikelihood
 from .engine import LikelihoodEngine
 
-_ENGINES: dict = {}
+_ENGINES: "OrderedDict" = None
+# Resident engines are kept for repeated calls on the same tip data, at most
+# _MAX_ENGINES of them and at most _MAX_CACHED_BYTES of device workspace in
+# total (least recently used first out).  An engine that alone exceeds the
+# byte budget is not cached at all.
+_MAX_ENGINES = 4
+_MAX_CACHED_BYTES = 8 << 30
+
+
+def _identity(t: torch.Tensor):
+    """Identity of a tensor's current contents: the object, its storage and
+    its version counter (bumped by every in-place change)."""
+    return (id(t), t.data_ptr(), t._version, tuple(t.shape), t.dtype)
 
 
 def _engine(tips, weights, post_indexing, S, K, batch, precision, tip_states):
-    key = (tuple(map(tuple, post_indexing)), tuple(id(t) for t in tips), id(weights), S, K, batch,
-           precision, tip_states)
+    global _ENGINES
+    from collections import OrderedDict
+
+    if _ENGINES is None:
+        _ENGINES = OrderedDict()
+    key = (tuple(map(tuple, post_indexing)), tuple(_identity(t) for t in tips), _identity(weights), S, K,
+           batch, precision, tip_states)
     hit = _ENGINES.get(key)
     if hit is not None:
+        _ENGINES.move_to_end(key)
         return hit[0]
     w = weights.detach().cpu().numpy()
     if tip_states:
@@ -47,14 +66,18 @@ def _engine(tips, weights, post_indexing, S, K, batch, precision, tip_states):
     device = None
     eng = LikelihoodEngine(np.asarray(post_indexing, dtype=np.int32), len(tips), S, K, ca.codes, ca.table,
                            w, batch=batch, precision=precision, device=device)
-    if len(_ENGINES) > 16:
-        _ENGINES.pop(next(iter(_ENGINES)))
-    _ENGINES[key] = (eng, tips, weights)  # keep the tensors alive so ids stay unique
+    size = eng.workspace_bytes
+    if size <= _MAX_CACHED_BYTES:
+        while _ENGINES and (len(_ENGINES) >= _MAX_ENGINES or
+                            sum(v[0].workspace_bytes for v in _ENGINES.values()) + size > _MAX_CACHED_BYTES):
+            _ENGINES.popitem(last=False)  # freed once no autograd graph holds it
+        _ENGINES[key] = (eng, tips, weights)  # keep the tensors alive so that ids stay unique
     return eng
 
 
 def clear_cache() -> None:
-    _ENGINES.clear()
+    if _ENGINES is not None:
+        _ENGINES.clear()
 
 
 def _run(partials, weights, post_indexing, mats, freqs, props, rescale, precision, tip_states):
