@@ -3,10 +3,12 @@
 
 Workload (default ``gtr_g4_t1000_b8``): GTR+Gamma4 on a 1,000-taxon Yule tree
 with 100,000 simulated DNA sites (compressed to N unique patterns), a batch of
-8 branch-length samples.  One *step* = one batched evaluation: transition
-matrices, post-order pass, pre-order adjoint pass and all reductions, giving
-lnL and the full gradient (branch lengths, eigen system -> exchangeabilities
-and frequencies, category rates/weights) for every sample.  One *evaluation*
+8 branch-length samples.  One *step* = one batched evaluation: the model
+set-up (Gamma category rates by the quantile kernel, the normalised rate
+matrix, its FP64 eigen system by the Jacobi kernel), transition matrices,
+post-order pass, pre-order adjoint pass and all reductions, giving lnL and
+the full gradient (branch lengths, rate matrix -> exchangeabilities and
+frequencies, category rates/weights) for every sample.  One *evaluation*
 = lnL + gradient for one sample; ``value`` = evaluations / second over all
 ranks.  Inputs stay resident in HBM; the stored partials (tens of GB) exceed
 the 129 MB L2, so no explicit L2 flush is used.
@@ -239,6 +241,71 @@ def bench_config(args, wl, n_patterns, sites, slab=None):
         cfg["slabs"] = ("partials held one pattern slab at a time; the pre_order_adjoint time includes the "
                         "post-order recompute")
     return cfg
+
+
+def plugin_e2e(args, wl, dev, steps):
+    """lnL + gradient through the torchtree plug-in class, as a torchtree user
+    calls it: ``torchtree_gb300.TreeLikelihoodModel`` built by torchtree's JSON
+    machinery over torchtree's GTR / HKY model, this package's GammaSiteModel
+    and a fixed-topology tree model, parameters as CPU tensors (the class
+    copies them to the device, runs the engine and returns lnL to the host;
+    ``backward`` brings the gradients back).  None when torchtree cannot be
+    imported or the model is not GTR / HKY."""
+    import torch
+
+    from oracle import reference as R
+    from oracle import reference_arm as RA
+
+    if wl.model not in ("gtr", "hky") or R.import_torchtree() is None:
+        return None
+    from torchtree import Parameter
+    from torchtree.core.utils import process_object
+    from torchtree.evolution.substitution_model import GTR, HKY
+
+    from torchtree_gb300.model import GammaSiteModel  # noqa: F401  (registers the class)
+
+    tips, weights = RA.compress(wl.sequences, wl.data_type)
+    names = wl.topology.tip_names
+    leaf = lambda a: torch.tensor(np.asarray(a), dtype=torch.float64).requires_grad_()  # noqa: E731
+    p_bl, p_pi, p_shape = Parameter("bl", leaf(wl.branch_lengths)), Parameter("pi", leaf(wl.pi)), \
+        Parameter("shape", leaf(wl.shape))
+    if wl.model == "hky":
+        p_ex = Parameter("kappa", leaf(wl.exch[:, 1:2]))
+        subst = HKY("subst", p_ex, p_pi)
+    else:
+        p_ex = Parameter("exch", leaf(wl.exch))
+        subst = GTR("subst", p_ex, p_pi)
+    dic = {"tree": R.fixed_tree_class()(wl.topology.postorder, names, p_bl), "subst": subst,
+           "sp": R.PatternSource(tips, weights)}
+    dic["site"] = process_object({"id": "site", "type": "torchtree_gb300.GammaSiteModel", "shape": "shape",
+                                  "categories": wl.categories}, dict(dic, shape=p_shape))
+    like = process_object({"id": "like", "type": "torchtree_gb300.TreeLikelihoodModel", "tree_model": "tree",
+                           "site_model": "site", "substitution_model": "subst", "site_pattern": "sp",
+                           "precision": args.precision}, dic)
+    like.rescale = True
+    params = (p_bl, p_ex, p_pi, p_shape)
+    hosts = [p.tensor.detach().clone() for p in params]
+
+    def one():
+        for p, h in zip(params, hosts):  # new parameter values: listeners invalidate the cached lnL
+            p.tensor = h.clone().requires_grad_()
+        lnl = like()
+        lnl.sum().backward()
+        return sum(p.tensor.grad.numel() * 8 for p in params) + lnl.numel() * 8
+
+    for _ in range(2):
+        one()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(steps):
+        d2h = one()
+    torch.cuda.synchronize()
+    sec = time.perf_counter() - t0
+    b = int(wl.branch_lengths.shape[0])
+    return {"value": b * steps / sec, "unit": UNIT, "h2d_bytes_per_step": int(sum(h.numel() * 8 for h in hosts)),
+            "d2h_bytes_per_step": int(d2h),
+            "what": "torchtree_gb300.TreeLikelihoodModel from JSON (torchtree GTR/HKY, GammaSiteModel, CPU "
+                    "parameters) called and back-propagated like the reference class"}
 
 
 def reference_error(res, ref_lnl, ref_grads, n_free):
@@ -580,14 +647,19 @@ def main():
     b = int(wl.branch_lengths.shape[0])
     T, N, K, S = wl.topology.tip_count, ca.pattern_count, wl.categories, ca.table.shape[1]
     bl, exch, pi, shape = batch_inputs(wl, dev)
-    rates, probs = site_models.gamma_rates(shape, K)
-    probs = probs.expand(b, K).contiguous()
-    # resident inputs of the timed step: the eigen system is set-up work (host LAPACK)
-    q = rate_matrix(wl.model, exch.cpu(), pi.cpu())
-    lam, u, w = (t.detach().to(dev).contiguous() for t in substitution.eigen_system(q, pi.cpu()))
     zeros = torch.zeros(b, 1, dtype=torch.float64, device=dev)
     bls = torch.cat([bl, zeros], -1).contiguous()
-    rates = rates.detach().contiguous()
+
+    def model_setup():
+        """The per-step model work on the device: Gamma category rates
+        (quantile kernel), the normalised rate matrix (a few torch ops) and
+        its FP64 eigen system (Jacobi kernel)."""
+        r, p = site_models.gamma_rates(shape, K)
+        qn = substitution.normalise(rate_matrix(wl.model, exch, pi), pi)
+        lam_, u_, w_ = substitution.device_eigen(qn, pi)
+        return lam_, u_, w_, r.contiguous(), p.expand(b, K).contiguous()
+
+    lam, u, w, rates, probs = model_setup()
 
     def make_engine(precision):
         return LikelihoodEngine(wl.topology.postorder, T, S, K, ca.codes, ca.table, ca.weights, batch=b,
@@ -600,10 +672,11 @@ def main():
     stream = torch.cuda.current_stream()
 
     def step(e):
-        e.set_eigen(lam, u, w, bls, rates)
-        lnl = e.log_likelihood(probs, pi, rescale=True, keep_partials=True)
-        e.gradient(probs, pi)
-        return (lnl,) + e.rate_matrix_gradient(lam, u, w, bls, rates)
+        lam_, u_, w_, r_, p_ = model_setup()
+        e.set_eigen(lam_, u_, w_, bls, r_)
+        lnl = e.log_likelihood(p_, pi, rescale=True, keep_partials=True)
+        e.gradient(p_, pi)
+        return (lnl,) + e.rate_matrix_gradient(lam_, u_, w_, bls, r_)
 
     for _ in range(max(args.warmup, 3)):
         step(eng)
@@ -620,7 +693,7 @@ def main():
             ev[i + 1].record(stream)
         torch.cuda.synchronize()
     barrier()
-    launches = eng.launch_count - launches0
+    launches = eng.launch_count - launches0 + 2 * args.steps  # + the quantile and eigen kernels
     per_step = [ev[i].elapsed_time(ev[i + 1]) for i in range(args.steps)]
     slowest_s, value = replica_throughput(ev[0].elapsed_time(ev[-1]) / 1e3, b * args.steps, world, dev)
     total_ms = slowest_s * 1e3
@@ -749,6 +822,9 @@ def main():
         _, e2e_value = replica_throughput(time.perf_counter() - t0, b * args.steps, world, dev)
         e2e = {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h}
         del lik
+        torch.cuda.empty_cache()
+        if world == 1:
+            e2e["plugin"] = plugin_e2e(args, wl, dev, args.steps)
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:

@@ -202,6 +202,40 @@ int tt_schedule(int32_t tip_count, const int32_t *postorder, int32_t *steps,
                 int32_t *slot_counts);
 
 /*
+ * Eigen system of reversible rate matrices on the device, FP64.  Replaces
+ * the eigendecomposition inside SymmetricSubstitutionModel.p_t
+ * (torchtree/evolution/substitution_model/abstract.py:57-79: Q normalised,
+ * symmetrised with Pi^1/2, eigh).
+ *   q: device double [b][S][S], normalised rate matrices (rows sum to 0,
+ *      reversible with respect to `frequencies`); only the lower triangle of
+ *      Pi^1/2 Q Pi^-1/2 is read, as eigh does;
+ *   frequencies: device double [b][S];
+ *   eigenvalues [b][S] (ascending), u [b][S][S], w [b][S][S] with
+ *   Q = U diag(eigenvalues) W and W = U^-1 (device);
+ *   status: device int32, set to TT_ERR_UNSUPPORTED if a matrix did not
+ *   converge (never cleared here).
+ * 1 <= S <= 64.  Cyclic Jacobi, one CTA per matrix.
+ */
+int tt_reversible_eigen(int32_t batch, int32_t state_count, const double *q,
+                        const double *frequencies, double *eigenvalues,
+                        double *u, double *w, int32_t *status, void *stream);
+
+/*
+ * Quantiles of the Gamma(shape, rate 1) distribution at (2k+1)/(2K),
+ * k = 0..K-1, and their derivative with respect to the shape (FP64,
+ * analytic).  The discretised Gamma site model's rates are x_k / mean(x)
+ * (the quantile construction of site_model.py:173-195; torchtree itself
+ * ships no Gamma model).  shape [b], x [b][K], dx_dshape [b][K].
+ * tt_gamma_quantiles takes device pointers and writes NaN where the shape is
+ * not finite and positive; tt_gamma_quantiles_host takes host pointers and
+ * returns TT_ERR_INVALID_ARGUMENT instead.
+ */
+int tt_gamma_quantiles(int32_t batch, int32_t category_count, const double *shape,
+                       double *x, double *dx_dshape, void *stream);
+int tt_gamma_quantiles_host(int32_t batch, int32_t category_count,
+                            const double *shape, double *x, double *dx_dshape);
+
+/*
  * FP64 log-likelihood that allocates no device memory.  No counterpart in
  * the reference: it exists for callers that cannot call cudaMalloc (an
  * application whose own memory manager owns every device byte, or a host

@@ -70,3 +70,63 @@ def describe() -> str:
     if root is None:
         return "absent"
     return "source tree (TORCHTREE_REFERENCE)" if root == source_root() else "installed copy (baseline/_ref)"
+
+
+def fixed_tree_class():
+    """A minimal torchtree ``TreeModel``: fixed post-order, branch lengths from a Parameter."""
+    from torchtree.evolution.tree_model import TreeModel
+
+    class FixedTree(TreeModel):
+        def __init__(self, post, names, bl):
+            super().__init__(None)
+            self._post = [list(map(int, t)) for t in post]
+            self._names = list(names)
+            self._bl = bl
+            self.taxa_count = len(names)
+
+        def branch_lengths(self):
+            return self._bl.tensor
+
+        @property
+        def postorder(self):
+            return self._post
+
+        @property
+        def taxa(self):
+            return self._names
+
+        def write_newick(self, stream, **kwargs):
+            stream.write("();")
+
+        def _sample_shape(self):
+            return self._bl.tensor.shape[:-1]
+
+        def handle_model_changed(self, model, obj, index):
+            pass
+
+        def handle_parameter_changed(self, variable, index, event):
+            self.fire_model_changed()
+
+        @classmethod
+        def from_json(cls, data, dic):
+            raise NotImplementedError
+
+    return FixedTree
+
+
+class PatternSource:
+    """Stands in for torchtree's ``SitePattern`` where its pure-Python
+    compression would take minutes (a 1,000 x 100,000 alignment): it hands
+    ``TreeLikelihoodModel`` the tip partials and weights of the numpy
+    compression in ``oracle/reference_arm.py`` (same pattern order and
+    values as ``compress_alignment(..., use_ambiguities=False)``,
+    site_pattern.py:100-124)."""
+
+    def __init__(self, tips, weights):
+        import torch
+
+        self._tips = [torch.from_numpy(t) for t in tips]
+        self._weights = torch.from_numpy(weights)
+
+    def compute_tips_partials(self, use_ambiguities=False):
+        return list(self._tips), self._weights

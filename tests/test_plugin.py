@@ -15,7 +15,7 @@ import numpy as np
 import pytest
 import torch
 
-from tests.reference_models import fixed_tree_class, import_torchtree
+from tests.reference_models import fixed_tree_class, import_torchtree, reference_objects as _models
 
 
 
@@ -77,57 +77,6 @@ def _oracle_lnl(route, tensors, topo, alignment, rescale):
     fn = OL.treelikelihood_discrete_rescaled if rescale else OL.treelikelihood_discrete
     return fn(parts, torch.tensor(alignment.weights, dtype=torch.float64), topo.postorder_list(), mats,
               freqs.unsqueeze(-2), probs[..., None, None]).reshape(-1)
-
-
-def _models(case, wl, b):
-    """Reference-side objects of one case: (tree, site pattern, subst, site, clock, tip_states)."""
-    from torchtree import Parameter
-    from torchtree.evolution.alignment import Alignment, Sequence
-    from torchtree.evolution.branch_model import StrictClockModel
-    from torchtree.evolution.datatype import NucleotideDataType
-    from torchtree.evolution.site_model import ConstantSiteModel, WeibullSiteModel
-    from torchtree.evolution.site_pattern import SitePattern
-    from torchtree.evolution.substitution_model import GTR, HKY, JC69
-    from torchtree.evolution.taxa import Taxa, Taxon
-
-    names = wl.topology.tip_names
-    taxa = Taxa(None, [Taxon(n, {}) for n in names])
-    aln = Alignment(None, [Sequence(n, s) for n, s in zip(names, wl.sequences)], taxa, NucleotideDataType(None))
-    sp = SitePattern(None, aln)
-    T = wl.topology.tip_count
-    leaf = lambda a: torch.tensor(np.asarray(a), dtype=torch.float64, requires_grad=True)  # noqa: E731
-    bl = torch.tensor(wl.branch_lengths[:b])
-    clock = None
-    if case == "hky_weibull_clock":  # rooted time lengths (2T-2) times a strict clock
-        bl = leaf(torch.cat((bl, torch.full((b, 1), 0.02)), -1).numpy() * 10.0)
-        rate = leaf(np.full((b, 1), 0.1))
-        tree = fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
-        clock = StrictClockModel(None, Parameter(None, rate), tree)
-        leaves = [bl, rate]
-    else:
-        bl = leaf(bl.numpy())
-        tree = fixed_tree_class()(wl.topology.postorder, names, Parameter(None, bl))
-        leaves = [bl]
-    pi_t = leaf(wl.pi[:b])
-    pi = Parameter(None, pi_t)
-    if case.startswith("gtr"):
-        ex = leaf(wl.exch[:b])
-        subst = GTR(None, Parameter(None, ex), pi)
-        leaves += [ex, pi_t]
-    elif case.startswith("hky"):
-        kappa = leaf(wl.exch[:b, 1:2])
-        subst = HKY(None, Parameter(None, kappa), pi)
-        leaves += [kappa, pi_t]
-    else:
-        subst = JC69(None)
-    if "weibull" in case:
-        shape = leaf(wl.shape[:b])
-        site = WeibullSiteModel(None, Parameter(None, shape), 4)
-        leaves.append(shape)
-    else:
-        site = ConstantSiteModel(None)
-    assert T == len(names)
-    return tree, sp, subst, site, clock, case.endswith("tipstates"), leaves
 
 
 @pytest.mark.parametrize("case,b", [("gtr_weibull", 1), ("gtr_weibull", 2), ("jc69_constant", 1),
@@ -598,3 +547,31 @@ def test_site_models_match_torchtree(torchtree_ref, seed):
     r2, p2 = site_models.invariant_rates(p, mu=torch.tensor(mu_v) if mu_v is not None else None)
     np.testing.assert_allclose(r2.numpy(), inv_ref.rates().numpy(), rtol=1e-14)
     np.testing.assert_allclose(p2.numpy(), inv_ref.probabilities().numpy(), rtol=1e-14)
+
+
+def test_gamma_site_model_from_json(torchtree_ref):
+    """``torchtree_gb300.GammaSiteModel`` resolves by its dotted path and gives
+    the package's Gamma rates (plain, with invariant sites and mu, batched),
+    with the shape gradient flowing into the torchtree Parameter."""
+    from torchtree import Parameter
+    from torchtree.core.utils import process_object
+
+    from torchtree_gb300 import site_models
+    from torchtree_gb300.model import GammaSiteModel
+
+    shape = torch.tensor([[0.3], [1.7]], dtype=torch.float64, requires_grad=True)
+    inv = torch.tensor([[0.1], [0.25]], dtype=torch.float64, requires_grad=True)
+    mu = torch.tensor([[1.5], [0.5]], dtype=torch.float64)
+    dic = {"shape": Parameter("shape", shape), "inv": Parameter("inv", inv), "mu": Parameter("mu", mu)}
+    for extra in ({}, {"invariant": "inv", "mu": "mu"}):
+        site = process_object({"id": "sm", "type": "torchtree_gb300.GammaSiteModel", "shape": "shape",
+                               "categories": 4, **extra}, dic)
+        assert isinstance(site, GammaSiteModel)
+        want_r, want_p = site_models.gamma_rates(shape, 4, inv if extra else None, mu if extra else None)
+        np.testing.assert_allclose(site.rates().detach().numpy(), want_r.detach().numpy(), rtol=1e-14)
+        got_p = site.probabilities().detach().numpy()  # [K] without invariant sites, as torchtree keeps it
+        np.testing.assert_allclose(np.broadcast_to(got_p, want_p.shape), want_p.detach().numpy(), rtol=1e-14)
+        (g,) = torch.autograd.grad(site.rates()[:, -1].sum(), shape)
+        (gw,) = torch.autograd.grad(want_r[:, -1].sum(), shape)
+        np.testing.assert_allclose(g.numpy(), gw.numpy(), rtol=1e-12)
+        dic.pop("sm")

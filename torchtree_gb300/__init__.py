@@ -7,7 +7,8 @@ and host utilities (``tree``, ``patterns``, ``datatype``, ``substitution``,
 ``site_models``, ``synthetic``).
 
 With torchtree installed, ``torchtree_gb300.TreeLikelihoodModel`` is the
-JSON-configurable plug-in class and ``__plugin__`` names the CLI plug-in.
+JSON-configurable plug-in class, ``torchtree_gb300.GammaSiteModel`` a
+discretised Gamma site model for it, and ``__plugin__`` names the CLI plug-in.
 """
 from __future__ import annotations
 
@@ -18,10 +19,10 @@ from . import datatype, patterns, site_models, substitution, synthetic, tree  # 
 
 
 def __getattr__(name):
-    if name == "TreeLikelihoodModel":
-        from .model import TreeLikelihoodModel
+    if name in ("TreeLikelihoodModel", "GammaSiteModel"):
+        from . import model
 
-        return TreeLikelihoodModel
+        return getattr(model, name)
     if name in ("LikelihoodEngine",):
         from .engine import LikelihoodEngine
 

@@ -55,6 +55,9 @@ SIGNATURES = {
     "tt_constant_coalescent": (ctypes.c_int, [_P, _I32, _P, _P, _P, _P, _P, _P]),
     "tt_compress_columns": (ctypes.c_int, [_P, ctypes.c_int64, ctypes.c_int64, _P, _P, _P, _P]),
     "tt_plan_get_option": (ctypes.c_int, [_P, _I32, _PI32]),
+    "tt_reversible_eigen": (ctypes.c_int, [_I32, _I32, _P, _P, _P, _P, _P, _P, _P]),
+    "tt_gamma_quantiles": (ctypes.c_int, [_I32, _I32, _P, _P, _P, _P]),
+    "tt_gamma_quantiles_host": (ctypes.c_int, [_I32, _I32, _P, _P, _P]),
     "tt_log_likelihood_static": (ctypes.c_int, [_I32, _PI32, _I32, _I32, _I32, _I32, _P, _P, _I32, _P, _P, _P,
                                                 _P, _I32, _P, _P]),
 }
@@ -109,6 +112,11 @@ def schedule(tip_count: int, postorder):
     check(lib.tt_schedule(int(tip_count), post.ctypes.data_as(p32), steps.ctypes.data_as(p32),
                           slots.ctypes.data_as(p32)))
     return steps, (int(slots[0]), int(slots[1]))
+
+
+def ptr_value(address: int) -> ctypes.c_void_p:
+    """A raw address (e.g. a cudaStream_t from torch) as a C pointer."""
+    return ctypes.c_void_p(int(address))
 
 
 def ptr(t) -> ctypes.c_void_p:

@@ -12,7 +12,7 @@ from __future__ import annotations
 
 import torch
 
-from .substitution import eigen_of_normalised
+from .substitution import device_eigen, eigen_of_normalised
 
 
 def _scale(g: torch.Tensor, x: torch.Tensor, like: torch.Tensor) -> torch.Tensor:
@@ -51,14 +51,18 @@ class EigenLikelihood(torch.autograd.Function):
 class RateMatrixLikelihood(torch.autograd.Function):
     """lnL ``[b]`` from the normalised rate matrix ``q [b,S,S]`` (stationary
     distribution ``pi_q``), node branch lengths, category rates/weights and
-    root frequencies.  The eigen system is formed here without autograd; the
+    root frequencies.  The eigen system is formed here without autograd (on
+    the device, by the engine's Jacobi kernel, for CUDA tensors); the
     backward returns dlnL/dQ from the derivative of the matrix exponential in
     the eigenbasis (``tt_rate_matrix_gradient``), so no eigenvector
     derivative enters the chain to the rate-matrix parameters."""
 
     @staticmethod
     def forward(ctx, q, pi_q, bls, rates, props, freqs, engine, rescale):
-        lam, u, w = eigen_of_normalised(q.detach().cpu(), pi_q.detach().cpu())
+        if q.is_cuda:
+            lam, u, w = device_eigen(q, pi_q)
+        else:
+            lam, u, w = eigen_of_normalised(q.detach(), pi_q.detach())
         lam, u, w = (t.to(q.device).contiguous() for t in (lam, u, w))
         engine.set_eigen(lam, u, w, bls, rates)
         keep = any(ctx.needs_input_grad[:6])

@@ -19,9 +19,9 @@ from __future__ import annotations
 import math
 
 import torch
-from torchtree.core.utils import process_object, register_class
+from torchtree.core.utils import process_object, process_object_with_key, register_class
 from torchtree.evolution.branch_model import BranchModel
-from torchtree.evolution.site_model import SiteModel
+from torchtree.evolution.site_model import SiteModel, UnivariateDiscretizedSiteModel
 from torchtree.evolution.site_pattern import SitePattern
 from torchtree.evolution.substitution_model.abstract import (
     SubstitutionModel,
@@ -33,6 +33,7 @@ from torchtree.evolution.tree_model import TreeModel
 from . import patterns
 from .autograd import MatrixLikelihood, RateMatrixLikelihood
 from .engine import LikelihoodEngine
+from .site_models import _GammaQuantile
 from .substitution import normalise
 
 
@@ -154,3 +155,37 @@ class TreeLikelihoodModel(_ReferenceModel):
         return cls(data["id"], site_pattern, tree_model, subst_model, site_model, clock_model,
                    data.get("use_ambiguities", False), data.get("use_tip_states", False),
                    data.get("precision", "f64"))
+
+
+@register_class
+class GammaSiteModel(UnivariateDiscretizedSiteModel):
+    """Discretised Gamma(shape, rate = shape) rate heterogeneity.
+
+    torchtree 1.0.2 ships only constant, proportion-invariant and discretised
+    Weibull models (site_model.py:37-256).  This one is built exactly like
+    ``WeibullSiteModel`` (categories at the quantiles (2i+1)/(2K), rates
+    divided by their mean, optional invariant proportion and ``mu``;
+    site_model.py:173-195, 223-256) with the Gamma quantile in place of the
+    Weibull one.  The quantiles and their analytic shape derivative come from
+    the engine (``tt_gamma_quantiles``).  JSON:
+    ``{"type": "torchtree_gb300.GammaSiteModel", "shape": ..., "categories": K,
+    ["invariant": ...], ["mu": ...]}``.
+    """
+
+    @property
+    def shape(self) -> torch.Tensor:
+        return self._parameter.tensor
+
+    def inverse_cdf(self, parameter, quantile, invariant):
+        x = _GammaQuantile.apply(parameter, quantile.shape[-1])
+        if invariant is not None:
+            return torch.cat((torch.zeros_like(invariant), x), dim=-1)
+        return x
+
+    @classmethod
+    def from_json(cls, data, dic):
+        shape = process_object(data["shape"], dic)
+        invariant = process_object_with_key("invariant", data, dic)
+        mu = process_object_with_key("mu", data, dic)
+        return cls(data["id"], shape, data["categories"], invariant, mu)
+

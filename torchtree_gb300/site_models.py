@@ -4,13 +4,13 @@
 (torchtree/evolution/site_model.py:173-195, 237-247).  ``gamma_rates`` is
 the discretised Gamma(shape, rate=shape) model, which torchtree 1.0.2 does
 not ship: it uses the same (2i+1)/(2K) quantiles and mean-one
-normalisation, scipy's ``gammaincinv`` for the quantiles, and implicit
-differentiation for the shape gradient (checked against central finite
-differences in the tests).
+normalisation.  The quantiles and their analytic shape derivative come from
+the engine (``tt_gamma_quantiles``: on the device for CUDA tensors, so no
+host round trip enters a step; the same code on the host for CPU tensors);
+the tests check them against scipy's ``gammaincinv`` and finite differences.
 """
 from __future__ import annotations
 
-import numpy as np
 import torch
 
 
@@ -39,22 +39,35 @@ def weibull_rates(shape: torch.Tensor, categories: int, invariant=None, mu=None)
 
 
 class _GammaQuantile(torch.autograd.Function):
-    """x(alpha) / alpha with x = inverse regularised lower incomplete gamma."""
+    """x(alpha) / alpha, x the Gamma(alpha, 1) quantile at each of the K
+    quantile levels (2k+1)/(2K), with the analytic shape derivative.  Both
+    come from the engine (``tt_gamma_quantiles`` on the device,
+    ``tt_gamma_quantiles_host`` for CPU tensors): Halley's method on the
+    regularised incomplete gamma series, dx/dalpha by differentiating the
+    series term by term.  ``alpha [..., 1]`` -> ``[..., K]``."""
 
     @staticmethod
-    def forward(ctx, alpha, q):
-        from scipy.special import gammainc, gammaincinv, gammaln
+    def forward(ctx, alpha, categories):
+        from . import _native
 
-        a = alpha.detach().cpu().double().numpy()
-        qq = q.detach().cpu().double().numpy()
-        x = gammaincinv(a, qq)
-        h = 1e-6 * np.maximum(a, 1e-3)
-        dpda = (gammainc(a + h, x) - gammainc(a - h, x)) / (2 * h)
-        dpdx = np.exp((a - 1.0) * np.log(x) - x - gammaln(a))
-        dxda = -dpda / dpdx
-        drda = dxda / a - x / (a * a)
-        ctx.save_for_backward(torch.as_tensor(drda, dtype=alpha.dtype, device=alpha.device))
-        return torch.as_tensor(x / a, dtype=alpha.dtype, device=alpha.device)
+        lib = _native.load()
+        a = alpha.detach().to(torch.float64).reshape(-1).contiguous()
+        b = a.shape[0]
+        x = torch.empty(b, categories, dtype=torch.float64, device=alpha.device)
+        dx = torch.empty_like(x)
+        if alpha.is_cuda:
+            with torch.cuda.device(alpha.device):
+                stream = torch.cuda.current_stream(alpha.device).cuda_stream
+                _native.check(lib.tt_gamma_quantiles(b, categories, _native.ptr(a), _native.ptr(x), _native.ptr(dx),
+                                                     _native.ptr_value(stream)))
+        else:
+            _native.check(lib.tt_gamma_quantiles_host(b, categories, _native.ptr(a), _native.ptr(x),
+                                                      _native.ptr(dx)))
+        a1 = a.unsqueeze(-1)
+        shape = alpha.shape[:-1] + (categories,)
+        drda = (dx / a1 - x / (a1 * a1)).reshape(shape).to(alpha.dtype)
+        ctx.save_for_backward(drda)
+        return (x / a1).reshape(shape).to(alpha.dtype)
 
     @staticmethod
     def backward(ctx, grad):
@@ -64,8 +77,7 @@ class _GammaQuantile(torch.autograd.Function):
 
 def gamma_rates(shape: torch.Tensor, categories: int, invariant=None, mu=None):
     """Discretised Gamma rates; ``shape [...,1]`` (not in the reference)."""
-    q = _quantiles(categories, shape.dtype, shape.device)
-    rates = _GammaQuantile.apply(shape, q)
+    rates = _GammaQuantile.apply(shape, categories)
     return _finish(rates, categories, invariant, mu)
 
 

@@ -4,10 +4,13 @@ The pruning engine consumes ``(lambda, U, W)`` with
 ``Q = U diag(lambda) W`` for the normalised rate matrix, exactly the
 factorisation of torchtree's ``SymmetricSubstitutionModel.p_t``
 (torchtree/evolution/substitution_model/abstract.py:57-76): symmetrise with
-Pi^1/2, ``eigh``, ``U = Pi^-1/2 V``, ``W = V^-1 Pi^1/2``.  These few small
-ops stay in torch so that autograd carries the engine's gradients back to
-exchangeabilities and frequencies; the eigendecomposition runs on the GPU
-in FP64.
+Pi^1/2, ``eigh``, ``U = Pi^-1/2 V``, ``W = V^-1 Pi^1/2``.  The rate-matrix
+builders stay in torch so that autograd carries the engine's gradients back
+to exchangeabilities and frequencies.  The eigendecomposition of device
+tensors runs in the engine's FP64 Jacobi kernel (``tt_reversible_eigen``)
+whenever no gradient has to flow through it, as in the rate-matrix route,
+whose backward needs no eigenvector derivative; otherwise ``torch.linalg.eigh``
+keeps the autograd graph.
 """
 from __future__ import annotations
 
@@ -27,8 +30,35 @@ def eigen_system(q_unnorm: torch.Tensor, pi: torch.Tensor):
     return eigen_of_normalised(normalise(q_unnorm, pi), pi)
 
 
+def device_eigen(q: torch.Tensor, pi: torch.Tensor):
+    """``(lambda, U, W)`` of normalised reversible ``q [b,S,S]`` (CUDA, FP64)
+    by the engine's Jacobi kernel; no autograd graph."""
+    from . import _native
+
+    lib = _native.load()
+    q = q.detach().to(torch.float64).contiguous()
+    pi = pi.detach().to(torch.float64).expand(q.shape[:-1]).contiguous()
+    b, S = q.shape[0], q.shape[-1]
+    lam = torch.empty(b, S, dtype=torch.float64, device=q.device)
+    u = torch.empty(b, S, S, dtype=torch.float64, device=q.device)
+    w = torch.empty_like(u)
+    status = torch.zeros(1, dtype=torch.int32, device=q.device)
+    with torch.cuda.device(q.device):
+        stream = torch.cuda.current_stream(q.device).cuda_stream
+        _native.check(lib.tt_reversible_eigen(b, S, _native.ptr(q), _native.ptr(pi), _native.ptr(lam),
+                                              _native.ptr(u), _native.ptr(w), _native.ptr(status),
+                                              _native.ptr_value(stream)))
+    return lam, u, w
+
+
 def eigen_of_normalised(q: torch.Tensor, pi: torch.Tensor):
     """Eigen system of an already normalised reversible Q with stationary ``pi``."""
+    needs_graph = torch.is_grad_enabled() and (q.requires_grad or pi.requires_grad)
+    if q.is_cuda and not needs_graph:
+        lead = q.shape[:-2]
+        S = q.shape[-1]
+        lam, u, w = device_eigen(q.reshape(-1, S, S), pi.expand(lead + (S,)).reshape(-1, S))
+        return lam.reshape(lead + (S,)), u.reshape(lead + (S, S)), w.reshape(lead + (S, S))
     sp = pi.sqrt()
     a = sp.unsqueeze(-1) * q / sp.unsqueeze(-2)
     lam, v = torch.linalg.eigh(a)
