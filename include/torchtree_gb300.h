@@ -221,6 +221,39 @@ int tt_reversible_eigen(int32_t batch, int32_t state_count, const double *q,
                         double *u, double *w, int32_t *status, void *stream);
 
 /*
+ * Transition matrices of general (not necessarily reversible) rate
+ * matrices: P[b][br][k] = exp(Q_b * branch_lengths[b][br] *
+ * category_rates[b][k]), FP64, every matrix in one launch (scaling and
+ * squaring with the [13/13] Pade approximant).  Replaces
+ * NonSymmetricSubstitutionModel.p_t (torchtree/evolution/substitution_model/
+ * abstract.py:86-94: torch.matrix_exp of the normalised Q times t).
+ *   q [b][S][S] (normalised), branch_lengths [b][B], category_rates [b][K],
+ *   matrices [b][B][K][S][S]; all device; S <= 64.  The result goes to a
+ *   plan through tt_set_transition_matrices.
+ */
+int tt_transition_matrices_expm(int32_t batch, int32_t state_count,
+                                int32_t branch_count, int32_t category_count,
+                                const double *q, const double *branch_lengths,
+                                const double *category_rates, double *matrices,
+                                void *stream);
+
+/*
+ * Adjoint of tt_transition_matrices_expm (autograd through torch.matrix_exp
+ * in the reference, abstract.py:86-94): for G = dlnL/dP [b][B][K][S][S] (tt_gradient's
+ * grad_matrices), grad_q_parts[b][br][k] = tau L(tau Q^T, G) (the Frechet
+ * derivative, tau = t r) and grad_times[b][br][k] = tr(G^T Q P); dlnL/dQ is
+ * the sum of the parts over branches and categories, dlnL/dt_br =
+ * sum_k r_k grad_times, dlnL/dr_k = sum_br t_br grad_times.  S <= 32.
+ */
+int tt_transition_matrices_expm_adjoint(int32_t batch, int32_t state_count,
+                                        int32_t branch_count, int32_t category_count,
+                                        const double *q, const double *branch_lengths,
+                                        const double *category_rates,
+                                        const double *grad_matrices,
+                                        double *grad_q_parts, double *grad_times,
+                                        void *stream);
+
+/*
  * Quantiles of the Gamma(shape, rate 1) distribution at (2k+1)/(2K),
  * k = 0..K-1, and their derivative with respect to the shape (FP64,
  * analytic).  The discretised Gamma site model's rates are x_k / mean(x)

@@ -70,6 +70,10 @@ def _oracle_lnl(route, tensors, topo, alignment, rescale):
         qn, _, bls, rates, probs, freqs = tensors
         times = bls.unsqueeze(-1) * rates.unsqueeze(-2)  # [b, B, K]
         mats = torch.linalg.matrix_exp(qn[:, None, None] * times[..., None, None])
+    elif route == "general_rate_matrix":
+        qn, bls, rates, probs, freqs = tensors
+        times = bls.unsqueeze(-1) * rates.unsqueeze(-2)
+        mats = torch.linalg.matrix_exp(qn[:, None, None] * times[..., None, None])
     else:
         mats, probs, freqs = tensors
     tips = [torch.tensor(alignment.table[c].T) for c in alignment.codes]  # [S, N] per tip
@@ -575,3 +579,45 @@ def test_gamma_site_model_from_json(torchtree_ref):
         (gw,) = torch.autograd.grad(want_r[:, -1].sum(), shape)
         np.testing.assert_allclose(g.numpy(), gw.numpy(), rtol=1e-12)
         dic.pop("sm")
+
+
+@pytest.mark.parametrize("b", [1, 2])
+def test_model_inputs_for_a_nonreversible_model(torchtree_ref, b):
+    """torchtree's GeneralNonSymmetricSubstitutionModel (12 free rates) takes the
+    plug-in's matrix-exponential route; its gathered inputs give torchtree's
+    own lnL (unscaled and rescaled) and gradients (1e-12 / 1e-9)."""
+    from torchtree import Parameter
+    from torchtree.evolution.datatype import NucleotideDataType
+    from torchtree.evolution.substitution_model.general import GeneralNonSymmetricSubstitutionModel
+    from torchtree.evolution.tree_likelihood import TreeLikelihoodModel as Reference
+
+    from torchtree_gb300 import synthetic
+    from torchtree_gb300.model import TreeLikelihoodModel
+
+    wl = synthetic.dna_workload("nr", tip_count=10, site_count=200, batch=2, seed=94, shape=0.5,
+                                site_model="weibull")
+    rng = np.random.default_rng(7)
+    rates0 = rng.gamma(1.0, 1.0, (b, 12))
+    for rescale in (False, True):
+        def build():
+            tree, sp, _, site, clock, tip_states, leaves = _models("gtr_weibull", wl, b)
+            r = torch.tensor(rates0, requires_grad=True)
+            pi = torch.tensor(wl.pi[:b], requires_grad=True)
+            subst = GeneralNonSymmetricSubstitutionModel(None, NucleotideDataType(None),
+                                                         Parameter(None, torch.arange(12)), Parameter(None, r),
+                                                         Parameter(None, pi), True)
+            return tree, sp, subst, site, [leaves[0], r, pi, leaves[-1]]
+
+        tree, sp, subst, site, leaves = build()
+        ref = Reference(None, sp, tree, subst, site)
+        ref.rescale = rescale
+        want = ref().reshape(-1)
+        gwant = torch.autograd.grad(want.sum(), leaves)
+        tree, sp, subst, site, leaves = build()
+        ours = TreeLikelihoodModel(None, sp, tree, subst, site)
+        route, tensors, _, (nb, S, _) = ours.engine_inputs(torch.device("cpu"))
+        assert route == "general_rate_matrix" and (nb, S) == (b, 4)
+        got = _oracle_lnl(route, tensors, wl.topology, ours._alignment, rescale)
+        np.testing.assert_allclose(got.detach().numpy(), want.detach().numpy(), rtol=1e-12)
+        for g, w in zip(torch.autograd.grad(got.sum(), leaves), gwant):
+            np.testing.assert_allclose(g.numpy(), w.numpy(), rtol=1e-9, atol=1e-9 * float(w.abs().max()))

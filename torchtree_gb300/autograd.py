@@ -113,3 +113,37 @@ class MatrixLikelihood(torch.autograd.Function):
         g = g.to(torch.float64)
         dmats = _scale(g, dP, mats) if dP is not None else None
         return dmats, _scale(g, dc, props), _scale(g, dpi, freqs), None, None
+
+
+class GeneralRateMatrixLikelihood(torch.autograd.Function):
+    """lnL ``[b]`` from a normalised rate matrix ``q [b,S,S]`` that need not
+    be reversible (NonSymmetricSubstitutionModel.p_t, abstract.py:86-94):
+    P = exp(Q t r) by the engine's scaling-and-squaring Pade kernel; the
+    backward chains dlnL/dP through the Frechet derivative of the exponential
+    to dlnL/dQ, branch lengths and category rates."""
+
+    @staticmethod
+    def forward(ctx, q, bls, rates, props, freqs, engine, rescale):
+        mats = engine.expm_matrices(q.detach(), bls.detach(), rates.detach())
+        engine.set_matrices(mats)
+        keep = any(ctx.needs_input_grad[:5])
+        lnl = engine.log_likelihood(props, freqs, rescale=rescale, keep_partials=keep)
+        ctx.engine = engine
+        ctx.token = engine.token
+        ctx.rescale = rescale
+        ctx.save_for_backward(q, bls, rates, props, freqs, mats)
+        return lnl.to(q.dtype)
+
+    @staticmethod
+    def backward(ctx, g):
+        q, bls, rates, props, freqs, mats = ctx.saved_tensors
+        eng = ctx.engine
+        if eng.token != ctx.token:
+            eng.set_matrices(mats)
+            eng.log_likelihood(props, freqs, rescale=ctx.rescale, keep_partials=True)
+        dP, dpi, dc = eng.gradient(props, freqs, want_matrices=True)
+        dq, dt, dr = eng.expm_gradient(q.detach(), bls.detach(), rates.detach(), dP)
+        g = g.to(torch.float64)
+        return (_scale(g, dq, q), _scale(g, dt, bls), _scale(g, dr, rates), _scale(g, dc, props),
+                _scale(g, dpi, freqs), None, None)
+

@@ -177,6 +177,26 @@ class LikelihoodEngine:
         check(self.lib.tt_rate_matrix_gradient(self._plan, *map(ptr, args), ptr(dq), ptr(dt), ptr(dr), _stream()))
         return dq, dt, dr
 
+    def expm_matrices(self, q, branch_lengths, rates):
+        """``exp(Q t r)`` for every (sample, branch, category) of a normalised,
+        possibly non-reversible ``q [b,S,S]`` (FP64, one launch): ``[b,B,K,S,S]``."""
+        args = [_dev(x, self.device) for x in (q, branch_lengths, rates)]
+        b, S, K, B = self.batch, self.state_count, self.category_count, self.branch_count
+        mats = torch.empty(b, B, K, S, S, dtype=torch.float64, device=self.device)
+        check(self.lib.tt_transition_matrices_expm(b, S, B, K, *map(ptr, args), ptr(mats), _stream()))
+        self._keep_expm = args
+        return mats
+
+    def expm_gradient(self, q, branch_lengths, rates, grad_matrices):
+        """Chain dlnL/dP through ``P = exp(Q t r)``: ``(dQ [b,S,S], dt [b,B], dr [b,K])``."""
+        qd, bl, r, g = (_dev(x, self.device) for x in (q, branch_lengths, rates, grad_matrices))
+        b, S, K, B = self.batch, self.state_count, self.category_count, self.branch_count
+        parts = torch.empty(b, B, K, S, S, dtype=torch.float64, device=self.device)
+        dtau = torch.empty(b, B, K, dtype=torch.float64, device=self.device)
+        check(self.lib.tt_transition_matrices_expm_adjoint(b, S, B, K, ptr(qd), ptr(bl), ptr(r), ptr(g),
+                                                           ptr(parts), ptr(dtau), _stream()))
+        return parts.sum((1, 2)), (dtau * r.unsqueeze(1)).sum(-1), (dtau * bl.unsqueeze(-1)).sum(1)
+
     def _per_sample(self, x, width):
         """``[..., width]`` (one row or one per sample) -> contiguous ``[batch, width]``."""
         t = _dev(x, self.device).reshape(-1, width)

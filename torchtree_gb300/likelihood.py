@@ -17,7 +17,7 @@ from __future__ import annotations
 import numpy as np
 import torch
 
-from .autograd import EigenLikelihood, MatrixLikelihood, RateMatrixLikelihood
+from .autograd import EigenLikelihood, GeneralRateMatrixLikelihood, MatrixLikelihood, RateMatrixLikelihood
 from .engine import LikelihoodEngine
 from .patterns import CompressedAlignment
 from .substitution import normalise
@@ -76,6 +76,22 @@ class PhyloLikelihood:
         if torch.isinf(lnl).any():
             self.rescale = True
             lnl = EigenLikelihood.apply(lam, u, w, bls, rates, props, frequencies, self.engine, True)
+        return lnl
+
+    def evaluate_general(self, q, bls, rates, props, frequencies):
+        """lnL from a normalised rate matrix that need not be reversible
+        (``q [b,S,S]``): P = exp(Q t r) on the device by the scaling-and-squaring
+        Pade kernel; gradients reach ``q``, ``bls`` and ``rates`` through the
+        Frechet derivative of the exponential (S <= 32 for gradients)."""
+        def run(rescale):
+            return GeneralRateMatrixLikelihood.apply(q, bls, rates, props, frequencies, self.engine, rescale)
+
+        if self.rescale:
+            return run(True)
+        lnl = run(False)
+        if torch.isinf(lnl).any():
+            self.rescale = True
+            lnl = run(True)
         return lnl
 
     def evaluate_matrices(self, mats, props, frequencies):

@@ -11,8 +11,9 @@ GPU path.  A JSON configuration selects it with
 
 Reversible models that inherit torchtree's eigen-based ``p_t`` use the
 eigen route (the transition-matrix kernel forms every P on the device);
-any other substitution model (JC69's closed form, non-reversible models)
-hands its ``p_t`` matrices to the engine directly.
+non-reversible models that inherit its matrix-exponential ``p_t`` use the
+device Pade kernel; any other substitution model (JC69's closed form) hands
+its ``p_t`` matrices to the engine directly.
 """
 from __future__ import annotations
 
@@ -24,6 +25,7 @@ from torchtree.evolution.branch_model import BranchModel
 from torchtree.evolution.site_model import SiteModel, UnivariateDiscretizedSiteModel
 from torchtree.evolution.site_pattern import SitePattern
 from torchtree.evolution.substitution_model.abstract import (
+    NonSymmetricSubstitutionModel,
     SubstitutionModel,
     SymmetricSubstitutionModel,
 )
@@ -31,7 +33,7 @@ from torchtree.evolution.tree_likelihood import TreeLikelihoodModel as _Referenc
 from torchtree.evolution.tree_model import TreeModel
 
 from . import patterns
-from .autograd import MatrixLikelihood, RateMatrixLikelihood
+from .autograd import GeneralRateMatrixLikelihood, MatrixLikelihood, RateMatrixLikelihood
 from .engine import LikelihoodEngine
 from .site_models import _GammaQuantile
 from .substitution import normalise
@@ -40,6 +42,13 @@ from .substitution import normalise
 def _uses_eigen_form(subst_model) -> bool:
     return (isinstance(subst_model, SymmetricSubstitutionModel)
             and type(subst_model).p_t is SymmetricSubstitutionModel.p_t)
+
+
+def _uses_matrix_exp(subst_model) -> bool:
+    """torchtree's non-reversible p_t: torch.matrix_exp of the normalised Q
+    (abstract.py:86-94)."""
+    return (isinstance(subst_model, NonSymmetricSubstitutionModel)
+            and type(subst_model).p_t is NonSymmetricSubstitutionModel.p_t)
 
 
 @register_class
@@ -82,6 +91,9 @@ class TreeLikelihoodModel(_ReferenceModel):
         * route ``"rate_matrix"`` (reversible models with the eigen-form
           ``p_t``): ``(Q normalised, frequencies, node lengths, rates,
           probabilities, frequencies)``;
+        * route ``"general_rate_matrix"`` (non-reversible models with the
+          matrix-exponential ``p_t``, up to 32 states): ``(Q normalised, node
+          lengths, rates, probabilities, frequencies)``;
         * route ``"matrices"`` (any other ``p_t``): ``(P [b, 2T-2, K, S, S],
           probabilities, frequencies)``.
 
@@ -121,6 +133,12 @@ class TreeLikelihoodModel(_ReferenceModel):
             qn = normalise(flat(q, S, S), flat(freqs, S))  # abstract.py:49-50
             tensors = (qn, flat(freqs, S), flat(bls, bls.shape[-1]), flat(rates, K), flat(probs, K), flat(freqs, S))
             return "rate_matrix", tensors, sample_shape, (b, S, K)
+        if _uses_matrix_exp(self.subst_model) and S <= 32:
+            q = self.subst_model.q()
+            q = q.expand(sample_shape + (S, S)) if q.dim() == 2 else q.reshape(sample_shape + (S, S))
+            qn = normalise(flat(q, S, S), flat(freqs, S))  # abstract.py:88-94
+            tensors = (qn, flat(bls, bls.shape[-1]), flat(rates, K), flat(probs, K), flat(freqs, S))
+            return "general_rate_matrix", tensors, sample_shape, (b, S, K)
         mats = self.subst_model.p_t(bls.reshape(sample_shape + (-1, 1)) * rates.unsqueeze(-2))
         tensors = (flat(mats, mats.shape[-4], K, S, S), flat(probs, K), flat(freqs, S))
         return "matrices", tensors, sample_shape, (b, S, K)
@@ -129,8 +147,9 @@ class TreeLikelihoodModel(_ReferenceModel):
         dev = torch.device("cuda", torch.cuda.current_device())  # raises without CUDA: no CPU fallback
         route, tensors, sample_shape, (b, S, K) = self.engine_inputs(dev)
         eng = self._engine(b, S, K)
-        # rate-matrix route: gradients reach Q through dlnL/dQ (no eigenvector derivatives)
-        fn = RateMatrixLikelihood if route == "rate_matrix" else MatrixLikelihood
+        # rate-matrix routes: gradients reach Q through dlnL/dQ (no eigenvector derivatives)
+        fn = {"rate_matrix": RateMatrixLikelihood, "general_rate_matrix": GeneralRateMatrixLikelihood,
+              "matrices": MatrixLikelihood}[route]
 
         def run(rescale):
             return fn.apply(*tensors, eng, rescale)
