@@ -31,7 +31,9 @@ def _random_q(rng, b, S):
 
 
 def _engine_stub(b, S, B, K):
-    """An engine with the right shape for the expm entry points (any topology)."""
+    """An engine with the right shape for the expm entry points (any topology
+    with B = 2T - 2 branches; B even)."""
+    assert B % 2 == 0
     from torchtree_gb300 import synthetic
     from torchtree_gb300.engine import LikelihoodEngine
 
@@ -60,7 +62,7 @@ def test_expm_matches_torch_matrix_exp(S):
 @pytest.mark.parametrize("S", [2, 4, 20, 32])
 def test_expm_adjoint_matches_autograd(S):
     rng = np.random.default_rng(600 + S)
-    b, B, K = 2, 5, 2
+    b, B, K = 2, 6, 2  # B = 2T - 2 branches of the stub engine's tree
     q, _ = _random_q(rng, b, S)
     bl = torch.tensor(rng.exponential(0.3, (b, B)))
     bl[:, 1] = 12.0
