@@ -97,6 +97,12 @@ __device__ __forceinline__ void bulk_copy_g2s(void *dst, const void *src, uint32
       : "memory");
 }
 
+// Bulk prefetch of global memory into L2 (TMA engine, no completion to wait
+// for).  Address 16-byte aligned, bytes a multiple of 16.
+__device__ __forceinline__ void bulk_prefetch_l2(const void *src, uint32_t bytes) {
+  asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(src), "r"(bytes) : "memory");
+}
+
 // ---------------------------------------------------------------- vectors
 template <typename T>
 struct Vec16;  // 16-byte packet of T

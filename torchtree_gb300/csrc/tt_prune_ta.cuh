@@ -46,7 +46,7 @@ __host__ __device__ inline TaStage ta_stage(int KQ, int P) {
 }
 
 struct TaLayout {
-  int stages, bars, recs, table, xbuf, red_root, total;
+  int stages, bars, recs, table, onehot, xbuf, red_root, total;
 };
 
 __host__ __device__ inline TaLayout ta_layout(int KQ, int C, int P, int NT, int nstage) {
@@ -62,6 +62,8 @@ __host__ __device__ inline TaLayout ta_layout(int KQ, int C, int P, int NT, int 
   off = int(align16(off + 2 * kTaRecChunk * 48));
   L.table = off;
   off = int(align16(off + C * 32));
+  L.onehot = off;
+  off = int(align16(off + C));
   L.xbuf = off;
   off = int(align16(off + 2 * P * vbytes));
   L.red_root = off;
@@ -110,6 +112,9 @@ __device__ __forceinline__ void ta_issue(const PruneArgs<float> &a, int KQ, unsi
     else
       bulk_copy_g2s(stage + g.kids + c * int(tile_bytes), ta_tile(a, KQ, b, child[c], tile, P), tile_bytes, bar);
   }
+  // this step reads back the outside tile its parent's step stored: bring it
+  // into L2 now, a step ahead of the threads' loads
+  if (rec[2].y & kTaPreStored) bulk_prefetch_l2(ta_tile(a, KQ, b, rec[0].x, tile, P), tile_bytes);
 }
 
 // o[jj][q] = sum_i P_q[i][jj] x[i][q] with the pair matrices of one side in
@@ -166,7 +171,9 @@ __global__ void __launch_bounds__(NT, ta_min_blocks(KQ)) ta_backward_kernel(cons
     for (int st = 0; st < NSTAGE + 2; ++st) mbar_init(&bars[st], 1);
     fence_barrier_init();
   }
+  signed char *onehot = reinterpret_cast<signed char *>(smem + L.onehot);
   for (int i = tid; i < a.C * 4; i += NT) tab2[i] = make_float2(a.table[i], a.table[i]);
+  for (int c = tid; c < a.C; c += NT) onehot[c] = onehot_state(a.table, c);
   __syncthreads();
 
   // producer state (thread 0): the next reversed step to stage
@@ -238,12 +245,26 @@ __global__ void __launch_bounds__(NT, ta_min_blocks(KQ)) ta_backward_kernel(cons
     } else {
       pre = carry;
     }
-    if (ltip) vec_tip<KQ>(vl, tab2, stg[G.codes + tid]);
-    else vec_load_pm<KQ>(vl, kidl, tid, P);
-    if (rtip) vec_tip<KQ>(vr, tab2, stg[G.codes + P + tid]);
-    else vec_load_pm<KQ>(vr, kidr, tid, P);
-    mat_vec<KQ>(ar, pmr, vr);
-    mat_vec<KQ>(al, pml, vl);
+    // a tip with a one-hot code contributes a column of P; any other vector
+    // goes through the matrix-vector product
+    {
+      const int sr = rtip ? int(onehot[stg[G.codes + P + tid]]) : -1;
+      if (sr >= 0) {
+        mat_col<KQ>(ar, pmr, sr);
+      } else {
+        if (rtip) vec_tip<KQ>(vr, tab2, stg[G.codes + P + tid]);
+        else vec_load_pm<KQ>(vr, kidr, tid, P);
+        mat_vec<KQ>(ar, pmr, vr);
+      }
+      const int sl = ltip ? int(onehot[stg[G.codes + tid]]) : -1;
+      if (sl >= 0) {
+        mat_col<KQ>(al, pml, sl);
+      } else {
+        if (ltip) vec_tip<KQ>(vl, tab2, stg[G.codes + tid]);
+        else vec_load_pm<KQ>(vl, kidl, tid, P);
+        mat_vec<KQ>(al, pml, vl);
+      }
+    }
     // outside partials at the tops of the two branches: xl = pre*ar, xr = pre*al
     Vec<KQ> xl, xr;
     float2 d2[2] = {make_float2(0.0f, 0.0f), make_float2(0.0f, 0.0f)};  // two chains

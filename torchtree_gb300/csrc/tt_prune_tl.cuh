@@ -54,7 +54,7 @@ __host__ __device__ inline TlStage tl_stage(int KQ, int P, bool backward) {
 }
 
 struct TlLayout {
-  int stages, bars, recs, table, stack, xbuf, red, red_root, total;
+  int stages, bars, recs, table, onehot, stack, xbuf, red, red_root, total;
 };
 
 constexpr int kTlRecChunk = 32;
@@ -81,6 +81,8 @@ __host__ __device__ inline TlLayout tl_layout(int KQ, int C, int slots, int P, i
   off = int(align16(off + 2 * kTlRecChunk * 48));
   L.table = off;
   off = int(align16(off + C * 32));
+  L.onehot = off;
+  off = int(align16(off + C));
   L.stack = off;
   off = int(align16(off + slots * P * vbytes));
   L.xbuf = off;
@@ -282,6 +284,33 @@ __device__ __forceinline__ void mat_vec(Vec<KQ> &out, const float2 *pm, const Ve
       out.v[i][q] = __ffma2_rn(p[i][3], in.v[3][q], acc);
     }
   }
+}
+
+// State of a one-hot code-table row (exactly one 1 and zeros elsewhere), or
+// -1: a tip with such a code contributes the column P[.][s] of each matrix.
+template <typename TT>
+__device__ __forceinline__ signed char onehot_state(const TT *table, int code) {
+  int s = -1, ones = 0;
+#pragma unroll
+  for (int j = 0; j < 4; ++j) {
+    const TT v = table[code * 4 + j];
+    if (v == TT(1)) {
+      s = j;
+      ++ones;
+    } else if (v != TT(0)) {
+      return -1;
+    }
+  }
+  return ones == 1 ? static_cast<signed char>(s) : -1;
+}
+
+// out[i][q] = P_q[i][s]: the matrix-vector product with the unit vector e_s
+template <int KQ>
+__device__ __forceinline__ void mat_col(Vec<KQ> &out, const float2 *pm, int s) {
+#pragma unroll
+  for (int q = 0; q < KQ; ++q)
+#pragma unroll
+    for (int i = 0; i < 4; ++i) out.v[i][q] = pm[(q * 4 + i) * 4 + s];
 }
 
 template <int KQ>
@@ -492,7 +521,9 @@ __global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ, NT)) tl_forward_
     abort_flag = 0;
     fence_barrier_init();
   }
+  signed char *onehot = reinterpret_cast<signed char *>(smem + L.onehot);
   for (int i = tid; i < a.C * 4; i += NT + 32) tab2[i] = make_float2(a.table[i], a.table[i]);
+  for (int c = tid; c < a.C; c += NT + 32) onehot[c] = onehot_state(a.table, c);
   __syncthreads();
 
   if (tid >= NT) {  // producer warp
@@ -551,14 +582,25 @@ __global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ, NT)) tl_forward_
       const float2 *pmr = pml + KQ * 16;
       const int out_slot = r1.y;
       Vec<KQ> v, al, ar;
-      if (ltip) vec_tip<KQ>(v, tab2, stg[G.codes + p]);
-      else if (r0.w == kWsCarry) v = carry;
-      else vec_load<KQ>(v, stk + r0.w * NC * P + p, P);
-      mat_vec<KQ>(al, pml, v);
-      if (rtip) vec_tip<KQ>(v, tab2, stg[G.codes + P + p]);
-      else if (r1.x == kWsCarry) v = carry;
-      else vec_load<KQ>(v, stk + r1.x * NC * P + p, P);
-      mat_vec<KQ>(ar, pmr, v);
+      // a tip with a one-hot code contributes a column of P
+      const int sl = ltip ? int(onehot[stg[G.codes + p]]) : -1;
+      if (sl >= 0) {
+        mat_col<KQ>(al, pml, sl);
+      } else {
+        if (ltip) vec_tip<KQ>(v, tab2, stg[G.codes + p]);
+        else if (r0.w == kWsCarry) v = carry;
+        else vec_load<KQ>(v, stk + r0.w * NC * P + p, P);
+        mat_vec<KQ>(al, pml, v);
+      }
+      const int sr = rtip ? int(onehot[stg[G.codes + P + p]]) : -1;
+      if (sr >= 0) {
+        mat_col<KQ>(ar, pmr, sr);
+      } else {
+        if (rtip) vec_tip<KQ>(v, tab2, stg[G.codes + P + p]);
+        else if (r1.x == kWsCarry) v = carry;
+        else vec_load<KQ>(v, stk + r1.x * NC * P + p, P);
+        mat_vec<KQ>(ar, pmr, v);
+      }
       __syncwarp();
       if (lane == 0) mbar_arrive(&empty[st]);  // stage consumed by this warp
 #pragma unroll
