@@ -382,6 +382,9 @@ int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
  *     partials over the stored post-order tiles (1, the default: a second
  *     tt_gradient then needs a new tt_log_likelihood with keep_partials=1)
  *     or keeps them in a shared-memory stack (0);
+ *   TT_OPT_PAIR_ADJOINT: that in-place adjoint with the category pairs of a
+ *     pattern on adjacent threads (1) or all in one thread (0); K in 1-4 or
+ *     7-8; either reads the same stored partials;
  *   TT_OPT_SLAB_PATTERNS: how many patterns' post-order partials are held
  *     at once (rounded up to a multiple of 512; 0 = all, the default when
  *     they fit).  With a slab size set, tt_gradient recomputes the post-order
@@ -404,7 +407,8 @@ enum {
   TT_OPT_PAIR_THREADS = 4,
   TT_OPT_PRODUCER_WARP = 5,
   TT_OPT_INPLACE_ADJOINT = 6,
-  TT_OPT_SLAB_PATTERNS = 7
+  TT_OPT_SLAB_PATTERNS = 7,
+  TT_OPT_PAIR_ADJOINT = 8
 };
 int tt_plan_set_option(tt_plan *plan, int32_t option, int32_t value);
 int tt_plan_get_option(const tt_plan *plan, int32_t option, int32_t *value);

@@ -302,7 +302,8 @@ def test_forward_without_gradient_matches(golden_likelihood):
 def test_pair_thread_kernels_match_one_thread_kernels():
     """FP32 4-state kernels: one thread per (pattern, category pair) vs one per
     pattern, and the adjoint with a shared-memory stack vs the one that stores
-    outside partials over the post-order tiles (which consumes them)."""
+    outside partials over the post-order tiles (which consumes them), with all
+    category pairs of a pattern in one thread or on adjacent threads."""
     from torchtree_gb300 import _native, patterns, site_models, substitution, synthetic
     from torchtree_gb300.engine import LikelihoodEngine
 
@@ -322,9 +323,11 @@ def test_pair_thread_kernels_match_one_thread_kernels():
         eng = LikelihoodEngine(wl.topology.postorder, wl.topology.tip_count, 4, K, ca.codes, ca.table, ca.weights,
                                batch=b, precision="f32")
         out = {}
-        for mode, (pair, inplace) in {"stack": (0, 0), "inplace": (0, 1), "pair": (1, 0)}.items():
+        modes = {"stack": (0, 0, 0), "inplace": (0, 1, 0), "pair": (1, 0, 0), "pair_adjoint": (0, 1, 1)}
+        for mode, (pair, inplace, pair_adjoint) in modes.items():
             eng.set_option(_native.TT_OPT_PAIR_THREADS, pair)
             eng.set_option(_native.TT_OPT_INPLACE_ADJOINT, inplace)
+            eng.set_option(_native.TT_OPT_PAIR_ADJOINT, pair_adjoint)
             eng.set_eigen(*eig)
             lnl = eng.log_likelihood(props, pid, rescale=True, keep_partials=True)
             dP, dpi, dc = eng.gradient(props, pid, want_matrices=True)
@@ -332,7 +335,7 @@ def test_pair_thread_kernels_match_one_thread_kernels():
             if inplace:  # the post-order tiles are gone: a second adjoint is refused
                 with pytest.raises(_native.EngineError):
                     eng.gradient(props, pid)
-        for mode in ("inplace", "pair"):
+        for mode in ("inplace", "pair", "pair_adjoint"):
             # identical FP32 partials; the FP64 root sums run in a different order
             np.testing.assert_allclose(out[mode][0], out["stack"][0], rtol=1e-13)
             for a_, b_ in zip(out["stack"][1:], out[mode][1:]):
@@ -388,16 +391,20 @@ def test_fp32_adjoints_on_edge_trees(shape, T, K):
     eig = [lam, u, w, bls, rates.to(dev).contiguous()]
     props, pid = probs.expand(b, K).to(dev).contiguous(), pit.to(dev)
     out = {}
-    for name, precision, inplace in (("f64", "f64", None), ("f32", "f32", 1), ("f32_stack", "f32", 0)):
+    variants = [("f64", "f64", None, 0), ("f32", "f32", 1, 0), ("f32_stack", "f32", 0, 0)]
+    if (K + 1) // 2 in (1, 2, 4):  # the pair-thread adjoint takes 1, 2 or 4 category pairs
+        variants.append(("f32_pair_adjoint", "f32", 1, 1))
+    for name, precision, inplace, pair_adjoint in variants:
         eng = LikelihoodEngine(topo.postorder, T, 4, K, ca.codes, ca.table, ca.weights, batch=b, precision=precision)
         if inplace is not None:
             eng.set_option(_native.TT_OPT_INPLACE_ADJOINT, inplace)
+            eng.set_option(_native.TT_OPT_PAIR_ADJOINT, pair_adjoint)
         eng.set_eigen(*eig)
         lnl = eng.log_likelihood(props, pid, rescale=precision == "f32", keep_partials=True)
         dP, dpi, dc = eng.gradient(props, pid, want_matrices=True)
         out[name] = [x.cpu().numpy() for x in (lnl, dP, dpi, dc)]
     ref = out["f64"]
-    for name in ("f32", "f32_stack"):
+    for name in [v[0] for v in variants[1:]]:
         np.testing.assert_allclose(out[name][0], ref[0], rtol=1e-6)
         for got, want in zip(out[name][1:], ref[1:]):
             np.testing.assert_allclose(got, want, rtol=1e-4, atol=1e-4 * np.abs(want).max())

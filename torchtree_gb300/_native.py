@@ -29,6 +29,7 @@ _PI32 = ctypes.POINTER(ctypes.c_int32)
 TT_OPT_FWD_STAGES, TT_OPT_BWD_STAGES, TT_OPT_TENSOR_CORES, TT_OPT_PAIR_THREADS, TT_OPT_PRODUCER_WARP = 1, 2, 3, 4, 5
 TT_OPT_INPLACE_ADJOINT = 6
 TT_OPT_SLAB_PATTERNS = 7
+TT_OPT_PAIR_ADJOINT = 8
 
 SIGNATURES = {
     "tt_version": (ctypes.c_char_p, []),

@@ -472,7 +472,8 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
     const int ns = bwd ? p->nstage_b : p->nstage_f;
     return f32 ? std::max({tt::tl_smem_bytes(p->K, 256, slots, bwd, ns), tt::tq_smem_bytes(p->K, 256, slots, bwd, ns),
                            bwd ? size_t(0) : tt::tl_ws_smem_bytes(p->K, 256, p->slots_ws, ns),
-                           bwd ? tt::ta_smem_bytes(p->K, 256, ns) : size_t(0)})
+                           bwd ? std::max(tt::ta_smem_bytes(p->K, 256, ns), tt::tp_smem_bytes(p->K, 256, ns))
+                               : size_t(0)})
                : tt::prune_smem_bytes<double>(4, p->K, 256, slots, tile, bwd);
   };
   // optional overrides for tuning sweeps: TT_FWD_TILE / TT_BWD_TILE.  FP32 rings
@@ -510,6 +511,10 @@ int tt_plan_create(tt_plan **plan, int32_t tip_count, const int32_t *postorder,
   {
     const char *env = getenv("TT_INPLACE_ADJOINT");
     p->inplace_adjoint = f32 && !(env && atoi(env) == 0);
+  }
+  if (f32 && tt::pair_adjoint_supported(p->K)) {
+    const char *env = getenv("TT_PAIR_ADJOINT");
+    p->pair_adjoint = env && atoi(env) == 1;
   }
   if (f32 && tt::pair_threads_supported(p->K)) {  // measured slower on GB300: off unless TT_PAIR_THREADS=1
     const char *env = getenv("TT_PAIR_THREADS");
@@ -747,7 +752,11 @@ int tt_gradient(tt_plan *p, const double *props, const double *freqs, double *gr
       a.nstage = p->nstage_b;
       slab_args(a, p0, n, p->tile_b);
       e = tt::launch_prune_f32(a, true, p->tile_b, p->batch,
-                               p->pair_threads ? tt::kF32PairThreads : (p->inplace_adjoint ? tt::kF32InPlaceAdjoint : 0), s);
+                               p->pair_threads ? tt::kF32PairThreads
+                                               : (p->inplace_adjoint ? tt::kF32InPlaceAdjoint |
+                                                                           (p->pair_adjoint ? tt::kF32PairAdjoint : 0)
+                                                                     : 0),
+                               s);
       if (e == cudaSuccess)
         e = tt::launch_reduce_f32(static_cast<const float *>(p->d_gpart),
                                   static_cast<const float *>(p->d_rootpart), p->d_G, p->d_rootgrad,
@@ -859,7 +868,8 @@ int tt_plan_set_option(tt_plan *p, int32_t option, int32_t value) {
       const int sl = bwd ? p->slots_bwd : p->slots_fwd;
       if (std::max({tt::tl_smem_bytes(p->K, 256, sl, bwd, value), tt::tq_smem_bytes(p->K, 256, sl, bwd, value),
                     bwd ? size_t(0) : tt::tl_ws_smem_bytes(p->K, 256, p->slots_ws, value),
-                    bwd ? tt::ta_smem_bytes(p->K, 256, value) : size_t(0)}) > size_t(smem_max))
+                    bwd ? std::max(tt::ta_smem_bytes(p->K, 256, value), tt::tp_smem_bytes(p->K, 256, value))
+                        : size_t(0)}) > size_t(smem_max))
         return fail(TT_ERR_UNSUPPORTED, "ring does not fit in shared memory");
       (bwd ? p->nstage_b : p->nstage_f) = value;
       return TT_OK;
@@ -884,6 +894,12 @@ int tt_plan_set_option(tt_plan *p, int32_t option, int32_t value) {
         return fail(TT_ERR_UNSUPPORTED, "the in-place adjoint serves FP32 4-state plans");
       if (p->inplace_adjoint != (value != 0)) p->partials_valid = false;
       p->inplace_adjoint = value != 0;
+      return TT_OK;
+    case TT_OPT_PAIR_ADJOINT:
+      if (value && (p->wide || p->precision != TT_PRECISION_F32 || !tt::pair_adjoint_supported(p->K)))
+        return fail(TT_ERR_UNSUPPORTED, "the pair-thread in-place adjoint serves FP32 4-state plans with 1-4 or 7-8 "
+                                        "categories");
+      p->pair_adjoint = value != 0;  // same partial layout: stored partials stay valid
       return TT_OK;
     case TT_OPT_SLAB_PATTERNS: {
       if (value < 0) return fail(TT_ERR_INVALID_ARGUMENT, "the slab size must be >= 0 (0 = all patterns)");
@@ -914,6 +930,7 @@ int tt_plan_get_option(const tt_plan *p, int32_t option, int32_t *value) {
     case TT_OPT_PRODUCER_WARP: *value = p->producer_warp ? 1 : 0; return TT_OK;
     case TT_OPT_INPLACE_ADJOINT: *value = p->inplace_adjoint ? 1 : 0; return TT_OK;
     case TT_OPT_SLAB_PATTERNS: *value = p->slab; return TT_OK;
+    case TT_OPT_PAIR_ADJOINT: *value = p->pair_adjoint ? 1 : 0; return TT_OK;
     default: return fail(TT_ERR_INVALID_ARGUMENT, "unknown option");
   }
 }

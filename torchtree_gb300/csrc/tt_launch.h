@@ -59,13 +59,17 @@ inline size_t tl_smem_bytes(int K, int C, int slots, bool backward, int nstage) 
 // flags: kF32PairThreads = one thread per (pattern, category pair) kernels
 // (K in 1-4 or 7-8); kF32ProducerWarp = post-order with a producer warp;
 // kF32InPlaceAdjoint = adjoint that stores outside partials over the
-// post-order tiles (consumes them) instead of a shared-memory stack
-constexpr int kF32PairThreads = 1, kF32ProducerWarp = 2, kF32InPlaceAdjoint = 4;
+// post-order tiles (consumes them) instead of a shared-memory stack;
+// kF32PairAdjoint = that adjoint with one thread per (pattern, category pair)
+// (K in 1-2, 3-4 or 7-8)
+constexpr int kF32PairThreads = 1, kF32ProducerWarp = 2, kF32InPlaceAdjoint = 4, kF32PairAdjoint = 8;
 cudaError_t launch_prune_f32(const PruneArgs<float> &a, bool backward, int tile, int batch, int flags,
                              cudaStream_t stream);
 size_t tq_smem_bytes(int K, int C, int slots, bool backward, int nstage);
 size_t ta_smem_bytes(int K, int C, int nstage);
+size_t tp_smem_bytes(int K, int C, int nstage);
 bool pair_threads_supported(int K);
+bool pair_adjoint_supported(int K);
 cudaError_t launch_prune_f64(const PruneArgs<double> &a, bool backward, int tile, int batch,
                              cudaStream_t stream);
 

@@ -23,6 +23,7 @@ struct tt_plan {
   bool pair_threads = false;  // FP32 4-state: one thread per (pattern, category pair)
   bool producer_warp = true;  // FP32 4-state post-order with a producer warp
   bool inplace_adjoint = true;  // FP32 4-state adjoint storing outside partials over the post-order tiles
+  bool pair_adjoint = false;    // ... with one thread per (pattern, category pair) (tp_backward_kernel)
   bool tips_set = false, pmat_set = false, partials_valid = false, grads_valid = false;
   // patterns whose post-order partials are held at once (0 = all).  When
   // nonzero, tt_gradient recomputes the post-order one pattern slab at a

@@ -1,8 +1,11 @@
 // FP32 (rescaled) pruning kernels on packed FP32x2 arithmetic, S = 4.
+#include <cstdlib>
+
 #include "tt_launch.h"
 #include "tt_pmatrix.cuh"
 #include "tt_prune_ta.cuh"
 #include "tt_prune_tl.cuh"
+#include "tt_prune_tp.cuh"
 #include "tt_prune_tq.cuh"
 
 namespace tt {
@@ -94,10 +97,41 @@ cudaError_t launch_ta(const PruneArgs<float> &a, int batch, cudaStream_t stream)
   return cudaGetLastError();
 }
 
+size_t tp_smem_bytes(int K, int C, int nstage) {
+  const int KQ = kpairs_for(K);
+  return size_t(ta_layout(KQ, C, kTpTile, kTpTile * KQ, nstage).total);
+}
+
+bool pair_adjoint_supported(int K) {
+  const int KQ = kpairs_for(K);
+  return KQ == 1 || KQ == 2 || KQ == 4;
+}
+
+template <int KQ, int MB = tp_min_blocks(KQ)>
+cudaError_t launch_tp(const PruneArgs<float> &a, int batch, cudaStream_t stream) {
+  const size_t smem = tp_smem_bytes(a.K, a.C, a.nstage);
+  const dim3 grid(a.ntiles, batch);
+  auto kern = tp_backward_kernel<KQ, MB>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  kern<<<grid, kTpTile * KQ, smem, stream>>>(a);
+  return cudaGetLastError();
+}
+
 cudaError_t launch_prune_f32(const PruneArgs<float> &a, bool backward, int tile, int batch, int flags,
                              cudaStream_t stream) {
   if (tile != kTlTile) return cudaErrorInvalidValue;
   const bool pair_threads = flags & kF32PairThreads;
+  if (backward && !pair_threads && (flags & kF32InPlaceAdjoint) && (flags & kF32PairAdjoint) &&
+      pair_adjoint_supported(a.K)) {
+    switch (kpairs_for(a.K)) {
+      case 1: return launch_tp<1>(a, batch, stream);
+      case 2:  // register budget for 7 CTAs per SM (72 registers), or 8 (64, a few spills) on request
+        return getenv("TT_TP_MINBLOCKS") && atoi(getenv("TT_TP_MINBLOCKS")) == 8 ? launch_tp<2, 8>(a, batch, stream)
+                                                                                 : launch_tp<2>(a, batch, stream);
+      default: return launch_tp<4>(a, batch, stream);
+    }
+  }
   if (backward && !pair_threads && (flags & kF32InPlaceAdjoint)) {
     switch (kpairs_for(a.K)) {
       case 1: return launch_ta<1>(a, batch, stream);
