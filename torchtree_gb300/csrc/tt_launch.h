@@ -70,6 +70,14 @@ size_t ta_smem_bytes(int K, int C, int nstage);
 size_t tp_smem_bytes(int K, int C, int nstage);
 bool pair_threads_supported(int K);
 bool pair_adjoint_supported(int K);
+// One launch over the plans of `m` (all with the same category-pair count):
+// the producer-warp post-order (`total` CTAs, kTlWsPatterns patterns each),
+// or the in-place adjoint (one stored tile per CTA; `pair_adjoint` selects
+// the pair-thread kernel).  `smem` = the largest dynamic shared memory any
+// of the plans needs.
+cudaError_t launch_forward_multi(const MultiPrune<float> &m, int total, size_t smem, cudaStream_t stream);
+cudaError_t launch_adjoint_multi(const MultiPrune<float> &m, int total, size_t smem, bool pair_adjoint,
+                                 cudaStream_t stream);
 cudaError_t launch_prune_f64(const PruneArgs<double> &a, bool backward, int tile, int batch,
                              cudaStream_t stream);
 

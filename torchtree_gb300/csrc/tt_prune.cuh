@@ -82,6 +82,25 @@ struct PruneArgs {
   const int4 *steps_ws = nullptr;
 };
 
+// Arguments of one launch over several plans (one kernel parameter block):
+// plan i owns CTAs [first[i], first[i+1]) of the 1-D grid, `per_sample[i]`
+// of them per batch sample.
+constexpr int kMaxMultiPlans = 16;
+template <typename T>
+struct MultiPrune {
+  int count;
+  int first[kMaxMultiPlans + 1];
+  int per_sample[kMaxMultiPlans];
+  PruneArgs<T> a[kMaxMultiPlans];
+  __device__ __forceinline__ void locate(int cta, int &pi, int &tile, int &b) const {
+    pi = 0;
+    while (pi + 1 < count && cta >= first[pi + 1]) ++pi;
+    const int r = cta - first[pi];
+    b = r / per_sample[pi];
+    tile = r - b * per_sample[pi];
+  }
+};
+
 __host__ __device__ inline size_t align16(size_t x) { return (x + 15) & ~size_t(15); }
 
 // Layout of one ring stage: step record | matrix pair | 2 code rows | 2 child tiles

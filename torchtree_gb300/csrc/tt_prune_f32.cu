@@ -118,6 +118,57 @@ cudaError_t launch_tp(const PruneArgs<float> &a, int batch, cudaStream_t stream)
   return cudaGetLastError();
 }
 
+namespace {
+
+template <int KQ>
+cudaError_t launch_forward_multi_k(const MultiPrune<float> &m, int total, size_t smem, cudaStream_t stream) {
+  auto kern = tl_forward_ws_multi_kernel<KQ, kTlWsPatterns>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  kern<<<total, kTlWsPatterns + 32, smem, stream>>>(m);
+  return cudaGetLastError();
+}
+
+template <int KQ>
+cudaError_t launch_adjoint_multi_k(const MultiPrune<float> &m, int total, size_t smem, bool pair_adjoint,
+                                   cudaStream_t stream) {
+  if constexpr (KQ == 1 || KQ == 2 || KQ == 4) {
+    if (pair_adjoint) {
+      auto kern = tp_backward_multi_kernel<KQ>;
+      cudaError_t e = set_smem(kern, smem);
+      if (e != cudaSuccess) return e;
+      kern<<<total, kTpTile * KQ, smem, stream>>>(m);
+      return cudaGetLastError();
+    }
+  }
+  auto kern = ta_backward_multi_kernel<KQ, kTlBwdThreads>;
+  cudaError_t e = set_smem(kern, smem);
+  if (e != cudaSuccess) return e;
+  kern<<<total, kTlBwdThreads, smem, stream>>>(m);
+  return cudaGetLastError();
+}
+
+}  // namespace
+
+cudaError_t launch_forward_multi(const MultiPrune<float> &m, int total, size_t smem, cudaStream_t stream) {
+  switch (kpairs_for(m.a[0].K)) {
+    case 1: return launch_forward_multi_k<1>(m, total, smem, stream);
+    case 2: return launch_forward_multi_k<2>(m, total, smem, stream);
+    case 3: return launch_forward_multi_k<3>(m, total, smem, stream);
+    default: return launch_forward_multi_k<4>(m, total, smem, stream);
+  }
+}
+
+cudaError_t launch_adjoint_multi(const MultiPrune<float> &m, int total, size_t smem, bool pair_adjoint,
+                                 cudaStream_t stream) {
+  switch (kpairs_for(m.a[0].K)) {
+    case 1: return launch_adjoint_multi_k<1>(m, total, smem, pair_adjoint, stream);
+    case 2: return launch_adjoint_multi_k<2>(m, total, smem, pair_adjoint, stream);
+    case 3: return launch_adjoint_multi_k<3>(m, total, smem, false, stream);
+    default: return launch_adjoint_multi_k<4>(m, total, smem, pair_adjoint, stream);
+  }
+}
+
 cudaError_t launch_prune_f32(const PruneArgs<float> &a, bool backward, int tile, int batch, int flags,
                              cudaStream_t stream) {
   if (tile != kTlTile) return cudaErrorInvalidValue;

@@ -492,7 +492,7 @@ __global__ void __launch_bounds__(NT) tl_forward_kernel(const PruneArgs<float> a
 // only its own pattern's stack entries, so the compute warps need no block
 // barrier per step and drift up to NSTAGE - 1 steps apart.
 template <int KQ, int NT>
-__global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ, NT)) tl_forward_ws_kernel(const PruneArgs<float> a) {
+__device__ __forceinline__ void tl_forward_ws_body(const PruneArgs<float> &a, const int tile, const int b) {
   constexpr int P = NT;  // patterns of this CTA: NT / kTlPartTile stored tiles of one sample
   constexpr int TPC = NT / kTlPartTile;
   static_assert(NT % kTlPartTile == 0, "whole stored tiles per CTA");
@@ -505,8 +505,6 @@ __global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ, NT)) tl_forward_
   const int NSTAGE = a.nstage;
   const int tid = threadIdx.x, lane = tid & 31;
   const int K = a.K;
-  const int b = blockIdx.y;
-  const int tile = blockIdx.x;
   const int nst = a.n_steps;
   const TlLayout L = tl_layout(KQ, a.C, a.slots, P, NT, NSTAGE, false);
   const TlStage G = tl_stage(KQ, P, false);
@@ -644,6 +642,23 @@ __global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ, NT)) tl_forward_
     for (int w = 0; w < WPT; ++w) tot += warp_tot[tid * WPT + w];
     if (tile * TPC + tid < a.ntiles) a.tile_lnl[size_t(b) * a.ntiles + tile * TPC + tid] = tot;
   }
+}
+
+template <int KQ, int NT>
+__global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ, NT))
+    tl_forward_ws_kernel(const __grid_constant__ PruneArgs<float> a) {
+  tl_forward_ws_body<KQ, NT>(a, blockIdx.x, blockIdx.y);
+}
+
+// The same post-order over the tiles of several plans in one launch (plans
+// of one category-pair count): CTA x of the 1-D grid walks tile `tile` of
+// sample `b` of plan `pi` (MultiPrune::locate).
+template <int KQ, int NT>
+__global__ void __launch_bounds__(NT + 32, tl_ws_min_blocks(KQ, NT))
+    tl_forward_ws_multi_kernel(const __grid_constant__ MultiPrune<float> m) {
+  int pi, tile, b;
+  m.locate(blockIdx.x, pi, tile, b);
+  tl_forward_ws_body<KQ, NT>(m.a[pi], tile, b);
 }
 
 // ----------------------------------------------------------------- backward

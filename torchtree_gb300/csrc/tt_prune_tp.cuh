@@ -65,8 +65,8 @@ __device__ __forceinline__ void pmat_col(Vp &out, const float2 *pm, int q, int s
   for (int i = 0; i < 4; ++i) out.v[i] = pm[(q * 4 + i) * 4 + s];
 }
 
-template <int KQ, int MB = tp_min_blocks(KQ)>
-__global__ void __launch_bounds__(kTpTile * KQ, MB) tp_backward_kernel(const PruneArgs<float> a) {
+template <int KQ>
+__device__ __forceinline__ void tp_backward_body(const PruneArgs<float> &a, const int tile, const int b) {
   static_assert(KQ == 1 || KQ == 2 || KQ == 4, "pairs per pattern must be a power of two");
   constexpr int P = kTpTile;
   constexpr int NT = P * KQ;
@@ -79,8 +79,6 @@ __global__ void __launch_bounds__(kTpTile * KQ, MB) tp_backward_kernel(const Pru
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int q = tid & (KQ - 1), p = tid / KQ;  // category pair, pattern of this thread
   const int K = a.K;
-  const int b = blockIdx.y;
-  const int tile = blockIdx.x;
   const int n = tile * P + p;
   const bool act = n < a.N;
   const int rem = min(P, a.N - tile * P);
@@ -355,6 +353,20 @@ __global__ void __launch_bounds__(kTpTile * KQ, MB) tp_backward_kernel(const Pru
         a.rootpart[(size_t(b) * a.ntiles + tile) * (4 + K) + e] = acc;
       }
   }
+}
+
+template <int KQ, int MB = tp_min_blocks(KQ)>
+__global__ void __launch_bounds__(kTpTile * KQ, MB) tp_backward_kernel(const __grid_constant__ PruneArgs<float> a) {
+  tp_backward_body<KQ>(a, blockIdx.x, blockIdx.y);
+}
+
+// the same adjoint over the tiles of several plans in one launch
+template <int KQ, int MB = tp_min_blocks(KQ)>
+__global__ void __launch_bounds__(kTpTile * KQ, MB)
+    tp_backward_multi_kernel(const __grid_constant__ MultiPrune<float> m) {
+  int pi, tile, b;
+  m.locate(blockIdx.x, pi, tile, b);
+  tp_backward_body<KQ>(m.a[pi], tile, b);
 }
 
 }  // namespace tt
