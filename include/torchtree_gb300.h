@@ -202,6 +202,31 @@ int tt_schedule(int32_t tip_count, const int32_t *postorder, int32_t *steps,
                 int32_t *slot_counts);
 
 /*
+ * tt_log_likelihood / tt_gradient of several plans in one call.  No
+ * counterpart in the reference (it evaluates one model per call); it serves a
+ * server that batches the work of many data sets.  Plans on the default FP32
+ * 4-state kernels (producer-warp post-order, in-place adjoint, whole
+ * alignment resident) with one category-pair count are merged into one
+ * post-order launch and one adjoint launch over all their tiles (up to 16
+ * plans per launch); every other plan runs its own calls.  Each plan's
+ * results are the ones its own calls give, bit for bit.
+ *   plans[count], category_weights[count], frequencies[count] (device, per
+ *   plan as for tt_log_likelihood), log_likelihood[count] (device);
+ *   grad_frequencies / grad_weights: NULL or arrays of `count` device
+ *   pointers (entries may be NULL).  A plan may appear once per call.
+ */
+int tt_plans_log_likelihood(int32_t count, tt_plan *const *plans,
+                            const double *const *category_weights,
+                            const double *const *frequencies, int32_t rescale,
+                            int32_t keep_partials, double *const *log_likelihood,
+                            void *stream);
+int tt_plans_gradient(int32_t count, tt_plan *const *plans,
+                      const double *const *category_weights,
+                      const double *const *frequencies,
+                      double *const *grad_frequencies,
+                      double *const *grad_weights, void *stream);
+
+/*
  * Eigen system of reversible rate matrices on the device, FP64.  Replaces
  * the eigendecomposition inside SymmetricSubstitutionModel.p_t
  * (torchtree/evolution/substitution_model/abstract.py:57-79: Q normalised,

@@ -61,6 +61,8 @@ SIGNATURES = {
     "tt_gamma_quantiles_host": (ctypes.c_int, [_I32, _I32, _P, _P, _P]),
     "tt_transition_matrices_expm": (ctypes.c_int, [_I32, _I32, _I32, _I32, _P, _P, _P, _P, _P]),
     "tt_transition_matrices_expm_adjoint": (ctypes.c_int, [_I32, _I32, _I32, _I32, _P, _P, _P, _P, _P, _P, _P]),
+    "tt_plans_log_likelihood": (ctypes.c_int, [_I32, _P, _P, _P, _I32, _I32, _P, _P]),
+    "tt_plans_gradient": (ctypes.c_int, [_I32, _P, _P, _P, _P, _P, _P]),
     "tt_log_likelihood_static": (ctypes.c_int, [_I32, _PI32, _I32, _I32, _I32, _I32, _P, _P, _I32, _P, _P, _P,
                                                 _P, _I32, _P, _P]),
 }

@@ -713,6 +713,179 @@ int tt_log_likelihood(tt_plan *p, const double *props, const double *freqs, int3
   return TT_OK;
 }
 
+}  // extern "C"
+
+namespace {
+
+// Whether plan p runs the default FP32 4-state kernels that a multi-plan
+// launch can merge: producer-warp post-order and in-place adjoint, one
+// pattern per thread in the post-order, the whole alignment resident.
+bool mergeable(const tt_plan *p) {
+  return p->precision == TT_PRECISION_F32 && !p->wide && p->S == 4 && !p->slab && p->producer_warp &&
+         !p->pair_threads && p->inplace_adjoint && p->nstage_f <= 8;
+}
+
+int check_multi(int32_t count, tt_plan *const *plans, const double *const *props, const double *const *freqs) {
+  if (count < 1 || !plans || !props || !freqs) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument or empty plan list");
+  for (int i = 0; i < count; ++i) {
+    if (!plans[i] || !props[i] || !freqs[i]) return fail(TT_ERR_INVALID_ARGUMENT, "NULL plan or argument");
+    for (int j = 0; j < i; ++j)
+      if (plans[j] == plans[i]) return fail(TT_ERR_INVALID_ARGUMENT, "a plan appears twice in one call");
+    const int rc = check_device(plans[i]);
+    if (rc) return rc;
+  }
+  return TT_OK;
+}
+
+// Groups of up to kMaxMultiPlans mergeable plans with one category-pair count
+// (and, for the adjoint, one adjoint kernel) among the plans `todo`.
+std::vector<std::vector<int>> merge_groups(const std::vector<int> &todo, tt_plan *const *plans, bool adjoint) {
+  std::vector<std::vector<int>> groups;
+  for (int i : todo) {
+    const tt_plan *p = plans[i];
+    bool placed = false;
+    for (auto &g : groups) {
+      const tt_plan *q = plans[g[0]];
+      if (int(g.size()) < tt::kMaxMultiPlans && tt::kpairs_for(q->K) == tt::kpairs_for(p->K) &&
+          (!adjoint || q->pair_adjoint == p->pair_adjoint)) {
+        g.push_back(i);
+        placed = true;
+        break;
+      }
+    }
+    if (!placed) groups.push_back({i});
+  }
+  return groups;
+}
+
+}  // namespace
+
+extern "C" {
+
+int tt_plans_log_likelihood(int32_t count, tt_plan *const *plans, const double *const *category_weights,
+                            const double *const *frequencies, int32_t rescale, int32_t keep_partials,
+                            double *const *log_likelihood, void *stream) {
+  int rc = check_multi(count, plans, category_weights, frequencies);
+  if (rc) return rc;
+  if (!log_likelihood) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::vector<int> merge;
+  for (int i = 0; i < count; ++i) {
+    tt_plan *p = plans[i];
+    if (!log_likelihood[i]) return fail(TT_ERR_INVALID_ARGUMENT, "NULL log_likelihood");
+    if (!p->tips_set) return fail(TT_ERR_NOT_READY, "tt_plan_set_tips has not been called");
+    if (!p->pmat_set) return fail(TT_ERR_NOT_READY, "transition matrices have not been set");
+    if (mergeable(p) && (!keep_partials || p->d_partials)) {
+      merge.push_back(i);
+    } else {  // other kernel shapes: the plan's own call
+      rc = tt_log_likelihood(p, category_weights[i], frequencies[i], rescale, keep_partials, log_likelihood[i],
+                             nullptr, stream);
+      if (rc) return rc;
+    }
+  }
+  constexpr int TPC = tt::kTlWsPatterns / tt::kTlTile;  // stored tiles per post-order CTA
+  for (const auto &g : merge_groups(merge, plans, false)) {
+    tt::MultiPrune<float> m;
+    std::memset(&m, 0, sizeof m);
+    m.count = int(g.size());
+    size_t smem = 0;
+    long long total = 0;
+    for (int k = 0; k < m.count; ++k) {
+      tt_plan *p = plans[g[k]];
+      auto a = make_args<float>(p, category_weights[g[k]], frequencies[g[k]], rescale ? 1 : 0, keep_partials != 0,
+                                nullptr);
+      a.slots = p->slots_ws;
+      m.a[k] = a;
+      m.first[k] = int(total);
+      m.per_sample[k] = (p->ntiles_f + TPC - 1) / TPC;
+      total += (long long)m.per_sample[k] * p->batch;
+      smem = std::max(smem, tt::tl_ws_smem_bytes(p->K, p->C, p->slots_ws, p->nstage_f));
+    }
+    if (total > 0x7fffffffll) return fail(TT_ERR_UNSUPPORTED, "too many CTAs for one merged launch");
+    m.first[m.count] = int(total);
+    cudaError_t e = tt::launch_forward_multi(m, int(total), smem, s);
+    if (e != cudaSuccess) return cuda_fail(e, "merged post-order launch");
+    for (int k = 0; k < m.count; ++k) {
+      tt_plan *p = plans[g[k]];
+      e = tt::launch_reduce_lnl(p->d_tile_lnl, log_likelihood[g[k]], p->batch, p->ntiles_f, 0, s);
+      if (e != cudaSuccess) return cuda_fail(e, "likelihood reduction launch");
+      p->launches += 1;
+      p->last_rescale = rescale ? 1 : 0;
+      p->partials_valid = keep_partials != 0;
+    }
+    plans[g[0]]->launches += 1;  // the merged post-order, counted once
+  }
+  return TT_OK;
+}
+
+int tt_plans_gradient(int32_t count, tt_plan *const *plans, const double *const *category_weights,
+                      const double *const *frequencies, double *const *grad_frequencies,
+                      double *const *grad_weights, void *stream) {
+  int rc = check_multi(count, plans, category_weights, frequencies);
+  if (rc) return rc;
+  cudaStream_t s = static_cast<cudaStream_t>(stream);
+  std::vector<int> merge;
+  for (int i = 0; i < count; ++i) {
+    tt_plan *p = plans[i];
+    double *gf = grad_frequencies ? grad_frequencies[i] : nullptr;
+    double *gw = grad_weights ? grad_weights[i] : nullptr;
+    if (!p->partials_valid)
+      return fail(TT_ERR_NOT_READY,
+                  "tt_plans_gradient needs a preceding log-likelihood with keep_partials=1 for the same matrices");
+    if (mergeable(p) && p->d_partials && p->d_gpart && p->d_rootpart) {
+      merge.push_back(i);
+    } else {
+      rc = tt_gradient(p, category_weights[i], frequencies[i], nullptr, gf, gw, stream);
+      if (rc) return rc;
+    }
+  }
+  for (const auto &g : merge_groups(merge, plans, true)) {
+    tt::MultiPrune<float> m;
+    std::memset(&m, 0, sizeof m);
+    m.count = int(g.size());
+    size_t smem = 0;
+    long long total = 0;
+    const bool pair = plans[g[0]]->pair_adjoint && tt::pair_adjoint_supported(plans[g[0]]->K);
+    for (int k = 0; k < m.count; ++k) {
+      tt_plan *p = plans[g[k]];
+      auto a = make_args<float>(p, category_weights[g[k]], frequencies[g[k]], 1, true, nullptr);
+      a.slots = p->slots_bwd;
+      a.nstage = p->nstage_b;
+      a.ntiles = (p->N + p->tile_b - 1) / p->tile_b;
+      a.site_lnl = nullptr;
+      m.a[k] = a;
+      m.first[k] = int(total);
+      m.per_sample[k] = a.ntiles;
+      total += (long long)a.ntiles * p->batch;
+      smem = std::max(smem, pair ? tt::tp_smem_bytes(p->K, p->C, p->nstage_b) : tt::ta_smem_bytes(p->K, p->C, p->nstage_b));
+    }
+    if (total > 0x7fffffffll) return fail(TT_ERR_UNSUPPORTED, "too many CTAs for one merged launch");
+    m.first[m.count] = int(total);
+    cudaError_t e = tt::launch_adjoint_multi(m, int(total), smem, pair, s);
+    if (e != cudaSuccess) return cuda_fail(e, "merged adjoint launch");
+    plans[g[0]]->launches += 1;
+    for (int k = 0; k < m.count; ++k) {
+      const int i = g[k];
+      tt_plan *p = plans[i];
+      const int ntiles = m.per_sample[k];
+      e = tt::launch_reduce_f32(static_cast<const float *>(p->d_gpart), static_cast<const float *>(p->d_rootpart),
+                                p->d_G, p->d_rootgrad, p->d_rootgrad + size_t(p->batch) * p->S, p->batch, p->B, ntiles,
+                                p->S, p->K, 0, s);
+      if (e == cudaSuccess && grad_frequencies && grad_frequencies[i])
+        e = cudaMemcpyAsync(grad_frequencies[i], p->d_rootgrad, size_t(p->batch) * p->S * sizeof(double),
+                            cudaMemcpyDeviceToDevice, s);
+      if (e == cudaSuccess && grad_weights && grad_weights[i])
+        e = cudaMemcpyAsync(grad_weights[i], p->d_rootgrad + size_t(p->batch) * p->S,
+                            size_t(p->batch) * p->K * sizeof(double), cudaMemcpyDeviceToDevice, s);
+      if (e != cudaSuccess) return cuda_fail(e, "merged adjoint reductions");
+      p->launches += 2;
+      p->partials_valid = false;  // the outside partials overwrote the post-order tiles
+      p->grads_valid = true;
+    }
+  }
+  return TT_OK;
+}
+
 int tt_gradient(tt_plan *p, const double *props, const double *freqs, double *grad_matrices,
                 double *grad_frequencies, double *grad_weights, void *stream) {
   if (!p || !props || !freqs) return fail(TT_ERR_INVALID_ARGUMENT, "NULL argument");

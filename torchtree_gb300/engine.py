@@ -211,3 +211,54 @@ class LikelihoodEngine:
                              ("category rates", r, (b, K))):
             if tuple(t.shape) != shp:
                 raise ValueError(f"{name} must have shape {shp}, got {tuple(t.shape)}")
+
+
+def _ptr_array(values):
+    arr = (ctypes.c_void_p * len(values))()
+    for i, v in enumerate(values):
+        arr[i] = ptr(v).value if v is not None else None
+    return arr
+
+
+def plans_log_likelihood(engines, props, freqs, rescale: bool = True, keep_partials: bool = False):
+    """lnL ``[b_i]`` of several engines in one C-ABI call (``tt_plans_log_likelihood``):
+    plans on the default FP32 4-state kernels share one post-order launch;
+    each result equals that engine's own ``log_likelihood``."""
+    if not engines:
+        return []
+    lib = engines[0].lib
+    p = [e._per_sample(x, e.category_count) for e, x in zip(engines, props)]
+    f = [e._per_sample(x, e.state_count) for e, x in zip(engines, freqs)]
+    outs = [torch.empty(e.batch, dtype=torch.float64, device=e.device) for e in engines]
+    plans = (ctypes.c_void_p * len(engines))(*[e._plan for e in engines])
+    with torch.cuda.device(engines[0].device):
+        check(lib.tt_plans_log_likelihood(len(engines), plans, _ptr_array(p), _ptr_array(f), int(rescale),
+                                          int(keep_partials), _ptr_array(outs), _stream()))
+    for e, pi, fi in zip(engines, p, f):
+        if keep_partials:
+            e.token += 1
+        e._root_inputs = (pi, fi)
+    return outs
+
+
+def plans_gradient(engines, props, freqs):
+    """``[(dlnL/dpi [b,S], dlnL/dc [b,K])]`` of several engines in one call
+    (``tt_plans_gradient``); dlnL/dP stays in each plan for
+    ``rate_matrix_gradient``."""
+    if not engines:
+        return []
+    lib = engines[0].lib
+    p = [e._per_sample(x, e.category_count) for e, x in zip(engines, props)]
+    f = [e._per_sample(x, e.state_count) for e, x in zip(engines, freqs)]
+    kw = [dict(dtype=torch.float64, device=e.device) for e in engines]
+    dpi = [torch.empty(e.batch, e.state_count, **k) for e, k in zip(engines, kw)]
+    dc = [torch.empty(e.batch, e.category_count, **k) for e, k in zip(engines, kw)]
+    plans = (ctypes.c_void_p * len(engines))(*[e._plan for e in engines])
+    with torch.cuda.device(engines[0].device):
+        check(lib.tt_plans_gradient(len(engines), plans, _ptr_array(p), _ptr_array(f), _ptr_array(dpi),
+                                    _ptr_array(dc), _stream()))
+    for e in engines:
+        if e.state_count != 4 or e.precision == "f32":
+            e.token += 1
+    return list(zip(dpi, dc))
+
