@@ -464,9 +464,9 @@ def run_serving(args):
         lik = lik_cache[name]
         prep = serving.host_prepare(serving.Dataset(name, topo, ca, S, spec), p)
         dev = lik.device
-        x = [prep[k].to(dev).unsqueeze(0) for k in ("lam", "u", "w", "bls", "rates", "probs", "pi")]
+        q, bls_, r_, p_, pi_ = (prep[k].to(dev).unsqueeze(0) for k in ("q", "bls", "rates", "probs", "pi"))
         lik.rescale = True
-        lnl = lik.evaluate_eigen(*x)
+        lnl = lik.evaluate_rate_matrix(q, pi_, bls_, r_, p_, pi_)
         lnl.sum().backward()
         torch.cuda.synchronize()
     fp64_rate = len(sample) / (time.perf_counter() - t2)
@@ -477,7 +477,9 @@ def run_serving(args):
         "value": len(futs) / wall, "unit": "requests/s", "higher_is_better": True, "n_gpus": 1,
         "latency_ms": {"p50": stats.get("p50_ms"), "p99": stats.get("p99_ms"), "mean": stats.get("mean_ms")},
         "offered_rate": rate, "capacity_closed_loop": capacity, "requests": len(futs),
-        "batches": stats.get("batches"), "admissions": stats.get("admissions"), "evictions": stats.get("evictions"),
+        "batches": stats.get("batches"), "launches": stats.get("launches"),
+        "requests_per_launch": stats.get("requests_per_launch"),
+        "admissions": stats.get("admissions"), "evictions": stats.get("evictions"),
         "setup_s": setup_s, "dtype": "f32",
         "fp64_one_at_a_time": {"value": fp64_rate, "unit": "requests/s", "sample": len(sample),
                                "what": "PhyloLikelihood FP64, batch 1, eager, sequential"},

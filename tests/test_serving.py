@@ -2,8 +2,9 @@
 that are the same alone and in a mix.
 
 The scheduler tests run on the CPU with stand-in executors; the end-to-end
-test (``gpu``) serves three resident data sets (two DNA, one amino-acid)
-through captured CUDA graphs.
+test (``gpu``) serves four resident data sets (three DNA, one of them held in
+pattern slabs, and one amino-acid) alone through captured CUDA graphs and in
+a mix with the DNA work merged across data sets.
 """
 import threading
 import time
@@ -111,9 +112,12 @@ def _datasets():
                                 site_model="weibull", shape=0.8, branch_mean=0.05)
     w3 = synthetic.protein_workload("p1", tip_count=15, site_count=120, batch=6, seed=43, site_model="gamma",
                                     shape=0.5)
+    w4 = synthetic.dna_workload("s1", tip_count=45, site_count=2500, batch=6, seed=44, model="gtr",
+                                site_model="gamma", shape=0.7, branch_mean=0.05)
     for name, w, spec, dt in (("d1", w1, serving.ModelSpec("gtr"), datatype.Nucleotide()),
                               ("d2", w2, serving.ModelSpec("gtr", site_model="weibull"), datatype.Nucleotide()),
-                              ("p1", w3, serving.ModelSpec("general"), datatype.AminoAcid())):
+                              ("p1", w3, serving.ModelSpec("general"), datatype.AminoAcid()),
+                              ("s1", w4, serving.ModelSpec("gtr"), datatype.Nucleotide())):
         ca = patterns.compress(w.sequences, dt)
         reqs = [{"branch_lengths": w.branch_lengths[i], "exch": w.exch[i], "pi": w.pi[i], "shape": w.shape[i]}
                 for i in range(w.branch_lengths.shape[0])]
@@ -123,26 +127,38 @@ def _datasets():
 
 @pytest.mark.gpu
 def test_results_same_alone_and_in_the_mix():
+    """Each request's result is the same served alone through its data set's
+    own captured graph and served in a mix where the DNA data sets' work goes
+    out as merged steps (one post-order and one adjoint launch over all their
+    tiles).  Data set "s1" is held in pattern slabs of 512 (the path a data set
+    too large for the memory budget takes) in both runs."""
     import torch
 
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
     data = _datasets()
 
-    def make():
-        srv = serving.LikelihoodServer(slots=4, precision="f32")
+    def make(merge):
+        dev = torch.device("cuda", torch.cuda.current_device())
+
+        def factory(ds, slab=0):
+            return serving.GraphExecutor(ds, 4, "f32", dev, tune=False, slab=512 if ds.name == "s1" else slab,
+                                         merge=merge)
+
+        srv = serving.LikelihoodServer(slots=4, precision="f32", executor_factory=factory, merge=merge,
+                                       hbm_budget=int(0.5 * torch.cuda.mem_get_info()[0]), device=dev)
         for name, (topo, ca, S, spec, _) in data.items():
             srv.add_dataset(name, topo, ca, S, spec)
         return srv.start()
 
     alone = {}
-    srv = make()
+    srv = make(merge=False)
     for name, (_, _, _, _, reqs) in data.items():
         for i, p in enumerate(reqs):
             alone[(name, i)] = srv.submit(name, p).result(timeout=300)
     srv.stop()
 
-    srv = make()
+    srv = make(merge=True)
     futs = {}
     rng = np.random.default_rng(0)
     keys = [(name, i) for name, d in data.items() for i in range(len(d[4]))]
@@ -163,6 +179,7 @@ def test_results_same_alone_and_in_the_mix():
     stats = srv.latency_stats()
     srv.stop()
     assert stats["count"] == len(keys) and stats["p99_ms"] >= stats["p50_ms"] > 0
+    assert stats["requests_per_launch"] > 1.0, stats
     for k in keys:
         a, b = alone[k], mixed[k]
         assert np.isfinite(a["lnl"])

@@ -11,6 +11,12 @@ chain -- as one captured CUDA graph on the data set's own stream:
   requests (up to ``slots``) as soon as its previous batch has left the GPU;
   requests that arrive while a batch is in flight wait only for that batch,
   and batches of different data sets run concurrently on their streams;
+* same-level work merged across data sets: the waiting batches of every
+  FP32 4-state data set go out as one step, whose post-order and adjoint are
+  each ONE launch over the pattern tiles of all those trees and alignments
+  (``tt_plans_log_likelihood`` / ``tt_plans_gradient``: per-CTA arguments
+  name each CTA's plan, sample and tile); other data sets (20 / 61 states,
+  pattern slabs) run their own captured graphs;
 * admission by HBM footprint: a data set's plan is created only when its
   workspace fits the budget, evicting idle plans (least recently used)
   otherwise; requests of a data set that does not fit wait.  A data set
@@ -24,11 +30,12 @@ chain -- as one captured CUDA graph on the data set's own stream:
   kernels are deterministic.
 
 The rate-matrix construction and the site model stay in torch on the host
-(FP64, autograd), as in ``PhyloLikelihood``; the graph receives the eigen
-system of the normalised Q, branch lengths, category rates and weights
-through pinned host buffers and returns dlnL/dQ (matrix-exponential
-derivative), branch-length, rate, weight and frequency gradients, which the
-host chains back to the request's parameters.
+(FP64, autograd), as in ``PhyloLikelihood``; the step receives the
+normalised Q, branch lengths, category rates and weights through pinned
+host buffers, forms the eigen system on the device (Jacobi kernel) and
+returns dlnL/dQ (matrix-exponential derivative), branch-length, rate, weight
+and frequency gradients, which the host chains back to the request's
+parameters.
 """
 from __future__ import annotations
 
@@ -42,7 +49,7 @@ import numpy as np
 import torch
 
 from . import _native, autotune, site_models, substitution
-from .engine import LikelihoodEngine
+from .engine import LikelihoodEngine, plans_gradient, plans_log_likelihood
 from .patterns import CompressedAlignment
 from .tree import Topology
 
@@ -99,7 +106,6 @@ def host_prepare(ds: Dataset, params: dict) -> dict:
     pi = torch.tensor(np.asarray(params["pi"], dtype=np.float64), dtype=f64, requires_grad=True)
     shape = torch.tensor(np.asarray(params["shape"], dtype=np.float64).reshape(1), dtype=f64, requires_grad=True)
     q = substitution.normalise(rate_matrix(ds.spec, exch, pi, ds.state_count), pi)
-    lam, u, w = substitution.eigen_of_normalised(q.detach(), pi.detach())
     K = ds.spec.categories
     if ds.spec.site_model == "gamma":
         rates, probs = site_models.gamma_rates(shape, K)
@@ -108,7 +114,7 @@ def host_prepare(ds: Dataset, params: dict) -> dict:
     probs = probs.expand(K)
     bl = np.asarray(params["branch_lengths"], dtype=np.float64)
     bls = np.concatenate([bl, [0.0]]) if bl.shape[-1] == 2 * ds.topology.tip_count - 3 else bl
-    return {"leaves": (exch, pi, shape), "q": q, "lam": lam, "u": u, "w": w, "rates": rates, "probs": probs, "pi": pi,
+    return {"leaves": (exch, pi, shape), "q": q, "rates": rates, "probs": probs, "pi": pi,
             "bls": torch.tensor(bls, dtype=f64), "free": bl.shape[-1]}
 
 
@@ -163,19 +169,25 @@ class GraphExecutor:
     """One admitted data set: plan, stream, static buffers, captured step."""
 
     def __init__(self, ds: Dataset, slots: int, precision: str, device, use_graph: bool = True,
-                 tune: bool = True, slab: int = 0):
+                 tune: bool = True, slab: int = 0, merge: bool = False):
         self.ds = ds
         self.slots = slots
         self.device = device
         T, S, K = ds.topology.tip_count, ds.state_count, ds.spec.categories
+        # FP32 4-state plans with the whole alignment resident run in merged
+        # steps (one post-order and one adjoint launch for many data sets) on
+        # the default kernel shapes, without a graph of their own
+        self.mergeable = merge and S == 4 and precision == "f32" and not slab
+        if self.mergeable:
+            use_graph, tune = False, False
         B = 2 * T - 2
         self.engine = LikelihoodEngine(ds.topology.postorder, T, S, K, ds.alignment.codes, ds.alignment.table,
                                        ds.alignment.weights, batch=slots, precision=precision, device=device)
         if slab:  # partials held one pattern slab at a time (before tuning and capture)
             self.engine.set_option(_native.TT_OPT_SLAB_PATTERNS, slab)
         kw = dict(dtype=torch.float64, device=device)
-        eye = torch.eye(S, **kw).expand(slots, S, S).contiguous()
-        self.inputs = {"lam": torch.zeros(slots, S, **kw), "u": eye.clone(), "w": eye.clone(),
+        jc = torch.full((S, S), 1.0 / (S - 1), **kw) - torch.eye(S, **kw) * (S / (S - 1))  # a valid placeholder Q
+        self.inputs = {"q": jc.expand(slots, S, S).contiguous(),
                        "bls": torch.full((slots, B), 0.1, **kw), "rates": torch.ones(slots, K, **kw),
                        "props": torch.full((slots, K), 1.0 / K, **kw), "pi": torch.full((slots, S), 1.0 / S, **kw)}
         self.host_in = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in self.inputs.items()}
@@ -200,22 +212,28 @@ class GraphExecutor:
 
     def _step(self) -> dict:
         e, x = self.engine, self.inputs
-        e.set_eigen(x["lam"], x["u"], x["w"], x["bls"], x["rates"])
+        lam, u, w = substitution.device_eigen(x["q"], x["pi"])  # FP64 Jacobi kernel, no host round trip
+        e.set_eigen(lam, u, w, x["bls"], x["rates"])
         lnl = e.log_likelihood(x["props"], x["pi"], rescale=True, keep_partials=True)
         _, dpi, dc = e.gradient(x["props"], x["pi"])
-        dq, dt, dr = e.rate_matrix_gradient(x["lam"], x["u"], x["w"], x["bls"], x["rates"])
+        dq, dt, dr = e.rate_matrix_gradient(lam, u, w, x["bls"], x["rates"])
         return {"lnl": lnl, "dpi": dpi, "dc": dc, "dq": dq, "dt": dt, "dr": dr}
 
-    def launch(self, reqs: list) -> None:
+    def fill(self, reqs: list) -> list:
+        """Host side of a batch: each request's engine inputs into the pinned
+        input buffers (idle slots repeat the last request)."""
         preps = [host_prepare(self.ds, r.params) for r in reqs]
-        for name, key in (("lam", "lam"), ("u", "u"), ("w", "w"), ("bls", "bls"), ("rates", "rates"),
-                          ("props", "probs"), ("pi", "pi")):
+        for name, key in (("q", "q"), ("bls", "bls"), ("rates", "rates"), ("props", "probs"), ("pi", "pi")):
             buf = self.host_in[name]
             for s in range(self.slots):
                 buf[s].copy_(preps[min(s, len(preps) - 1)][key].detach())
         now = time.perf_counter()
         for r in reqs:
             r.t_launch = now
+        return preps
+
+    def launch(self, reqs: list) -> None:
+        preps = self.fill(reqs)
         with torch.cuda.device(self.device), torch.cuda.stream(self.stream):
             for k, v in self.inputs.items():
                 v.copy_(self.host_in[k], non_blocking=True)
@@ -252,12 +270,51 @@ class GraphExecutor:
         self.engine.close()
 
 
+def merged_step(batches: list, stream, device) -> None:
+    """Launch the batches of several mergeable executors as one step on
+    ``stream``: their inputs in, eigen systems and transition matrices per
+    data set, then ONE post-order and ONE adjoint launch over the tiles of all
+    of them (``tt_plans_log_likelihood`` / ``tt_plans_gradient``), the
+    rate-matrix chain per data set, results out.  ``batches``:
+    ``[(executor, requests)]``.  Each request's result equals what its data
+    set's own step gives."""
+    preps = [ex.fill(reqs) for ex, reqs in batches]
+    execs = [ex for ex, _ in batches]
+    event = torch.cuda.Event()
+    with torch.cuda.device(device), torch.cuda.stream(stream):
+        eig = []
+        for ex in execs:
+            x = ex.inputs
+            for k, v in x.items():
+                v.copy_(ex.host_in[k], non_blocking=True)
+            lam, u, w = substitution.device_eigen(x["q"], x["pi"])
+            eig.append((lam, u, w))
+            ex.engine.set_eigen(lam, u, w, x["bls"], x["rates"])
+        engines = [ex.engine for ex in execs]
+        props = [ex.inputs["props"] for ex in execs]
+        pis = [ex.inputs["pi"] for ex in execs]
+        lnls = plans_log_likelihood(engines, props, pis, rescale=True, keep_partials=True)
+        grads = plans_gradient(engines, props, pis)
+        for ex, lnl, (dpi, dc), (lam, u, w) in zip(execs, lnls, grads, eig):
+            x = ex.inputs
+            dq, dt, dr = ex.engine.rate_matrix_gradient(lam, u, w, x["bls"], x["rates"])
+            ex.outputs = {"lnl": lnl, "dpi": dpi, "dc": dc, "dq": dq, "dt": dt, "dr": dr}
+            for k, v in ex.outputs.items():
+                ex.host_out[k].copy_(v, non_blocking=True)
+        event.record(stream)
+    for (ex, reqs), pr in zip(batches, preps):
+        ex.event = event
+        ex.busy = True
+        ex.batch = (reqs, pr)
+
+
 class LikelihoodServer:
     """Persistent request loop over resident data sets (see the module docstring)."""
 
     def __init__(self, slots: int = 8, precision: str = "f32", device=None, hbm_budget: int | None = None,
-                 use_graphs: bool = True, tune: bool = True, executor_factory=None):
+                 use_graphs: bool = True, tune: bool = True, executor_factory=None, merge: bool = True):
         self.slots = slots
+        self.merge = merge
         self.precision = precision
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         if hbm_budget is None and executor_factory is None:
@@ -266,7 +323,7 @@ class LikelihoodServer:
         self.budget = hbm_budget
         self.factory = executor_factory or (lambda ds, slab=0: GraphExecutor(ds, slots, precision, self.device,
                                                                              use_graph=use_graphs, tune=tune,
-                                                                             slab=slab))
+                                                                             slab=slab, merge=merge))
         self.estimate = (lambda ds: estimate_bytes(ds, slots, precision))
         self.slab_fit = (lambda ds, room: slab_fit(ds, slots, precision, room))
         self.datasets: dict = {}
@@ -277,6 +334,8 @@ class LikelihoodServer:
         self.admissions = 0
         self.evictions = 0
         self.batches = 0
+        self.launches = 0  # merged steps plus single-data-set steps
+        self.merge_stream = None
         self._queue: queue.Queue = queue.Queue()
         self._stop = threading.Event()
         self._thread = None
@@ -318,7 +377,9 @@ class LikelihoodServer:
             return {"count": 0}
         return {"count": int(lat.size), "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
-                "batches": self.batches, "admissions": self.admissions, "evictions": self.evictions}
+                "batches": self.batches, "launches": self.launches,
+                "requests_per_launch": int(lat.size) / max(self.launches, 1),
+                "admissions": self.admissions, "evictions": self.evictions}
 
     # -------------------------------------------------------------- scheduler
     def _admit(self, name: str):
@@ -370,6 +431,7 @@ class LikelihoodServer:
                 break
             self.pending.setdefault(r.dataset, []).append(r)
         order = sorted((reqs[0].t_submit, n) for n, reqs in self.pending.items() if reqs)
+        merged = []
         for _, name in order:
             ex = self.executors.get(name)
             if ex is None:
@@ -379,9 +441,18 @@ class LikelihoodServer:
             if not ex.busy:
                 reqs = self.pending[name][: self.slots]
                 del self.pending[name][: len(reqs)]
-                ex.launch(reqs)
+                if getattr(ex, "mergeable", False):
+                    merged.append((ex, reqs))
+                else:
+                    ex.launch(reqs)
+                    self.launches += 1
                 self.batches += 1
                 progressed = True
+        if merged:  # every ready 4-state data set in one step
+            if self.merge_stream is None:
+                self.merge_stream = torch.cuda.Stream(self.device)
+            merged_step(merged, self.merge_stream, self.device)
+            self.launches += 1
         return progressed
 
     def _busy(self) -> bool:
