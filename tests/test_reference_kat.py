@@ -10,18 +10,21 @@ lnL = -4618.2062529058 with and without rescaling.  Here the same chain runs
 through this package's Newick parser, tip-date heights and pattern
 compression and the oracle's ratio transform and pruning, which pins the
 oracle's time-tree, clock and Weibull chain to the reference's own number.
-The source location comes from ``tests/reference_models.py``; the tests are
-skipped where the data are absent.
+The data come from the reference source tree where it is present
+(``tests/reference_models.py``) and otherwise from ``tests/golden/flua.json``,
+which ``tests/golden/make_flua.py`` wrote from that source tree: the names,
+the Newick tree and the alignment as compressed by torchtree's own
+``compress_alignment``; its columns, each repeated by its weight, make an
+alignment with the same site patterns and weights.
 """
 import numpy as np
 import pytest
 import torch
 
+from tests.conftest import GOLDEN
 from tests.reference_models import DATA, fixed_tree_class, import_torchtree
 
 KAT = -4618.2062529058
-
-pytestmark = pytest.mark.skipif(not (DATA / "fluA.fa").exists(), reason="reference data not present")
 
 
 def _fasta(path):
@@ -36,6 +39,19 @@ def _fasta(path):
     return names, ["".join(s) for s in seqs]
 
 
+def _flua():
+    """(taxon names, sequences, Newick) of the reference's influenza A data."""
+    if (DATA / "fluA.fa").exists():
+        names, seqs = _fasta(DATA / "fluA.fa")
+        return names, seqs, (DATA / "fluA.tree").read_text().strip()
+    import json
+
+    d = json.loads((GOLDEN / "flua.json").read_text())
+    reps = np.asarray(d["weights"])
+    seqs = ["".join(np.repeat(np.array(list(p)), reps)) for p in d["patterns"]]
+    return d["names"], seqs, d["newick"]
+
+
 def _sampling_times(names):
     """Leaf heights from the dates that end the taxon names (tree_model.py:363-378)."""
     dates = np.array([float(n.split("_")[-1]) for n in names])
@@ -48,8 +64,8 @@ def test_flu_a_time_tree_weibull_strict_clock_known_answer():
     from torchtree_gb300 import patterns
     from torchtree_gb300.tree import Topology
 
-    names, seqs = _fasta(DATA / "fluA.fa")
-    topo = Topology.from_newick((DATA / "fluA.tree").read_text().strip(), names)
+    names, seqs, newick = _flua()
+    topo = Topology.from_newick(newick, names)
     T = topo.tip_count
     assert T == 69
     times = _sampling_times(names)
@@ -104,8 +120,8 @@ def test_flu_a_known_answer_through_the_gpu_path():
     from torchtree_gb300.timetree import TimeTree
     from torchtree_gb300.tree import Topology
 
-    names, seqs = _fasta(DATA / "fluA.fa")
-    topo = Topology.from_newick((DATA / "fluA.tree").read_text().strip(), names)
+    names, seqs, newick = _flua()
+    topo = Topology.from_newick(newick, names)
     times = _sampling_times(names)
     ratios, heights = _ratios_from_newick(topo, times)
     dev = torch.device("cuda")
@@ -154,8 +170,8 @@ def test_flu_a_gradients_of_the_oracle_chain_match_torchtree():
     from torchtree_gb300 import patterns
     from torchtree_gb300.tree import Topology
 
-    names, seqs = _fasta(DATA / "fluA.fa")
-    topo = Topology.from_newick((DATA / "fluA.tree").read_text().strip(), names)
+    names, seqs, newick = _flua()
+    topo = Topology.from_newick(newick, names)
     times = _sampling_times(names)
     ratios, _ = _ratios_from_newick(topo, times)
     _, lengths, _ = OT.ratio_transform(topo.postorder_list(), times.tolist(), ratios)
