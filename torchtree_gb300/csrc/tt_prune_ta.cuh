@@ -341,146 +341,71 @@ __device__ __forceinline__ void ta_backward_body(const PruneArgs<float> &a, cons
 
     // reduction over the tile's patterns, register-blocked:
     //   G[c][k][i][jj] = sum_p (coef x_c)[p][i][k] * v_c[p][jj][k]
-    // UR lanes own the 4x4 blocks of one (child, category pair) and each
-    // accumulates the block over its own patterns.
+    // UR lanes own the 4x4 blocks of one (child, category pair) over patterns
+    // s, s+UR, ...; recursive halving across the UR lanes leaves each lane NV
+    // consecutive floats of the block's 32, written straight to HBM.
     {
       const int unit = tid / UR, sidx = tid - unit * UR;
       const bool uact = unit < UNITS;
       const int c = unit / KQ, t = unit - (unit / KQ) * KQ;
-      const bool tipc = c ? rtip : ltip;
-      float2 *xs = xbuf + c * KQ * 4 * P + t * 4 * P;  // pair t rows of child c (this unit's alone)
-      const float2 *vs = (c ? kidr : kidl) + t * 4 * P;
-      const unsigned char *csd = stg + G.codes + c * P;
       float2 acc[4][4];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) acc[i][jj] = make_float2(0.0f, 0.0f);
-      if constexpr (UR == 8 || UR == 16) {
-        // Patterns two at a time (16-byte loads of adjacent patterns), then
-        // the UR partial blocks summed column-wise through this unit's own
-        // region of xbuf (its 2 KB hold UR rows of 32 floats; 16-byte chunks
-        // XOR-swizzled by row against bank conflicts).  Fixed summation order.
-        if (uact) {
-#pragma unroll 1
-          for (int m = 2 * sidx; m < rem; m += 2 * UR) {
-            const bool two = m + 1 < rem;
-            float2 v0[4], v1[4];
-            if (tipc) {
-              const float4 *r0 = reinterpret_cast<const float4 *>(tab2 + int(csd[m]) * 4);
-              const float4 *r1 = reinterpret_cast<const float4 *>(tab2 + int(csd[two ? m + 1 : m]) * 4);
-              const float4 a0 = r0[0], a1 = r0[1], b0 = r1[0], b1 = r1[1];
-              v0[0] = make_float2(a0.x, a0.y), v0[1] = make_float2(a0.z, a0.w);
-              v0[2] = make_float2(a1.x, a1.y), v0[3] = make_float2(a1.z, a1.w);
-              v1[0] = make_float2(b0.x, b0.y), v1[1] = make_float2(b0.z, b0.w);
-              v1[2] = make_float2(b1.x, b1.y), v1[3] = make_float2(b1.z, b1.w);
-            } else {
-#pragma unroll
-              for (int jj = 0; jj < 4; ++jj) {
-                const float4 vv = *reinterpret_cast<const float4 *>(vs + jj * P + m);
-                v0[jj] = make_float2(vv.x, vv.y);
-                v1[jj] = make_float2(vv.z, vv.w);
-              }
-            }
-            if (!two)  // the partner pattern is padding: its x is zero, keep its v finite
-#pragma unroll
-              for (int jj = 0; jj < 4; ++jj) v1[jj] = make_float2(0.0f, 0.0f);
-#pragma unroll
-            for (int i = 0; i < 4; ++i) {
-              const float4 xi = *reinterpret_cast<const float4 *>(xs + i * P + m);
-              const float2 x0 = make_float2(xi.x, xi.y), x1 = make_float2(xi.z, xi.w);
-#pragma unroll
-              for (int jj = 0; jj < 4; ++jj) {
-                acc[i][jj] = __ffma2_rn(x0, v0[jj], acc[i][jj]);
-                acc[i][jj] = __ffma2_rn(x1, v1[jj], acc[i][jj]);
-              }
-            }
-          }
-        }
-        __syncwarp();  // every lane of the warp has read its unit's rows of xbuf
-        // block float e: category 2t + (e >> 4), element (i, jj) = e & 15;
-        // row sidx of the unit's partial table, chunk k (floats 4k..4k+3) at k ^ (sidx & 7)
-        float4 *tab = reinterpret_cast<float4 *>(xs);
-        if (uact) {
-#pragma unroll
-          for (int k = 0; k < 8; ++k) {
-            const int e = 4 * k;  // floats e..e+3: category (e >> 4), elements e & 15 .. +3
-            const int i = (e & 15) >> 2;
-            const float4 v = (e >> 4) == 0 ? make_float4(acc[i][0].x, acc[i][1].x, acc[i][2].x, acc[i][3].x)
-                                           : make_float4(acc[i][0].y, acc[i][1].y, acc[i][2].y, acc[i][3].y);
-            tab[sidx * 8 + (k ^ (sidx & 7))] = v;
-          }
-        }
-        __syncwarp();
-        if (uact) {
-          constexpr int OUT = 32 / UR;  // floats summed by each lane: 2 or 4
-          const int e0 = OUT * sidx, k = e0 >> 2, off = e0 & 3;
-          float2 s0 = make_float2(0.0f, 0.0f), s1 = make_float2(0.0f, 0.0f);
-#pragma unroll
-          for (int r = 0; r < UR; ++r) {
-            const float *row = reinterpret_cast<const float *>(tab + r * 8 + (k ^ (r & 7)));
-            s0 = __fadd2_rn(s0, *reinterpret_cast<const float2 *>(row + off));
-            if (OUT == 4) s1 = __fadd2_rn(s1, *reinterpret_cast<const float2 *>(row + 2));
-          }
-          const int branch = c ? right : left;
-          float *dst = a.gpart + ((size_t(b) * a.branch_count + branch) * a.ntiles + tile) * KSS + 32 * t;
-          if (2 * t + (e0 >> 4) < K) {
-            *reinterpret_cast<float2 *>(dst + e0) = s0;
-            if (OUT == 4) *reinterpret_cast<float2 *>(dst + e0 + 2) = s1;
-          }
-        }
-      } else {
-        if (uact) {
+      if (uact) {
+        const bool tipc = c ? rtip : ltip;
+        const float2 *xs = xbuf + c * KQ * 4 * P + t * 4 * P;  // pair t rows
+        const float2 *vs = (c ? kidr : kidl) + t * 4 * P;
+        const unsigned char *csd = stg + G.codes + c * P;
 #pragma unroll 4
-          for (int m = sidx; m < rem; m += UR) {
-            float2 x[4], v[4];
+        for (int m = sidx; m < rem; m += UR) {
+          float2 x[4], v[4];
 #pragma unroll
-            for (int i = 0; i < 4; ++i) x[i] = xs[i * P + m];
-            if (tipc) {
-              const float4 *tr = reinterpret_cast<const float4 *>(tab2 + int(csd[m]) * 4);
-              const float4 t0 = tr[0], t1 = tr[1];
-              v[0] = make_float2(t0.x, t0.y);
-              v[1] = make_float2(t0.z, t0.w);
-              v[2] = make_float2(t1.x, t1.y);
-              v[3] = make_float2(t1.z, t1.w);
-            } else {
+          for (int i = 0; i < 4; ++i) x[i] = xs[i * P + m];
+          if (tipc) {
+            const float4 *tr = reinterpret_cast<const float4 *>(tab2 + int(csd[m]) * 4);
+            const float4 t0 = tr[0], t1 = tr[1];
+            v[0] = make_float2(t0.x, t0.y);
+            v[1] = make_float2(t0.z, t0.w);
+            v[2] = make_float2(t1.x, t1.y);
+            v[3] = make_float2(t1.z, t1.w);
+          } else {
 #pragma unroll
-              for (int jj = 0; jj < 4; ++jj) v[jj] = vs[jj * P + m];
-            }
-#pragma unroll
-            for (int i = 0; i < 4; ++i)
-#pragma unroll
-              for (int jj = 0; jj < 4; ++jj) acc[i][jj] = __ffma2_rn(x[i], v[jj], acc[i][jj]);
+            for (int jj = 0; jj < 4; ++jj) v[jj] = vs[jj * P + m];
           }
+#pragma unroll
+          for (int i = 0; i < 4; ++i)
+#pragma unroll
+            for (int jj = 0; jj < 4; ++jj) acc[i][jj] = __ffma2_rn(x[i], v[jj], acc[i][jj]);
         }
-        // recursive halving across the UR lanes leaves each lane NV
-        // consecutive floats of the block's 32, written straight to HBM
-        float f[32];
+      }
+      // block float e: category 2t + (e >> 4), element (i, jj) = e & 15
+      float f[32];
 #pragma unroll
-        for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < 4; ++i)
 #pragma unroll
-          for (int jj = 0; jj < 4; ++jj) {
-            f[i * 4 + jj] = acc[i][jj].x;
-            f[16 + i * 4 + jj] = acc[i][jj].y;
-          }
-#pragma unroll
-        for (int o = UR / 2, h = 16; o >= 1; o >>= 1, h >>= 1) {
-          const bool up = (lane & o) != 0;
-#pragma unroll
-          for (int e = 0; e < h; ++e) {
-            const float send = up ? f[e] : f[e + h];
-            const float keep = up ? f[e + h] : f[e];
-            f[e] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-          }
+        for (int jj = 0; jj < 4; ++jj) {
+          f[i * 4 + jj] = acc[i][jj].x;
+          f[16 + i * 4 + jj] = acc[i][jj].y;
         }
-        if (uact) {
-          const int branch = c ? right : left;
-          float *dst = a.gpart + ((size_t(b) * a.branch_count + branch) * a.ntiles + tile) * KSS + 32 * t;
 #pragma unroll
-          for (int e = 0; e < NV; ++e) {
-            const int fe = NV * sidx + e;
-            if (2 * t + (fe >> 4) < K) dst[fe] = f[e];
-          }
+      for (int o = UR / 2, h = 16; o >= 1; o >>= 1, h >>= 1) {
+        const bool up = (lane & o) != 0;
+#pragma unroll
+        for (int e = 0; e < h; ++e) {
+          const float send = up ? f[e] : f[e + h];
+          const float keep = up ? f[e + h] : f[e];
+          f[e] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+        }
+      }
+      if (uact) {
+        const int branch = c ? right : left;
+        float *dst = a.gpart + ((size_t(b) * a.branch_count + branch) * a.ntiles + tile) * KSS + 32 * t;
+#pragma unroll
+        for (int e = 0; e < NV; ++e) {
+          const int fe = NV * sidx + e;
+          if (2 * t + (fe >> 4) < K) dst[fe] = f[e];
         }
       }
     }
