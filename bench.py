@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--serving-chains", type=int, default=256)
     ap.add_argument("--serving-requests", type=int, default=1024)
     ap.add_argument("--serving-slots", type=int, default=4)
+    ap.add_argument("--serving-merge-depth", type=int, default=2,
+                    help="merged DNA steps in flight at once (0: no merging, one graph per data set)")
     ap.add_argument("--serving-max-tips", type=int, default=2000)
     ap.add_argument("--serving-max-sites", type=int, default=50000)
     ap.add_argument("--timetree", action="store_true",
@@ -409,7 +411,8 @@ def run_serving(args):
     mix = serving_mix(args, rng)
     chains = [(c % len(mix), chain_params(rng, mix[c % len(mix)][1], mix[c % len(mix)][3]))
               for c in range(args.serving_chains)]
-    srv = serving.LikelihoodServer(slots=args.serving_slots, precision="f32")
+    srv = serving.LikelihoodServer(slots=args.serving_slots, precision="f32", merge=args.serving_merge_depth > 0,
+                                   merge_depth=max(1, args.serving_merge_depth))
     for name, topo, ca, S, spec in mix:
         srv.add_dataset(name, topo, ca, S, spec)
     srv.start()
@@ -475,10 +478,13 @@ def run_serving(args):
     line = {
         "metric": "serving lnL+grad requests/s, Poisson mix over resident data sets, 1 GB300; p50/p99 latency",
         "value": len(futs) / wall, "unit": "requests/s", "higher_is_better": True, "n_gpus": 1,
-        "latency_ms": {"p50": stats.get("p50_ms"), "p99": stats.get("p99_ms"), "mean": stats.get("mean_ms")},
+        "latency_ms": {"p50": stats.get("p50_ms"), "p99": stats.get("p99_ms"), "mean": stats.get("mean_ms"),
+                       "queue_wait_p50": stats.get("wait_p50_ms"), "service_p50": stats.get("service_p50_ms")},
         "offered_rate": rate, "capacity_closed_loop": capacity, "requests": len(futs),
         "batches": stats.get("batches"), "launches": stats.get("launches"),
         "requests_per_launch": stats.get("requests_per_launch"),
+        "merged_steps": stats.get("merged_steps"), "requests_per_merged_step": stats.get("requests_per_merged_step"),
+        "merge_host_ms_per_step": stats.get("merge_host_ms_per_step"), "merge_depth": args.serving_merge_depth,
         "admissions": stats.get("admissions"), "evictions": stats.get("evictions"),
         "setup_s": setup_s, "dtype": "f32",
         "fp64_one_at_a_time": {"value": fp64_rate, "unit": "requests/s", "sample": len(sample),
@@ -755,8 +761,10 @@ def main():
                 "kernels": kernels}
     if S != 4:  # amino-acid / codon: level-scheduled kernels; algorithmic flops of the products
         s_flop = 2 * S * S * K * N * b  # one S x S matrix applied to one category's patterns
-        fw_flops = I * 2 * s_flop
-        bw_flops = 2 * fw_flops + (2 * T - 2) * s_flop
+        fw_flops = I * 2 * s_flop  # the two children's products of every internal node
+        # adjoint: P^T u for every internal child (outside partials) and sum_p u x^T for every
+        # branch (gradient blocks); the children's products come from the post-order
+        bw_flops = ((I - 1) + (2 * T - 2)) * s_flop
         for name, fl in (("post_order", fw_flops), ("pre_order_adjoint", bw_flops)):
             kernels[name]["flops"] = fl
             kernels[name]["tflops"] = fl / kernels[name]["ms"] / 1e9
@@ -766,6 +774,12 @@ def main():
             "unit": "TFLOP/s", "frac": kernels["post_order"]["tflops"] / tflops_peak,
             "what": "codon post-order as split-TF32 tcgen05 MMAs (3 MMAs per product, counted once); "
                     "peak = measured dense BF16 (TF32 runs at half that rate)"} if S > 20 else None
+        if S > 20 and args.precision == "f32" and eng.get_option(_native.TT_OPT_TENSOR_CORE_ADJOINT):
+            roofline["tensor_adjoint"] = {
+                "bound": "tensor", "achieved": kernels["pre_order_adjoint"]["tflops"], "peak": tflops_peak,
+                "unit": "TFLOP/s", "frac": kernels["pre_order_adjoint"]["tflops"] / tflops_peak,
+                "what": "codon adjoint as split-TF32 tcgen05 MMAs (outside partials and gradient blocks, "
+                        "3 MMAs per product, counted once); peak = measured dense BF16"}
     traffic_file = ROOT / "profiles" / "traffic.json"
     if traffic_file.exists():
         tr = json.loads(traffic_file.read_text()).get(args.workload, {}).get(dom)

@@ -398,6 +398,9 @@ int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
  *     does not fit in shared memory);
  *   TT_OPT_TENSOR_CORES: 1 = FP32 codon post-order on the tensor cores,
  *     0 = CUDA-core kernel;
+ *   TT_OPT_TENSOR_CORE_ADJOINT: 1 = FP32 codon adjoint on the tensor cores
+ *     (the default; holds split copies of the transition matrices, 32 KB per
+ *     sample, branch and category), 0 = CUDA-core kernel;
  *   TT_OPT_PAIR_THREADS: FP32 4-state kernels with one thread per (pattern,
  *     category pair) (1) or per pattern (0, the default);
  *   TT_OPT_PRODUCER_WARP: FP32 4-state post-order with a warp that only
@@ -433,7 +436,8 @@ enum {
   TT_OPT_PRODUCER_WARP = 5,
   TT_OPT_INPLACE_ADJOINT = 6,
   TT_OPT_SLAB_PATTERNS = 7,
-  TT_OPT_PAIR_ADJOINT = 8
+  TT_OPT_PAIR_ADJOINT = 8,
+  TT_OPT_TENSOR_CORE_ADJOINT = 9
 };
 int tt_plan_set_option(tt_plan *plan, int32_t option, int32_t value);
 int tt_plan_get_option(const tt_plan *plan, int32_t option, int32_t *value);

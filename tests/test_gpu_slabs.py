@@ -140,11 +140,11 @@ def _wide_problem(kind, precision):
     return wl.topology, ca, S, K, b, eig, probs.expand(b, K).to(dev).contiguous(), pi.to(dev)
 
 
-@pytest.mark.parametrize("kind,precision,tc", [
-    ("protein", "f64", None), ("protein", "f32", None),
-    ("codon", "f64", None), ("codon", "f32", 1), ("codon", "f32", 0),
+@pytest.mark.parametrize("kind,precision,tc,tca", [
+    ("protein", "f64", None, None), ("protein", "f32", None, None),
+    ("codon", "f64", None, None), ("codon", "f32", 1, 1), ("codon", "f32", 0, 1), ("codon", "f32", 1, 0),
 ])
-def test_wide_slabs_equal_the_whole_alignment(kind, precision, tc):
+def test_wide_slabs_equal_the_whole_alignment(kind, precision, tc, tca):
     """20- and 61-state plans run both passes slab by slab.  Per-pattern
     results (site lnL) are bit-identical; lnL differs by the grouping of its
     FP64 sum; gradients by the grouping of the chunk sums (FP64 plans 1e-12,
@@ -161,6 +161,9 @@ def test_wide_slabs_equal_the_whole_alignment(kind, precision, tc):
                            precision=precision)
     if tc is not None:
         eng.set_option(_native.TT_OPT_TENSOR_CORES, tc)
+    if tca is not None:
+        eng.set_option(_native.TT_OPT_TENSOR_CORE_ADJOINT, tca)
+        assert eng.get_option(_native.TT_OPT_TENSOR_CORE_ADJOINT) == tca
 
     def run(second=False):
         eng.set_eigen(*eig)

@@ -43,7 +43,7 @@ def _setup(wl):
         probs.expand(b, K).to(dev).contiguous(), pi.to(dev)
 
 
-def _run(wl, precision, tc=True, rescale=True, grads=True):
+def _run(wl, precision, tc=True, rescale=True, grads=True, tca=None):
     from torchtree_gb300.engine import LikelihoodEngine
 
     ca, S, K, b, eig, probs, pi = _setup(wl)
@@ -57,13 +57,18 @@ def _run(wl, precision, tc=True, rescale=True, grads=True):
             del os.environ["TT_WIDE_TC"]
         else:
             os.environ["TT_WIDE_TC"] = old
+    if tca is not None:
+        from torchtree_gb300 import _native
+
+        eng.set_option(_native.TT_OPT_TENSOR_CORE_ADJOINT, tca)
     eng.set_eigen(*eig)
     lnl = eng.log_likelihood(probs, pi, rescale=rescale, keep_partials=grads)
     out = {"lnl": lnl.cpu().numpy()}
     if grads:
         _, dpi, dc = eng.gradient(probs, pi)
         dlam, du, dw, dt, dr = eng.eigen_gradient(*eig)
-        out.update(dpi=dpi.cpu().numpy(), dt=dt.cpu().numpy())
+        out.update(dpi=dpi.cpu().numpy(), dc=dc.cpu().numpy(), dt=dt.cpu().numpy(), dr=dr.cpu().numpy(),
+                   dlam=dlam.cpu().numpy(), du=du.cpu().numpy(), dw=dw.cpu().numpy())
     assert eng.device_status() == 0
     return out
 
@@ -76,6 +81,27 @@ def test_codon_tensor_core_matches_cuda_core():
     c = _run(wl, "f32", tc=False)
     np.testing.assert_allclose(a["lnl"], c["lnl"], rtol=1e-6)  # split-TF32 products, FP32 tensor accumulation
     np.testing.assert_allclose(a["dt"], c["dt"], rtol=1e-4, atol=1e-4 * np.abs(c["dt"]).max())
+
+
+@pytest.mark.parametrize("tips,sites,batch,seed", [(40, 700, 2, 34), (7, 300, 3, 35)])
+def test_codon_tensor_core_adjoint_matches_cuda_core(tips, sites, batch, seed):
+    """The tcgen05 codon adjoint (split-TF32 GEMMs, 128-pattern tiles, outside
+    partials stored in place) against the CUDA-core adjoint on the same stored
+    post-order: every gradient within FP32 rounding of the largest entry, on a
+    tree deep enough to store outside partials and on one whose internal
+    children are few."""
+    from torchtree_gb300 import synthetic
+
+    wl = synthetic.codon_workload("c", tip_count=tips, site_count=sites, batch=batch, seed=seed, shape=0.5)
+    a = _run(wl, "f32", tca=1)
+    c = _run(wl, "f32", tca=0)
+    np.testing.assert_array_equal(a["lnl"], c["lnl"])  # the same post-order
+    for key in ("dt", "dpi", "dc", "dr", "dlam", "du", "dw"):
+        scale = np.abs(c[key]).max()
+        np.testing.assert_allclose(a[key], c[key], rtol=1e-4, atol=1e-4 * scale, err_msg=key)
+    d = _run(wl, "f64")
+    for key in ("dt", "dpi", "dr"):
+        np.testing.assert_allclose(a[key], d[key], rtol=1e-4, atol=1e-4 * np.abs(d[key]).max(), err_msg=key)
 
 
 def test_codon_fp32_against_fp64():

@@ -180,6 +180,7 @@ def test_results_same_alone_and_in_the_mix():
     srv.stop()
     assert stats["count"] == len(keys) and stats["p99_ms"] >= stats["p50_ms"] > 0
     assert stats["requests_per_launch"] > 1.0, stats
+    assert stats["merged_steps"] > 0 and stats["requests_per_merged_step"] > 1.0, stats
     for k in keys:
         a, b = alone[k], mixed[k]
         assert np.isfinite(a["lnl"])

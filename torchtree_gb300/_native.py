@@ -30,6 +30,7 @@ TT_OPT_FWD_STAGES, TT_OPT_BWD_STAGES, TT_OPT_TENSOR_CORES, TT_OPT_PAIR_THREADS, 
 TT_OPT_INPLACE_ADJOINT = 6
 TT_OPT_SLAB_PATTERNS = 7
 TT_OPT_PAIR_ADJOINT = 8
+TT_OPT_TENSOR_CORE_ADJOINT = 9
 
 SIGNATURES = {
     "tt_version": (ctypes.c_char_p, []),

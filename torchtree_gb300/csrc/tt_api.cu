@@ -1049,6 +1049,8 @@ int tt_plan_set_option(tt_plan *p, int32_t option, int32_t value) {
     }
     case TT_OPT_TENSOR_CORES:
       return tt::wide_set_tensor_cores(p, value != 0);
+    case TT_OPT_TENSOR_CORE_ADJOINT:
+      return tt::wide_set_tensor_core_adjoint(p, value != 0);
     case TT_OPT_PRODUCER_WARP:
       if (value && (p->wide || p->precision != TT_PRECISION_F32))
         return fail(TT_ERR_UNSUPPORTED, "the producer-warp post-order serves FP32 4-state plans");
@@ -1099,6 +1101,7 @@ int tt_plan_get_option(const tt_plan *p, int32_t option, int32_t *value) {
     case TT_OPT_FWD_STAGES: *value = p->nstage_f; return TT_OK;
     case TT_OPT_BWD_STAGES: *value = p->nstage_b; return TT_OK;
     case TT_OPT_TENSOR_CORES: *value = tt::wide_tensor_cores(p) ? 1 : 0; return TT_OK;
+    case TT_OPT_TENSOR_CORE_ADJOINT: *value = tt::wide_tensor_core_adjoint(p) ? 1 : 0; return TT_OK;
     case TT_OPT_PAIR_THREADS: *value = p->pair_threads ? 1 : 0; return TT_OK;
     case TT_OPT_PRODUCER_WARP: *value = p->producer_warp ? 1 : 0; return TT_OK;
     case TT_OPT_INPLACE_ADJOINT: *value = p->inplace_adjoint ? 1 : 0; return TT_OK;

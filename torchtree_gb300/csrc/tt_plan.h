@@ -79,6 +79,8 @@ int wide_matrices_gradient(tt_plan *p, const double *lam, const double *U, const
                            const double *rates, double *dlam, double *dU, double *dW, double *dbl,
                            double *drates, cudaStream_t s);
 int wide_set_tensor_cores(tt_plan *p, bool on);
+int wide_set_tensor_core_adjoint(tt_plan *p, bool on);
+bool wide_tensor_core_adjoint(const tt_plan *p);
 // dlnL/dQ, branch lengths and category rates from the plan's dlnL/dP (tt_qgrad.cu)
 int rate_matrix_gradient(tt_plan *p, const double *lam, const double *U, const double *W, const double *bl,
                          const double *rates, double *dQ, double *dbl, double *drates, cudaStream_t s);

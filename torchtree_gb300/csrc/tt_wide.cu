@@ -7,10 +7,13 @@
 #include <string>
 #include <vector>
 
+#include <cudaTypedefs.h>
+
 #include "../../include/torchtree_gb300.h"
 #include "tt_plan.h"
 #include "tt_wide.cuh"
 #include "tt_wide_tc.cuh"
+#include "tt_wide_tc_bwd.cuh"
 
 namespace tt {
 
@@ -69,6 +72,8 @@ struct WideState {
   int bchunk = 8, nbchunks = 1;
   bool tc = false;  // FP32 codon post-order on the tensor cores
   bool store_products = false;  // FP32 codon: the adjoint reads the post-order's children's products
+  bool tc_bwd = false;  // FP32 codon adjoint on the tensor cores (needs the stored products)
+  float *d_pimg = nullptr;  // its GEMM2 operands: split P^T images [b][B][K][2][64][64]
   // pattern slabs (p->slab != 0): the pattern-sized buffers below hold one
   // slab; tail_valid = they still hold the last slab's post-order (from a
   // tt_log_likelihood with keep_partials), which the gradient then reuses
@@ -115,6 +120,34 @@ WideGeo wide_geo(const tt_plan *p, int n) {
   return g;
 }
 
+// cuTensorMapEncodeTiled through the runtime's driver entry point (no libcuda link)
+PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  if (!fn) {
+    void *ptr = nullptr;
+    cudaDriverEntryPointQueryResult q = cudaDriverEntryPointSymbolNotFound;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &ptr, 12000, cudaEnableDefault, &q) ==
+            cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(ptr);
+  }
+  return fn;
+}
+
+// A row-major FP32 array [rows][cols] (cols a multiple of 4) as a 2-D tensor
+// map with bx x by boxes, no swizzle.
+bool encode_rows(CUtensorMap *m, const float *base, uint64_t rows, uint64_t cols, uint32_t bx, uint32_t by) {
+  const PFN_cuTensorMapEncodeTiled_v12000 fn = tensor_map_encoder();
+  if (!fn) return false;
+  const cuuint64_t dims[2] = {cols, rows};
+  const cuuint64_t strides[1] = {cols * sizeof(float)};
+  const cuuint32_t box[2] = {bx, by};
+  const cuuint32_t elem[2] = {1, 1};
+  return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides, box, elem,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
 int wcuda(cudaError_t e, const char *where) {
   return wfail(e == cudaErrorMemoryAllocation ? TT_ERR_OUT_OF_MEMORY : TT_ERR_CUDA,
                std::string(where) + ": " + cudaGetErrorString(e));
@@ -157,6 +190,11 @@ struct Wide {
       e = cudaFuncSetAttribute(wide_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tc::kSmem);
     if (std::is_same<T, float>::value && SP == 64 && e == cudaSuccess)  // two CTAs per SM
       e = cudaFuncSetAttribute(wide_forward_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
+                               int(cudaSharedmemCarveoutMaxShared));
+    if (std::is_same<T, float>::value && SP == 64 && e == cudaSuccess)
+      e = cudaFuncSetAttribute(wide_backward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, tcb::kSmem);
+    if (std::is_same<T, float>::value && SP == 64 && e == cudaSuccess)
+      e = cudaFuncSetAttribute(wide_backward_tc_kernel, cudaFuncAttributePreferredSharedMemoryCarveout,
                                int(cudaSharedmemCarveoutMaxShared));
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(wide_pmatrix_kernel<T, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -250,6 +288,9 @@ struct Wide {
     const WideGeo g = wide_geo(p, n);
     WideArgs<T> a = args(p, props, freqs, 1, g, p0, n);
     a.prod = static_cast<T *>(w.d_prod);
+    if constexpr (std::is_same<T, float>::value && SP == 64) {
+      if (w.tc_bwd && a.prod && w.d_pimg) return backward_tc(p, a, g, accumulate, s);
+    }
     constexpr int NT = WideCfg<T, SP, PTB>::NT;
     const size_t smem = wide_bwd_smem<T, SP, PTB>(a.prod != nullptr);
     for (size_t lv = 0; lv + 1 < w.bwd_off.size(); ++lv) {
@@ -263,6 +304,45 @@ struct Wide {
     wide_root_reduce_kernel<T><<<p->batch, 64, 0, s>>>(static_cast<const T *>(w.d_rootpart), p->d_rootgrad,
                                                        p->d_rootgrad + size_t(p->batch) * p->S, g.nchunks, p->K,
                                                        p->S, SP, accumulate);
+    p->launches += 2;
+    return cudaGetLastError();
+  }
+
+  // the tensor-core adjoint (FP32 codon plans): split P^T images, then one
+  // launch per depth level over chunks of 128-pattern tiles
+  static cudaError_t backward_tc(tt_plan *p, WideArgs<float> a, const WideGeo &g, int accumulate, cudaStream_t s) {
+    WideState &w = *p->wide;
+    const long long count = (long long)p->batch * p->B * p->K;
+    wide_pimage_kernel<<<unsigned((count * 4096 + 255) / 256), 256, 0, s>>>(static_cast<const float *>(p->d_pmat),
+                                                                         w.d_pimg, count);
+    p->launches += 1;
+    const int ntc = g.Npad / tcb::kPT;
+    const int want = (2 * 152 + p->batch * p->K - 1) / (p->batch * p->K);
+    const int cmax = std::max(1, std::min({want, ntc, g.cmax}));
+    const int tpc = (ntc + cmax - 1) / cmax;
+    a.ntiles = ntc;
+    a.tiles_per_chunk = tpc;
+    a.nchunks = (ntc + tpc - 1) / tpc;
+    // the raw rows as 2-D tensors: partials [b I K 64][Npad], products [b I K 128][Npad]
+    TcbMaps maps;
+    const uint64_t blocks = uint64_t(p->batch) * p->I * p->K;
+    if (!encode_rows(&maps.part32, a.part, blocks * 64, uint64_t(g.Npad), 32, 64) ||
+        !encode_rows(&maps.prod32, a.prod, blocks * 128, uint64_t(g.Npad), 32, 64) ||
+        !encode_rows(&maps.part128, a.part, blocks * 64, uint64_t(g.Npad), 128, 16) ||
+        !encode_rows(&maps.prod128, a.prod, blocks * 128, uint64_t(g.Npad), 128, 16))
+      return cudaErrorInvalidValue;
+    for (size_t lv = 0; lv + 1 < w.bwd_off.size(); ++lv) {
+      a.nodes = w.d_bwd + w.bwd_off[lv];
+      const dim3 grid(a.nchunks, w.bwd_off[lv + 1] - w.bwd_off[lv], p->batch * p->K);
+      wide_backward_tc_kernel<<<grid, tcb::kThreads, tcb::kSmem, s>>>(a, maps, w.d_pimg, p->d_status, 2000000000ull);
+      p->launches += 1;
+    }
+    wide_grad_reduce_kernel<float><<<dim3(p->B, p->batch), 256, 0, s>>>(static_cast<const float *>(w.d_gpart),
+                                                                         p->d_G, p->B, a.nchunks, p->K, p->S, 64,
+                                                                         accumulate);
+    wide_root_reduce_kernel<float><<<p->batch, 64, 0, s>>>(static_cast<const float *>(w.d_rootpart), p->d_rootgrad,
+                                                           p->d_rootgrad + size_t(p->batch) * p->S, a.nchunks, p->K,
+                                                           p->S, 64, accumulate);
     p->launches += 2;
     return cudaGetLastError();
   }
@@ -368,6 +448,10 @@ int wide_create(tt_plan *p) {
      // states the extra stores cost more than the products they save
     const char *env = getenv("TT_WIDE_STORE_PRODUCTS");
     w->store_products = f32 && SP == 64 && !(env && atoi(env) == 0);
+  }
+  {  // tensor-core adjoint for those plans (TT_WIDE_TC_BWD=0 selects the CUDA-core kernel)
+    const char *env = getenv("TT_WIDE_TC_BWD");
+    if (!rc && w->store_products && !(env && atoi(env) == 0)) rc = wide_set_tensor_core_adjoint(p, true);
   }
   // the pattern-sized buffers (partials, exponents, products, root and
   // gradient chunks) come from wide_alloc_slab once the slab size is chosen
@@ -478,11 +562,33 @@ int wide_set_tensor_cores(tt_plan *p, bool on) {
 
 bool wide_tensor_cores(const tt_plan *p) { return p->wide && p->wide->tc; }
 
+int wide_set_tensor_core_adjoint(tt_plan *p, bool on) {
+  WideState *w = p->wide;
+  if (!w || p->precision != TT_PRECISION_F32 || w->SP != 64 || !w->store_products)
+    return on ? wfail(TT_ERR_UNSUPPORTED,
+                      "the tensor-core adjoint serves FP32 codon (> 20-state) plans that keep the children's products")
+              : TT_OK;
+  if (on && !w->d_pimg) {  // the split P^T images: 32 KB per (sample, branch, category)
+    const size_t bytes = size_t(p->batch) * p->B * p->K * tcb::kImgFloats * sizeof(float);
+    const int rc = walloc(p, &w->d_pimg, bytes, "split transition-matrix images");
+    if (rc) return rc;
+  } else if (!on && w->d_pimg) {
+    cudaFree(w->d_pimg);
+    w->d_pimg = nullptr;
+    p->bytes -= std::min(p->bytes, size_t(p->batch) * p->B * p->K * tcb::kImgFloats * sizeof(float));
+  }
+  w->tc_bwd = on;
+  return TT_OK;
+}
+
+bool wide_tensor_core_adjoint(const tt_plan *p) { return p->wide && p->wide->tc_bwd; }
+
 void wide_destroy(tt_plan *p) {
   WideState *w = p->wide;
   if (!w) return;
   void *bufs[] = {w->d_left, w->d_right, w->d_fwd, w->d_bwd, w->d_part, w->d_expo, w->d_root_site, w->d_root_expo,
-                  w->d_log2L, w->d_block_lnl, w->d_gpart, w->d_rootpart, w->d_pgpart, w->d_prod, w->d_site};
+                  w->d_log2L, w->d_block_lnl, w->d_gpart, w->d_rootpart, w->d_pgpart, w->d_prod, w->d_site,
+                  w->d_pimg};
   for (void *x : bufs)
     if (x) cudaFree(x);
   delete w;

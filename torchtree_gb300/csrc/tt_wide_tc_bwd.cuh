@@ -1,0 +1,560 @@
+// Codon (SP = 64) adjoint on the 5th-generation tensor cores.
+//
+// One CTA = (chunk of pattern tiles, node v, sample b x category k), 256
+// threads; a tile is 128 patterns.  For each side c of v (child c, the other
+// child c') and tile:
+//   u_c[i][p] = pre_v[i][p] * (P_c' x_c')[i][p]   (outside partial of v times
+//                                                  the other side's product,
+//                                                  stored by the post-order)
+//   GEMM3  G_c[i][j] += sum_p u_c[i][p] (coef_p x_c[j][p])   M = 64 (i),
+//          N = 64 (j), K = patterns, accumulated in tensor memory over all
+//          tiles of the chunk;
+//   GEMM2  o_c[p][j]  = sum_i u_c[i][p] P_c[i][j]             M = 128
+//          (patterns), N = 64 (j), K = 64 (i), for internal children only:
+//          the child's outside partial, rescaled by the power of two of its
+//          per-pattern maximum and stored over the child's post-order partial
+//          (which GEMM3 of the same side has already staged).
+// Both are tcgen05.mma kind::tf32 with the split-TF32 scheme (operands as
+// big + small, three products per K-step) of wide_forward_tc_kernel, and the
+// same K-major no-swizzle operand layout (8-row x 16-byte core matrices, SBO
+// = 128 B between 8-row groups, LBO between 4-element K groups).
+//
+// The work of a tile is a sequence of units: per side, four GEMM3 units of
+// 32 patterns (K = 32) and, for an internal child, four GEMM2 units of 16
+// states (K = 16), then the side's epilogue.  The CTA (one per SM) is warp
+// specialised: a control warp issues each unit's raw rows (tiles of the
+// pattern-contiguous partial and product rows) as 2-D bulk tensor copies
+// into a ring of four raw slots, and the MMAs of each converted unit; sixteen
+// converter warps turn a unit's raw rows into its MMA operands (products,
+// TF32 split, K-major stores) in a ring of three operand slots and run the
+// epilogues.  Full / empty mbarriers per slot order the roles; the
+// converters meet at a named barrier only at epilogues and tile ends.
+// GEMM2's B operand, P_c transposed into the operand layout and split, is
+// written once per (sample, branch, category) by wide_pimage_kernel; the
+// control warp brings a GEMM2 unit's 16-state slice in with two 4 KB bulk
+// copies.
+//
+// Accumulator layouts in tensor memory (cta_group::1): for M = 128 row m is
+// lane m; for M = 64 rows 16q .. 16q + 15 are lanes 32q .. 32q + 15
+// (q = 0..3); column n is column n in both.  A warp reads the 32 lanes of
+// its quarter (warp id mod 4).
+#pragma once
+
+#include <cuda.h>
+
+#include "tt_wide_tc.cuh"
+
+namespace tt {
+
+namespace tcb {
+
+constexpr int kPT = 128;                  // patterns per tile (GEMM2 M)
+constexpr int kConv = 512;                // converter threads (16 warps)
+constexpr int kThreads = kConv + 32;      // + the control warp
+constexpr int kKC3 = 32;                  // patterns (K) per GEMM3 unit
+constexpr int kKC2 = 16;                  // states (K) per GEMM2 unit
+constexpr int kU3 = kPT / kKC3;           // GEMM3 units per side and tile
+constexpr int kU2 = 64 / kKC2;            // GEMM2 units per internal side and tile
+constexpr int kOpSlot = 32768;            // one unit's operands (A big, A small, B big, B small)
+constexpr int kNS = 3;                    // operand slots
+constexpr int kRawSlot = 24576;           // one unit's raw rows: three 8 KB tensor tiles
+constexpr int kNR = 4;                    // raw slots
+constexpr int kMeta = kPT * 16 + 2 * kPT; // a tile's coefficients, exponents and tip codes
+constexpr int kOffRaw = kNS * kOpSlot;
+constexpr int kOffMeta = kOffRaw + kNR * kRawSlot;
+constexpr int kOffMraw = kOffMeta + 2 * kMeta;  // the next tile's weights and site log2 L (FP64) as copied
+constexpr int kOffRed = kOffMraw + 2 * kPT * 8; // float [4][128]
+constexpr int kOffRoot = kOffRed + 4 * kPT * 4; // float [512] root partial sums
+constexpr int kOffBar = kOffRoot + kConv * 4;
+// mbarriers: raw full / empty [kNR], operand full / empty [kNS], image [kNS], accumulator full / empty, done
+constexpr int kBars = 2 * kNR + 3 * kNS + 3;
+constexpr int kSmem = kOffBar + 8 * kBars + 16;
+constexpr uint32_t kTmemCols = 256;       // G_l [0, 64), G_r [64, 128), o [128, 192)
+constexpr int kImgFloats = 2 * 64 * 64;   // one P^T image: big then small
+
+}  // namespace tcb
+
+// P^T images for GEMM2: image m (sample, branch, category) holds P_m^T in the
+// K-major layout (row j, K element i, LBO = 1024 B) as TF32 big then small.
+// One thread per output float (coalesced stores).
+__global__ void __launch_bounds__(256) wide_pimage_kernel(const float *pmat, float *img, long long count) {
+  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= count * 4096) return;
+  const long long m = t >> 12;
+  const int o = int(t & 4095);
+  // o (a float index) -> byte offset 4o = (i >> 2) * 1024 + (j >> 3) * 128 + (j & 7) * 16 + (i & 3) * 4
+  const int byte = 4 * o;
+  const int i = (byte >> 10) * 4 + ((byte & 15) >> 2);
+  const int j = ((byte & 1023) >> 7) * 8 + ((byte & 127) >> 4);
+  float big, small;
+  tc::split_tf32(pmat[m * 4096 + i * 64 + j], big, small);
+  img[m * tcb::kImgFloats + o] = big;
+  img[m * tcb::kImgFloats + 4096 + o] = small;
+}
+
+__device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
+
+__device__ __forceinline__ void split4_store(unsigned char *big, unsigned char *small, float4 v) {
+  float4 hb, hs;
+  tc::split_tf32(v.x, hb.x, hs.x);
+  tc::split_tf32(v.y, hb.y, hs.y);
+  tc::split_tf32(v.z, hb.z, hs.z);
+  tc::split_tf32(v.w, hb.w, hs.w);
+  *reinterpret_cast<float4 *>(big) = hb;
+  *reinterpret_cast<float4 *>(small) = hs;
+}
+
+__device__ __forceinline__ void cp_async16(void *dst, const void *src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async4(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async8(void *dst, const void *src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(smem_u32(dst)), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// 2-D bulk tensor copy of the box at (x, y) of `map` into shared memory,
+// completion counted on `bar`.  x (the pattern coordinate) is a multiple of
+// 32 floats, so the copy starts on a 128-byte boundary.
+__device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
+      ::"r"(smem_u32(dst)), "l"(map), "r"(x), "r"(y), "r"(smem_u32(bar))
+      : "memory");
+}
+
+// A tile's per-pattern data in shared memory.
+struct TcbMeta {
+  float *cf;              // [128] w_p 2^(Ep + El + Er - log2 L_p)
+  int *el, *er, *ep;      // [128] exponents of x_l, x_r and of v's outside partial
+  unsigned char *codes;   // [2][128] tip codes of the left / right child
+};
+
+__device__ __forceinline__ TcbMeta tcb_meta(unsigned char *base) {
+  TcbMeta m;
+  m.cf = reinterpret_cast<float *>(base);
+  m.el = reinterpret_cast<int *>(base + 512);
+  m.er = m.el + 128;
+  m.ep = m.er + 128;
+  m.codes = base + 2048;
+  return m;
+}
+
+// Tensor maps of the adjoint's raw rows: the partials [b][I][K][64][Npad]
+// and the children's products [b][I][K][2][64][Npad] as 2-D arrays of rows,
+// with 32-pattern x 64-row boxes (GEMM3 units) and 128-pattern x 16-row
+// boxes (GEMM2 units).
+struct TcbMaps {
+  CUtensorMap part32, prod32, part128, prod128;
+};
+
+// Barrier among the converter warps (named barrier 1) that also ORs a
+// failure flag across them.
+__device__ __forceinline__ bool conv_sync_any(bool flag) {
+  uint32_t r;
+  asm volatile(
+      "{\n\t.reg .pred p, q;\n\t"
+      "setp.ne.u32 p, %1, 0;\n\t"
+      "bar.red.or.pred q, 1, %2, p;\n\t"
+      "selp.u32 %0, 1, 0, q;\n\t}"
+      : "=r"(r)
+      : "r"(flag ? 1u : 0u), "n"(tcb::kConv)
+      : "memory");
+  return r != 0;
+}
+
+// Adjoint level kernel for FP32 codon plans: a.tiles_per_chunk / a.ntiles /
+// a.nchunks count 128-pattern tiles.
+__global__ void __launch_bounds__(tcb::kThreads, 1)
+    wide_backward_tc_kernel(const WideArgs<float> a, const __grid_constant__ TcbMaps maps, const float *pimg,
+                            int *status, unsigned long long timeout_ns) {
+  using namespace tcb;
+  constexpr int SP = 64, PT = kPT;
+  extern __shared__ __align__(128) unsigned char smem[];
+  float *red = reinterpret_cast<float *>(smem + kOffRed);
+  float *rsum = reinterpret_cast<float *>(smem + kOffRoot);
+  uint64_t *raw_full = reinterpret_cast<uint64_t *>(smem + kOffBar);  // [kNR] count 1 + bytes
+  uint64_t *raw_empty = raw_full + kNR;                                // [kNR] 16 converter warps
+  uint64_t *op_full = raw_empty + kNR;                                 // [kNS] 16 converter warps
+  uint64_t *op_empty = op_full + kNS;                                  // [kNS] MMA commit
+  uint64_t *img_full = op_empty + kNS;                                 // [kNS] count 1 + bytes
+  uint64_t *acc_full = img_full + kNS;                                 // MMA commit: a side's GEMM2 done
+  uint64_t *acc_empty = acc_full + 1;                                  // 16 converter warps: o read
+  uint64_t *done = acc_empty + 1;                                      // MMA commit: every MMA done
+  uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int v = a.nodes[blockIdx.y];
+  const int b = blockIdx.z / a.K, k = blockIdx.z - (blockIdx.z / a.K) * a.K;
+  const int chunk = blockIdx.x;
+  const int l = a.left[v - a.tips], r = a.right[v - a.tips];
+  const bool is_root = v == 2 * a.tips - 2;
+  const double wk = a.props[size_t(b) * a.K + k];
+  const size_t npad = size_t(a.Npad);
+  const int vblk = ((b * a.I + (v - a.tips)) * a.K + k);  // v's (b, node, k) block of 64 rows
+  const bool int0 = l >= a.tips, int1 = r >= a.tips;
+  const int lblk = int0 ? (b * a.I + (l - a.tips)) * a.K + k : 0;
+  const int rblk = int1 ? (b * a.I + (r - a.tips)) * a.K + k : 0;
+  const int t0 = chunk * a.tiles_per_chunk, t1 = min(a.ntiles, t0 + a.tiles_per_chunk);
+  const int per_side0 = kU3 + (int0 ? kU2 : 0), per_side1 = kU3 + (int1 ? kU2 : 0);
+  const int total = (t1 - t0) * (per_side0 + per_side1);
+
+  struct Cur {  // a unit: tile index tt, side, index within the side's units
+    int tt, side, rr;
+  };
+  auto advance = [&](Cur &c) {
+    if (++c.rr == (c.side ? per_side1 : per_side0)) {
+      c.rr = 0;
+      if (c.side) ++c.tt;
+      c.side ^= 1;
+    }
+  };
+
+  if (warp == 0) tc::tmem_alloc(tslot, kTmemCols);
+  if (tid == kConv) {
+    for (int i = 0; i < 2 * kNR; ++i) mbar_init(&raw_full[i], i < kNR ? 1 : 16);
+    for (int i = 0; i < kNS; ++i) {
+      mbar_init(&op_full[i], 16);
+      mbar_init(&op_empty[i], 1);
+      mbar_init(&img_full[i], 1);
+    }
+    mbar_init(acc_full, 1);
+    mbar_init(acc_empty, 16);
+    mbar_init(done, 1);
+    fence_barrier_init();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = *tslot;
+
+  if (warp == kConv / 32) {
+    // ------------------------------------------------------------ control warp
+    if (lane == 0) {
+      const float *img0 = pimg + ((size_t(b) * a.B + l) * a.K + k) * kImgFloats;
+      const float *img1 = pimg + ((size_t(b) * a.B + r) * a.K + k) * kImgFloats;
+      if (int0) bulk_prefetch_l2(img0, uint32_t(kImgFloats * sizeof(float)));
+      if (int1) bulk_prefetch_l2(img1, uint32_t(kImgFloats * sizeof(float)));
+      uint32_t ph_re = 0xFu, ph_of = 0, ph_oe = 0x7u, ph_img = 0, pend_rf = 0, pend_img = 0;
+      uint32_t ph_ae = 1u, started = 0;
+      bool ok = true;
+      Cur ct{0, 0, 0}, cm{0, 0, 0};  // next unit to copy / to multiply
+      int ut = 0;
+      for (int u = 0; u < total && ok; ++u) {
+        // keep the raw ring full: units up to u + kNR - 1
+        for (; ut < total && ut < u + kNR && ok; ++ut) {
+          const int rs = ut % kNR;
+          ok = mbar_wait_bounded(&raw_empty[rs], ph_re >> rs & 1u, timeout_ns);  // converters read it
+          if (!ok) break;
+          ph_re ^= 1u << rs;
+          unsigned char *raw = smem + kOffRaw + rs * kRawSlot;
+          const int n0 = (t0 + ct.tt) * PT, oblk = vblk * 2 + (1 - ct.side);
+          if (ct.rr < kU3) {
+            const int x = n0 + ct.rr * kKC3;
+            const bool xin = ct.side ? int1 : int0;
+            mbar_arrive_expect_tx(&raw_full[rs], uint32_t(8192 * (1 + (is_root ? 0 : 1) + (xin ? 1 : 0))));
+            tma_load_2d(raw, &maps.prod32, x, oblk * SP, &raw_full[rs]);
+            if (!is_root) tma_load_2d(raw + 8192, &maps.part32, x, vblk * SP, &raw_full[rs]);
+            if (xin) tma_load_2d(raw + 16384, &maps.part32, x, (ct.side ? rblk : lblk) * SP, &raw_full[rs]);
+          } else {
+            const int y = (ct.rr - kU3) * kKC2;
+            mbar_arrive_expect_tx(&raw_full[rs], uint32_t(8192 * (1 + (is_root ? 0 : 1))));
+            tma_load_2d(raw, &maps.prod128, n0, oblk * SP + y, &raw_full[rs]);
+            if (!is_root) tma_load_2d(raw + 8192, &maps.part128, n0, vblk * SP + y, &raw_full[rs]);
+          }
+          pend_rf |= 1u << rs;
+          advance(ct);
+        }
+        if (!ok) break;
+        pend_rf &= ~(1u << (u % kNR));  // the converters wait for unit u's copies before arriving below
+        const int sl = u % kNS, side = cm.side, rr = cm.rr;
+        const bool g2 = rr >= kU3;
+        const int idx = g2 ? rr - kU3 : rr;
+        ok = mbar_wait_bounded(&op_empty[sl], ph_oe >> sl & 1u, timeout_ns);  // the slot's last MMAs are done
+        if (!ok) break;
+        ph_oe ^= 1u << sl;
+        unsigned char *op = smem + sl * kOpSlot;
+        if (g2) {  // the unit's 16-state slice of the P^T image, big and small
+          mbar_arrive_expect_tx(&img_full[sl], 8192u);
+          const float *src = (side ? img1 : img0) + idx * 1024;  // K groups 4 idx .. 4 idx + 3: 4 KB per half
+          bulk_copy_g2s(op + 16384, src, 4096u, &img_full[sl]);
+          bulk_copy_g2s(op + 20480, src + 4096, 4096u, &img_full[sl]);
+          pend_img |= 1u << sl;
+        }
+        ok = mbar_wait_bounded(&op_full[sl], ph_of >> sl & 1u, timeout_ns);  // the converters wrote it
+        if (!ok) break;
+        ph_of ^= 1u << sl;
+        tc::fence_after_sync();
+        const uint32_t sb = smem_u32(op);
+        if (!g2) {
+          constexpr uint32_t idesc = tc::idesc_tf32(64, 64);
+          const uint32_t d = tmem + uint32_t(64 * side);
+#pragma unroll
+          for (int kk = 0; kk < kKC3 / 8; ++kk) {
+            const uint64_t dab = tc::smem_desc(sb + kk * 2048, 1024, 128), das = tc::smem_desc(sb + 8192 + kk * 2048, 1024, 128);
+            const uint64_t dbb = tc::smem_desc(sb + 16384 + kk * 2048, 1024, 128),
+                           dbs = tc::smem_desc(sb + 24576 + kk * 2048, 1024, 128);
+            tc::mma_tf32(d, dab, dbb, idesc, ((started >> side & 1u) || kk > 0) ? 1u : 0u);
+            tc::mma_tf32(d, dab, dbs, idesc, 1u);
+            tc::mma_tf32(d, das, dbb, idesc, 1u);
+          }
+          started |= 1u << side;
+          tc::mma_commit(&op_empty[sl]);
+        } else {
+          ok = mbar_wait_bounded(&img_full[sl], ph_img >> sl & 1u, timeout_ns);
+          if (!ok) break;
+          ph_img ^= 1u << sl;
+          pend_img &= ~(1u << sl);
+          if (idx == 0) {  // the previous epilogue has read o
+            ok = mbar_wait_bounded(acc_empty, ph_ae, timeout_ns);
+            if (!ok) break;
+            ph_ae ^= 1u;
+            tc::fence_after_sync();
+          }
+          constexpr uint32_t idesc = tc::idesc_tf32(128, 64);
+#pragma unroll
+          for (int kk = 0; kk < kKC2 / 8; ++kk) {
+            const uint64_t dab = tc::smem_desc(sb + kk * 4096, 2048, 128), das = tc::smem_desc(sb + 8192 + kk * 4096, 2048, 128);
+            const uint64_t dbb = tc::smem_desc(sb + 16384 + kk * 2048, 1024, 128),
+                           dbs = tc::smem_desc(sb + 20480 + kk * 2048, 1024, 128);
+            tc::mma_tf32(tmem + 128u, dab, dbb, idesc, (idx > 0 || kk > 0) ? 1u : 0u);
+            tc::mma_tf32(tmem + 128u, dab, dbs, idesc, 1u);
+            tc::mma_tf32(tmem + 128u, das, dbb, idesc, 1u);
+          }
+          tc::mma_commit(&op_empty[sl]);
+          if (idx == kU2 - 1) tc::mma_commit(acc_full);  // the side's o is complete
+        }
+        advance(cm);
+      }
+      tc::mma_commit(done);  // every MMA issued so far
+      if (!ok) {
+        atomicExch(status, kDeviceTimeout);
+        for (int rs = 0; rs < kNR; ++rs)  // copies in flight land before the CTA exits
+          if (pend_rf >> rs & 1u) mbar_wait_bounded(&raw_full[rs], (ph_re >> rs & 1u) ^ 1u, 100000000ull);
+        for (int sl = 0; sl < kNS; ++sl)
+          if (pend_img >> sl & 1u) mbar_wait_bounded(&img_full[sl], ph_img >> sl & 1u, 100000000ull);
+      }
+    }
+    __syncwarp();
+  } else {
+    // ------------------------------------------------------------ converter warps
+    double *mw = reinterpret_cast<double *>(smem + kOffMraw), *ml2 = mw + PT;
+    auto fetch_meta = [&](int t, TcbMeta m) {  // cp.async into buffer m (pattern tid; codes four per copy)
+      const int n = t * PT + (tid & (PT - 1));
+      if (tid < PT) {
+        if (!is_root) cp_async4(&m.ep[tid], a.expo + size_t(vblk) * npad + n);
+        if (int0) cp_async4(&m.el[tid], a.expo + size_t(lblk) * npad + n);
+        if (int1) cp_async4(&m.er[tid], a.expo + size_t(rblk) * npad + n);
+        if (n < a.N) cp_async8(&mw[tid], a.weights + n);
+        cp_async8(&ml2[tid], a.log2L + size_t(b) * npad + n);
+      } else if (tid < PT + 64) {
+        const int sd = (tid - PT) >> 5, t4 = (tid - PT) & 31;
+        if (!(sd ? int1 : int0))
+          cp_async4(m.codes + sd * PT + 4 * t4, a.codes + size_t(sd ? r : l) * a.code_stride + t * PT + 4 * t4);
+      }
+      cp_async_commit();
+    };
+    auto finish_meta = [&](int t, TcbMeta m) {  // own copies landed: zeros for tips / root, coefficient
+      if (tid < PT) {
+        const int n = t * PT + tid;
+        const int Ep = is_root ? 0 : m.ep[tid], El = int0 ? m.el[tid] : 0, Er = int1 ? m.er[tid] : 0;
+        m.ep[tid] = Ep;
+        m.el[tid] = El;
+        m.er[tid] = Er;
+        const double w = n < a.N ? mw[tid] : 0.0;
+        m.cf[tid] = float(w * exp2(double(Ep + El + Er) - ml2[tid]));
+      }
+    };
+    uint32_t ph_rf = 0, ph_oe = 0x7u, ph_af = 0;
+    bool ok = true;        // uniform across the converters after every conv_sync_any
+    float root_acc = 0.0f; // root: this thread's share of sum_p c_p al[i][p] ar[i][p], i = tid & 63
+    if (t0 < t1) {
+      fetch_meta(t0, tcb_meta(smem + kOffMeta));
+      cp_async_wait<0>();
+      finish_meta(t0, tcb_meta(smem + kOffMeta));
+    }
+    ok = !conv_sync_any(!ok);
+    Cur cu{0, 0, 0};
+    for (int u = 0; u < total; ++u) {
+      const int tt = cu.tt, side = cu.side, rr = cu.rr;
+      const bool g2 = rr >= kU3;
+      const int idx = g2 ? rr - kU3 : rr;
+      const int tile = t0 + tt, n0 = tile * PT;
+      const TcbMeta meta = tcb_meta(smem + kOffMeta + (tt & 1) * kMeta);
+      if (ok && side == 0 && rr == 0) {
+        if (tile + 1 < t1) fetch_meta(tile + 1, tcb_meta(smem + kOffMeta + ((tt + 1) & 1) * kMeta));
+        if (is_root) {  // R[i][p] = c_p al[i][p] ar[i][p]: row i = tid & 63, patterns 4 (tid >> 6 + 8 m) ..
+          const float *pb = a.prod + size_t(vblk) * 2 * SP * npad;
+          const int i = tid & 63;
+#pragma unroll
+          for (int m = 0; m < 4; ++m) {
+            const int quad = (tid >> 6) + 8 * m;
+            const float4 al = ldg4(pb + size_t(i) * npad + n0 + 4 * quad);
+            const float4 ar = ldg4(pb + size_t(SP + i) * npad + n0 + 4 * quad);
+            const float4 c4 = *reinterpret_cast<const float4 *>(meta.cf + 4 * quad);
+            root_acc += c4.x * al.x * ar.x + c4.y * al.y * ar.y + c4.z * al.z * ar.z + c4.w * al.w * ar.w;
+          }
+        }
+      }
+      const int rs = u % kNR, sl = u % kNS;
+      if (ok) ok = mbar_wait_bounded(&raw_full[rs], ph_rf >> rs & 1u, timeout_ns);   // the unit's rows landed
+      if (ok) ok = mbar_wait_bounded(&op_empty[sl], ph_oe >> sl & 1u, timeout_ns);  // the slot is free
+      ph_rf ^= 1u << rs;
+      ph_oe ^= 1u << sl;
+      if (ok) {
+        unsigned char *op = smem + sl * kOpSlot;
+        const unsigned char *raw = smem + kOffRaw + rs * kRawSlot;
+        if (!g2) {
+          // item (row i, 4-pattern group q) on a diagonal: the 8 lanes of a quarter warp read 8
+          // different 16-byte columns of the raw rows and write 8 different rows of a core matrix
+          const int q = tid & 7, g = (tid >> 3) & 7, sd = tid >> 6;
+          const int i = 8 * g + ((q + sd) & 7);
+          const int pt = idx * kKC3 + 4 * q;  // pattern offset in the tile
+          const float4 o4 = *reinterpret_cast<const float4 *>(raw + i * 128 + q * 16);
+          float4 p4;
+          if (is_root) {
+            const float pr = i < a.S ? float(wk * a.freqs[size_t(b) * a.S + i]) : 0.0f;
+            p4 = make_float4(pr, pr, pr, pr);
+          } else {
+            p4 = *reinterpret_cast<const float4 *>(raw + 8192 + i * 128 + q * 16);
+          }
+          float4 x4;
+          if (side ? int1 : int0) {
+            x4 = *reinterpret_cast<const float4 *>(raw + 16384 + i * 128 + q * 16);
+          } else {
+            const unsigned char *cc = meta.codes + side * PT + pt;
+            x4 = make_float4(__ldg(a.table + int(cc[0]) * SP + i), __ldg(a.table + int(cc[1]) * SP + i),
+                             __ldg(a.table + int(cc[2]) * SP + i), __ldg(a.table + int(cc[3]) * SP + i));
+          }
+          const float4 c4 = *reinterpret_cast<const float4 *>(meta.cf + pt);
+          const uint32_t off = tc::kmajor_off(i, 4 * q, 1024);
+          split4_store(op + off, op + 8192 + off, make_float4(p4.x * o4.x, p4.y * o4.y, p4.z * o4.z, p4.w * o4.w));
+          split4_store(op + 16384 + off, op + 24576 + off,
+                       make_float4(x4.x * c4.x, x4.y * c4.y, x4.z * c4.z, x4.w * c4.w));
+        } else {
+          // item (pattern p, states 16 idx + 4 sq ..): A = u^T, row p, K = 4 states
+          const int pp = tid & (PT - 1), sq = tid >> 7;
+          float uu[4];
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            const int row = 4 * sq + e, i = idx * kKC2 + row;
+            const float ot = *reinterpret_cast<const float *>(raw + row * 512 + pp * 4);
+            const float pv = is_root ? (i < a.S ? float(wk * a.freqs[size_t(b) * a.S + i]) : 0.0f)
+                                     : *reinterpret_cast<const float *>(raw + 8192 + row * 512 + pp * 4);
+            uu[e] = pv * ot;
+          }
+          const uint32_t off = tc::kmajor_off(pp, 4 * sq, 2048);
+          split4_store(op + off, op + 8192 + off, make_float4(uu[0], uu[1], uu[2], uu[3]));
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor cores
+        __syncwarp();
+        if (lane == 0) {
+          mbar_arrive(&op_full[sl]);
+          mbar_arrive(&raw_empty[rs]);
+        }
+      }
+      if (g2 && idx == kU2 - 1) {  // the side's outside partials: o = P_c^T u, rescaled, over x_c
+        if (ok) ok = mbar_wait_bounded(acc_full, ph_af, timeout_ns);
+        ph_af ^= 1u;
+        tc::fence_after_sync();
+        const int cblk = side ? rblk : lblk;
+        const int qd = warp & 3, cg = warp >> 2, pp = 32 * qd + lane;  // columns [16 cg, 16 cg + 16)
+        uint32_t rg[16];
+        float mx = 0.0f;
+        if (ok) {
+          asm volatile(
+              "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+              : "=r"(rg[0]), "=r"(rg[1]), "=r"(rg[2]), "=r"(rg[3]), "=r"(rg[4]), "=r"(rg[5]), "=r"(rg[6]),
+                "=r"(rg[7]), "=r"(rg[8]), "=r"(rg[9]), "=r"(rg[10]), "=r"(rg[11]), "=r"(rg[12]), "=r"(rg[13]),
+                "=r"(rg[14]), "=r"(rg[15])
+              : "r"(tmem + (uint32_t(32 * qd) << 16) + 128u + uint32_t(16 * cg)));
+          asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+          for (int jj = 0; jj < 16; ++jj) mx = fmaxf(mx, __uint_as_float(rg[jj]));
+          red[cg * PT + pp] = mx;
+        }
+        tc::fence_before_sync();
+        __syncwarp();
+        if (lane == 0) mbar_arrive(acc_empty);  // o is in registers: the next side's GEMM2 may overwrite it
+        ok = !conv_sync_any(!ok);
+        if (ok) {
+          const int e =
+              scale_exponent(fmaxf(fmaxf(red[pp], red[PT + pp]), fmaxf(red[2 * PT + pp], red[3 * PT + pp])));
+          float *dst = a.part + size_t(cblk) * SP * npad + n0 + pp;
+#pragma unroll
+          for (int jj = 0; jj < 16; ++jj) dst[size_t(16 * cg + jj) * npad] = times_pow2_neg(__uint_as_float(rg[jj]), e);
+          if (cg == 0) a.expo[size_t(cblk) * npad + n0 + pp] = meta.ep[pp] + (side ? meta.el[pp] : meta.er[pp]) + e;
+        }
+        ok = !conv_sync_any(!ok);  // red is reused
+        if (!ok) break;
+      }
+      if (side == 1 && rr == per_side1 - 1 && tile + 1 < t1) {  // the next tile's per-pattern data
+        cp_async_wait<0>();
+        if (ok) finish_meta(tile + 1, tcb_meta(smem + kOffMeta + ((tt + 1) & 1) * kMeta));
+        ok = !conv_sync_any(!ok);
+        if (!ok) break;
+      }
+      advance(cu);
+    }
+    cp_async_wait<0>();  // no copy into this CTA's shared memory is left in flight
+    ok = !conv_sync_any(!ok);
+    const bool fin = mbar_wait_bounded(done, 0, timeout_ns);  // every MMA is complete
+    tc::fence_after_sync();
+    ok = !conv_sync_any(!(ok && fin));
+    if (ok) {
+      // the chunk's gradient blocks: G_c row i = 16 (w & 3) + lane (lanes < 16), columns [16 cg, 16 cg + 16)
+      const int qd = warp & 3, cg = warp >> 2;
+#pragma unroll 1
+      for (int c = 0; c < 2; ++c) {
+        uint32_t rg[16];
+        asm volatile(
+            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+            : "=r"(rg[0]), "=r"(rg[1]), "=r"(rg[2]), "=r"(rg[3]), "=r"(rg[4]), "=r"(rg[5]), "=r"(rg[6]),
+              "=r"(rg[7]), "=r"(rg[8]), "=r"(rg[9]), "=r"(rg[10]), "=r"(rg[11]), "=r"(rg[12]), "=r"(rg[13]),
+              "=r"(rg[14]), "=r"(rg[15])
+            : "r"(tmem + (uint32_t(32 * qd) << 16) + uint32_t(64 * c + 16 * cg)));
+        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+        if (lane < 16) {
+          const int i = 16 * qd + lane;
+          float *dst = a.gpart + (((size_t(b) * a.B + (c ? r : l)) * a.nchunks + chunk) * a.K + k) * SP * SP +
+                       i * SP + 16 * cg;
+#pragma unroll
+          for (int jj = 0; jj < 16; jj += 4)
+            *reinterpret_cast<float4 *>(dst + jj) = make_float4(__uint_as_float(rg[jj]), __uint_as_float(rg[jj + 1]),
+                                                                 __uint_as_float(rg[jj + 2]),
+                                                                 __uint_as_float(rg[jj + 3]));
+        }
+      }
+      if (is_root) {  // dlnL/dpi rows (times w_k) and dlnL/dw_k of the chunk, fixed order
+        rsum[tid] = root_acc;
+        conv_sync_any(false);
+        float *dst = a.rootpart + ((size_t(b) * a.nchunks + chunk) * a.K + k) * (SP + 1);
+        if (tid < SP) {  // the eight threads of row i: i + 64 j
+          float s = 0.0f;
+#pragma unroll
+          for (int j = 0; j < 8; ++j) s += rsum[tid + 64 * j];
+          red[tid] = s;
+          dst[tid] = float(wk) * s;
+        }
+        conv_sync_any(false);
+        if (tid == 0) {
+          float s = 0.0f;
+          for (int i = 0; i < a.S; ++i) s += float(a.freqs[size_t(b) * a.S + i]) * red[i];
+          dst[SP] = s;
+        }
+      }
+    } else if (tid == 0) {
+      atomicExch(status, kDeviceTimeout);
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) tc::tmem_dealloc(tmem, kTmemCols);
+}
+
+}  // namespace tt

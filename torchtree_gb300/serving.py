@@ -270,26 +270,30 @@ class GraphExecutor:
         self.engine.close()
 
 
-def merged_step(batches: list, stream, device) -> None:
+def merged_step(batches: list, stream, device) -> torch.cuda.Event:
     """Launch the batches of several mergeable executors as one step on
-    ``stream``: their inputs in, eigen systems and transition matrices per
-    data set, then ONE post-order and ONE adjoint launch over the tiles of all
-    of them (``tt_plans_log_likelihood`` / ``tt_plans_gradient``), the
-    rate-matrix chain per data set, results out.  ``batches``:
-    ``[(executor, requests)]``.  Each request's result equals what its data
-    set's own step gives."""
+    ``stream``: their inputs in, ONE eigendecomposition launch for all their
+    rate matrices, transition matrices per data set, then ONE post-order and
+    ONE adjoint launch over the tiles of all of them
+    (``tt_plans_log_likelihood`` / ``tt_plans_gradient``), the rate-matrix
+    chain per data set, results out.  ``batches``: ``[(executor, requests)]``.
+    Each request's result equals what its data set's own step gives.  Returns
+    the event recorded after the step's last copy."""
     preps = [ex.fill(reqs) for ex, reqs in batches]
     execs = [ex for ex, _ in batches]
     event = torch.cuda.Event()
     with torch.cuda.device(device), torch.cuda.stream(stream):
-        eig = []
         for ex in execs:
-            x = ex.inputs
-            for k, v in x.items():
+            for k, v in ex.inputs.items():
                 v.copy_(ex.host_in[k], non_blocking=True)
-            lam, u, w = substitution.device_eigen(x["q"], x["pi"])
-            eig.append((lam, u, w))
-            ex.engine.set_eigen(lam, u, w, x["bls"], x["rates"])
+        # all members are 4-state: their Q and pi stack into one Jacobi launch
+        lam, u, w = substitution.device_eigen(torch.cat([ex.inputs["q"] for ex in execs]),
+                                              torch.cat([ex.inputs["pi"] for ex in execs]))
+        eig = []
+        for i, ex in enumerate(execs):
+            x, sl = ex.inputs, slice(i * ex.slots, (i + 1) * ex.slots)
+            eig.append((lam[sl], u[sl], w[sl]))
+            ex.engine.set_eigen(lam[sl], u[sl], w[sl], x["bls"], x["rates"])
         engines = [ex.engine for ex in execs]
         props = [ex.inputs["props"] for ex in execs]
         pis = [ex.inputs["pi"] for ex in execs]
@@ -306,15 +310,20 @@ def merged_step(batches: list, stream, device) -> None:
         ex.event = event
         ex.busy = True
         ex.batch = (reqs, pr)
+    return event
 
 
 class LikelihoodServer:
     """Persistent request loop over resident data sets (see the module docstring)."""
 
     def __init__(self, slots: int = 8, precision: str = "f32", device=None, hbm_budget: int | None = None,
-                 use_graphs: bool = True, tune: bool = True, executor_factory=None, merge: bool = True):
+                 use_graphs: bool = True, tune: bool = True, executor_factory=None, merge: bool = True,
+                 merge_depth: int = 2):
         self.slots = slots
         self.merge = merge
+        # merged steps in flight at once, each on its own stream: while they
+        # run, the requests that arrive wait and go out together in the next one
+        self.merge_depth = max(1, merge_depth)
         self.precision = precision
         self.device = torch.device("cuda", torch.cuda.current_device()) if device is None else torch.device(device)
         if hbm_budget is None and executor_factory is None:
@@ -335,7 +344,11 @@ class LikelihoodServer:
         self.evictions = 0
         self.batches = 0
         self.launches = 0  # merged steps plus single-data-set steps
-        self.merge_stream = None
+        self.merged_steps = 0
+        self.merged_requests = 0
+        self.merge_host_s = 0.0  # host time spent issuing merged steps
+        self.merge_streams: list = []
+        self.merge_inflight: list = []  # (stream index, event) of merged steps not yet finished
         self._queue: queue.Queue = queue.Queue()
         self._stop = threading.Event()
         self._thread = None
@@ -375,10 +388,15 @@ class LikelihoodServer:
         lat = np.array([r.t_done - r.t_submit for r in self.completed]) * 1e3
         if lat.size == 0:
             return {"count": 0}
+        wait = np.array([r.t_launch - r.t_submit for r in self.completed]) * 1e3
         return {"count": int(lat.size), "p50_ms": float(np.percentile(lat, 50)),
                 "p99_ms": float(np.percentile(lat, 99)), "mean_ms": float(lat.mean()),
+                "wait_p50_ms": float(np.percentile(wait, 50)), "service_p50_ms": float(np.percentile(lat - wait, 50)),
                 "batches": self.batches, "launches": self.launches,
                 "requests_per_launch": int(lat.size) / max(self.launches, 1),
+                "merged_steps": self.merged_steps,
+                "requests_per_merged_step": self.merged_requests / max(self.merged_steps, 1),
+                "merge_host_ms_per_step": 1e3 * self.merge_host_s / max(self.merged_steps, 1),
                 "admissions": self.admissions, "evictions": self.evictions}
 
     # -------------------------------------------------------------- scheduler
@@ -430,6 +448,8 @@ class LikelihoodServer:
             except queue.Empty:
                 break
             self.pending.setdefault(r.dataset, []).append(r)
+        self.merge_inflight = [(i, ev) for i, ev in self.merge_inflight if not ev.query()]
+        merge_open = len(self.merge_inflight) < self.merge_depth
         order = sorted((reqs[0].t_submit, n) for n, reqs in self.pending.items() if reqs)
         merged = []
         for _, name in order:
@@ -438,21 +458,32 @@ class LikelihoodServer:
                 ex = self._admit(name)
                 if ex is None:
                     continue
-            if not ex.busy:
-                reqs = self.pending[name][: self.slots]
-                del self.pending[name][: len(reqs)]
-                if getattr(ex, "mergeable", False):
-                    merged.append((ex, reqs))
-                else:
-                    ex.launch(reqs)
-                    self.launches += 1
-                self.batches += 1
-                progressed = True
+            if ex.busy:
+                continue
+            mergeable = getattr(ex, "mergeable", False)
+            if mergeable and not merge_open:
+                continue  # waits for a merged step to finish, gathering more requests
+            reqs = self.pending[name][: self.slots]
+            del self.pending[name][: len(reqs)]
+            if mergeable:
+                merged.append((ex, reqs))
+            else:
+                ex.launch(reqs)
+                self.launches += 1
+            self.batches += 1
+            progressed = True
         if merged:  # every ready 4-state data set in one step
-            if self.merge_stream is None:
-                self.merge_stream = torch.cuda.Stream(self.device)
-            merged_step(merged, self.merge_stream, self.device)
+            busy = {i for i, _ in self.merge_inflight}
+            idx = next(i for i in range(self.merge_depth) if i not in busy)
+            while len(self.merge_streams) <= idx:
+                self.merge_streams.append(torch.cuda.Stream(self.device))
+            t0 = time.perf_counter()
+            ev = merged_step(merged, self.merge_streams[idx], self.device)
+            self.merge_host_s += time.perf_counter() - t0
+            self.merge_inflight.append((idx, ev))
             self.launches += 1
+            self.merged_steps += 1
+            self.merged_requests += sum(len(r) for _, r in merged)
         return progressed
 
     def _busy(self) -> bool:
