@@ -326,15 +326,16 @@ struct Wide {
     // the raw rows as 2-D tensors: partials [b I K 64][Npad], products [b I K 128][Npad]
     TcbMaps maps;
     const uint64_t blocks = uint64_t(p->batch) * p->I * p->K;
-    if (!encode_rows(&maps.part32, a.part, blocks * 64, uint64_t(g.Npad), 32, 64) ||
-        !encode_rows(&maps.prod32, a.prod, blocks * 128, uint64_t(g.Npad), 32, 64) ||
+    if (!encode_rows(&maps.part16, a.part, blocks * 64, uint64_t(g.Npad), 16, 64) ||
+        !encode_rows(&maps.prod16, a.prod, blocks * 128, uint64_t(g.Npad), 16, 128) ||
         !encode_rows(&maps.part128, a.part, blocks * 64, uint64_t(g.Npad), 128, 16) ||
         !encode_rows(&maps.prod128, a.prod, blocks * 128, uint64_t(g.Npad), 128, 16))
       return cudaErrorInvalidValue;
     for (size_t lv = 0; lv + 1 < w.bwd_off.size(); ++lv) {
       a.nodes = w.d_bwd + w.bwd_off[lv];
       const dim3 grid(a.nchunks, w.bwd_off[lv + 1] - w.bwd_off[lv], p->batch * p->K);
-      wide_backward_tc_kernel<<<grid, tcb::kThreads, tcb::kSmem, s>>>(a, maps, w.d_pimg, p->d_status, 2000000000ull);
+      wide_backward_tc_kernel<<<grid, tcb::kThreads, tcb::kSmem, s>>>(a, maps, w.d_pimg, p->C, p->d_status,
+                                                                       2000000000ull);
       p->launches += 1;
     }
     wide_grad_reduce_kernel<float><<<dim3(p->B, p->batch), 256, 0, s>>>(static_cast<const float *>(w.d_gpart),

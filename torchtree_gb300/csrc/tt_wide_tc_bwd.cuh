@@ -6,9 +6,11 @@
 //   u_c[i][p] = pre_v[i][p] * (P_c' x_c')[i][p]   (outside partial of v times
 //                                                  the other side's product,
 //                                                  stored by the post-order)
-//   GEMM3  G_c[i][j] += sum_p u_c[i][p] (coef_p x_c[j][p])   M = 64 (i),
-//          N = 64 (j), K = patterns, accumulated in tensor memory over all
-//          tiles of the chunk;
+//   GEMM3  G_c[i][j] += sum_p u_c[i][p] (coef_p x_c[j][p]), both sides in one
+//          block-diagonal product: M = 128 rows (side, i), N = 128 rows
+//          (side, j), K = patterns; the diagonal 64 x 64 blocks are G_l and
+//          G_r, accumulated in tensor memory over all tiles of the chunk (the
+//          off-diagonal blocks are not read);
 //   GEMM2  o_c[p][j]  = sum_i u_c[i][p] P_c[i][j]             M = 128
 //          (patterns), N = 64 (j), K = 64 (i), for internal children only:
 //          the child's outside partial, rescaled by the power of two of its
@@ -19,20 +21,20 @@
 // same K-major no-swizzle operand layout (8-row x 16-byte core matrices, SBO
 // = 128 B between 8-row groups, LBO between 4-element K groups).
 //
-// The work of a tile is a sequence of units: per side, four GEMM3 units of
-// 32 patterns (K = 32) and, for an internal child, four GEMM2 units of 16
-// states (K = 16), then the side's epilogue.  The CTA (one per SM) is warp
-// specialised: a control warp issues each unit's raw rows (tiles of the
+// The work of a tile is a sequence of units: eight GEMM3 units of 16
+// patterns (K = 16, both sides), then for each internal child four GEMM2
+// units of 16 states (K = 16) and that side's epilogue.  The CTA (one per SM)
+// is warp specialised: a copy warp issues each unit's raw rows (tiles of the
 // pattern-contiguous partial and product rows) as 2-D bulk tensor copies
-// into a ring of four raw slots, and the MMAs of each converted unit; sixteen
-// converter warps turn a unit's raw rows into its MMA operands (products,
-// TF32 split, K-major stores) in a ring of three operand slots and run the
-// epilogues.  Full / empty mbarriers per slot order the roles; the
-// converters meet at a named barrier only at epilogues and tile ends.
-// GEMM2's B operand, P_c transposed into the operand layout and split, is
-// written once per (sample, branch, category) by wide_pimage_kernel; the
-// control warp brings a GEMM2 unit's 16-state slice in with two 4 KB bulk
-// copies.
+// into a ring of four raw slots; sixteen converter warps turn a unit's raw
+// rows into its MMA operands (products, TF32 split, K-major stores) in a ring
+// of three operand slots and run the epilogues; an MMA warp issues the
+// tensor-core work of each converted unit.  Full / empty mbarriers per slot
+// order the roles; the converters meet at a named barrier only at epilogues
+// and tile ends.  GEMM2's B operand, P_c transposed into the operand layout
+// and split, is written once per (sample, branch, category) by
+// wide_pimage_kernel; a GEMM2 unit's 16-state slice of it travels in the
+// unit's raw slot (two 4 KB bulk copies) and the MMAs read it there.
 //
 // Accumulator layouts in tensor memory (cta_group::1): for M = 128 row m is
 // lane m; for M = 64 rows 16q .. 16q + 15 are lanes 32q .. 32q + 15
@@ -50,14 +52,14 @@ namespace tcb {
 
 constexpr int kPT = 128;                  // patterns per tile (GEMM2 M)
 constexpr int kConv = 512;                // converter threads (16 warps)
-constexpr int kThreads = kConv + 32;      // + the control warp
-constexpr int kKC3 = 32;                  // patterns (K) per GEMM3 unit
+constexpr int kThreads = kConv + 64;      // + the copy warp and the MMA warp
+constexpr int kKC3 = 16;                  // patterns (K) per GEMM3 unit
 constexpr int kKC2 = 16;                  // states (K) per GEMM2 unit
-constexpr int kU3 = kPT / kKC3;           // GEMM3 units per side and tile
+constexpr int kU3 = kPT / kKC3;           // GEMM3 units per tile (both sides)
 constexpr int kU2 = 64 / kKC2;            // GEMM2 units per internal side and tile
 constexpr int kOpSlot = 32768;            // one unit's operands (A big, A small, B big, B small)
 constexpr int kNS = 3;                    // operand slots
-constexpr int kRawSlot = 24576;           // one unit's raw rows: three 8 KB tensor tiles
+constexpr int kRawSlot = 24576;           // one unit's raw rows (GEMM2: with its image slice)
 constexpr int kNR = 4;                    // raw slots
 constexpr int kMeta = kPT * 16 + 2 * kPT; // a tile's coefficients, exponents and tip codes
 constexpr int kOffRaw = kNS * kOpSlot;
@@ -65,11 +67,13 @@ constexpr int kOffMeta = kOffRaw + kNR * kRawSlot;
 constexpr int kOffMraw = kOffMeta + 2 * kMeta;  // the next tile's weights and site log2 L (FP64) as copied
 constexpr int kOffRed = kOffMraw + 2 * kPT * 8; // float [4][128]
 constexpr int kOffRoot = kOffRed + 4 * kPT * 4; // float [512] root partial sums
-constexpr int kOffBar = kOffRoot + kConv * 4;
-// mbarriers: raw full / empty [kNR], operand full / empty [kNS], image [kNS], accumulator full / empty, done
-constexpr int kBars = 2 * kNR + 3 * kNS + 3;
+constexpr int kTabRows = 64;               // code-table rows held in shared memory (tip children)
+constexpr int kOffTab = kOffRoot + kConv * 4;   // float [kTabRows][64]
+constexpr int kOffBar = kOffTab + kTabRows * 64 * 4;
+// mbarriers: raw full / empty [kNR], operand full / empty [kNS], accumulator full / empty, done
+constexpr int kBars = 2 * kNR + 2 * kNS + 3;
 constexpr int kSmem = kOffBar + 8 * kBars + 16;
-constexpr uint32_t kTmemCols = 256;       // G_l [0, 64), G_r [64, 128), o [128, 192)
+constexpr uint32_t kTmemCols = 256;       // G (block-diagonal) [0, 128), o [128, 192)
 constexpr int kImgFloats = 2 * 64 * 64;   // one P^T image: big then small
 
 }  // namespace tcb
@@ -148,10 +152,10 @@ __device__ __forceinline__ TcbMeta tcb_meta(unsigned char *base) {
 
 // Tensor maps of the adjoint's raw rows: the partials [b][I][K][64][Npad]
 // and the children's products [b][I][K][2][64][Npad] as 2-D arrays of rows,
-// with 32-pattern x 64-row boxes (GEMM3 units) and 128-pattern x 16-row
-// boxes (GEMM2 units).
+// with 16-pattern boxes of 64 partial rows / 128 product rows (GEMM3 units)
+// and 128-pattern x 16-row boxes (GEMM2 units).
 struct TcbMaps {
-  CUtensorMap part32, prod32, part128, prod128;
+  CUtensorMap part16, prod16, part128, prod128;
 };
 
 // Barrier among the converter warps (named barrier 1) that also ORs a
@@ -173,18 +177,17 @@ __device__ __forceinline__ bool conv_sync_any(bool flag) {
 // a.nchunks count 128-pattern tiles.
 __global__ void __launch_bounds__(tcb::kThreads, 1)
     wide_backward_tc_kernel(const WideArgs<float> a, const __grid_constant__ TcbMaps maps, const float *pimg,
-                            int *status, unsigned long long timeout_ns) {
+                            int code_count, int *status, unsigned long long timeout_ns) {
   using namespace tcb;
   constexpr int SP = 64, PT = kPT;
   extern __shared__ __align__(128) unsigned char smem[];
   float *red = reinterpret_cast<float *>(smem + kOffRed);
   float *rsum = reinterpret_cast<float *>(smem + kOffRoot);
   uint64_t *raw_full = reinterpret_cast<uint64_t *>(smem + kOffBar);  // [kNR] count 1 + bytes
-  uint64_t *raw_empty = raw_full + kNR;                                // [kNR] 16 converter warps
+  uint64_t *raw_empty = raw_full + kNR;                                // [kNR] 16 converter warps + MMA warp
   uint64_t *op_full = raw_empty + kNR;                                 // [kNS] 16 converter warps
   uint64_t *op_empty = op_full + kNS;                                  // [kNS] MMA commit
-  uint64_t *img_full = op_empty + kNS;                                 // [kNS] count 1 + bytes
-  uint64_t *acc_full = img_full + kNS;                                 // MMA commit: a side's GEMM2 done
+  uint64_t *acc_full = op_empty + kNS;                                 // MMA commit: a side's GEMM2 done
   uint64_t *acc_empty = acc_full + 1;                                  // 16 converter warps: o read
   uint64_t *done = acc_empty + 1;                                      // MMA commit: every MMA done
   uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
@@ -201,27 +204,34 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
   const int lblk = int0 ? (b * a.I + (l - a.tips)) * a.K + k : 0;
   const int rblk = int1 ? (b * a.I + (r - a.tips)) * a.K + k : 0;
   const int t0 = chunk * a.tiles_per_chunk, t1 = min(a.ntiles, t0 + a.tiles_per_chunk);
-  const int per_side0 = kU3 + (int0 ? kU2 : 0), per_side1 = kU3 + (int1 ? kU2 : 0);
-  const int total = (t1 - t0) * (per_side0 + per_side1);
+  const int UT = kU3 + (int0 ? kU2 : 0) + (int1 ? kU2 : 0);  // units per tile
+  const int total = (t1 - t0) * UT;
 
-  struct Cur {  // a unit: tile index tt, side, index within the side's units
-    int tt, side, rr;
+  // a unit: tile index tt and position rr in the tile -> GEMM3 (idx) or GEMM2 of a side (idx)
+  struct Unit {
+    bool g2;
+    int side, idx;
   };
-  auto advance = [&](Cur &c) {
-    if (++c.rr == (c.side ? per_side1 : per_side0)) {
-      c.rr = 0;
-      if (c.side) ++c.tt;
-      c.side ^= 1;
+  auto unit_of = [&](int rr) {
+    Unit un;
+    un.g2 = rr >= kU3;
+    if (!un.g2) {
+      un.side = 0;
+      un.idx = rr;
+    } else {
+      const int q = rr - kU3;
+      un.side = (int0 && q < kU2) ? 0 : 1;
+      un.idx = q - (un.side && int0 ? kU2 : 0);
     }
+    return un;
   };
 
   if (warp == 0) tc::tmem_alloc(tslot, kTmemCols);
   if (tid == kConv) {
-    for (int i = 0; i < 2 * kNR; ++i) mbar_init(&raw_full[i], i < kNR ? 1 : 16);
+    for (int i = 0; i < 2 * kNR; ++i) mbar_init(&raw_full[i], i < kNR ? 1 : 17);
     for (int i = 0; i < kNS; ++i) {
       mbar_init(&op_full[i], 16);
       mbar_init(&op_empty[i], 1);
-      mbar_init(&img_full[i], 1);
     }
     mbar_init(acc_full, 1);
     mbar_init(acc_empty, 16);
@@ -232,113 +242,115 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
   __syncthreads();
   tc::fence_after_sync();
   const uint32_t tmem = *tslot;
+  const float *img0 = pimg + ((size_t(b) * a.B + l) * a.K + k) * kImgFloats;
+  const float *img1 = pimg + ((size_t(b) * a.B + r) * a.K + k) * kImgFloats;
 
   if (warp == kConv / 32) {
-    // ------------------------------------------------------------ control warp
+    // ------------------------------------------------------------ copy warp (lane 0)
     if (lane == 0) {
-      const float *img0 = pimg + ((size_t(b) * a.B + l) * a.K + k) * kImgFloats;
-      const float *img1 = pimg + ((size_t(b) * a.B + r) * a.K + k) * kImgFloats;
       if (int0) bulk_prefetch_l2(img0, uint32_t(kImgFloats * sizeof(float)));
       if (int1) bulk_prefetch_l2(img1, uint32_t(kImgFloats * sizeof(float)));
-      uint32_t ph_re = 0xFu, ph_of = 0, ph_oe = 0x7u, ph_img = 0, pend_rf = 0, pend_img = 0;
-      uint32_t ph_ae = 1u, started = 0;
+      uint32_t ph_re = 0xFu, pend_rf = 0;
       bool ok = true;
-      Cur ct{0, 0, 0}, cm{0, 0, 0};  // next unit to copy / to multiply
-      int ut = 0;
-      for (int u = 0; u < total && ok; ++u) {
-        // keep the raw ring full: units up to u + kNR - 1
-        for (; ut < total && ut < u + kNR && ok; ++ut) {
-          const int rs = ut % kNR;
-          ok = mbar_wait_bounded(&raw_empty[rs], ph_re >> rs & 1u, timeout_ns);  // converters read it
-          if (!ok) break;
-          ph_re ^= 1u << rs;
-          unsigned char *raw = smem + kOffRaw + rs * kRawSlot;
-          const int n0 = (t0 + ct.tt) * PT, oblk = vblk * 2 + (1 - ct.side);
-          if (ct.rr < kU3) {
-            const int x = n0 + ct.rr * kKC3;
-            const bool xin = ct.side ? int1 : int0;
-            mbar_arrive_expect_tx(&raw_full[rs], uint32_t(8192 * (1 + (is_root ? 0 : 1) + (xin ? 1 : 0))));
-            tma_load_2d(raw, &maps.prod32, x, oblk * SP, &raw_full[rs]);
-            if (!is_root) tma_load_2d(raw + 8192, &maps.part32, x, vblk * SP, &raw_full[rs]);
-            if (xin) tma_load_2d(raw + 16384, &maps.part32, x, (ct.side ? rblk : lblk) * SP, &raw_full[rs]);
-          } else {
-            const int y = (ct.rr - kU3) * kKC2;
-            mbar_arrive_expect_tx(&raw_full[rs], uint32_t(8192 * (1 + (is_root ? 0 : 1))));
-            tma_load_2d(raw, &maps.prod128, n0, oblk * SP + y, &raw_full[rs]);
-            if (!is_root) tma_load_2d(raw + 8192, &maps.part128, n0, vblk * SP + y, &raw_full[rs]);
-          }
-          pend_rf |= 1u << rs;
-          advance(ct);
-        }
+      int tt = 0, rr = 0;
+      for (int u = 0; u < total; ++u) {
+        const int rs = u % kNR;
+        // the slot is free once its last unit is converted and, for a GEMM2 unit, multiplied
+        ok = mbar_wait_bounded(&raw_empty[rs], ph_re >> rs & 1u, timeout_ns);
         if (!ok) break;
-        pend_rf &= ~(1u << (u % kNR));  // the converters wait for unit u's copies before arriving below
-        const int sl = u % kNS, side = cm.side, rr = cm.rr;
-        const bool g2 = rr >= kU3;
-        const int idx = g2 ? rr - kU3 : rr;
-        ok = mbar_wait_bounded(&op_empty[sl], ph_oe >> sl & 1u, timeout_ns);  // the slot's last MMAs are done
-        if (!ok) break;
-        ph_oe ^= 1u << sl;
-        unsigned char *op = smem + sl * kOpSlot;
-        if (g2) {  // the unit's 16-state slice of the P^T image, big and small
-          mbar_arrive_expect_tx(&img_full[sl], 8192u);
-          const float *src = (side ? img1 : img0) + idx * 1024;  // K groups 4 idx .. 4 idx + 3: 4 KB per half
-          bulk_copy_g2s(op + 16384, src, 4096u, &img_full[sl]);
-          bulk_copy_g2s(op + 20480, src + 4096, 4096u, &img_full[sl]);
-          pend_img |= 1u << sl;
-        }
-        ok = mbar_wait_bounded(&op_full[sl], ph_of >> sl & 1u, timeout_ns);  // the converters wrote it
-        if (!ok) break;
-        ph_of ^= 1u << sl;
-        tc::fence_after_sync();
-        const uint32_t sb = smem_u32(op);
-        if (!g2) {
-          constexpr uint32_t idesc = tc::idesc_tf32(64, 64);
-          const uint32_t d = tmem + uint32_t(64 * side);
-#pragma unroll
-          for (int kk = 0; kk < kKC3 / 8; ++kk) {
-            const uint64_t dab = tc::smem_desc(sb + kk * 2048, 1024, 128), das = tc::smem_desc(sb + 8192 + kk * 2048, 1024, 128);
-            const uint64_t dbb = tc::smem_desc(sb + 16384 + kk * 2048, 1024, 128),
-                           dbs = tc::smem_desc(sb + 24576 + kk * 2048, 1024, 128);
-            tc::mma_tf32(d, dab, dbb, idesc, ((started >> side & 1u) || kk > 0) ? 1u : 0u);
-            tc::mma_tf32(d, dab, dbs, idesc, 1u);
-            tc::mma_tf32(d, das, dbb, idesc, 1u);
-          }
-          started |= 1u << side;
-          tc::mma_commit(&op_empty[sl]);
+        ph_re ^= 1u << rs;
+        // the converters wait for every earlier use of this slot before the MMA warp releases it
+        pend_rf &= ~(1u << rs);
+        unsigned char *raw = smem + kOffRaw + rs * kRawSlot;
+        const Unit un = unit_of(rr);
+        const int n0 = (t0 + tt) * PT;
+        if (!un.g2) {
+          const int x = n0 + un.idx * kKC3;
+          mbar_arrive_expect_tx(&raw_full[rs],
+                                uint32_t(8192 + 4096 * ((is_root ? 0 : 1) + (int0 ? 1 : 0) + (int1 ? 1 : 0))));
+          tma_load_2d(raw, &maps.prod16, x, vblk * 2 * SP, &raw_full[rs]);
+          if (!is_root) tma_load_2d(raw + 8192, &maps.part16, x, vblk * SP, &raw_full[rs]);
+          if (int0) tma_load_2d(raw + 12288, &maps.part16, x, lblk * SP, &raw_full[rs]);
+          if (int1) tma_load_2d(raw + 16384, &maps.part16, x, rblk * SP, &raw_full[rs]);
         } else {
-          ok = mbar_wait_bounded(&img_full[sl], ph_img >> sl & 1u, timeout_ns);
-          if (!ok) break;
-          ph_img ^= 1u << sl;
-          pend_img &= ~(1u << sl);
-          if (idx == 0) {  // the previous epilogue has read o
-            ok = mbar_wait_bounded(acc_empty, ph_ae, timeout_ns);
-            if (!ok) break;
-            ph_ae ^= 1u;
-            tc::fence_after_sync();
-          }
-          constexpr uint32_t idesc = tc::idesc_tf32(128, 64);
-#pragma unroll
-          for (int kk = 0; kk < kKC2 / 8; ++kk) {
-            const uint64_t dab = tc::smem_desc(sb + kk * 4096, 2048, 128), das = tc::smem_desc(sb + 8192 + kk * 4096, 2048, 128);
-            const uint64_t dbb = tc::smem_desc(sb + 16384 + kk * 2048, 1024, 128),
-                           dbs = tc::smem_desc(sb + 20480 + kk * 2048, 1024, 128);
-            tc::mma_tf32(tmem + 128u, dab, dbb, idesc, (idx > 0 || kk > 0) ? 1u : 0u);
-            tc::mma_tf32(tmem + 128u, dab, dbs, idesc, 1u);
-            tc::mma_tf32(tmem + 128u, das, dbb, idesc, 1u);
-          }
-          tc::mma_commit(&op_empty[sl]);
-          if (idx == kU2 - 1) tc::mma_commit(acc_full);  // the side's o is complete
+          const int y = un.idx * kKC2, oblk = vblk * 2 + (1 - un.side);
+          mbar_arrive_expect_tx(&raw_full[rs], uint32_t(8192 * (2 + (is_root ? 0 : 1))));
+          tma_load_2d(raw, &maps.prod128, n0, oblk * SP + y, &raw_full[rs]);
+          if (!is_root) tma_load_2d(raw + 8192, &maps.part128, n0, vblk * SP + y, &raw_full[rs]);
+          // the unit's 16-state slice of the P^T image (K groups 4 idx .. 4 idx + 3), big and small
+          const float *src = (un.side ? img1 : img0) + un.idx * 1024;
+          bulk_copy_g2s(raw + 16384, src, 4096u, &raw_full[rs]);
+          bulk_copy_g2s(raw + 20480, src + 4096, 4096u, &raw_full[rs]);
         }
-        advance(cm);
+        pend_rf |= 1u << rs;
+        if (++rr == UT) {
+          rr = 0;
+          ++tt;
+        }
       }
-      tc::mma_commit(done);  // every MMA issued so far
       if (!ok) {
         atomicExch(status, kDeviceTimeout);
         for (int rs = 0; rs < kNR; ++rs)  // copies in flight land before the CTA exits
           if (pend_rf >> rs & 1u) mbar_wait_bounded(&raw_full[rs], (ph_re >> rs & 1u) ^ 1u, 100000000ull);
-        for (int sl = 0; sl < kNS; ++sl)
-          if (pend_img >> sl & 1u) mbar_wait_bounded(&img_full[sl], ph_img >> sl & 1u, 100000000ull);
       }
+    }
+    __syncwarp();
+  } else if (warp == kConv / 32 + 1) {
+    // ------------------------------------------------------------ MMA warp (the whole warp runs the
+    // loop, lane 0 issues)
+    const bool leader = lane == 0;
+    // operand descriptors: slot / raw-slot bases, advanced by (byte offset >> 4) per K step
+    const uint64_t dA = tc::smem_desc(smem_u32(smem), 2048, 128);
+    const uint64_t dB = tc::smem_desc(smem_u32(smem + kOffRaw), 1024, 128);
+    uint32_t ph_of = 0, ph_ae = 1u;
+    bool ok = true, started = false;
+    int rr = 0;
+    for (int u = 0; u < total && ok; ++u) {
+      const int rs = u % kNR, sl = u % kNS;
+      const Unit un = unit_of(rr);
+      ok = __all_sync(0xffffffffu, mbar_wait_bounded(&op_full[sl], ph_of >> sl & 1u, timeout_ns));
+      if (!ok) break;
+      ph_of ^= 1u << sl;
+      if (un.g2 && un.idx == 0) {  // the previous epilogue has read o
+        ok = __all_sync(0xffffffffu, mbar_wait_bounded(acc_empty, ph_ae, timeout_ns));
+        if (!ok) break;
+        ph_ae ^= 1u;
+      }
+      tc::fence_after_sync();
+      const uint64_t so = uint64_t(sl * kOpSlot) >> 4, ro = uint64_t(rs * kRawSlot) >> 4;
+      if (leader) {
+        if (!un.g2) {
+          constexpr uint32_t idesc = tc::idesc_tf32(128, 128);
+#pragma unroll
+          for (int kk = 0; kk < kKC3 / 8; ++kk) {
+            const uint64_t o = so + uint64_t(kk * 4096 >> 4);
+            tc::mma_tf32(tmem, dA + o, dA + o + (16384 >> 4), idesc, (started || kk > 0) ? 1u : 0u);
+            tc::mma_tf32(tmem, dA + o, dA + o + (24576 >> 4), idesc, 1u);
+            tc::mma_tf32(tmem, dA + o + (8192 >> 4), dA + o + (16384 >> 4), idesc, 1u);
+          }
+          tc::mma_commit(&op_empty[sl]);
+          mbar_arrive(&raw_empty[rs]);  // the MMAs do not read the raw slot
+        } else {
+          constexpr uint32_t idesc = tc::idesc_tf32(128, 64);
+#pragma unroll
+          for (int kk = 0; kk < kKC2 / 8; ++kk) {
+            const uint64_t oa = so + uint64_t(kk * 4096 >> 4), ob = ro + uint64_t(16384 + kk * 2048 >> 4);
+            tc::mma_tf32(tmem + 128u, dA + oa, dB + ob, idesc, (un.idx > 0 || kk > 0) ? 1u : 0u);
+            tc::mma_tf32(tmem + 128u, dA + oa, dB + ob + (4096 >> 4), idesc, 1u);
+            tc::mma_tf32(tmem + 128u, dA + oa + (8192 >> 4), dB + ob, idesc, 1u);
+          }
+          tc::mma_commit(&op_empty[sl]);
+          tc::mma_commit(&raw_empty[rs]);  // the raw slot held B
+          if (un.idx == kU2 - 1) tc::mma_commit(acc_full);  // the side's o is complete
+        }
+      }
+      __syncwarp();
+      if (!un.g2) started = true;
+      if (++rr == UT) rr = 0;
+    }
+    if (leader) {
+      tc::mma_commit(done);  // every MMA issued so far
+      if (!ok) atomicExch(status, kDeviceTimeout);
     }
     __syncwarp();
   } else {
@@ -370,6 +382,20 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
         m.cf[tid] = float(w * exp2(double(Ep + El + Er) - ml2[tid]));
       }
     };
+    // a tip child's rows of the code table, in shared memory when the table is small
+    const bool tab_smem = (!int0 || !int1) && code_count <= kTabRows;
+    float *tab = reinterpret_cast<float *>(smem + kOffTab);
+    const float *tabsrc = tab_smem ? tab : a.table;
+    if (tab_smem)
+      for (int e = tid; e < code_count * 16; e += kConv)
+        reinterpret_cast<float4 *>(tab)[e] = ldg4(a.table + 4 * e);
+    // GEMM3 item of this thread: row R = (side, i) of the block-diagonal product, 4-pattern group q
+    // on a diagonal (a quarter warp reads 8 different 16-byte columns of the raw rows and writes
+    // 8 different rows of a core matrix)
+    const int j3 = tid & 7, R3 = 8 * ((tid >> 3) & 15) + j3, q3 = ((j3 >> 1) + (tid >> 7)) & 3;
+    const int s3 = R3 >> 6, i3 = R3 & 63;
+    const bool x3in = s3 ? int1 : int0;
+    const float pre3 = is_root && i3 < a.S ? float(wk * a.freqs[size_t(b) * a.S + i3]) : 0.0f;
     uint32_t ph_rf = 0, ph_oe = 0x7u, ph_af = 0;
     bool ok = true;        // uniform across the converters after every conv_sync_any
     float root_acc = 0.0f; // root: this thread's share of sum_p c_p al[i][p] ar[i][p], i = tid & 63
@@ -379,14 +405,12 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
       finish_meta(t0, tcb_meta(smem + kOffMeta));
     }
     ok = !conv_sync_any(!ok);
-    Cur cu{0, 0, 0};
+    int tt = 0, rr = 0;
     for (int u = 0; u < total; ++u) {
-      const int tt = cu.tt, side = cu.side, rr = cu.rr;
-      const bool g2 = rr >= kU3;
-      const int idx = g2 ? rr - kU3 : rr;
+      const Unit un = unit_of(rr);
       const int tile = t0 + tt, n0 = tile * PT;
       const TcbMeta meta = tcb_meta(smem + kOffMeta + (tt & 1) * kMeta);
-      if (ok && side == 0 && rr == 0) {
+      if (ok && rr == 0) {
         if (tile + 1 < t1) fetch_meta(tile + 1, tcb_meta(smem + kOffMeta + ((tt + 1) & 1) * kMeta));
         if (is_root) {  // R[i][p] = c_p al[i][p] ar[i][p]: row i = tid & 63, patterns 4 (tid >> 6 + 8 m) ..
           const float *pb = a.prod + size_t(vblk) * 2 * SP * npad;
@@ -409,30 +433,22 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
       if (ok) {
         unsigned char *op = smem + sl * kOpSlot;
         const unsigned char *raw = smem + kOffRaw + rs * kRawSlot;
-        if (!g2) {
-          // item (row i, 4-pattern group q) on a diagonal: the 8 lanes of a quarter warp read 8
-          // different 16-byte columns of the raw rows and write 8 different rows of a core matrix
-          const int q = tid & 7, g = (tid >> 3) & 7, sd = tid >> 6;
-          const int i = 8 * g + ((q + sd) & 7);
-          const int pt = idx * kKC3 + 4 * q;  // pattern offset in the tile
-          const float4 o4 = *reinterpret_cast<const float4 *>(raw + i * 128 + q * 16);
-          float4 p4;
-          if (is_root) {
-            const float pr = i < a.S ? float(wk * a.freqs[size_t(b) * a.S + i]) : 0.0f;
-            p4 = make_float4(pr, pr, pr, pr);
-          } else {
-            p4 = *reinterpret_cast<const float4 *>(raw + 8192 + i * 128 + q * 16);
-          }
+        if (!un.g2) {
+          const int pt = un.idx * kKC3 + 4 * q3;  // pattern offset in the tile
+          // u_s = pre * (the other side's product): product rows (1 - s) * 64 + i
+          const float4 o4 = *reinterpret_cast<const float4 *>(raw + ((1 - s3) * 64 + i3) * 64 + q3 * 16);
+          const float4 p4 = is_root ? make_float4(pre3, pre3, pre3, pre3)
+                                    : *reinterpret_cast<const float4 *>(raw + 8192 + i3 * 64 + q3 * 16);
           float4 x4;
-          if (side ? int1 : int0) {
-            x4 = *reinterpret_cast<const float4 *>(raw + 16384 + i * 128 + q * 16);
+          if (x3in) {
+            x4 = *reinterpret_cast<const float4 *>(raw + 12288 + s3 * 4096 + i3 * 64 + q3 * 16);
           } else {
-            const unsigned char *cc = meta.codes + side * PT + pt;
-            x4 = make_float4(__ldg(a.table + int(cc[0]) * SP + i), __ldg(a.table + int(cc[1]) * SP + i),
-                             __ldg(a.table + int(cc[2]) * SP + i), __ldg(a.table + int(cc[3]) * SP + i));
+            const unsigned char *cc = meta.codes + s3 * PT + pt;
+            x4 = make_float4(tabsrc[int(cc[0]) * SP + i3], tabsrc[int(cc[1]) * SP + i3],
+                             tabsrc[int(cc[2]) * SP + i3], tabsrc[int(cc[3]) * SP + i3]);
           }
           const float4 c4 = *reinterpret_cast<const float4 *>(meta.cf + pt);
-          const uint32_t off = tc::kmajor_off(i, 4 * q, 1024);
+          const uint32_t off = tc::kmajor_off(R3, 4 * q3, 2048);
           split4_store(op + off, op + 8192 + off, make_float4(p4.x * o4.x, p4.y * o4.y, p4.z * o4.z, p4.w * o4.w));
           split4_store(op + 16384 + off, op + 24576 + off,
                        make_float4(x4.x * c4.x, x4.y * c4.y, x4.z * c4.z, x4.w * c4.w));
@@ -442,7 +458,7 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
           float uu[4];
 #pragma unroll
           for (int e = 0; e < 4; ++e) {
-            const int row = 4 * sq + e, i = idx * kKC2 + row;
+            const int row = 4 * sq + e, i = un.idx * kKC2 + row;
             const float ot = *reinterpret_cast<const float *>(raw + row * 512 + pp * 4);
             const float pv = is_root ? (i < a.S ? float(wk * a.freqs[size_t(b) * a.S + i]) : 0.0f)
                                      : *reinterpret_cast<const float *>(raw + 8192 + row * 512 + pp * 4);
@@ -458,7 +474,8 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
           mbar_arrive(&raw_empty[rs]);
         }
       }
-      if (g2 && idx == kU2 - 1) {  // the side's outside partials: o = P_c^T u, rescaled, over x_c
+      if (un.g2 && un.idx == kU2 - 1) {  // the side's outside partials: o = P_c^T u, rescaled, over x_c
+        const int side = un.side;
         if (ok) ok = mbar_wait_bounded(acc_full, ph_af, timeout_ns);
         ph_af ^= 1u;
         tc::fence_after_sync();
@@ -493,13 +510,16 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
         ok = !conv_sync_any(!ok);  // red is reused
         if (!ok) break;
       }
-      if (side == 1 && rr == per_side1 - 1 && tile + 1 < t1) {  // the next tile's per-pattern data
+      if (rr == UT - 1 && tile + 1 < t1) {  // the next tile's per-pattern data
         cp_async_wait<0>();
         if (ok) finish_meta(tile + 1, tcb_meta(smem + kOffMeta + ((tt + 1) & 1) * kMeta));
         ok = !conv_sync_any(!ok);
         if (!ok) break;
       }
-      advance(cu);
+      if (++rr == UT) {
+        rr = 0;
+        ++tt;
+      }
     }
     cp_async_wait<0>();  // no copy into this CTA's shared memory is left in flight
     ok = !conv_sync_any(!ok);
@@ -507,45 +527,39 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
     tc::fence_after_sync();
     ok = !conv_sync_any(!(ok && fin));
     if (ok) {
-      // the chunk's gradient blocks: G_c row i = 16 (w & 3) + lane (lanes < 16), columns [16 cg, 16 cg + 16)
-      const int qd = warp & 3, cg = warp >> 2;
-#pragma unroll 1
-      for (int c = 0; c < 2; ++c) {
-        uint32_t rg[16];
-        asm volatile(
-            "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
-            : "=r"(rg[0]), "=r"(rg[1]), "=r"(rg[2]), "=r"(rg[3]), "=r"(rg[4]), "=r"(rg[5]), "=r"(rg[6]),
-              "=r"(rg[7]), "=r"(rg[8]), "=r"(rg[9]), "=r"(rg[10]), "=r"(rg[11]), "=r"(rg[12]), "=r"(rg[13]),
-              "=r"(rg[14]), "=r"(rg[15])
-            : "r"(tmem + (uint32_t(32 * qd) << 16) + uint32_t(64 * c + 16 * cg)));
-        asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
-        if (lane < 16) {
-          const int i = 16 * qd + lane;
-          float *dst = a.gpart + (((size_t(b) * a.B + (c ? r : l)) * a.nchunks + chunk) * a.K + k) * SP * SP +
-                       i * SP + 16 * cg;
+      // the chunk's gradient blocks: G_side row i = lane quarter 32 (w & 3) + lane - 64 side,
+      // side = (w & 3) >> 1, columns 64 side + [16 cg, 16 cg + 16)
+      const int qd = warp & 3, cg = warp >> 2, side = qd >> 1, i = (32 * qd + lane) & 63;
+      uint32_t rg[16];
+      asm volatile(
+          "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0,%1,%2,%3,%4,%5,%6,%7,%8,%9,%10,%11,%12,%13,%14,%15}, [%16];"
+          : "=r"(rg[0]), "=r"(rg[1]), "=r"(rg[2]), "=r"(rg[3]), "=r"(rg[4]), "=r"(rg[5]), "=r"(rg[6]),
+            "=r"(rg[7]), "=r"(rg[8]), "=r"(rg[9]), "=r"(rg[10]), "=r"(rg[11]), "=r"(rg[12]), "=r"(rg[13]),
+            "=r"(rg[14]), "=r"(rg[15])
+          : "r"(tmem + (uint32_t(32 * qd) << 16) + uint32_t(64 * side + 16 * cg)));
+      asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+      float *dst = a.gpart + (((size_t(b) * a.B + (side ? r : l)) * a.nchunks + chunk) * a.K + k) * SP * SP +
+                   i * SP + 16 * cg;
 #pragma unroll
-          for (int jj = 0; jj < 16; jj += 4)
-            *reinterpret_cast<float4 *>(dst + jj) = make_float4(__uint_as_float(rg[jj]), __uint_as_float(rg[jj + 1]),
-                                                                 __uint_as_float(rg[jj + 2]),
-                                                                 __uint_as_float(rg[jj + 3]));
-        }
-      }
+      for (int jj = 0; jj < 16; jj += 4)
+        *reinterpret_cast<float4 *>(dst + jj) = make_float4(__uint_as_float(rg[jj]), __uint_as_float(rg[jj + 1]),
+                                                             __uint_as_float(rg[jj + 2]), __uint_as_float(rg[jj + 3]));
       if (is_root) {  // dlnL/dpi rows (times w_k) and dlnL/dw_k of the chunk, fixed order
         rsum[tid] = root_acc;
         conv_sync_any(false);
-        float *dst = a.rootpart + ((size_t(b) * a.nchunks + chunk) * a.K + k) * (SP + 1);
+        float *dr = a.rootpart + ((size_t(b) * a.nchunks + chunk) * a.K + k) * (SP + 1);
         if (tid < SP) {  // the eight threads of row i: i + 64 j
           float s = 0.0f;
 #pragma unroll
-          for (int j = 0; j < 8; ++j) s += rsum[tid + 64 * j];
+          for (int jr = 0; jr < 8; ++jr) s += rsum[tid + 64 * jr];
           red[tid] = s;
-          dst[tid] = float(wk) * s;
+          dr[tid] = float(wk) * s;
         }
         conv_sync_any(false);
         if (tid == 0) {
           float s = 0.0f;
-          for (int i = 0; i < a.S; ++i) s += float(a.freqs[size_t(b) * a.S + i]) * red[i];
-          dst[SP] = s;
+          for (int ii = 0; ii < a.S; ++ii) s += float(a.freqs[size_t(b) * a.S + ii]) * red[ii];
+          dr[SP] = s;
         }
       }
     } else if (tid == 0) {
