@@ -189,6 +189,24 @@ def test_results_same_alone_and_in_the_mix():
             np.testing.assert_allclose(b[g], a[g], rtol=1e-12, atol=1e-12 * np.abs(a[g]).max(), err_msg=f"{k} {g}")
 
 
+def test_slots_follow_the_data_set_size():
+    """A plan batches enough samples to fill the GPU with pattern tiles and no
+    more: every slot is computed whether or not a request waits for it."""
+    from types import SimpleNamespace
+
+    def ds(n, s=4, k=4):
+        return serving.Dataset("d", None, SimpleNamespace(pattern_count=n), s, serving.ModelSpec("gtr", k))
+
+    assert serving.slots_for(ds(500), 4) == 4       # 8 tiles of 64 patterns per sample
+    assert serving.slots_for(ds(10_000), 4) == 2    # 157 tiles
+    assert serving.slots_for(ds(50_000), 4) == 1    # 782 tiles fill the GPU alone
+    assert serving.slots_for(ds(5_000, 20), 4) == 2  # 40 tiles of 128 x 4 categories
+    assert serving.slots_for(ds(500), 8) == 8
+    srv = serving.LikelihoodServer(slots=4, hbm_budget=100, executor_factory=lambda d: None, device="cpu",
+                                   size_slots=False)
+    assert srv.slots_of(ds(50_000)) == 4
+
+
 def test_autotune_candidates_cover_the_kernel_shape_options():
     """Host logic only: the option sets the tuner times for each kind of plan."""
     from types import SimpleNamespace

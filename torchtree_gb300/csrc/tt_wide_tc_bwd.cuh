@@ -160,6 +160,7 @@ struct TcbMaps {
 
 // Barrier among the converter warps (named barrier 1) that also ORs a
 // failure flag across them.
+template <int NT = tcb::kConv>
 __device__ __forceinline__ bool conv_sync_any(bool flag) {
   uint32_t r;
   asm volatile(
@@ -168,7 +169,7 @@ __device__ __forceinline__ bool conv_sync_any(bool flag) {
       "bar.red.or.pred q, 1, %2, p;\n\t"
       "selp.u32 %0, 1, 0, q;\n\t}"
       : "=r"(r)
-      : "r"(flag ? 1u : 0u), "n"(tcb::kConv)
+      : "r"(flag ? 1u : 0u), "n"(NT)
       : "memory");
   return r != 0;
 }
@@ -362,8 +363,10 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
         if (!is_root) cp_async4(&m.ep[tid], a.expo + size_t(vblk) * npad + n);
         if (int0) cp_async4(&m.el[tid], a.expo + size_t(lblk) * npad + n);
         if (int1) cp_async4(&m.er[tid], a.expo + size_t(rblk) * npad + n);
-        if (n < a.N) cp_async8(&mw[tid], a.weights + n);
-        cp_async8(&ml2[tid], a.log2L + size_t(b) * npad + n);
+        if (n < a.N) {  // padding patterns have neither (log2 L is written for n < N only)
+          cp_async8(&mw[tid], a.weights + n);
+          cp_async8(&ml2[tid], a.log2L + size_t(b) * npad + n);
+        }
       } else if (tid < PT + 64) {
         const int sd = (tid - PT) >> 5, t4 = (tid - PT) & 31;
         if (!(sd ? int1 : int0))
@@ -378,8 +381,7 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
         m.ep[tid] = Ep;
         m.el[tid] = El;
         m.er[tid] = Er;
-        const double w = n < a.N ? mw[tid] : 0.0;
-        m.cf[tid] = float(w * exp2(double(Ep + El + Er) - ml2[tid]));
+        m.cf[tid] = n < a.N ? float(mw[tid] * exp2(double(Ep + El + Er) - ml2[tid])) : 0.0f;
       }
     };
     // a tip child's rows of the code table, in shared memory when the table is small

@@ -132,6 +132,17 @@ def host_finish(p: dict, out: dict) -> dict:
 SLAB_ALIGN = 512  # pattern-slab sizes are multiples of this (TT_OPT_SLAB_PATTERNS)
 
 
+def slots_for(ds: Dataset, max_slots: int, fill_ctas: int = 2 * 152) -> int:
+    """Batch slots of a data set's plan: enough samples that one launch's
+    pattern tiles fill the GPU (``fill_ctas`` CTAs), at most ``max_slots``.
+    A plan computes every slot whatever the number of waiting requests, so a
+    large data set, which fills the GPU with one sample, gets fewer slots and
+    spends no work on idle ones."""
+    N, K = ds.alignment.pattern_count, ds.spec.categories
+    per_sample = -(-N // 64) if ds.state_count == 4 else -(-N // 128) * K
+    return max(1, min(max_slots, -(-fill_ctas // max(per_sample, 1))))
+
+
 def estimate_bytes(ds: Dataset, slots: int, precision: str, slab: int = 0) -> int:
     """Device bytes a plan for ``ds`` with ``slots`` samples will hold (upper
     estimate); with ``slab`` > 0 its partials cover that many patterns at once."""
@@ -290,8 +301,10 @@ def merged_step(batches: list, stream, device) -> torch.cuda.Event:
         lam, u, w = substitution.device_eigen(torch.cat([ex.inputs["q"] for ex in execs]),
                                               torch.cat([ex.inputs["pi"] for ex in execs]))
         eig = []
-        for i, ex in enumerate(execs):
-            x, sl = ex.inputs, slice(i * ex.slots, (i + 1) * ex.slots)
+        first = 0
+        for ex in execs:
+            x, sl = ex.inputs, slice(first, first + ex.slots)
+            first += ex.slots
             eig.append((lam[sl], u[sl], w[sl]))
             ex.engine.set_eigen(lam[sl], u[sl], w[sl], x["bls"], x["rates"])
         engines = [ex.engine for ex in execs]
@@ -318,8 +331,11 @@ class LikelihoodServer:
 
     def __init__(self, slots: int = 8, precision: str = "f32", device=None, hbm_budget: int | None = None,
                  use_graphs: bool = True, tune: bool = True, executor_factory=None, merge: bool = True,
-                 merge_depth: int = 2):
+                 merge_depth: int = 2, size_slots: bool = True):
+        # slots: the most samples a plan batches; with size_slots a data set whose one sample
+        # fills the GPU gets fewer (slots_for)
         self.slots = slots
+        self.size_slots = size_slots
         self.merge = merge
         # merged steps in flight at once, each on its own stream: while they
         # run, the requests that arrive wait and go out together in the next one
@@ -330,11 +346,11 @@ class LikelihoodServer:
             free, _ = torch.cuda.mem_get_info(self.device)
             hbm_budget = int(0.85 * free)
         self.budget = hbm_budget
-        self.factory = executor_factory or (lambda ds, slab=0: GraphExecutor(ds, slots, precision, self.device,
-                                                                             use_graph=use_graphs, tune=tune,
-                                                                             slab=slab, merge=merge))
-        self.estimate = (lambda ds: estimate_bytes(ds, slots, precision))
-        self.slab_fit = (lambda ds, room: slab_fit(ds, slots, precision, room))
+        self.factory = executor_factory or (lambda ds, slab=0: GraphExecutor(ds, self.slots_of(ds), precision,
+                                                                             self.device, use_graph=use_graphs,
+                                                                             tune=tune, slab=slab, merge=merge))
+        self.estimate = (lambda ds: estimate_bytes(ds, self.slots_of(ds), precision))
+        self.slab_fit = (lambda ds, room: slab_fit(ds, self.slots_of(ds), precision, room))
         self.datasets: dict = {}
         self.executors: dict = {}
         self.pending: dict = {}
@@ -353,6 +369,9 @@ class LikelihoodServer:
         self._stop = threading.Event()
         self._thread = None
         self._error = None
+
+    def slots_of(self, ds: Dataset) -> int:
+        return slots_for(ds, self.slots) if self.size_slots else self.slots
 
     # -------------------------------------------------------------- client API
     def add_dataset(self, name: str, topology: Topology, alignment: CompressedAlignment, state_count: int,
@@ -463,7 +482,7 @@ class LikelihoodServer:
             mergeable = getattr(ex, "mergeable", False)
             if mergeable and not merge_open:
                 continue  # waits for a merged step to finish, gathering more requests
-            reqs = self.pending[name][: self.slots]
+            reqs = self.pending[name][: getattr(ex, "slots", self.slots)]
             del self.pending[name][: len(reqs)]
             if mergeable:
                 merged.append((ex, reqs))
