@@ -175,9 +175,11 @@ def test_results_same_alone_and_in_the_mix():
         t.start()
     for t in threads:
         t.join()
-    mixed = {k: f.result(timeout=300) for k, f in futs.items()}
-    stats = srv.latency_stats()
-    srv.stop()
+    try:
+        mixed = {k: f.result(timeout=300) for k, f in futs.items()}
+        stats = srv.latency_stats()
+    finally:
+        srv.stop()  # raises the scheduler's own error, if it had one
     assert stats["count"] == len(keys) and stats["p99_ms"] >= stats["p50_ms"] > 0
     assert stats["requests_per_launch"] > 1.0, stats
     assert stats["merged_steps"] > 0 and stats["requests_per_merged_step"] > 1.0, stats
@@ -187,6 +189,25 @@ def test_results_same_alone_and_in_the_mix():
         np.testing.assert_allclose(b["lnl"], a["lnl"], rtol=1e-12, err_msg=str(k))
         for g in ("grad_branch_lengths", "grad_exch", "grad_pi", "grad_shape"):
             np.testing.assert_allclose(b[g], a[g], rtol=1e-12, atol=1e-12 * np.abs(a[g]).max(), err_msg=f"{k} {g}")
+
+
+def test_a_failing_step_fails_the_requests_in_flight():
+    """An error in the scheduler fails every request it holds, waiting or in
+    flight, instead of leaving their futures unresolved; stop() raises it."""
+    srv, log, made = _server(budget=100, slots=2, sizes={"a": 10})
+    futs = [srv.submit("a", {"i": i}) for i in range(3)]
+    srv.step()  # admits "a" and launches its first batch
+
+    def broken():
+        raise RuntimeError("step failed")
+
+    made["a"].poll = broken
+    srv.start()
+    for f in futs:
+        with pytest.raises(RuntimeError, match="step failed"):
+            f.result(timeout=5)
+    with pytest.raises(RuntimeError, match="step failed"):
+        srv.stop()
 
 
 def test_slots_follow_the_data_set_size():

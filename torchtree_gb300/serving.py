@@ -516,9 +516,14 @@ class LikelihoodServer:
             while not self._stop.is_set() or self._busy():
                 if not self.step():
                     time.sleep(50e-6)
-        except Exception as exc:  # surface on stop(); fail the waiting requests
+        except Exception as exc:  # surface on stop(); fail every waiting and in-flight request
             self._error = exc
-            for reqs in self.pending.values():
-                for r in reqs:
-                    if not r.future.done():
-                        r.future.set_exception(exc)
+            waiting = [r for reqs in self.pending.values() for r in reqs]
+            in_flight = []
+            for ex in self.executors.values():
+                batch = getattr(ex, "batch", None)
+                if batch:  # GraphExecutor: (requests, host inputs)
+                    in_flight += list(batch[0] if isinstance(batch, tuple) else batch)
+            for r in waiting + in_flight:
+                if not r.future.done():
+                    r.future.set_exception(exc)
