@@ -74,6 +74,7 @@ struct WideState {
   bool store_products = false;  // FP32 codon: the adjoint reads the post-order's children's products
   bool tc_bwd = false;  // FP32 codon adjoint on the tensor cores (needs the stored products)
   float *d_pimg = nullptr;  // its GEMM2 operands: split P^T images [b][B][K][2][64][64]
+  float *d_pimg_f = nullptr;  // the tensor-core post-order's B operands: split P images, same shape
   // pattern slabs (p->slab != 0): the pattern-sized buffers below hold one
   // slab; tail_valid = they still hold the last slab's post-order (from a
   // tt_log_likelihood with keep_partials), which the gradient then reuses
@@ -255,12 +256,20 @@ struct Wide {
     if (keep) a.prod = static_cast<T *>(w.d_prod);
     constexpr int NT = WideCfg<T, SP, PTF>::NT;
     const size_t smem = wide_fwd_smem<T, SP, PTF>();
+    if constexpr (std::is_same<T, float>::value && SP == 64) {
+      if (w.tc && w.d_pimg_f) {  // the post-order's split P images, once per call
+        const long long count = (long long)p->batch * p->B * p->K;
+        wide_pimage_kernel<<<unsigned((count * 4096 + 255) / 256), 256, 0, s>>>(
+            static_cast<const float *>(p->d_pmat), w.d_pimg_f, count, 0);
+        p->launches += 1;
+      }
+    }
     for (size_t lv = 0; lv + 1 < w.fwd_off.size(); ++lv) {
       a.nodes = w.d_fwd + w.fwd_off[lv];
       if constexpr (std::is_same<T, float>::value && SP == 64) {
         if (w.tc) {
           const dim3 grid(g.Npad / tc::kPT, w.fwd_off[lv + 1] - w.fwd_off[lv], p->batch * p->K);
-          wide_forward_tc_kernel<<<grid, tc::kThreads, tc::kSmem, s>>>(a, p->d_status, 2000000000ull);
+          wide_forward_tc_kernel<<<grid, tc::kThreads, tc::kSmem, s>>>(a, w.d_pimg_f, p->d_status, 2000000000ull);
           p->launches += 1;
           continue;
         }
@@ -314,7 +323,7 @@ struct Wide {
     WideState &w = *p->wide;
     const long long count = (long long)p->batch * p->B * p->K;
     wide_pimage_kernel<<<unsigned((count * 4096 + 255) / 256), 256, 0, s>>>(static_cast<const float *>(p->d_pmat),
-                                                                         w.d_pimg, count);
+                                                                         w.d_pimg, count, 1);
     p->launches += 1;
     const int ntc = g.Npad / tcb::kPT;
     const int want = (2 * 152 + p->batch * p->K - 1) / (p->batch * p->K);
@@ -454,6 +463,7 @@ int wide_create(tt_plan *p) {
     const char *env = getenv("TT_WIDE_TC_BWD");
     if (!rc && w->store_products && !(env && atoi(env) == 0)) rc = wide_set_tensor_core_adjoint(p, true);
   }
+  if (!rc && w->tc) rc = wide_set_tensor_cores(p, true);  // its split P images
   // the pattern-sized buffers (partials, exponents, products, root and
   // gradient chunks) come from wide_alloc_slab once the slab size is chosen
   if (!rc)
@@ -555,9 +565,19 @@ int wide_alloc_slab(tt_plan *p, int slab) {
 bool wide_has_buffers(const tt_plan *p) { return p->wide && p->wide->d_part; }
 
 int wide_set_tensor_cores(tt_plan *p, bool on) {
-  if (!p->wide || p->precision != TT_PRECISION_F32 || p->wide->SP != 64)
+  WideState *w = p->wide;
+  if (!w || p->precision != TT_PRECISION_F32 || w->SP != 64)
     return on ? wfail(TT_ERR_UNSUPPORTED, "the tensor-core post-order serves FP32 codon (> 20-state) plans") : TT_OK;
-  p->wide->tc = on;
+  const size_t bytes = size_t(p->batch) * p->B * p->K * tcb::kImgFloats * sizeof(float);
+  if (on && !w->d_pimg_f) {  // the split P images: 32 KB per (sample, branch, category)
+    const int rc = walloc(p, &w->d_pimg_f, bytes, "split transition-matrix images");
+    if (rc) return rc;
+  } else if (!on && w->d_pimg_f) {
+    cudaFree(w->d_pimg_f);
+    w->d_pimg_f = nullptr;
+    p->bytes -= std::min(p->bytes, bytes);
+  }
+  w->tc = on;
   return TT_OK;
 }
 
@@ -589,7 +609,7 @@ void wide_destroy(tt_plan *p) {
   if (!w) return;
   void *bufs[] = {w->d_left, w->d_right, w->d_fwd, w->d_bwd, w->d_part, w->d_expo, w->d_root_site, w->d_root_expo,
                   w->d_log2L, w->d_block_lnl, w->d_gpart, w->d_rootpart, w->d_pgpart, w->d_prod, w->d_site,
-                  w->d_pimg};
+                  w->d_pimg, w->d_pimg_f};
   for (void *x : bufs)
     if (x) cudaFree(x);
   delete w;

@@ -618,15 +618,24 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT, wide_bwd_min_blocks<T,
 template <typename T>
 __global__ void wide_grad_reduce_kernel(const T *gpart, double *G, int B, int nchunks, int K, int S, int SP,
                                         int accumulate) {
+  // one warp per (category, row) at a time, lanes along the row: coalesced chunk loads; the
+  // chunk sum in the plan's precision and a fixed order, then FP64 (FP64 arithmetic is scarce on
+  // this GPU and the chunk blocks themselves are in the plan's precision)
   const int br = blockIdx.x, b = blockIdx.y;
-  const int kss = K * S * S;
-  for (int e = threadIdx.x; e < kss; e += blockDim.x) {
-    const int k = e / (S * S), ij = e - k * S * S, i = ij / S, j = ij - i * S;
-    double s = 0.0;
-    for (int c = 0; c < nchunks; ++c)
-      s += double(gpart[(((size_t(b) * B + br) * nchunks + c) * K + k) * SP * SP + i * SP + j]);
-    double *g = G + (size_t(b) * B + br) * kss + e;
-    *g = accumulate ? *g + s : s;
+  const int kss = K * S * S, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const size_t cstride = size_t(K) * SP * SP;  // between chunks
+  const T *base = gpart + (size_t(b) * B + br) * nchunks * cstride;
+  double *gb = G + (size_t(b) * B + br) * kss;
+  for (int kr = threadIdx.x >> 5; kr < K * S; kr += nw) {
+    const int k = kr / S, i = kr - k * S;
+    for (int j = lane; j < S; j += 32) {
+      const T *src = base + size_t(k) * SP * SP + i * SP + j;
+      T s = T(0);
+#pragma unroll 4
+      for (int c = 0; c < nchunks; ++c) s += src[c * cstride];
+      double *g = gb + (size_t(k) * S + i) * S + j;
+      *g = accumulate ? *g + double(s) : double(s);
+    }
   }
 }
 

@@ -118,14 +118,18 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 }  // namespace tc
 
 // Post-order level kernel for FP32 codon plans on the tensor cores.
-__global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const WideArgs<float> a, int *status,
-                                                                         unsigned long long timeout_ns) {
+// pimg: split P images (row i, K element j, big then small; wide_pimage_kernel
+// with transposed = 0), one 32 KB bulk copy per side; NULL stages P by the
+// threads.
+__global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const WideArgs<float> a, const float *pimg,
+                                                                         int *status, unsigned long long timeout_ns) {
   constexpr int SP = 64;
   extern __shared__ __align__(128) unsigned char smem[];
   unsigned char *sB = smem + tc::kOffB;
   unsigned char *sA = smem + tc::kOffA;
   uint64_t *bar = reinterpret_cast<uint64_t *>(smem + tc::kOffBar);
   uint32_t *tslot = reinterpret_cast<uint32_t *>(smem + tc::kOffBar + 8);
+  uint64_t *bar_b = reinterpret_cast<uint64_t *>(smem + tc::kOffBar + 16);  // the image copy
   const int tid = threadIdx.x, warp = tid >> 5;
   const int v = a.nodes[blockIdx.y];
   const int b = blockIdx.z / a.K, k = blockIdx.z - (blockIdx.z / a.K) * a.K;
@@ -136,18 +140,27 @@ __global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const 
   if (warp == 0) tc::tmem_alloc(tslot, tc::kTmemCols);
   if (tid == 0) {
     mbar_init(bar, 1);
+    mbar_init(bar_b, 1);
     fence_barrier_init();
   }
+  __syncthreads();  // barriers initialised before the first copy
   // per side c: stage, then one thread issues the side's MMAs into TMEM
   // columns [64c, 64c + 64); the next side's staging waits for their completion
   bool ok = true;
-  int phase = 0;
+  int phase = 0, phase_b = 0;
+  bool b_pending = false;  // thread 0: an image copy whose completion it has not seen
   uint32_t tmem = 0;  // read from the slot after the first barrier
   for (int c = 0; c < 2 && ok; ++c) {
     const int child = c ? r : l;
-    // B operand: P_c[i][j], N = i, K = j; eight 16-byte loads per thread in
-    // flight before the split
-    {
+    // B operand: P_c[i][j], N = i, K = j: the split image in one bulk copy, or
+    // eight 16-byte loads per thread in flight before the split
+    if (pimg) {
+      if (tid == 0) {
+        b_pending = true;
+        mbar_arrive_expect_tx(bar_b, uint32_t(2 * tc::kBbytes));
+        bulk_copy_g2s(sB, pimg + ((size_t(b) * a.B + child) * a.K + k) * 2 * SP * SP, uint32_t(2 * tc::kBbytes), bar_b);
+      }
+    } else {
       float4 pv[8];
 #pragma unroll
       for (int m = 0; m < 8; ++m) {
@@ -204,7 +217,13 @@ __global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const 
     __syncthreads();
     tc::fence_after_sync();
     tmem = *tslot;
-    if (tid == 0) {
+    if (tid == 0 && b_pending) {  // the image has landed
+      if (mbar_wait_bounded(bar_b, phase_b, timeout_ns)) {
+        b_pending = false;
+        phase_b ^= 1;
+      }
+    }
+    if (tid == 0 && !b_pending) {
       constexpr uint32_t idesc = tc::idesc_tf32(128, 64);
       const uint32_t d = tmem + uint32_t(64 * c);
       const uint32_t ab = smem_u32(sA), as = ab + tc::kAbytes;
@@ -218,6 +237,8 @@ __global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const 
         tc::mma_tf32(d, das, dbb, idesc, 1u);
       }
       tc::mma_commit(bar);
+    } else if (tid == 0) {
+      mbar_arrive(bar);  // no MMAs (the image never landed): complete the phase; the side fails below
     }
     if (c == 0 && r >= a.tips) {  // while the MMAs run: the other child's rows into L2 (lane j: rows j, j + 32)
       const float *nxt = a.part + ((size_t(b) * a.I + (r - a.tips)) * a.K + k) * SP * size_t(a.Npad) + n0 + 32 * warp;
@@ -226,13 +247,16 @@ __global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const 
       asm volatile("prefetch.global.L2 [%0];" ::"l"(nxt + size_t(lane + 32) * a.Npad));
     }
     // every thread sees the side's MMAs complete before the shared memory is restaged or TMEM read
-    ok = mbar_wait_bounded(bar, phase, timeout_ns);
+    ok = mbar_wait_bounded(bar, phase, timeout_ns) && !(tid == 0 && b_pending);
     tc::fence_after_sync();
     ok = !__syncthreads_or(!ok);
     if (ok) phase ^= 1;
   }
   if (!ok) {
-    if (tid == 0) atomicExch(status, kDeviceTimeout);
+    if (tid == 0) {
+      atomicExch(status, kDeviceTimeout);
+      if (b_pending) mbar_wait_bounded(bar_b, phase_b, 100000000ull);  // the image copy lands before exit
+    }
     mbar_wait_bounded(bar, phase, 100000000ull);  // give the tensor cores a last chance before freeing TMEM
   } else {
     // this thread's pattern = TMEM lane 32 * warp + lane

@@ -78,18 +78,22 @@ constexpr int kImgFloats = 2 * 64 * 64;   // one P^T image: big then small
 
 }  // namespace tcb
 
-// P^T images for GEMM2: image m (sample, branch, category) holds P_m^T in the
-// K-major layout (row j, K element i, LBO = 1024 B) as TF32 big then small.
-// One thread per output float (coalesced stores).
-__global__ void __launch_bounds__(256) wide_pimage_kernel(const float *pmat, float *img, long long count) {
+// Split K-major images of the transition matrices, one per (sample, branch,
+// category), TF32 big then small (LBO = 1024 B between 4-element K groups):
+// transposed = 1 holds P^T (row j, K element i: the adjoint's GEMM2 B),
+// transposed = 0 holds P (row i, K element j: the post-order's B).  One
+// thread per output float (coalesced stores).
+__global__ void __launch_bounds__(256) wide_pimage_kernel(const float *pmat, float *img, long long count,
+                                                          int transposed) {
   const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= count * 4096) return;
   const long long m = t >> 12;
   const int o = int(t & 4095);
-  // o (a float index) -> byte offset 4o = (i >> 2) * 1024 + (j >> 3) * 128 + (j & 7) * 16 + (i & 3) * 4
+  // o (a float index) -> byte offset 4o = (kk >> 2) * 1024 + (row >> 3) * 128 + (row & 7) * 16 + (kk & 3) * 4
   const int byte = 4 * o;
-  const int i = (byte >> 10) * 4 + ((byte & 15) >> 2);
-  const int j = ((byte & 1023) >> 7) * 8 + ((byte & 127) >> 4);
+  const int kk = (byte >> 10) * 4 + ((byte & 15) >> 2);
+  const int row = ((byte & 1023) >> 7) * 8 + ((byte & 127) >> 4);
+  const int i = transposed ? kk : row, j = transposed ? row : kk;
   float big, small;
   tc::split_tf32(pmat[m * 4096 + i * 64 + j], big, small);
   img[m * tcb::kImgFloats + o] = big;

@@ -162,6 +162,8 @@ def estimate_bytes(ds: Dataset, slots: int, precision: str, slab: int = 0) -> in
     part = slots * T * K * npad * (sp * elem * (3 if precision == "f32" and sp == 64 else 1) + 4)
     chunks = min(64, max(1, -(-304 // (slots * K))))
     grad = slots * B * K * sp * sp * (chunks * elem + elem + 8)
+    if precision == "f32" and sp == 64:  # the tensor-core kernels' split P and P^T images
+        grad += slots * B * K * 2 * 2 * sp * sp * 4
     return int(1.1 * (part + grad + T * -(-N // 128) * 128)) + (64 << 20)
 
 
