@@ -239,7 +239,9 @@ int tt_plans_gradient(int32_t count, tt_plan *const *plans,
  *   Q = U diag(eigenvalues) W and W = U^-1 (device);
  *   status: device int32, set to TT_ERR_UNSUPPORTED if a matrix did not
  *   converge (never cleared here).
- * 1 <= S <= 64.  Cyclic Jacobi, one CTA per matrix.
+ * 1 <= S <= 64.  FP32 Jacobi, two FP64 Newton-Schulz steps on its
+ * eigenvectors, FP64 Jacobi on the rotated matrix; 7 launches on `stream`,
+ * no workspace.
  */
 int tt_reversible_eigen(int32_t batch, int32_t state_count, const double *q,
                         const double *frequencies, double *eigenvalues,

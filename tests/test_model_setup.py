@@ -110,6 +110,69 @@ def test_device_eigen_system_matches_lapack(S):
         assert float((p - p_ref).abs().max()) <= 1e-12, (S, t)
 
 
+def _eigen_cases(case):
+    """Rate matrices with repeated or nearly repeated eigenvalues: JC69 and
+    F81 (one eigenvalue of multiplicity S - 1), K80 (two repeated), a 61-state
+    matrix with a pair of eigenvalues 1e-9 apart, and a sparse codon-like one."""
+    rng = np.random.default_rng(7)
+    if case in ("jc4", "f81_20"):
+        S = 4 if case == "jc4" else 20
+        pi = np.full(S, 1.0 / S) if case == "jc4" else rng.dirichlet(np.ones(S))
+        q = np.tile(pi, (S, 1))
+    elif case == "k80_4":
+        S, pi = 4, np.full(4, 0.25)
+        q = np.ones((4, 4))
+        for i, j in ((0, 2), (2, 0), (1, 3), (3, 1)):
+            q[i, j] = 3.0  # transitions
+        q = q * pi[None]
+    elif case == "sparse61":
+        S, pi = 61, rng.dirichlet(np.ones(61))
+        r = rng.gamma(1.0, 1.0, (S, S)) * (rng.random((S, S)) < 0.15)
+        r = np.triu(r, 1) + np.triu(r, 1).T + 1e-3 * (np.ones((S, S)) - np.eye(S))
+        q = r * pi[None]
+    else:  # near_tie61: A = V diag(lambda) V^T with lambda_1 - lambda_0 = 1e-9
+        S, pi = 61, rng.dirichlet(np.ones(61))
+        lam = -np.sort(rng.uniform(0.1, 3.0, S))
+        lam[1] = lam[0] + 1e-9
+        v, _ = np.linalg.qr(rng.standard_normal((S, S)))
+        a = (v * lam) @ v.T
+        sp = np.sqrt(pi)
+        return (a / sp[:, None] * sp[None, :])[None], pi[None]
+    np.fill_diagonal(q, 0.0)
+    np.fill_diagonal(q, -q.sum(1))
+    q /= -(np.diag(q) * pi).sum()
+    return q[None], pi[None]
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("case", ["jc4", "k80_4", "f81_20", "sparse61", "near_tie61"])
+def test_device_eigen_with_repeated_or_close_eigenvalues(case):
+    """Checks that do not depend on the basis chosen inside a repeated
+    eigenspace: eigenvalues against LAPACK, W = U^-1, Q = U diag(lambda) W and
+    P(t) against LAPACK's eigen form."""
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from torchtree_gb300 import substitution
+
+    q, pi = _eigen_cases(case)
+    S = q.shape[-1]
+    qt, pit = torch.tensor(q), torch.tensor(pi)
+    lam, u, w = (t.cpu() for t in substitution.device_eigen(qt.cuda(), pit.cuda()))
+    sp = pit.sqrt()
+    a = sp.unsqueeze(-1) * qt / sp.unsqueeze(-2)
+    lam_ref, v_ref = torch.linalg.eigh(a)
+    scale = lam_ref.abs().amax(-1, keepdim=True)
+    assert float(((lam - lam_ref).abs() / scale).max()) <= 1e-12, case
+    assert float((u @ w - torch.eye(S, dtype=torch.float64)).abs().max()) <= 1e-12, case
+    recon = u @ torch.diag_embed(lam) @ w
+    assert float(((recon - qt).abs().amax((-1, -2)) / qt.abs().amax((-1, -2))).max()) <= 1e-11, case
+    u_ref, w_ref = v_ref / sp.unsqueeze(-1), v_ref.transpose(-1, -2) * sp.unsqueeze(-2)
+    for t in (0.01, 0.7):
+        pt = u @ torch.diag_embed(torch.exp(lam * t)) @ w
+        p_ref = u_ref @ torch.diag_embed(torch.exp(lam_ref * t)) @ w_ref
+        assert float((pt - p_ref).abs().max()) <= 1e-12, (case, t)
+
+
 @pytest.mark.gpu
 @pytest.mark.parametrize("k", [4, 8])
 def test_device_gamma_quantiles_match_host_and_scipy(k):

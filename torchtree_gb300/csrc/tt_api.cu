@@ -8,6 +8,8 @@
 #include <cstdio>
 #include <cstdlib>
 #include <cstring>
+#include <map>
+#include <mutex>
 #include <set>
 #include <string>
 #include <vector>
@@ -37,6 +39,22 @@ constexpr unsigned long long kTimeoutNs = 2000000000ull;  // bounded device wait
 namespace tt {
 // Error reporting for entry points defined in other translation units.
 int record_error(int code, const char *msg) { return fail(code, msg); }
+
+cudaError_t kernel_smem(const void *func, size_t bytes, bool max_carveout) {
+  static std::mutex mu;
+  static std::map<std::pair<const void *, int>, size_t> done;  // largest size set per (kernel, device)
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  std::lock_guard<std::mutex> lock(mu);
+  auto it = done.find({func, dev});
+  if (it != done.end() && it->second >= bytes) return cudaSuccess;
+  e = cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, int(bytes));
+  if (e == cudaSuccess && max_carveout)
+    e = cudaFuncSetAttribute(func, cudaFuncAttributePreferredSharedMemoryCarveout, int(cudaSharedmemCarveoutMaxShared));
+  if (e == cudaSuccess) done[{func, dev}] = bytes;
+  return e;
+}
 }  // namespace tt
 
 

@@ -9,16 +9,27 @@
 // Q = U diag(lambda) W with U = Pi^-1/2 V, W = V^T Pi^1/2 (V is orthogonal,
 // so W is the inverse of U without a matrix inverse).
 //
-// The eigensolver is the cyclic Jacobi method with the parallel
-// (round-robin) ordering of Brent and Luk (1985): one CTA per matrix, A and V
-// in shared memory; each round rotates n/2 disjoint (p, q) pairs at once
-// (Golub & Van Loan, Algorithm 8.4.2 "sym.schur2" for each rotation), so that
-// every pair is met once per sweep; sweeps stop when the off-diagonal norm is
-// below 1e-14 of the Frobenius norm (at most 40 sweeps; a matrix that does
-// not get there sets the status word to TT_ERR_UNSUPPORTED).  Eigenvalues are
-// returned in ascending order, as eigh returns them.
+// FP64 arithmetic is scarce on this GPU (a few FP64 FMAs per cycle per SM),
+// so the solver does most of its sweeps in FP32 and spreads the FP64 matrix
+// products over many CTAs:
+//  1. eigen_start_kernel, one CTA per matrix: cyclic Jacobi in FP32 (parallel
+//     round-robin ordering of Brent and Luk, 1985; each rotation Golub & Van
+//     Loan, Algorithm 8.4.2 "sym.schur2"): eigenvectors X0 good to ~1e-5;
+//  2. two Newton-Schulz steps X <- X (3I - X^T X) / 2 (Higham, "Functions of
+//     Matrices", 8.3) in FP64, each squaring X's distance from orthonormal
+//     (eigen_gram_kernel forms R = I - X^T X, eigen_orth_kernel X <- X + X R/2),
+//     kEigRows rows of the products per CTA;
+//  3. eigen_gram_kernel forms S = X^T A X (off-diagonal ~1e-5 of its norm) and
+//     eigen_finish_kernel, one CTA per matrix, diagonalises S by FP64 Jacobi
+//     sweeps accumulated into X (quadratic convergence from there: two or
+//     three sweeps) to 1e-14 of the Frobenius norm.
+// A matrix whose FP64 sweeps do not converge (30 of them) sets the status
+// word to TT_ERR_UNSUPPORTED.  Eigenvalues are returned in ascending order,
+// as eigh returns them.  The buffers u, w and eigenvalues hold X, S / R and
+// R's diagonal between the steps, so the call needs no workspace.
 #include <math.h>
 
+#include <algorithm>
 #include <string>
 
 #include "../../include/torchtree_gb300.h"
@@ -32,6 +43,7 @@ namespace {
 constexpr int kEigMax = 64;      // largest state count
 constexpr int kEigLd = kEigMax + 1;
 constexpr int kEigThreads = 256;
+constexpr int kEigRows = 4;  // rows of the FP64 products per CTA
 
 // pair i of round r in the round-robin over m players (m even): player m-1
 // stays, the others rotate
@@ -50,112 +62,284 @@ __device__ __forceinline__ void rr_pair(int r, int i, int m, int &p, int &q) {
   }
 }
 
-__global__ void __launch_bounds__(kEigThreads) reversible_eigen_kernel(const double *q, const double *pi, int n,
-                                                                       double *lam, double *U, double *W,
-                                                                       int *status) {
-  extern __shared__ __align__(16) double esm[];
-  double *A = esm;                     // [n][kEigLd]
-  double *V = A + kEigMax * kEigLd;    // [n][kEigLd]
-  double *cs = V + kEigMax * kEigLd;   // [kEigMax/2][2] rotation (c, s) per pair
-  double *red = cs + kEigMax;          // [kEigThreads/32] reduction
-  double *sq = red + kEigThreads / 32; // [n] sqrt(pi)
-  __shared__ int flag;
-  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
-  const double *qb = q + size_t(b) * n * n;
-  for (int i = tid; i < n; i += kEigThreads) sq[i] = sqrt(pi[size_t(b) * n + i]);
-  __syncthreads();
-  // A = Pi^1/2 Q Pi^-1/2 from the lower triangle (mirrored), V = I
-  for (int e = tid; e < n * n; e += kEigThreads) {
-    const int i = e / n, j = e - i * n;
-    const int r = i >= j ? i : j, c = i >= j ? j : i;
-    A[i * kEigLd + j] = sq[r] * qb[r * n + c] / sq[c];
-    V[i * kEigLd + j] = i == j ? 1.0 : 0.0;
-  }
-  __syncthreads();
+// Cyclic Jacobi sweeps on A (n x n, leading dimension kEigLd) accumulating
+// the rotations into V, in T arithmetic, until the off-diagonal norm squared
+// is at most tol2 times the Frobenius norm squared; true when converged within
+// max_sweeps.  cs and pq hold a round's rotations and pairs.  Called by the
+// whole CTA.
+template <typename T>
+__device__ bool jacobi_sweeps(T *A, T *V, T *cs, int *pq, double *red, int *flag, int n, double tol2,
+                              int max_sweeps) {
+  constexpr int NW = kEigThreads / 32;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int m = n + (n & 1);  // an odd n gets a dummy player that never rotates
   const int npairs = m / 2;
-  int sweep = 0;
-  for (; sweep < 40; ++sweep) {
+  for (int sweep = 0; sweep <= max_sweeps; ++sweep) {
     // convergence: off-diagonal norm against the Frobenius norm
     double off = 0.0, tot = 0.0;
-    for (int e = tid; e < n * n; e += kEigThreads) {
-      const int i = e / n, j = e - i * n;
-      const double v = A[i * kEigLd + j];
-      tot += v * v;
-      if (i != j) off += v * v;
-    }
+    for (int i = warp; i < n; i += NW)
+      for (int j = lane; j < n; j += 32) {
+        const double v = double(A[i * kEigLd + j]);
+        tot += v * v;
+        if (i != j) off += v * v;
+      }
     for (int o = 16; o; o >>= 1) {
       off += __shfl_xor_sync(0xffffffffu, off, o);
       tot += __shfl_xor_sync(0xffffffffu, tot, o);
     }
-    if (lane == 0) red[warp] = off;
-    __syncthreads();
-    if (tid == 0) {
-      double s = 0.0;
-      for (int w = 0; w < kEigThreads / 32; ++w) s += red[w];
-      off = s;
+    if (lane == 0) {
+      red[warp] = off;
+      red[NW + warp] = tot;
     }
     __syncthreads();
-    if (lane == 0) red[warp] = tot;
-    __syncthreads();
     if (tid == 0) {
-      double s = 0.0;
-      for (int w = 0; w < kEigThreads / 32; ++w) s += red[w];
-      flag = !(off > 1e-28 * s) || n == 1;
+      double so = 0.0, st = 0.0;
+      for (int w = 0; w < NW; ++w) {
+        so += red[w];
+        st += red[NW + w];
+      }
+      *flag = !(so > tol2 * st) || n == 1;
     }
     __syncthreads();
-    if (flag) break;
+    if (*flag) return true;
+    if (sweep == max_sweeps) return false;
     for (int r = 0; r < m - 1; ++r) {
-      // rotations of this round's pairs
+      // this round's pairs and rotations
       if (tid < npairs) {
         int p, qq;
         rr_pair(r, tid, m, p, qq);
-        double c = 1.0, s = 0.0;
+        T c = T(1), s = T(0);
         if (qq < n) {
-          const double apq = A[p * kEigLd + qq];
-          if (apq != 0.0) {
-            const double tau = (A[qq * kEigLd + qq] - A[p * kEigLd + p]) / (2.0 * apq);
-            double t;
-            if (fabs(tau) > 1e150) t = 0.5 / tau;
-            else t = (tau >= 0.0 ? 1.0 : -1.0) / (fabs(tau) + sqrt(1.0 + tau * tau));
-            c = 1.0 / sqrt(1.0 + t * t);
+          const T apq = A[p * kEigLd + qq];
+          if (apq != T(0)) {
+            const T tau = (A[qq * kEigLd + qq] - A[p * kEigLd + p]) / (T(2) * apq);
+            T t;
+            if (fabs(tau) > (sizeof(T) == 4 ? T(1e18) : T(1e150))) t = T(0.5) / tau;
+            else t = (tau >= T(0) ? T(1) : T(-1)) / (fabs(tau) + sqrt(T(1) + tau * tau));
+            c = T(1) / sqrt(T(1) + t * t);
             s = t * c;
           }
         }
         cs[2 * tid] = c;
         cs[2 * tid + 1] = s;
+        pq[2 * tid] = p;
+        pq[2 * tid + 1] = qq;
       }
       __syncthreads();
-      // rows: A <- J^T A  (rows p, q of every pair)
-      for (int e = tid; e < npairs * n; e += kEigThreads) {
-        const int i = e / n, j = e - i * n;
-        int p, qq;
-        rr_pair(r, i, m, p, qq);
-        if (qq >= n) continue;
-        const double c = cs[2 * i], s = cs[2 * i + 1];
-        const double ap = A[p * kEigLd + j], aq = A[qq * kEigLd + j];
-        A[p * kEigLd + j] = c * ap - s * aq;
-        A[qq * kEigLd + j] = s * ap + c * aq;
+      // rows: A <- J^T A (rows p, q of every pair), a warp per pair, lanes
+      // along the row.  Distinct pairs touch distinct rows, so all of a
+      // thread's loads go first (independent shared-memory latencies).
+      {
+        constexpr int PK = (kEigMax / 2 + NW - 1) / NW;  // pairs per warp
+        T ap[PK][2], aq[PK][2], cr[PK], sr[PK];
+        int pr[PK], qr[PK];
+#pragma unroll
+        for (int k = 0; k < PK; ++k) {
+          const int i = warp + k * NW;
+          pr[k] = i < npairs ? pq[2 * i] : 0;
+          qr[k] = i < npairs ? pq[2 * i + 1] : n;
+          cr[k] = i < npairs ? cs[2 * i] : T(1);
+          sr[k] = i < npairs ? cs[2 * i + 1] : T(0);
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int j = lane + 32 * h;
+            const bool go = qr[k] < n && sr[k] != T(0) && j < n;  // not the dummy player nor the identity
+            ap[k][h] = go ? A[pr[k] * kEigLd + j] : T(0);
+            aq[k][h] = go ? A[qr[k] * kEigLd + j] : T(0);
+          }
+        }
+#pragma unroll
+        for (int k = 0; k < PK; ++k)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int j = lane + 32 * h;
+            if (qr[k] < n && sr[k] != T(0) && j < n) {
+              A[pr[k] * kEigLd + j] = cr[k] * ap[k][h] - sr[k] * aq[k][h];
+              A[qr[k] * kEigLd + j] = sr[k] * ap[k][h] + cr[k] * aq[k][h];
+            }
+          }
       }
       __syncthreads();
-      // columns: A <- A J, V <- V J
-      for (int e = tid; e < npairs * n; e += kEigThreads) {
-        const int i = e / n, row = e - i * n;
-        int p, qq;
-        rr_pair(r, i, m, p, qq);
-        if (qq >= n) continue;
-        const double c = cs[2 * i], s = cs[2 * i + 1];
-        const double ap = A[row * kEigLd + p], aq = A[row * kEigLd + qq];
-        A[row * kEigLd + p] = c * ap - s * aq;
-        A[row * kEigLd + qq] = s * ap + c * aq;
-        const double vp = V[row * kEigLd + p], vq = V[row * kEigLd + qq];
-        V[row * kEigLd + p] = c * vp - s * vq;
-        V[row * kEigLd + qq] = s * vp + c * vq;
+      // columns: A <- A J, V <- V J, a warp per row, lanes over the pairs
+      {
+        constexpr int RK = (kEigMax + NW - 1) / NW;  // rows per warp
+        const int i = lane;                           // npairs <= 32
+        const int pc = i < npairs ? pq[2 * i] : 0, qc = i < npairs ? pq[2 * i + 1] : n;
+        const T c = i < npairs ? cs[2 * i] : T(1), s = i < npairs ? cs[2 * i + 1] : T(0);
+        const bool go = qc < n && s != T(0);
+        T a0[RK], a1[RK], v0[RK], v1[RK];
+#pragma unroll
+        for (int k = 0; k < RK; ++k) {
+          const int row = warp + k * NW;
+          const bool g = go && row < n;
+          a0[k] = g ? A[row * kEigLd + pc] : T(0);
+          a1[k] = g ? A[row * kEigLd + qc] : T(0);
+          v0[k] = g ? V[row * kEigLd + pc] : T(0);
+          v1[k] = g ? V[row * kEigLd + qc] : T(0);
+        }
+#pragma unroll
+        for (int k = 0; k < RK; ++k) {
+          const int row = warp + k * NW;
+          if (go && row < n) {
+            A[row * kEigLd + pc] = c * a0[k] - s * a1[k];
+            A[row * kEigLd + qc] = s * a0[k] + c * a1[k];
+            V[row * kEigLd + pc] = c * v0[k] - s * v1[k];
+            V[row * kEigLd + qc] = s * v0[k] + c * v1[k];
+          }
+        }
       }
       __syncthreads();
     }
   }
-  if (tid == 0 && sweep == 40) atomicExch(status, TT_ERR_UNSUPPORTED);
+  return false;
+}
+
+// sqrt(pi) of matrix b into sq, then A = Pi^1/2 Q Pi^-1/2 from the lower
+// triangle (mirrored) into A (leading dimension kEigLd) as T; whole CTA.
+template <typename T>
+__device__ void load_symmetrised(const double *q, const double *pi, int b, int n, double *sq, T *A) {
+  constexpr int NW = kEigThreads / 32;
+  const double *qb = q + size_t(b) * n * n;
+  for (int i = threadIdx.x; i < n; i += kEigThreads) sq[i] = sqrt(pi[size_t(b) * n + i]);
+  __syncthreads();
+  for (int i = threadIdx.x >> 5; i < n; i += NW)
+    for (int j = threadIdx.x & 31; j < n; j += 32) {
+      const int r = i >= j ? i : j, c = i >= j ? j : i;
+      A[i * kEigLd + j] = T(sq[r] * qb[r * n + c] / sq[c]);
+    }
+  __syncthreads();
+}
+
+// Step 1, one CTA per matrix: FP32 Jacobi sweeps on A until the off-diagonal
+// norm is below 1e-6 of the Frobenius norm (at most 10 sweeps: FP32 rounding
+// may stop short of that); the eigenvector matrix X0, in FP64, into x.
+__global__ void __launch_bounds__(kEigThreads) eigen_start_kernel(const double *q, const double *pi, int n,
+                                                                  double *x) {
+  constexpr int NW = kEigThreads / 32;
+  __shared__ float A[kEigMax * kEigLd], V[kEigMax * kEigLd], cs[kEigMax];
+  __shared__ int pq[kEigMax];
+  __shared__ double red[2 * NW], sq[kEigMax];
+  __shared__ int flag;
+  const int b = blockIdx.x, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  load_symmetrised(q, pi, b, n, sq, A);
+  for (int i = warp; i < n; i += NW)
+    for (int j = lane; j < n; j += 32) V[i * kEigLd + j] = i == j ? 1.0f : 0.0f;
+  __syncthreads();
+  jacobi_sweeps<float>(A, V, cs, pq, red, &flag, n, 1e-12, 10);
+  double *xb = x + size_t(b) * n * n;
+  for (int i = warp; i < n; i += NW)
+    for (int j = lane; j < n; j += 32) xb[i * n + j] = double(V[i * kEigLd + j]);
+}
+
+// Step 2 / 3, kEigRows rows per CTA (grid: row blocks x matrices), FP64: for
+// the current eigenvector estimate X (x),
+//   R = I - X^T X   (strict lower triangle into w, diagonal into lam),
+//   S = X^T A X     (upper triangle with the diagonal into w; with_s only).
+// Both are symmetric, so one n x n buffer holds the two.
+__global__ void __launch_bounds__(kEigThreads) eigen_gram_kernel(const double *q, const double *pi, int n,
+                                                                 const double *x, double *w, double *lam,
+                                                                 int with_s) {
+  constexpr int NW = kEigThreads / 32;
+  extern __shared__ __align__(16) double gsm[];
+  double *A = gsm;                      // [n][kEigLd]
+  double *X = A + kEigMax * kEigLd;     // [n][kEigLd]
+  double *M = X + kEigMax * kEigLd;     // [kEigRows][kEigLd]: rows of X^T A
+  double *sq = M + kEigRows * kEigLd;   // [n]
+  const int b = blockIdx.y, i0 = blockIdx.x * kEigRows, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int rows = min(kEigRows, n - i0);
+  const double *xb = x + size_t(b) * n * n;
+  for (int i = warp; i < n; i += NW)
+    for (int j = lane; j < n; j += 32) X[i * kEigLd + j] = xb[i * n + j];
+  if (with_s) load_symmetrised(q, pi, b, n, sq, A);
+  else __syncthreads();
+  double *wb = w + size_t(b) * n * n;
+  // R rows i0 .. i0 + rows - 1, columns j <= i; two warps per row
+  for (int t = warp; t < 2 * rows; t += NW) {
+    const int r = t >> 1, i = i0 + r;
+    for (int j = (t & 1) * 32 + lane; j <= i; j += 64) {
+      double s = 0.0;
+      for (int k = 0; k < n; ++k) s = fma(X[k * kEigLd + i], X[k * kEigLd + j], s);
+      if (j < i) wb[i * n + j] = -s;
+      else lam[size_t(b) * n + i] = 1.0 - s;
+    }
+  }
+  if (!with_s) return;
+  for (int t = warp; t < 2 * rows; t += NW) {
+    const int r = t >> 1, i = i0 + r;
+    for (int j = (t & 1) * 32 + lane; j < n; j += 64) {
+      double s = 0.0;
+      for (int k = 0; k < n; ++k) s = fma(X[k * kEigLd + i], A[k * kEigLd + j], s);
+      M[r * kEigLd + j] = s;
+    }
+  }
+  __syncthreads();
+  for (int t = warp; t < 2 * rows; t += NW) {
+    const int r = t >> 1, i = i0 + r;
+    for (int j = i + (t & 1) * 32 + lane; j < n; j += 64) {
+      double s = 0.0;
+      for (int k = 0; k < n; ++k) s = fma(M[r * kEigLd + k], X[k * kEigLd + j], s);
+      wb[i * n + j] = s;
+    }
+  }
+}
+
+// Step 2, kEigRows rows per CTA, FP64: one Newton-Schulz step
+// X <- X + X R / 2 = X (3I - X^T X) / 2 with R = I - X^T X from the last
+// eigen_gram_kernel.  A row of the result needs only that row of X, so each
+// CTA updates its own rows in place.
+__global__ void __launch_bounds__(kEigThreads) eigen_orth_kernel(int n, double *x, const double *w,
+                                                                 const double *lam) {
+  constexpr int NW = kEigThreads / 32;
+  extern __shared__ __align__(16) double osm[];
+  double *R = osm;                      // [n][kEigLd], halved
+  double *Xr = R + kEigMax * kEigLd;    // [kEigRows][kEigLd]
+  const int b = blockIdx.y, i0 = blockIdx.x * kEigRows, lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int rows = min(kEigRows, n - i0);
+  const double *wb = w + size_t(b) * n * n, *rd = lam + size_t(b) * n;
+  double *xb = x + size_t(b) * n * n;
+  for (int i = warp; i < n; i += NW)
+    for (int j = lane; j < n; j += 32)
+      R[i * kEigLd + j] = 0.5 * (i == j ? rd[i] : wb[max(i, j) * n + min(i, j)]);
+  for (int r = warp; r < rows; r += NW)
+    for (int j = lane; j < n; j += 32) Xr[r * kEigLd + j] = xb[(i0 + r) * n + j];
+  __syncthreads();
+  for (int t = warp; t < 2 * rows; t += NW) {
+    const int r = t >> 1;
+    for (int j = (t & 1) * 32 + lane; j < n; j += 64) {
+      double s = Xr[r * kEigLd + j];
+      for (int k = 0; k < n; ++k) s = fma(Xr[r * kEigLd + k], R[k * kEigLd + j], s);
+      xb[(i0 + r) * n + j] = s;
+    }
+  }
+}
+
+// Step 3, one CTA per matrix, FP64: S = X^T A X (in W, upper triangle) and X
+// (in U); FP64 Jacobi sweeps on S, accumulated into X, to 1e-14 of the
+// Frobenius norm; a matrix that does not converge in 30 sweeps sets the
+// status word.  Eigenvalues ascending, with U = Pi^-1/2 X and W = X^T Pi^1/2.
+__global__ void __launch_bounds__(kEigThreads) eigen_finish_kernel(const double *pi, int n, double *lam, double *U,
+                                                                   double *W, int *status) {
+  constexpr int NW = kEigThreads / 32;
+  extern __shared__ __align__(16) double fsm[];
+  double *A = fsm;                       // [n][kEigLd] S, symmetric
+  double *V = A + kEigMax * kEigLd;      // [n][kEigLd] X
+  double *cs = V + kEigMax * kEigLd;     // [kEigMax/2][2]
+  double *red = cs + kEigMax;            // [2 * NW]
+  double *sq = red + 2 * NW;             // [n]
+  int *pq = reinterpret_cast<int *>(sq + kEigMax);  // [kEigMax/2][2]
+  __shared__ int flag;
+  const int b = blockIdx.x, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const size_t mo = size_t(b) * n * n;
+  for (int i = tid; i < n; i += kEigThreads) sq[i] = sqrt(pi[size_t(b) * n + i]);
+  for (int i = warp; i < n; i += NW)
+    for (int j = lane; j < n; j += 32) {
+      A[i * kEigLd + j] = W[mo + size_t(min(i, j)) * n + max(i, j)];
+      V[i * kEigLd + j] = U[mo + size_t(i) * n + j];
+    }
+  __syncthreads();
+  // (every thread's reads of U and W are done: the sweeps begin with a barrier)
+  const bool ok = jacobi_sweeps<double>(A, V, cs, pq, red, &flag, n, 1e-28, 30);
+  if (tid == 0 && !ok) atomicExch(status, TT_ERR_UNSUPPORTED);
   // ascending order: the rank of each eigenvalue (ties by index)
   for (int k = tid; k < n; k += kEigThreads) {
     const double lk = A[k * kEigLd + k];
@@ -197,14 +381,31 @@ int tt_reversible_eigen(int32_t batch, int32_t state_count, const double *q, con
     return tt::efail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
   if (batch < 1 || state_count < 1 || state_count > tt::kEigMax)
     return tt::efail(TT_ERR_INVALID_ARGUMENT, "tt_reversible_eigen: batch >= 1 and 1 <= state_count <= 64");
-  const size_t smem = (2 * size_t(tt::kEigMax) * tt::kEigLd + tt::kEigMax + tt::kEigThreads / 32 + tt::kEigMax) *
-                      sizeof(double);
+  using namespace tt;
+  const int n = state_count;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
-  cudaError_t e = cudaFuncSetAttribute(tt::reversible_eigen_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(smem));
-  if (e == cudaSuccess) {
-    tt::reversible_eigen_kernel<<<batch, tt::kEigThreads, smem, s>>>(q, frequencies, state_count, eigenvalues, u, w,
-                                                                      status);
+  const size_t gram_smem = (2 * size_t(kEigMax) * kEigLd + kEigRows * kEigLd + kEigMax) * sizeof(double);
+  const size_t orth_smem = (size_t(kEigMax) * kEigLd + kEigRows * kEigLd) * sizeof(double);
+  const size_t finish_smem =
+      (2 * size_t(kEigMax) * kEigLd + kEigMax + 2 * (kEigThreads / 32) + kEigMax) * sizeof(double) +
+      kEigMax * sizeof(int);
+  cudaError_t e = kernel_smem(eigen_gram_kernel, gram_smem);
+  if (e == cudaSuccess) e = kernel_smem(eigen_orth_kernel, orth_smem);
+  if (e == cudaSuccess) e = kernel_smem(eigen_finish_kernel, finish_smem);
+  // matrices in groups of at most 65,535 (the grid's y extent of the row-block kernels)
+  for (int b0 = 0; e == cudaSuccess && b0 < batch; b0 += 65535) {
+    const int nb = std::min(batch - b0, 65535);
+    const size_t mo = size_t(b0) * n * n, vo = size_t(b0) * n;
+    const double *qb = q + mo, *pib = frequencies + vo;
+    double *ub = u + mo, *wb = w + mo, *lb = eigenvalues + vo;
+    const dim3 rows_grid((n + kEigRows - 1) / kEigRows, nb);
+    eigen_start_kernel<<<nb, kEigThreads, 0, s>>>(qb, pib, n, ub);
+    for (int it = 0; it < 2; ++it) {
+      eigen_gram_kernel<<<rows_grid, kEigThreads, gram_smem, s>>>(qb, pib, n, ub, wb, lb, 0);
+      eigen_orth_kernel<<<rows_grid, kEigThreads, orth_smem, s>>>(n, ub, wb, lb);
+    }
+    eigen_gram_kernel<<<rows_grid, kEigThreads, gram_smem, s>>>(qb, pib, n, ub, wb, lb, 1);
+    eigen_finish_kernel<<<nb, kEigThreads, finish_smem, s>>>(pib, n, lb, ub, wb, status);
     e = cudaGetLastError();
   }
   return e == cudaSuccess ? TT_OK : tt::efail(TT_ERR_CUDA, std::string("eigen launch: ") + cudaGetErrorString(e));

@@ -266,8 +266,7 @@ int tt_transition_matrices_expm(int32_t batch, int32_t state_count, int32_t bran
   if (size_t(branch_count) * category_count > 0x7fffffffu || batch > 65535)
     return tt::xfail(TT_ERR_INVALID_ARGUMENT, "too many matrices for one launch");
   const size_t smem = tt::expm_smem_bytes(state_count);
-  cudaError_t e = cudaFuncSetAttribute(tt::expm_pmatrix_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(smem));
+  cudaError_t e = tt::kernel_smem(tt::expm_pmatrix_kernel, smem);
   if (e == cudaSuccess) {
     tt::expm_pmatrix_kernel<<<dim3(branch_count * category_count, batch), tt::kExpmThreads, smem,
                               static_cast<cudaStream_t>(stream)>>>(q, branch_lengths, category_rates, state_count,
@@ -288,8 +287,7 @@ int tt_transition_matrices_expm_adjoint(int32_t batch, int32_t state_count, int3
   if (size_t(branch_count) * category_count > 0x7fffffffu || batch > 65535)
     return tt::xfail(TT_ERR_INVALID_ARGUMENT, "too many matrices for one launch");
   const size_t smem = tt::expm_smem_bytes(2 * state_count);
-  cudaError_t e = cudaFuncSetAttribute(tt::expm_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                       int(smem));
+  cudaError_t e = tt::kernel_smem(tt::expm_adjoint_kernel, smem);
   if (e == cudaSuccess) {
     tt::expm_adjoint_kernel<<<dim3(branch_count * category_count, batch), tt::kExpmThreads, smem,
                               static_cast<cudaStream_t>(stream)>>>(q, branch_lengths, category_rates, grad_matrices,

@@ -12,6 +12,17 @@ namespace tt {
 // Set the calling thread's tt_last_error() message; returns `code`.
 int record_error(int code, const char *msg);
 
+// Raise a kernel's dynamic shared-memory limit to `bytes` on the current
+// device; with max_carveout also prefer the largest shared-memory carveout.
+// The attribute is set once per (kernel, device) and size: later launches of
+// the same kernel make no attribute call, so a launch inside stream capture
+// or while the kernel runs on another stream touches no function state.
+cudaError_t kernel_smem(const void *func, size_t bytes, bool max_carveout = false);
+template <typename F>
+cudaError_t kernel_smem(F *func, size_t bytes, bool max_carveout = false) {
+  return kernel_smem(reinterpret_cast<const void *>(func), bytes, max_carveout);
+}
+
 // Pattern tile widths compiled per precision and pass (preferred first).
 // FP32 plans: both passes use one tile width (the stored partials are laid
 // out per tile): forward kTlFwdThreads threads x (kTlTile / kTlFwdThreads)

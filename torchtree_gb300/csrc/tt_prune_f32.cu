@@ -16,10 +16,7 @@ namespace {
 // CTAs the shared memory allows per SM are all resident
 template <typename F>
 cudaError_t set_smem(F kern, size_t smem) {
-  cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
-  if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(kern, cudaFuncAttributePreferredSharedMemoryCarveout, int(cudaSharedmemCarveoutMaxShared));
-  return e;
+  return kernel_smem(kern, smem, true);
 }
 
 template <int KQ>

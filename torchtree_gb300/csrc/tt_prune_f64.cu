@@ -14,12 +14,12 @@ cudaError_t launch_one(const PruneArgs<double> &a, int batch, cudaStream_t strea
   const dim3 grid(a.ntiles, batch);
   if (BACKWARD) {
     auto kern = prune_backward_kernel<double, 4, KMAX, TILE, kStages>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaError_t e = kernel_smem(kern, smem);
     if (e != cudaSuccess) return e;
     kern<<<grid, TILE, smem, stream>>>(a);
   } else {
     auto kern = prune_forward_kernel<double, 4, KMAX, TILE, kStages>;
-    cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+    cudaError_t e = kernel_smem(kern, smem);
     if (e != cudaSuccess) return e;
     kern<<<grid, TILE, smem, stream>>>(a);
   }

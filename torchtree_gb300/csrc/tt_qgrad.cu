@@ -282,8 +282,7 @@ cudaError_t launch_wide_qgrad(tt_plan *p, const double *lam, const double *U, co
                               const double *rates, double *dbl, double *part, int bchunk, int nchunks,
                               cudaStream_t s) {
   const size_t smem = 4 * SP * SP * sizeof(T) + SP * sizeof(T) + (SP / 4 + 2) * sizeof(double) + 16;
-  cudaError_t e =
-      cudaFuncSetAttribute(wide_qgrad_kernel<T, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaError_t e = kernel_smem(wide_qgrad_kernel<T, SP>, smem);
   if (e != cudaSuccess) return e;
   wide_qgrad_kernel<T, SP><<<dim3(nchunks, p->batch), 256, smem, s>>>(p->d_G, lam, U, W, bl, rates, p->S, p->B,
                                                                       p->K, bchunk, dbl, part);
@@ -325,8 +324,7 @@ int rate_matrix_gradient(tt_plan *p, const double *lam, const double *U, const d
               : launch_wide_qgrad<double, 64>(p, lam, U, W, bl, rates, dbl, p->d_qpart, bchunk, nchunks, s);
   }
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(qgrad_finish_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             int(2 * S * S * sizeof(double)));
+    e = kernel_smem(qgrad_finish_kernel, 2 * S * S * sizeof(double));
   if (e == cudaSuccess) {
     qgrad_finish_kernel<<<p->batch, 256, 2 * S * S * sizeof(double), s>>>(p->d_qpart, nchunks, U, W, S, K, dQ,
                                                                          drates);

@@ -339,7 +339,7 @@ int tt_ratio_transform(tt_time_tree *t, int32_t batch, const double *ratios, dou
   const size_t smem = 2 * size_t(t->T - 1) * sizeof(double);
   if (3 * size_t(t->T - 1) * sizeof(double) > 227 * 1024)
     return tfail(TT_ERR_UNSUPPORTED, "the ratio transform holds a sample's rows in shared memory: at most 9,600 tips");
-  cudaError_t e = cudaFuncSetAttribute(ratio_forward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaError_t e = tt::kernel_smem(ratio_forward_kernel, smem);
   if (e == cudaSuccess) {
     ratio_forward_kernel<<<batch, kTimeTreeThreads, smem, s>>>(t->d_lvl_nodes, t->d_lvl_off, t->levels, t->d_parent,
                                                                t->d_lb, t->d_times, ratios, heights, branch_lengths,
@@ -358,7 +358,7 @@ int tt_ratio_transform_backward(tt_time_tree *t, int32_t batch, const double *ra
   const size_t smem = 3 * size_t(t->T - 1) * sizeof(double);
   if (smem > 227 * 1024)
     return tfail(TT_ERR_UNSUPPORTED, "the ratio transform holds a sample's rows in shared memory: at most 9,600 tips");
-  cudaError_t e = cudaFuncSetAttribute(ratio_backward_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaError_t e = tt::kernel_smem(ratio_backward_kernel, smem);
   if (e == cudaSuccess) {
     ratio_backward_kernel<<<batch, kTimeTreeThreads, smem, s>>>(t->d_lvl_nodes, t->d_lvl_off, t->levels, t->d_kids,
                                                                 t->d_lb, ratios, heights, grad_heights,
@@ -379,7 +379,7 @@ int tt_constant_coalescent(tt_time_tree *t, int32_t batch, const double *heights
   while (m2 < I) m2 <<= 1;
   cudaStream_t s = static_cast<cudaStream_t>(stream);
   const size_t smem = size_t(m2 + n + T) * sizeof(double) + size_t(m2 + n) * sizeof(int);
-  cudaError_t e = cudaFuncSetAttribute(coalescent_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, int(smem));
+  cudaError_t e = tt::kernel_smem(coalescent_kernel, smem);
   if (e == cudaSuccess) {  // every internal node's gradient is written once: no clearing needed
     coalescent_kernel<<<batch, 256, smem, s>>>(t->d_tip_t, t->d_tip_i, heights, theta, T, m2, log_prob,
                                                grad_heights, grad_theta);

@@ -618,24 +618,43 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT, wide_bwd_min_blocks<T,
 template <typename T>
 __global__ void wide_grad_reduce_kernel(const T *gpart, double *G, int B, int nchunks, int K, int S, int SP,
                                         int accumulate) {
-  // one warp per (category, row) at a time, lanes along the row: coalesced chunk loads; the
-  // chunk sum in the plan's precision and a fixed order, then FP64 (FP64 arithmetic is scarce on
-  // this GPU and the chunk blocks themselves are in the plan's precision)
+  // four consecutive columns per thread, threads along the row: 16-byte (FP32) or 2 x 16-byte
+  // (FP64) loads of every chunk's block, the chunk sum in the plan's precision and a fixed
+  // order, then FP64 (FP64 arithmetic is scarce on this GPU and the chunk blocks themselves are
+  // in the plan's precision).  SP is a multiple of 4, so every load is aligned.
   const int br = blockIdx.x, b = blockIdx.y;
-  const int kss = K * S * S, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const int kss = K * S * S, q4 = SP / 4;
   const size_t cstride = size_t(K) * SP * SP;  // between chunks
   const T *base = gpart + (size_t(b) * B + br) * nchunks * cstride;
   double *gb = G + (size_t(b) * B + br) * kss;
-  for (int kr = threadIdx.x >> 5; kr < K * S; kr += nw) {
+  for (int e = threadIdx.x; e < K * S * q4; e += blockDim.x) {
+    const int kr = e / q4, j0 = (e - kr * q4) * 4;
+    if (j0 >= S) continue;
     const int k = kr / S, i = kr - k * S;
-    for (int j = lane; j < S; j += 32) {
-      const T *src = base + size_t(k) * SP * SP + i * SP + j;
-      T s = T(0);
+    const T *src = base + size_t(k) * SP * SP + i * SP + j0;
+    T s0 = T(0), s1 = T(0), s2 = T(0), s3 = T(0);
 #pragma unroll 4
-      for (int c = 0; c < nchunks; ++c) s += src[c * cstride];
-      double *g = gb + (size_t(k) * S + i) * S + j;
-      *g = accumulate ? *g + double(s) : double(s);
+    for (int c = 0; c < nchunks; ++c) {
+      const T *cs = src + c * cstride;
+      if constexpr (sizeof(T) == 4) {
+        const float4 v = *reinterpret_cast<const float4 *>(cs);
+        s0 += v.x;
+        s1 += v.y;
+        s2 += v.z;
+        s3 += v.w;
+      } else {
+        const double2 v0 = reinterpret_cast<const double2 *>(cs)[0], v1 = reinterpret_cast<const double2 *>(cs)[1];
+        s0 += v0.x;
+        s1 += v0.y;
+        s2 += v1.x;
+        s3 += v1.y;
+      }
     }
+    const T sv[4] = {s0, s1, s2, s3};
+    double *g = gb + (size_t(k) * S + i) * S + j0;
+#pragma unroll
+    for (int t = 0; t < 4; ++t)
+      if (j0 + t < S) g[t] = accumulate ? g[t] + double(sv[t]) : double(sv[t]);
   }
 }
 

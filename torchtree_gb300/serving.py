@@ -213,7 +213,9 @@ class GraphExecutor:
             self.stream.synchronize()
             if use_graph:
                 self.graph = torch.cuda.CUDAGraph()
-                with torch.cuda.graph(self.graph, stream=self.stream):
+                # thread-local capture: CUDA calls that client threads make meanwhile
+                # (pinned copies of their own, allocations) cannot invalidate it
+                with torch.cuda.graph(self.graph, stream=self.stream, capture_error_mode="thread_local"):
                     outs = self._step()
         self.outputs = outs
         self.host_out = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in outs.items()}
@@ -225,7 +227,7 @@ class GraphExecutor:
 
     def _step(self) -> dict:
         e, x = self.engine, self.inputs
-        lam, u, w = substitution.device_eigen(x["q"], x["pi"])  # FP64 Jacobi kernel, no host round trip
+        lam, u, w = substitution.device_eigen(x["q"], x["pi"])  # device eigensolver, no host round trip
         e.set_eigen(lam, u, w, x["bls"], x["rates"])
         lnl = e.log_likelihood(x["props"], x["pi"], rescale=True, keep_partials=True)
         _, dpi, dc = e.gradient(x["props"], x["pi"])

@@ -32,7 +32,8 @@ def eigen_system(q_unnorm: torch.Tensor, pi: torch.Tensor):
 
 def device_eigen(q: torch.Tensor, pi: torch.Tensor):
     """``(lambda, U, W)`` of normalised reversible ``q [b,S,S]`` (CUDA, FP64)
-    by the engine's Jacobi kernel; no autograd graph."""
+    by the engine's eigensolver (``tt_reversible_eigen``: FP32 Jacobi, FP64
+    refinement of the eigenvectors); no autograd graph."""
     from . import _native
 
     lib = _native.load()
