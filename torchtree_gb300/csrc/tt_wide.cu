@@ -137,7 +137,8 @@ PFN_cuTensorMapEncodeTiled_v12000 tensor_map_encoder() {
 
 // A row-major FP32 array [rows][cols] (cols a multiple of 4) as a 2-D tensor
 // map with bx x by boxes, no swizzle.
-bool encode_rows(CUtensorMap *m, const float *base, uint64_t rows, uint64_t cols, uint32_t bx, uint32_t by) {
+bool encode_rows(CUtensorMap *m, const float *base, uint64_t rows, uint64_t cols, uint32_t bx, uint32_t by,
+                 CUtensorMapSwizzle swizzle = CU_TENSOR_MAP_SWIZZLE_NONE) {
   const PFN_cuTensorMapEncodeTiled_v12000 fn = tensor_map_encoder();
   if (!fn) return false;
   const cuuint64_t dims[2] = {cols, rows};
@@ -145,7 +146,7 @@ bool encode_rows(CUtensorMap *m, const float *base, uint64_t rows, uint64_t cols
   const cuuint32_t box[2] = {bx, by};
   const cuuint32_t elem[2] = {1, 1};
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides, box, elem,
-            CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+            CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
 }
 
@@ -335,8 +336,8 @@ struct Wide {
     // the raw rows as 2-D tensors: partials [b I K 64][Npad], products [b I K 128][Npad]
     TcbMaps maps;
     const uint64_t blocks = uint64_t(p->batch) * p->I * p->K;
-    if (!encode_rows(&maps.part16, a.part, blocks * 64, uint64_t(g.Npad), 16, 64) ||
-        !encode_rows(&maps.prod16, a.prod, blocks * 128, uint64_t(g.Npad), 16, 128) ||
+    if (!encode_rows(&maps.part16, a.part, blocks * 64, uint64_t(g.Npad), 16, 64, CU_TENSOR_MAP_SWIZZLE_64B) ||
+        !encode_rows(&maps.prod16, a.prod, blocks * 128, uint64_t(g.Npad), 16, 128, CU_TENSOR_MAP_SWIZZLE_64B) ||
         !encode_rows(&maps.part128, a.part, blocks * 64, uint64_t(g.Npad), 128, 16) ||
         !encode_rows(&maps.prod128, a.prod, blocks * 128, uint64_t(g.Npad), 128, 16))
       return cudaErrorInvalidValue;

@@ -25,21 +25,29 @@
 // patterns (K = 16, both sides), then for each internal child four GEMM2
 // units of 16 states (K = 16) and that side's epilogue.  The CTA (one per SM)
 // is warp specialised: a copy warp issues each unit's raw rows (tiles of the
-// pattern-contiguous partial and product rows) as 2-D bulk tensor copies
-// into a ring of four raw slots; sixteen converter warps turn a unit's raw
-// rows into its MMA operands (products, TF32 split, K-major stores) in a ring
-// of three operand slots and run the epilogues; an MMA warp issues the
-// tensor-core work of each converted unit.  Full / empty mbarriers per slot
+// pattern-contiguous partial and product rows; GEMM3 rows with the 64-byte
+// swizzle, so that a warp reading one 16-byte column of 32 rows meets no
+// bank conflict) as 2-D bulk tensor copies into a ring of four raw slots;
+// sixteen converter warps turn a unit's raw rows into its MMA operands
+// (products, TF32 split) and run the epilogues; an MMA warp issues the
+// tensor-core work of each converted unit.  A operands (u for GEMM3, u^T for
+// GEMM2: M = 128 rows = TMEM lanes, K = columns) go to tensor memory by
+// tcgen05.st, in a ring of three 32-column slots; GEMM3's B operand goes to
+// shared memory (K-major stores) in a ring of three operand slots.  Shared
+// memory bandwidth bounds this kernel (TMA writes, the converters' reads and
+// writes and the MMAs' operand reads all share it); A in tensor memory takes
+// the A writes and reads off it.  Full / empty mbarriers per slot
 // order the roles; the converters meet at a named barrier only at epilogues
 // and tile ends.  GEMM2's B operand, P_c transposed into the operand layout
 // and split, is written once per (sample, branch, category) by
 // wide_pimage_kernel; a GEMM2 unit's 16-state slice of it travels in the
 // unit's raw slot (two 4 KB bulk copies) and the MMAs read it there.
 //
-// Accumulator layouts in tensor memory (cta_group::1): for M = 128 row m is
-// lane m; for M = 64 rows 16q .. 16q + 15 are lanes 32q .. 32q + 15
-// (q = 0..3); column n is column n in both.  A warp reads the 32 lanes of
-// its quarter (warp id mod 4).
+// Tensor memory (cta_group::1, M = 128): row m is lane m, column n is column
+// n, for the accumulators (G in columns [0, 128), o in [128, 192)) and for
+// the A operands (slot sl in [256 + 32 sl, 256 + 32 sl + 32): TF32 big in
+// the first 16 columns, small in the next 16).  A warp reads and writes the
+// 32 lanes of its quarter (warp id mod 4).
 #pragma once
 
 #include <cuda.h>
@@ -57,7 +65,7 @@ constexpr int kKC3 = 16;                  // patterns (K) per GEMM3 unit
 constexpr int kKC2 = 16;                  // states (K) per GEMM2 unit
 constexpr int kU3 = kPT / kKC3;           // GEMM3 units per tile (both sides)
 constexpr int kU2 = 64 / kKC2;            // GEMM2 units per internal side and tile
-constexpr int kOpSlot = 32768;            // one unit's operands (A big, A small, B big, B small)
+constexpr int kOpSlot = 16384;            // one GEMM3 unit's B operand (big, small)
 constexpr int kNS = 3;                    // operand slots
 constexpr int kRawSlot = 24576;           // one unit's raw rows (GEMM2: with its image slice)
 constexpr int kNR = 4;                    // raw slots
@@ -73,7 +81,8 @@ constexpr int kOffBar = kOffTab + kTabRows * 64 * 4;
 // mbarriers: raw full / empty [kNR], operand full / empty [kNS], accumulator full / empty, done
 constexpr int kBars = 2 * kNR + 2 * kNS + 3;
 constexpr int kSmem = kOffBar + 8 * kBars + 16;
-constexpr uint32_t kTmemCols = 256;       // G (block-diagonal) [0, 128), o [128, 192)
+constexpr uint32_t kTmemCols = 512;       // G (block-diagonal) [0, 128), o [128, 192), A slots [256, 352)
+constexpr uint32_t kTmA = 256;            // first A-slot column
 constexpr int kImgFloats = 2 * 64 * 64;   // one P^T image: big then small
 
 }  // namespace tcb
@@ -102,6 +111,37 @@ __global__ void __launch_bounds__(256) wide_pimage_kernel(const float *pmat, flo
 
 __device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 
+// four consecutive 32-bit TMEM columns of this thread's lane (the warp's lane quarter)
+__device__ __forceinline__ void tmem_st4(uint32_t taddr, float4 v) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(taddr),
+               "r"(__float_as_uint(v.x)), "r"(__float_as_uint(v.y)), "r"(__float_as_uint(v.z)),
+               "r"(__float_as_uint(v.w))
+               : "memory");
+}
+__device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
+
+// v split into TF32 big and small, stored to TMEM columns c and c + 16
+__device__ __forceinline__ void split4_tmem(uint32_t taddr, float4 v) {
+  float4 hb, hs;
+  tc::split_tf32(v.x, hb.x, hs.x);
+  tc::split_tf32(v.y, hb.y, hs.y);
+  tc::split_tf32(v.z, hb.z, hs.z);
+  tc::split_tf32(v.w, hb.w, hs.w);
+  tmem_st4(taddr, hb);
+  tmem_st4(taddr + 16u, hs);
+}
+
+// D (TMEM) (+)= A (TMEM, M = 128 lanes x K = 8 columns) x B (shared-memory descriptor)
+__device__ __forceinline__ void mma_tf32_ta(uint32_t dtmem, uint32_t atmem, uint64_t bdesc, uint32_t idesc,
+                                            uint32_t accumulate) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(dtmem),
+      "r"(atmem), "l"(bdesc), "r"(idesc), "r"(accumulate)
+      : "memory");
+}
+
 __device__ __forceinline__ void split4_store(unsigned char *big, unsigned char *small, float4 v) {
   float4 hb, hs;
   tc::split_tf32(v.x, hb.x, hs.x);
@@ -129,7 +169,8 @@ __device__ __forceinline__ void cp_async_wait() {
 
 // 2-D bulk tensor copy of the box at (x, y) of `map` into shared memory,
 // completion counted on `bar`.  x (the pattern coordinate) is a multiple of
-// 32 floats, so the copy starts on a 128-byte boundary.
+// 16 floats (64 bytes); dst is 1024-byte aligned (a multiple of the 64-byte
+// swizzle's 512-byte period).
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
@@ -156,8 +197,10 @@ __device__ __forceinline__ TcbMeta tcb_meta(unsigned char *base) {
 
 // Tensor maps of the adjoint's raw rows: the partials [b][I][K][64][Npad]
 // and the children's products [b][I][K][2][64][Npad] as 2-D arrays of rows,
-// with 16-pattern boxes of 64 partial rows / 128 product rows (GEMM3 units)
-// and 128-pattern x 16-row boxes (GEMM2 units).
+// with 16-pattern boxes of 64 partial rows / 128 product rows (GEMM3 units,
+// 64-byte swizzle: the 16-byte chunk c of box row r lands at chunk
+// c ^ ((r >> 1) & 3), address bits 4-5 XOR bits 7-8) and 128-pattern x 16-row
+// boxes (GEMM2 units, no swizzle).
 struct TcbMaps {
   CUtensorMap part16, prod16, part128, prod128;
 };
@@ -185,7 +228,7 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
                             int code_count, int *status, unsigned long long timeout_ns) {
   using namespace tcb;
   constexpr int SP = 64, PT = kPT;
-  extern __shared__ __align__(128) unsigned char smem[];
+  extern __shared__ __align__(1024) unsigned char smem[];
   float *red = reinterpret_cast<float *>(smem + kOffRed);
   float *rsum = reinterpret_cast<float *>(smem + kOffRoot);
   uint64_t *raw_full = reinterpret_cast<uint64_t *>(smem + kOffBar);  // [kNR] count 1 + bytes
@@ -197,6 +240,11 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
   uint64_t *done = acc_empty + 1;                                      // MMA commit: every MMA done
   uint32_t *tslot = reinterpret_cast<uint32_t *>(done + 1);
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  // the swizzled raw rows assume a 1024-byte-aligned shared-memory window
+  if (smem_u32(smem) & 1023u) {
+    if (tid == 0) atomicExch(status, TT_ERR_CUDA);
+    return;
+  }
   const int v = a.nodes[blockIdx.y];
   const int b = blockIdx.z / a.K, k = blockIdx.z - (blockIdx.z / a.K) * a.K;
   const int chunk = blockIdx.x;
@@ -305,8 +353,8 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
     // loop, lane 0 issues)
     const bool leader = lane == 0;
     // operand descriptors: slot / raw-slot bases, advanced by (byte offset >> 4) per K step
-    const uint64_t dA = tc::smem_desc(smem_u32(smem), 2048, 128);
-    const uint64_t dB = tc::smem_desc(smem_u32(smem + kOffRaw), 1024, 128);
+    const uint64_t dOp = tc::smem_desc(smem_u32(smem), 2048, 128);         // GEMM3 B (operand slots)
+    const uint64_t dB = tc::smem_desc(smem_u32(smem + kOffRaw), 1024, 128);  // GEMM2 B (image in the raw slot)
     uint32_t ph_of = 0, ph_ae = 1u;
     bool ok = true, started = false;
     int rr = 0;
@@ -323,15 +371,17 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
       }
       tc::fence_after_sync();
       const uint64_t so = uint64_t(sl * kOpSlot) >> 4, ro = uint64_t(rs * kRawSlot) >> 4;
+      const uint32_t ta = tmem + kTmA + 32u * uint32_t(sl);  // the unit's A: big [ta, ta + 16), small + 16
       if (leader) {
         if (!un.g2) {
           constexpr uint32_t idesc = tc::idesc_tf32(128, 128);
 #pragma unroll
           for (int kk = 0; kk < kKC3 / 8; ++kk) {
             const uint64_t o = so + uint64_t(kk * 4096 >> 4);
-            tc::mma_tf32(tmem, dA + o, dA + o + (16384 >> 4), idesc, (started || kk > 0) ? 1u : 0u);
-            tc::mma_tf32(tmem, dA + o, dA + o + (24576 >> 4), idesc, 1u);
-            tc::mma_tf32(tmem, dA + o + (8192 >> 4), dA + o + (16384 >> 4), idesc, 1u);
+            const uint32_t at = ta + 8u * kk;
+            mma_tf32_ta(tmem, at, dOp + o, idesc, (started || kk > 0) ? 1u : 0u);
+            mma_tf32_ta(tmem, at, dOp + o + (8192 >> 4), idesc, 1u);
+            mma_tf32_ta(tmem, at + 16u, dOp + o, idesc, 1u);
           }
           tc::mma_commit(&op_empty[sl]);
           mbar_arrive(&raw_empty[rs]);  // the MMAs do not read the raw slot
@@ -339,10 +389,11 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
           constexpr uint32_t idesc = tc::idesc_tf32(128, 64);
 #pragma unroll
           for (int kk = 0; kk < kKC2 / 8; ++kk) {
-            const uint64_t oa = so + uint64_t(kk * 4096 >> 4), ob = ro + uint64_t(16384 + kk * 2048 >> 4);
-            tc::mma_tf32(tmem + 128u, dA + oa, dB + ob, idesc, (un.idx > 0 || kk > 0) ? 1u : 0u);
-            tc::mma_tf32(tmem + 128u, dA + oa, dB + ob + (4096 >> 4), idesc, 1u);
-            tc::mma_tf32(tmem + 128u, dA + oa + (8192 >> 4), dB + ob, idesc, 1u);
+            const uint64_t ob = ro + uint64_t(16384 + kk * 2048 >> 4);
+            const uint32_t at = ta + 8u * kk;
+            mma_tf32_ta(tmem + 128u, at, dB + ob, idesc, (un.idx > 0 || kk > 0) ? 1u : 0u);
+            mma_tf32_ta(tmem + 128u, at, dB + ob + (4096 >> 4), idesc, 1u);
+            mma_tf32_ta(tmem + 128u, at + 16u, dB + ob, idesc, 1u);
           }
           tc::mma_commit(&op_empty[sl]);
           tc::mma_commit(&raw_empty[rs]);  // the raw slot held B
@@ -395,13 +446,17 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
     if (tab_smem)
       for (int e = tid; e < code_count * 16; e += kConv)
         reinterpret_cast<float4 *>(tab)[e] = ldg4(a.table + 4 * e);
-    // GEMM3 item of this thread: row R = (side, i) of the block-diagonal product, 4-pattern group q
-    // on a diagonal (a quarter warp reads 8 different 16-byte columns of the raw rows and writes
-    // 8 different rows of a core matrix)
-    const int j3 = tid & 7, R3 = 8 * ((tid >> 3) & 15) + j3, q3 = ((j3 >> 1) + (tid >> 7)) & 3;
+    // GEMM3 item of this thread: row R3 = (side s3, state i3) = its TMEM lane (32 (warp & 3) + lane),
+    // patterns 4 q3 .. 4 q3 + 3 of the unit (q3 = warp >> 2).  It writes u[R3][..] (A) to tensor
+    // memory and (c x)[R3][..] (B) to eight rows of one core matrix per quarter warp; the raw rows'
+    // 64-byte swizzle puts chunk q3 of the 32 rows a warp reads in distinct banks.
+    const int R3 = 32 * (warp & 3) + lane, q3 = warp >> 2;
     const int s3 = R3 >> 6, i3 = R3 & 63;
+    const int sw3 = 16 * (q3 ^ ((i3 >> 1) & 3));  // swizzled byte offset of chunk q3 in rows i3, 64 + i3
     const bool x3in = s3 ? int1 : int0;
     const float pre3 = is_root && i3 < a.S ? float(wk * a.freqs[size_t(b) * a.S + i3]) : 0.0f;
+    // this warp's lane quarter of tensor memory
+    const uint32_t tq = tmem + (uint32_t(32 * (warp & 3)) << 16);
     uint32_t ph_rf = 0, ph_oe = 0x7u, ph_af = 0;
     bool ok = true;        // uniform across the converters after every conv_sync_any
     float root_acc = 0.0f; // root: this thread's share of sum_p c_p al[i][p] ar[i][p], i = tid & 63
@@ -434,32 +489,34 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
       const int rs = u % kNR, sl = u % kNS;
       if (ok) ok = mbar_wait_bounded(&raw_full[rs], ph_rf >> rs & 1u, timeout_ns);   // the unit's rows landed
       if (ok) ok = mbar_wait_bounded(&op_empty[sl], ph_oe >> sl & 1u, timeout_ns);  // the slot is free
+      ok = __all_sync(0xffffffffu, ok);  // the tcgen05.st below are warp-collective
       ph_rf ^= 1u << rs;
       ph_oe ^= 1u << sl;
       if (ok) {
+        tc::fence_after_sync();  // the MMAs that read this slot's A have completed
         unsigned char *op = smem + sl * kOpSlot;
         const unsigned char *raw = smem + kOffRaw + rs * kRawSlot;
+        const uint32_t ta = tq + kTmA + 32u * uint32_t(sl);
         if (!un.g2) {
           const int pt = un.idx * kKC3 + 4 * q3;  // pattern offset in the tile
           // u_s = pre * (the other side's product): product rows (1 - s) * 64 + i
-          const float4 o4 = *reinterpret_cast<const float4 *>(raw + ((1 - s3) * 64 + i3) * 64 + q3 * 16);
+          const float4 o4 = *reinterpret_cast<const float4 *>(raw + ((1 - s3) * 64 + i3) * 64 + sw3);
           const float4 p4 = is_root ? make_float4(pre3, pre3, pre3, pre3)
-                                    : *reinterpret_cast<const float4 *>(raw + 8192 + i3 * 64 + q3 * 16);
+                                    : *reinterpret_cast<const float4 *>(raw + 8192 + i3 * 64 + sw3);
           float4 x4;
           if (x3in) {
-            x4 = *reinterpret_cast<const float4 *>(raw + 12288 + s3 * 4096 + i3 * 64 + q3 * 16);
+            x4 = *reinterpret_cast<const float4 *>(raw + 12288 + s3 * 4096 + i3 * 64 + sw3);
           } else {
             const unsigned char *cc = meta.codes + s3 * PT + pt;
             x4 = make_float4(tabsrc[int(cc[0]) * SP + i3], tabsrc[int(cc[1]) * SP + i3],
                              tabsrc[int(cc[2]) * SP + i3], tabsrc[int(cc[3]) * SP + i3]);
           }
           const float4 c4 = *reinterpret_cast<const float4 *>(meta.cf + pt);
+          split4_tmem(ta + 4u * q3, make_float4(p4.x * o4.x, p4.y * o4.y, p4.z * o4.z, p4.w * o4.w));
           const uint32_t off = tc::kmajor_off(R3, 4 * q3, 2048);
-          split4_store(op + off, op + 8192 + off, make_float4(p4.x * o4.x, p4.y * o4.y, p4.z * o4.z, p4.w * o4.w));
-          split4_store(op + 16384 + off, op + 24576 + off,
-                       make_float4(x4.x * c4.x, x4.y * c4.y, x4.z * c4.z, x4.w * c4.w));
+          split4_store(op + off, op + 8192 + off, make_float4(x4.x * c4.x, x4.y * c4.y, x4.z * c4.z, x4.w * c4.w));
         } else {
-          // item (pattern p, states 16 idx + 4 sq ..): A = u^T, row p, K = 4 states
+          // item (pattern p = this thread's TMEM lane, states 16 idx + 4 sq ..): A = u^T, row p, K = 4 states
           const int pp = tid & (PT - 1), sq = tid >> 7;
           float uu[4];
 #pragma unroll
@@ -470,10 +527,11 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
                                      : *reinterpret_cast<const float *>(raw + 8192 + row * 512 + pp * 4);
             uu[e] = pv * ot;
           }
-          const uint32_t off = tc::kmajor_off(pp, 4 * sq, 2048);
-          split4_store(op + off, op + 8192 + off, make_float4(uu[0], uu[1], uu[2], uu[3]));
+          split4_tmem(ta + 4u * sq, make_float4(uu[0], uu[1], uu[2], uu[3]));
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // generic writes -> tensor cores
+        tmem_st_wait();
+        if (!un.g2) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // B: generic writes -> tensor cores
+        tc::fence_before_sync();
         __syncwarp();
         if (lane == 0) {
           mbar_arrive(&op_full[sl]);
