@@ -209,7 +209,8 @@ __global__ void __launch_bounds__(256) wide_qgrad_kernel(const double *G, const 
 #pragma unroll
             for (int x = 0; x < 4; ++x) {
               const int m = bm + IB * x;
-              if (m < S) dsum += double(ls[m]) * exp(double(ls[m]) * double(tau)) * double(M[x][x]);
+              // in the plan's type (an FP64 exp costs thousands of cycles of this GPU's FP64 pipe)
+              if (m < S) dsum += double(ls[m] * exp_t(ls[m] * tau) * M[x][x]);
             }
         }
       }

@@ -200,7 +200,7 @@ struct Wide {
                                int(cudaSharedmemCarveoutMaxShared));
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(wide_pmatrix_kernel<T, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                               int(2 * SP * SP * sizeof(T) + SP * sizeof(double)));
+                               int(3 * SP * SP * sizeof(T) + SP * sizeof(T)));
     if (e == cudaSuccess)
       e = cudaFuncSetAttribute(wide_pmatrix_backward_kernel<double, SP>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                int(Wide<double, SP, PTF, PTB>::pback_smem()));
@@ -360,7 +360,7 @@ struct Wide {
 
   static cudaError_t pmatrix(tt_plan *p, const double *lam, const double *U, const double *W, const double *bl,
                              const double *rates, cudaStream_t s) {
-    wide_pmatrix_kernel<T, SP><<<dim3(p->B, p->batch), 256, 2 * SP * SP * sizeof(T) + SP * sizeof(double), s>>>(
+    wide_pmatrix_kernel<T, SP><<<dim3(p->B, p->batch), 256, 3 * SP * SP * sizeof(T) + SP * sizeof(T), s>>>(
         lam, U, W, bl, rates, static_cast<T *>(p->d_pmat), p->S, p->B, p->K);
     p->launches += 1;
     return cudaGetLastError();

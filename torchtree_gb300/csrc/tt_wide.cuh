@@ -420,9 +420,17 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT, wide_bwd_min_blocks<T,
       el[tid] = El;
       er[tid] = Er;
       ep[tid] = Ep;
-      double c = 0.0;
-      if (n < a.N) c = a.weights[n] * exp2(double(Ep + El + Er) - a.log2L[size_t(b) * a.Npad + n]);
-      cf[tid] = T(c);
+      T c = T(0);
+      if (n < a.N) {
+        const double dd = double(Ep + El + Er) - a.log2L[size_t(b) * a.Npad + n];
+        if constexpr (sizeof(T) == 8) {
+          c = a.weights[n] * exp2(dd);
+        } else {  // the fraction's power in FP32 (an FP64 exp2 costs thousands of FP64-pipe cycles per warp)
+          const double fl = floor(dd);
+          c = ldexpf(float(a.weights[n]) * exp2f(float(dd - fl)), int(fl));
+        }
+      }
+      cf[tid] = c;
     }
     // this thread's block of the outside partial of v
     T pre[4][4];
@@ -681,7 +689,9 @@ __global__ void wide_root_reduce_kernel(const T *rootpart, double *dfreq, double
 // ------------------------------------------------------ transition matrices
 // P[b][br][k] = I + U diag(expm1(lambda t r_k)) W over the padded SP x SP
 // block (zero outside S x S), products in T, exponentials in FP64.  One CTA
-// per (branch, sample), all categories; 4 x 4 register tiles.
+// per (branch, sample), all categories; 4 x 4 register tiles.  U and W are
+// converted to T once per CTA, and U diag(d) is formed in T: FP64 arithmetic
+// (and conversions from FP64) run at a small fraction of the FP32 rate here.
 template <typename T, int SP>
 __global__ void __launch_bounds__(256) wide_pmatrix_kernel(const double *lam, const double *U, const double *W,
                                                            const double *bl, const double *rates, T *pmat, int S,
@@ -690,22 +700,22 @@ __global__ void __launch_bounds__(256) wide_pmatrix_kernel(const double *lam, co
   extern __shared__ __align__(128) unsigned char smem[];
   T *ut = reinterpret_cast<T *>(smem);  // [m][perm i] = U[i][m] * d_m
   T *wm = ut + SP * SP;                 // [m][perm j] = W[m][j]
-  double *d = reinterpret_cast<double *>(wm + SP * SP);
+  T *u0 = wm + SP * SP;                 // [m][perm i] = U[i][m]
+  T *dt = u0 + SP * SP;                 // [SP] d_m in T
   const int br = blockIdx.x, b = blockIdx.y, tid = threadIdx.x;
   const double t = bl[size_t(b) * B + br];
   for (int e = tid; e < SP * SP; e += 256) {
     const int m = e / SP, j = e - m * SP;
     wm[m * SP + wperm<IB>(j)] = (m < S && j < S) ? T(W[(size_t(b) * S + m) * S + j]) : T(0);
+    const int i = m, mm = j;  // u0[mm][perm i] = U[i][mm]
+    u0[mm * SP + wperm<IB>(i)] = (mm < S && i < S) ? T(U[(size_t(b) * S + i) * S + mm]) : T(0);
   }
   for (int k = 0; k < K; ++k) {
     const double tr = t * rates[size_t(b) * K + k];
     __syncthreads();
-    for (int m = tid; m < SP; m += 256) d[m] = m < S ? expm1(lam[size_t(b) * S + m] * tr) : 0.0;
+    for (int m = tid; m < SP; m += 256) dt[m] = m < S ? T(expm1(lam[size_t(b) * S + m] * tr)) : T(0);
     __syncthreads();
-    for (int e = tid; e < SP * SP; e += 256) {
-      const int i = e / SP, m = e - i * SP;
-      ut[m * SP + wperm<IB>(i)] = (m < S && i < S) ? T(U[(size_t(b) * S + i) * S + m] * d[m]) : T(0);
-    }
+    for (int e = tid; e < SP * SP; e += 256) ut[e] = u0[e] * dt[e / SP];
     __syncthreads();
     T *dst = pmat + ((size_t(b) * B + br) * K + k) * SP * SP;
     for (int blk = tid; blk < IB * IB; blk += 256) {

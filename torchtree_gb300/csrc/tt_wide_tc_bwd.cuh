@@ -436,7 +436,10 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
         m.ep[tid] = Ep;
         m.el[tid] = El;
         m.er[tid] = Er;
-        m.cf[tid] = n < a.N ? float(mw[tid] * exp2(double(Ep + El + Er) - ml2[tid])) : 0.0f;
+        // w 2^(E - log2 L): the exponent difference in FP64, its fraction's power in FP32 (an FP64
+        // exp2 costs thousands of cycles of this GPU's FP64 pipe per warp)
+        const double dd = double(Ep + El + Er) - ml2[tid], fl = floor(dd);
+        m.cf[tid] = n < a.N ? ldexpf(float(mw[tid]) * exp2f(float(dd - fl)), int(fl)) : 0.0f;
       }
     };
     // a tip child's rows of the code table, in shared memory when the table is small
