@@ -51,7 +51,8 @@ struct tt_plan {
   double *d_G = nullptr;
   double *d_rootgrad = nullptr;
   int *d_status = nullptr;
-  double *d_qpart = nullptr;  // rate-matrix gradient partials (first use)
+  double *d_qpart = nullptr;  // rate-matrix gradient partials and the finishing step's Z (first use)
+  int qpart_chunks = 0;       // chunk slots of d_qpart
   size_t bytes = 0;
   size_t grad_bytes = 0;  // of `bytes`: the stored partials and per-tile gradient blocks
   tt::WideState *wide = nullptr;  // non-NULL for S != 4 plans

@@ -246,34 +246,50 @@ __global__ void __launch_bounds__(256) wide_qgrad_kernel(const double *G, const 
     for (int k = 0; k < K; ++k) dst[S * S + k] = drs[k];
 }
 
-// per sample: X = sum of chunk partials, dQ = W^T X U^T (FP64), rate sums
-__global__ void qgrad_finish_kernel(const double *part, int nchunks, const double *U, const double *W, int S, int K,
-                                    double *dQ, double *drates) {
-  extern __shared__ __align__(16) double fin[];  // X [S][S], Z [S][S]
-  double *X = fin, *Z = fin + S * S;
-  const int b = blockIdx.x, tid = threadIdx.x, width = S * S + K;
-  for (int e = tid; e < width; e += blockDim.x) {
+// per sample, kQRows rows per CTA (grid: row blocks x samples), FP64:
+// X rows = sums of the chunk partials, then Z rows = X rows U^T; the first
+// row block also sums the rate terms.  Spreading the rows over CTAs keeps the
+// FP64 work off a single SM per sample.
+constexpr int kQRows = 4;
+
+__global__ void __launch_bounds__(256) qgrad_sum_rows_kernel(const double *part, int nchunks, const double *U, int S,
+                                                             int K, double *Z, double *drates) {
+  __shared__ double X[kQRows][64];
+  const int b = blockIdx.y, r0 = blockIdx.x * kQRows, tid = threadIdx.x, width = S * S + K;
+  const int rows = min(kQRows, S - r0);
+  for (int e = tid; e < rows * S; e += blockDim.x) {
+    const int r = e / S, c = e - r * S;
     double s = 0.0;
-    for (int c = 0; c < nchunks; ++c) s += part[(size_t(b) * nchunks + c) * width + e];
-    if (e < S * S) X[e] = s;
-    else if (drates) drates[size_t(b) * K + e - S * S] = s;
+    for (int ch = 0; ch < nchunks; ++ch) s += part[(size_t(b) * nchunks + ch) * width + (r0 + r) * S + c];
+    X[r][c] = s;
   }
-  __syncthreads();
-  const double *u = U + size_t(b) * S * S, *w = W + size_t(b) * S * S;
-  for (int e = tid; e < S * S; e += blockDim.x) {  // Z[m][j] = sum_n X[m][n] U[j][n]
-    const int m = e / S, j = e - m * S;
-    double acc = 0.0;
-    for (int n = 0; n < S; ++n) acc = fma(X[m * S + n], u[j * S + n], acc);
-    Z[e] = acc;
-  }
-  __syncthreads();
-  if (dQ)
-    for (int e = tid; e < S * S; e += blockDim.x) {  // dQ[i][j] = sum_m W[m][i] Z[m][j]
-      const int i = e / S, j = e - i * S;
-      double acc = 0.0;
-      for (int m = 0; m < S; ++m) acc = fma(w[m * S + i], Z[m * S + j], acc);
-      dQ[size_t(b) * S * S + e] = acc;
+  if (blockIdx.x == 0 && drates)
+    for (int k = tid; k < K; k += blockDim.x) {
+      double s = 0.0;
+      for (int ch = 0; ch < nchunks; ++ch) s += part[(size_t(b) * nchunks + ch) * width + S * S + k];
+      drates[size_t(b) * K + k] = s;
     }
+  __syncthreads();
+  const double *u = U + size_t(b) * S * S;
+  for (int e = tid; e < rows * S; e += blockDim.x) {  // Z[m][j] = sum_n X[m][n] U[j][n]
+    const int r = e / S, j = e - r * S;
+    double acc = 0.0;
+    for (int n = 0; n < S; ++n) acc = fma(X[r][n], u[j * S + n], acc);
+    Z[(size_t(b) * S + r0 + r) * S + j] = acc;
+  }
+}
+
+// dQ rows i = sum_m W[m][i] Z[m][j], kQRows rows per CTA, FP64.
+__global__ void __launch_bounds__(256) qgrad_dq_rows_kernel(const double *Z, const double *W, int S, double *dQ) {
+  const int b = blockIdx.y, r0 = blockIdx.x * kQRows, tid = threadIdx.x;
+  const int rows = min(kQRows, S - r0);
+  const double *w = W + size_t(b) * S * S, *z = Z + size_t(b) * S * S;
+  for (int e = tid; e < rows * S; e += blockDim.x) {
+    const int i = r0 + e / S, j = e - (e / S) * S;
+    double acc = 0.0;
+    for (int m = 0; m < S; ++m) acc = fma(w[m * S + i], z[m * S + j], acc);
+    dQ[size_t(b) * S * S + size_t(i) * S + j] = acc;
+  }
 }
 
 namespace {
@@ -301,12 +317,15 @@ int rate_matrix_gradient(tt_plan *p, const double *lam, const double *U, const d
   if (!p->d_qpart) {  // chunk partials, allocated on first use
     const int bchunk = 8;
     const size_t chunks = S == 4 ? size_t((p->B + 127) / 128) : size_t((p->B + bchunk - 1) / bchunk);
-    e = cudaMalloc(reinterpret_cast<void **>(&p->d_qpart), size_t(p->batch) * chunks * width * sizeof(double));
+    // the chunk partials, then Z [b][S][S] of the finishing step
+    e = cudaMalloc(reinterpret_cast<void **>(&p->d_qpart),
+                   (size_t(p->batch) * chunks * width + size_t(p->batch) * S * S) * sizeof(double));
     if (e != cudaSuccess) {
       cudaGetLastError();
       return record_error(TT_ERR_OUT_OF_MEMORY, "cudaMalloc of the rate-matrix gradient chunks failed");
     }
-    p->bytes += size_t(p->batch) * chunks * width * sizeof(double);
+    p->bytes += (size_t(p->batch) * chunks * width + size_t(p->batch) * S * S) * sizeof(double);
+    p->qpart_chunks = int(chunks);
   }
   if (S == 4) {
     nchunks = (p->B + 127) / 128;
@@ -324,14 +343,14 @@ int rate_matrix_gradient(tt_plan *p, const double *lam, const double *U, const d
       e = f32 ? launch_wide_qgrad<float, 64>(p, lam, U, W, bl, rates, dbl, p->d_qpart, bchunk, nchunks, s)
               : launch_wide_qgrad<double, 64>(p, lam, U, W, bl, rates, dbl, p->d_qpart, bchunk, nchunks, s);
   }
-  if (e == cudaSuccess)
-    e = kernel_smem(qgrad_finish_kernel, 2 * S * S * sizeof(double));
   if (e == cudaSuccess) {
-    qgrad_finish_kernel<<<p->batch, 256, 2 * S * S * sizeof(double), s>>>(p->d_qpart, nchunks, U, W, S, K, dQ,
-                                                                         drates);
+    double *Z = p->d_qpart + size_t(p->batch) * p->qpart_chunks * width;
+    const dim3 grid((S + kQRows - 1) / kQRows, p->batch);
+    qgrad_sum_rows_kernel<<<grid, 256, 0, s>>>(p->d_qpart, nchunks, U, S, K, Z, drates);
+    if (dQ) qgrad_dq_rows_kernel<<<grid, 256, 0, s>>>(Z, W, S, dQ);
     e = cudaGetLastError();
   }
-  p->launches += 2;
+  p->launches += dQ ? 3 : 2;
   if (e != cudaSuccess)
     return record_error(e == cudaErrorMemoryAllocation ? TT_ERR_OUT_OF_MEMORY : TT_ERR_CUDA,
                         (std::string("rate-matrix gradient launch: ") + cudaGetErrorString(e)).c_str());
