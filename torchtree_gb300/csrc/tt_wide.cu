@@ -336,8 +336,8 @@ struct Wide {
     // the raw rows as 2-D tensors: partials [b I K 64][Npad], products [b I K 128][Npad]
     TcbMaps maps;
     const uint64_t blocks = uint64_t(p->batch) * p->I * p->K;
-    if (!encode_rows(&maps.part16, a.part, blocks * 64, uint64_t(g.Npad), 16, 64, CU_TENSOR_MAP_SWIZZLE_64B) ||
-        !encode_rows(&maps.prod16, a.prod, blocks * 128, uint64_t(g.Npad), 16, 128, CU_TENSOR_MAP_SWIZZLE_64B) ||
+    if (!encode_rows(&maps.part32, a.part, blocks * 64, uint64_t(g.Npad), 32, 64, CU_TENSOR_MAP_SWIZZLE_128B) ||
+        !encode_rows(&maps.prod32, a.prod, blocks * 128, uint64_t(g.Npad), 32, 128, CU_TENSOR_MAP_SWIZZLE_128B) ||
         !encode_rows(&maps.part128, a.part, blocks * 64, uint64_t(g.Npad), 128, 16) ||
         !encode_rows(&maps.prod128, a.prod, blocks * 128, uint64_t(g.Npad), 128, 16))
       return cudaErrorInvalidValue;

@@ -21,19 +21,20 @@
 // same K-major no-swizzle operand layout (8-row x 16-byte core matrices, SBO
 // = 128 B between 8-row groups, LBO between 4-element K groups).
 //
-// The work of a tile is a sequence of units: eight GEMM3 units of 16
-// patterns (K = 16, both sides), then for each internal child four GEMM2
+// The work of a tile is a sequence of units: four GEMM3 units of 32
+// patterns (K = 32, both sides), then for each internal child four GEMM2
 // units of 16 states (K = 16) and that side's epilogue.  The CTA (one per SM)
 // is warp specialised: a copy warp issues each unit's raw rows (tiles of the
-// pattern-contiguous partial and product rows; GEMM3 rows with the 64-byte
+// pattern-contiguous partial and product rows; GEMM3 rows with the 128-byte
 // swizzle, so that a warp reading one 16-byte column of 32 rows meets no
-// bank conflict) as 2-D bulk tensor copies into a ring of four raw slots;
+// more bank conflicts than its 512 bytes need) as 2-D bulk tensor copies into
+// a ring of three raw slots;
 // sixteen converter warps turn a unit's raw rows into its MMA operands
 // (products, TF32 split) and run the epilogues; an MMA warp issues the
 // tensor-core work of each converted unit.  A operands (u for GEMM3, u^T for
 // GEMM2: M = 128 rows = TMEM lanes, K = columns) go to tensor memory by
-// tcgen05.st, in a ring of three 32-column slots; GEMM3's B operand goes to
-// shared memory (K-major stores) in a ring of three operand slots.  Shared
+// tcgen05.st, in a ring of two 64-column slots; GEMM3's B operand goes to
+// shared memory (K-major stores) in a ring of two operand slots.  Shared
 // memory bandwidth bounds this kernel (TMA writes, the converters' reads and
 // writes and the MMAs' operand reads all share it); A in tensor memory takes
 // the A writes and reads off it.  Full / empty mbarriers per slot
@@ -45,8 +46,8 @@
 //
 // Tensor memory (cta_group::1, M = 128): row m is lane m, column n is column
 // n, for the accumulators (G in columns [0, 128), o in [128, 192)) and for
-// the A operands (slot sl in [256 + 32 sl, 256 + 32 sl + 32): TF32 big in
-// the first 16 columns, small in the next 16).  A warp reads and writes the
+// the A operands (slot sl in [256 + 64 sl, 256 + 64 sl + 64): TF32 big in
+// the first 32 columns, small in the next 32; a GEMM2 unit uses 16 of each).  A warp reads and writes the
 // 32 lanes of its quarter (warp id mod 4).
 #pragma once
 
@@ -61,14 +62,14 @@ namespace tcb {
 constexpr int kPT = 128;                  // patterns per tile (GEMM2 M)
 constexpr int kConv = 512;                // converter threads (16 warps)
 constexpr int kThreads = kConv + 64;      // + the copy warp and the MMA warp
-constexpr int kKC3 = 16;                  // patterns (K) per GEMM3 unit
+constexpr int kKC3 = 32;                  // patterns (K) per GEMM3 unit
 constexpr int kKC2 = 16;                  // states (K) per GEMM2 unit
 constexpr int kU3 = kPT / kKC3;           // GEMM3 units per tile (both sides)
 constexpr int kU2 = 64 / kKC2;            // GEMM2 units per internal side and tile
-constexpr int kOpSlot = 16384;            // one GEMM3 unit's B operand (big, small)
-constexpr int kNS = 3;                    // operand slots
-constexpr int kRawSlot = 24576;           // one unit's raw rows (GEMM2: with its image slice)
-constexpr int kNR = 4;                    // raw slots
+constexpr int kOpSlot = 32768;            // one GEMM3 unit's B operand (big, small)
+constexpr int kNS = 2;                    // operand slots (shared memory B, TMEM A)
+constexpr int kRawSlot = 40960;           // one unit's raw rows (GEMM3: 32 patterns of 320 rows; GEMM2: 24 KB with its image slice)
+constexpr int kNR = 3;                    // raw slots
 constexpr int kMeta = kPT * 16 + 2 * kPT; // a tile's coefficients, exponents and tip codes
 constexpr int kOffRaw = kNS * kOpSlot;
 constexpr int kOffMeta = kOffRaw + kNR * kRawSlot;
@@ -81,8 +82,9 @@ constexpr int kOffBar = kOffTab + kTabRows * 64 * 4;
 // mbarriers: raw full / empty [kNR], operand full / empty [kNS], accumulator full / empty, done
 constexpr int kBars = 2 * kNR + 2 * kNS + 3;
 constexpr int kSmem = kOffBar + 8 * kBars + 16;
-constexpr uint32_t kTmemCols = 512;       // G (block-diagonal) [0, 128), o [128, 192), A slots [256, 352)
+constexpr uint32_t kTmemCols = 512;       // G (block-diagonal) [0, 128), o [128, 192), A slots [256, 384)
 constexpr uint32_t kTmA = 256;            // first A-slot column
+constexpr uint32_t kASlot = 64;           // columns per A slot: big [0, 32), small [32, 64)
 constexpr int kImgFloats = 2 * 64 * 64;   // one P^T image: big then small
 
 }  // namespace tcb
@@ -120,7 +122,7 @@ __device__ __forceinline__ void tmem_st4(uint32_t taddr, float4 v) {
 }
 __device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
 
-// v split into TF32 big and small, stored to TMEM columns c and c + 16
+// v split into TF32 big and small, stored to TMEM columns c and c + 32
 __device__ __forceinline__ void split4_tmem(uint32_t taddr, float4 v) {
   float4 hb, hs;
   tc::split_tf32(v.x, hb.x, hs.x);
@@ -128,7 +130,26 @@ __device__ __forceinline__ void split4_tmem(uint32_t taddr, float4 v) {
   tc::split_tf32(v.z, hb.z, hs.z);
   tc::split_tf32(v.w, hb.w, hs.w);
   tmem_st4(taddr, hb);
-  tmem_st4(taddr + 16u, hs);
+  tmem_st4(taddr + 32u, hs);
+}
+
+// eight consecutive 32-bit TMEM columns of this thread's lane
+__device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
+  asm volatile("tcgen05.st.sync.aligned.32x32b.x8.b32 [%0], {%1, %2, %3, %4, %5, %6, %7, %8};" ::"r"(taddr),
+               "r"(__float_as_uint(v[0])), "r"(__float_as_uint(v[1])), "r"(__float_as_uint(v[2])),
+               "r"(__float_as_uint(v[3])), "r"(__float_as_uint(v[4])), "r"(__float_as_uint(v[5])),
+               "r"(__float_as_uint(v[6])), "r"(__float_as_uint(v[7]))
+               : "memory");
+}
+
+// a and b split into TF32 big and small: columns c .. c + 7 (big) and c + 32 .. c + 39 (small)
+__device__ __forceinline__ void split8_tmem(uint32_t taddr, float4 a, float4 b) {
+  float hb[8], hs[8];
+  const float v[8] = {a.x, a.y, a.z, a.w, b.x, b.y, b.z, b.w};
+#pragma unroll
+  for (int e = 0; e < 8; ++e) tc::split_tf32(v[e], hb[e], hs[e]);
+  tmem_st8(taddr, hb);
+  tmem_st8(taddr + 32u, hs);
 }
 
 // D (TMEM) (+)= A (TMEM, M = 128 lanes x K = 8 columns) x B (shared-memory descriptor)
@@ -169,8 +190,8 @@ __device__ __forceinline__ void cp_async_wait() {
 
 // 2-D bulk tensor copy of the box at (x, y) of `map` into shared memory,
 // completion counted on `bar`.  x (the pattern coordinate) is a multiple of
-// 16 floats (64 bytes); dst is 1024-byte aligned (a multiple of the 64-byte
-// swizzle's 512-byte period).
+// 32 floats (128 bytes); dst is 1024-byte aligned (the 128-byte swizzle's
+// period).
 __device__ __forceinline__ void tma_load_2d(void *dst, const CUtensorMap *map, int x, int y, uint64_t *bar) {
   asm volatile(
       "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];"
@@ -197,12 +218,12 @@ __device__ __forceinline__ TcbMeta tcb_meta(unsigned char *base) {
 
 // Tensor maps of the adjoint's raw rows: the partials [b][I][K][64][Npad]
 // and the children's products [b][I][K][2][64][Npad] as 2-D arrays of rows,
-// with 16-pattern boxes of 64 partial rows / 128 product rows (GEMM3 units,
-// 64-byte swizzle: the 16-byte chunk c of box row r lands at chunk
-// c ^ ((r >> 1) & 3), address bits 4-5 XOR bits 7-8) and 128-pattern x 16-row
-// boxes (GEMM2 units, no swizzle).
+// with 32-pattern boxes of 64 partial rows / 128 product rows (GEMM3 units,
+// 128-byte swizzle: the 16-byte chunk c of box row r lands at chunk
+// c ^ (r & 7), address bits 4-6 XOR bits 7-9) and 128-pattern x 16-row boxes
+// (GEMM2 units, no swizzle).
 struct TcbMaps {
-  CUtensorMap part16, prod16, part128, prod128;
+  CUtensorMap part32, prod32, part128, prod128;
 };
 
 // Barrier among the converter warps (named barrier 1) that also ORs a
@@ -303,7 +324,7 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
     if (lane == 0) {
       if (int0) bulk_prefetch_l2(img0, uint32_t(kImgFloats * sizeof(float)));
       if (int1) bulk_prefetch_l2(img1, uint32_t(kImgFloats * sizeof(float)));
-      uint32_t ph_re = 0xFu, pend_rf = 0;
+      uint32_t ph_re = (1u << kNR) - 1u, pend_rf = 0;  // every raw slot starts free
       bool ok = true;
       int tt = 0, rr = 0;
       for (int u = 0; u < total; ++u) {
@@ -320,11 +341,11 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
         if (!un.g2) {
           const int x = n0 + un.idx * kKC3;
           mbar_arrive_expect_tx(&raw_full[rs],
-                                uint32_t(8192 + 4096 * ((is_root ? 0 : 1) + (int0 ? 1 : 0) + (int1 ? 1 : 0))));
-          tma_load_2d(raw, &maps.prod16, x, vblk * 2 * SP, &raw_full[rs]);
-          if (!is_root) tma_load_2d(raw + 8192, &maps.part16, x, vblk * SP, &raw_full[rs]);
-          if (int0) tma_load_2d(raw + 12288, &maps.part16, x, lblk * SP, &raw_full[rs]);
-          if (int1) tma_load_2d(raw + 16384, &maps.part16, x, rblk * SP, &raw_full[rs]);
+                                uint32_t(16384 + 8192 * ((is_root ? 0 : 1) + (int0 ? 1 : 0) + (int1 ? 1 : 0))));
+          tma_load_2d(raw, &maps.prod32, x, vblk * 2 * SP, &raw_full[rs]);
+          if (!is_root) tma_load_2d(raw + 16384, &maps.part32, x, vblk * SP, &raw_full[rs]);
+          if (int0) tma_load_2d(raw + 24576, &maps.part32, x, lblk * SP, &raw_full[rs]);
+          if (int1) tma_load_2d(raw + 32768, &maps.part32, x, rblk * SP, &raw_full[rs]);
         } else {
           const int y = un.idx * kKC2, oblk = vblk * 2 + (1 - un.side);
           mbar_arrive_expect_tx(&raw_full[rs], uint32_t(8192 * (2 + (is_root ? 0 : 1))));
@@ -371,7 +392,7 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
       }
       tc::fence_after_sync();
       const uint64_t so = uint64_t(sl * kOpSlot) >> 4, ro = uint64_t(rs * kRawSlot) >> 4;
-      const uint32_t ta = tmem + kTmA + 32u * uint32_t(sl);  // the unit's A: big [ta, ta + 16), small + 16
+      const uint32_t ta = tmem + kTmA + kASlot * uint32_t(sl);  // the unit's A: big at ta, small at ta + 32
       if (leader) {
         if (!un.g2) {
           constexpr uint32_t idesc = tc::idesc_tf32(128, 128);
@@ -380,8 +401,8 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
             const uint64_t o = so + uint64_t(kk * 4096 >> 4);
             const uint32_t at = ta + 8u * kk;
             mma_tf32_ta(tmem, at, dOp + o, idesc, (started || kk > 0) ? 1u : 0u);
-            mma_tf32_ta(tmem, at, dOp + o + (8192 >> 4), idesc, 1u);
-            mma_tf32_ta(tmem, at + 16u, dOp + o, idesc, 1u);
+            mma_tf32_ta(tmem, at, dOp + o + (16384 >> 4), idesc, 1u);
+            mma_tf32_ta(tmem, at + 32u, dOp + o, idesc, 1u);
           }
           tc::mma_commit(&op_empty[sl]);
           mbar_arrive(&raw_empty[rs]);  // the MMAs do not read the raw slot
@@ -393,7 +414,7 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
             const uint32_t at = ta + 8u * kk;
             mma_tf32_ta(tmem + 128u, at, dB + ob, idesc, (un.idx > 0 || kk > 0) ? 1u : 0u);
             mma_tf32_ta(tmem + 128u, at, dB + ob + (4096 >> 4), idesc, 1u);
-            mma_tf32_ta(tmem + 128u, at + 16u, dB + ob, idesc, 1u);
+            mma_tf32_ta(tmem + 128u, at + 32u, dB + ob, idesc, 1u);
           }
           tc::mma_commit(&op_empty[sl]);
           tc::mma_commit(&raw_empty[rs]);  // the raw slot held B
@@ -450,17 +471,18 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
       for (int e = tid; e < code_count * 16; e += kConv)
         reinterpret_cast<float4 *>(tab)[e] = ldg4(a.table + 4 * e);
     // GEMM3 item of this thread: row R3 = (side s3, state i3) = its TMEM lane (32 (warp & 3) + lane),
-    // patterns 4 q3 .. 4 q3 + 3 of the unit (q3 = warp >> 2).  It writes u[R3][..] (A) to tensor
-    // memory and (c x)[R3][..] (B) to eight rows of one core matrix per quarter warp; the raw rows'
-    // 64-byte swizzle puts chunk q3 of the 32 rows a warp reads in distinct banks.
+    // patterns 8 q3 .. 8 q3 + 7 of the unit (q3 = warp >> 2, the row's 16-byte chunks 2 q3 and
+    // 2 q3 + 1).  It writes u[R3][..] (A) to tensor memory and (c x)[R3][..] (B) to eight rows of
+    // one core matrix per quarter warp; the raw rows' 128-byte swizzle moves chunk c of row r to
+    // c ^ (r & 7).
     const int R3 = 32 * (warp & 3) + lane, q3 = warp >> 2;
     const int s3 = R3 >> 6, i3 = R3 & 63;
-    const int sw3 = 16 * (q3 ^ ((i3 >> 1) & 3));  // swizzled byte offset of chunk q3 in rows i3, 64 + i3
+    const int sw3a = 16 * ((2 * q3) ^ (i3 & 7)), sw3b = 16 * ((2 * q3 + 1) ^ (i3 & 7));  // rows i3, 64 + i3
     const bool x3in = s3 ? int1 : int0;
     const float pre3 = is_root && i3 < a.S ? float(wk * a.freqs[size_t(b) * a.S + i3]) : 0.0f;
     // this warp's lane quarter of tensor memory
     const uint32_t tq = tmem + (uint32_t(32 * (warp & 3)) << 16);
-    uint32_t ph_rf = 0, ph_oe = 0x7u, ph_af = 0;
+    uint32_t ph_rf = 0, ph_oe = (1u << kNS) - 1u, ph_af = 0;  // every operand slot starts free
     bool ok = true;        // uniform across the converters after every conv_sync_any
     float root_acc = 0.0f; // root: this thread's share of sum_p c_p al[i][p] ar[i][p], i = tid & 63
     if (t0 < t1) {
@@ -499,25 +521,34 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
         tc::fence_after_sync();  // the MMAs that read this slot's A have completed
         unsigned char *op = smem + sl * kOpSlot;
         const unsigned char *raw = smem + kOffRaw + rs * kRawSlot;
-        const uint32_t ta = tq + kTmA + 32u * uint32_t(sl);
+        const uint32_t ta = tq + kTmA + kASlot * uint32_t(sl);
         if (!un.g2) {
-          const int pt = un.idx * kKC3 + 4 * q3;  // pattern offset in the tile
+          const int pt = un.idx * kKC3 + 8 * q3;  // pattern offset in the tile
           // u_s = pre * (the other side's product): product rows (1 - s) * 64 + i
-          const float4 o4 = *reinterpret_cast<const float4 *>(raw + ((1 - s3) * 64 + i3) * 64 + sw3);
-          const float4 p4 = is_root ? make_float4(pre3, pre3, pre3, pre3)
-                                    : *reinterpret_cast<const float4 *>(raw + 8192 + i3 * 64 + sw3);
-          float4 x4;
+          const unsigned char *orow = raw + ((1 - s3) * 64 + i3) * 128, *prow = raw + 16384 + i3 * 128;
+          const float4 oa = *reinterpret_cast<const float4 *>(orow + sw3a);
+          const float4 ob = *reinterpret_cast<const float4 *>(orow + sw3b);
+          const float4 pa = is_root ? make_float4(pre3, pre3, pre3, pre3) : *reinterpret_cast<const float4 *>(prow + sw3a);
+          const float4 pb = is_root ? make_float4(pre3, pre3, pre3, pre3) : *reinterpret_cast<const float4 *>(prow + sw3b);
+          float4 xa, xb;
           if (x3in) {
-            x4 = *reinterpret_cast<const float4 *>(raw + 12288 + s3 * 4096 + i3 * 64 + sw3);
+            const unsigned char *xrow = raw + 24576 + s3 * 8192 + i3 * 128;
+            xa = *reinterpret_cast<const float4 *>(xrow + sw3a);
+            xb = *reinterpret_cast<const float4 *>(xrow + sw3b);
           } else {
             const unsigned char *cc = meta.codes + s3 * PT + pt;
-            x4 = make_float4(tabsrc[int(cc[0]) * SP + i3], tabsrc[int(cc[1]) * SP + i3],
+            xa = make_float4(tabsrc[int(cc[0]) * SP + i3], tabsrc[int(cc[1]) * SP + i3],
                              tabsrc[int(cc[2]) * SP + i3], tabsrc[int(cc[3]) * SP + i3]);
+            xb = make_float4(tabsrc[int(cc[4]) * SP + i3], tabsrc[int(cc[5]) * SP + i3],
+                             tabsrc[int(cc[6]) * SP + i3], tabsrc[int(cc[7]) * SP + i3]);
           }
-          const float4 c4 = *reinterpret_cast<const float4 *>(meta.cf + pt);
-          split4_tmem(ta + 4u * q3, make_float4(p4.x * o4.x, p4.y * o4.y, p4.z * o4.z, p4.w * o4.w));
-          const uint32_t off = tc::kmajor_off(R3, 4 * q3, 2048);
-          split4_store(op + off, op + 8192 + off, make_float4(x4.x * c4.x, x4.y * c4.y, x4.z * c4.z, x4.w * c4.w));
+          const float4 ca = *reinterpret_cast<const float4 *>(meta.cf + pt);
+          const float4 cb = *reinterpret_cast<const float4 *>(meta.cf + pt + 4);
+          split8_tmem(ta + 8u * q3, make_float4(pa.x * oa.x, pa.y * oa.y, pa.z * oa.z, pa.w * oa.w),
+                      make_float4(pb.x * ob.x, pb.y * ob.y, pb.z * ob.z, pb.w * ob.w));
+          const uint32_t offa = tc::kmajor_off(R3, 8 * q3, 2048), offb = tc::kmajor_off(R3, 8 * q3 + 4, 2048);
+          split4_store(op + offa, op + 16384 + offa, make_float4(xa.x * ca.x, xa.y * ca.y, xa.z * ca.z, xa.w * ca.w));
+          split4_store(op + offb, op + 16384 + offb, make_float4(xb.x * cb.x, xb.y * cb.y, xb.z * cb.z, xb.w * cb.w));
         } else {
           // item (pattern p = this thread's TMEM lane, states 16 idx + 4 sq ..): A = u^T, row p, K = 4 states
           const int pp = tid & (PT - 1), sq = tid >> 7;
