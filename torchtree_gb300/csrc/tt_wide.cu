@@ -338,8 +338,8 @@ struct Wide {
     const uint64_t blocks = uint64_t(p->batch) * p->I * p->K;
     if (!encode_rows(&maps.part32, a.part, blocks * 64, uint64_t(g.Npad), 32, 64, CU_TENSOR_MAP_SWIZZLE_128B) ||
         !encode_rows(&maps.prod32, a.prod, blocks * 128, uint64_t(g.Npad), 32, 128, CU_TENSOR_MAP_SWIZZLE_128B) ||
-        !encode_rows(&maps.part128, a.part, blocks * 64, uint64_t(g.Npad), 128, 16) ||
-        !encode_rows(&maps.prod128, a.prod, blocks * 128, uint64_t(g.Npad), 128, 16))
+        !encode_rows(&maps.part128, a.part, blocks * 64, uint64_t(g.Npad), 128, 32) ||
+        !encode_rows(&maps.prod128, a.prod, blocks * 128, uint64_t(g.Npad), 128, 32))
       return cudaErrorInvalidValue;
     for (size_t lv = 0; lv + 1 < w.bwd_off.size(); ++lv) {
       a.nodes = w.d_bwd + w.bwd_off[lv];

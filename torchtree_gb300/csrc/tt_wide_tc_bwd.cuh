@@ -22,8 +22,8 @@
 // = 128 B between 8-row groups, LBO between 4-element K groups).
 //
 // The work of a tile is a sequence of units: four GEMM3 units of 32
-// patterns (K = 32, both sides), then for each internal child four GEMM2
-// units of 16 states (K = 16) and that side's epilogue.  The CTA (one per SM)
+// patterns (K = 32, both sides), then for each internal child two GEMM2
+// units of 32 states (K = 32) and that side's epilogue.  The CTA (one per SM)
 // is warp specialised: a copy warp issues each unit's raw rows (tiles of the
 // pattern-contiguous partial and product rows; GEMM3 rows with the 128-byte
 // swizzle, so that a warp reading one 16-byte column of 32 rows meets no
@@ -41,13 +41,13 @@
 // order the roles; the converters meet at a named barrier only at epilogues
 // and tile ends.  GEMM2's B operand, P_c transposed into the operand layout
 // and split, is written once per (sample, branch, category) by
-// wide_pimage_kernel; a GEMM2 unit's 16-state slice of it travels in the
-// unit's raw slot (two 4 KB bulk copies) and the MMAs read it there.
+// wide_pimage_kernel; a GEMM2 unit's 32-state slice of it travels in the
+// unit's raw slot (two 8 KB bulk copies) and the MMAs read it there.
 //
 // Tensor memory (cta_group::1, M = 128): row m is lane m, column n is column
 // n, for the accumulators (G in columns [0, 128), o in [128, 192)) and for
 // the A operands (slot sl in [256 + 64 sl, 256 + 64 sl + 64): TF32 big in
-// the first 32 columns, small in the next 32; a GEMM2 unit uses 16 of each).  A warp reads and writes the
+// the first 32 columns, small in the next 32).  A warp reads and writes the
 // 32 lanes of its quarter (warp id mod 4).
 #pragma once
 
@@ -63,12 +63,12 @@ constexpr int kPT = 128;                  // patterns per tile (GEMM2 M)
 constexpr int kConv = 512;                // converter threads (16 warps)
 constexpr int kThreads = kConv + 64;      // + the copy warp and the MMA warp
 constexpr int kKC3 = 32;                  // patterns (K) per GEMM3 unit
-constexpr int kKC2 = 16;                  // states (K) per GEMM2 unit
+constexpr int kKC2 = 32;                  // states (K) per GEMM2 unit
 constexpr int kU3 = kPT / kKC3;           // GEMM3 units per tile (both sides)
 constexpr int kU2 = 64 / kKC2;            // GEMM2 units per internal side and tile
 constexpr int kOpSlot = 32768;            // one GEMM3 unit's B operand (big, small)
 constexpr int kNS = 2;                    // operand slots (shared memory B, TMEM A)
-constexpr int kRawSlot = 40960;           // one unit's raw rows (GEMM3: 32 patterns of 320 rows; GEMM2: 24 KB with its image slice)
+constexpr int kRawSlot = 49152;           // one unit's raw rows (GEMM3: 32 patterns of 320 rows, 40 KB; GEMM2: 32 rows x 2 and the image slice)
 constexpr int kNR = 3;                    // raw slots
 constexpr int kMeta = kPT * 16 + 2 * kPT; // a tile's coefficients, exponents and tip codes
 constexpr int kOffRaw = kNS * kOpSlot;
@@ -77,8 +77,8 @@ constexpr int kOffMraw = kOffMeta + 2 * kMeta;  // the next tile's weights and s
 constexpr int kOffRed = kOffMraw + 2 * kPT * 8; // float [4][128]
 constexpr int kOffRoot = kOffRed + 4 * kPT * 4; // float [512] root partial sums
 constexpr int kTabRows = 64;               // code-table rows held in shared memory (tip children)
-constexpr int kOffTab = kOffRoot + kConv * 4;   // float [kTabRows][64]
-constexpr int kOffBar = kOffTab + kTabRows * 64 * 4;
+constexpr int kOffTab = kOffRoot + kConv * 4;   // uint2 [kTabRows]: the rows of a 0 / 1 table as bit masks
+constexpr int kOffBar = kOffTab + kTabRows * 8;
 // mbarriers: raw full / empty [kNR], operand full / empty [kNS], accumulator full / empty, done
 constexpr int kBars = 2 * kNR + 2 * kNS + 3;
 constexpr int kSmem = kOffBar + 8 * kBars + 16;
@@ -113,25 +113,7 @@ __global__ void __launch_bounds__(256) wide_pimage_kernel(const float *pmat, flo
 
 __device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
 
-// four consecutive 32-bit TMEM columns of this thread's lane (the warp's lane quarter)
-__device__ __forceinline__ void tmem_st4(uint32_t taddr, float4 v) {
-  asm volatile("tcgen05.st.sync.aligned.32x32b.x4.b32 [%0], {%1, %2, %3, %4};" ::"r"(taddr),
-               "r"(__float_as_uint(v.x)), "r"(__float_as_uint(v.y)), "r"(__float_as_uint(v.z)),
-               "r"(__float_as_uint(v.w))
-               : "memory");
-}
 __device__ __forceinline__ void tmem_st_wait() { asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory"); }
-
-// v split into TF32 big and small, stored to TMEM columns c and c + 32
-__device__ __forceinline__ void split4_tmem(uint32_t taddr, float4 v) {
-  float4 hb, hs;
-  tc::split_tf32(v.x, hb.x, hs.x);
-  tc::split_tf32(v.y, hb.y, hs.y);
-  tc::split_tf32(v.z, hb.z, hs.z);
-  tc::split_tf32(v.w, hb.w, hs.w);
-  tmem_st4(taddr, hb);
-  tmem_st4(taddr + 32u, hs);
-}
 
 // eight consecutive 32-bit TMEM columns of this thread's lane
 __device__ __forceinline__ void tmem_st8(uint32_t taddr, const float (&v)[8]) {
@@ -220,7 +202,7 @@ __device__ __forceinline__ TcbMeta tcb_meta(unsigned char *base) {
 // and the children's products [b][I][K][2][64][Npad] as 2-D arrays of rows,
 // with 32-pattern boxes of 64 partial rows / 128 product rows (GEMM3 units,
 // 128-byte swizzle: the 16-byte chunk c of box row r lands at chunk
-// c ^ (r & 7), address bits 4-6 XOR bits 7-9) and 128-pattern x 16-row boxes
+// c ^ (r & 7), address bits 4-6 XOR bits 7-9) and 128-pattern x 32-row boxes
 // (GEMM2 units, no swizzle).
 struct TcbMaps {
   CUtensorMap part32, prod32, part128, prod128;
@@ -348,13 +330,13 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
           if (int1) tma_load_2d(raw + 32768, &maps.part32, x, rblk * SP, &raw_full[rs]);
         } else {
           const int y = un.idx * kKC2, oblk = vblk * 2 + (1 - un.side);
-          mbar_arrive_expect_tx(&raw_full[rs], uint32_t(8192 * (2 + (is_root ? 0 : 1))));
+          mbar_arrive_expect_tx(&raw_full[rs], uint32_t(16384 * (2 + (is_root ? 0 : 1))));
           tma_load_2d(raw, &maps.prod128, n0, oblk * SP + y, &raw_full[rs]);
-          if (!is_root) tma_load_2d(raw + 8192, &maps.part128, n0, vblk * SP + y, &raw_full[rs]);
-          // the unit's 16-state slice of the P^T image (K groups 4 idx .. 4 idx + 3), big and small
-          const float *src = (un.side ? img1 : img0) + un.idx * 1024;
-          bulk_copy_g2s(raw + 16384, src, 4096u, &raw_full[rs]);
-          bulk_copy_g2s(raw + 20480, src + 4096, 4096u, &raw_full[rs]);
+          if (!is_root) tma_load_2d(raw + 16384, &maps.part128, n0, vblk * SP + y, &raw_full[rs]);
+          // the unit's 32-state slice of the P^T image (K groups 8 idx .. 8 idx + 7), big and small
+          const float *src = (un.side ? img1 : img0) + un.idx * 2048;
+          bulk_copy_g2s(raw + 32768, src, 8192u, &raw_full[rs]);
+          bulk_copy_g2s(raw + 40960, src + 4096, 8192u, &raw_full[rs]);
         }
         pend_rf |= 1u << rs;
         if (++rr == UT) {
@@ -410,10 +392,10 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
           constexpr uint32_t idesc = tc::idesc_tf32(128, 64);
 #pragma unroll
           for (int kk = 0; kk < kKC2 / 8; ++kk) {
-            const uint64_t ob = ro + uint64_t(16384 + kk * 2048 >> 4);
+            const uint64_t ob = ro + uint64_t(32768 + kk * 2048 >> 4);
             const uint32_t at = ta + 8u * kk;
             mma_tf32_ta(tmem + 128u, at, dB + ob, idesc, (un.idx > 0 || kk > 0) ? 1u : 0u);
-            mma_tf32_ta(tmem + 128u, at, dB + ob + (4096 >> 4), idesc, 1u);
+            mma_tf32_ta(tmem + 128u, at, dB + ob + (8192 >> 4), idesc, 1u);
             mma_tf32_ta(tmem + 128u, at + 32u, dB + ob, idesc, 1u);
           }
           tc::mma_commit(&op_empty[sl]);
@@ -463,13 +445,34 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
         m.cf[tid] = n < a.N ? ldexpf(float(mw[tid]) * exp2f(float(dd - fl)), int(fl)) : 0.0f;
       }
     };
-    // a tip child's rows of the code table, in shared memory when the table is small
-    const bool tab_smem = (!int0 || !int1) && code_count <= kTabRows;
-    float *tab = reinterpret_cast<float *>(smem + kOffTab);
-    const float *tabsrc = tab_smem ? tab : a.table;
-    if (tab_smem)
-      for (int e = tid; e < code_count * 16; e += kConv)
-        reinterpret_cast<float4 *>(tab)[e] = ldg4(a.table + 4 * e);
+    // a tip child's rows of the code table: as bit masks in shared memory when every entry is 0 or 1
+    // (the encodings' indicator rows) and the table is small, else read from global memory
+    uint2 *tabm = reinterpret_cast<uint2 *>(smem + kOffTab);
+    bool tab_bits = (!int0 || !int1) && code_count <= kTabRows;
+    if (tab_bits) {
+      bool binary = true;
+      for (int e = tid; e < code_count * 2; e += kConv) {  // row e >> 1, states 32 (e & 1) .. + 31
+        const float *row = a.table + (e >> 1) * SP + 32 * (e & 1);
+        uint32_t m = 0;
+#pragma unroll 8
+        for (int j = 0; j < 32; ++j) {
+          const float t = __ldg(row + j);
+          binary = binary && (t == 0.0f || t == 1.0f);
+          m |= (t == 1.0f ? 1u : 0u) << j;
+        }
+        if (e & 1) tabm[e >> 1].y = m;
+        else tabm[e >> 1].x = m;
+      }
+      tab_bits = !conv_sync_any(!binary);
+    }
+    // x of tip code c at state i
+    auto tipx = [&](int c, int i) -> float {
+      if (tab_bits) {
+        const uint2 m = tabm[c];
+        return ((i < 32 ? m.x >> i : m.y >> (i - 32)) & 1u) ? 1.0f : 0.0f;
+      }
+      return __ldg(a.table + c * SP + i);
+    };
     // GEMM3 item of this thread: row R3 = (side s3, state i3) = its TMEM lane (32 (warp & 3) + lane),
     // patterns 8 q3 .. 8 q3 + 7 of the unit (q3 = warp >> 2, the row's 16-byte chunks 2 q3 and
     // 2 q3 + 1).  It writes u[R3][..] (A) to tensor memory and (c x)[R3][..] (B) to eight rows of
@@ -537,10 +540,8 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
             xb = *reinterpret_cast<const float4 *>(xrow + sw3b);
           } else {
             const unsigned char *cc = meta.codes + s3 * PT + pt;
-            xa = make_float4(tabsrc[int(cc[0]) * SP + i3], tabsrc[int(cc[1]) * SP + i3],
-                             tabsrc[int(cc[2]) * SP + i3], tabsrc[int(cc[3]) * SP + i3]);
-            xb = make_float4(tabsrc[int(cc[4]) * SP + i3], tabsrc[int(cc[5]) * SP + i3],
-                             tabsrc[int(cc[6]) * SP + i3], tabsrc[int(cc[7]) * SP + i3]);
+            xa = make_float4(tipx(cc[0], i3), tipx(cc[1], i3), tipx(cc[2], i3), tipx(cc[3], i3));
+            xb = make_float4(tipx(cc[4], i3), tipx(cc[5], i3), tipx(cc[6], i3), tipx(cc[7], i3));
           }
           const float4 ca = *reinterpret_cast<const float4 *>(meta.cf + pt);
           const float4 cb = *reinterpret_cast<const float4 *>(meta.cf + pt + 4);
@@ -550,18 +551,18 @@ __global__ void __launch_bounds__(tcb::kThreads, 1)
           split4_store(op + offa, op + 16384 + offa, make_float4(xa.x * ca.x, xa.y * ca.y, xa.z * ca.z, xa.w * ca.w));
           split4_store(op + offb, op + 16384 + offb, make_float4(xb.x * cb.x, xb.y * cb.y, xb.z * cb.z, xb.w * cb.w));
         } else {
-          // item (pattern p = this thread's TMEM lane, states 16 idx + 4 sq ..): A = u^T, row p, K = 4 states
+          // item (pattern p = this thread's TMEM lane, states 32 idx + 8 sq ..): A = u^T, row p, K = 8 states
           const int pp = tid & (PT - 1), sq = tid >> 7;
-          float uu[4];
+          float uu[8];
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            const int row = 4 * sq + e, i = un.idx * kKC2 + row;
+          for (int e = 0; e < 8; ++e) {
+            const int row = 8 * sq + e, i = un.idx * kKC2 + row;
             const float ot = *reinterpret_cast<const float *>(raw + row * 512 + pp * 4);
             const float pv = is_root ? (i < a.S ? float(wk * a.freqs[size_t(b) * a.S + i]) : 0.0f)
-                                     : *reinterpret_cast<const float *>(raw + 8192 + row * 512 + pp * 4);
+                                     : *reinterpret_cast<const float *>(raw + 16384 + row * 512 + pp * 4);
             uu[e] = pv * ot;
           }
-          split4_tmem(ta + 4u * sq, make_float4(uu[0], uu[1], uu[2], uu[3]));
+          split8_tmem(ta + 8u * sq, make_float4(uu[0], uu[1], uu[2], uu[3]), make_float4(uu[4], uu[5], uu[6], uu[7]));
         }
         tmem_st_wait();
         if (!un.g2) asm volatile("fence.proxy.async.shared::cta;" ::: "memory");  // B: generic writes -> tensor cores
