@@ -5,7 +5,7 @@ Workload (default ``gtr_g4_t1000_b8``): GTR+Gamma4 on a 1,000-taxon Yule tree
 with 100,000 simulated DNA sites (compressed to N unique patterns), a batch of
 8 branch-length samples.  One *step* = one batched evaluation: the model
 set-up (Gamma category rates by the quantile kernel, the normalised rate
-matrix, its FP64 eigen system by the Jacobi kernel), transition matrices,
+matrix, its FP64 eigen system by the device eigensolver), transition matrices,
 post-order pass, pre-order adjoint pass and all reductions, giving lnL and
 the full gradient (branch lengths, rate matrix -> exchangeabilities and
 frequencies, category rates/weights) for every sample.  One *evaluation*
@@ -661,7 +661,7 @@ def main():
     def model_setup():
         """The per-step model work on the device: Gamma category rates
         (quantile kernel), the normalised rate matrix (a few torch ops) and
-        its FP64 eigen system (Jacobi kernel)."""
+        its FP64 eigen system (device eigensolver)."""
         r, p = site_models.gamma_rates(shape, K)
         qn = substitution.normalise(rate_matrix(wl.model, exch, pi), pi)
         lam_, u_, w_ = substitution.device_eigen(qn, pi)

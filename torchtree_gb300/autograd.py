@@ -52,7 +52,7 @@ class RateMatrixLikelihood(torch.autograd.Function):
     """lnL ``[b]`` from the normalised rate matrix ``q [b,S,S]`` (stationary
     distribution ``pi_q``), node branch lengths, category rates/weights and
     root frequencies.  The eigen system is formed here without autograd (on
-    the device, by the engine's Jacobi kernel, for CUDA tensors); the
+    the device, by the engine's eigensolver, for CUDA tensors); the
     backward returns dlnL/dQ from the derivative of the matrix exponential in
     the eigenbasis (``tt_rate_matrix_gradient``), so no eigenvector
     derivative enters the chain to the rate-matrix parameters."""

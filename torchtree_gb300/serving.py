@@ -32,7 +32,7 @@ chain -- as one captured CUDA graph on the data set's own stream:
 The rate-matrix construction and the site model stay in torch on the host
 (FP64, autograd), as in ``PhyloLikelihood``; the step receives the
 normalised Q, branch lengths, category rates and weights through pinned
-host buffers, forms the eigen system on the device (Jacobi kernel) and
+host buffers, forms the eigen system on the device (device eigensolver) and
 returns dlnL/dQ (matrix-exponential derivative), branch-length, rate, weight
 and frequency gradients, which the host chains back to the request's
 parameters.
@@ -301,7 +301,7 @@ def merged_step(batches: list, stream, device) -> torch.cuda.Event:
         for ex in execs:
             for k, v in ex.inputs.items():
                 v.copy_(ex.host_in[k], non_blocking=True)
-        # all members are 4-state: their Q and pi stack into one Jacobi launch
+        # all members are 4-state: their Q and pi stack into one eigensolver call
         lam, u, w = substitution.device_eigen(torch.cat([ex.inputs["q"] for ex in execs]),
                                               torch.cat([ex.inputs["pi"] for ex in execs]))
         eig = []

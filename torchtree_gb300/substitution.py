@@ -7,7 +7,7 @@ factorisation of torchtree's ``SymmetricSubstitutionModel.p_t``
 Pi^1/2, ``eigh``, ``U = Pi^-1/2 V``, ``W = V^-1 Pi^1/2``.  The rate-matrix
 builders stay in torch so that autograd carries the engine's gradients back
 to exchangeabilities and frequencies.  The eigendecomposition of device
-tensors runs in the engine's FP64 Jacobi kernel (``tt_reversible_eigen``)
+tensors runs in the engine's eigensolver (``tt_reversible_eigen``)
 whenever no gradient has to flow through it, as in the rate-matrix route,
 whose backward needs no eigenvector derivative; otherwise ``torch.linalg.eigh``
 keeps the autograd graph.
