@@ -43,14 +43,18 @@ def _setup(wl):
         probs.expand(b, K).to(dev).contiguous(), pi.to(dev)
 
 
-def _run(wl, precision, tc=True, rescale=True, grads=True, tca=None):
+def _run(wl, precision, tc=True, rescale=True, grads=True, tca=None, halve_row=None):
     from torchtree_gb300.engine import LikelihoodEngine
 
     ca, S, K, b, eig, probs, pi = _setup(wl)
+    table = ca.table
+    if halve_row is not None:  # a code-table row that is not 0 / 1 (tip partials with weights)
+        table = np.array(table, dtype=np.float64, copy=True)
+        table[halve_row] *= 0.5
     old = os.environ.get("TT_WIDE_TC")
     os.environ["TT_WIDE_TC"] = "1" if tc else "0"
     try:
-        eng = LikelihoodEngine(wl.topology.postorder, wl.topology.tip_count, S, K, ca.codes, ca.table, ca.weights,
+        eng = LikelihoodEngine(wl.topology.postorder, wl.topology.tip_count, S, K, ca.codes, table, ca.weights,
                                batch=b, precision=precision)
     finally:
         if old is None:
@@ -117,6 +121,23 @@ def test_codon_tensor_core_adjoint_matches_cuda_core(tips, sites, batch, seed):
     d = _run(wl, "f64")
     for key in ("dt", "dpi", "dr"):
         np.testing.assert_allclose(a[key], d[key], rtol=1e-4, atol=1e-4 * np.abs(d[key]).max(), err_msg=key)
+
+
+def test_codon_tensor_core_adjoint_with_a_non_binary_code_table():
+    """A code table with a row that is not 0 / 1 keeps the tcgen05 adjoint off
+    its bit-mask copy of the table (tip rows read from global memory): still
+    the CUDA-core adjoint's gradients within FP32 rounding."""
+    from torchtree_gb300 import datatype, patterns, synthetic
+
+    wl = synthetic.codon_workload("c", tip_count=12, site_count=300, batch=2, seed=36, shape=0.5)
+    codes = patterns.compress(wl.sequences, datatype.get(wl.data_type)).codes
+    row = int(np.bincount(np.asarray(codes).ravel()).argmax())  # the most used code
+    a = _run(wl, "f32", tca=1, halve_row=row)
+    c = _run(wl, "f32", tca=0, halve_row=row)
+    np.testing.assert_array_equal(a["lnl"], c["lnl"])
+    for key in ("dt", "dpi", "dc", "dr"):
+        scale = np.abs(c[key]).max()
+        np.testing.assert_allclose(a[key], c[key], rtol=1e-4, atol=1e-4 * scale, err_msg=key)
 
 
 def test_codon_fp32_against_fp64():
