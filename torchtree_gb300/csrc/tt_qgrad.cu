@@ -38,6 +38,25 @@ __device__ __forceinline__ T frechet(T lm, T ln, T tau) {
   return tau * exp_t(a > c ? a : c) * phi;
 }
 
+// The same divided difference from the states' exponentials em = exp(am),
+// en = exp(an) (am = lambda_m tau, an = lambda_n tau), FP32: far apart,
+// tau (em - en) / (am - an) has no cancellation; within 0.5, the Taylor
+// series of expm1(x) / x to x^7 (remainder below 1.1e-8 for |x| <= 0.5).
+__device__ __forceinline__ float frechet_e(float am, float an, float em, float en, float tau) {
+  const float d = am - an;
+  if (fabsf(d) > 0.5f) return tau * (em - en) / d;
+  const float x = -fabsf(d);
+  float phi = 1.0f / 40320.0f;
+  phi = fmaf(phi, x, 1.0f / 5040.0f);
+  phi = fmaf(phi, x, 1.0f / 720.0f);
+  phi = fmaf(phi, x, 1.0f / 120.0f);
+  phi = fmaf(phi, x, 1.0f / 24.0f);
+  phi = fmaf(phi, x, 1.0f / 6.0f);
+  phi = fmaf(phi, x, 0.5f);
+  phi = fmaf(phi, x, 1.0f);
+  return tau * fmaxf(em, en) * phi;
+}
+
 }  // namespace
 
 // 4 states, FP64: one CTA per (chunk of 128 branches, sample), one branch per
@@ -131,7 +150,9 @@ __global__ void __launch_bounds__(256) wide_qgrad_kernel(const double *G, const 
   T *gt = wt + SP * SP;                  // [j][perm i] = G[i][j]
   T *hs = gt + SP * SP;                  // [i][perm n] = H[i][n]
   T *ls = hs + SP * SP;                  // lambda [SP]
-  double *dred = reinterpret_cast<double *>(ls + SP);  // [IB] diagonal sums
+  T *lt = ls + SP;                       // lambda tau [SP] (FP32 plans)
+  T *es = lt + SP;                       // exp(lambda tau) [SP] (FP32 plans)
+  double *dred = reinterpret_cast<double *>(es + SP);  // [IB] diagonal sums
   const int chunk = blockIdx.x, b = blockIdx.y, tid = threadIdx.x;
   for (int e = tid; e < SP * SP; e += 256) {
     const int x = e / SP, y = e - x * SP;
@@ -154,7 +175,12 @@ __global__ void __launch_bounds__(256) wide_qgrad_kernel(const double *G, const 
     double dt = 0.0;
     for (int k = 0; k < K; ++k) {
       const T tau = T(t * rates[size_t(b) * K + k]);
-      __syncthreads();  // previous products done with gt / hs
+      __syncthreads();  // previous products done with gt / hs / es
+      if constexpr (sizeof(T) == 4)
+        for (int m = tid; m < SP; m += 256) {
+          lt[m] = ls[m] * tau;
+          es[m] = m < S ? exp_t(ls[m] * tau) : T(0);
+        }
       const double *g = G + ((size_t(b) * B + br) * K + k) * S * S;
       for (int e = tid; e < SP * SP; e += 256) {
         const int i = e / SP, j = e - i * SP;
@@ -201,16 +227,26 @@ __global__ void __launch_bounds__(256) wide_qgrad_kernel(const double *G, const 
           }
 #pragma unroll
           for (int x = 0; x < 4; ++x) {
-            const T lm = ls[bm + IB * x];
+            const int m = bm + IB * x;
 #pragma unroll
-            for (int y = 0; y < 4; ++y) X[nb][x][y] += frechet(lm, ls[bn + IB * y], tau) * M[x][y];
+            for (int y = 0; y < 4; ++y) {
+              const int n = bn + IB * y;
+              if constexpr (sizeof(T) == 4)
+                X[nb][x][y] += frechet_e(lt[m], lt[n], es[m], es[n], tau) * M[x][y];
+              else
+                X[nb][x][y] += frechet(ls[m], ls[n], tau) * M[x][y];
+            }
           }
           if (bm == bn)
 #pragma unroll
             for (int x = 0; x < 4; ++x) {
               const int m = bm + IB * x;
               // in the plan's type (an FP64 exp costs thousands of cycles of this GPU's FP64 pipe)
-              if (m < S) dsum += double(ls[m] * exp_t(ls[m] * tau) * M[x][x]);
+              if constexpr (sizeof(T) == 4) {
+                if (m < S) dsum += double(ls[m] * es[m] * M[x][x]);
+              } else {
+                if (m < S) dsum += double(ls[m] * exp_t(ls[m] * tau) * M[x][x]);
+              }
             }
         }
       }
@@ -298,7 +334,7 @@ template <typename T, int SP>
 cudaError_t launch_wide_qgrad(tt_plan *p, const double *lam, const double *U, const double *W, const double *bl,
                               const double *rates, double *dbl, double *part, int bchunk, int nchunks,
                               cudaStream_t s) {
-  const size_t smem = 4 * SP * SP * sizeof(T) + SP * sizeof(T) + (SP / 4 + 2) * sizeof(double) + 16;
+  const size_t smem = 4 * SP * SP * sizeof(T) + 3 * SP * sizeof(T) + (SP / 4 + 2) * sizeof(double) + 16;
   cudaError_t e = kernel_smem(wide_qgrad_kernel<T, SP>, smem);
   if (e != cudaSuccess) return e;
   wide_qgrad_kernel<T, SP><<<dim3(nchunks, p->batch), 256, smem, s>>>(p->d_G, lam, U, W, bl, rates, p->S, p->B,
