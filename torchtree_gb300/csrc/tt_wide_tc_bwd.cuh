@@ -1,6 +1,6 @@
 // Codon (SP = 64) adjoint on the 5th-generation tensor cores.
 //
-// One CTA = (chunk of pattern tiles, node v, sample b x category k), 256
+// One CTA = (chunk of pattern tiles, node v, sample b x category k), 576
 // threads; a tile is 128 patterns.  For each side c of v (child c, the other
 // child c') and tile:
 //   u_c[i][p] = pre_v[i][p] * (P_c' x_c')[i][p]   (outside partial of v times
@@ -34,10 +34,10 @@
 // tensor-core work of each converted unit.  A operands (u for GEMM3, u^T for
 // GEMM2: M = 128 rows = TMEM lanes, K = columns) go to tensor memory by
 // tcgen05.st, in a ring of two 64-column slots; GEMM3's B operand goes to
-// shared memory (K-major stores) in a ring of two operand slots.  Shared
-// memory bandwidth bounds this kernel (TMA writes, the converters' reads and
-// writes and the MMAs' operand reads all share it); A in tensor memory takes
-// the A writes and reads off it.  Full / empty mbarriers per slot
+// shared memory (K-major stores) in a ring of two operand slots.  The
+// converters' issue rate and the per-unit synchronisation bound this kernel,
+// so units are wide (32 patterns or states) and A in tensor memory keeps the
+// A writes and reads off shared memory.  Full / empty mbarriers per slot
 // order the roles; the converters meet at a named barrier only at epilogues
 // and tile ends.  GEMM2's B operand, P_c transposed into the operand layout
 // and split, is written once per (sample, branch, category) by
