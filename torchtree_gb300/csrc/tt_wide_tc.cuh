@@ -120,7 +120,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 // Post-order level kernel for FP32 codon plans on the tensor cores.
 // pimg: split P images (row i, K element j, big then small; wide_pimage_kernel
 // with transposed = 0), one 32 KB bulk copy per side; NULL stages P by the
-// threads.
+// threads.  The second side's child values are loaded into registers while
+// the first side's MMAs run.
 __global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const WideArgs<float> a, const float *pimg,
                                                                          int *status, unsigned long long timeout_ns) {
   constexpr int SP = 64;
@@ -150,6 +151,25 @@ __global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const 
   int phase = 0, phase_b = 0;
   bool b_pending = false;  // thread 0: an image copy whose completion it has not seen
   uint32_t tmem = 0;  // read from the slot after the first barrier
+  // the A operand values of a side: x_c^T, M = pattern (this thread's), K = j, all 64 loads in
+  // flight at once; the second side's are issued while the first side's MMAs run
+  float xv[SP];
+  auto load_x = [&](int child) {
+    if (child < a.tips) {
+      const int code = a.codes[size_t(child) * a.code_stride + n0 + tid];
+      const float4 *row = reinterpret_cast<const float4 *>(a.table + size_t(code) * SP);
+#pragma unroll
+      for (int j = 0; j < SP; j += 4) {
+        const float4 t4 = __ldg(row + j / 4);
+        xv[j] = t4.x, xv[j + 1] = t4.y, xv[j + 2] = t4.z, xv[j + 3] = t4.w;
+      }
+    } else {
+      const float *src = a.part + ((size_t(b) * a.I + (child - a.tips)) * a.K + k) * SP * size_t(a.Npad) + n0 + tid;
+#pragma unroll
+      for (int j = 0; j < SP; ++j) xv[j] = __ldg(src + size_t(j) * a.Npad);
+    }
+  };
+  load_x(l);
   for (int c = 0; c < 2 && ok; ++c) {
     const int child = c ? r : l;
     // B operand: P_c[i][j], N = i, K = j: the split image in one bulk copy, or
@@ -181,24 +201,8 @@ __global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const 
         *reinterpret_cast<float4 *>(sB + tc::kBbytes + off) = hs;
       }
     }
-    // A operand: x_c^T, M = pattern (this thread's), K = j; all 64 loads in
-    // flight before the split, four j per 16-byte store
+    // A operand: the side's loaded values split, four j per 16-byte store
     {
-      float xv[SP];
-      if (child < a.tips) {
-        const int code = a.codes[size_t(child) * a.code_stride + n0 + tid];
-        const float4 *row = reinterpret_cast<const float4 *>(a.table + size_t(code) * SP);
-#pragma unroll
-        for (int j = 0; j < SP; j += 4) {
-          const float4 t4 = __ldg(row + j / 4);
-          xv[j] = t4.x, xv[j + 1] = t4.y, xv[j + 2] = t4.z, xv[j + 3] = t4.w;
-        }
-      } else {
-        const float *src =
-            a.part + ((size_t(b) * a.I + (child - a.tips)) * a.K + k) * SP * size_t(a.Npad) + n0 + tid;
-#pragma unroll
-        for (int j = 0; j < SP; ++j) xv[j] = __ldg(src + size_t(j) * a.Npad);
-      }
 #pragma unroll
       for (int j = 0; j < SP; j += 4) {
         float4 hb, hs;
@@ -240,12 +244,7 @@ __global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const 
     } else if (tid == 0) {
       mbar_arrive(bar);  // no MMAs (the image never landed): complete the phase; the side fails below
     }
-    if (c == 0 && r >= a.tips) {  // while the MMAs run: the other child's rows into L2 (lane j: rows j, j + 32)
-      const float *nxt = a.part + ((size_t(b) * a.I + (r - a.tips)) * a.K + k) * SP * size_t(a.Npad) + n0 + 32 * warp;
-      const int lane = tid & 31;
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(nxt + size_t(lane) * a.Npad));
-      asm volatile("prefetch.global.L2 [%0];" ::"l"(nxt + size_t(lane + 32) * a.Npad));
-    }
+    if (c == 0) load_x(r);  // while the MMAs run: the other side's values into registers
     // every thread sees the side's MMAs complete before the shared memory is restaged or TMEM read
     ok = mbar_wait_bounded(bar, phase, timeout_ns) && !(tid == 0 && b_pending);
     tc::fence_after_sync();
