@@ -83,6 +83,7 @@ struct WideState {
   double *d_site = nullptr;  // slab mode: one slab's site log-likelihoods [b][slab]
   std::vector<int> fwd_off, bwd_off;  // level boundaries in d_fwd / d_bwd
   int *d_left = nullptr, *d_right = nullptr, *d_fwd = nullptr, *d_bwd = nullptr;
+  int *d_branch_lvn = nullptr;  // [B] node count of each branch's parent level (adjoint chunking)
   void *d_part = nullptr;
   int *d_expo = nullptr;
   double *d_root_site = nullptr;
@@ -341,16 +342,22 @@ struct Wide {
         !encode_rows(&maps.part128, a.part, blocks * 64, uint64_t(g.Npad), 128, 32) ||
         !encode_rows(&maps.prod128, a.prod, blocks * 128, uint64_t(g.Npad), 128, 32))
       return cudaErrorInvalidValue;
+    // a.nchunks stays the chunk stride of the gradient blocks; each level launches
+    // tc_level_chunks(...) <= a.nchunks chunks (the root's level all of them)
+    const int bk = p->batch * p->K;
     for (size_t lv = 0; lv + 1 < w.bwd_off.size(); ++lv) {
+      const int nodes = w.bwd_off[lv + 1] - w.bwd_off[lv];
+      const int chunks = tc_level_chunks(nodes, bk, ntc, cmax);
       a.nodes = w.d_bwd + w.bwd_off[lv];
-      const dim3 grid(a.nchunks, w.bwd_off[lv + 1] - w.bwd_off[lv], p->batch * p->K);
+      a.tiles_per_chunk = (ntc + chunks - 1) / chunks;
+      const dim3 grid(chunks, nodes, bk);
       wide_backward_tc_kernel<<<grid, tcb::kThreads, tcb::kSmem, s>>>(a, maps, w.d_pimg, p->C, p->d_status,
                                                                        2000000000ull);
       p->launches += 1;
     }
     wide_grad_reduce_kernel<float><<<dim3(p->B, p->batch), 256, 0, s>>>(static_cast<const float *>(w.d_gpart),
                                                                          p->d_G, p->B, a.nchunks, p->K, p->S, 64,
-                                                                         accumulate);
+                                                                         accumulate, w.d_branch_lvn, bk, ntc, cmax);
     wide_root_reduce_kernel<float><<<p->batch, 64, 0, s>>>(static_cast<const float *>(w.d_rootpart), p->d_rootgrad,
                                                            p->d_rootgrad + size_t(p->batch) * p->S, a.nchunks, p->K,
                                                            p->S, 64, accumulate);
@@ -439,9 +446,17 @@ int wide_create(tt_plan *p) {
     w->fwd_off.push_back(int(fwd.size()));
   }
   w->bwd_off.push_back(0);
+  std::vector<int> branch_lvn(size_t(p->B), 1);
   for (int d = 0; d <= D; ++d) {
+    const size_t first = bwd.size();
     for (int v = T; v < NN; ++v)
       if (depth[v] == d) bwd.push_back(v);
+    const int n = int(bwd.size() - first);
+    for (size_t i = first; i < bwd.size(); ++i) {
+      const int v = bwd[i];
+      branch_lvn[left[v - T]] = n;
+      branch_lvn[right[v - T]] = n;
+    }
     w->bwd_off.push_back(int(bwd.size()));
   }
   const size_t es = p->elem, SP = size_t(w->SP), b = size_t(p->batch), K = size_t(p->K);
@@ -450,6 +465,7 @@ int wide_create(tt_plan *p) {
   if (!rc) rc = walloc(p, &w->d_right, I * sizeof(int), "children");
   if (!rc) rc = walloc(p, &w->d_fwd, I * sizeof(int), "levels");
   if (!rc) rc = walloc(p, &w->d_bwd, I * sizeof(int), "levels");
+  if (!rc) rc = walloc(p, &w->d_branch_lvn, size_t(p->B) * sizeof(int), "branch levels");
   if (!rc) rc = walloc(p, &p->d_codes, size_t(T) * p->code_stride, "tip codes");
   if (!rc) rc = walloc(p, &p->d_table, 256 * SP * es, "code table");
   if (!rc) rc = walloc(p, &p->d_weights, size_t(p->N) * sizeof(double), "weights");
@@ -478,6 +494,8 @@ int wide_create(tt_plan *p) {
   if (e == cudaSuccess) e = cudaMemcpy(w->d_right, right.data(), I * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(w->d_fwd, fwd.data(), I * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemcpy(w->d_bwd, bwd.data(), I * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(w->d_branch_lvn, branch_lvn.data(), size_t(p->B) * sizeof(int), cudaMemcpyHostToDevice);
   if (e == cudaSuccess) e = cudaMemset(p->d_status, 0, sizeof(int));
   if (e == cudaSuccess)
     e = dispatch(p, [](auto W) { return decltype(W)::prepare(); });
@@ -608,7 +626,7 @@ bool wide_tensor_core_adjoint(const tt_plan *p) { return p->wide && p->wide->tc_
 void wide_destroy(tt_plan *p) {
   WideState *w = p->wide;
   if (!w) return;
-  void *bufs[] = {w->d_left, w->d_right, w->d_fwd, w->d_bwd, w->d_part, w->d_expo, w->d_root_site, w->d_root_expo,
+  void *bufs[] = {w->d_left, w->d_right, w->d_fwd, w->d_bwd, w->d_branch_lvn, w->d_part, w->d_expo, w->d_root_site, w->d_root_expo,
                   w->d_log2L, w->d_block_lnl, w->d_gpart, w->d_rootpart, w->d_pgpart, w->d_prod, w->d_site,
                   w->d_pimg, w->d_pimg_f};
   for (void *x : bufs)
