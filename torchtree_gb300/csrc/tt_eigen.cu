@@ -112,12 +112,30 @@ __device__ bool jacobi_sweeps(T *A, T *V, T *cs, int *pq, double *red, int *flag
         if (qq < n) {
           const T apq = A[p * kEigLd + qq];
           if (apq != T(0)) {
-            const T tau = (A[qq * kEigLd + qq] - A[p * kEigLd + p]) / (T(2) * apq);
-            T t;
-            if (fabs(tau) > (sizeof(T) == 4 ? T(1e18) : T(1e150))) t = T(0.5) / tau;
-            else t = (tau >= T(0) ? T(1) : T(-1)) / (fabs(tau) + sqrt(T(1) + tau * tau));
-            c = T(1) / sqrt(T(1) + t * t);
-            s = t * c;
+            if constexpr (sizeof(T) == 4) {
+              const T tau = (A[qq * kEigLd + qq] - A[p * kEigLd + p]) / (T(2) * apq);
+              T t;
+              if (fabs(tau) > T(1e18)) t = T(0.5) / tau;
+              else t = (tau >= T(0) ? T(1) : T(-1)) / (fabs(tau) + sqrt(T(1) + tau * tau));
+              c = T(1) / sqrt(T(1) + t * t);
+              s = t * c;
+            } else {
+              // FP64 division and square root are long dependency chains on this GPU, and
+              // every round waits for its rotations: the angle to FP32 accuracy (a slightly
+              // inexact angle leaves a residual the next sweep removes), then c = (1 + t^2)^-1/2
+              // from an FP32 seed by two Newton steps y <- y (3 - x y^2) / 2 in FP64, so that
+              // c^2 + s^2 = 1 to FP64 rounding and the rotation stays orthogonal
+              const float tf = float(A[qq * kEigLd + qq] - A[p * kEigLd + p]) / float(2.0 * apq);
+              float t32;
+              if (!(fabsf(tf) <= 1e18f)) t32 = 0.5f / tf;
+              else t32 = (tf >= 0.0f ? 1.0f : -1.0f) / (fabsf(tf) + sqrtf(1.0f + tf * tf));
+              const double t = double(t32), x = 1.0 + t * t;
+              double y = double(rsqrtf(float(x)));
+              y = y * (1.5 - 0.5 * x * y * y);
+              y = y * (1.5 - 0.5 * x * y * y);
+              c = T(y);
+              s = T(t * y);
+            }
           }
         }
         cs[2 * tid] = c;
