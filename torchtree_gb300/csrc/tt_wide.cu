@@ -75,6 +75,8 @@ struct WideState {
   bool tc_bwd = false;  // FP32 codon adjoint on the tensor cores (needs the stored products)
   float *d_pimg = nullptr;  // its GEMM2 operands: split P^T images [b][B][K][2][64][64]
   float *d_pimg_f = nullptr;  // the tensor-core post-order's B operands: split P images, same shape
+  // the images hold the current transition matrices (written right after them, in one pass)
+  bool img_f_valid = false, img_b_valid = false;
   // pattern slabs (p->slab != 0): the pattern-sized buffers below hold one
   // slab; tail_valid = they still hold the last slab's post-order (from a
   // tt_log_likelihood with keep_partials), which the gradient then reuses
@@ -149,6 +151,20 @@ bool encode_rows(CUtensorMap *m, const float *base, uint64_t rows, uint64_t cols
   return fn(m, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 2, const_cast<float *>(base), dims, strides, box, elem,
             CU_TENSOR_MAP_INTERLEAVE_NONE, swizzle, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
             CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS;
+}
+
+// Both split images of the FP32 codon transition matrices that the tensor-core
+// kernels use, from d_pmat in one pass (either may be skipped).
+cudaError_t launch_pimages(tt_plan *p, bool fwd, bool bwd, cudaStream_t s) {
+  WideState &w = *p->wide;
+  float *f = fwd ? w.d_pimg_f : nullptr, *b = bwd ? w.d_pimg : nullptr;
+  if (!f && !b) return cudaSuccess;
+  const long long count = (long long)p->batch * p->B * p->K;
+  wide_pimages_kernel<<<unsigned(count), 256, 0, s>>>(static_cast<const float *>(p->d_pmat), f, b);
+  p->launches += 1;
+  if (f) w.img_f_valid = true;
+  if (b) w.img_b_valid = true;
+  return cudaGetLastError();
 }
 
 int wcuda(cudaError_t e, const char *where) {
@@ -259,11 +275,9 @@ struct Wide {
     constexpr int NT = WideCfg<T, SP, PTF>::NT;
     const size_t smem = wide_fwd_smem<T, SP, PTF>();
     if constexpr (std::is_same<T, float>::value && SP == 64) {
-      if (w.tc && w.d_pimg_f) {  // the post-order's split P images, once per call
-        const long long count = (long long)p->batch * p->B * p->K;
-        wide_pimage_kernel<<<unsigned((count * 4096 + 255) / 256), 256, 0, s>>>(
-            static_cast<const float *>(p->d_pmat), w.d_pimg_f, count, 0);
-        p->launches += 1;
+      if (w.tc && w.d_pimg_f && !w.img_f_valid) {  // the post-order's split P images, if not written with P
+        const cudaError_t e = launch_pimages(p, true, false, s);
+        if (e != cudaSuccess) return e;
       }
     }
     for (size_t lv = 0; lv + 1 < w.fwd_off.size(); ++lv) {
@@ -323,10 +337,10 @@ struct Wide {
   // launch per depth level over chunks of 128-pattern tiles
   static cudaError_t backward_tc(tt_plan *p, WideArgs<float> a, const WideGeo &g, int accumulate, cudaStream_t s) {
     WideState &w = *p->wide;
-    const long long count = (long long)p->batch * p->B * p->K;
-    wide_pimage_kernel<<<unsigned((count * 4096 + 255) / 256), 256, 0, s>>>(static_cast<const float *>(p->d_pmat),
-                                                                         w.d_pimg, count, 1);
-    p->launches += 1;
+    if (!w.img_b_valid) {  // the split P^T images, if not written with P
+      const cudaError_t e = launch_pimages(p, false, true, s);
+      if (e != cudaSuccess) return e;
+    }
     const int ntc = g.Npad / tcb::kPT;
     const int want = (2 * 152 + p->batch * p->K - 1) / (p->batch * p->K);
     const int cmax = std::max(1, std::min({want, ntc, g.cmax}));
@@ -370,6 +384,12 @@ struct Wide {
     wide_pmatrix_kernel<T, SP><<<dim3(p->B, p->batch), 256, 3 * SP * SP * sizeof(T) + SP * sizeof(T), s>>>(
         lam, U, W, bl, rates, static_cast<T *>(p->d_pmat), p->S, p->B, p->K);
     p->launches += 1;
+    p->wide->img_f_valid = p->wide->img_b_valid = false;
+    if constexpr (std::is_same<T, float>::value && SP == 64) {  // the tensor-core kernels' images with P
+      const cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) return e;
+      return launch_pimages(p, p->wide->tc, p->wide->tc_bwd, s);
+    }
     return cudaGetLastError();
   }
 
@@ -591,6 +611,7 @@ int wide_set_tensor_cores(tt_plan *p, bool on) {
   if (on && !w->d_pimg_f) {  // the split P images: 32 KB per (sample, branch, category)
     const int rc = walloc(p, &w->d_pimg_f, bytes, "split transition-matrix images");
     if (rc) return rc;
+    w->img_f_valid = false;
   } else if (!on && w->d_pimg_f) {
     cudaFree(w->d_pimg_f);
     w->d_pimg_f = nullptr;
@@ -612,6 +633,7 @@ int wide_set_tensor_core_adjoint(tt_plan *p, bool on) {
     const size_t bytes = size_t(p->batch) * p->B * p->K * tcb::kImgFloats * sizeof(float);
     const int rc = walloc(p, &w->d_pimg, bytes, "split transition-matrix images");
     if (rc) return rc;
+    w->img_b_valid = false;
   } else if (!on && w->d_pimg) {
     cudaFree(w->d_pimg);
     w->d_pimg = nullptr;
@@ -675,7 +697,10 @@ int wide_set_matrices(tt_plan *p, const double *matrices, cudaStream_t s) {
     wide_pmatrix_copy_kernel<double><<<blocks, 256, 0, s>>>(matrices, static_cast<double *>(p->d_pmat), p->S, SP,
                                                             count);
   p->launches += 1;
+  p->wide->img_f_valid = p->wide->img_b_valid = false;
   cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && p->precision == TT_PRECISION_F32 && SP == 64)  // the tensor-core kernels' images
+    e = launch_pimages(p, p->wide->tc, p->wide->tc_bwd, s);
   return e == cudaSuccess ? TT_OK : wcuda(e, "transition-matrix copy launch");
 }
 

@@ -118,8 +118,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 }  // namespace tc
 
 // Post-order level kernel for FP32 codon plans on the tensor cores.
-// pimg: split P images (row i, K element j, big then small; wide_pimage_kernel
-// with transposed = 0), one 32 KB bulk copy per side; NULL stages P by the
+// pimg: split P images (row i, K element j, big then small; wide_pimages_kernel),
+// one 32 KB bulk copy per side; NULL stages P by the
 // threads.  The second side's child values are loaded into registers while
 // the first side's MMAs run.
 __global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const WideArgs<float> a, const float *pimg,

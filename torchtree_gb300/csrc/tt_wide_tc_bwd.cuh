@@ -41,7 +41,7 @@
 // order the roles; the converters meet at a named barrier only at epilogues
 // and tile ends.  GEMM2's B operand, P_c transposed into the operand layout
 // and split, is written once per (sample, branch, category) by
-// wide_pimage_kernel; a GEMM2 unit's 32-state slice of it travels in the
+// wide_pimages_kernel; a GEMM2 unit's 32-state slice of it travels in the
 // unit's raw slot (two 8 KB bulk copies) and the MMAs read it there.
 //
 // Tensor memory (cta_group::1, M = 128): row m is lane m, column n is column
@@ -91,24 +91,42 @@ constexpr int kImgFloats = 2 * 64 * 64;   // one P^T image: big then small
 
 // Split K-major images of the transition matrices, one per (sample, branch,
 // category), TF32 big then small (LBO = 1024 B between 4-element K groups):
-// transposed = 1 holds P^T (row j, K element i: the adjoint's GEMM2 B),
-// transposed = 0 holds P (row i, K element j: the post-order's B).  One
-// thread per output float (coalesced stores).
-__global__ void __launch_bounds__(256) wide_pimage_kernel(const float *pmat, float *img, long long count,
-                                                          int transposed) {
-  const long long t = (long long)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= count * 4096) return;
-  const long long m = t >> 12;
-  const int o = int(t & 4095);
-  // o (a float index) -> byte offset 4o = (kk >> 2) * 1024 + (row >> 3) * 128 + (row & 7) * 16 + (kk & 3) * 4
-  const int byte = 4 * o;
-  const int kk = (byte >> 10) * 4 + ((byte & 15) >> 2);
-  const int row = ((byte & 1023) >> 7) * 8 + ((byte & 127) >> 4);
-  const int i = transposed ? kk : row, j = transposed ? row : kk;
-  float big, small;
-  tc::split_tf32(pmat[m * 4096 + i * 64 + j], big, small);
-  img[m * tcb::kImgFloats + o] = big;
-  img[m * tcb::kImgFloats + 4096 + o] = small;
+// img_f holds P (row i, K element j: the post-order's B), img_b holds P^T
+// (row j, K element i: the adjoint's GEMM2 B); either may be NULL.  One CTA
+// per matrix: the matrix is read once, coalesced, into shared memory (rows
+// padded to 65 floats), then both images are written with coalesced stores.
+__global__ void __launch_bounds__(256) wide_pimages_kernel(const float *pmat, float *img_f, float *img_b) {
+  __shared__ float sp[64 * 65];
+  const long long m = blockIdx.x;
+  const float4 *src = reinterpret_cast<const float4 *>(pmat + m * 4096);
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int f = threadIdx.x + 256 * q, i = f >> 4, j = (f & 15) * 4;
+    const float4 v = __ldg(src + f);
+    sp[i * 65 + j] = v.x;
+    sp[i * 65 + j + 1] = v.y;
+    sp[i * 65 + j + 2] = v.z;
+    sp[i * 65 + j + 3] = v.w;
+  }
+  __syncthreads();
+#pragma unroll 4
+  for (int o = threadIdx.x; o < 4096; o += 256) {
+    // o (a float index) -> byte offset 4o = (kk >> 2) * 1024 + (row >> 3) * 128 + (row & 7) * 16 + (kk & 3) * 4
+    const int byte = 4 * o;
+    const int kk = (byte >> 10) * 4 + ((byte & 15) >> 2);
+    const int row = ((byte & 1023) >> 7) * 8 + ((byte & 127) >> 4);
+    float big, small;
+    if (img_f) {
+      tc::split_tf32(sp[row * 65 + kk], big, small);
+      img_f[m * tcb::kImgFloats + o] = big;
+      img_f[m * tcb::kImgFloats + 4096 + o] = small;
+    }
+    if (img_b) {
+      tc::split_tf32(sp[kk * 65 + row], big, small);
+      img_b[m * tcb::kImgFloats + o] = big;
+      img_b[m * tcb::kImgFloats + 4096 + o] = small;
+    }
+  }
 }
 
 __device__ __forceinline__ float4 ldg4(const float *p) { return __ldg(reinterpret_cast<const float4 *>(p)); }
