@@ -229,7 +229,7 @@ __device__ void load_symmetrised(const double *q, const double *pi, int b, int n
 }
 
 // Step 1, one CTA per matrix: FP32 Jacobi sweeps on A until the off-diagonal
-// norm is below 1e-6 of the Frobenius norm (at most 10 sweeps: FP32 rounding
+// norm is below 1e-6 of the Frobenius norm (at most 6 sweeps: FP32 rounding
 // may stop short of that); the eigenvector matrix X0, in FP64, into x.
 __global__ void __launch_bounds__(kEigThreads) eigen_start_kernel(const double *q, const double *pi, int n,
                                                                   double *x) {
@@ -243,7 +243,7 @@ __global__ void __launch_bounds__(kEigThreads) eigen_start_kernel(const double *
   for (int i = warp; i < n; i += NW)
     for (int j = lane; j < n; j += 32) V[i * kEigLd + j] = i == j ? 1.0f : 0.0f;
   __syncthreads();
-  jacobi_sweeps<float>(A, V, cs, pq, red, &flag, n, 1e-12, 10);
+  jacobi_sweeps<float>(A, V, cs, pq, red, &flag, n, 1e-12, 6);
   double *xb = x + size_t(b) * n * n;
   for (int i = warp; i < n; i += NW)
     for (int j = lane; j < n; j += 32) xb[i * n + j] = double(V[i * kEigLd + j]);
