@@ -658,14 +658,25 @@ def main():
     zeros = torch.zeros(b, 1, dtype=torch.float64, device=dev)
     bls = torch.cat([bl, zeros], -1).contiguous()
 
+    side = torch.cuda.Stream(device=dev)
+
     def model_setup():
         """The per-step model work on the device: Gamma category rates
-        (quantile kernel), the normalised rate matrix (a few torch ops) and
-        its FP64 eigen system (device eigensolver)."""
-        r, p = site_models.gamma_rates(shape, K)
+        (quantile kernel, on a side stream: it and the eigensolver are
+        independent and each fills only a few SMs), the normalised rate
+        matrix (a few torch ops) and its FP64 eigen system (device
+        eigensolver)."""
+        main = torch.cuda.current_stream()
+        side.wait_stream(main)
+        with torch.cuda.stream(side):
+            r, p = site_models.gamma_rates(shape, K)
+            r, p = r.contiguous(), p.expand(b, K).contiguous()
         qn = substitution.normalise(rate_matrix(wl.model, exch, pi), pi)
         lam_, u_, w_ = substitution.device_eigen(qn, pi)
-        return lam_, u_, w_, r.contiguous(), p.expand(b, K).contiguous()
+        main.wait_stream(side)
+        r.record_stream(main)
+        p.record_stream(main)
+        return lam_, u_, w_, r, p
 
     lam, u, w, rates, probs = model_setup()
 
