@@ -29,6 +29,8 @@
 // R's diagonal between the steps, so the call needs no workspace.
 #include <math.h>
 
+#include <cooperative_groups.h>
+
 #include <algorithm>
 #include <string>
 
@@ -60,6 +62,29 @@ __device__ __forceinline__ void rr_pair(int r, int i, int m, int &p, int &q) {
     p = q;
     q = t;
   }
+}
+
+// The Jacobi rotation (c, s) that zeroes a_pq of [[a_pp, a_pq], [a_pq, a_qq]]
+// in FP64.  FP64 division and square root are long dependency chains on this
+// GPU, and every round waits for its rotations: the angle to FP32 accuracy (a
+// slightly inexact angle leaves a residual the next sweep removes), then
+// c = (1 + t^2)^-1/2 from an FP32 seed by two Newton steps y <- y (3 - x y^2) / 2
+// in FP64, so that c^2 + s^2 = 1 to FP64 rounding and the rotation stays
+// orthogonal.  a_pq != 0.
+__device__ __forceinline__ void jacobi_rotation_f64(double app, double aqq, double apq, double &c, double &s) {
+  c = 1.0;
+  s = 0.0;
+  if (apq == 0.0) return;
+  const float tf = float(aqq - app) / float(2.0 * apq);
+  float t32;
+  if (!(fabsf(tf) <= 1e18f)) t32 = 0.5f / tf;
+  else t32 = (tf >= 0.0f ? 1.0f : -1.0f) / (fabsf(tf) + sqrtf(1.0f + tf * tf));
+  const double t = double(t32), x = 1.0 + t * t;
+  double y = double(rsqrtf(float(x)));
+  y = y * (1.5 - 0.5 * x * y * y);
+  y = y * (1.5 - 0.5 * x * y * y);
+  c = y;
+  s = t * y;
 }
 
 // Cyclic Jacobi sweeps on A (n x n, leading dimension kEigLd) accumulating
@@ -120,21 +145,10 @@ __device__ bool jacobi_sweeps(T *A, T *V, T *cs, int *pq, double *red, int *flag
               c = T(1) / sqrt(T(1) + t * t);
               s = t * c;
             } else {
-              // FP64 division and square root are long dependency chains on this GPU, and
-              // every round waits for its rotations: the angle to FP32 accuracy (a slightly
-              // inexact angle leaves a residual the next sweep removes), then c = (1 + t^2)^-1/2
-              // from an FP32 seed by two Newton steps y <- y (3 - x y^2) / 2 in FP64, so that
-              // c^2 + s^2 = 1 to FP64 rounding and the rotation stays orthogonal
-              const float tf = float(A[qq * kEigLd + qq] - A[p * kEigLd + p]) / float(2.0 * apq);
-              float t32;
-              if (!(fabsf(tf) <= 1e18f)) t32 = 0.5f / tf;
-              else t32 = (tf >= 0.0f ? 1.0f : -1.0f) / (fabsf(tf) + sqrtf(1.0f + tf * tf));
-              const double t = double(t32), x = 1.0 + t * t;
-              double y = double(rsqrtf(float(x)));
-              y = y * (1.5 - 0.5 * x * y * y);
-              y = y * (1.5 - 0.5 * x * y * y);
-              c = T(y);
-              s = T(t * y);
+              double cd, sd;
+              jacobi_rotation_f64(A[p * kEigLd + p], A[qq * kEigLd + qq], apq, cd, sd);
+              c = T(cd);
+              s = T(sd);
             }
           }
         }
@@ -374,6 +388,154 @@ __global__ void __launch_bounds__(kEigThreads) eigen_finish_kernel(const double 
   }
 }
 
+// Step 3 for matrices of more than 32 states: the same FP64 Jacobi sweeps on
+// a cluster of kEigCluster CTAs per matrix (FP64 arithmetic on one SM bounds
+// the single-CTA sweeps).  Every CTA keeps a copy of A; each round, all CTAs
+// form the same rotations from their identical copies, a CTA updates the rows
+// p, q of its share of the pairs (pairs i = rank mod kEigCluster) and writes
+// them into every copy through distributed shared memory, then, after a
+// cluster barrier, updates columns p, q of its share of the rows (rows = rank
+// mod kEigCluster) in every copy of A and in its own rows of V.  The
+// convergence test runs on each CTA's (identical) copy, so every CTA leaves
+// the sweeps together.  Each CTA writes its rows of U and W.
+constexpr int kEigCluster = 4;
+
+__global__ void __cluster_dims__(kEigCluster, 1, 1) __launch_bounds__(kEigThreads)
+    eigen_finish_cluster_kernel(const double *pi, int n, double *lam, double *U, double *W, int *status) {
+  namespace cg = cooperative_groups;
+  constexpr int NW = kEigThreads / 32, C = kEigCluster;
+  extern __shared__ __align__(16) double csm[];
+  double *A = csm;                       // [n][kEigLd] S, symmetric (a copy per CTA)
+  double *V = A + kEigMax * kEigLd;      // [n][kEigLd] X (rows = rank mod C are this CTA's)
+  double *cs = V + kEigMax * kEigLd;     // [kEigMax/2][2]
+  double *red = cs + kEigMax;            // [2 * NW]
+  double *sq = red + 2 * NW;             // [n]
+  int *pq = reinterpret_cast<int *>(sq + kEigMax);  // [kEigMax/2][2]
+  __shared__ int flag;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int rank = int(cluster.block_rank());
+  const int b = blockIdx.x / C, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  double *Ac[C];
+#pragma unroll
+  for (int q = 0; q < C; ++q) Ac[q] = cluster.map_shared_rank(A, q);
+  const size_t mo = size_t(b) * n * n;
+  for (int i = tid; i < n; i += kEigThreads) sq[i] = sqrt(pi[size_t(b) * n + i]);
+  for (int i = warp; i < n; i += NW)
+    for (int j = lane; j < n; j += 32) {
+      A[i * kEigLd + j] = W[mo + size_t(min(i, j)) * n + max(i, j)];
+      if (i % C == rank) V[i * kEigLd + j] = U[mo + size_t(i) * n + j];
+    }
+  cluster.sync();  // every CTA has read U and W before any writes its outputs
+  const int m = n + (n & 1), npairs = m / 2;
+  bool ok = false;
+  for (int sweep = 0; sweep <= 30; ++sweep) {
+    double off = 0.0, tot = 0.0;
+    for (int i = warp; i < n; i += NW)
+      for (int j = lane; j < n; j += 32) {
+        const double v = A[i * kEigLd + j];
+        tot += v * v;
+        if (i != j) off += v * v;
+      }
+    for (int o = 16; o; o >>= 1) {
+      off += __shfl_xor_sync(0xffffffffu, off, o);
+      tot += __shfl_xor_sync(0xffffffffu, tot, o);
+    }
+    if (lane == 0) {
+      red[warp] = off;
+      red[NW + warp] = tot;
+    }
+    __syncthreads();
+    if (tid == 0) {
+      double so = 0.0, st = 0.0;
+      for (int w = 0; w < NW; ++w) {
+        so += red[w];
+        st += red[NW + w];
+      }
+      flag = !(so > 1e-28 * st) || n == 1;
+    }
+    __syncthreads();
+    if (flag) {
+      ok = true;
+      break;
+    }
+    if (sweep == 30) break;
+    for (int r = 0; r < m - 1; ++r) {
+      if (tid < npairs) {  // the round's rotations, the same in every CTA
+        int p, qq;
+        rr_pair(r, tid, m, p, qq);
+        double c = 1.0, sn = 0.0;
+        if (qq < n) jacobi_rotation_f64(A[p * kEigLd + p], A[qq * kEigLd + qq], A[p * kEigLd + qq], c, sn);
+        cs[2 * tid] = c;
+        cs[2 * tid + 1] = sn;
+        pq[2 * tid] = p;
+        pq[2 * tid + 1] = qq;
+      }
+      __syncthreads();
+      // rows p, q of this CTA's pairs (a warp per pair), into every copy
+      for (int i = rank + C * warp; i < npairs; i += C * NW) {
+        const int p = pq[2 * i], qq = pq[2 * i + 1];
+        const double c = cs[2 * i], sn = cs[2 * i + 1];
+        if (qq >= n || sn == 0.0) continue;
+        double np_[2], nq_[2];
+#pragma unroll
+        for (int h = 0; h < 2; ++h) {
+          const int j = lane + 32 * h;
+          const double ap = j < n ? A[p * kEigLd + j] : 0.0, aq = j < n ? A[qq * kEigLd + j] : 0.0;
+          np_[h] = c * ap - sn * aq;
+          nq_[h] = sn * ap + c * aq;
+        }
+#pragma unroll
+        for (int q = 0; q < C; ++q)
+#pragma unroll
+          for (int h = 0; h < 2; ++h) {
+            const int j = lane + 32 * h;
+            if (j < n) {
+              Ac[q][p * kEigLd + j] = np_[h];
+              Ac[q][qq * kEigLd + j] = nq_[h];
+            }
+          }
+      }
+      cluster.sync();
+      // columns p, q of this CTA's rows (a warp per row, lanes over the pairs), into every copy of
+      // A and this CTA's rows of V
+      for (int row = rank + C * warp; row < n; row += C * NW) {
+        const int i = lane;
+        if (i >= npairs) continue;
+        const int p = pq[2 * i], qq = pq[2 * i + 1];
+        const double c = cs[2 * i], sn = cs[2 * i + 1];
+        if (qq >= n || sn == 0.0) continue;
+        const double ap = A[row * kEigLd + p], aq = A[row * kEigLd + qq];
+        const double np_ = c * ap - sn * aq, nq_ = sn * ap + c * aq;
+#pragma unroll
+        for (int q = 0; q < C; ++q) {
+          Ac[q][row * kEigLd + p] = np_;
+          Ac[q][row * kEigLd + qq] = nq_;
+        }
+        const double vp = V[row * kEigLd + p], vq = V[row * kEigLd + qq];
+        V[row * kEigLd + p] = c * vp - sn * vq;
+        V[row * kEigLd + qq] = sn * vp + c * vq;
+      }
+      cluster.sync();
+    }
+  }
+  if (tid == 0 && rank == 0 && !ok) atomicExch(status, TT_ERR_UNSUPPORTED);
+  // ascending order: the rank of each eigenvalue (ties by index); this CTA's rows of U and W
+  for (int k = tid; k < n; k += kEigThreads) {
+    const double lk = A[k * kEigLd + k];
+    int rk = 0;
+    for (int j = 0; j < n; ++j) {
+      const double lj = A[j * kEigLd + j];
+      rk += lj < lk || (lj == lk && j < k);
+    }
+    if (rank == 0) lam[size_t(b) * n + rk] = lk;
+    for (int i = rank; i < n; i += C) {
+      U[(size_t(b) * n + i) * n + rk] = V[i * kEigLd + k] / sq[i];  // U = Pi^-1/2 V
+      W[(size_t(b) * n + rk) * n + i] = V[i * kEigLd + k] * sq[i];  // W = V^T Pi^1/2
+    }
+  }
+  cluster.sync();  // no CTA leaves while another may still write into its shared memory
+}
+
 __global__ void gamma_quantiles_kernel(const double *shape, int batch, int K, double *x, double *dxda) {
   const int e = blockIdx.x * blockDim.x + threadIdx.x;
   if (e >= batch * K) return;
@@ -410,6 +572,7 @@ int tt_reversible_eigen(int32_t batch, int32_t state_count, const double *q, con
   cudaError_t e = kernel_smem(eigen_gram_kernel, gram_smem);
   if (e == cudaSuccess) e = kernel_smem(eigen_orth_kernel, orth_smem);
   if (e == cudaSuccess) e = kernel_smem(eigen_finish_kernel, finish_smem);
+  if (e == cudaSuccess) e = kernel_smem(eigen_finish_cluster_kernel, finish_smem);
   // matrices in groups of at most 65,535 (the grid's y extent of the row-block kernels)
   for (int b0 = 0; e == cudaSuccess && b0 < batch; b0 += 65535) {
     const int nb = std::min(batch - b0, 65535);
@@ -423,7 +586,10 @@ int tt_reversible_eigen(int32_t batch, int32_t state_count, const double *q, con
       eigen_orth_kernel<<<rows_grid, kEigThreads, orth_smem, s>>>(n, ub, wb, lb);
     }
     eigen_gram_kernel<<<rows_grid, kEigThreads, gram_smem, s>>>(qb, pib, n, ub, wb, lb, 1);
-    eigen_finish_kernel<<<nb, kEigThreads, finish_smem, s>>>(pib, n, lb, ub, wb, status);
+    if (n > 32)  // FP64 sweeps on a cluster of CTAs per matrix
+      eigen_finish_cluster_kernel<<<nb * kEigCluster, kEigThreads, finish_smem, s>>>(pib, n, lb, ub, wb, status);
+    else
+      eigen_finish_kernel<<<nb, kEigThreads, finish_smem, s>>>(pib, n, lb, ub, wb, status);
     e = cudaGetLastError();
   }
   return e == cudaSuccess ? TT_OK : tt::efail(TT_ERR_CUDA, std::string("eigen launch: ") + cudaGetErrorString(e));
