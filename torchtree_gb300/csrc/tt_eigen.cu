@@ -600,7 +600,8 @@ int tt_gamma_quantiles(int32_t batch, int32_t category_count, const double *shap
   if (!shape || !x || !dx_dshape) return tt::efail(TT_ERR_INVALID_ARGUMENT, "NULL argument");
   if (batch < 1 || category_count < 1) return tt::efail(TT_ERR_INVALID_ARGUMENT, "batch and categories must be >= 1");
   const int n = batch * category_count;
-  tt::gamma_quantiles_kernel<<<(n + 127) / 128, 128, 0, static_cast<cudaStream_t>(stream)>>>(
+  // one warp per CTA: the quantiles' FP64 work spreads over as many SMs as warps
+  tt::gamma_quantiles_kernel<<<(n + 31) / 32, 32, 0, static_cast<cudaStream_t>(stream)>>>(
       shape, batch, category_count, x, dx_dshape);
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? TT_OK

@@ -59,63 +59,83 @@ __device__ __forceinline__ float frechet_e(float am, float an, float em, float e
 
 }  // namespace
 
-// 4 states, FP64: one CTA per (chunk of 128 branches, sample), one branch per
-// thread; X and the rate sums reduced in a fixed order through shared memory.
+// 4 states: one CTA per (chunk of 128 branches, sample), one branch per
+// thread, products in T (the plan's precision: FP64 arithmetic is scarce on
+// this GPU), sums over a thread's branches in T and across the CTA in FP64;
+// X and the rate sums reduced in a fixed order through shared memory.
+template <typename T>
 __global__ void __launch_bounds__(128) qgrad_small_kernel(const double *G, const double *lam, const double *U,
                                                           const double *W, const double *bl, const double *rates,
                                                           int B, int K, double *part, double *dbl) {
   constexpr int S = 4;
   __shared__ double red[128][S * S + 8];
   const int chunk = blockIdx.x, b = blockIdx.y, tid = threadIdx.x;
-  double u[S][S], w[S][S], l[S];
+  T u[S][S], w[S][S], l[S];
 #pragma unroll
   for (int i = 0; i < S; ++i) {
-    l[i] = lam[b * S + i];
+    l[i] = T(lam[b * S + i]);
 #pragma unroll
     for (int j = 0; j < S; ++j) {
-      u[i][j] = U[(size_t(b) * S + i) * S + j];
-      w[i][j] = W[(size_t(b) * S + i) * S + j];
+      u[i][j] = T(U[(size_t(b) * S + i) * S + j]);
+      w[i][j] = T(W[(size_t(b) * S + i) * S + j]);
     }
   }
-  double X[S][S], dr[8];
+  T X[S][S];
+  double dr[8];
 #pragma unroll
   for (int i = 0; i < S; ++i)
 #pragma unroll
-    for (int j = 0; j < S; ++j) X[i][j] = 0.0;
+    for (int j = 0; j < S; ++j) X[i][j] = T(0);
 #pragma unroll
   for (int k = 0; k < 8; ++k) dr[k] = 0.0;
   for (int br = chunk * 128 + tid; br < min(B, chunk * 128 + 128); br += 128) {
     const double t = bl[size_t(b) * B + br];
     double dt = 0.0;
     for (int k = 0; k < K; ++k) {
-      const double tau = t * rates[b * K + k];
+      const T tau = T(t * rates[b * K + k]);
       const double *g = G + ((size_t(b) * B + br) * K + k) * S * S;
-      double h[S][S], M[S][S];
+      T h[S][S], M[S][S];
 #pragma unroll
       for (int i = 0; i < S; ++i)
 #pragma unroll
         for (int n = 0; n < S; ++n) {
-          double acc = 0.0;
+          T acc = T(0);
 #pragma unroll
-          for (int j = 0; j < S; ++j) acc = fma(g[i * S + j], w[n][j], acc);
+          for (int j = 0; j < S; ++j) acc = fma(T(g[i * S + j]), w[n][j], acc);
           h[i][n] = acc;
         }
 #pragma unroll
       for (int m = 0; m < S; ++m)
 #pragma unroll
         for (int n = 0; n < S; ++n) {
-          double acc = 0.0;
+          T acc = T(0);
 #pragma unroll
           for (int i = 0; i < S; ++i) acc = fma(u[i][m], h[i][n], acc);
           M[m][n] = acc;
         }
-      double s = 0.0;
+      T sk = T(0);
+      if constexpr (sizeof(T) == 4) {  // the states' exponentials once, the divided differences from them
+        T lt[S], es[S];
 #pragma unroll
-      for (int m = 0; m < S; ++m) {
-        s = fma(l[m] * exp(l[m] * tau), M[m][m], s);
+        for (int m = 0; m < S; ++m) {
+          lt[m] = l[m] * tau;
+          es[m] = exp_t(lt[m]);
+        }
 #pragma unroll
-        for (int n = 0; n < S; ++n) X[m][n] = fma(frechet(l[m], l[n], tau), M[m][n], X[m][n]);
+        for (int m = 0; m < S; ++m) {
+          sk = fma(l[m] * es[m], M[m][m], sk);
+#pragma unroll
+          for (int n = 0; n < S; ++n) X[m][n] = fma(frechet_e(lt[m], lt[n], es[m], es[n], tau), M[m][n], X[m][n]);
+        }
+      } else {
+#pragma unroll
+        for (int m = 0; m < S; ++m) {
+          sk = fma(l[m] * exp_t(l[m] * tau), M[m][m], sk);
+#pragma unroll
+          for (int n = 0; n < S; ++n) X[m][n] = fma(frechet(l[m], l[n], tau), M[m][n], X[m][n]);
+        }
       }
+      const double s = double(sk);
       dt = fma(s, rates[b * K + k], dt);
       if (k < 8) dr[k] = fma(s, t, dr[k]);
     }
@@ -124,7 +144,7 @@ __global__ void __launch_bounds__(128) qgrad_small_kernel(const double *G, const
 #pragma unroll
   for (int i = 0; i < S; ++i)
 #pragma unroll
-    for (int j = 0; j < S; ++j) red[tid][i * S + j] = X[i][j];
+    for (int j = 0; j < S; ++j) red[tid][i * S + j] = double(X[i][j]);
 #pragma unroll
   for (int k = 0; k < 8; ++k) red[tid][S * S + k] = dr[k];
   __syncthreads();
@@ -365,8 +385,12 @@ int rate_matrix_gradient(tt_plan *p, const double *lam, const double *U, const d
   }
   if (S == 4) {
     nchunks = (p->B + 127) / 128;
-    qgrad_small_kernel<<<dim3(nchunks, p->batch), 128, 0, s>>>(p->d_G, lam, U, W, bl, rates, p->B, K, p->d_qpart,
-                                                               dbl);
+    if (p->precision == TT_PRECISION_F32)
+      qgrad_small_kernel<float><<<dim3(nchunks, p->batch), 128, 0, s>>>(p->d_G, lam, U, W, bl, rates, p->B, K,
+                                                                        p->d_qpart, dbl);
+    else
+      qgrad_small_kernel<double><<<dim3(nchunks, p->batch), 128, 0, s>>>(p->d_G, lam, U, W, bl, rates, p->B, K,
+                                                                         p->d_qpart, dbl);
     e = cudaGetLastError();
   } else {
     const int bchunk = 8;
