@@ -318,14 +318,21 @@ struct Wide {
     }
     constexpr int NT = WideCfg<T, SP, PTB>::NT;
     const size_t smem = wide_bwd_smem<T, SP, PTB>(a.prod != nullptr);
+    // FP32 20-state plans: a chunk count per level (three CTAs per SM), as the tensor-core adjoint does
+    constexpr bool per_level = std::is_same<T, float>::value && SP == 20;
+    const int bk = p->batch * p->K, target = 8 * 152 * 3;
     for (size_t lv = 0; lv + 1 < w.bwd_off.size(); ++lv) {
+      const int nodes = w.bwd_off[lv + 1] - w.bwd_off[lv];
+      const int chunks = per_level ? tc_level_chunks(nodes, bk, g.ntiles_b, g.cmax, target) : g.nchunks;
       a.nodes = w.d_bwd + w.bwd_off[lv];
-      const dim3 grid(g.nchunks, w.bwd_off[lv + 1] - w.bwd_off[lv], p->batch * p->K);
+      a.tiles_per_chunk = per_level ? (g.ntiles_b + chunks - 1) / chunks : g.tpc;
+      const dim3 grid(chunks, nodes, bk);
       wide_backward_kernel<T, SP, PTB><<<grid, NT, smem, s>>>(a);
       p->launches += 1;
     }
-    wide_grad_reduce_kernel<T><<<dim3(p->B, p->batch), 256, 0, s>>>(static_cast<const T *>(w.d_gpart), p->d_G,
-                                                                     p->B, g.nchunks, p->K, p->S, SP, accumulate);
+    wide_grad_reduce_kernel<T><<<dim3(p->B, p->batch), 256, 0, s>>>(
+        static_cast<const T *>(w.d_gpart), p->d_G, p->B, g.nchunks, p->K, p->S, SP, accumulate,
+        per_level ? w.d_branch_lvn : nullptr, bk, g.ntiles_b, g.cmax, target);
     wide_root_reduce_kernel<T><<<p->batch, 64, 0, s>>>(static_cast<const T *>(w.d_rootpart), p->d_rootgrad,
                                                        p->d_rootgrad + size_t(p->batch) * p->S, g.nchunks, p->K,
                                                        p->S, SP, accumulate);

@@ -620,13 +620,13 @@ __global__ void __launch_bounds__(WideCfg<T, SP, PT>::NT, wide_bwd_min_blocks<T,
   }
 }
 
-// Chunks of 128-pattern tiles of one level launch of the tensor-core codon
-// adjoint: enough CTAs for about eight waves of one CTA per SM over the
-// level's nodes x samples x categories (bk), at most cmax chunks of the ntc
-// tiles.  Levels with many nodes get one or two long chunks: fewer CTAs,
-// so less per-CTA set-up and fewer gradient blocks to write and sum.
-__host__ __device__ inline int tc_level_chunks(int nodes, int bk, int ntc, int cmax) {
-  const long long want = (8LL * 152 + (long long)nodes * bk - 1) / ((long long)nodes * bk);
+// Chunks of pattern tiles of one level launch of a wide-state adjoint: about
+// target CTAs (eight waves at the kernel's CTAs per SM) over the level's
+// nodes x samples x categories (bk), at most cmax chunks of the ntc tiles.
+// Levels with many nodes get few long chunks: fewer CTAs, so less per-CTA
+// set-up and fewer gradient blocks to write and sum.
+__host__ __device__ inline int tc_level_chunks(int nodes, int bk, int ntc, int cmax, int target = 8 * 152) {
+  const long long want = ((long long)target + (long long)nodes * bk - 1) / ((long long)nodes * bk);
   const int c = int(want < 1 ? 1 : (want > cmax ? cmax : want));
   const int tpc = (ntc + c - 1) / c;
   return (ntc + tpc - 1) / tpc;
@@ -641,7 +641,7 @@ __host__ __device__ inline int tc_level_chunks(int nodes, int bk, int ntc, int c
 template <typename T>
 __global__ void wide_grad_reduce_kernel(const T *gpart, double *G, int B, int nchunks, int K, int S, int SP,
                                         int accumulate, const int *branch_lvn = nullptr, int bk = 0, int ntc = 0,
-                                        int cmax = 0) {
+                                        int cmax = 0, int target = 8 * 152) {
   // four consecutive columns per thread, threads along the row: 16-byte (FP32) or 2 x 16-byte
   // (FP64) loads of every chunk's block, the chunk sum in the plan's precision and a fixed
   // order, then FP64 (FP64 arithmetic is scarce on this GPU and the chunk blocks themselves are
@@ -650,7 +650,7 @@ __global__ void wide_grad_reduce_kernel(const T *gpart, double *G, int B, int nc
   const int kss = K * S * S, q4 = SP / 4;
   const size_t cstride = size_t(K) * SP * SP;  // between chunks
   const T *base = gpart + (size_t(b) * B + br) * nchunks * cstride;
-  const int used = branch_lvn ? tc_level_chunks(branch_lvn[br], bk, ntc, cmax) : nchunks;
+  const int used = branch_lvn ? tc_level_chunks(branch_lvn[br], bk, ntc, cmax, target) : nchunks;
   double *gb = G + (size_t(b) * B + br) * kss;
   for (int e = threadIdx.x; e < K * S * q4; e += blockDim.x) {
     const int kr = e / q4, j0 = (e - kr * q4) * 4;
