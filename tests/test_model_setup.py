@@ -83,7 +83,7 @@ def _random_reversible(rng, b, S):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("S", [2, 3, 4, 5, 20, 61, 64])
+@pytest.mark.parametrize("S", [2, 3, 4, 5, 20, 32, 33, 47, 61, 64])
 def test_device_eigen_system_matches_lapack(S):
     if not torch.cuda.is_available():
         pytest.skip("no CUDA device")
