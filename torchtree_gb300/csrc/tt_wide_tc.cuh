@@ -121,7 +121,8 @@ __device__ __forceinline__ void tmem_ld32(uint32_t taddr, float (&v)[32]) {
 // pimg: split P images (row i, K element j, big then small; wide_pimages_kernel),
 // one 32 KB bulk copy per side; NULL stages P by the
 // threads.  The second side's child values are loaded into registers while
-// the first side's MMAs run.
+// the first side's MMAs run.  A CTA walks a.tiles_per_chunk tiles of one
+// (node, sample, category), reusing its TMEM and barriers.
 __global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const WideArgs<float> a, const float *pimg,
                                                                          int *status, unsigned long long timeout_ns) {
   constexpr int SP = 64;
@@ -134,7 +135,9 @@ __global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const 
   const int tid = threadIdx.x, warp = tid >> 5;
   const int v = a.nodes[blockIdx.y];
   const int b = blockIdx.z / a.K, k = blockIdx.z - (blockIdx.z / a.K) * a.K;
-  const int n0 = blockIdx.x * tc::kPT;
+  // this CTA's 128-pattern tiles [t0, t1): TMEM, barriers and set-up paid once for them
+  const int t0 = blockIdx.x * a.tiles_per_chunk, t1 = min(a.ntiles, t0 + a.tiles_per_chunk);
+  int n0 = t0 * tc::kPT;
   const int l = a.left[v - a.tips], r = a.right[v - a.tips];
   const bool is_root = v == 2 * a.tips - 2;
 
@@ -169,140 +172,145 @@ __global__ void __launch_bounds__(tc::kThreads, 2) wide_forward_tc_kernel(const 
       for (int j = 0; j < SP; ++j) xv[j] = __ldg(src + size_t(j) * a.Npad);
     }
   };
-  load_x(l);
-  for (int c = 0; c < 2 && ok; ++c) {
-    const int child = c ? r : l;
-    // B operand: P_c[i][j], N = i, K = j: the split image in one bulk copy, or
-    // eight 16-byte loads per thread in flight before the split
-    if (pimg) {
-      if (tid == 0) {
-        b_pending = true;
-        mbar_arrive_expect_tx(bar_b, uint32_t(2 * tc::kBbytes));
-        bulk_copy_g2s(sB, pimg + ((size_t(b) * a.B + child) * a.K + k) * 2 * SP * SP, uint32_t(2 * tc::kBbytes), bar_b);
-      }
-    } else {
-      float4 pv[8];
+  for (int tile = t0; tile < t1 && ok; ++tile) {
+    n0 = tile * tc::kPT;
+    load_x(l);
+    for (int c = 0; c < 2 && ok; ++c) {
+      const int child = c ? r : l;
+      // B operand: P_c[i][j], N = i, K = j: the split image in one bulk copy, or
+      // eight 16-byte loads per thread in flight before the split
+      if (pimg) {
+        if (tid == 0) {
+          b_pending = true;
+          mbar_arrive_expect_tx(bar_b, uint32_t(2 * tc::kBbytes));
+          bulk_copy_g2s(sB, pimg + ((size_t(b) * a.B + child) * a.K + k) * 2 * SP * SP, uint32_t(2 * tc::kBbytes),
+                        bar_b);
+        }
+      } else {
+        float4 pv[8];
 #pragma unroll
-      for (int m = 0; m < 8; ++m) {
-        const int f = (tid + m * tc::kThreads) * 4, i = f / SP;
-        pv[m] = __ldg(reinterpret_cast<const float4 *>(
-            a.pmat + ((size_t(b) * a.B + child) * a.K + k) * SP * SP + (f - i * SP) + i * SP));
-      }
+        for (int m = 0; m < 8; ++m) {
+          const int f = (tid + m * tc::kThreads) * 4, i = f / SP;
+          pv[m] = __ldg(reinterpret_cast<const float4 *>(
+              a.pmat + ((size_t(b) * a.B + child) * a.K + k) * SP * SP + (f - i * SP) + i * SP));
+        }
 #pragma unroll
-      for (int m = 0; m < 8; ++m) {
-        const int f = (tid + m * tc::kThreads) * 4, i = f / SP, j = f - i * SP;
-        float4 hb, hs;
-        tc::split_tf32(pv[m].x, hb.x, hs.x);
-        tc::split_tf32(pv[m].y, hb.y, hs.y);
-        tc::split_tf32(pv[m].z, hb.z, hs.z);
-        tc::split_tf32(pv[m].w, hb.w, hs.w);
-        const uint32_t off = tc::kmajor_off(i, j, 1024);
-        *reinterpret_cast<float4 *>(sB + off) = hb;
-        *reinterpret_cast<float4 *>(sB + tc::kBbytes + off) = hs;
+        for (int m = 0; m < 8; ++m) {
+          const int f = (tid + m * tc::kThreads) * 4, i = f / SP, j = f - i * SP;
+          float4 hb, hs;
+          tc::split_tf32(pv[m].x, hb.x, hs.x);
+          tc::split_tf32(pv[m].y, hb.y, hs.y);
+          tc::split_tf32(pv[m].z, hb.z, hs.z);
+          tc::split_tf32(pv[m].w, hb.w, hs.w);
+          const uint32_t off = tc::kmajor_off(i, j, 1024);
+          *reinterpret_cast<float4 *>(sB + off) = hb;
+          *reinterpret_cast<float4 *>(sB + tc::kBbytes + off) = hs;
+        }
+      }
+      // A operand: the side's loaded values split, four j per 16-byte store
+      {
+#pragma unroll
+        for (int j = 0; j < SP; j += 4) {
+          float4 hb, hs;
+          tc::split_tf32(xv[j], hb.x, hs.x);
+          tc::split_tf32(xv[j + 1], hb.y, hs.y);
+          tc::split_tf32(xv[j + 2], hb.z, hs.z);
+          tc::split_tf32(xv[j + 3], hb.w, hs.w);
+          const uint32_t off = tc::kmajor_off(tid, j, 2048);
+          *reinterpret_cast<float4 *>(sA + off) = hb;
+          *reinterpret_cast<float4 *>(sA + tc::kAbytes + off) = hs;
+        }
+      }
+      // generic-proxy writes -> visible to the tensor cores (async proxy)
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      tc::fence_before_sync();
+      __syncthreads();
+      tc::fence_after_sync();
+      tmem = *tslot;
+      if (tid == 0 && b_pending) {  // the image has landed
+        if (mbar_wait_bounded(bar_b, phase_b, timeout_ns)) {
+          b_pending = false;
+          phase_b ^= 1;
+        }
+      }
+      if (tid == 0 && !b_pending) {
+        constexpr uint32_t idesc = tc::idesc_tf32(128, 64);
+        const uint32_t d = tmem + uint32_t(64 * c);
+        const uint32_t ab = smem_u32(sA), as = ab + tc::kAbytes;
+        const uint32_t bb = smem_u32(sB), bs = bb + tc::kBbytes;
+#pragma unroll
+        for (int kk = 0; kk < SP / 8; ++kk) {
+          const uint64_t dab = tc::smem_desc(ab + kk * 4096, 2048, 128), das = tc::smem_desc(as + kk * 4096, 2048, 128);
+          const uint64_t dbb = tc::smem_desc(bb + kk * 2048, 1024, 128), dbs = tc::smem_desc(bs + kk * 2048, 1024, 128);
+          tc::mma_tf32(d, dab, dbb, idesc, kk > 0 ? 1u : 0u);
+          tc::mma_tf32(d, dab, dbs, idesc, 1u);
+          tc::mma_tf32(d, das, dbb, idesc, 1u);
+        }
+        tc::mma_commit(bar);
+      } else if (tid == 0) {
+        mbar_arrive(bar);  // no MMAs (the image never landed): complete the phase; the side fails below
+      }
+      if (c == 0) load_x(r);  // while the MMAs run: the other side's values into registers
+      // every thread sees the side's MMAs complete before the shared memory is restaged or TMEM read
+      ok = mbar_wait_bounded(bar, phase, timeout_ns) && !(tid == 0 && b_pending);
+      tc::fence_after_sync();
+      ok = !__syncthreads_or(!ok);
+      if (ok) phase ^= 1;
+    }
+    if (ok) {
+      // this thread's pattern = TMEM lane 32 * warp + lane
+      const uint32_t lane_addr = tmem + (uint32_t(32 * warp) << 16);
+      const int n = n0 + tid;
+      float *pd = a.prod ? a.prod + ((size_t(b) * a.I + (v - a.tips)) * a.K + k) * 2 * SP * size_t(a.Npad) + n
+                         : nullptr;
+      float L[64];
+#pragma unroll
+      for (int h = 0; h < 2; ++h) {
+        float dl[32], dr[32];
+        tc::tmem_ld32(lane_addr + uint32_t(32 * h), dl);
+        tc::tmem_ld32(lane_addr + uint32_t(64 + 32 * h), dr);
+        if (pd) {  // the children's products for the adjoint
+#pragma unroll
+          for (int i = 0; i < 32; ++i) {
+            pd[size_t(32 * h + i) * a.Npad] = dl[i];
+            pd[size_t(SP + 32 * h + i) * a.Npad] = dr[i];
+          }
+        }
+#pragma unroll
+        for (int i = 0; i < 32; ++i) L[32 * h + i] = dl[i] * dr[i];
+      }
+      const int El = wide_child_expo(a, l, b, k, n), Er = wide_child_expo(a, r, b, k, n);
+      if (is_root) {
+        double s = 0.0;
+#pragma unroll
+        for (int i = 0; i < 64; ++i)
+          if (i < a.S) s = fma(a.freqs[size_t(b) * a.S + i], double(L[i]), s);
+        const size_t o = (size_t(b) * a.K + k) * a.Npad + n;
+        a.root_site[o] = s;
+        a.root_expo[o] = El + Er;
+      } else {
+        int e = 0;
+        if (a.rescale) {
+          float m = 0.0f;
+#pragma unroll
+          for (int i = 0; i < 64; ++i) m = fmaxf(m, L[i]);
+          e = scale_exponent(m);
+#pragma unroll
+          for (int i = 0; i < 64; ++i) L[i] = times_pow2_neg(L[i], e);
+        }
+        float *dst = a.part + ((size_t(b) * a.I + (v - a.tips)) * a.K + k) * SP * size_t(a.Npad) + n;
+#pragma unroll
+        for (int i = 0; i < 64; ++i) dst[size_t(i) * a.Npad] = L[i];
+        a.expo[((size_t(b) * a.I + (v - a.tips)) * a.K + k) * a.Npad + n] = El + Er + e;
       }
     }
-    // A operand: the side's loaded values split, four j per 16-byte store
-    {
-#pragma unroll
-      for (int j = 0; j < SP; j += 4) {
-        float4 hb, hs;
-        tc::split_tf32(xv[j], hb.x, hs.x);
-        tc::split_tf32(xv[j + 1], hb.y, hs.y);
-        tc::split_tf32(xv[j + 2], hb.z, hs.z);
-        tc::split_tf32(xv[j + 3], hb.w, hs.w);
-        const uint32_t off = tc::kmajor_off(tid, j, 2048);
-        *reinterpret_cast<float4 *>(sA + off) = hb;
-        *reinterpret_cast<float4 *>(sA + tc::kAbytes + off) = hs;
-      }
-    }
-    // generic-proxy writes -> visible to the tensor cores (async proxy)
-    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-    tc::fence_before_sync();
-    __syncthreads();
-    tc::fence_after_sync();
-    tmem = *tslot;
-    if (tid == 0 && b_pending) {  // the image has landed
-      if (mbar_wait_bounded(bar_b, phase_b, timeout_ns)) {
-        b_pending = false;
-        phase_b ^= 1;
-      }
-    }
-    if (tid == 0 && !b_pending) {
-      constexpr uint32_t idesc = tc::idesc_tf32(128, 64);
-      const uint32_t d = tmem + uint32_t(64 * c);
-      const uint32_t ab = smem_u32(sA), as = ab + tc::kAbytes;
-      const uint32_t bb = smem_u32(sB), bs = bb + tc::kBbytes;
-#pragma unroll
-      for (int kk = 0; kk < SP / 8; ++kk) {
-        const uint64_t dab = tc::smem_desc(ab + kk * 4096, 2048, 128), das = tc::smem_desc(as + kk * 4096, 2048, 128);
-        const uint64_t dbb = tc::smem_desc(bb + kk * 2048, 1024, 128), dbs = tc::smem_desc(bs + kk * 2048, 1024, 128);
-        tc::mma_tf32(d, dab, dbb, idesc, kk > 0 ? 1u : 0u);
-        tc::mma_tf32(d, dab, dbs, idesc, 1u);
-        tc::mma_tf32(d, das, dbb, idesc, 1u);
-      }
-      tc::mma_commit(bar);
-    } else if (tid == 0) {
-      mbar_arrive(bar);  // no MMAs (the image never landed): complete the phase; the side fails below
-    }
-    if (c == 0) load_x(r);  // while the MMAs run: the other side's values into registers
-    // every thread sees the side's MMAs complete before the shared memory is restaged or TMEM read
-    ok = mbar_wait_bounded(bar, phase, timeout_ns) && !(tid == 0 && b_pending);
-    tc::fence_after_sync();
-    ok = !__syncthreads_or(!ok);
-    if (ok) phase ^= 1;
-  }
+  }  // tiles
   if (!ok) {
     if (tid == 0) {
       atomicExch(status, kDeviceTimeout);
       if (b_pending) mbar_wait_bounded(bar_b, phase_b, 100000000ull);  // the image copy lands before exit
     }
     mbar_wait_bounded(bar, phase, 100000000ull);  // give the tensor cores a last chance before freeing TMEM
-  } else {
-    // this thread's pattern = TMEM lane 32 * warp + lane
-    const uint32_t lane_addr = tmem + (uint32_t(32 * warp) << 16);
-    const int n = n0 + tid;
-    float *pd = a.prod ? a.prod + ((size_t(b) * a.I + (v - a.tips)) * a.K + k) * 2 * SP * size_t(a.Npad) + n
-                       : nullptr;
-    float L[64];
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      float dl[32], dr[32];
-      tc::tmem_ld32(lane_addr + uint32_t(32 * h), dl);
-      tc::tmem_ld32(lane_addr + uint32_t(64 + 32 * h), dr);
-      if (pd) {  // the children's products for the adjoint
-#pragma unroll
-        for (int i = 0; i < 32; ++i) {
-          pd[size_t(32 * h + i) * a.Npad] = dl[i];
-          pd[size_t(SP + 32 * h + i) * a.Npad] = dr[i];
-        }
-      }
-#pragma unroll
-      for (int i = 0; i < 32; ++i) L[32 * h + i] = dl[i] * dr[i];
-    }
-    const int El = wide_child_expo(a, l, b, k, n), Er = wide_child_expo(a, r, b, k, n);
-    if (is_root) {
-      double s = 0.0;
-#pragma unroll
-      for (int i = 0; i < 64; ++i)
-        if (i < a.S) s = fma(a.freqs[size_t(b) * a.S + i], double(L[i]), s);
-      const size_t o = (size_t(b) * a.K + k) * a.Npad + n;
-      a.root_site[o] = s;
-      a.root_expo[o] = El + Er;
-    } else {
-      int e = 0;
-      if (a.rescale) {
-        float m = 0.0f;
-#pragma unroll
-        for (int i = 0; i < 64; ++i) m = fmaxf(m, L[i]);
-        e = scale_exponent(m);
-#pragma unroll
-        for (int i = 0; i < 64; ++i) L[i] = times_pow2_neg(L[i], e);
-      }
-      float *dst = a.part + ((size_t(b) * a.I + (v - a.tips)) * a.K + k) * SP * size_t(a.Npad) + n;
-#pragma unroll
-      for (int i = 0; i < 64; ++i) dst[size_t(i) * a.Npad] = L[i];
-      a.expo[((size_t(b) * a.I + (v - a.tips)) * a.K + k) * a.Npad + n] = El + Er + e;
-    }
   }
   tc::fence_before_sync();
   __syncthreads();
