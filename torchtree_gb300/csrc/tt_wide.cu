@@ -283,9 +283,9 @@ struct Wide {
     for (size_t lv = 0; lv + 1 < w.fwd_off.size(); ++lv) {
       a.nodes = w.d_fwd + w.fwd_off[lv];
       if constexpr (std::is_same<T, float>::value && SP == 64) {
-        if (w.tc) {  // tiles per CTA by level: about eight waves of two CTAs per SM
+        if (w.tc) {  // tiles per CTA by level: about sixteen waves of two CTAs per SM
           const int nodes = w.fwd_off[lv + 1] - w.fwd_off[lv], ntf = g.Npad / tc::kPT;
-          const int chunks = tc_level_chunks(nodes, p->batch * p->K, ntf, ntf, 8 * 152 * 2);
+          const int chunks = tc_level_chunks(nodes, p->batch * p->K, ntf, ntf, 16 * 152 * 2);
           WideArgs<T> at = a;
           at.ntiles = ntf;
           at.tiles_per_chunk = (ntf + chunks - 1) / chunks;
