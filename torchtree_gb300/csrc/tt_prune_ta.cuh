@@ -343,60 +343,92 @@ __device__ __forceinline__ void ta_backward_body(const PruneArgs<float> &a, cons
     //   G[c][k][i][jj] = sum_p (coef x_c)[p][i][k] * v_c[p][jj][k]
     // UR lanes own the 4x4 blocks of one (child, category pair) over patterns
     // s, s+UR, ...; recursive halving across the UR lanes leaves each lane NV
-    // consecutive floats of the block's 32, written straight to HBM.
+    // floats of the block's 32, written straight to HBM.
+    // The halving splits the block index (i1 i0 jj1 jj0 k) from the top bit
+    // down, lane bit UR/2 first.  A lane whose bits are (a1 a0 b1 b0 ..) loads
+    // row i ^ a of x and, for an internal child, row jj ^ b of v, so register
+    // slot (i', jj') holds element (i' ^ a, jj' ^ b): every lane then keeps
+    // the lower half of its slots at every level and sends the upper half,
+    // which holds the partner's kept elements, with no lane-dependent selects.
+    // A tip child's v comes from the code table unpermuted; its jj levels and
+    // the category level select as plain recursive halving.
     {
+      constexpr int LV = UR >= 32 ? 5 : UR >= 16 ? 4 : UR >= 8 ? 3 : UR >= 4 ? 2 : UR >= 2 ? 1 : 0;
+      constexpr int PL = (P + UR - 1) / UR;  // patterns per lane
       const int unit = tid / UR, sidx = tid - unit * UR;
       const bool uact = unit < UNITS;
       const int c = unit / KQ, t = unit - (unit / KQ) * KQ;
+      const bool tipc = uact && (c ? rtip : ltip);
+      // permutation bits: the top LV bits of the 5-bit block index
+      const int bits = LV > 0 ? (sidx << (5 - LV)) : 0;
+      const int pa = bits >> 3, pb = tipc ? 0 : (bits >> 1) & 3;
       float2 acc[4][4];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) acc[i][jj] = make_float2(0.0f, 0.0f);
       if (uact) {
-        const bool tipc = c ? rtip : ltip;
-        const float2 *xs = xbuf + c * KQ * 4 * P + t * 4 * P;  // pair t rows
-        const float2 *vs = (c ? kidr : kidl) + t * 4 * P;
-        const unsigned char *csd = stg + G.codes + c * P;
-#pragma unroll 4
-        for (int m = sidx; m < rem; m += UR) {
-          float2 x[4], v[4];
+        const float2 *xs = xbuf + c * KQ * 4 * P + t * 4 * P + sidx;  // pair t rows
+        const float2 *vs = (c ? kidr : kidl) + t * 4 * P + sidx;
+        const unsigned char *csd = stg + G.codes + c * P + sidx;
+        const float2 *xr[4], *vr[4];
 #pragma unroll
-          for (int i = 0; i < 4; ++i) x[i] = xs[i * P + m];
-          if (tipc) {
-            const float4 *tr = reinterpret_cast<const float4 *>(tab2 + int(csd[m]) * 4);
-            const float4 t0 = tr[0], t1 = tr[1];
-            v[0] = make_float2(t0.x, t0.y);
-            v[1] = make_float2(t0.z, t0.w);
-            v[2] = make_float2(t1.x, t1.y);
-            v[3] = make_float2(t1.z, t1.w);
-          } else {
+        for (int i = 0; i < 4; ++i) {
+          xr[i] = xs + (i ^ pa) * P;
+          vr[i] = vs + (i ^ pb) * P;
+        }
 #pragma unroll
-            for (int jj = 0; jj < 4; ++jj) v[jj] = vs[jj * P + m];
+        for (int kk = 0; kk < PL; ++kk) {
+          if (sidx + kk * UR < rem) {
+            float2 x[4], v[4];
+#pragma unroll
+            for (int i = 0; i < 4; ++i) x[i] = xr[i][kk * UR];
+            if (tipc) {
+              const float4 *tr = reinterpret_cast<const float4 *>(tab2 + int(csd[kk * UR]) * 4);
+              const float4 t0 = tr[0], t1 = tr[1];
+              v[0] = make_float2(t0.x, t0.y);
+              v[1] = make_float2(t0.z, t0.w);
+              v[2] = make_float2(t1.x, t1.y);
+              v[3] = make_float2(t1.z, t1.w);
+            } else {
+#pragma unroll
+              for (int jj = 0; jj < 4; ++jj) v[jj] = vr[jj][kk * UR];
+            }
+#pragma unroll
+            for (int i = 0; i < 4; ++i)
+#pragma unroll
+              for (int jj = 0; jj < 4; ++jj) acc[i][jj] = __ffma2_rn(x[i], v[jj], acc[i][jj]);
           }
-#pragma unroll
-          for (int i = 0; i < 4; ++i)
-#pragma unroll
-            for (int jj = 0; jj < 4; ++jj) acc[i][jj] = __ffma2_rn(x[i], v[jj], acc[i][jj]);
         }
       }
-      // block float e: category 2t + (e >> 4), element (i, jj) = e & 15
+      // slot e = i' * 8 + jj' * 2 + k (k: category 2t + k)
       float f[32];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
         for (int jj = 0; jj < 4; ++jj) {
-          f[i * 4 + jj] = acc[i][jj].x;
-          f[16 + i * 4 + jj] = acc[i][jj].y;
+          f[i * 8 + jj * 2] = acc[i][jj].x;
+          f[i * 8 + jj * 2 + 1] = acc[i][jj].y;
         }
+      // a warp with no tip-child lane skips the jj levels' selects
+      const bool sel_jj = __any_sync(0xffffffffu, tipc);
 #pragma unroll
       for (int o = UR / 2, h = 16; o >= 1; o >>= 1, h >>= 1) {
         const bool up = (lane & o) != 0;
+        if (h >= 8) {  // i levels: permuted for every lane
 #pragma unroll
-        for (int e = 0; e < h; ++e) {
-          const float send = up ? f[e] : f[e + h];
-          const float keep = up ? f[e + h] : f[e];
-          f[e] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+          for (int e = 0; e < h; ++e) f[e] += __shfl_xor_sync(0xffffffffu, f[e + h], o);
+        } else if (h >= 2 && !sel_jj) {  // jj levels, all lanes permuted
+#pragma unroll
+          for (int e = 0; e < h; ++e) f[e] += __shfl_xor_sync(0xffffffffu, f[e + h], o);
+        } else {  // jj levels of tip lanes (internal lanes never swap), category level
+          const bool swap = up && (h == 1 || tipc);
+#pragma unroll
+          for (int e = 0; e < h; ++e) {
+            const float send = swap ? f[e] : f[e + h];
+            const float keep = swap ? f[e + h] : f[e];
+            f[e] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+          }
         }
       }
       if (uact) {
@@ -404,8 +436,10 @@ __device__ __forceinline__ void ta_backward_body(const PruneArgs<float> &a, cons
         float *dst = a.gpart + ((size_t(b) * a.branch_count + branch) * a.ntiles + tile) * KSS + 32 * t;
 #pragma unroll
         for (int e = 0; e < NV; ++e) {
-          const int fe = NV * sidx + e;
-          if (2 * t + (fe >> 4) < K) dst[fe] = f[e];
+          // kept slot e holds block element (bits | e): i = >> 3, jj = >> 1 & 3, k = & 1
+          const int idx = bits | e;
+          const int k = idx & 1;
+          if (2 * t + k < K) dst[k * 16 + (idx >> 3) * 4 + ((idx >> 1) & 3)] = f[e];
         }
       }
     }
