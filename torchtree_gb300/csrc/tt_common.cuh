@@ -220,26 +220,6 @@ __device__ __forceinline__ T times_pow2_neg(T x, int e) {
 }
 
 // ------------------------------------------------------------ reductions
-// Recursive-halving warp reduction of V values (V a multiple of 32): on
-// return lane l holds the warp sums of elements [l*V/32, (l+1)*V/32) in
-// v[0 .. V/32).
-template <int V, typename T>
-__device__ __forceinline__ void warp_reduce_halving(T (&v)[V], int lane) {
-  static_assert(V % 32 == 0, "pad the reduction to a multiple of 32");
-#pragma unroll
-  for (int lev = 0; lev < 5; ++lev) {
-    const int o = 16 >> lev;
-    const int h = (V >> lev) / 2;
-    const bool up = (lane & o) != 0;
-#pragma unroll
-    for (int j = 0; j < h; ++j) {
-      const T send = up ? v[j] : v[j + h];
-      const T keep = up ? v[j + h] : v[j];
-      v[j] = keep + __shfl_xor_sync(0xffffffffu, send, o);
-    }
-  }
-}
-
 template <typename T>
 __device__ __forceinline__ T warp_sum(T x) {
 #pragma unroll
