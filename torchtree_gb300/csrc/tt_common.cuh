@@ -220,6 +220,10 @@ __device__ __forceinline__ T times_pow2_neg(T x, int e) {
 }
 
 // ------------------------------------------------------------ reductions
+__device__ __forceinline__ float2 shfl_xor_f2(float2 v, int o) {
+  return make_float2(__shfl_xor_sync(0xffffffffu, v.x, o), __shfl_xor_sync(0xffffffffu, v.y, o));
+}
+
 template <typename T>
 __device__ __forceinline__ T warp_sum(T x) {
 #pragma unroll

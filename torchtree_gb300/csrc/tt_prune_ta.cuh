@@ -143,7 +143,6 @@ __device__ __forceinline__ void ta_backward_body(const PruneArgs<float> &a, cons
   constexpr int NW = NT / 32;
   constexpr int UNITS = 2 * KQ;                   // (child, category pair) blocks
   constexpr int UR = ta_red_lanes(NT / UNITS);    // lanes per block
-  constexpr int NV = 32 / UR;                     // block floats per lane after the shuffles
   static_assert(UNITS * UR <= NT, "reduction lanes exceed the CTA");
   extern __shared__ __align__(128) unsigned char smem[];
   const int NSTAGE = a.nstage;
@@ -342,8 +341,8 @@ __device__ __forceinline__ void ta_backward_body(const PruneArgs<float> &a, cons
     // reduction over the tile's patterns, register-blocked:
     //   G[c][k][i][jj] = sum_p (coef x_c)[p][i][k] * v_c[p][jj][k]
     // UR lanes own the 4x4 blocks of one (child, category pair) over patterns
-    // s, s+UR, ...; recursive halving across the UR lanes leaves each lane NV
-    // floats of the block's 32, written straight to HBM.
+    // s, s+UR, ...; recursive halving across the UR lanes (packed pair adds)
+    // leaves each lane 32 / UR floats of the block, written straight to HBM.
     // The halving splits the block index (i1 i0 jj1 jj0 k) from the top bit
     // down, lane bit UR/2 first.  A lane whose bits are (a1 a0 b1 b0 ..) loads
     // row i ^ a of x and, for an internal child, row jj ^ b of v, so register
@@ -401,45 +400,49 @@ __device__ __forceinline__ void ta_backward_body(const PruneArgs<float> &a, cons
           }
         }
       }
-      // slot e = i' * 8 + jj' * 2 + k (k: category 2t + k)
-      float f[32];
+      // slot s = i' * 4 + jj' holds categories (2t, 2t + 1) of element (i', jj')
+      float2 g[16];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
 #pragma unroll
-        for (int jj = 0; jj < 4; ++jj) {
-          f[i * 8 + jj * 2] = acc[i][jj].x;
-          f[i * 8 + jj * 2 + 1] = acc[i][jj].y;
-        }
+        for (int jj = 0; jj < 4; ++jj) g[i * 4 + jj] = acc[i][jj];
       // a warp with no tip-child lane skips the jj levels' selects
       const bool sel_jj = __any_sync(0xffffffffu, tipc);
 #pragma unroll
-      for (int o = UR / 2, h = 16; o >= 1; o >>= 1, h >>= 1) {
-        const bool up = (lane & o) != 0;
-        if (h >= 8) {  // i levels: permuted for every lane
+      for (int o = UR / 2, h = 8; o >= 1 && h >= 1; o >>= 1, h >>= 1) {
+        if (h >= 4 || !sel_jj) {  // i levels, and jj levels with every lane permuted
 #pragma unroll
-          for (int e = 0; e < h; ++e) f[e] += __shfl_xor_sync(0xffffffffu, f[e + h], o);
-        } else if (h >= 2 && !sel_jj) {  // jj levels, all lanes permuted
-#pragma unroll
-          for (int e = 0; e < h; ++e) f[e] += __shfl_xor_sync(0xffffffffu, f[e + h], o);
-        } else {  // jj levels of tip lanes (internal lanes never swap), category level
-          const bool swap = up && (h == 1 || tipc);
+          for (int e = 0; e < h; ++e) g[e] = __fadd2_rn(g[e], shfl_xor_f2(g[e + h], o));
+        } else {  // jj levels of tip lanes (internal lanes never swap)
+          const bool swap = tipc && (lane & o) != 0;
 #pragma unroll
           for (int e = 0; e < h; ++e) {
-            const float send = swap ? f[e] : f[e + h];
-            const float keep = swap ? f[e + h] : f[e];
-            f[e] = keep + __shfl_xor_sync(0xffffffffu, send, o);
+            const float2 send = swap ? g[e] : g[e + h];
+            const float2 keep = swap ? g[e + h] : g[e];
+            g[e] = __fadd2_rn(keep, shfl_xor_f2(send, o));
           }
         }
+      }
+      if (LV == 5) {  // 32 lanes per block: a last level over the pair's two categories
+        const bool up = (lane & 1) != 0;
+        const float send = up ? g[0].x : g[0].y, keep = up ? g[0].y : g[0].x;
+        g[0].x = keep + __shfl_xor_sync(0xffffffffu, send, 1);
       }
       if (uact) {
         const int branch = c ? right : left;
         float *dst = a.gpart + ((size_t(b) * a.branch_count + branch) * a.ntiles + tile) * KSS + 32 * t;
+        if (LV == 5) {
+          const int k = sidx & 1;
+          if (2 * t + k < K) dst[k * 16 + (sidx >> 1)] = g[0].x;
+        } else {
+          // kept slot s holds element (sidx << (4 - LV)) | s = i * 4 + jj
+          constexpr int NG = LV >= 4 ? 1 : 16 >> LV;
 #pragma unroll
-        for (int e = 0; e < NV; ++e) {
-          // kept slot e holds block element (bits | e): i = >> 3, jj = >> 1 & 3, k = & 1
-          const int idx = bits | e;
-          const int k = idx & 1;
-          if (2 * t + k < K) dst[k * 16 + (idx >> 3) * 4 + ((idx >> 1) & 3)] = f[e];
+          for (int s = 0; s < NG; ++s) {
+            const int el = (sidx << (LV >= 4 ? 0 : 4 - LV)) | s;
+            dst[el] = g[s].x;
+            if (2 * t + 1 < K) dst[16 + el] = g[s].y;
+          }
         }
       }
     }
