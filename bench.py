@@ -429,13 +429,15 @@ def run_serving(args):
     for c in range(len(mix)):
         srv.submit(*request(c)).result()
     setup_s = time.perf_counter() - t0
+    srv.reset_stats()
     burst = [srv.submit(*request(c)) for c in range(min(len(chains), 4 * len(mix)))]
     t1 = time.perf_counter()
     for f in burst:
         f.result()
     capacity = len(burst) / (time.perf_counter() - t1)
+    burst_stats = srv.latency_stats()
     rate = 0.7 * capacity
-    srv.completed.clear()
+    srv.reset_stats()
     # open-loop Poisson arrivals at 70 % of the measured capacity
     gaps = rng.exponential(1.0 / rate, args.serving_requests)
     picks = rng.integers(0, len(chains), args.serving_requests)
@@ -480,7 +482,15 @@ def run_serving(args):
         "value": len(futs) / wall, "unit": "requests/s", "higher_is_better": True, "n_gpus": 1,
         "latency_ms": {"p50": stats.get("p50_ms"), "p99": stats.get("p99_ms"), "mean": stats.get("mean_ms"),
                        "queue_wait_p50": stats.get("wait_p50_ms"), "service_p50": stats.get("service_p50_ms")},
-        "offered_rate": rate, "capacity_closed_loop": capacity, "requests": len(futs),
+        "offered_rate": rate, "capacity_closed_loop": capacity,
+        "closed_loop": {"requests": burst_stats.get("count"), "launches": burst_stats.get("launches"),
+                        "requests_per_launch": burst_stats.get("requests_per_launch"),
+                        "merged_steps": burst_stats.get("merged_steps"),
+                        "requests_per_merged_step": burst_stats.get("requests_per_merged_step"),
+                        "latency_p50_ms": burst_stats.get("p50_ms"),
+                        "what": f"{len(burst)} requests submitted at once (chain c on data set c mod {len(mix)}); "
+                                "counters of this phase only"},
+        "requests": len(futs),
         "batches": stats.get("batches"), "launches": stats.get("launches"),
         "requests_per_launch": stats.get("requests_per_launch"),
         "merged_steps": stats.get("merged_steps"), "requests_per_merged_step": stats.get("requests_per_merged_step"),

@@ -75,6 +75,28 @@ def test_continuous_batching_admits_arrivals_after_the_batch_in_flight():
     assert srv.latency_stats()["count"] == 9
 
 
+def test_reset_stats_counts_one_phase_only():
+    srv, log, made = _server(budget=100, slots=4, sizes={"a": 10})
+    first = [srv.submit("a", {"i": i}) for i in range(2)]
+    srv.step()
+    made["a"].release = True
+    srv.step()
+    assert [f.result(timeout=1)["lnl"] for f in first] == [0.0, -1.0]
+    assert srv.latency_stats()["launches"] == 1
+    srv.reset_stats()
+    assert srv.latency_stats() == {"count": 0}
+    futs = [srv.submit("a", {"i": i}) for i in range(2, 10)]
+    srv.step()  # four of the eight
+    made["a"].release = True
+    srv.step()  # completes them and launches the other four
+    made["a"].release = True
+    srv.step()
+    assert [f.result(timeout=1)["lnl"] for f in futs] == [-float(i) for i in range(2, 10)]
+    stats = srv.latency_stats()
+    assert stats["count"] == 8 and stats["launches"] == 2 and stats["batches"] == 2
+    assert stats["requests_per_launch"] == 4.0 and stats["admissions"] == 0
+
+
 def test_admission_by_footprint_waits_and_evicts_idle_plans():
     srv, log, made = _server(budget=100, slots=2, sizes={"a": 60, "b": 60, "c": 30})
     fa = srv.submit("a", {"i": 0})

@@ -407,6 +407,15 @@ class LikelihoodServer:
         if self._error is not None:
             raise self._error
 
+    def reset_stats(self) -> None:
+        """Start a new measurement phase: forget completed requests and zero the
+        launch, batch, merge, admission and eviction counters (call it while no
+        request is waiting or in flight)."""
+        self.completed.clear()
+        self.batches = self.launches = self.merged_steps = self.merged_requests = 0
+        self.merge_host_s = 0.0
+        self.admissions = self.evictions = 0
+
     def latency_stats(self) -> dict:
         lat = np.array([r.t_done - r.t_submit for r in self.completed]) * 1e3
         if lat.size == 0:
