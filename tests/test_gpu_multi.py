@@ -106,3 +106,37 @@ def test_merged_plans_match_the_oracle():
     plans_gradient(engines, [c["props"] for c in cases], [c["pi"] for c in cases])
     for lnl, ref in zip(lnls, refs):
         np.testing.assert_allclose(lnl.cpu().numpy(), ref, rtol=1e-6)
+
+
+def test_active_samples_equal_the_whole_batch_for_those_samples():
+    """TT_OPT_ACTIVE_SAMPLES: the pruning passes and their reductions over the
+    first n samples only, alone and in a merged call, give those samples'
+    results of a call over every sample bit for bit."""
+    from torchtree_gb300 import _native
+    from torchtree_gb300.engine import plans_gradient, plans_log_likelihood
+
+    cases = [_plan(120, 1500, 4, 21, 4), _plan(45, 700, 4, 22, 3)]
+    full = [_alone(c) for c in cases]
+    e0 = cases[0]["eng"]
+    with pytest.raises(_native.EngineError):
+        e0.set_option(_native.TT_OPT_ACTIVE_SAMPLES, 5)  # more than the batch
+    for n in (1, 2, 4):  # one plan's own calls
+        e0.set_option(_native.TT_OPT_ACTIVE_SAMPLES, n)
+        assert e0.get_option(_native.TT_OPT_ACTIVE_SAMPLES) == n
+        got = _alone(cases[0])
+        for name, x, y in zip(("lnl", "dpi", "dc", "dq", "dt", "dr"), full[0], got):
+            np.testing.assert_array_equal(y[:n], x[:n], err_msg=f"n={n} {name}")
+    active = (3, 2)  # a merged call with a different count per plan
+    for c, n in zip(cases, active):
+        c["eng"].set_option(_native.TT_OPT_ACTIVE_SAMPLES, n)
+        c["eng"].set_eigen(*c["eig"])
+    engines = [c["eng"] for c in cases]
+    lnls = plans_log_likelihood(engines, [c["props"] for c in cases], [c["pi"] for c in cases], rescale=True,
+                                keep_partials=True)
+    grads = plans_gradient(engines, [c["props"] for c in cases], [c["pi"] for c in cases])
+    for c, n, ref, lnl, (dpi, dc) in zip(cases, active, full, lnls, grads):
+        dq, dt, dr = c["eng"].rate_matrix_gradient(*c["eig"])
+        for name, x, y in zip(("lnl", "dpi", "dc", "dq", "dt", "dr"), ref, (lnl, dpi, dc, dq, dt, dr)):
+            np.testing.assert_array_equal(y.cpu().numpy()[:n], x[:n], err_msg=f"merged n={n} {name}")
+        c["eng"].set_option(_native.TT_OPT_ACTIVE_SAMPLES, 0)
+        assert c["eng"].get_option(_native.TT_OPT_ACTIVE_SAMPLES) == 0

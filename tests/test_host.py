@@ -36,6 +36,17 @@ def test_library_loads_and_exports_every_header_symbol():
     assert lib.tt_version().startswith(b"torchtree_gb300")
 
 
+def test_option_and_status_constants_match_the_header():
+    from torchtree_gb300 import _native
+
+    text = "\n".join(p.read_text() for p in sorted((ROOT / "include").glob("*.h")))
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    header = {k: int(v) for k, v in re.findall(r"\b(TT_OPT_[A-Z_]+)\s*=\s*(\d+)", text)}
+    assert "TT_OPT_ACTIVE_SAMPLES" in header
+    mirrored = {k: getattr(_native, k) for k in dir(_native) if k.startswith("TT_OPT_")}
+    assert mirrored == header
+
+
 def test_invalid_postorder_is_rejected_by_the_schedule():
     from torchtree_gb300 import _native
 

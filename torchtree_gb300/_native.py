@@ -31,6 +31,7 @@ TT_OPT_INPLACE_ADJOINT = 6
 TT_OPT_SLAB_PATTERNS = 7
 TT_OPT_PAIR_ADJOINT = 8
 TT_OPT_TENSOR_CORE_ADJOINT = 9
+TT_OPT_ACTIVE_SAMPLES = 10
 
 SIGNATURES = {
     "tt_version": (ctypes.c_char_p, []),

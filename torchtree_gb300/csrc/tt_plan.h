@@ -31,6 +31,7 @@ struct tt_plan {
   // slab by slab).
   int slab = 0;
   int last_rescale = 1;  // rescale flag of the last post-order (repeated by the slab recompute)
+  int active = 0;        // 4-state plans: samples the pruning passes run over (0 = all)
   long long launches = 0;
   std::vector<int> steps;       // host copy of the schedule (I x 12)
   std::vector<int> steps_ws;    // records of the producer-warp post-order (I x 12)

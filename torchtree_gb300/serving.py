@@ -135,9 +135,10 @@ SLAB_ALIGN = 512  # pattern-slab sizes are multiples of this (TT_OPT_SLAB_PATTER
 def slots_for(ds: Dataset, max_slots: int, fill_ctas: int = 2 * 152) -> int:
     """Batch slots of a data set's plan: enough samples that one launch's
     pattern tiles fill the GPU (``fill_ctas`` CTAs), at most ``max_slots``.
-    A plan computes every slot whatever the number of waiting requests, so a
-    large data set, which fills the GPU with one sample, gets fewer slots and
-    spends no work on idle ones."""
+    A captured step computes every slot whatever the number of waiting
+    requests (merged 4-state steps run only the slots that hold requests,
+    TT_OPT_ACTIVE_SAMPLES), and every slot holds its own partials, so a large
+    data set, which fills the GPU with one sample, gets fewer slots."""
     N, K = ds.alignment.pattern_count, ds.spec.categories
     per_sample = -(-N // 64) if ds.state_count == 4 else -(-N // 128) * K
     return max(1, min(max_slots, -(-fill_ctas // max(per_sample, 1))))
@@ -290,7 +291,8 @@ def merged_step(batches: list, stream, device) -> torch.cuda.Event:
     ``stream``: their inputs in, ONE eigendecomposition launch for all their
     rate matrices, transition matrices per data set, then ONE post-order and
     ONE adjoint launch over the tiles of all of them
-    (``tt_plans_log_likelihood`` / ``tt_plans_gradient``), the rate-matrix
+    (``tt_plans_log_likelihood`` / ``tt_plans_gradient``; each plan's
+    pruning passes cover only the slots that hold requests), the rate-matrix
     chain per data set, results out.  ``batches``: ``[(executor, requests)]``.
     Each request's result equals what its data set's own step gives.  Returns
     the event recorded after the step's last copy."""
@@ -306,10 +308,12 @@ def merged_step(batches: list, stream, device) -> torch.cuda.Event:
                                               torch.cat([ex.inputs["pi"] for ex in execs]))
         eig = []
         first = 0
-        for ex in execs:
+        for ex, reqs in batches:
             x, sl = ex.inputs, slice(first, first + ex.slots)
             first += ex.slots
             eig.append((lam[sl], u[sl], w[sl]))
+            # the pruning passes run over the slots that hold requests only
+            ex.engine.set_option(_native.TT_OPT_ACTIVE_SAMPLES, len(reqs))
             ex.engine.set_eigen(lam[sl], u[sl], w[sl], x["bls"], x["rates"])
         engines = [ex.engine for ex in execs]
         props = [ex.inputs["props"] for ex in execs]
