@@ -428,10 +428,9 @@ int tt_plan_launch_count(const tt_plan *plan, int64_t *count);
  *     free device memory.  Setting it reallocates those buffers and drops
  *     any kept partials.  Results equal the unslabbed ones up to the order
  *     of the FP64 sums over slabs.
- *   TT_OPT_ACTIVE_SAMPLES: 4-state plans: run the post-order, the adjoint
- *     and their reductions (tt_log_likelihood, tt_gradient and the
- *     tt_plans_* calls) over samples 0 .. n-1 only (1 <= n <= batch; 0 = all,
- *     the default).  Transition matrices and the rate-matrix chain still
+ *   TT_OPT_ACTIVE_SAMPLES: run the post-order, the adjoint and their
+ *     reductions (tt_log_likelihood, tt_gradient and the tt_plans_* calls)
+ *     over samples 0 .. n-1 only (1 <= n <= batch; 0 = all, the default).  Transition matrices and the rate-matrix chain still
  *     cover every sample; the log-likelihoods and gradients of samples >= n
  *     are left unspecified.  The results of samples < n equal those of a
  *     call over all samples.  A change of n drops any kept partials.

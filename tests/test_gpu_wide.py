@@ -43,7 +43,7 @@ def _setup(wl):
         probs.expand(b, K).to(dev).contiguous(), pi.to(dev)
 
 
-def _run(wl, precision, tc=True, rescale=True, grads=True, tca=None, halve_row=None):
+def _run(wl, precision, tc=True, rescale=True, grads=True, tca=None, halve_row=None, active=None):
     from torchtree_gb300.engine import LikelihoodEngine
 
     ca, S, K, b, eig, probs, pi = _setup(wl)
@@ -65,6 +65,11 @@ def _run(wl, precision, tc=True, rescale=True, grads=True, tca=None, halve_row=N
         from torchtree_gb300 import _native
 
         eng.set_option(_native.TT_OPT_TENSOR_CORE_ADJOINT, tca)
+    if active is not None:
+        from torchtree_gb300 import _native
+
+        eng.set_option(_native.TT_OPT_ACTIVE_SAMPLES, active)
+        assert eng.get_option(_native.TT_OPT_ACTIVE_SAMPLES) == active
     eng.set_eigen(*eig)
     lnl = eng.log_likelihood(probs, pi, rescale=rescale, keep_partials=grads)
     out = {"lnl": lnl.cpu().numpy()}
@@ -212,3 +217,23 @@ def test_nonreversible_model_through_given_matrices():
         (g,) = torch.autograd.grad(lnl.sum(), r)
         np.testing.assert_allclose(lnl.detach().cpu().numpy(), ref.detach().numpy().reshape(-1), rtol=ltol)
         np.testing.assert_allclose(g.cpu().numpy(), gref.numpy(), rtol=gtol, atol=gtol * np.abs(gref.numpy()).max())
+
+
+@pytest.mark.parametrize("kind,precision,tc", [("protein", "f32", True), ("protein", "f64", True),
+                                               ("codon", "f32", True), ("codon", "f32", False)])
+def test_active_samples_equal_the_whole_batch_for_those_samples(kind, precision, tc):
+    """TT_OPT_ACTIVE_SAMPLES on 20- and 61-state plans (CUDA-core and
+    tensor-core kernels): the passes over the first n samples give those
+    samples' lnL and gradients of a call over every sample bit for bit (the
+    adjoint's chunking stays that of the whole batch)."""
+    from torchtree_gb300 import synthetic
+
+    if kind == "protein":
+        wl = synthetic.protein_workload("p", tip_count=30, site_count=600, batch=3, seed=41, shape=0.5)
+    else:
+        wl = synthetic.codon_workload("c", tip_count=20, site_count=300, batch=3, seed=42, shape=0.5)
+    full = _run(wl, precision, tc=tc)
+    for n in (1, 2):
+        got = _run(wl, precision, tc=tc, active=n)
+        for key in ("lnl", "dpi", "dc", "dt", "dr"):
+            np.testing.assert_array_equal(got[key][:n], full[key][:n], err_msg=f"n={n} {key}")

@@ -405,9 +405,6 @@ void slab_args(tt::PruneArgs<T> &a, int p0, int n, int tile) {
   a.site_lnl = nullptr;
 }
 
-// Samples the 4-state pruning passes and their reductions run over.
-int run_samples(const tt_plan *p) { return p->active > 0 ? std::min(p->active, p->batch) : p->batch; }
-
 // Post-order pass over patterns [p0, p0 + n) in the plan's kernel shape;
 // store = keep the partials of that range (for the adjoint).
 template <typename T>
@@ -417,11 +414,11 @@ cudaError_t post_order(tt_plan *p, const double *props, const double *freqs, int
   if (p0 != 0 || n != p->N) slab_args(a, p0, n, p->tile_f);
   if constexpr (sizeof(T) == 4) {
     a.slots = p->producer_warp && !p->pair_threads ? p->slots_ws : p->slots_fwd;
-    return tt::launch_prune_f32(a, false, p->tile_f, run_samples(p),
+    return tt::launch_prune_f32(a, false, p->tile_f, plan_run_samples(p),
                                 (p->pair_threads ? tt::kF32PairThreads : 0) | (p->producer_warp ? tt::kF32ProducerWarp : 0), s);
   } else {
     a.slots = p->slots_fwd;
-    return tt::launch_prune_f64(a, false, p->tile_f, run_samples(p), s);
+    return tt::launch_prune_f64(a, false, p->tile_f, plan_run_samples(p), s);
   }
 }
 
@@ -726,7 +723,7 @@ int tt_log_likelihood(tt_plan *p, const double *props, const double *freqs, int3
   cudaError_t e = p->precision == TT_PRECISION_F32 ? post_order<float>(p, props, freqs, rescale ? 1 : 0, store, site_lnl, 0, p->N, s)
                                                    : post_order<double>(p, props, freqs, rescale ? 1 : 0, store, site_lnl, 0, p->N, s);
   if (e != cudaSuccess) return cuda_fail(e, "post-order launch");
-  e = tt::launch_reduce_lnl(p->d_tile_lnl, lnl, run_samples(p), p->ntiles_f, 0, s);
+  e = tt::launch_reduce_lnl(p->d_tile_lnl, lnl, plan_run_samples(p), p->ntiles_f, 0, s);
   if (e != cudaSuccess) return cuda_fail(e, "likelihood reduction launch");
   p->launches += 2;
   p->last_rescale = rescale ? 1 : 0;
@@ -819,7 +816,7 @@ int tt_plans_log_likelihood(int32_t count, tt_plan *const *plans, const double *
       m.a[k] = a;
       m.first[k] = int(total);
       m.per_sample[k] = (p->ntiles_f + TPC - 1) / TPC;
-      total += (long long)m.per_sample[k] * run_samples(p);
+      total += (long long)m.per_sample[k] * plan_run_samples(p);
       smem = std::max(smem, tt::tl_ws_smem_bytes(p->K, p->C, p->slots_ws, p->nstage_f));
     }
     if (total > 0x7fffffffll) return fail(TT_ERR_UNSUPPORTED, "too many CTAs for one merged launch");
@@ -828,7 +825,7 @@ int tt_plans_log_likelihood(int32_t count, tt_plan *const *plans, const double *
     if (e != cudaSuccess) return cuda_fail(e, "merged post-order launch");
     for (int k = 0; k < m.count; ++k) {
       tt_plan *p = plans[g[k]];
-      e = tt::launch_reduce_lnl(p->d_tile_lnl, log_likelihood[g[k]], run_samples(p), p->ntiles_f, 0, s);
+      e = tt::launch_reduce_lnl(p->d_tile_lnl, log_likelihood[g[k]], plan_run_samples(p), p->ntiles_f, 0, s);
       if (e != cudaSuccess) return cuda_fail(e, "likelihood reduction launch");
       p->launches += 1;
       p->last_rescale = rescale ? 1 : 0;
@@ -877,7 +874,7 @@ int tt_plans_gradient(int32_t count, tt_plan *const *plans, const double *const 
       m.a[k] = a;
       m.first[k] = int(total);
       m.per_sample[k] = a.ntiles;
-      total += (long long)a.ntiles * run_samples(p);
+      total += (long long)a.ntiles * plan_run_samples(p);
       smem = std::max(smem, pair ? tt::tp_smem_bytes(p->K, p->C, p->nstage_b) : tt::ta_smem_bytes(p->K, p->C, p->nstage_b));
     }
     if (total > 0x7fffffffll) return fail(TT_ERR_UNSUPPORTED, "too many CTAs for one merged launch");
@@ -890,7 +887,7 @@ int tt_plans_gradient(int32_t count, tt_plan *const *plans, const double *const 
       tt_plan *p = plans[i];
       const int ntiles = m.per_sample[k];
       e = tt::launch_reduce_f32(static_cast<const float *>(p->d_gpart), static_cast<const float *>(p->d_rootpart),
-                                p->d_G, p->d_rootgrad, p->d_rootgrad + size_t(p->batch) * p->S, run_samples(p), p->B, ntiles,
+                                p->d_G, p->d_rootgrad, p->d_rootgrad + size_t(p->batch) * p->S, plan_run_samples(p), p->B, ntiles,
                                 p->S, p->K, 0, s);
       if (e == cudaSuccess && grad_frequencies && grad_frequencies[i])
         e = cudaMemcpyAsync(grad_frequencies[i], p->d_rootgrad, size_t(p->batch) * p->S * sizeof(double),
@@ -945,7 +942,7 @@ int tt_gradient(tt_plan *p, const double *props, const double *freqs, double *gr
       a.slots = p->slots_bwd;
       a.nstage = p->nstage_b;
       slab_args(a, p0, n, p->tile_b);
-      e = tt::launch_prune_f32(a, true, p->tile_b, run_samples(p),
+      e = tt::launch_prune_f32(a, true, p->tile_b, plan_run_samples(p),
                                p->pair_threads ? tt::kF32PairThreads
                                                : (p->inplace_adjoint ? tt::kF32InPlaceAdjoint |
                                                                            (p->pair_adjoint ? tt::kF32PairAdjoint : 0)
@@ -954,17 +951,17 @@ int tt_gradient(tt_plan *p, const double *props, const double *freqs, double *gr
       if (e == cudaSuccess)
         e = tt::launch_reduce_f32(static_cast<const float *>(p->d_gpart),
                                   static_cast<const float *>(p->d_rootpart), p->d_G, p->d_rootgrad,
-                                  p->d_rootgrad + size_t(p->batch) * p->S, run_samples(p), p->B, ntiles, p->S,
+                                  p->d_rootgrad + size_t(p->batch) * p->S, plan_run_samples(p), p->B, ntiles, p->S,
                                   p->K, p0 > 0, s);
     } else {
       auto a = make_args<double>(p, props, freqs, 1, true, nullptr);
       a.slots = p->slots_bwd;
       slab_args(a, p0, n, p->tile_b);
-      e = tt::launch_prune_f64(a, true, p->tile_b, run_samples(p), s);
+      e = tt::launch_prune_f64(a, true, p->tile_b, plan_run_samples(p), s);
       if (e == cudaSuccess)
         e = tt::launch_reduce_f64(static_cast<const double *>(p->d_gpart),
                                   static_cast<const double *>(p->d_rootpart), p->d_G, p->d_rootgrad,
-                                  p->d_rootgrad + size_t(p->batch) * p->S, run_samples(p), p->B, ntiles, p->S,
+                                  p->d_rootgrad + size_t(p->batch) * p->S, plan_run_samples(p), p->B, ntiles, p->S,
                                   p->K, p0 > 0, s);
     }
     p->launches += 3;
@@ -1114,9 +1111,7 @@ int tt_plan_set_option(tt_plan *p, int32_t option, int32_t value) {
     case TT_OPT_ACTIVE_SAMPLES:
       if (value < 0 || value > p->batch)
         return fail(TT_ERR_INVALID_ARGUMENT, "the active sample count must be in [0, batch] (0 = all)");
-      if (value && value != p->batch && p->wide)
-        return fail(TT_ERR_UNSUPPORTED, "an active sample count serves 4-state plans");
-      if (run_samples(p) != (value ? value : p->batch)) p->partials_valid = false;
+      if (plan_run_samples(p) != (value ? value : p->batch)) p->partials_valid = false;
       p->active = value;
       return TT_OK;
     default:

@@ -31,7 +31,7 @@ struct tt_plan {
   // slab by slab).
   int slab = 0;
   int last_rescale = 1;  // rescale flag of the last post-order (repeated by the slab recompute)
-  int active = 0;        // 4-state plans: samples the pruning passes run over (0 = all)
+  int active = 0;        // samples the pruning passes run over (0 = all)
   long long launches = 0;
   std::vector<int> steps;       // host copy of the schedule (I x 12)
   std::vector<int> steps_ws;    // records of the producer-warp post-order (I x 12)
@@ -58,6 +58,9 @@ struct tt_plan {
   size_t grad_bytes = 0;  // of `bytes`: the stored partials and per-tile gradient blocks
   tt::WideState *wide = nullptr;  // non-NULL for S != 4 plans
 };
+
+// Samples the pruning passes and their reductions run over (TT_OPT_ACTIVE_SAMPLES).
+inline int plan_run_samples(const tt_plan *p) { return p->active > 0 && p->active < p->batch ? p->active : p->batch; }
 
 namespace tt {
 // Wide-state path (tt_wide.cu): same contracts as the C entry points.

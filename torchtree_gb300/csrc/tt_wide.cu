@@ -289,22 +289,22 @@ struct Wide {
           WideArgs<T> at = a;
           at.ntiles = ntf;
           at.tiles_per_chunk = (ntf + chunks - 1) / chunks;
-          const dim3 grid(chunks, nodes, p->batch * p->K);
+          const dim3 grid(chunks, nodes, plan_run_samples(p) * p->K);
           wide_forward_tc_kernel<<<grid, tc::kThreads, tc::kSmem, s>>>(at, w.d_pimg_f, p->d_status, 2000000000ull);
           p->launches += 1;
           continue;
         }
       }
-      const dim3 grid(g.ntiles_f, w.fwd_off[lv + 1] - w.fwd_off[lv], p->batch * p->K);
+      const dim3 grid(g.ntiles_f, w.fwd_off[lv + 1] - w.fwd_off[lv], plan_run_samples(p) * p->K);
       wide_forward_kernel<T, SP, PTF><<<grid, NT, smem, s>>>(a);
       p->launches += 1;
     }
-    wide_root_kernel<<<dim3(g.nblk, p->batch), 256, 0, s>>>(w.d_root_site, w.d_root_expo, props, a.weights,
+    wide_root_kernel<<<dim3(g.nblk, plan_run_samples(p)), 256, 0, s>>>(w.d_root_site, w.d_root_expo, props, a.weights,
                                                            site_lnl, w.d_log2L, w.d_block_lnl, p->K, n, g.Npad);
     p->launches += 1;
     cudaError_t e = cudaSuccess;
     if (lnl) {
-      e = launch_reduce_lnl(w.d_block_lnl, lnl, p->batch, g.nblk, accumulate, s);
+      e = launch_reduce_lnl(w.d_block_lnl, lnl, plan_run_samples(p), g.nblk, accumulate, s);
       p->launches += 1;
     }
     return e == cudaSuccess ? cudaGetLastError() : e;
@@ -331,14 +331,14 @@ struct Wide {
       const int chunks = per_level ? tc_level_chunks(nodes, bk, g.ntiles_b, g.cmax, target) : g.nchunks;
       a.nodes = w.d_bwd + w.bwd_off[lv];
       a.tiles_per_chunk = per_level ? (g.ntiles_b + chunks - 1) / chunks : g.tpc;
-      const dim3 grid(chunks, nodes, bk);
+      const dim3 grid(chunks, nodes, plan_run_samples(p) * p->K);
       wide_backward_kernel<T, SP, PTB><<<grid, NT, smem, s>>>(a);
       p->launches += 1;
     }
-    wide_grad_reduce_kernel<T><<<dim3(p->B, p->batch), 256, 0, s>>>(
+    wide_grad_reduce_kernel<T><<<dim3(p->B, plan_run_samples(p)), 256, 0, s>>>(
         static_cast<const T *>(w.d_gpart), p->d_G, p->B, g.nchunks, p->K, p->S, SP, accumulate,
         per_level ? w.d_branch_lvn : nullptr, bk, g.ntiles_b, g.cmax, target);
-    wide_root_reduce_kernel<T><<<p->batch, 64, 0, s>>>(static_cast<const T *>(w.d_rootpart), p->d_rootgrad,
+    wide_root_reduce_kernel<T><<<plan_run_samples(p), 64, 0, s>>>(static_cast<const T *>(w.d_rootpart), p->d_rootgrad,
                                                        p->d_rootgrad + size_t(p->batch) * p->S, g.nchunks, p->K,
                                                        p->S, SP, accumulate);
     p->launches += 2;
@@ -376,15 +376,15 @@ struct Wide {
       const int chunks = tc_level_chunks(nodes, bk, ntc, cmax);
       a.nodes = w.d_bwd + w.bwd_off[lv];
       a.tiles_per_chunk = (ntc + chunks - 1) / chunks;
-      const dim3 grid(chunks, nodes, bk);
+      const dim3 grid(chunks, nodes, plan_run_samples(p) * p->K);
       wide_backward_tc_kernel<<<grid, tcb::kThreads, tcb::kSmem, s>>>(a, maps, w.d_pimg, p->C, p->d_status,
                                                                        2000000000ull);
       p->launches += 1;
     }
-    wide_grad_reduce_kernel<float><<<dim3(p->B, p->batch), 256, 0, s>>>(static_cast<const float *>(w.d_gpart),
+    wide_grad_reduce_kernel<float><<<dim3(p->B, plan_run_samples(p)), 256, 0, s>>>(static_cast<const float *>(w.d_gpart),
                                                                          p->d_G, p->B, a.nchunks, p->K, p->S, 64,
                                                                          accumulate, w.d_branch_lvn, bk, ntc, cmax);
-    wide_root_reduce_kernel<float><<<p->batch, 64, 0, s>>>(static_cast<const float *>(w.d_rootpart), p->d_rootgrad,
+    wide_root_reduce_kernel<float><<<plan_run_samples(p), 64, 0, s>>>(static_cast<const float *>(w.d_rootpart), p->d_rootgrad,
                                                            p->d_rootgrad + size_t(p->batch) * p->S, a.nchunks, p->K,
                                                            p->S, 64, accumulate);
     p->launches += 2;

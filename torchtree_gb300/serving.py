@@ -5,7 +5,8 @@ a set of resident data sets (tree topology + compressed alignment + model
 family).  The server keeps each admitted data set's tip codes, pattern
 weights and workspace resident in one plan with ``slots`` batch slots, and
 runs its step -- transition matrices, post-order, adjoint, matrix-gradient
-chain -- as one captured CUDA graph on the data set's own stream:
+chain -- as captured CUDA graphs on the data set's own stream, one per number
+of occupied slots, whose pruning passes skip the idle slots:
 
 * continuous batching: a scheduler thread launches a data set's waiting
   requests (up to ``slots``) as soon as its previous batch has left the GPU;
@@ -180,7 +181,7 @@ def slab_fit(ds: Dataset, slots: int, precision: str, room: int):
 
 
 class GraphExecutor:
-    """One admitted data set: plan, stream, static buffers, captured step."""
+    """One admitted data set: plan, stream, static buffers, captured steps."""
 
     def __init__(self, ds: Dataset, slots: int, precision: str, device, use_graph: bool = True,
                  tune: bool = True, slab: int = 0, merge: bool = False):
@@ -206,18 +207,22 @@ class GraphExecutor:
                        "props": torch.full((slots, K), 1.0 / K, **kw), "pi": torch.full((slots, S), 1.0 / S, **kw)}
         self.host_in = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in self.inputs.items()}
         self.stream = torch.cuda.Stream(device)
-        self.graph = None
+        self.graphs: dict = {}  # occupied slots n -> (graph, outputs) of the step over slots 0 .. n-1
         with torch.cuda.device(device), torch.cuda.stream(self.stream):
             if tune:
                 autotune.tune(self.engine, self._step)
             outs = self._step()  # eager warm-up (also sets the plan's state for capture)
             self.stream.synchronize()
             if use_graph:
-                self.graph = torch.cuda.CUDAGraph()
-                # thread-local capture: CUDA calls that client threads make meanwhile
-                # (pinned copies of their own, allocations) cannot invalidate it
-                with torch.cuda.graph(self.graph, stream=self.stream, capture_error_mode="thread_local"):
-                    outs = self._step()
+                for n in range(1, slots + 1):
+                    # the pruning passes over the slots that hold requests only
+                    self.engine.set_option(_native.TT_OPT_ACTIVE_SAMPLES, n)
+                    graph = torch.cuda.CUDAGraph()
+                    # thread-local capture: CUDA calls that client threads make meanwhile
+                    # (pinned copies of their own, allocations) cannot invalidate it
+                    with torch.cuda.graph(graph, stream=self.stream, capture_error_mode="thread_local"):
+                        self.graphs[n] = (graph, self._step())
+                outs = self.graphs[slots][1]
         self.outputs = outs
         self.host_out = {k: torch.empty(v.shape, dtype=v.dtype, pin_memory=True) for k, v in outs.items()}
         self.event = torch.cuda.Event()
@@ -253,9 +258,11 @@ class GraphExecutor:
         with torch.cuda.device(self.device), torch.cuda.stream(self.stream):
             for k, v in self.inputs.items():
                 v.copy_(self.host_in[k], non_blocking=True)
-            if self.graph is not None:
-                self.graph.replay()
+            if self.graphs:
+                graph, self.outputs = self.graphs[len(reqs)]
+                graph.replay()
             else:
+                self.engine.set_option(_native.TT_OPT_ACTIVE_SAMPLES, len(reqs))
                 self.outputs = self._step()
             for k, v in self.outputs.items():
                 self.host_out[k].copy_(v, non_blocking=True)
@@ -282,7 +289,7 @@ class GraphExecutor:
         return done
 
     def close(self) -> None:
-        self.graph = None
+        self.graphs = {}
         self.engine.close()
 
 
