@@ -70,6 +70,9 @@ def parse():
     ap.add_argument("--serving-chains", type=int, default=256)
     ap.add_argument("--serving-requests", type=int, default=1024)
     ap.add_argument("--serving-slots", type=int, default=4)
+    ap.add_argument("--serving-fixed-slots", action="store_true",
+                    help="every plan gets --serving-slots slots (default: fewer for data sets whose one sample "
+                         "fills the GPU, serving.slots_for)")
     ap.add_argument("--serving-merge-depth", type=int, default=2,
                     help="merged DNA steps in flight at once (0: no merging, one graph per data set)")
     ap.add_argument("--serving-max-tips", type=int, default=2000)
@@ -412,7 +415,8 @@ def run_serving(args):
     chains = [(c % len(mix), chain_params(rng, mix[c % len(mix)][1], mix[c % len(mix)][3]))
               for c in range(args.serving_chains)]
     srv = serving.LikelihoodServer(slots=args.serving_slots, precision="f32", merge=args.serving_merge_depth > 0,
-                                   merge_depth=max(1, args.serving_merge_depth))
+                                   merge_depth=max(1, args.serving_merge_depth),
+                                   size_slots=not args.serving_fixed_slots)
     for name, topo, ca, S, spec in mix:
         srv.add_dataset(name, topo, ca, S, spec)
     srv.start()
@@ -502,7 +506,7 @@ def run_serving(args):
         "speedup_vs_fp64_one_at_a_time": (len(futs) / wall) / fp64_rate,
         "data": "synthetic: Yule trees, i.i.d. uniform tip states, GTR+G4 / general 20-state+G4",
         "config": {"workload": "serving_mix", "datasets": len(mix), "chains": len(chains),
-                   "slots": args.serving_slots, "dna": sum(1 for s in sizes if s[2] == 4),
+                   "slots": args.serving_slots, "fixed_slots": args.serving_fixed_slots, "dna": sum(1 for s in sizes if s[2] == 4),
                    "protein": sum(1 for s in sizes if s[2] == 20), "tips_range": [min(s[0] for s in sizes),
                                                                                     max(s[0] for s in sizes)],
                    "patterns_range": [min(s[1] for s in sizes), max(s[1] for s in sizes)]},
