@@ -274,8 +274,10 @@ __device__ __forceinline__ void ta_backward_body(const PruneArgs<float> &a, cons
         d2[i & 1] = __ffma2_rn(xl.v[i][q], al.v[i][q], d2[i & 1]);
       }
     const float den = (d2[0].x + d2[1].x) + (d2[0].y + d2[1].y);
-    // dlnL_n/dP = w_n * x (outer) v / L_n; per-pattern scales cancel against den
-    const float coef = (act && den > 0.0f) ? w / den : 0.0f;
+    // dlnL_n/dP = w_n * x (outer) v / L_n; per-pattern scales cancel against den.
+    // den is a sum of 16 products of rescaled vectors (well inside the range
+    // where the approximate division is within 2 ulp)
+    const float coef = (act && den > 0.0f) ? __fdividef(w, den) : 0.0f;
     if (is_root) {
       // dlnL/dpi_i = sum_k c_k R[k][i] / L and dlnL/dc_k = sum_i pi_i R[k][i] / L, R = al * ar
       float rpi[4] = {0.0f, 0.0f, 0.0f, 0.0f}, rc[2 * KQ];
