@@ -108,14 +108,16 @@ def test_merged_plans_match_the_oracle():
         np.testing.assert_allclose(lnl.cpu().numpy(), ref, rtol=1e-6)
 
 
-def test_active_samples_equal_the_whole_batch_for_those_samples():
+@pytest.mark.parametrize("precision", ["f32", "f64"])
+def test_active_samples_equal_the_whole_batch_for_those_samples(precision):
     """TT_OPT_ACTIVE_SAMPLES: the pruning passes and their reductions over the
-    first n samples only, alone and in a merged call, give those samples'
-    results of a call over every sample bit for bit."""
+    first n samples only, alone and in a merged call (FP64 plans: each its own
+    calls), give those samples' results of a call over every sample bit for
+    bit."""
     from torchtree_gb300 import _native
     from torchtree_gb300.engine import plans_gradient, plans_log_likelihood
 
-    cases = [_plan(120, 1500, 4, 21, 4), _plan(45, 700, 4, 22, 3)]
+    cases = [_plan(120, 1500, 4, 21, 4, precision=precision), _plan(45, 700, 4, 22, 3, precision=precision)]
     full = [_alone(c) for c in cases]
     e0 = cases[0]["eng"]
     with pytest.raises(ValueError):
