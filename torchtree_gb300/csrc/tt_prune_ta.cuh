@@ -351,8 +351,9 @@ __device__ __forceinline__ void ta_backward_body(const PruneArgs<float> &a, cons
     // slot (i', jj') holds element (i' ^ a, jj' ^ b): every lane then keeps
     // the lower half of its slots at every level and sends the upper half,
     // which holds the partner's kept elements, with no lane-dependent selects.
-    // A tip child's v comes from the code table unpermuted; its jj levels and
-    // the category level select as plain recursive halving.
+    // A tip child's v comes from the code table, whose row halves a lane
+    // loads in the order b1 gives (jj1 permuted); its jj0 level and the
+    // category level select as plain recursive halving.
     {
       constexpr int LV = UR >= 32 ? 5 : UR >= 16 ? 4 : UR >= 8 ? 3 : UR >= 4 ? 2 : UR >= 2 ? 1 : 0;
       constexpr int PL = (P + UR - 1) / UR;  // patterns per lane
@@ -362,7 +363,7 @@ __device__ __forceinline__ void ta_backward_body(const PruneArgs<float> &a, cons
       const bool tipc = uact && (c ? rtip : ltip);
       // permutation bits: the top LV bits of the 5-bit block index
       const int bits = LV > 0 ? (sidx << (5 - LV)) : 0;
-      const int pa = bits >> 3, pb = tipc ? 0 : (bits >> 1) & 3;
+      const int pa = bits >> 3, pb = (bits >> 1) & (tipc ? 2 : 3);
       float2 acc[4][4];
 #pragma unroll
       for (int i = 0; i < 4; ++i)
@@ -386,7 +387,7 @@ __device__ __forceinline__ void ta_backward_body(const PruneArgs<float> &a, cons
             for (int i = 0; i < 4; ++i) x[i] = xr[i][kk * UR];
             if (tipc) {
               const float4 *tr = reinterpret_cast<const float4 *>(tab2 + int(csd[kk * UR]) * 4);
-              const float4 t0 = tr[0], t1 = tr[1];
+              const float4 t0 = tr[pb >> 1], t1 = tr[(pb >> 1) ^ 1];
               v[0] = make_float2(t0.x, t0.y);
               v[1] = make_float2(t0.z, t0.w);
               v[2] = make_float2(t1.x, t1.y);
@@ -412,10 +413,10 @@ __device__ __forceinline__ void ta_backward_body(const PruneArgs<float> &a, cons
       const bool sel_jj = __any_sync(0xffffffffu, tipc);
 #pragma unroll
       for (int o = UR / 2, h = 8; o >= 1 && h >= 1; o >>= 1, h >>= 1) {
-        if (h >= 4 || !sel_jj) {  // i levels, and jj levels with every lane permuted
+        if (h >= 2 || !sel_jj) {  // i and jj1 levels, and jj0 with every lane permuted
 #pragma unroll
           for (int e = 0; e < h; ++e) g[e] = __fadd2_rn(g[e], shfl_xor_f2(g[e + h], o));
-        } else {  // jj levels of tip lanes (internal lanes never swap)
+        } else {  // jj0 level of tip lanes (internal lanes never swap)
           const bool swap = tipc && (lane & o) != 0;
 #pragma unroll
           for (int e = 0; e < h; ++e) {
